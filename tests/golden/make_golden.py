@@ -1,0 +1,283 @@
+"""Generate golden vectors by running the unmodified TreeTime package.
+
+Run in a container where the TreeTime sources are available (they are not
+shipped with this repository and are not needed to run the tests):
+
+    python tests/golden/make_golden.py /path/to/treetime-source
+
+Biopython and pandas are replaced by the test-only stand-ins under
+``oracle/bioshim``.  Inputs are seeded synthetic workloads from
+``treetime_gb300.synth``; each case stores its inputs (Newick text, the
+alignment, the raw model parameters) together with TreeTime's outputs in
+``tests/golden/<case>.npz``.
+"""
+
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def _setup(ref_path):
+    sys.path.insert(0, os.path.join(REPO, "oracle", "bioshim"))
+    sys.path.insert(0, ref_path)
+    sys.path.insert(0, REPO)
+
+
+def _bio_inputs(newick, aln):
+    from Bio import Phylo
+    from Bio.Align import MultipleSeqAlignment
+    from Bio.Seq import Seq
+    from Bio.SeqRecord import SeqRecord
+    tree = Phylo.read(io.StringIO(newick), "newick")
+    recs = MultipleSeqAlignment([SeqRecord(Seq(s), id=k, name=k) for k, s in aln.items()])
+    return tree, recs
+
+
+def _codes(chars):
+    return np.frombuffer(np.asarray(chars).astype("S1").tobytes(), dtype=np.uint8)
+
+
+def _ref_gtr(kind, params):
+    from treetime import GTR, GTR_site_specific
+    alphabet = params["alphabet"]
+    if isinstance(alphabet, np.ndarray) and alphabet.ndim == 0:
+        alphabet = str(alphabet)
+    if kind == "gtr":
+        return GTR.custom(mu=params["mu"], pi=params["pi"], W=params["W"], alphabet=alphabet)
+    g = GTR_site_specific(seq_len=params["pi"].shape[1], approximate=bool(params["approximate"]),
+                          alphabet=alphabet)
+    g.assign_rates(mu=params["mu"], pi=params["pi"], W=params["W"])
+    return g
+
+
+def run_case(name, newick, aln, kind, params, compress=True, masks=None, reconstruct_tip_states=False,
+             keep_profiles=True, marginal_bl=True, ignore_gaps=True, rng_seed=1234, sample_root=False):
+    from treetime import TreeAnc
+    out = {"case": name, "newick": newick, "kind": kind, "compress": compress,
+           "reconstruct_tip_states": reconstruct_tip_states, "ignore_gaps": ignore_gaps,
+           "aln_names": np.array(list(aln.keys())), "aln_seqs": np.array(list(aln.values())),
+           "rng_seed": rng_seed, "sample_root": sample_root}
+    for k, v in params.items():
+        out["param_" + k] = np.asarray(v)
+
+    def make():
+        tree, recs = _bio_inputs(newick, aln)
+        t = TreeAnc(tree=tree, aln=recs, gtr=_ref_gtr(kind, params), compress=compress, verbose=0,
+                    rng_seed=rng_seed, ignore_gaps=ignore_gaps)
+        if masks:
+            for n in t.tree.find_clades():
+                if n.name in masks:
+                    n.mask = masks[n.name]
+        return t
+
+    # ---- marginal
+    t = make()
+    g = t.gtr
+    out["eigenvals"], out["v"], out["v_inv"] = g.eigenvals, g.v, g.v_inv
+    out["W_norm"], out["Pi"], out["mu"] = g.W, g.Pi, g.mu
+    out["compressed_names"] = np.array(t.data.sequence_names)
+    out["compressed_codes"] = np.stack([_codes(t.data.compressed_alignment[k]) for k in t.data.sequence_names])
+    out["multiplicity"] = t.data.multiplicity()
+    out["full_to_compressed"] = t.data.full_to_compressed_sequence_map
+    nodes = list(t.tree.find_clades())
+    out["node_names"] = np.array([n.name for n in nodes])
+    out["node_parent"] = np.array([nodes.index(n.up) if n.up is not None else -1 for n in nodes])
+    out["node_bl"] = np.array([n.branch_length for n in nodes], dtype=float)
+    if masks:
+        out["mask_names"] = np.array(list(masks.keys()))
+        out["mask_rows"] = np.stack([masks[k] for k in masks])
+    ndiff = t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=reconstruct_tip_states,
+                                        sample_from_profile="root" if sample_root else False)
+    out["marg_N_diff"] = ndiff
+    out["marg_sequence_LH"] = t.tree.sequence_LH
+    out["marg_total_LH"] = t.tree.total_sequence_LH
+    recon = [n for n in nodes if hasattr(n, "_cseq")]
+    out["marg_cseq_names"] = np.array([n.name for n in recon])
+    out["marg_cseq"] = np.stack([_codes(n._cseq) for n in recon])
+    if keep_profiles:
+        inner = [n for n in nodes if not n.is_terminal() or reconstruct_tip_states]
+        out["marg_profile_names"] = np.array([n.name for n in inner])
+        out["marg_profile"] = np.stack([n.marginal_profile for n in inner])
+        out["marg_subtree_names"] = np.array([n.name for n in nodes if not n.is_terminal()])
+        out["marg_subtree"] = np.stack([n.marginal_subtree_LH for n in nodes if not n.is_terminal()])
+        nr = [n for n in nodes if n.up is not None]
+        out["marg_outgroup_names"] = np.array([n.name for n in nr])
+        out["marg_outgroup"] = np.stack([n.marginal_outgroup_LH for n in nr])
+    # second marginal call: N_diff against the first reconstruction
+    out["marg_N_diff_again"] = t.infer_ancestral_sequences(marginal=True,
+                                                           reconstruct_tip_states=reconstruct_tip_states)
+    if marginal_bl and kind == "gtr":
+        nr = [n for n in t.tree.find_clades() if n.up is not None]
+        out["mbl_names"] = np.array([n.name for n in nr])
+        out["mbl"] = np.array([t.optimal_marginal_branch_length(n) for n in nr])
+
+    # ---- joint
+    t = make()
+    ndiff = t.infer_ancestral_sequences(marginal=False, reconstruct_tip_states=reconstruct_tip_states, debug=True,
+                                        sample_from_profile="root" if sample_root else False)
+    nodes = list(t.tree.find_clades())
+    out["joint_N_diff"] = ndiff
+    out["joint_sequence_LH"] = t.tree.sequence_LH
+    out["joint_total_LH"] = t.tree.sequence_joint_LH
+    recon = [n for n in nodes if hasattr(n, "_cseq")]
+    out["joint_cseq_names"] = np.array([n.name for n in recon])
+    out["joint_cseq"] = np.stack([_codes(n._cseq) for n in recon])
+    # ---- joint branch lengths (TreeAnc.optimize_branch_lengths_joint)
+    if kind == "gtr":
+        t.optimize_branch_lengths_joint()
+        nr = [n for n in t.tree.find_clades() if n.up is not None]
+        out["jbl_names"] = np.array([n.name for n in nr])
+        out["jbl"] = np.array([n.branch_length for n in nr])
+        if not masks:
+            # (TreeTime compares full-length sequences with the compressed-length
+            # mask here, which fails for compressed alignments with masks)
+            mut = [(n.name, a, int(p), d) for n in nr for (a, p, d) in n.mutations]
+            out["mutations"] = np.array(["%s|%s|%d|%s" % m for m in mut])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
+
+
+def main(ref_path):
+    _setup(ref_path)
+    from treetime_gb300 import synth
+    from treetime_gb300.tree import to_newick
+
+    def gtr_params(g, raw_pi, raw_W, alphabet, mu=1.0, approximate=None):
+        d = {"pi": raw_pi, "W": raw_W, "alphabet": alphabet if isinstance(alphabet, str) else np.asarray(alphabet),
+             "mu": mu}
+        if approximate is not None:
+            d["approximate"] = approximate
+        return d
+
+    # c0-shaped, small
+    rng = np.random.default_rng(11)
+    tree = synth.coalescent_tree(24, 0.02, rng)
+    pi = rng.dirichlet(np.ones(4))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(4, 4)), 1)
+    W = W + W.T
+    from treetime_gb300.gtr import GTR
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap")
+    states = synth.evolve(tree, g, 120, rng)
+    aln = synth._to_text(states, g.alphabet, 0.05, rng)
+    nwk = to_newick(tree)
+    run_case("c0_small", nwk, aln, "gtr", gtr_params(g, pi, W, "nuc_nogap"))
+    run_case("c0_small_tips", nwk, aln, "gtr", gtr_params(g, pi, W, "nuc_nogap"), reconstruct_tip_states=True)
+    run_case("c0_small_sample", nwk, aln, "gtr", gtr_params(g, pi, W, "nuc_nogap"), sample_root=True,
+             marginal_bl=False)
+
+    # 5-state alphabet with gaps, ambiguity codes and invariant columns
+    rng = np.random.default_rng(12)
+    tree = synth.coalescent_tree(20, 0.05, rng)
+    pi = rng.dirichlet(np.ones(5))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(5, 5)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc")
+    states = synth.evolve(tree, g, 200, rng, invariant_frac=0.5)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    names = list(aln)
+    for k in names:
+        s = np.array(list(aln[k]))
+        r = rng.random(len(s))
+        s[r < 0.03] = "N"
+        s[(r > 0.03) & (r < 0.05)] = rng.choice(list("RYKMSW"))
+        if rng.random() < 0.3:
+            s[: rng.integers(1, 10)] = "-"
+        aln[k] = "".join(s)
+    run_case("nuc5", to_newick(tree), aln, "gtr", gtr_params(g, pi, W, "nuc"))
+
+    # masks on a few branches
+    rng = np.random.default_rng(13)
+    tree = synth.coalescent_tree(16, 0.03, rng)
+    pi = rng.dirichlet(np.ones(4))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(4, 4)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap")
+    states = synth.evolve(tree, g, 120, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    tree_names = [c.name for c in tree.find_clades() if c.name]
+    masks = {}
+    for k in tree_names[:6]:
+        masks[k] = None
+    # the compressed length is only known after compression: run once to get it
+    from treetime_gb300.seqdata import SequenceData
+    P = SequenceData(aln, compress=True, ambiguous="N").compressed_length
+    masks = {k: (rng.random(P) < 0.7).astype(float) for k in tree_names[:6]}
+    run_case("masked", to_newick(tree), aln, "gtr", gtr_params(g, pi, W, "nuc_nogap"), masks=masks,
+             marginal_bl=False)
+
+    # polytomies, a tip without sequence, an unknown character
+    rng = np.random.default_rng(14)
+    tree = synth.coalescent_tree(18, 0.04, rng)
+    inner = [c for c in tree.find_clades(order="postorder") if c.clades and c is not tree.root]
+    for c in inner[:3]:
+        # collapse: splice the clade's children into its parent
+        for par in tree.find_clades():
+            if c in par.clades:
+                i = par.clades.index(c)
+                par.clades[i:i + 1] = c.clades
+                break
+    g = GTR.custom(mu=1.0, pi=np.ones(4), W=np.ones((4, 4)), alphabet="nuc_nogap")
+    states = synth.evolve(tree, g, 100, rng)
+    aln = synth._to_text(states, g.alphabet, 0.02, rng)
+    first = list(aln)[0]
+    del aln[first]
+    k2 = list(aln)[1]
+    s = list(aln[k2])
+    s[5] = "?"
+    aln[k2] = "".join(s)
+    run_case("polytomy", to_newick(tree), aln, "gtr", gtr_params(g, np.ones(4), np.ones((4, 4)), "nuc_nogap"),
+             reconstruct_tip_states=True)
+
+    # 22-state amino-acid alphabet, standard GTR (large-alphabet state_pair branch)
+    rng = np.random.default_rng(15)
+    tree = synth.coalescent_tree(12, 0.1, rng)
+    pi = rng.random(22)
+    W = rng.random((22, 22))
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="aa")
+    states = synth.evolve(tree, g, 80, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    k = list(aln)[2]
+    s = list(aln[k])
+    s[3] = "X"
+    s[4] = "B"
+    aln[k] = "".join(s)
+    run_case("aa22", to_newick(tree), aln, "gtr", gtr_params(g, pi, W, "aa"))
+
+    # site-specific protein model, both P(t) paths
+    rng = np.random.default_rng(16)
+    L = 40
+    tree = synth.yule_tree(14, 0.05, rng)
+    pi = rng.dirichlet(np.full(21, 0.5), size=L).T
+    W = np.triu(rng.uniform(0.1, 5.0, size=(21, 21)), 1)
+    W = W + W.T
+    from treetime_gb300.gtr import GTR_site_specific
+    g = GTR_site_specific(seq_len=L, approximate=True, alphabet=synth.AA21)
+    g.assign_rates(mu=1.0, pi=pi, W=W)
+    states = synth.evolve_site_specific(tree, g, L, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    for approx in (True, False):
+        run_case("aa_site_specific_%s" % ("interp" if approx else "exact"), to_newick(tree), aln, "ss",
+                 gtr_params(g, pi, W, synth.AA21, approximate=approx), compress=False, marginal_bl=False)
+
+    # full-size C0 workload: sequences, likelihoods and branch lengths only
+    wl = synth.make_workload("c0", seed=0)
+    g = wl["gtr"]
+    rng = np.random.default_rng(0)
+    # make_workload's model draws: recover the raw parameters by re-drawing
+    tree = synth.coalescent_tree(100, 0.01, rng)
+    pi = rng.dirichlet(np.ones(4))
+    W = rng.uniform(0.5, 2.0, size=(4, 4))
+    W = np.triu(W, 1)
+    W = W + W.T
+    assert np.allclose(GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap").W, g.W)
+    run_case("c0_full", to_newick(wl["tree"]), wl["aln"], "gtr", gtr_params(g, pi, W, "nuc_nogap"),
+             keep_profiles=False, marginal_bl=False)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,150 @@
+"""Pin the CPU oracle (``oracle/anc.py``) and the host-side set-up code
+against golden vectors produced by running TreeTime itself
+(``tests/golden/make_golden.py``).  CPU only."""
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from oracle import anc
+from treetime_gb300.seqdata import SequenceData
+from treetime_gb300.alphabets import extend_profile
+
+CASES = gc.case_names()
+
+
+def _names_map(names, arr):
+    return {str(k): arr[i] for i, k in enumerate(names)}
+
+
+def _prepared(g):
+    tree, aln, model, masks = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    if masks:
+        for n in anc.preorder(tree.root):
+            if n.name in masks:
+                n.mask = masks[n.name]
+    return tree, aln, model, masks
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_tree_preparation_names_and_order(case):
+    g = gc.load(case)
+    tree, _, _, _ = _prepared(g)
+    nodes = list(anc.preorder(tree.root))
+    assert [n.name for n in nodes] == g["node_names"].tolist()
+    parent = [nodes.index(n.up) if n.up is not None else -1 for n in nodes]
+    assert parent == g["node_parent"].tolist()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_model_eigendecomposition(case):
+    g = gc.load(case)
+    m = gc.model_from(g)
+    np.testing.assert_allclose(m.W, g["W_norm"], rtol=1e-14, atol=1e-14)
+    np.testing.assert_allclose(m.Pi, g["Pi"], rtol=1e-14, atol=1e-15)
+    np.testing.assert_allclose(m.mu, g["mu"], rtol=1e-14)
+    np.testing.assert_allclose(m.eigenvals, g["eigenvals"], rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(m.v, g["v"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(m.v_inv, g["v_inv"], rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_host_compression_bit_exact(case):
+    g = gc.load(case)
+    _, aln, model, _ = gc.inputs_from(g)
+    sd = SequenceData(aln, compress=bool(g["compress"]), ambiguous=model.ambiguous)
+    assert sd.sequence_names == g["compressed_names"].tolist()
+    np.testing.assert_array_equal(sd.compressed_codes, g["compressed_codes"])
+    np.testing.assert_array_equal(sd.multiplicity(), g["multiplicity"])
+    np.testing.assert_array_equal(sd.full_to_compressed_sequence_map, g["full_to_compressed"])
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if not c.startswith("aa_site")])
+def test_oracle_compression_restatement(case):
+    g = gc.load(case)
+    _, aln, model, _ = gc.inputs_from(g)
+    arrays = {k: anc.seq2array(v, fill_overhangs=True, ambiguous=model.ambiguous) for k, v in aln.items()}
+    comp, mult, f2c, _ = anc.compress_alignment(list(arrays), arrays, model.ambiguous)
+    chars = g["compressed_codes"].view("S1").astype("U1")
+    for i, k in enumerate(g["compressed_names"].tolist()):
+        np.testing.assert_array_equal(comp[k], chars[i])
+    np.testing.assert_array_equal(mult, g["multiplicity"])
+    np.testing.assert_array_equal(f2c, g["full_to_compressed"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_marginal_matches_treetime(case):
+    g = gc.load(case)
+    tree, _, model, _ = _prepared(g)
+    aln = gc.compressed_from(g, model)
+    rng = np.random.default_rng(int(g["rng_seed"]))
+    res = anc.marginal(tree, aln, g["multiplicity"], model, len(g["full_to_compressed"]),
+                       sample_from_profile="root" if bool(g["sample_root"]) else False,
+                       reconstruct_tip_states=bool(g["reconstruct_tip_states"]), rng=rng)
+    np.testing.assert_allclose(res["sequence_LH"], g["marg_sequence_LH"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(res["total_sequence_LH"], g["marg_total_LH"], rtol=1e-13)
+    assert res["N_diff"] == int(g["marg_N_diff"])
+    want = _names_map(g["marg_cseq_names"], g["marg_cseq"])
+    assert set(want) == set(res["cseq"])
+    for k, v in want.items():
+        np.testing.assert_array_equal(gc.codes_of(res["cseq"][k]), v, err_msg=k)
+    if "marg_profile" in g:
+        for key, gk in (("profile", "marg_profile"), ("subtree_LH", "marg_subtree"), ("outgroup_LH", "marg_outgroup")):
+            want = _names_map(g[gk + "_names"], g[gk])
+            for k, v in want.items():
+                np.testing.assert_allclose(res[key][k], v, rtol=1e-10, atol=1e-13, err_msg="%s %s" % (key, k))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_joint_matches_treetime(case):
+    g = gc.load(case)
+    tree, _, model, _ = _prepared(g)
+    aln = gc.compressed_from(g, model)
+    rng = np.random.default_rng(int(g["rng_seed"]))
+    res = anc.joint(tree, aln, g["multiplicity"], model, len(g["full_to_compressed"]),
+                    sample_from_profile="root" if bool(g["sample_root"]) else False,
+                    reconstruct_tip_states=bool(g["reconstruct_tip_states"]), rng=rng)
+    np.testing.assert_allclose(res["sequence_LH"], g["joint_sequence_LH"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(res["sequence_joint_LH"], g["joint_total_LH"], rtol=1e-13)
+    assert res["N_diff"] == int(g["joint_N_diff"])
+    want = _names_map(g["joint_cseq_names"], g["joint_cseq"])
+    for k, v in want.items():
+        np.testing.assert_array_equal(gc.codes_of(res["cseq"][k]), v, err_msg=k)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "jbl" in gc.load(c)])
+def test_oracle_joint_branch_lengths_match_treetime(case):
+    g = gc.load(case)
+    tree, _, model, _ = _prepared(g)
+    aln = gc.compressed_from(g, model)
+    res = anc.joint(tree, aln, g["multiplicity"], model, len(g["full_to_compressed"]),
+                    reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    cseq = dict(res["cseq"])
+    if not bool(g["reconstruct_tip_states"]):
+        cseq.update({k: v for k, v in aln.items()})
+    bl = anc.optimize_branch_lengths_joint(tree, lambda n: cseq[n.name], g["multiplicity"], model,
+                                           ignore_gaps=bool(g["ignore_gaps"]))
+    want = _names_map(g["jbl_names"], g["jbl"])
+    # the argmin of a smooth objective is only defined to ~sqrt(machine eps)
+    # relative; 1e-6 relative (+1e-10 absolute) is the branch-length bar
+    for k, v in want.items():
+        assert abs(bl[k] - v) <= 1e-6 * abs(v) + 1e-10, (k, bl[k], v)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "mbl" in gc.load(c)])
+def test_oracle_marginal_branch_lengths_match_treetime(case):
+    g = gc.load(case)
+    tree, _, model, _ = _prepared(g)
+    aln = gc.compressed_from(g, model)
+    res = anc.marginal(tree, aln, g["multiplicity"], model, len(g["full_to_compressed"]),
+                       reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    want = _names_map(g["mbl_names"], g["mbl"])
+    for n in anc.preorder(tree.root):
+        if n.up is None:
+            continue
+        m = g["multiplicity"] if n.mask is None else g["multiplicity"] * n.mask
+        t, _ = anc.optimal_t_compressed(model, (res["outgroup_LH"][n.name], res["subtree_LH"][n.name]), m,
+                                        profiles=True)
+        v = want[n.name]
+        assert abs(t - v) <= 1e-6 * abs(v) + 1e-10, (n.name, t, v)

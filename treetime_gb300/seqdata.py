@@ -1,0 +1,243 @@
+"""Alignment ingest and column-pattern compression.
+
+``SequenceData`` keeps the alignment as a uint8 byte matrix (tips × sites)
+and compresses it into alignment patterns with the exact semantics of
+treetime/sequence_data.py:325-464:
+
+  * a column with exactly two letters, one of them the ambiguous character,
+    is rewritten to the other letter first;
+  * only constant columns merge: a column with two or more letters gets a
+    private pattern (TreeTime keys it by '<column>_<position>');
+  * patterns are numbered by first occurrence, ``multiplicity`` counts the
+    merged columns, and the two maps full<->compressed are kept;
+  * ``compress=False`` is the identity.
+
+The compression is vectorised over columns (numpy on the host, or the
+``tt_compress_columns`` CUDA entry point for large alignments); both give
+bit-identical patterns, multiplicities and maps.
+"""
+
+import os
+from collections import OrderedDict
+
+import numpy as np
+
+from . import config as ttconf
+from .alphabets import seq2array, guess_alphabet, chars_to_codes, codes_to_chars
+from .errors import MissingDataError
+
+
+def read_fasta(path_or_handle):
+    if hasattr(path_or_handle, "read"):
+        text = path_or_handle.read()
+    else:
+        with open(path_or_handle) as fh:
+            text = fh.read()
+    out = OrderedDict()
+    name, chunks = None, []
+    for line in text.splitlines():
+        line = line.strip()
+        if not line:
+            continue
+        if line.startswith(">"):
+            if name is not None:
+                out[name] = "".join(chunks)
+            parts = line[1:].split()
+            name, chunks = (parts[0] if parts else ""), []
+        else:
+            chunks.append(line)
+    if name is not None:
+        out[name] = "".join(chunks)
+    return out
+
+
+def _record_name(rec):
+    """Name of an alignment record as TreeTime picks it
+    (treetime/sequence_data.py:161-173)."""
+    rid, rname = getattr(rec, "id", None), getattr(rec, "name", None)
+    if rid == rname:
+        return rid
+    if rid is not None and "<unknown" in str(rid):
+        return rname
+    if rname is not None and "<unknown" in str(rname):
+        return rid
+    return rname
+
+
+def compress_codes(codes, ambiguous_code, compress=True):
+    """Column-pattern compression of a tips × sites uint8 matrix.
+
+    Returns (pattern_codes [tips × P] uint8, multiplicity [P] float64,
+    full_to_compressed [L] int64, compressed_to_full dict p -> positions).
+    """
+    n, L = codes.shape
+    if not compress:
+        return (codes.copy(), np.ones(L, dtype=float), np.arange(L),
+                {p: np.array([p]) for p in range(L)})
+    if n == 0:
+        raise MissingDataError("empty alignment")
+    amb = -1 if ambiguous_code is None else int(ambiguous_code)
+    c16 = codes.astype(np.int16)
+    is_amb = c16 == amb
+    big, small = np.int16(1000), np.int16(-1)
+    non_amb_min = np.where(is_amb, big, c16).min(axis=0)
+    non_amb_max = np.where(is_amb, small, c16).max(axis=0)
+    any_non_amb = non_amb_max >= 0
+    any_amb = is_amb.any(axis=0)
+    all_same = codes.min(axis=0) == codes.max(axis=0)
+    # {X, ambiguous} columns collapse to X
+    amb_fix = any_non_amb & any_amb & (non_amb_min == non_amb_max)
+    constant = all_same | amb_fix
+    fixed = codes
+    if amb_fix.any():
+        fixed = codes.copy()
+        cols = np.flatnonzero(amb_fix)
+        sub = fixed[:, cols]
+        sub[is_amb[:, cols]] = np.broadcast_to(non_amb_min[cols].astype(np.uint8), sub.shape)[is_amb[:, cols]]
+        fixed[:, cols] = sub
+    letter = np.where(amb_fix, non_amb_min, codes[0].astype(np.int16)).astype(np.int64)
+    key = np.where(constant, letter, 256 + np.arange(L, dtype=np.int64))
+    uniq, first, inverse, counts = np.unique(key, return_index=True, return_inverse=True, return_counts=True)
+    order = np.argsort(first, kind="stable")          # pattern number by first occurrence
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    full_to_compressed = rank[inverse].astype(np.int64)
+    multiplicity = counts[order].astype(float)
+    pattern_codes = np.ascontiguousarray(fixed[:, first[order]])
+    pos_sorted = np.argsort(full_to_compressed, kind="stable")
+    bounds = np.concatenate(([0], np.cumsum(counts[order])))
+    c2f = {p: pos_sorted[bounds[p]:bounds[p + 1]].astype(int) for p in range(len(order))}
+    return pattern_codes, multiplicity, full_to_compressed, c2f
+
+
+class SequenceData:
+    """Alignment container with TreeTime's SequenceData interface for dense
+    alignments (dict name -> sequence, an iterable of records with id/name/seq,
+    or a FASTA file)."""
+
+    def __init__(self, aln, ref=None, logger=None, convert_upper=True, sequence_length=None, compress=True,
+                 word_length=1, sequence_type=None, fill_overhangs=True, seq_multiplicity=None, ambiguous=None,
+                 **kwargs):
+        self.logger = logger if logger else (lambda *a, **k: None)
+        self.convert_upper = convert_upper
+        self.compress = compress
+        self.word_length = word_length
+        self.fill_overhangs = fill_overhangs
+        self.ambiguous = ambiguous
+        self.sequence_type = sequence_type
+        self.seq_multiplicity = seq_multiplicity or {}
+        self.additional_constant_sites = kwargs.get("additional_constant_sites", 0)
+        self.is_sparse = False
+        self.ref = ref
+        self._full_length = int(sequence_length) if sequence_length else None
+        self._aln = None
+        self._compressed_alignment = None
+        self.aln = aln
+
+    # ------------------------------------------------------------ ingest
+    @property
+    def aln(self):
+        return self._aln
+
+    @aln.setter
+    def aln(self, in_aln):
+        self._aln = None
+        self._compressed_alignment = None
+        if in_aln is None:
+            return
+        if isinstance(in_aln, str) and os.path.isfile(in_aln):
+            in_aln = read_fasta(in_aln)
+        if isinstance(in_aln, dict):
+            raw = [(k, v) for k, v in in_aln.items()]
+        else:
+            try:
+                raw = [(_record_name(r), r) for r in in_aln]
+            except TypeError:
+                raise MissingDataError("SequenceData: loading alignment failed... " + str(in_aln))
+        if not raw:
+            raise MissingDataError("SequenceData: loading alignment failed... empty alignment")
+        first = [seq2array(s, convert_upper=self.convert_upper) for _, s in raw[:50]]
+        self.likely_alphabet = guess_alphabet(first)
+        if self.ambiguous is None:
+            self.ambiguous = "N" if self.likely_alphabet == "nuc" else "X"
+        arrays = OrderedDict()
+        for name, s in raw:
+            arrays[name] = seq2array(s, convert_upper=self.convert_upper, fill_overhangs=self.fill_overhangs,
+                                     ambiguous=self.ambiguous)
+        lengths = {len(a) for a in arrays.values()}
+        if len(lengths) != 1:
+            raise MissingDataError("SequenceData: sequences have different lengths")
+        L = lengths.pop()
+        if self._full_length:
+            if self._full_length < L:
+                raise AttributeError("SequenceData.aln: specified sequence length is smaller than alignment length!")
+            self.additional_constant_sites = max(0, self._full_length - L)
+            if self.additional_constant_sites:
+                raise NotImplementedError("additional constant sites are not supported")
+        else:
+            self._full_length = L
+        self._aln = arrays
+        self.sequence_names = list(arrays.keys())
+        self.codes = np.stack([chars_to_codes(arrays[k]) for k in self.sequence_names]) \
+            if arrays else np.zeros((0, L), np.uint8)
+        self.make_compressed_alignment()
+
+    @property
+    def full_length(self):
+        return self._full_length
+
+    @property
+    def compressed_length(self):
+        return self._compressed_length
+
+    def make_compressed_alignment(self, device=None):
+        amb = ord(self.ambiguous) if self.ambiguous else None
+        if device is not None and self.compress:
+            from . import engine
+            pc, mult, f2c, c2f = engine.compress_columns(self.codes, amb, device)
+        else:
+            pc, mult, f2c, c2f = compress_codes(self.codes, amb, self.compress)
+        self.compressed_codes = pc
+        self._multiplicity = mult
+        self.full_to_compressed_sequence_map = f2c
+        self.compressed_to_full_sequence_map = c2f
+        self._compressed_length = len(mult)
+        self._compressed_alignment = None
+        self.name_to_row = {k: i for i, k in enumerate(self.sequence_names)}
+        return ttconf.SUCCESS
+
+    @property
+    def compressed_alignment(self):
+        if self._compressed_alignment is None:
+            if not self.compress:
+                self._compressed_alignment = self._aln
+            else:
+                chars = codes_to_chars(self.compressed_codes)
+                self._compressed_alignment = OrderedDict(
+                    (k, chars[i]) for i, k in enumerate(self.sequence_names))
+        return self._compressed_alignment
+
+    def multiplicity(self, mask=None):
+        if mask is None:
+            return self._multiplicity
+        return self._multiplicity * mask
+
+    # ------------------------------------------------------ sequence maps
+    def compressed_to_full_sequence(self, sequence, include_additional_constant_sites=False, as_string=False):
+        tmp = sequence[self.full_to_compressed_sequence_map[: self.full_length]]
+        if as_string:
+            return "".join(tmp.astype("U"))
+        return tmp
+
+    def differences(self, seq1, seq2, seq1_compressed=True, seq2_compressed=True, mask=None):
+        """Sorted (anc, pos, der) list between two sequences, expanded to full
+        length (treetime/sequence_data.py:541-568, dense alignments)."""
+        if seq1_compressed:
+            seq1 = self.compressed_to_full_sequence(seq1)
+        if seq2_compressed:
+            seq2 = self.compressed_to_full_sequence(seq2)
+        if mask is None:
+            pos = np.flatnonzero(seq1 != seq2)
+        else:
+            pos = np.flatnonzero((seq1 != seq2) & (mask > 0))
+        return [(seq1[p], int(p), seq2[p]) for p in pos]

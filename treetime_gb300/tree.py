@@ -1,0 +1,273 @@
+"""Rooted trees with the traversal interface TreeTime relies on.
+
+``Clade`` and ``Tree`` expose the Bio.Phylo.BaseTree calls that the
+reconstruction path uses (find_clades with 'preorder' / 'postorder' / 'level',
+get_terminals, get_nonterminals, count_terminals, ladderize,
+total_branch_length, is_terminal, iteration over children), with Biopython's
+documented order semantics: preorder is depth-first with children in list
+order, postorder visits children first, ladderize is a stable ascending sort
+of each clade's children by their number of tips.  Node order fixes internal
+node names and so it is part of the output contract.
+
+All traversals are iterative, so caterpillar trees with many thousands of
+levels do not hit Python's recursion limit.  Any object with the same
+attributes (for instance a real Bio.Phylo tree) works wherever a ``Tree`` is
+accepted.
+"""
+
+import io
+import os
+
+
+def _iter_preorder(root):
+    stack = [root]
+    while stack:
+        node = stack.pop()
+        yield node
+        ch = node.clades
+        for i in range(len(ch) - 1, -1, -1):
+            stack.append(ch[i])
+
+
+def _iter_postorder(root):
+    stack = [(root, False)]
+    while stack:
+        node, expanded = stack.pop()
+        if expanded or not node.clades:
+            yield node
+        else:
+            stack.append((node, True))
+            ch = node.clades
+            for i in range(len(ch) - 1, -1, -1):
+                stack.append((ch[i], False))
+
+
+def _iter_level(root):
+    queue = [root]
+    i = 0
+    while i < len(queue):
+        node = queue[i]
+        i += 1
+        yield node
+        queue.extend(node.clades)
+
+
+_ORDERS = {"preorder": _iter_preorder, "postorder": _iter_postorder, "level": _iter_level}
+
+
+def iter_clades(root, order="preorder"):
+    """Traverse any duck-typed clade (``.clades`` lists) in the given order."""
+    return _ORDERS[order](root)
+
+
+class _Traversal:
+    def _start(self):
+        raise NotImplementedError
+
+    def find_clades(self, target=None, terminal=None, order="preorder"):
+        for node in _ORDERS[order](self._start()):
+            if terminal is not None and (not node.clades) != terminal:
+                continue
+            if target is not None:
+                if isinstance(target, str):
+                    if node.name != target:
+                        continue
+                elif callable(target):
+                    if not target(node):
+                        continue
+            yield node
+
+    def get_terminals(self, order="preorder"):
+        return [c for c in _ORDERS[order](self._start()) if not c.clades]
+
+    def get_nonterminals(self, order="preorder"):
+        return [c for c in _ORDERS[order](self._start()) if c.clades]
+
+    def count_terminals(self):
+        return sum(1 for c in _iter_preorder(self._start()) if not c.clades)
+
+    def total_branch_length(self):
+        return sum(c.branch_length for c in _iter_preorder(self._start()) if c.branch_length)
+
+    def ladderize(self, reverse=False):
+        """Stable sort of every clade's children by number of tips."""
+        ntips = {}
+        for node in _iter_postorder(self._start()):
+            if node.clades:
+                node.clades.sort(key=lambda c: ntips[id(c)], reverse=reverse)
+                ntips[id(node)] = sum(ntips[id(c)] for c in node.clades)
+            else:
+                ntips[id(node)] = 1
+
+
+class Clade(_Traversal):
+    def __init__(self, branch_length=None, name=None, clades=None, confidence=None):
+        self.branch_length = branch_length
+        self.name = name
+        self.clades = list(clades) if clades else []
+        self.confidence = confidence
+
+    def _start(self):
+        return self
+
+    def is_terminal(self):
+        return not self.clades
+
+    def __iter__(self):
+        return iter(self.clades)
+
+    def __len__(self):
+        return len(self.clades)
+
+    def __getitem__(self, i):
+        return self.clades[i]
+
+    def __repr__(self):
+        return "Clade(name=%r, branch_length=%r)" % (self.name, self.branch_length)
+
+
+class Tree(_Traversal):
+    def __init__(self, root=None, rooted=True, name=None):
+        self.root = root if root is not None else Clade()
+        self.rooted = rooted
+        self.name = name
+
+    def _start(self):
+        return self.root
+
+    @property
+    def clade(self):
+        return self.root
+
+    def is_terminal(self):
+        return not self.root.clades
+
+    def __iter__(self):
+        return iter(self.root.clades)
+
+
+# --------------------------------------------------------------------------
+# Newick I/O
+# --------------------------------------------------------------------------
+
+def _is_number(s):
+    try:
+        float(s)
+        return True
+    except ValueError:
+        return False
+
+
+def parse_newick(text):
+    """Parse one Newick tree.  A label after ')' that parses as a number is a
+    support value (``confidence``), otherwise the clade name, as in
+    Bio.Phylo's Newick reader."""
+    root = Clade()
+    stack = []
+    cur = root
+    i, n = 0, len(text)
+    expect_len = False
+    after_close = False
+    while i < n:
+        ch = text[i]
+        if ch == "(":
+            child = Clade()
+            cur.clades.append(child)
+            stack.append(cur)
+            cur = child
+            after_close = False
+            i += 1
+        elif ch == ",":
+            if not stack:
+                raise ValueError("malformed Newick: ',' at top level")
+            child = Clade()
+            stack[-1].clades.append(child)
+            cur = child
+            after_close = False
+            expect_len = False
+            i += 1
+        elif ch == ")":
+            if not stack:
+                raise ValueError("malformed Newick: unbalanced ')'")
+            cur = stack.pop()
+            after_close = True
+            expect_len = False
+            i += 1
+        elif ch == ":":
+            expect_len = True
+            i += 1
+        elif ch == ";":
+            break
+        elif ch == "[":
+            j = text.find("]", i)
+            i = n if j < 0 else j + 1
+        elif ch.isspace():
+            i += 1
+        else:
+            if ch == "'":
+                j = text.index("'", i + 1)
+                tok = text[i + 1:j]
+                i = j + 1
+            else:
+                j = i
+                while j < n and text[j] not in "(),:;[" and not text[j].isspace():
+                    j += 1
+                tok = text[i:j]
+                i = j
+            if expect_len:
+                cur.branch_length = float(tok)
+                expect_len = False
+            elif after_close and _is_number(tok):
+                cur.confidence = float(tok)
+            else:
+                cur.name = tok
+    if stack:
+        raise ValueError("malformed Newick: unbalanced '('")
+    return Tree(root=root, rooted=False)
+
+
+def read_newick(source):
+    """Tree from a Newick string, a file name or an open file."""
+    if hasattr(source, "read"):
+        return parse_newick(source.read())
+    if isinstance(source, str) and os.path.isfile(source):
+        with open(source) as fh:
+            return parse_newick(fh.read())
+    if isinstance(source, str) and source.strip().endswith(";"):
+        return parse_newick(source)
+    raise ValueError("not a Newick string or file: %r" % (source[:80] if isinstance(source, str) else source))
+
+
+def to_newick(tree, precision=None):
+    """Newick text of a tree (iterative, no recursion limit)."""
+    out = io.StringIO()
+    root = tree.root if hasattr(tree, "root") else tree
+    fmt = (lambda x: repr(float(x))) if precision is None else (lambda x: ("%." + str(precision) + "g") % x)
+    # explicit stack of (node, state): state 0 = open, 1 = close
+    stack = [(root, 0)]
+    parts = []
+    while stack:
+        node, state = stack.pop()
+        if state == 0:
+            if node.clades:
+                parts.append("(")
+                stack.append((node, 1))
+                for k in range(len(node.clades) - 1, -1, -1):
+                    stack.append((node.clades[k], 0))
+                    if k > 0:
+                        stack.append((None, 2))
+            else:
+                parts.append(_label(node, fmt))
+        elif state == 1:
+            parts.append(")" + _label(node, fmt))
+        else:
+            parts.append(",")
+    out.write("".join(parts) + ";")
+    return out.getvalue()
+
+
+def _label(node, fmt):
+    s = node.name or ""
+    if node.branch_length is not None:
+        s += ":" + fmt(node.branch_length)
+    return s

@@ -1,0 +1,260 @@
+/*
+ * treetime_gb300: C ABI of the GB300 (sm_103a) Felsenstein-pruning library.
+ *
+ * The library replaces the numpy hot path of TreeTime's TreeAnc / GTR classes:
+ *
+ *   tt_branch_pmats      GTR.expQt / GTR._exp_lt                treetime/gtr.py:1027-1067
+ *   tt_propagate         GTR.propagate_profile / GTR.evolve      treetime/gtr.py:965-1025
+ *   tt_marginal          TreeAnc._ml_anc_marginal with its post-order, root and
+ *                        pre-order passes                        treetime/treeanc.py:762-932
+ *                        (normalize_profile, prof2seq argmax     treetime/seq_utils.py:232-307)
+ *   tt_marginal_ss       the same for GTR_site_specific models   treetime/gtr_site_specific.py:331-437
+ *   tt_joint             TreeAnc._ml_anc_joint                   treetime/treeanc.py:934-1080
+ *   tt_state_pairs       GTR.state_pair + TreeAnc.add_branch_state
+ *                                                                treetime/gtr.py:631-712, treetime/treeanc.py:1148-1163
+ *   tt_optimal_t_pairs   GTR.optimal_t_compressed (state pairs) with GTR.prob_t_compressed
+ *                                                                treetime/gtr.py:717-749, :816-920
+ *   tt_optimal_t_profiles GTR.optimal_t_compressed(profiles=True) with GTR.prob_t_profiles
+ *                                                                treetime/gtr.py:816-963
+ *   tt_compress_columns  SequenceData.make_compressed_alignment  treetime/sequence_data.py:325-464
+ *
+ * Conventions
+ *   - Every pointer inside the structs and every array argument is DEVICE memory owned by the
+ *     caller, unless its comment says "host".  The library allocates nothing on the hot path.
+ *   - Every call is enqueued on `stream` (a cudaStream_t passed as void*; NULL = legacy default
+ *     stream) and returns a tt_status.  Launch/argument errors are reported synchronously; numeric
+ *     conditions found by kernels are written to a device status word (`status` argument, one
+ *     int32 the caller zeroes) and read back by the caller after synchronising.
+ *   - Kernels never trap and never wait without bound.
+ *   - One "forest" holds one or many independent trees with their own pattern counts and models;
+ *     one launch covers the whole forest (batched mode).
+ */
+#ifndef TREETIME_GB300_H
+#define TREETIME_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TT_ABI_VERSION 1
+
+typedef int32_t tt_status;
+enum {
+    TT_OK = 0,
+    TT_ERR_INVALID = 1,      /* bad sizes / pointers / unsupported alphabet size (host check)   */
+    TT_ERR_NUMERIC = 2,      /* exp(mu*lambda*t) argument > 10, as GTR._exp_lt raises ValueError */
+    TT_ERR_OOM = 3,          /* caller-provided workspace too small                              */
+    TT_ERR_TIMEOUT = 4,      /* a bounded device wait ran out                                    */
+    TT_ERR_CUDA = 5,         /* CUDA runtime error (message via tt_last_error)                  */
+    TT_ERR_UNSUPPORTED = 6,  /* combination of options not implemented                          */
+    TT_ERR_BRACKET = 7       /* Brent bracket invalid: f(xb) < f(xa), f(xc) fails (scipy raises) */
+};
+
+/* Precision of the marginal pass. */
+enum {
+    TT_PREC_F64 = 0,         /* FP64, log-domain arithmetic of TreeTime                         */
+    TT_PREC_F32 = 1          /* FP32 profiles with per-node power-of-two rescaling; FP64 log-LH */
+};
+
+/* One tree of a forest.  Local node ids: internal nodes 0..n_int-1 sorted by height (children
+ * before parents, the root last); tips n_int..n_int+n_tip-1. */
+typedef struct tt_tree {
+    int64_t node_base;    /* global id of local node 0 (index into the per-node arrays)            */
+    int64_t level_base;   /* first entry of this tree in tt_forest.level_off                       */
+    int64_t pat_base;     /* first pattern of this tree in per-pattern arrays (mult, site_lh, ...) */
+    int64_t tip_base;     /* byte offset of the tree's tip codes: tip row r, pattern p at
+                             tip_codes[tip_base + r*n_patterns + p]                                 */
+    int64_t prof_base;    /* first profile row of the tree: internal node k, pattern p ->
+                             row prof_base + k*n_patterns + p (rows hold `width` elements)         */
+    int64_t tipprof_base; /* first tip-profile row: tip j (= local id - n_int) -> row
+                             tipprof_base + j*n_patterns + p                                        */
+    int64_t state_base;   /* state byte of local node k, pattern p: state_base + k*n_patterns + p  */
+    int32_t n_int;
+    int32_t n_tip;
+    int32_t n_levels;     /* number of height levels of internal nodes                             */
+    int32_t n_patterns;
+    int32_t model;        /* row of this tree's model in tt_model arrays                           */
+    int32_t reserved;
+} tt_tree;
+
+typedef struct tt_forest {
+    int32_t n_trees;
+    int32_t n_states;          /* q: 2..32                                                         */
+    int32_t width;             /* row width of profile buffers: q rounded up to a multiple of 4    */
+    int32_t max_levels;        /* max over trees of n_levels                                       */
+    int64_t n_nodes;           /* total nodes over all trees                                       */
+    int64_t n_patterns;        /* total patterns over all trees                                    */
+    const tt_tree* trees;      /* [n_trees]                                                        */
+    const int32_t* level_off;  /* per tree n_levels+1 entries: level h = local internal ids
+                                  [level_off[level_base+h], level_off[level_base+h+1])             */
+    const int32_t* child_off;  /* [n_nodes+1] CSR by global id; children listed in clade order     */
+    const int32_t* child_idx;  /* local ids of children                                            */
+    const int32_t* parent;     /* [n_nodes] local id of the parent, -1 at the root                 */
+    const int32_t* tip_row;    /* [n_nodes] tips: row of the tip's codes, -1 = tip has no sequence */
+    const int64_t* mask_off;   /* [n_nodes] element offset of the node's mask row, -1 = no mask;
+                                  may be NULL when no node has a mask                               */
+    const double*  masks;      /* mask values (per pattern, in [0,1])                              */
+    const double*  bl;         /* [n_nodes] branch length above the node as used by the model       */
+    const uint8_t* tip_codes;  /* tip character bytes                                              */
+    const double*  mult;       /* [n_patterns] pattern multiplicities                              */
+    /* Schedule of the persistent pruning kernels: tiles of 32 consecutive patterns of one tree,
+       given as (tree, first pattern) pairs, largest trees first.  One CTA walks a whole tree for a
+       tile; tiles never wait on each other. */
+    const int32_t* work;       /* [n_work][2]                                                      */
+    int32_t n_work;
+    int32_t warps_per_block;   /* 4, 8, 16 or 32 warps share the nodes of a level (0: 8)           */
+    int32_t max_blocks;        /* grid size cap (0: one CTA per tile)                              */
+    int32_t reserved;
+} tt_forest;
+
+typedef struct tt_model {
+    int32_t n_models;
+    int32_t n_states;
+    const double* V;           /* [n_models][q][q] right eigenvectors                              */
+    const double* Vinv;        /* [n_models][q][q]                                                 */
+    const double* lam;         /* [n_models][q] eigenvalues                                        */
+    const double* mu;          /* [n_models]                                                       */
+    const double* pi;          /* [n_models][q] equilibrium frequencies                            */
+    const double* lut;         /* [256][q] profile row of each character byte                     */
+} tt_model;
+
+/* Branch matrices produced by tt_branch_pmats for every node (the branch above it), rows padded
+ * to `width`: entry (i, j) = P(child state i | parent state j) at [node][i][j]. */
+typedef struct tt_pmats {
+    double* p64;               /* [n_nodes][q][width]  P(t) = max(0, V diag(exp(mu lam t)) V^-1)  */
+    float*  p32;               /* [n_nodes][q][width]  FP32 copy (may be NULL)                     */
+    double* logp64;            /* [n_nodes][q][width]  log(max(1e-12, P))  (may be NULL)           */
+} tt_pmats;
+
+/* Outputs of the marginal pass.  Buffers hold float (TT_PREC_F32) or double (TT_PREC_F64). */
+typedef struct tt_marginal_out {
+    void*    partial;          /* internal nodes' subtree profiles (marginal_subtree_LH; FP32 rows
+                                  are power-of-two scaled, not normalised)       REQUIRED           */
+    void*    posterior;        /* internal nodes' marginal profiles              REQUIRED           */
+    void*    outgroup;         /* internal nodes' outgroup profiles, or NULL                        */
+    void*    tip_posterior;    /* tips' marginal profiles, or NULL (needs reconstruct_tips)         */
+    void*    tip_outgroup;     /* tips' outgroup profiles, or NULL                                  */
+    uint8_t* states;           /* argmax state per node and pattern              REQUIRED           */
+    double*  site_lh;          /* [n_patterns] log-likelihood of each pattern    REQUIRED           */
+    double*  tree_lh;          /* [n_trees] sum of site_lh * mult                REQUIRED           */
+    unsigned long long* n_diff;/* [n_trees] states that changed, or NULL                            */
+    const double* root_uniform;/* [n_patterns] draws for sampling the root state, or NULL (argmax) */
+    int32_t  reconstruct_tips; /* also run the pre-order step at tips                              */
+    int32_t  count_diff;       /* compare with the states already in `states` to count n_diff      */
+} tt_marginal_out;
+
+typedef struct tt_joint_out {
+    double*  lx;               /* [rows of internal nodes][width] joint_Lx scratch (FP64)           */
+    uint8_t* cx;               /* [rows of internal nodes][width] argmax child state per parent state */
+    uint8_t* states;           /* state per node and pattern                                        */
+    double*  site_lh;          /* [n_patterns] joint log-likelihood of each pattern                 */
+    double*  tree_lh;          /* [n_trees] multiplicity-weighted sum                               */
+    unsigned long long* n_diff;/* [n_trees] or NULL                                                 */
+    const double* root_uniform;/* [n_patterns] or NULL                                              */
+    int32_t  reconstruct_tips;
+    int32_t  count_diff;
+} tt_joint_out;
+
+/* ---------------------------------------------------------------- library */
+int32_t     tt_abi_version(void);
+const char* tt_status_string(tt_status s);
+/* Copies the last error message of the calling thread into buf (host). Returns its length. */
+size_t      tt_last_error(char* buf, size_t n);
+/* Number of streaming multiprocessors of the current device (host query, no launch). */
+int32_t     tt_device_sm_count(void);
+
+/* -------------------------------------------------------------- a4: P(t)
+ * P(t) for the branch above every node of the forest (FP64 + optional FP32 / log copies).
+ * Replaces GTR.expQt (treetime/gtr.py:1051-1067); a kernel that finds mu*lambda*t > 10 sets
+ * *status = TT_ERR_NUMERIC, as GTR._exp_lt raises ValueError (treetime/gtr.py:1042-1047). */
+tt_status tt_branch_pmats(const tt_forest* f, const tt_model* m, tt_pmats out, int32_t* status, void* stream);
+
+/* ------------------------------------------------- a5/a6: profile transport
+ * res[a, :] = prof[a, :] . P(t_a) (transpose = 0, propagate_profile) or
+ * prof[a, :] . P(t_a)^T (transpose = 1, evolve) for n rows; optional log.  `t_index[a]` selects
+ * the branch matrix row in `pmat` (q*q doubles each).  Replaces GTR.propagate_profile / evolve
+ * (treetime/gtr.py:965-1025). */
+tt_status tt_propagate(int32_t q, int64_t n, const double* prof, const double* pmat, const int32_t* t_index,
+                       int32_t transpose, int32_t return_log, double* res, void* stream);
+
+/* ------------------------------------------------------- a8-a12: marginal
+ * Post-order pruning, root posterior and likelihood, pre-order outgroup/posterior passes and
+ * argmax (or sampled) states for every tree of the forest, in one persistent launch.
+ * Requires tt_branch_pmats first (p64 for TT_PREC_F64, p32 for TT_PREC_F32).
+ * Replaces TreeAnc._ml_anc_marginal (treetime/treeanc.py:762-932). */
+tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt_pmats* pm, int32_t precision,
+                      const tt_marginal_out* out, int32_t* status, void* stream);
+
+/* Site-specific model (GTR_site_specific): per-pattern V, V^-1, eigenvalues, rates and
+ * equilibrium frequencies; P_a(t) evaluated in the eigenbasis, with TreeTime's linear
+ * interpolation on the time grid `t_grid` (n_grid points) when `approximate` is set and
+ * t * rate_scale < 10 (treetime/gtr_site_specific.py:331-437).  Single-tree forests only.
+ *   lam [P][q], V [P][q][q], Vinv [P][q][q], mu [P], pi [P][q]  (FP64, per pattern) */
+tt_status tt_marginal_ss(const tt_forest* f, const double* lam, const double* V, const double* Vinv,
+                         const double* mu, const double* pi, const double* lut, const double* t_grid,
+                         int32_t n_grid, double rate_scale, int32_t approximate, int32_t precision,
+                         const tt_marginal_out* out, int32_t* status, void* stream);
+
+/* ------------------------------------------------------------ a13: joint
+ * Max-product reconstruction in FP64 (log domain), root argmax/sampling, pre-order backtrack.
+ * Requires tt_branch_pmats with logp64.  Replaces TreeAnc._ml_anc_joint
+ * (treetime/treeanc.py:934-1080). */
+tt_status tt_joint(const tt_forest* f, const tt_model* m, const tt_pmats* pm, const tt_joint_out* out,
+                   int32_t* status, void* stream);
+
+/* ---------------------------------------------------- a14: state pairs
+ * For every non-root node k with use[k] != 0: the (parent, child) state-pair histogram
+ * hist[k][i][j] = sum over patterns of mult (times the node's mask) where the parent has state i
+ * and the child state j, from the node states in `states` (internal / reconstructed nodes) or the
+ * tips' characters (through `char_state`: byte -> state index, 255 = not a state; for q >= 10
+ * TreeTime maps unknown characters to state 1, which the caller encodes in char_state).
+ * Pairs touching `gap_state` are skipped when ignore_gaps (gap_state < 0: none).
+ * Replaces GTR.state_pair + TreeAnc.add_branch_state (treetime/gtr.py:631-712). */
+tt_status tt_state_pairs(const tt_forest* f, const uint8_t* states, const uint8_t* char_state,
+                         int32_t tips_use_states, int32_t gap_state, int32_t ignore_gaps,
+                         const uint8_t* use, double* hist, void* stream);
+
+/* ----------------------------------------------- a15/a17: Brent, pairs
+ * For each of n branches: counts[b][i][j] (state-pair counts of parent state i and child state
+ * j; TreeTime truncates histogram counts to integers before this step), model row model_of[b]; minimises -sum count*log(max(P(s^2)[j][i], 1e-24)) over s with
+ * Brent's method (bracket (-2, sqrt(hamming), 2), tolerance tol, at most 500 iterations) and
+ * writes t = s^2 (the Hamming distance when unsuccessful).  info[b]: iterations, or -1 when the
+ * bracket condition failed (TreeTime lets scipy raise ValueError).
+ * Replaces GTR.optimal_t_compressed(profiles=False) (treetime/gtr.py:816-920). */
+tt_status tt_optimal_t_pairs(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
+                             const tt_model* m, double tol, double* t_out, int32_t* info, void* stream);
+
+/* Objective values -sum count*log(max(P(t)[j][i],1e-24)) for n (branch, t) pairs: prob_t_compressed
+ * with return_log (treetime/gtr.py:717-749), for tests and the GTR API. */
+tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
+                          const tt_model* m, const double* t, double* logp_out, void* stream);
+
+/* ------------------------------------------- a16/a17: Brent, profiles
+ * For each of n branches b (node id node_of[b] of the forest): parent-side profiles pp (the
+ * outgroup) and child-side profiles pc (subtree) as rows of `width` elements at row offsets
+ * pp_row[b], pc_row[b] (+ pattern), tips' child profiles from their codes when pc_row[b] < 0;
+ * minimises -sum mult*mask*log(pc.P(s^2).pp + 1e-24)*non_gap + exp(s^4/1e4) with Brent.
+ * `prec` says whether the profile buffers hold float or double.
+ * Replaces GTR.optimal_t_compressed(profiles=True) with GTR.prob_t_profiles
+ * (treetime/gtr.py:816-963). */
+tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
+                                const void* pp, const int64_t* pp_row, const void* pc, const int64_t* pc_row,
+                                int32_t prec, int32_t gap_state, int32_t ignore_gaps, double tol,
+                                double* t_out, int32_t* info, void* stream);
+
+/* -------------------------------------------------- a1: compression
+ * Column classes of a tips x sites byte matrix (row-major, n_rows x n_cols): key[c] = the letter
+ * of a constant column (after rewriting {X, ambiguous} columns to X) or 256 + c for a variable
+ * column, and fixed_letter[c] = the letter that replaces `ambiguous` in such columns (or -1).
+ * The host turns keys into pattern numbers by first occurrence.  Replaces the column loop of
+ * SequenceData.make_compressed_alignment (treetime/sequence_data.py:370-412). */
+tt_status tt_compress_columns(const uint8_t* codes, int64_t n_rows, int64_t n_cols, int32_t ambiguous,
+                              int64_t* key, int32_t* fixed_letter, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TREETIME_GB300_H */

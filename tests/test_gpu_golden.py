@@ -1,0 +1,185 @@
+"""GPU parity against TreeTime's own outputs (golden vectors) and the CPU
+oracle, through the public TreeAnc API (which drives the C-ABI library).
+
+Tolerances (written here, per the contract of this port):
+  * FP64 kernels: log-likelihoods 1e-10 relative, profiles 1e-10 absolute;
+  * FP32-scaled kernels: profiles 1e-5 absolute, total log-likelihood 1e-6
+    relative, per-pattern log-likelihood 1e-5 absolute;
+  * joint states bit-exact, except patterns where the reference's own top-two
+    margin at some node is below 1e-9 (counted, reported);
+  * marginal argmax states bit-exact except where the reference profile's
+    top-two margin is below 1e-9 (FP64) / 1e-5 (FP32);
+  * branch lengths 1e-6 relative + 1e-10 absolute (FP64 profiles / pairs).
+"""
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from oracle import anc
+
+pytestmark = pytest.mark.gpu
+
+CASES = gc.case_names()
+PRECISIONS = ["f64", "f32"]
+
+
+def _tree_anc(g, precision):
+    from treetime_gb300 import TreeAnc
+    tree, aln, model, masks = gc.inputs_from(g)
+    t = TreeAnc(tree=tree, aln=aln, gtr=model, compress=bool(g["compress"]), verbose=0, rng_seed=int(g["rng_seed"]),
+                ignore_gaps=bool(g["ignore_gaps"]), precision=precision)
+    if masks:
+        for n in t.tree.find_clades():
+            if n.name in masks:
+                n.mask = masks[n.name]
+    return t
+
+
+def _by_name(t):
+    return {n.name: n for n in t.tree.find_clades()}
+
+
+def _names_map(names, arr):
+    return {str(k): arr[i] for i, k in enumerate(names)}
+
+
+def _top2(p):
+    s = np.sort(p, axis=1)
+    return s[:, -1] - s[:, -2]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("case", CASES)
+def test_marginal_matches_treetime(case, precision):
+    g = gc.load(case)
+    t = _tree_anc(g, precision)
+    sample = "root" if bool(g["sample_root"]) else False
+    ndiff = t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=bool(g["reconstruct_tip_states"]),
+                                        sample_from_profile=sample)
+    f32 = precision == "f32"
+    assert ndiff == int(g["marg_N_diff"])
+    rel = 1e-6 if f32 else 1e-10
+    assert abs(t.tree.total_sequence_LH - float(g["marg_total_LH"])) <= rel * abs(float(g["marg_total_LH"]))
+    np.testing.assert_allclose(t.tree.sequence_LH, g["marg_sequence_LH"], rtol=0 if f32 else 1e-10,
+                               atol=1e-5 if f32 else 1e-10)
+    nodes = _by_name(t)
+    tol_prof = 1e-5 if f32 else 1e-10
+    margin_tol = 1e-5 if f32 else 1e-9
+    have_prof = "marg_profile" in g
+    # the reference's own profiles (oracle, pinned to TreeTime) give the top-two margins
+    tree_o, _, model_o, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree_o)
+    if "mask_names" in g:
+        masks = _names_map(g["mask_names"], g["mask_rows"])
+        for n in anc.preorder(tree_o.root):
+            if n.name in masks:
+                n.mask = masks[n.name]
+    ores = anc.marginal(tree_o, gc.compressed_from(g, model_o), g["multiplicity"], model_o,
+                        len(g["full_to_compressed"]), reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    want = _names_map(g["marg_cseq_names"], g["marg_cseq"])
+    for name, codes in want.items():
+        got = gc.codes_of(nodes[name]._cseq)
+        if sample and nodes[name].up is None:
+            np.testing.assert_array_equal(got, codes, err_msg=name)
+            continue
+        ok = (got == codes) | (_top2(ores["profile"][name]) < margin_tol)
+        assert ok.all(), (name, np.flatnonzero(~ok)[:10])
+    if have_prof:
+        for key, attr in (("marg_profile", "marginal_profile"), ("marg_subtree", "marginal_subtree_LH"),
+                          ("marg_outgroup", "marginal_outgroup_LH")):
+            for name, v in _names_map(g[key + "_names"], g[key]).items():
+                np.testing.assert_allclose(getattr(nodes[name], attr), v, rtol=0, atol=tol_prof,
+                                           err_msg="%s %s" % (attr, name))
+    # second call counts changes against the first reconstruction
+    again = t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    if not sample:
+        assert again == int(g["marg_N_diff_again"])
+
+
+def _joint_margin_mask(g, model, tree_prepared):
+    """Patterns where the reference's max-product choice at some node has a
+    top-two margin below 1e-9 (oracle margins)."""
+    aln = gc.compressed_from(g, model)
+    res = anc.joint(tree_prepared, aln, g["multiplicity"], model, len(g["full_to_compressed"]),
+                    reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    bad = res["root_margin"] < 1e-9
+    for n in anc.preorder(tree_prepared.root):
+        if n.up is None or n.name not in res["margin"]:
+            continue
+        ps = res["seq_idx"].get(n.up.name)
+        if ps is None:
+            continue
+        m = res["margin"][n.name][np.arange(len(ps)), ps]
+        bad |= m < 1e-9
+    return bad
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_joint_matches_treetime(case):
+    g = gc.load(case)
+    if str(g["kind"]) != "gtr":
+        pytest.skip("joint reconstruction is defined for single-matrix models")
+    t = _tree_anc(g, "f64")
+    sample = "root" if bool(g["sample_root"]) else False
+    ndiff = t.infer_ancestral_sequences(marginal=False, reconstruct_tip_states=bool(g["reconstruct_tip_states"]),
+                                        sample_from_profile=sample)
+    assert ndiff == int(g["joint_N_diff"])
+    np.testing.assert_allclose(t.tree.sequence_LH, g["joint_sequence_LH"], rtol=1e-12, atol=1e-12)
+    assert abs(t.tree.sequence_joint_LH - float(g["joint_total_LH"])) <= 1e-12 * abs(float(g["joint_total_LH"]))
+    tree, _, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    near_tie = _joint_margin_mask(g, model, tree)
+    nodes = _by_name(t)
+    for name, codes in _names_map(g["joint_cseq_names"], g["joint_cseq"]).items():
+        got = gc.codes_of(nodes[name]._cseq)
+        diff = got != codes
+        assert not (diff & ~near_tie).any(), (name, np.flatnonzero(diff & ~near_tie)[:10])
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "jbl" in gc.load(c)])
+def test_joint_branch_lengths_and_mutations_match_treetime(case):
+    g = gc.load(case)
+    t = _tree_anc(g, "f64")
+    t.infer_ancestral_sequences(marginal=False, reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    t.optimize_branch_lengths_joint()
+    nodes = _by_name(t)
+    for name, v in _names_map(g["jbl_names"], g["jbl"]).items():
+        got = nodes[name].branch_length
+        if abs(got - v) > 1e-6 * abs(v) + 1e-10:
+            # equally optimal: same objective value at both lengths
+            n = nodes[name]
+            pairs, cnt = n.branch_state["pair"], n.branch_state["multiplicity"]
+            f = lambda tt: -anc.prob_t_compressed(n.tt.gtr, pairs, cnt, tt, return_log=True)
+            assert abs(f(got) - f(v)) <= 1e-9 * abs(f(v)) + 1e-12, (name, got, v)
+        assert nodes[name].mutation_length == got
+    if "mutations" in g:
+        got = sorted("%s|%s|%d|%s" % (n.name, a, p, d) for n in t.tree.find_clades() if n.up is not None
+                     for (a, p, d) in n.mutations)
+        assert got == sorted(g["mutations"].tolist())
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("case", [c for c in CASES if "mbl" in gc.load(c)])
+def test_marginal_branch_lengths_match_treetime(case, precision):
+    g = gc.load(case)
+    t = _tree_anc(g, precision)
+    t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    nodes = _by_name(t)
+    names = g["mbl_names"].tolist()
+    got = t._marginal_branch_lengths([nodes[n] for n in names], 1e-10)
+    # reference profiles (oracle, FP64) to judge flat objectives
+    tree_o, _, model_o, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree_o)
+    ores = anc.marginal(tree_o, gc.compressed_from(g, model_o), g["multiplicity"], model_o,
+                        len(g["full_to_compressed"]), reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
+    rel = 1e-6 if precision == "f64" else 2e-3
+    obj_rel = 1e-9 if precision == "f64" else 1e-6
+    for name, v, x in zip(names, g["mbl"], got):
+        if abs(x - v) <= rel * abs(v) + 1e-10:
+            continue
+        # equally optimal: the objective at both lengths agrees (flat objective, argmin is noise)
+        pp, pc = ores["outgroup_LH"][name], ores["subtree_LH"][name]
+        f = lambda tt: -anc.prob_t_profiles(model_o, (pp, pc), g["multiplicity"], tt, return_log=True) \
+            + np.exp(tt * tt / 1e4)
+        assert abs(f(x) - f(v)) <= obj_rel * abs(f(v)) + 1e-12, (name, x, v, f(x), f(v))

@@ -1,0 +1,78 @@
+"""CPU-only checks of the C-ABI library and the host-side schedule: the shared
+library loads, exports every entry point the public header declares, and the
+tree flattening produces a valid height-levelled CSR schedule."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from treetime_gb300 import _lib, synth
+from treetime_gb300.engine import TreeLayout
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "treetime_gb300.h")
+
+
+def _declared():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tt_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from treetime_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_bound_entry_points():
+    assert _declared() == _lib.exported_names()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    raw = ctypes.CDLL(_lib.LIB_PATH)
+    for name in _declared():
+        assert hasattr(raw, name), name
+    assert lib.tt_abi_version() == 1
+    assert lib.tt_status_string(7).decode().startswith("Brent")
+
+
+def _check_layout(tree):
+    L = TreeLayout(tree.root)
+    n = L.n_nodes
+    assert L.nodes[L.n_int - 1] is tree.root
+    assert L.parent[L.n_int - 1] == -1
+    assert (L.parent[:L.n_int - 1] >= 0).all() and (L.parent[L.n_int:] >= 0).all()
+    # children are listed in clade order and always come before the parent level
+    lev = L.level_off
+    height = np.zeros(n, dtype=int)
+    for h in range(L.n_levels):
+        height[lev[h]:lev[h + 1]] = h + 1
+    for k in range(L.n_int):
+        ch = L.child_idx[L.child_off[k]:L.child_off[k + 1]]
+        assert [L.nodes[c] for c in ch] == list(L.nodes[k].clades)
+        assert all(height[c] < height[k] for c in ch)
+        assert all(L.parent[c] == k for c in ch)
+    assert lev[0] == 0 and lev[-1] == L.n_int
+    # tips in preorder
+    assert [t.name for t in L.nodes[L.n_int:]] == [t.name for t in tree.get_terminals()]
+    return L
+
+
+@pytest.mark.parametrize("n", [3, 17, 200])
+def test_tree_layout_coalescent(n):
+    tree = synth.coalescent_tree(n, 0.01, np.random.default_rng(n))
+    _check_layout(tree)
+
+
+def test_tree_layout_caterpillar_and_polytomy():
+    from treetime_gb300.tree import parse_newick
+    cat = "(" * 300 + "a:1,b:1)" + "".join(",t%d:1)" % i for i in range(299)) + ";"
+    L = _check_layout(parse_newick(cat))
+    assert L.n_levels == 300
+    L = _check_layout(parse_newick("((a,b,c,d)x,(e,f)y,g,h)r;"))
+    assert L.n_levels == 2

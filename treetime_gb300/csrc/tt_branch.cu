@@ -1,0 +1,434 @@
+// Branch-length optimisation (TreeAnc.optimize_branch_lengths_joint and the marginal variant):
+//   - state-pair histograms per branch (GTR.state_pair, treetime/gtr.py:631-712);
+//   - Brent minimisation over s = sqrt(t) of the pair likelihood (GTR.optimal_t_compressed with
+//     GTR.prob_t_compressed, treetime/gtr.py:717-749, :816-920), one warp per branch;
+//   - the same for profile pairs (GTR.prob_t_profiles, treetime/gtr.py:922-963), one CTA per
+//     branch with the per-pattern eigen coefficients staged in shared memory.
+//
+// Brent's method (R. P. Brent, Algorithms for Minimization without Derivatives, 1973, ch. 5:
+// golden-section steps safeguarded parabolic interpolation) is restated in FP64 with the
+// parameters of scipy.optimize.minimize_scalar(method='brent') that TreeTime calls: a given
+// bracket (xa, xb, xc) with f(xb) below both ends, tolerance tol*|x| + 1e-11, golden ratio
+// constant 0.3819660, at most 500 iterations, success = converged and not NaN.
+#include "tt_internal.cuh"
+
+namespace tt {
+
+__device__ __forceinline__ int tree_of(const tt_tree* trees, int n_trees, int64_t g) {
+    int lo = 0, hi = n_trees - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (trees[mid].node_base <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// -------------------------------------------------------------- state pairs
+__global__ void state_pairs_kernel(tt_forest f, const uint8_t* __restrict__ states,
+                                   const uint8_t* __restrict__ char_state, int tips_use_states, int gap,
+                                   int ignore_gaps, const uint8_t* __restrict__ use, double* __restrict__ hist) {
+    extern __shared__ double h[];
+    const int q = f.n_states;
+    for (int64_t g = blockIdx.x; g < f.n_nodes; g += gridDim.x) {
+        if (use && !use[g]) continue;
+        const tt_tree tr = f.trees[tree_of(f.trees, f.n_trees, g)];
+        const int k = (int)(g - tr.node_base);
+        const int par = f.parent[g];
+        if (par < 0) continue;
+        for (int i = threadIdx.x; i < q * q; i += blockDim.x) h[i] = 0.0;
+        __syncthreads();
+        const int P = tr.n_patterns;
+        const bool tip = k >= tr.n_int && !tips_use_states;
+        const int r = tip ? f.tip_row[g] : 0;
+        const int64_t mo = f.mask_off ? f.mask_off[g] : -1;
+        for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            const int sp = states[tr.state_base + (int64_t)par * P + p];
+            int sc;
+            if (tip) sc = r < 0 ? 255 : char_state[f.tip_codes[tr.tip_base + (int64_t)r * P + p]];
+            else sc = states[tr.state_base + (int64_t)k * P + p];
+            if (sp >= q || sc >= q) continue;
+            if (ignore_gaps && (sp == gap || sc == gap)) continue;
+            double w = f.mult[tr.pat_base + p];
+            if (mo >= 0) w *= f.masks[mo + p];
+            atomicAdd(&h[sp * q + sc], w);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < q * q; i += blockDim.x) hist[g * q * q + i] = h[i];
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------- Brent
+struct BrentOut {
+    double x, fx;
+    int iters;
+    int state;  // 0 ok, 1 not converged / NaN, 2 bracket invalid
+};
+
+template <class F>
+__device__ BrentOut brent_minimize(F&& f, double xa, double xb, double xc, double tol, int maxiter) {
+    const double mintol = 1.0e-11, cg = 0.3819660;
+    BrentOut r{xb, 0.0, 0, 0};
+    if (xa > xc) { double t = xa; xa = xc; xc = t; }
+    const double fa = f(xa), fb = f(xb), fc = f(xc);
+    if (!(xa < xb && xb < xc) || !(fb < fa && fb < fc)) { r.fx = fb; r.state = 2; return r; }
+    double x = xb, w = xb, v = xb, fx = fb, fw = fb, fv = fb;
+    double a = xa, b = xc;
+    double deltax = 0.0, rat = 0.0;
+    int it = 0;
+    for (; it < maxiter; ++it) {
+        const double tol1 = tol * fabs(x) + mintol, tol2 = 2.0 * tol1;
+        const double xmid = 0.5 * (a + b);
+        if (fabs(x - xmid) < tol2 - 0.5 * (b - a)) break;
+        bool golden = true;
+        if (fabs(deltax) > tol1) {
+            // parabola through (v, fv), (w, fw), (x, fx)
+            double t1 = (x - w) * (fx - fv);
+            double t2 = (x - v) * (fx - fw);
+            double pn = (x - v) * t2 - (x - w) * t1;
+            t2 = 2.0 * (t2 - t1);
+            if (t2 > 0.0) pn = -pn;
+            t2 = fabs(t2);
+            const double prev = deltax;
+            deltax = rat;
+            if (pn > t2 * (a - x) && pn < t2 * (b - x) && fabs(pn) < fabs(0.5 * t2 * prev)) {
+                rat = pn / t2;
+                const double u = x + rat;
+                if ((u - a) < tol2 || (b - u) < tol2) rat = (xmid - x >= 0) ? tol1 : -tol1;
+                golden = false;
+            }
+        }
+        if (golden) {
+            deltax = (x >= xmid) ? a - x : b - x;
+            rat = cg * deltax;
+        }
+        const double u = fabs(rat) < tol1 ? (rat >= 0 ? x + tol1 : x - tol1) : x + rat;
+        const double fu = f(u);
+        if (fu > fx) {
+            if (u < x) a = u; else b = u;
+            if (fu <= fw || w == x) { v = w; w = u; fv = fw; fw = fu; }
+            else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
+        } else {
+            if (u >= x) a = x; else b = x;
+            v = w; w = x; x = u;
+            fv = fw; fw = fx; fx = fu;
+        }
+    }
+    r.x = x;
+    r.fx = fx;
+    r.iters = it;
+    r.state = (it < maxiter && !isnan(x) && !isnan(fx)) ? 0 : 1;
+    return r;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// -log-likelihood of the pair histogram at t (lanes split the q*q pairs)
+struct PairObjective {
+    int q;
+    const double* V;
+    const double* Vi;
+    const double* lam;
+    double mu;
+    const double* cnt;   // [q][q] truncated counts, parent-major
+    int lane;
+    __device__ double operator()(double s) const {
+        const double t = s * s;
+        double acc = 0.0;
+        for (int idx = lane; idx < q * q; idx += 32) {
+            const double c = cnt[idx];
+            if (c == 0.0) continue;
+            const int ip = idx / q, jc = idx % q;  // parent state, child state
+            double pv = 0.0;
+            for (int k = 0; k < q; ++k) pv = fma(V[jc * q + k], exp(mu * lam[k] * t) * Vi[k * q + ip], pv);
+            pv = pv > 0.0 ? pv : 0.0;
+            acc += log(pv > kSuperTiny ? pv : kSuperTiny) * c;
+        }
+        return -warp_sum(acc);
+    }
+};
+
+__global__ void optimal_t_pairs_kernel(int q, int64_t n, const double* __restrict__ counts,
+                                       const int32_t* __restrict__ model_of, tt_model m, double tol,
+                                       double* __restrict__ t_out, int32_t* __restrict__ info) {
+    extern __shared__ double cnt_s[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    double* cnt = cnt_s + warp * q * q;
+    for (int64_t b = (int64_t)blockIdx.x * nw + warp; b < n; b += (int64_t)gridDim.x * nw) {
+        double tot = 0.0, diff = 0.0;
+        for (int idx = lane; idx < q * q; idx += 32) {
+            const double c = counts[b * q * q + idx];
+            cnt[idx] = c;
+            tot += c;
+            if (idx / q != idx % q) diff += c;
+        }
+        __syncwarp();
+        tot = warp_sum(tot);
+        diff = warp_sum(diff);
+        const int mi = model_of ? model_of[b] : 0;
+        PairObjective f{q, m.V + (int64_t)mi * q * q, m.Vinv + (int64_t)mi * q * q, m.lam + (int64_t)mi * q,
+                        m.mu[mi], cnt, lane};
+        const double hamming = diff / tot;
+        BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, tol, 500);
+        if (lane == 0) {
+            t_out[b] = r.state == 0 ? r.x * r.x : hamming;
+            if (info) info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void prob_t_pairs_kernel(int q, int64_t n, const double* __restrict__ counts,
+                                    const int32_t* __restrict__ model_of, tt_model m, const double* __restrict__ t,
+                                    double* __restrict__ out) {
+    extern __shared__ double cnt_s[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    double* cnt = cnt_s + warp * q * q;
+    for (int64_t b = (int64_t)blockIdx.x * nw + warp; b < n; b += (int64_t)gridDim.x * nw) {
+        for (int idx = lane; idx < q * q; idx += 32) cnt[idx] = counts[b * q * q + idx];
+        __syncwarp();
+        const int mi = model_of ? model_of[b] : 0;
+        PairObjective f{q, m.V + (int64_t)mi * q * q, m.Vinv + (int64_t)mi * q * q, m.lam + (int64_t)mi * q,
+                        m.mu[mi], cnt, lane};
+        const double v = t[b] < 0 ? kBig : f(sqrt(t[b]));
+        if (lane == 0) out[b] = -v;
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------ profile pairs
+template <typename T>
+__device__ __forceinline__ void read_prof(const void* base, int64_t row, int w, int q, double* x) {
+    const T* p = reinterpret_cast<const T*>(base) + row * w;
+    for (int j = 0; j < q; ++j) x[j] = (double)p[j];
+}
+
+struct ProfParams {
+    tt_forest f;
+    tt_model m;
+    int64_t n;
+    const int32_t* node_of;
+    const void* pp;
+    const int64_t* pp_row;
+    const void* pc;
+    const int64_t* pc_row;
+    int prec;
+    int gap;
+    int ignore_gaps;
+    double tol;
+    double* t_out;
+    int32_t* info;
+    int cap;  // patterns staged in shared memory
+};
+
+__device__ double block_sum(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += red[w];
+    return s;
+}
+
+// Per-pattern coefficients u_k = (pc.V)_k (V^-1.pp)_k and weight mult*mask*non_gap, so that
+// pc.P(t).pp = sum_k u_k exp(mu lam_k t).
+__device__ __forceinline__ void pattern_coeffs(const ProfParams& a, const tt_tree& tr, int64_t g, int k, int64_t b,
+                                               int p, const double* V, const double* Vi, double* u, double& wgt,
+                                               double& overlap) {
+    const int q = a.f.n_states, w = a.f.width;
+    double pp[32], pc[32];
+    if (a.prec == TT_PREC_F32) read_prof<float>(a.pp, a.pp_row[b] + p, w, q, pp);
+    else read_prof<double>(a.pp, a.pp_row[b] + p, w, q, pp);
+    const bool tip = a.pc_row[b] < 0;
+    if (tip) {
+        const int r = a.f.tip_row[g];
+        const int code = r < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)r * tr.n_patterns + p];
+        for (int j = 0; j < q; ++j) pc[j] = a.m.lut[code * q + j];
+    } else {
+        if (a.prec == TT_PREC_F32) {
+            read_prof<float>(a.pc, a.pc_row[b] + p, w, q, pc);
+            double s = 0.0;  // FP32 partials are power-of-two scaled: normalise
+            for (int j = 0; j < q; ++j) s += pc[j];
+            for (int j = 0; j < q; ++j) pc[j] /= s;
+        } else {
+            read_prof<double>(a.pc, a.pc_row[b] + p, w, q, pc);
+        }
+    }
+    double m = a.f.mult[tr.pat_base + p];
+    if (a.f.mask_off) {
+        const int64_t mo = a.f.mask_off[g];
+        if (mo >= 0) m *= a.f.masks[mo + p];
+    }
+    double ov = 0.0;
+    for (int j = 0; j < q; ++j) ov += pp[j] * pc[j];
+    overlap = m * ov;
+    double ngf = 1.0;
+    if (a.ignore_gaps && a.gap >= 0) ngf = (1.0 - pp[a.gap]) * (1.0 - pc[a.gap]);
+    wgt = m * ngf;
+    for (int kk = 0; kk < q; ++kk) {
+        double y = 0.0, z = 0.0;
+        for (int i = 0; i < q; ++i) y = fma(pc[i], V[i * q + kk], y);
+        for (int j = 0; j < q; ++j) z = fma(Vi[kk * q + j], pp[j], z);
+        u[kk] = y * z;
+    }
+}
+
+__global__ void optimal_t_profiles_kernel(ProfParams a) {
+    extern __shared__ double sm[];
+    __shared__ double red[32];
+    const int q = a.f.n_states;
+    for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
+        const int64_t g = a.node_of[b];
+        const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
+        const int k = (int)(g - tr.node_base);
+        const int P = tr.n_patterns;
+        const int mi = tr.model;
+        const double* V = a.m.V + (int64_t)mi * q * q;
+        const double* Vi = a.m.Vinv + (int64_t)mi * q * q;
+        const double* lam = a.m.lam + (int64_t)mi * q;
+        const double mu = a.m.mu[mi];
+        const int staged = P < a.cap ? P : a.cap;
+        double* us = sm;                       // [staged][q]
+        double* ws = sm + (int64_t)staged * q;  // [staged]
+        double msum = 0.0, ovsum = 0.0;
+        for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            double u[32], wgt, ov;
+            pattern_coeffs(a, tr, g, k, b, p, V, Vi, u, wgt, ov);
+            double m = a.f.mult[tr.pat_base + p];
+            if (a.f.mask_off) {
+                const int64_t mo = a.f.mask_off[g];
+                if (mo >= 0) m *= a.f.masks[mo + p];
+            }
+            msum += m;
+            ovsum += ov;
+            if (p < staged) {
+                for (int kk = 0; kk < q; ++kk) us[p * q + kk] = u[kk];
+                ws[p] = wgt;
+            }
+        }
+        msum = block_sum(msum, red);
+        ovsum = block_sum(ovsum, red);
+        __syncthreads();
+        const double hamming = 1.0 - ovsum / msum;
+        auto f = [&](double s) -> double {
+            const double t = s * s;
+            double e[32];
+            for (int kk = 0; kk < q; ++kk) e[kk] = exp(mu * lam[kk] * t);
+            double acc = 0.0;
+            for (int p = threadIdx.x; p < P; p += blockDim.x) {
+                double res = 0.0, wgt;
+                if (p < staged) {
+                    for (int kk = 0; kk < q; ++kk) res = fma(us[p * q + kk], e[kk], res);
+                    wgt = ws[p];
+                } else {
+                    double u[32], ov;
+                    pattern_coeffs(a, tr, g, k, b, p, V, Vi, u, wgt, ov);
+                    for (int kk = 0; kk < q; ++kk) res = fma(u[kk], e[kk], res);
+                }
+                acc += wgt * log(res + kSuperTiny);
+            }
+            const double tot = block_sum(acc, red);
+            return -tot + exp(t * t / 10000.0);
+        };
+        BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
+        if (threadIdx.x == 0) {
+            a.t_out[b] = r.state == 0 ? r.x * r.x : hamming;
+            if (a.info) a.info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace tt
+
+using namespace tt;
+
+extern "C" tt_status tt_state_pairs(const tt_forest* f, const uint8_t* states, const uint8_t* char_state,
+                                    int32_t tips_use_states, int32_t gap_state, int32_t ignore_gaps,
+                                    const uint8_t* use, double* hist, void* stream) {
+    if (!f || !states || !char_state || !hist || f->n_states < 2 || f->n_states > 32) {
+        set_error("tt_state_pairs: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (f->n_nodes == 0) return TT_OK;
+    const int q = f->n_states;
+    int64_t blocks = f->n_nodes < 65535 * 4 ? f->n_nodes : 65535 * 4;
+    state_pairs_kernel<<<(unsigned)blocks, 256, q * q * sizeof(double), as_stream(stream)>>>(
+        *f, states, char_state, tips_use_states, gap_state, ignore_gaps, use, hist);
+    return check_launch("tt_state_pairs");
+}
+
+extern "C" tt_status tt_optimal_t_pairs(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
+                                        const tt_model* m, double tol, double* t_out, int32_t* info,
+                                        void* stream) {
+    if (!m || q < 2 || q > 32 || m->n_states != q || n < 0 || (n > 0 && (!counts || !t_out))) {
+        set_error("tt_optimal_t_pairs: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n == 0) return TT_OK;
+    const int warps = 4;
+    int64_t blocks = (n + warps - 1) / warps;
+    if (blocks > 65535 * 4) blocks = 65535 * 4;
+    optimal_t_pairs_kernel<<<(unsigned)blocks, warps * 32, warps * q * q * sizeof(double), as_stream(stream)>>>(
+        q, n, counts, model_of, *m, tol, t_out, info);
+    return check_launch("tt_optimal_t_pairs");
+}
+
+extern "C" tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
+                                     const tt_model* m, const double* t, double* logp_out, void* stream) {
+    if (!m || q < 2 || q > 32 || m->n_states != q || n < 0 || (n > 0 && (!counts || !t || !logp_out))) {
+        set_error("tt_prob_t_pairs: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n == 0) return TT_OK;
+    const int warps = 4;
+    int64_t blocks = (n + warps - 1) / warps;
+    if (blocks > 65535 * 4) blocks = 65535 * 4;
+    prob_t_pairs_kernel<<<(unsigned)blocks, warps * 32, warps * q * q * sizeof(double), as_stream(stream)>>>(
+        q, n, counts, model_of, *m, t, logp_out);
+    return check_launch("tt_prob_t_pairs");
+}
+
+extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
+                                           const void* pp, const int64_t* pp_row, const void* pc,
+                                           const int64_t* pc_row, int32_t prec, int32_t gap_state,
+                                           int32_t ignore_gaps, double tol, double* t_out, int32_t* info,
+                                           void* stream) {
+    if (!f || !m || n < 0 || (n > 0 && (!node_of || !pp || !pp_row || !pc_row || !t_out)) || f->n_states > 32) {
+        set_error("tt_optimal_t_profiles: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n == 0) return TT_OK;
+    static bool configured = false;
+    const int q = f->n_states;
+    const size_t smem_max = 200 * 1024;
+    if (!configured) {
+        cudaFuncSetAttribute(optimal_t_profiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        configured = true;
+    }
+    ProfParams a;
+    a.f = *f;
+    a.m = *m;
+    a.n = n;
+    a.node_of = node_of;
+    a.pp = pp;
+    a.pp_row = pp_row;
+    a.pc = pc;
+    a.pc_row = pc_row;
+    a.prec = prec;
+    a.gap = gap_state;
+    a.ignore_gaps = ignore_gaps;
+    a.tol = tol;
+    a.t_out = t_out;
+    a.info = info;
+    a.cap = (int)(smem_max / ((q + 1) * sizeof(double)));
+    int64_t blocks = n < 65535 * 4 ? n : 65535 * 4;
+    optimal_t_profiles_kernel<<<(unsigned)blocks, 256, smem_max, as_stream(stream)>>>(a);
+    return check_launch("tt_optimal_t_profiles");
+}

@@ -1,0 +1,70 @@
+// C entry point of the marginal reconstruction (kernels in tt_marginal_kernels.cuh).
+#include "tt_marginal_kernels.cuh"
+
+namespace tt {
+
+// Per-tree multiplicity-weighted sum of the site log-likelihoods, fixed summation order.
+__global__ void tree_sum_kernel(const tt_tree* trees, const double* site_lh, const double* mult, double* tree_lh) {
+    __shared__ double red[256];
+    const tt_tree tr = trees[blockIdx.x];
+    double s = 0.0;
+    for (int p = threadIdx.x; p < tr.n_patterns; p += blockDim.x) s += site_lh[tr.pat_base + p] * mult[tr.pat_base + p];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tree_lh[blockIdx.x] = red[0];
+}
+
+tt_status tree_sums(const tt_forest* f, const double* site_lh, double* tree_lh, cudaStream_t s) {
+    tree_sum_kernel<<<f->n_trees, 256, 0, s>>>(f->trees, site_lh, f->mult, tree_lh);
+    return check_launch("tree_sum");
+}
+
+}  // namespace tt
+
+using namespace tt;
+
+extern "C" tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt_pmats* pm, int32_t precision,
+                                 const tt_marginal_out* out, int32_t* status, void* stream) {
+    if (!f || !m || !pm || !out || !out->partial || !out->posterior || !out->states || !out->site_lh ||
+        !out->tree_lh || f->width != round4(f->n_states) || m->n_states != f->n_states) {
+        set_error("tt_marginal: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (!f->work || f->n_work <= 0) {
+        set_error("tt_marginal: empty work list");
+        return TT_ERR_INVALID;
+    }
+    if (out->reconstruct_tips && !out->tip_posterior) {
+        set_error("tt_marginal: reconstruct_tips needs tip_posterior");
+        return TT_ERR_INVALID;
+    }
+    MargParams prm;
+    prm.f = *f;
+    prm.pi = m->pi;
+    prm.lut = m->lut;
+    prm.o = *out;
+    prm.status = status;
+    prm.items = reinterpret_cast<const WorkItem*>(f->work);
+    prm.n_items = f->n_work;
+    cudaStream_t s = as_stream(stream);
+    int blocks = f->max_blocks > 0 && f->max_blocks < f->n_work ? f->max_blocks : f->n_work;
+    const int warps = f->warps_per_block ? f->warps_per_block : 8;
+    tt_status st;
+    if (precision == TT_PREC_F32) {
+        if (!pm->p32) { set_error("tt_marginal: FP32 needs p32"); return TT_ERR_INVALID; }
+        prm.pmat = pm->p32;
+        st = launch_marginal_f32(f->n_states, warps, prm, blocks, s);
+    } else if (precision == TT_PREC_F64) {
+        prm.pmat = pm->p64;
+        st = launch_marginal_f64(f->n_states, warps, prm, blocks, s);
+    } else {
+        set_error("tt_marginal: unknown precision %d", precision);
+        return TT_ERR_INVALID;
+    }
+    if (st != TT_OK) return st;
+    return tree_sums(f, out->site_lh, out->tree_lh, s);
+}

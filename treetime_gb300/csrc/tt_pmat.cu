@@ -1,0 +1,99 @@
+// Branch transition matrices and standalone profile transport.
+//
+// P(t) = max(0, V · diag(exp(mu·lambda·t)) · V⁻¹) per branch in FP64, the arithmetic of
+// GTR.expQt (treetime/gtr.py:1051-1067): the diagonal scaling is applied to V⁻¹'s rows and the
+// product summed over the eigen index in order.  Row layout [node][i][width], entry (i, j) =
+// probability of child state i given parent state j.
+#include "tt_internal.cuh"
+
+namespace tt {
+
+__device__ __forceinline__ int tree_of_node(const tt_tree* trees, int n_trees, int64_t g) {
+    int lo = 0, hi = n_trees - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (trees[mid].node_base <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void pmats_kernel(tt_forest f, tt_model m, tt_pmats out, int32_t* status) {
+    const int q = f.n_states, w = f.width;
+    const int64_t total = f.n_nodes * q * w;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = idx / (q * w);
+        const int r = (int)(idx % (q * w));
+        const int i = r / w, j = r % w;
+        double p = 0.0;
+        if (j < q) {
+            const int t = tree_of_node(f.trees, f.n_trees, g);
+            const int mi = f.trees[t].model;
+            const double* V = m.V + (int64_t)mi * q * q;
+            const double* Vi = m.Vinv + (int64_t)mi * q * q;
+            const double* lam = m.lam + (int64_t)mi * q;
+            const double mu = m.mu[mi];
+            const double bl = f.bl[g];
+            double acc = 0.0;
+            for (int k = 0; k < q; ++k) {
+                const double lv = mu * bl * lam[k];
+                if (lv > 10.0) set_status(status, TT_ERR_NUMERIC);
+                acc = fma(V[i * q + k], exp(lv) * Vi[k * q + j], acc);
+            }
+            p = acc > 0.0 ? acc : 0.0;
+        }
+        out.p64[g * q * w + r] = p;
+        if (out.p32) out.p32[g * q * w + r] = (float)p;
+        if (out.logp64) out.logp64[g * q * w + r] = j < q ? log(p > kTiny ? p : kTiny) : 0.0;
+    }
+}
+
+__global__ void propagate_kernel(int q, int64_t n, const double* __restrict__ prof,
+                                 const double* __restrict__ pmat, const int32_t* __restrict__ t_index,
+                                 int transpose, int return_log, double* __restrict__ res) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        const double* P = pmat + (int64_t)(t_index ? t_index[a] : 0) * q * q;
+        const double* x = prof + a * q;
+        for (int j = 0; j < q; ++j) {
+            double s = 0.0;
+            for (int i = 0; i < q; ++i) s = fma(x[i], transpose ? P[j * q + i] : P[i * q + j], s);
+            res[a * q + j] = return_log ? log(s) : s;
+        }
+    }
+}
+
+}  // namespace tt
+
+using namespace tt;
+
+extern "C" tt_status tt_branch_pmats(const tt_forest* f, const tt_model* m, tt_pmats out, int32_t* status,
+                                     void* stream) {
+    if (!f || !m || !out.p64 || f->n_states < 2 || f->n_states > 32 || f->width != round4(f->n_states) ||
+        m->n_states != f->n_states) {
+        set_error("tt_branch_pmats: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    const int64_t total = f->n_nodes * f->n_states * f->width;
+    if (total == 0) return TT_OK;
+    const int threads = 256;
+    int64_t blocks = (total + threads - 1) / threads;
+    if (blocks > 65535LL * 8) blocks = 65535LL * 8;
+    pmats_kernel<<<(unsigned)blocks, threads, 0, as_stream(stream)>>>(*f, *m, out, status);
+    return check_launch("tt_branch_pmats");
+}
+
+extern "C" tt_status tt_propagate(int32_t q, int64_t n, const double* prof, const double* pmat,
+                                  const int32_t* t_index, int32_t transpose, int32_t return_log, double* res,
+                                  void* stream) {
+    if (q < 1 || q > 64 || n < 0 || (n > 0 && (!prof || !pmat || !res))) {
+        set_error("tt_propagate: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n == 0) return TT_OK;
+    const int threads = 128;
+    int64_t blocks = (n + threads - 1) / threads;
+    if (blocks > 65535LL * 8) blocks = 65535LL * 8;
+    propagate_kernel<<<(unsigned)blocks, threads, 0, as_stream(stream)>>>(q, n, prof, pmat, t_index, transpose,
+                                                                          return_log, res);
+    return check_launch("tt_propagate");
+}

@@ -1,0 +1,716 @@
+"""Device engine: flattening of trees into the height-levelled CSR schedule,
+HBM layout of a forest (one or many trees), and the calls into the CUDA
+library.  torch provides device memory and the current stream; all compute
+runs in the library's kernels.
+
+Layout of a forest in device memory (see include/treetime_gb300.h):
+  * per node (global id = tree node_base + local id): parent, tip row, branch
+    length, mask offset; children as a CSR in clade order;
+  * internal nodes of a tree are numbered by height (children before parents,
+    the root last); the level offsets delimit each height;
+  * tip characters as raw bytes, [tip][pattern] per tree;
+  * profiles as [node][pattern][width] rows, width = q rounded up to 4
+    (16-byte vector loads); states as [node][pattern] bytes.
+"""
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from . import config as ttconf
+from ._lib import TTForest, TTJointOut, TTMarginalOut, TTModel, TTPmats, TTTree, check
+from .alphabets import MISSING_CODE, profile_lut
+
+TILE = 32
+WIDTHS = {q: (q + 3) // 4 * 4 for q in range(1, 33)}
+
+_torch = None
+
+
+def torch():
+    global _torch
+    if _torch is None:
+        import torch as t
+        _torch = t
+    return _torch
+
+
+def require_device(device=None):
+    """The CUDA library and a CUDA device are mandatory (no CPU path)."""
+    t = torch()
+    if not t.cuda.is_available():
+        raise RuntimeError("treetime_gb300 needs a CUDA device: there is no CPU implementation of its kernels")
+    _lib.load()
+    dev = t.device(device) if device is not None else t.device("cuda", t.cuda.current_device())
+    return dev
+
+
+def _p(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return C.c_void_p(torch().cuda.current_stream().cuda_stream)
+
+
+def _to_dev(arr, device, dtype=None):
+    t = torch()
+    a = np.ascontiguousarray(arr)
+    x = t.from_numpy(a)
+    if dtype is not None:
+        x = x.to(dtype)
+    return x.to(device, non_blocking=False)
+
+
+# ----------------------------------------------------------------------------
+# tree flattening
+# ----------------------------------------------------------------------------
+class TreeLayout:
+    """Height-levelled CSR schedule of one rooted tree.
+
+    ``nodes[k]`` is the clade with local id k: internal nodes first, sorted by
+    height and then by preorder position (the root last), then tips in
+    preorder (the order of ``get_terminals``)."""
+
+    def __init__(self, root):
+        pre = []
+        stack = [root]
+        while stack:
+            n = stack.pop()
+            pre.append(n)
+            ch = n.clades
+            for i in range(len(ch) - 1, -1, -1):
+                stack.append(ch[i])
+        pos = {id(n): i for i, n in enumerate(pre)}
+        height = {}
+        for n in reversed(pre):  # reverse preorder: children before parents
+            height[id(n)] = 0 if not n.clades else 1 + max(height[id(c)] for c in n.clades)
+        internal = [n for n in pre if n.clades]
+        tips = [n for n in pre if not n.clades]
+        internal.sort(key=lambda n: (height[id(n)], pos[id(n)]))
+        self.nodes = internal + tips
+        self.n_int = len(internal)
+        self.n_tip = len(tips)
+        self.root = root
+        local = {id(n): k for k, n in enumerate(self.nodes)}
+        self.local = local
+        N = len(self.nodes)
+        h = np.array([height[id(n)] for n in internal], dtype=np.int64)
+        self.n_levels = int(h[-1]) if len(h) else 0
+        # level_off[h-1] .. level_off[h]: internal nodes of height h
+        self.level_off = np.searchsorted(h, np.arange(1, self.n_levels + 2), side="left").astype(np.int32)
+        self.parent = np.full(N, -1, dtype=np.int32)
+        counts = np.zeros(N + 1, dtype=np.int32)
+        child_idx = []
+        for k, n in enumerate(self.nodes):
+            counts[k + 1] = len(n.clades)
+            for c in n.clades:
+                child_idx.append(local[id(c)])
+                self.parent[local[id(c)]] = k
+        self.child_off = np.cumsum(counts).astype(np.int32)
+        self.child_idx = np.array(child_idx, dtype=np.int32)
+        self.preorder_local = np.array([local[id(n)] for n in pre], dtype=np.int64)
+
+    @property
+    def n_nodes(self):
+        return self.n_int + self.n_tip
+
+
+def branch_lengths(layout, full_length, use_mutation_length=False):
+    """Branch length used by the model: max(1e-3 / L, length)
+    (TreeAnc._branch_length_to_gtr, treetime/treeanc.py:752-760)."""
+    floor = ttconf.MIN_BRANCH_LENGTH * (1.0 / full_length)
+    attr = "mutation_length" if use_mutation_length else "branch_length"
+    bl = np.array([getattr(n, attr) or 0.0 for n in layout.nodes], dtype=np.float64)
+    return np.maximum(floor, bl)
+
+
+# ----------------------------------------------------------------------------
+# models
+# ----------------------------------------------------------------------------
+class DeviceModel:
+    """FP64 device copies of one or several standard GTR models (stacked) and
+    the character -> profile table of their (shared) alphabet."""
+
+    def __init__(self, gtrs, device=None, profile_map=None):
+        if not isinstance(gtrs, (list, tuple)):
+            gtrs = [gtrs]
+        dev = require_device(device)
+        self.device = dev
+        self.gtrs = list(gtrs)
+        q = gtrs[0].n_states
+        for g in gtrs:
+            if g.n_states != q:
+                raise ValueError("all models of a forest need the same alphabet size")
+        self.q = q
+        self.V = _to_dev(np.stack([g.v for g in gtrs]).astype(np.float64), dev)
+        self.Vinv = _to_dev(np.stack([g.v_inv for g in gtrs]).astype(np.float64), dev)
+        self.lam = _to_dev(np.stack([g.eigenvals for g in gtrs]).astype(np.float64), dev)
+        self.mu = _to_dev(np.array([float(g.mu) for g in gtrs], dtype=np.float64), dev)
+        self.pi = _to_dev(np.stack([g.Pi for g in gtrs]).astype(np.float64), dev)
+        pm = profile_map if profile_map is not None else gtrs[0].profile_map
+        self.lut_host = profile_lut(pm, q)
+        self.lut = _to_dev(self.lut_host, dev)
+        self.struct = TTModel(len(gtrs), q, _p(self.V), _p(self.Vinv), _p(self.lam), _p(self.mu), _p(self.pi),
+                              _p(self.lut))
+
+
+def char_state_table(gtr):
+    """byte -> state index of the alphabet; TreeTime's state_pair leaves
+    non-alphabet characters out for alphabets below 10 states and counts them
+    as state 1 for larger ones (treetime/gtr.py:674-707)."""
+    tab = np.full(256, 255, dtype=np.uint8)
+    if len(gtr.alphabet) >= 10:
+        tab[:] = 1
+    for i, c in enumerate(gtr.alphabet):
+        tab[ord(str(c))] = i
+    return tab
+
+
+# ----------------------------------------------------------------------------
+# forest
+# ----------------------------------------------------------------------------
+class TreeInput:
+    """One tree's inputs: layout, tip rows (compressed codes), multiplicities,
+    branch lengths, masks {local id: per-pattern array}, model index."""
+
+    def __init__(self, layout, tip_codes, tip_row, mult, bl, masks=None, model=0):
+        self.layout = layout
+        self.tip_codes = np.ascontiguousarray(tip_codes, dtype=np.uint8)  # [rows, P]
+        self.tip_row = np.asarray(tip_row, dtype=np.int32)                # per tip local (len n_tip)
+        self.mult = np.asarray(mult, dtype=np.float64)
+        self.bl = np.asarray(bl, dtype=np.float64)
+        self.masks = masks or {}
+        self.model = model
+
+    @property
+    def n_patterns(self):
+        return len(self.mult)
+
+
+class Forest:
+    """Device-resident schedule and inputs of a list of trees, plus the
+    C-ABI struct that points at them."""
+
+    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, need_tip_rows=False):
+        dev = require_device(device)
+        self.device = dev
+        self.inputs = list(inputs)
+        self.q = q
+        self.w = WIDTHS[q]
+        trees = np.zeros(len(inputs), dtype=[(n, np.int64) for n in
+                                             ("node_base", "level_base", "pat_base", "tip_base", "prof_base",
+                                              "tipprof_base", "state_base")] +
+                         [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model",
+                                                   "reserved")])
+        node_base = level_base = pat_base = tip_base = prof_base = tipprof_base = state_base = 0
+        lev, coff, cidx, par, trow, bl, mult, codes, moff, mvals = [], [], [], [], [], [], [], [], [], []
+        mask_elems = 0
+        child_base = 0
+        work = []
+        for t, ti in enumerate(inputs):
+            L = ti.layout
+            P = ti.n_patterns
+            trees[t] = (node_base, level_base, pat_base, tip_base, prof_base, tipprof_base, state_base,
+                        L.n_int, L.n_tip, L.n_levels, P, ti.model, 0)
+            lev.append(L.level_off)
+            coff.append(L.child_off[:-1] + child_base)
+            cidx.append(L.child_idx)
+            child_base += len(L.child_idx)
+            par.append(L.parent)
+            tr = np.full(L.n_nodes, -1, dtype=np.int32)
+            tr[L.n_int:] = ti.tip_row
+            trow.append(tr)
+            bl.append(ti.bl)
+            mult.append(ti.mult)
+            codes.append(ti.tip_codes.reshape(-1))
+            mo = np.full(L.n_nodes, -1, dtype=np.int64)
+            for k, arr in ti.masks.items():
+                mo[k] = mask_elems
+                mvals.append(np.asarray(arr, dtype=np.float64))
+                mask_elems += P
+            moff.append(mo)
+            for p0 in range(0, P, TILE):
+                work.append((L.n_nodes * min(TILE, P - p0), t, p0))
+            node_base += L.n_nodes
+            level_base += len(L.level_off)
+            pat_base += P
+            tip_base += ti.tip_codes.size
+            prof_base += L.n_int * P
+            tipprof_base += L.n_tip * P
+            state_base += L.n_nodes * P
+        total_children = sum(len(c) for c in cidx)
+        child_off = np.concatenate(coff + [np.array([total_children], dtype=np.int32)]).astype(np.int32)
+        work.sort(key=lambda w: -w[0])
+        self.work_host = np.array([(t, p0) for _, t, p0 in work], dtype=np.int32).reshape(-1, 2)
+        self.trees_host = trees
+        self.n_nodes = node_base
+        self.n_patterns = pat_base
+        self.prof_rows = prof_base
+        self.tip_rows = tipprof_base
+        self.state_rows = state_base
+        self.d_trees = _to_dev(trees.view(np.uint8), dev)
+        self.d_level = _to_dev(np.concatenate(lev).astype(np.int32), dev)
+        self.d_child_off = _to_dev(child_off, dev)
+        self.d_child_idx = _to_dev(np.concatenate(cidx).astype(np.int32) if total_children else
+                                   np.zeros(1, np.int32), dev)
+        self.d_parent = _to_dev(np.concatenate(par), dev)
+        self.d_tip_row = _to_dev(np.concatenate(trow), dev)
+        self.bl_host = np.concatenate(bl)
+        self.d_bl = _to_dev(self.bl_host, dev)
+        self.d_mult = _to_dev(np.concatenate(mult), dev)
+        self.d_codes = _to_dev(np.concatenate(codes) if codes else np.zeros(1, np.uint8), dev)
+        self.has_masks = mask_elems > 0
+        self.d_mask_off = _to_dev(np.concatenate(moff), dev) if self.has_masks else None
+        self.d_masks = _to_dev(np.concatenate(mvals), dev) if self.has_masks else None
+        self.d_work = _to_dev(self.work_host, dev)
+        if warps_per_block is None:
+            warps_per_block = 32 if len(self.work_host) < 2 * _lib.load().tt_device_sm_count() else 8
+        self.struct = TTForest(
+            len(inputs), q, self.w, int(max((ti.layout.n_levels for ti in inputs), default=0)),
+            self.n_nodes, self.n_patterns, _p(self.d_trees), _p(self.d_level), _p(self.d_child_off),
+            _p(self.d_child_idx), _p(self.d_parent), _p(self.d_tip_row), _p(self.d_mask_off), _p(self.d_masks),
+            _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
+            warps_per_block, max_blocks, 0)
+
+    def set_branch_lengths(self, bl_list):
+        """Replace branch lengths (same topology) without rebuilding."""
+        self.bl_host = np.concatenate([np.asarray(b, dtype=np.float64) for b in bl_list])
+        self.d_bl.copy_(torch().from_numpy(self.bl_host))
+
+    def tree_slices(self, t):
+        """Host slices (node, pattern, profile row, state) of tree t."""
+        tr = self.trees_host[t]
+        return tr
+
+
+# ----------------------------------------------------------------------------
+# kernels
+# ----------------------------------------------------------------------------
+class Buffers:
+    """Device outputs of the pruning passes for a forest (reused across calls)."""
+
+    def __init__(self, forest):
+        self.f = forest
+        self.cache = {}
+
+    def get(self, name, shape, dtype):
+        t = torch()
+        key = name
+        buf = self.cache.get(key)
+        if buf is None or tuple(buf.shape) != tuple(shape) or buf.dtype != dtype:
+            buf = t.empty(shape, dtype=dtype, device=self.f.device)
+            self.cache[key] = buf
+        return buf
+
+
+def branch_pmats(forest, model, bufs, need32=False, needlog=False):
+    t = torch()
+    q, w = forest.q, forest.w
+    p64 = bufs.get("p64", (forest.n_nodes, q, w), t.float64)
+    p32 = bufs.get("p32", (forest.n_nodes, q, w), t.float32) if need32 else None
+    lg = bufs.get("logp", (forest.n_nodes, q, w), t.float64) if needlog else None
+    status = bufs.get("status", (1,), t.int32)
+    status.zero_()
+    lib = _lib.load()
+    check(lib.tt_branch_pmats(C.byref(forest.struct), C.byref(model.struct), TTPmats(_p(p64), _p(p32), _p(lg)),
+                              _p(status), _stream()), "tt_branch_pmats")
+    return TTPmats(_p(p64), _p(p32), _p(lg)), status
+
+
+def _check_status(status):
+    s = int(status.item())
+    if s:
+        check(s, "kernel status")
+
+
+def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_outgroup=False,
+             tip_outgroup=False, count_diff=False, root_uniform=None, sync=True):
+    """Run the marginal pass over the forest.  Returns the dict of device
+    buffers (partial, posterior, outgroup, tip_posterior, tip_outgroup, states,
+    site_lh, tree_lh, n_diff)."""
+    t = torch()
+    lib = _lib.load()
+    f32 = precision == "f32"
+    dt = t.float32 if f32 else t.float64
+    pm, status = branch_pmats(forest, model, bufs, need32=f32)
+    w = forest.w
+    out = {
+        "partial": bufs.get("partial", (forest.prof_rows, w), dt),
+        "posterior": bufs.get("posterior", (forest.prof_rows, w), dt),
+        "outgroup": bufs.get("outgroup", (forest.prof_rows, w), dt) if keep_outgroup else None,
+        "tip_posterior": bufs.get("tip_posterior", (forest.tip_rows, w), dt) if reconstruct_tips else None,
+        "tip_outgroup": bufs.get("tip_outgroup", (forest.tip_rows, w), dt) if tip_outgroup else None,
+        "states": bufs.get("states", (forest.state_rows,), t.uint8),
+        "site_lh": bufs.get("site_lh", (forest.n_patterns,), t.float64),
+        "tree_lh": bufs.get("tree_lh", (len(forest.inputs),), t.float64),
+        "n_diff": bufs.get("n_diff", (len(forest.inputs),), t.int64),
+    }
+    out["n_diff"].zero_()
+    ru = _to_dev(root_uniform, forest.device, t.float64) if root_uniform is not None else None
+    o = TTMarginalOut(_p(out["partial"]), _p(out["posterior"]), _p(out["outgroup"]), _p(out["tip_posterior"]),
+                      _p(out["tip_outgroup"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
+                      _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
+    check(lib.tt_marginal(C.byref(forest.struct), C.byref(model.struct), C.byref(pm),
+                          _lib.TT_PREC_F32 if f32 else _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()),
+          "tt_marginal")
+    if sync:
+        _check_status(status)
+    out["_keep"] = ru
+    return out
+
+
+def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=False, keep_outgroup=False,
+                           tip_outgroup=False, count_diff=False, root_uniform=None, sync=True):
+    """Marginal pass for a GTR_site_specific model (single tree)."""
+    t = torch()
+    lib = _lib.load()
+    f32 = precision == "f32"
+    dt = t.float32 if f32 else t.float64
+    dev = forest.device
+    key = id(gtr)
+    cache = bufs.cache.get("ss_model")
+    if cache is None or cache[0] != key:
+        lam, V, Vi = gtr.site_matrices()
+        arrs = dict(lam=_to_dev(lam, dev), V=_to_dev(V, dev), Vi=_to_dev(Vi, dev),
+                    mu=_to_dev(np.asarray(gtr.mu, dtype=np.float64), dev),
+                    pi=_to_dev(np.ascontiguousarray(gtr.Pi.T), dev),
+                    lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev),
+                    grid=_to_dev(np.asarray(gtr.t_grid, dtype=np.float64), dev))
+        bufs.cache["ss_model"] = (key, arrs)
+    arrs = bufs.cache["ss_model"][1]
+    w = forest.w
+    out = {
+        "partial": bufs.get("partial", (forest.prof_rows, w), dt),
+        "posterior": bufs.get("posterior", (forest.prof_rows, w), dt),
+        "outgroup": bufs.get("outgroup", (forest.prof_rows, w), dt) if keep_outgroup else None,
+        "tip_posterior": bufs.get("tip_posterior", (forest.tip_rows, w), dt) if reconstruct_tips else None,
+        "tip_outgroup": bufs.get("tip_outgroup", (forest.tip_rows, w), dt) if tip_outgroup else None,
+        "states": bufs.get("states", (forest.state_rows,), t.uint8),
+        "site_lh": bufs.get("site_lh", (forest.n_patterns,), t.float64),
+        "tree_lh": bufs.get("tree_lh", (len(forest.inputs),), t.float64),
+        "n_diff": bufs.get("n_diff", (len(forest.inputs),), t.int64),
+    }
+    out["n_diff"].zero_()
+    status = bufs.get("status", (1,), t.int32)
+    status.zero_()
+    ru = _to_dev(root_uniform, dev, t.float64) if root_uniform is not None else None
+    o = TTMarginalOut(_p(out["partial"]), _p(out["posterior"]), _p(out["outgroup"]), _p(out["tip_posterior"]),
+                      _p(out["tip_outgroup"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
+                      _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
+    check(lib.tt_marginal_ss(C.byref(forest.struct), _p(arrs["lam"]), _p(arrs["V"]), _p(arrs["Vi"]), _p(arrs["mu"]),
+                             _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]), len(gtr.t_grid),
+                             float(gtr.rate_scale), int(bool(gtr.approximate)),
+                             _lib.TT_PREC_F32 if f32 else _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()),
+          "tt_marginal_ss")
+    if sync:
+        _check_status(status)
+    out["_keep"] = ru
+    return out
+
+
+def joint(forest, model, bufs, reconstruct_tips=False, count_diff=False, root_uniform=None, sync=True):
+    t = torch()
+    lib = _lib.load()
+    pm, status = branch_pmats(forest, model, bufs, needlog=True)
+    w = forest.w
+    out = {
+        "lx": bufs.get("lx", (forest.prof_rows, w), t.float64),
+        "cx": bufs.get("cx", (forest.prof_rows, w), t.uint8),
+        "states": bufs.get("states", (forest.state_rows,), t.uint8),
+        "site_lh": bufs.get("joint_site_lh", (forest.n_patterns,), t.float64),
+        "tree_lh": bufs.get("joint_tree_lh", (len(forest.inputs),), t.float64),
+        "n_diff": bufs.get("n_diff", (len(forest.inputs),), t.int64),
+    }
+    out["n_diff"].zero_()
+    ru = _to_dev(root_uniform, forest.device, t.float64) if root_uniform is not None else None
+    o = TTJointOut(_p(out["lx"]), _p(out["cx"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
+                   _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
+    check(lib.tt_joint(C.byref(forest.struct), C.byref(model.struct), C.byref(pm), C.byref(o), _p(status),
+                       _stream()), "tt_joint")
+    if sync:
+        _check_status(status)
+    out["_keep"] = ru
+    return out
+
+
+def state_pairs(forest, bufs, char_state, gap_state, ignore_gaps, tips_use_states):
+    """[n_nodes, q, q] multiplicity-weighted (parent, child) histograms."""
+    t = torch()
+    lib = _lib.load()
+    q = forest.q
+    hist = bufs.get("hist", (forest.n_nodes, q, q), t.float64)
+    hist.zero_()
+    cs = _to_dev(char_state, forest.device)
+    check(lib.tt_state_pairs(C.byref(forest.struct), _p(bufs.cache["states"]), _p(cs), int(bool(tips_use_states)),
+                             -1 if gap_state is None else int(gap_state), int(bool(ignore_gaps)), None, _p(hist),
+                             _stream()), "tt_state_pairs")
+    return hist, cs
+
+
+def optimal_t_pairs(q, counts, model, model_of=None, tol=1e-10):
+    """Brent per branch on [n, q, q] counts (device tensor) -> (t, info)."""
+    t = torch()
+    lib = _lib.load()
+    n = counts.shape[0]
+    tout = t.empty(n, dtype=t.float64, device=counts.device)
+    info = t.empty(n, dtype=t.int32, device=counts.device)
+    mo = None
+    if model_of is not None:
+        mo = model_of if hasattr(model_of, "data_ptr") else _to_dev(np.asarray(model_of, np.int32), counts.device)
+    check(lib.tt_optimal_t_pairs(q, n, _p(counts), _p(mo), C.byref(model.struct), float(tol), _p(tout), _p(info),
+                                 _stream()), "tt_optimal_t_pairs")
+    return tout, info
+
+
+def optimal_t_profiles(forest, model, node_of, pp, pp_row, pc, pc_row, precision, gap_state, ignore_gaps,
+                       tol=1e-10):
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    n = len(node_of)
+    d_node = _to_dev(np.asarray(node_of, np.int32), dev)
+    d_pp_row = _to_dev(np.asarray(pp_row, np.int64), dev)
+    d_pc_row = _to_dev(np.asarray(pc_row, np.int64), dev)
+    tout = t.empty(n, dtype=t.float64, device=dev)
+    info = t.empty(n, dtype=t.int32, device=dev)
+    check(lib.tt_optimal_t_profiles(C.byref(forest.struct), C.byref(model.struct), n, _p(d_node), _p(pp),
+                                    _p(d_pp_row), _p(pc), _p(d_pc_row),
+                                    _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64,
+                                    -1 if gap_state is None else int(gap_state), int(bool(ignore_gaps)), float(tol),
+                                    _p(tout), _p(info), _stream()), "tt_optimal_t_profiles")
+    return tout, info
+
+
+# ----------------------------------------------------------------------------
+# single-call GTR API (device computations behind GTR methods)
+# ----------------------------------------------------------------------------
+def _mini_forest(n_nodes, q, bl, device, mult=None, parent=None, n_int=None, P=1):
+    """A one-tree forest struct for standalone per-branch calls."""
+    dev = require_device(device)
+    tr = np.zeros(1, dtype=[(n, np.int64) for n in ("node_base", "level_base", "pat_base", "tip_base", "prof_base",
+                                                    "tipprof_base", "state_base")] +
+                  [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model", "reserved")])
+    tr[0] = (0, 0, 0, 0, 0, 0, 0, n_nodes if n_int is None else n_int, 0, 0, P, 0, 0)
+    keep = {"trees": _to_dev(tr.view(np.uint8), dev), "bl": _to_dev(np.asarray(bl, np.float64), dev)}
+    keep["parent"] = _to_dev(np.asarray(parent if parent is not None else np.full(n_nodes, -1), np.int32), dev)
+    keep["mult"] = _to_dev(np.asarray(mult if mult is not None else np.ones(P), np.float64), dev)
+    keep["tip_row"] = _to_dev(np.full(n_nodes, -1, np.int32), dev)
+    w = WIDTHS[q]
+    f = TTForest(1, q, w, 0, n_nodes, P, _p(keep["trees"]), None, None, None, _p(keep["parent"]), _p(keep["tip_row"]),
+                 None, None, _p(keep["bl"]), None, _p(keep["mult"]), None, 0, 8, 0, 0)
+    return f, keep
+
+
+def expqt(gtr, t):
+    """P(t) on the device; scalar t -> [q, q], array -> [n, q, q]."""
+    if gtr.is_site_specific:
+        return expqt_site_specific(gtr, t)
+    tt = torch()
+    scalar = np.ndim(t) == 0
+    ts = np.atleast_1d(np.asarray(t, dtype=np.float64))
+    gtr.check_branch_lengths(ts)
+    model = gtr.device_model()
+    q = gtr.n_states
+    w = WIDTHS[q]
+    f, keep = _mini_forest(len(ts), q, ts, model.device)
+    p64 = tt.empty((len(ts), q, w), dtype=tt.float64, device=model.device)
+    status = tt.zeros(1, dtype=tt.int32, device=model.device)
+    check(_lib.load().tt_branch_pmats(C.byref(f), C.byref(model.struct), TTPmats(_p(p64), None, None), _p(status),
+                                      _stream()), "tt_branch_pmats")
+    _check_status(status)
+    res = p64[:, :, :q].cpu().numpy()
+    return res[0] if scalar else res
+
+
+def expqt_site_specific(gtr, t):
+    """[q, q, L] stack of per-site P(t) (interpolated when approximate) computed
+    on the device with torch from the site eigendecompositions."""
+    tt = torch()
+    dev = require_device(None)
+    lam, V, Vi = gtr.site_matrices()
+    mu = np.asarray(gtr.mu, dtype=np.float64)
+    Vd, Vid = _to_dev(V, dev), _to_dev(Vi, dev)
+
+    def exact(x):
+        e = tt.exp(_to_dev(lam * mu[:, None] * x, dev))
+        return tt.einsum("aik,ak,akj->aij", Vd, e, Vid)
+
+    if gtr.approximate and t * gtr.rate_scale < 10:
+        grid = np.asarray(gtr.t_grid)
+        hi = int(np.clip(np.searchsorted(grid, t), 1, len(grid) - 1))
+        lo = hi - 1
+        ylo, yhi = exact(grid[lo]), exact(grid[hi])
+        res = (yhi - ylo) / (grid[hi] - grid[lo]) * (t - grid[lo]) + ylo
+    else:
+        res = exact(t)
+    return res.permute(1, 2, 0).contiguous().cpu().numpy()
+
+
+def propagate(gtr, profile, t, transpose=False, return_log=False):
+    tt = torch()
+    prof = np.asarray(profile, dtype=np.float64)
+    if gtr.is_site_specific:
+        dev = require_device(None)
+        Qt = _to_dev(expqt_site_specific(gtr, t), dev)
+        x = _to_dev(prof, dev)
+        if transpose:
+            res = tt.einsum("ai,jia->aj", x, Qt)
+            return (tt.log(res) if return_log else res).cpu().numpy()
+        res = tt.einsum("ai,ija->aj", x, Qt)
+        return (tt.log(tt.clamp(res, min=ttconf.TINY_NUMBER)) if return_log else tt.clamp(res, min=0.0)).cpu().numpy()
+    P = expqt(gtr, t)
+    model = gtr.device_model()
+    dev = model.device
+    q = gtr.n_states
+    d_prof = _to_dev(prof.reshape(-1, q), dev)
+    d_p = _to_dev(np.ascontiguousarray(P), dev)
+    res = tt.empty_like(d_prof)
+    check(_lib.load().tt_propagate(q, d_prof.shape[0], _p(d_prof), _p(d_p), None, int(transpose), int(return_log),
+                                   _p(res), _stream()), "tt_propagate")
+    return res.cpu().numpy().reshape(prof.shape)
+
+
+def pairs_to_counts(q, seq_pair, multiplicity):
+    counts = np.zeros((q, q), dtype=np.float64)
+    sp = np.asarray(seq_pair, dtype=np.int64).reshape(-1, 2)
+    np.add.at(counts, (sp[:, 0], sp[:, 1]), np.asarray(multiplicity, dtype=np.float64))
+    return counts
+
+
+def state_pair(gtr, seq_p, seq_ch, pattern_multiplicity=None, ignore_gaps=False):
+    """Histogram of (parent, child) state pairs on the device, returned in
+    TreeTime's order and with its int cast (treetime/gtr.py:631-712)."""
+    tt = torch()
+    seq_p = np.asarray(seq_p)
+    seq_ch = np.asarray(seq_ch)
+    if seq_ch.shape != seq_p.shape:
+        raise ValueError("GTR.state_pair: Sequence lengths do not match!")
+    P = len(seq_p)
+    mult = np.ones(P) if pattern_multiplicity is None else np.asarray(pattern_multiplicity, dtype=np.float64)
+    q = gtr.n_states
+    from .alphabets import chars_to_codes
+    cs = char_state_table(gtr)
+    sp, sc = cs[chars_to_codes(seq_p)], cs[chars_to_codes(seq_ch)]
+    dev = require_device(None)
+    f, keep = _mini_forest(2, q, np.zeros(2), dev, mult=mult, parent=[-1, 0], n_int=2, P=P)
+    states = _to_dev(np.concatenate([sp, sc]).astype(np.uint8), dev)
+    d_cs = _to_dev(cs, dev)
+    hist = tt.zeros((2, q, q), dtype=tt.float64, device=dev)
+    gap = gtr.gap_index
+    check(_lib.load().tt_state_pairs(C.byref(f), _p(states), _p(d_cs), 1, -1 if gap is None else gap,
+                                     int(bool(ignore_gaps)), None, _p(hist), _stream()), "tt_state_pairs")
+    h = hist[1].cpu().numpy()
+    if q < 10:
+        order = [(i, j) for i in range(q) for j in range(q) if h[i, j]]
+    else:
+        codes = sp.astype(np.int64) * q + sc
+        keep_mask = np.ones(P, dtype=bool)
+        if ignore_gaps and gap is not None:
+            keep_mask = (sp != gap) & (sc != gap)
+        uniq, first = np.unique(codes[keep_mask], return_index=True)
+        order = [divmod(int(c), q) for c in uniq[np.argsort(first, kind="stable")]]
+    pairs = np.array(order, dtype=int).reshape(-1, 2)
+    counts = np.array([h[i, j] for i, j in order], dtype=int)
+    return pairs, counts
+
+
+def prob_t_compressed(gtr, seq_pair, multiplicity, t, return_log=False):
+    tt = torch()
+    model = gtr.device_model()
+    q = gtr.n_states
+    counts = _to_dev(pairs_to_counts(q, seq_pair, multiplicity)[None], model.device)
+    d_t = _to_dev(np.array([t], dtype=np.float64), model.device)
+    out = tt.empty(1, dtype=tt.float64, device=model.device)
+    check(_lib.load().tt_prob_t_pairs(q, 1, _p(counts), None, C.byref(model.struct), _p(d_t), _p(out), _stream()),
+          "tt_prob_t_pairs")
+    v = float(out.item())
+    if t < 0:
+        v = -ttconf.BIG_NUMBER
+    return v if return_log else float(np.exp(v))
+
+
+def prob_t_profiles(gtr, profile_pair, multiplicity, t, return_log=False, ignore_gaps=True):
+    """Objective of the marginal branch-length mode, evaluated on the device with
+    torch (treetime/gtr.py:922-963)."""
+    tt = torch()
+    if t < 0:
+        v = -ttconf.BIG_NUMBER
+    else:
+        dev = require_device(None)
+        Qt = _to_dev(np.asarray(expqt(gtr, t)), dev)
+        pp, pc = (_to_dev(np.asarray(x, np.float64), dev) for x in profile_pair)
+        m = _to_dev(np.asarray(multiplicity, np.float64), dev)
+        if Qt.dim() == 3:
+            res = tt.einsum("ai,ija,aj->a", pc, Qt, pp)
+        else:
+            res = tt.einsum("ai,ij,aj->a", pc, Qt, pp)
+        term = m * tt.log(res + ttconf.SUPERTINY_NUMBER)
+        if ignore_gaps and gtr.gap_index is not None:
+            term = term * (1 - pp[:, gtr.gap_index]) * (1 - pc[:, gtr.gap_index])
+        v = float(term.sum().item())
+    return v if return_log else float(np.exp(v))
+
+
+def optimal_t_compressed(gtr, seq_pair, multiplicity, profiles=False, tol=1e-10):
+    model = gtr.device_model()
+    q = gtr.n_states
+    if not profiles:
+        counts = _to_dev(pairs_to_counts(q, seq_pair, multiplicity)[None], model.device)
+        tout, info = optimal_t_pairs(q, counts, model, tol=tol)
+    else:
+        pp, pc = (np.asarray(x, np.float64) for x in seq_pair)
+        P = pp.shape[0]
+        w = WIDTHS[q]
+        dev = model.device
+        f, keep = _mini_forest(2, q, np.zeros(2), dev, mult=multiplicity, parent=[-1, 0], n_int=2, P=P)
+        pad = lambda a: np.pad(a, ((0, 0), (0, w - q)))
+        d_pp = _to_dev(pad(pp), dev)
+        d_pc = _to_dev(pad(pc), dev)
+        tout, info = optimal_t_profiles(_ForestView(f, dev), model, [1], d_pp, [0], d_pc, [0], "f64", gtr.gap_index,
+                                        True, tol)
+    if int(info[0].item()) == -1:
+        check(_lib.TT_ERR_BRACKET, "optimal_t_compressed")
+    return float(tout[0].item())
+
+
+class _ForestView:
+    def __init__(self, struct, device):
+        self.struct = struct
+        self.device = device
+
+
+# ----------------------------------------------------------------------------
+# column compression on the device
+# ----------------------------------------------------------------------------
+def compress_columns(codes, ambiguous_code, device=None):
+    """Pattern compression with the column classification on the device;
+    identical output to seqdata.compress_codes."""
+    tt = torch()
+    dev = require_device(device)
+    codes = np.ascontiguousarray(codes, dtype=np.uint8)
+    n, L = codes.shape
+    d = _to_dev(codes, dev)
+    key = tt.empty(L, dtype=tt.int64, device=dev)
+    fixed = tt.empty(L, dtype=tt.int32, device=dev)
+    check(_lib.load().tt_compress_columns(_p(d), n, L, -1 if ambiguous_code is None else int(ambiguous_code),
+                                          _p(key), _p(fixed), _stream()), "tt_compress_columns")
+    key_h = key.cpu().numpy()
+    fixed_h = fixed.cpu().numpy()
+    uniq, first, inverse, counts = np.unique(key_h, return_index=True, return_inverse=True, return_counts=True)
+    order = np.argsort(first, kind="stable")
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    f2c = rank[inverse].astype(np.int64)
+    mult = counts[order].astype(float)
+    cols = first[order]
+    pc = np.ascontiguousarray(codes[:, cols])
+    fx = fixed_h[cols]
+    for j in np.flatnonzero(fx >= 0):
+        col = pc[:, j]
+        col[col == ambiguous_code] = fx[j]
+    pos_sorted = np.argsort(f2c, kind="stable")
+    bounds = np.concatenate(([0], np.cumsum(counts[order])))
+    c2f = {p: pos_sorted[bounds[p]:bounds[p + 1]].astype(int) for p in range(len(order))}
+    return pc, mult, f2c, c2f

@@ -100,6 +100,11 @@ class _Traversal:
                 ntips[id(node)] = 1
 
 
+# Per-node results of a reconstruction that are materialised on first access
+# from the device results (see treeanc.ResultStore).
+LAZY_ATTRS = ("_cseq", "marginal_profile", "marginal_subtree_LH", "marginal_outgroup_LH", "branch_state")
+
+
 class Clade(_Traversal):
     def __init__(self, branch_length=None, name=None, clades=None, confidence=None):
         self.branch_length = branch_length
@@ -109,6 +114,51 @@ class Clade(_Traversal):
 
     def _start(self):
         return self
+
+    def __getattr__(self, name):
+        # only reached when normal lookup fails: lazy reconstruction results
+        if name in LAZY_ATTRS:
+            src = self.__dict__.get("_anc_src")
+            if src is not None:
+                val = src.fetch(name, self)
+                if val is not None:
+                    self.__dict__[name] = val
+                    return val
+        raise AttributeError(name)
+
+    @property
+    def cseq(self):
+        """Compressed sequence: the alignment for tips (unless tip states were
+        reconstructed), the reconstruction otherwise (treetime/treeanc.py:14-24)."""
+        tt = self.__dict__.get("tt")
+        if tt is not None and tt.data is not None and self.name in tt.data.name_to_row \
+                and not tt.reconstructed_tip_sequences:
+            return tt.data.compressed_alignment[self.name]
+        try:
+            return self._cseq
+        except AttributeError:
+            if not self.clades:
+                return None
+            raise ValueError("Ancestral sequences are not yet inferred")
+
+    @property
+    def sequence(self):
+        return self.tt.sequence(self, as_string=False)
+
+    @property
+    def mutations(self):
+        """(ancestral, position, derived) list of the branch above this node
+        (treetime/treeanc.py:27-42)."""
+        tt = self.tt
+        up = self.__dict__.get("up")
+        if up is None:
+            return []
+        mask = self.__dict__.get("mask")
+        if not tt.reconstructed_tip_sequences and self.name in tt.data.name_to_row:
+            return tt.data.differences(up.cseq, tt.data.aln[self.name], seq2_compressed=False, mask=mask)
+        if not self.clades and self.name not in tt.data.name_to_row:
+            return []
+        return tt.data.differences(up.cseq, self.cseq, mask=mask)
 
     def is_terminal(self):
         return not self.clades

@@ -1,0 +1,410 @@
+"""Benchmark: marginal ancestral reconstruction throughput on the
+2,000-tip x 30,000-site workload (coalescent tree, branch lengths Exp(5e-4),
+GTR with transition/transversion ratio 3, 90% invariant sites -> ~3k
+compressed patterns), seeded synthetic data.
+
+One step = one full marginal reconstruction of the tree (branch matrices,
+post-order, root, pre-order, per-tree log-likelihood) with its inputs resident
+in HBM.  Metric: node-pattern updates per second (nodes x patterns per step /
+step time).  The FP32-scaled kernels are the measured path; the FP64 plain
+kernel, the end-to-end call through host buffers, the roofline of the
+dominant kernel and the CPU reference are reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: independent replicas (one process per GPU, torchrun), no
+collective on the data path; rank 0 prints the max-over-ranks timing.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "node-pattern updates/s (marginal reconstruction, FP32-scaled; FP64 plain beside it)"
+UNIT = "node-pattern updates/s"
+WORKLOAD = "c1: 2000-tip coalescent tree x 30000 nucleotide sites (90% invariant), GTR kappa=3, marginal"
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel_key):
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic.json")) as fh:
+            d = json.load(fh)
+        return d.get(kernel_key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(HERE, "gpurun_out", "clocks_%d.csv" % index)
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload(seed=1):
+    from treetime_gb300 import TreeAnc, synth
+    wl = synth.make_workload("c1", seed=seed)
+    t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision="f32")
+    return t, wl
+
+
+def algorithmic_bytes(layout, P, w=4, e=4, s=4):
+    """Bytes per marginal reconstruction of one tree: P * [N_int * (5*w*e +
+    3*s + 1) + n_tips * 1] + P * (8 + 4): five profile touches per internal
+    node (write own partial, read it as a child, read the parent posterior,
+    read own partial, write own posterior), three scale words, one state byte;
+    one code byte per tip; the FP64 site log-likelihood and the multiplicity."""
+    return P * (layout.n_int * (5 * w * e + 3 * s + 1) + layout.n_tip * 1) + P * (8 + 4)
+
+
+def run_gpu(args):
+    import torch
+    from treetime_gb300 import engine
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    t, wl = build_workload()
+    t.device = dev
+    sess = t._get_session()
+    forest, model, bufs, layout = sess["forest"], sess["model"], sess["bufs"], sess["layout"]
+    P = t.data.compressed_length
+    N = layout.n_nodes
+    units = N * P
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def step(prec):
+        return engine.marginal(forest, model, bufs, precision=prec, sync=False)
+
+    def timed(prec, k, w):
+        for _ in range(w):
+            step(prec)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            step(prec)
+            b.record()
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        return times
+
+    # parity of the measured path against the FP64 kernel on this workload
+    out64 = engine.marginal(forest, model, bufs, precision="f64")
+    lh64 = float(out64["tree_lh"][0].item())
+    out32 = engine.marginal(forest, model, bufs, precision="f32")
+    lh32 = float(out32["tree_lh"][0].item())
+    rel_err = abs(lh32 - lh64) / abs(lh64)
+
+    # FP64 plain kernel (untimed against the contract; reported beside)
+    t64 = timed("f64", max(3, args.steps // 4), 1)
+
+    # the measured path
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t32 = timed("f32", args.steps, args.warmup)
+        # dominant kernel alone, same stream, for the roofline
+        kt = []
+        pm, status = engine.branch_pmats(forest, model, bufs, need32=True)
+        for _ in range(args.steps):
+            flush.zero_()
+            out = engine.marginal(forest, model, bufs, precision="f32", sync=False)  # warm buffers
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            a.record()
+            _marginal_only(engine, forest, model, bufs, pm, "f32")
+            b.record()
+            b.synchronize()
+            kt.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    ms32 = sum(t32) / len(t32)
+    if world > 1:
+        import torch.distributed as dist
+        x = torch.tensor([ms32], device=dev)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        ms32 = float(x.item())
+
+    # end-to-end through host buffers (pinned), copies inside the timed region
+    e2e_ms, h2d, d2h = _e2e(engine, t, forest, model, bufs, args.steps, args.warmup, flush)
+
+    if rank != 0:
+        return None
+    peak, peak_kind = _peaks()
+    ab = algorithmic_bytes(layout, P)
+    k_ms = sum(kt) / len(kt)
+    achieved = ab / (k_ms * 1e-3) / 1e9
+    traffic = _traffic("marginal_f32_q4/c1")
+    clocks = clk.summary()
+    res = {
+        "metric": METRIC,
+        "value": world * units / (ms32 * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms32,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
+        "config": {"workload": WORKLOAD, "tips": layout.n_tip, "nodes": N, "patterns": P, "sites": t.data.full_length,
+                   "node_patterns_per_step": units, "l2": "flushed (512 MiB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64_plain": {"value": units / (statistics.mean(t64) * 1e-3), "ms_per_step": statistics.mean(t64)},
+        "fp32_over_fp64": statistics.mean(t64) / ms32,
+        "rel_logLH_err_vs_fp64": rel_err,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": "marginal_kernel<float,4,4,32>",
+                     "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms},
+        "e2e": {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        res["cpu_baseline"] = cpu_baseline(t)
+    return res
+
+
+def _marginal_only(engine, forest, model, bufs, pm, prec):
+    """Launch only the marginal pruning kernel (branch matrices already made)."""
+    import ctypes as C
+    import torch
+    from treetime_gb300 import _lib
+    lib = _lib.load()
+    dt = torch.float32 if prec == "f32" else torch.float64
+    w = forest.w
+    g = bufs.get
+    o = _lib.TTMarginalOut(engine._p(g("partial", (forest.prof_rows, w), dt)),
+                           engine._p(g("posterior", (forest.prof_rows, w), dt)), None, None, None,
+                           engine._p(g("states", (forest.state_rows,), torch.uint8)),
+                           engine._p(g("site_lh", (forest.n_patterns,), torch.float64)),
+                           engine._p(g("tree_lh", (len(forest.inputs),), torch.float64)), None, None, 0, 0)
+    _lib.check(lib.tt_marginal(C.byref(forest.struct), C.byref(model.struct), C.byref(pm),
+                               _lib.TT_PREC_F32 if prec == "f32" else _lib.TT_PREC_F64, C.byref(o), None,
+                               engine._stream()), "tt_marginal")
+
+
+def _e2e(engine, t, forest, model, bufs, steps, warmup, flush):
+    """Host buffers in, host buffers out: tip codes, branch lengths and
+    multiplicities are copied from pinned host memory, the reconstruction runs,
+    and the states and per-pattern log-likelihoods come back to pinned host
+    memory, every step."""
+    import torch
+    codes_h = torch.from_numpy(np.ascontiguousarray(t.data.compressed_codes).reshape(-1)).pin_memory()
+    bl_h = torch.from_numpy(forest.bl_host.copy()).pin_memory()
+    mult_h = torch.from_numpy(t.data.multiplicity().copy()).pin_memory()
+    states_h = torch.empty(forest.state_rows, dtype=torch.uint8).pin_memory()
+    lh_h = torch.empty(forest.n_patterns, dtype=torch.float64).pin_memory()
+    h2d = codes_h.numel() + bl_h.numel() * 8 + mult_h.numel() * 8
+    d2h = states_h.numel() + lh_h.numel() * 8 + 8
+
+    def one():
+        forest.d_codes[: codes_h.numel()].copy_(codes_h, non_blocking=True)
+        forest.d_bl.copy_(bl_h, non_blocking=True)
+        forest.d_mult.copy_(mult_h, non_blocking=True)
+        out = engine.marginal(forest, model, bufs, precision="f32", sync=False)
+        states_h.copy_(out["states"], non_blocking=True)
+        lh_h.copy_(out["site_lh"], non_blocking=True)
+        return float(out["tree_lh"][0].item())
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        one()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return sum(times) / len(times), int(h2d), int(d2h)
+
+
+# ----------------------------------------------------------------------------
+# CPU reference: TreeTime's marginal algorithm restated in numpy (the oracle)
+# ----------------------------------------------------------------------------
+def _oracle_chunk(args):
+    newick, names, codes, mult, gtr_state, full_length = args
+    from oracle import anc
+    from treetime_gb300.tree import parse_newick
+    tree = anc.prepare_tree(parse_newick(newick))
+    chars = codes.view("S1").astype("U1")
+    aln = {k: chars[i] for i, k in enumerate(names)}
+    t0 = time.perf_counter()
+    anc.marginal(tree, aln, mult, gtr_state, full_length)
+    return time.perf_counter() - t0
+
+
+def _model_state(gtr):
+    """Picklable copy of the model attributes the oracle reads."""
+    import types
+    return types.SimpleNamespace(v=gtr.v, v_inv=gtr.v_inv, eigenvals=gtr.eigenvals, mu=gtr.mu, Pi=gtr.Pi,
+                                 alphabet=gtr.alphabet, profile_map=dict(gtr.profile_map), gap_index=gtr.gap_index,
+                                 is_site_specific=False)
+
+
+def _oracle_inputs(t, p_slices):
+    from treetime_gb300.tree import to_newick
+    nwk = to_newick(t.tree)
+    names = t.data.sequence_names
+    codes = t.data.compressed_codes
+    mult = t.data.multiplicity()
+    m = _model_state(t.gtr)
+    return [(nwk, names, np.ascontiguousarray(codes[:, s]), mult[s], m, t.data.full_length) for s in p_slices]
+
+
+def cpu_baseline(t):
+    """The oracle marginal on the full workload, one process (bounded: one
+    reconstruction, ~5-20 s)."""
+    P = t.data.compressed_length
+    N = t.tree.count_terminals() * 2 - 1
+    secs = _oracle_chunk(_oracle_inputs(t, [slice(0, P)])[0])
+    return {"value": N * P / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "one full marginal reconstruction of the workload (numpy restatement of TreeTime, 1 process)",
+            "seconds": secs}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path (numpy
+    restatement of TreeTime's marginal algorithm) on all host cores: patterns
+    split across a spawn-started process pool (patterns are independent)."""
+    world, rank, local = _dist()
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    t, wl = build_workload()
+    P = t.data.compressed_length
+    N = t.tree.count_terminals() * 2 - 1
+    cores = os.cpu_count() or 1
+    chunks = [slice(i * P // cores, (i + 1) * P // cores) for i in range(cores)]
+    inputs = _oracle_inputs(t, chunks)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_oracle_chunk, inputs)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            pool.map(_oracle_chunk, inputs)
+            times.append(time.perf_counter() - t0)
+    sec = sum(times) / len(times)
+    v = N * P / sec
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "patterns": P, "nodes": N},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "full marginal reconstruction per step, patterns split over %d processes"
+                                       % cores},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        res = run_reference(args)
+    else:
+        from treetime_gb300 import build
+        build.build()
+        res = run_gpu(args)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

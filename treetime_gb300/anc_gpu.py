@@ -1,0 +1,481 @@
+"""``GPUAncMixin``: the reconstruction and branch-length methods of TreeAnc
+implemented on the GPU.
+
+The mixin replaces exactly the hot-path methods of treetime/treeanc.py:
+``_ml_anc_marginal`` (:762), ``_ml_anc_joint`` (:934),
+``optimize_branch_lengths_joint`` (:1176), ``optimal_branch_length`` (:1244),
+``optimal_marginal_branch_length`` (:1272), ``optimize_tree_marginal``
+(:1297) and ``prune_short_branches`` (:1475).  It reads only the state
+TreeTime's own classes keep (``tree``, ``data``, ``gtr``, ``rng``,
+``sequence_reconstruction``, ``reconstructed_tip_sequences``,
+``use_mutation_length``, ``ignore_gaps``, ``logger``), so it composes with
+``treetime_gb300.TreeAnc`` and, placed first in the MRO, with TreeTime's own
+classes::
+
+    class TreeTimeGPU(GPUAncMixin, treetime.TreeTime): pass
+
+Nodes of ``treetime_gb300.tree.Clade`` receive their per-node arrays lazily;
+other clade objects (Bio.Phylo) receive them as attributes right away.
+"""
+
+import ctypes as C
+
+import numpy as np
+
+from . import config as ttconf
+from . import engine
+from .alphabets import chars_to_codes, profile_lut
+from .errors import MissingDataError
+from .tree import LAZY_ATTRS, Clade
+
+
+class ResultStore:
+    """Host view of one reconstruction's device results; node attributes are
+    built from it on first access."""
+
+    def __init__(self, tt, layout, kind, out, precision, reconstruct_tips):
+        self.tt = tt
+        self.layout = layout
+        self.kind = kind
+        self.out = out
+        self.precision = precision
+        self.reconstruct_tips = reconstruct_tips
+        self.P = tt.data.compressed_length
+        self.q = tt.gtr.n_states
+        n = layout.n_nodes
+        self.states = out["states"].view(-1)[: n * self.P].cpu().numpy().reshape(n, self.P)
+        self._host = {}
+
+    def _fetch_buf(self, key):
+        if key not in self._host:
+            buf = self.out.get(key)
+            self._host[key] = None if buf is None else buf.cpu().numpy()
+        return self._host[key]
+
+    def _rows(self, key, j):
+        buf = self._fetch_buf(key)
+        if buf is None:
+            return None
+        return buf[j * self.P:(j + 1) * self.P, :self.q].astype(np.float64)
+
+    def fetch(self, name, node):
+        L = self.layout
+        k = L.local.get(id(node))
+        if k is None:
+            return None
+        is_tip = k >= L.n_int
+        if name == "_cseq":
+            if is_tip and not self.reconstruct_tips:
+                return None
+            return self.tt.gtr.alphabet[self.states[k]]
+        if self.kind != "marginal":
+            return None
+        if name == "marginal_profile":
+            return self._rows("tip_posterior", k - L.n_int) if is_tip else self._rows("posterior", k)
+        if name == "marginal_subtree_LH":
+            if is_tip:
+                return self.tt._tip_profile(node)
+            x = self._rows("partial", k)
+            if self.precision == "f32":  # FP32 partials are power-of-two scaled
+                x = x / x.sum(axis=1, keepdims=True)
+            return x
+        if name == "marginal_outgroup_LH":
+            if k == L.n_int - 1:
+                return self.tt._root_outgroup()
+            return self._rows("tip_outgroup", k - L.n_int) if is_tip else self._rows("outgroup", k)
+        return None
+
+
+class BranchStateStore:
+    """``branch_state`` dictionaries from the device pair histograms."""
+
+    def __init__(self, layout, hist):
+        self.layout = layout
+        self.hist = hist
+
+    def fetch(self, name, node):
+        if name != "branch_state":
+            return None
+        k = self.layout.local.get(id(node))
+        if k is None or getattr(node, "up", None) is None:
+            return None
+        h = self.hist[k]
+        idx = np.argwhere(h != 0)
+        return {"pair": idx.astype(int), "multiplicity": h[idx[:, 0], idx[:, 1]].astype(int)}
+
+
+class _ChainedSource:
+    def __init__(self, *srcs):
+        self.srcs = [s for s in srcs if s is not None]
+
+    def fetch(self, name, node):
+        for s in self.srcs:
+            v = s.fetch(name, node)
+            if v is not None:
+                return v
+        return None
+
+
+class GPUAncMixin:
+    """GPU implementations of TreeAnc's reconstruction and branch-length methods."""
+
+    # ----------------------------------------------------------- device session
+    def _gpu_precision(self):
+        return getattr(self, "precision", "f64")
+
+    def _aln_index(self):
+        """(name -> row, compressed byte matrix) of the alignment."""
+        d = self.data
+        if hasattr(d, "compressed_codes") and hasattr(d, "name_to_row"):
+            return d.name_to_row, d.compressed_codes
+        key = (id(d), d.compressed_length, id(d.compressed_alignment))
+        cache = getattr(self, "_aln_index_cache", None)
+        if cache is None or cache[0] != key:
+            names = list(d.compressed_alignment.keys())
+            codes = np.stack([chars_to_codes(d.compressed_alignment[k]) for k in names])
+            cache = (key, {k: i for i, k in enumerate(names)}, codes)
+            self._aln_index_cache = cache
+        return cache[1], cache[2]
+
+    def _masks_changed(self, sess):
+        cur = {k: id(getattr(n, "mask", None)) for k, n in enumerate(sess["layout"].nodes)
+               if getattr(n, "mask", None) is not None}
+        return cur != sess["mask_ids"]
+
+    def _get_session(self):
+        """Device-resident schedule and inputs of the current tree, rebuilt when
+        the topology, alignment, model or masks change; branch lengths are
+        refreshed on every call."""
+        s = getattr(self, "_session", None)
+        gtr_key = engine.model_key(self.gtr)
+        if s is not None and s["root"] is self.tree.root and s["data"] is self.data and s["gtr_key"] == gtr_key \
+                and s["n_nodes"] == self.tree.count_terminals() + len(self.tree.get_nonterminals()) \
+                and not self._masks_changed(s):
+            bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
+            engine.check_exp(self.gtr, bl)
+            s["forest"].set_branch_lengths([bl])
+            return s
+        device = getattr(self, "device", None)
+        layout = engine.TreeLayout(self.tree.root)
+        name_to_row, codes = self._aln_index()
+        tip_row = np.full(layout.n_tip, -1, dtype=np.int32)
+        for j, n in enumerate(layout.nodes[layout.n_int:]):
+            r = name_to_row.get(n.name)
+            if r is not None:
+                tip_row[j] = r
+        masks, mask_ids = {}, {}
+        for k, n in enumerate(layout.nodes):
+            m = getattr(n, "mask", None)
+            if m is not None:
+                masks[k] = np.asarray(m, dtype=np.float64)
+                mask_ids[k] = id(m)
+        bl = engine.branch_lengths(layout, self.data.full_length, self.use_mutation_length)
+        engine.check_exp(self.gtr, bl)
+        ti = engine.TreeInput(layout, codes, tip_row, self.data.multiplicity(), bl, masks=masks)
+        forest = engine.Forest([ti], self.gtr.n_states, device=device)
+        model = None if self.gtr.is_site_specific else engine.model_for(self.gtr, device)
+        s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
+                 root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes)
+        self._session = s
+        return s
+
+    def _tip_profile(self, node):
+        name_to_row, codes = self._aln_index()
+        r = name_to_row.get(node.name)
+        if r is None:
+            return np.ones((self.data.compressed_length, self.gtr.n_states))
+        return profile_lut(self.gtr.profile_map, self.gtr.n_states)[codes[r]]
+
+    def _root_outgroup(self):
+        Pi = np.asarray(self.gtr.Pi)
+        L = self.data.compressed_length
+        return np.repeat([Pi], L, axis=0) if Pi.ndim == 1 else np.copy(Pi.T)
+
+    def _seed_tip_states(self, sess):
+        """Before the first reconstruction that includes tips, tip rows of the
+        state buffer hold the alignment's states (255 for characters that are not
+        states), so changed-site counts compare against the alignment as TreeTime
+        does."""
+        layout = sess["layout"]
+        P = self.data.compressed_length
+        name_to_row, codes = self._aln_index()
+        strict = np.full(256, 255, np.uint8)
+        for i, c in enumerate(self.gtr.alphabet):
+            strict[ord(str(c))] = i
+        tip = np.full((layout.n_tip, P), 255, dtype=np.uint8)
+        for j, n in enumerate(layout.nodes[layout.n_int:]):
+            r = name_to_row.get(n.name)
+            if r is not None:
+                tip[j] = strict[codes[r]]
+        states = sess["bufs"].get("states", (sess["forest"].state_rows,), engine.torch().uint8)
+        states[layout.n_int * P:].copy_(engine.torch().from_numpy(tip.reshape(-1)))
+
+    def _clear_results(self, layout):
+        for n in layout.nodes:
+            d = n.__dict__
+            for a in LAZY_ATTRS:
+                d.pop(a, None)
+            d.pop("_anc_src", None)
+            for a in ("joint_Lx", "joint_Cx", "seq_idx", "marginal_log_Lx", "marginal_subtree_LH_prefactor"):
+                d.pop(a, None)
+
+    def _install(self, src, layout):
+        for n in layout.nodes:
+            if isinstance(n, Clade):
+                n.__dict__["_anc_src"] = src
+            else:  # foreign clade objects: materialise eagerly
+                for a in LAZY_ATTRS:
+                    v = src.fetch(a, n)
+                    if v is not None:
+                        setattr(n, a, v)
+
+    def _root_draws(self, sample_from_profile):
+        if sample_from_profile is True:
+            raise NotImplementedError("sampling states at every node is not supported; use 'root' or False")
+        if sample_from_profile == "root":
+            return self.rng.random(size=self.data.compressed_length)
+        return None
+
+    # --------------------------------------------------------- reconstruction
+    def _ml_anc_marginal(self, sample_from_profile=False, reconstruct_tip_states=False, debug=False,
+                         keep_outgroup=True, **kwargs):
+        """Marginal reconstruction in one device pass (treetime/treeanc.py:762-932)."""
+        self.logger("TreeAnc._ml_anc_marginal: type of reconstruction: Marginal (GPU)", 2)
+        sess = self._get_session()
+        layout = sess["layout"]
+        count_diff = bool(self.sequence_reconstruction)
+        if reconstruct_tip_states and count_diff and not self.reconstructed_tip_sequences:
+            self._seed_tip_states(sess)
+        draws = self._root_draws(sample_from_profile)
+        prec = self._gpu_precision()
+        kw = dict(precision=prec, reconstruct_tips=reconstruct_tip_states, keep_outgroup=keep_outgroup,
+                  tip_outgroup=keep_outgroup, count_diff=count_diff, root_uniform=draws)
+        if self.gtr.is_site_specific:
+            out = engine.marginal_site_specific(sess["forest"], self.gtr, sess["bufs"], **kw)
+        else:
+            out = engine.marginal(sess["forest"], sess["model"], sess["bufs"], **kw)
+        self._clear_results(layout)
+        P = self.data.compressed_length
+        n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
+        N_diff = int(out["n_diff"][0].item()) if count_diff else P * n_recon
+        self._install(ResultStore(self, layout, "marginal", out, prec, reconstruct_tip_states), layout)
+        self.tree.sequence_LH = out["site_lh"].cpu().numpy()
+        self.tree.total_sequence_LH = float(out["tree_lh"][0].item())
+        self.tree.sequence_marginal_LH = self.tree.total_sequence_LH
+        self.reconstructed_tip_sequences = reconstruct_tip_states
+        self.sequence_reconstruction = "marginal"
+        self._last = ("marginal", out)
+        return N_diff
+
+    def _ml_anc_joint(self, sample_from_profile=False, reconstruct_tip_states=False, debug=False, **kwargs):
+        """Joint reconstruction in one device pass (treetime/treeanc.py:934-1080)."""
+        if self.gtr.is_site_specific:
+            raise NotImplementedError("joint reconstruction with site-specific models is not supported")
+        self.logger("TreeAnc._ml_anc_joint: type of reconstruction: Joint (GPU)", 2)
+        sess = self._get_session()
+        layout = sess["layout"]
+        count_diff = bool(self.sequence_reconstruction)
+        if reconstruct_tip_states and count_diff and not self.reconstructed_tip_sequences:
+            self._seed_tip_states(sess)
+        draws = self._root_draws(sample_from_profile)
+        out = engine.joint(sess["forest"], sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
+                           count_diff=count_diff, root_uniform=draws)
+        self._clear_results(layout)
+        P = self.data.compressed_length
+        n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
+        N_diff = int(out["n_diff"][0].item()) if count_diff else P * n_recon
+        self._install(ResultStore(self, layout, "joint", out, "f64", reconstruct_tip_states), layout)
+        self.tree.sequence_LH = out["site_lh"].cpu().numpy()
+        self.tree.sequence_joint_LH = float(out["tree_lh"][0].item())
+        self.reconstructed_tip_sequences = reconstruct_tip_states
+        self.sequence_reconstruction = "joint"
+        self._last = ("joint", out)
+        return N_diff
+
+    # --------------------------------------------------------- branch lengths
+    def _pair_histograms(self):
+        sess = self._get_session()
+        layout = sess["layout"]
+        name_to_row, _ = self._aln_index()
+        if not self.reconstructed_tip_sequences:
+            for n in layout.nodes[layout.n_int:]:
+                if n.name not in name_to_row:
+                    raise MissingDataError(
+                        "TreeAnc.optimal_branch_length: terminal node alignments required; sequence is missing for "
+                        "leaf: '%s'. Missing terminal sequences can be inferred from sister nodes by rerunning with "
+                        "`reconstruct_tip_states=True` or `--reconstruct-tip-states`" % n.name)
+        hist, _ = engine.state_pairs(sess["forest"], sess["bufs"], engine.char_state_table(self.gtr),
+                                     self.gtr.gap_index, self.ignore_gaps, self.reconstructed_tip_sequences)
+        return sess, hist
+
+    def optimize_branch_lengths_joint(self, **kwargs):
+        """All branches in one device pass: pair histograms, then Brent per
+        branch (treetime/treeanc.py:1176-1242)."""
+        self.logger("TreeAnc.optimize_branch_length: running branch length optimization using jointML ancestral "
+                    "sequences", 1)
+        if self.tree is None or self.data is None or self.data.aln is None:
+            raise MissingDataError("TreeAnc.optimize_branch_length: ERROR, alignment or tree are missing.")
+        if not self.sequence_reconstruction:
+            raise ValueError("Ancestral sequences are not yet inferred")
+        store_old = kwargs.get("store_old", False)
+        sess, hist = self._pair_histograms()
+        layout = sess["layout"]
+        counts = engine.torch().trunc(hist)  # TreeTime casts pair counts to int
+        t, info = engine.optimal_t_pairs(self.gtr.n_states, counts, sess["model"], tol=1e-10)
+        t = t.cpu().numpy()
+        info = info.cpu().numpy()
+        root_k = layout.n_int - 1
+        if any(info[k] == -1 for k in range(layout.n_nodes) if k != root_k):
+            engine.check(engine._lib.TT_ERR_BRACKET, "optimize_branch_lengths_joint")
+        max_bl = 0.0
+        for k, node in enumerate(layout.nodes):
+            if k == root_k:
+                continue
+            if store_old:
+                node._old_length = node.branch_length
+            new_len = max(0.0, float(t[k]))
+            if new_len > 0.9 * ttconf.MAX_BRANCH_LENGTH:
+                self.logger("WARNING: GTR.optimal_t_compressed -- The branch length seems to be very long!", 4,
+                            warn=True)
+            node.branch_length = new_len
+            node.mutation_length = new_len
+            max_bl = max(max_bl, new_len)
+        bstore = BranchStateStore(layout, counts.cpu().numpy())
+        for n in layout.nodes:
+            if isinstance(n, Clade):
+                n.__dict__.pop("branch_state", None)
+                prev = n.__dict__.get("_anc_src")
+                n.__dict__["_anc_src"] = _ChainedSource(prev, bstore) if prev is not None else bstore
+            else:
+                v = bstore.fetch("branch_state", n)
+                if v is not None:
+                    n.branch_state = v
+        if max_bl > 0.15:
+            self.logger("TreeAnc.optimize_branch_lengths_joint: THIS TREE HAS LONG BRANCHES."
+                        " \n\t ****TreeTime's JOINT IS NOT DESIGNED TO OPTIMIZE LONG BRANCHES."
+                        " \n\t ****PLEASE OPTIMIZE BRANCHES USING: "
+                        " \n\t ****branch_length_mode='input' or 'marginal'", 0, warn=True)
+        self.tree.root.up = None
+        self.tree.root.dist2root = 0.0
+        self._prepare_nodes()
+        return ttconf.SUCCESS
+
+    def optimal_branch_length(self, node):
+        """One branch: device pair histogram and Brent (treetime/treeanc.py:1244-1270)."""
+        if node.up is None:
+            return self.one_mutation
+        if node.cseq is None and not node.clades:
+            raise MissingDataError("TreeAnc.optimal_branch_length: terminal node alignments required; sequence is "
+                                   "missing for leaf: '%s'." % node.name)
+        pairs, mult = engine.state_pair(self.gtr, node.up.cseq, node.cseq,
+                                        self.data.multiplicity(mask=getattr(node, "mask", None)), self.ignore_gaps)
+        node.branch_state = {"pair": pairs, "multiplicity": mult}
+        return engine.optimal_t_compressed(self.gtr, pairs, mult)
+
+    def _marginal_branch_lengths(self, nodes, tol):
+        """Profile-mode Brent for the given nodes in one device pass, from the
+        outgroup and subtree profiles of the last marginal reconstruction."""
+        last = getattr(self, "_last", None)
+        if last is None or last[0] != "marginal" or last[1].get("outgroup") is None:
+            raise Exception("marginal ancestral inference needs to be performed first!")
+        out = last[1]
+        sess = self._get_session()
+        layout = sess["layout"]
+        P = self.data.compressed_length
+        ks = [layout.local[id(n)] for n in nodes]
+        res = np.zeros(len(nodes))
+        info = np.zeros(len(nodes), dtype=np.int32)
+        groups = (([i for i, k in enumerate(ks) if k < layout.n_int], out["outgroup"], False),
+                  ([i for i, k in enumerate(ks) if k >= layout.n_int], out["tip_outgroup"], True))
+        for idx, pp, tips in groups:
+            if not idx:
+                continue
+            kk = [ks[i] for i in idx]
+            pp_row = [((k - layout.n_int) if tips else k) * P for k in kk]
+            pc_row = [-1 if tips else k * P for k in kk]
+            t, inf = engine.optimal_t_profiles(sess["forest"], engine.model_for(self.gtr, getattr(self, "device", None)),
+                                               kk, pp, pp_row, out["partial"], pc_row, self._gpu_precision(),
+                                               self.gtr.gap_index, True, tol)
+            res[idx] = t.cpu().numpy()
+            info[idx] = inf.cpu().numpy()
+        if (info == -1).any():
+            engine.check(engine._lib.TT_ERR_BRACKET, "optimal_marginal_branch_length")
+        return res
+
+    def optimal_marginal_branch_length(self, node, tol=1e-10):
+        if node.up is None:
+            return self.one_mutation
+        return float(self._marginal_branch_lengths([node], tol)[0])
+
+    def optimize_tree_marginal(self, max_iter=10, infer_gtr=False, pc=1.0, damping=0.75, LHtol=0.1,
+                               site_specific_gtr=False, **kwargs):
+        """treetime/treeanc.py:1297-1360, with the branches of an iteration
+        optimised in one device pass."""
+        if infer_gtr:
+            parent = super()
+            if hasattr(parent, "optimize_tree_marginal"):
+                return parent.optimize_tree_marginal(max_iter=max_iter, infer_gtr=infer_gtr, pc=pc, damping=damping,
+                                                     LHtol=LHtol, site_specific_gtr=site_specific_gtr, **kwargs)
+            raise NotImplementedError("GTR inference is not part of the GPU hot path")
+        self.infer_ancestral_sequences(marginal=True, **kwargs)
+        oldLH = self.sequence_LH()
+        for i in range(max_iter):
+            old_bl = self.tree.total_branch_length()
+            tol = 1e-8 + 0.01 ** (i + 1)
+            root = self.tree.root
+            special = len(root.clades) == 2
+            nodes = [n for n in self.tree.find_clades() if n.up is not None and not (special and n.up is root)]
+            new = dict(zip([id(n) for n in nodes], self._marginal_branch_lengths(nodes, tol))) if nodes else {}
+            if special:
+                n1, n2 = root.clades
+                total_bl = n1.branch_length + n2.branch_length
+                bl_ratio = n1.branch_length / total_bl
+                prof_c = n1.marginal_subtree_LH
+                tmp = n2.marginal_subtree_LH * root.marginal_outgroup_LH
+                prof_p = np.einsum("ai,a->ai", tmp, 1.0 / tmp.sum(axis=1))
+                m1, m2 = getattr(n1, "mask", None), getattr(n2, "mask", None)
+                mult = self.data.multiplicity() if m1 is None or m2 is None else self.data.multiplicity(mask=m1 * m2)
+                new_bl = engine.optimal_t_compressed(self.gtr, (prof_p, prof_c), mult, profiles=True, tol=tol)
+                update = new_bl * (1 - damping ** (i + 1)) + total_bl * damping ** (i + 1)
+                n1.branch_length = update * bl_ratio
+                n2.branch_length = update * (1 - bl_ratio)
+                n1.mutation_length = n1.branch_length
+                n2.mutation_length = n2.branch_length
+            for n in nodes:
+                update = new[id(n)] * (1 - damping ** (i + 1)) + n.branch_length * damping ** (i + 1)
+                n.branch_length = update
+                n.mutation_length = update
+            self.infer_ancestral_sequences(marginal=True, **kwargs)
+            LH = self.sequence_LH()
+            deltaLH = LH - oldLH
+            oldLH = LH
+            self.logger("TreeAnc.optimize_tree_marginal: iteration %d, LH=%1.2f (%1.2f), delta branch_length=%1.4f"
+                        % (i, LH, deltaLH, self.tree.total_branch_length() - old_bl), 2)
+            if deltaLH < LHtol:
+                break
+        return ttconf.SUCCESS
+
+    def prune_short_branches(self):
+        """Collapse internal branches shorter than 0.1 / L whose sequences have
+        probability > 0.1 at distance zero (treetime/treeanc.py:1475-1497); the
+        histograms and zero-length likelihoods of all branches come from one
+        device pass."""
+        self.logger("TreeAnc.prune_short_branches: pruning short branches (max prob at zero)...", 1)
+        sess, hist = self._pair_histograms()
+        layout = sess["layout"]
+        counts = engine.torch().trunc(hist)
+        prob0 = np.exp(engine.prob_t_pairs_batch(self.gtr.n_states, counts, sess["model"], 0.0))
+        changed = False
+        for node in self.tree.find_clades():
+            if node.up is None or not node.clades:
+                continue
+            k = layout.local.get(id(node))
+            if k is None:
+                continue
+            if node.branch_length < 0.1 * self.one_mutation and prob0[k] > 0.1:
+                node.up.clades = [c for c in node.up.clades if c is not node] + node.clades
+                for c in node.clades:
+                    c.up = node.up
+                changed = True
+        if changed:
+            self._session = None

@@ -110,6 +110,32 @@ def compress_codes(codes, ambiguous_code, compress=True):
     return pattern_codes, multiplicity, full_to_compressed, c2f
 
 
+class _LazyCharRows(OrderedDict):
+    """name -> character array of the alignment, built from the byte matrix on
+    first access of each row."""
+
+    def __init__(self, names, codes):
+        super().__init__((k, None) for k in names)
+        self._codes = codes
+        self._row = {k: i for i, k in enumerate(names)}
+
+    def __getitem__(self, k):
+        v = super().__getitem__(k)
+        if v is None:
+            v = codes_to_chars(self._codes[self._row[k]])
+            super().__setitem__(k, v)
+        return v
+
+    def values(self):
+        return [self[k] for k in self.keys()]
+
+    def items(self):
+        return [(k, self[k]) for k in self.keys()]
+
+    def get(self, k, default=None):
+        return self[k] if k in self else default
+
+
 class SequenceData:
     """Alignment container with TreeTime's SequenceData interface for dense
     alignments (dict name -> sequence, an iterable of records with id/name/seq,
@@ -156,18 +182,26 @@ class SequenceData:
                 raise MissingDataError("SequenceData: loading alignment failed... " + str(in_aln))
         if not raw:
             raise MissingDataError("SequenceData: loading alignment failed... empty alignment")
-        first = [seq2array(s, convert_upper=self.convert_upper) for _, s in raw[:50]]
-        self.likely_alphabet = guess_alphabet(first)
+        rows = [self._to_codes(v) for _, v in raw]
+        sample = np.concatenate([r[:20000] for r in rows[:50]])
+        nucish = np.isin(sample, np.frombuffer(b"acgtACGT-N", dtype=np.uint8)).sum()
+        self.likely_alphabet = "nuc" if nucish > 0.9 * len(sample) else "aa"
         if self.ambiguous is None:
             self.ambiguous = "N" if self.likely_alphabet == "nuc" else "X"
-        arrays = OrderedDict()
-        for name, s in raw:
-            arrays[name] = seq2array(s, convert_upper=self.convert_upper, fill_overhangs=self.fill_overhangs,
-                                     ambiguous=self.ambiguous)
-        lengths = {len(a) for a in arrays.values()}
+        lengths = {len(r) for r in rows}
         if len(lengths) != 1:
             raise MissingDataError("SequenceData: sequences have different lengths")
         L = lengths.pop()
+        if self.fill_overhangs:
+            amb = ord(self.ambiguous)
+            gap = ord("-")
+            for r in rows:
+                ng = np.flatnonzero(r != gap)
+                if len(ng):
+                    r[: ng[0]] = amb
+                    r[ng[-1] + 1:] = amb
+                else:
+                    r[:] = amb
         if self._full_length:
             if self._full_length < L:
                 raise AttributeError("SequenceData.aln: specified sequence length is smaller than alignment length!")
@@ -176,11 +210,23 @@ class SequenceData:
                 raise NotImplementedError("additional constant sites are not supported")
         else:
             self._full_length = L
-        self._aln = arrays
-        self.sequence_names = list(arrays.keys())
-        self.codes = np.stack([chars_to_codes(arrays[k]) for k in self.sequence_names]) \
-            if arrays else np.zeros((0, L), np.uint8)
+        self.sequence_names = [k for k, _ in raw]
+        self.codes = np.stack(rows) if rows else np.zeros((0, L), np.uint8)
+        self._aln = _LazyCharRows(self.sequence_names, self.codes)
         self.make_compressed_alignment()
+
+    def _to_codes(self, v):
+        if isinstance(v, np.ndarray) and v.dtype == np.uint8:
+            return v.copy()
+        if isinstance(v, np.ndarray):
+            v = "".join(v.astype("U").tolist())
+        elif hasattr(v, "seq"):
+            v = str(v.seq)
+        elif not isinstance(v, str):
+            v = str(v)
+        if self.convert_upper:
+            v = v.upper()
+        return np.frombuffer(v.encode("latin-1"), dtype=np.uint8).copy()
 
     @property
     def full_length(self):

@@ -100,14 +100,23 @@ typedef struct tt_forest {
     const double*  bl;         /* [n_nodes] branch length above the node as used by the model       */
     const uint8_t* tip_codes;  /* tip character bytes                                              */
     const double*  mult;       /* [n_patterns] pattern multiplicities                              */
-    /* Schedule of the persistent pruning kernels: tiles of 32 consecutive patterns of one tree,
-       given as (tree, first pattern) pairs, largest trees first.  One CTA walks a whole tree for a
-       tile; tiles never wait on each other. */
+    /* Schedule of the persistent pruning kernels: tiles of consecutive patterns of one tree, given
+       as (tree, first pattern) pairs, largest trees first.  One CTA walks a whole tree for a tile;
+       tiles never wait on each other.  `work` holds 32-pattern tiles (one lane per pattern, used by
+       every kernel); the FP32 marginal kernel with lanes_per_pattern > 1 reads `work_f32`, whose
+       tiles hold 32 / lanes_per_pattern patterns. */
     const int32_t* work;       /* [n_work][2]                                                      */
     int32_t n_work;
-    int32_t warps_per_block;   /* 4, 8, 16 or 32 warps share the nodes of a level (0: 8)           */
+    int32_t warps_per_block;   /* 8 or >= 16 (wide CTAs) warps share the nodes of a level (0: 8)   */
     int32_t max_blocks;        /* grid size cap (0: one CTA per tile)                              */
+    int32_t lanes_per_pattern; /* 1, 2 or 4 lanes per pattern in the FP32 marginal kernel          */
+    const int32_t* work_f32;   /* [n_work_f32][2]                                                  */
+    int32_t n_work_f32;
     int32_t reserved;
+    const int32_t* node_rec;   /* [n_nodes][4]: first child entry, end of child entries, parent
+                                  local id (-1 at the root), tip row (-1 for internal nodes)      */
+    const int32_t* child_pair; /* [n_nodes][4] for nodes with two children: (child 0, its tip row,
+                                  child 1, its tip row); unused otherwise                          */
 } tt_forest;
 
 typedef struct tt_model {

@@ -1,0 +1,101 @@
+"""GPU: every launch shape of the FP32 marginal kernel (lanes per pattern,
+warps per CTA) and the FP64 kernel give the oracle's results, on a tree with
+polytomies, masks and missing data, for 4- and 5-state alphabets.  Also the
+multi-tree forest (one launch over several trees of different sizes and
+models) against per-tree oracle runs."""
+
+import numpy as np
+import pytest
+
+from oracle import anc
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(alphabet, seed, n=40, L=300):
+    from treetime_gb300 import synth
+    wl = synth.make_workload("c0", seed=seed, n=n, L=L, alphabet=alphabet, mean_bl=0.03)
+    tree = wl["tree"]
+    # a polytomy: splice one internal node's children into its parent
+    inner = [c for c in tree.find_clades(order="postorder") if c.clades and c is not tree.root]
+    c = inner[len(inner) // 2]
+    for par in tree.find_clades():
+        if c in par.clades:
+            i = par.clades.index(c)
+            par.clades[i:i + 1] = c.clades
+            break
+    return wl
+
+
+def _oracle(t):
+    from treetime_gb300.tree import parse_newick, to_newick
+    tree = anc.prepare_tree(parse_newick(to_newick(t.tree)))
+    byname = {n.name: n for n in t.tree.find_clades()}
+    for n in anc.preorder(tree.root):
+        n.mask = getattr(byname[n.name], "mask", None)
+    return anc.marginal(tree, t.data.compressed_alignment, t.data.multiplicity(), t.gtr, t.data.full_length,
+                        reconstruct_tip_states=True)
+
+
+@pytest.mark.parametrize("alphabet", ["nuc_nogap", "nuc"])
+@pytest.mark.parametrize("shape", [(1, 8), (1, 32), (2, 8), (2, 16), (4, 8), (4, 16), ("f64", 8), ("f64", 32)])
+def test_marginal_launch_shapes(alphabet, shape):
+    from treetime_gb300 import TreeAnc
+    lpp, warps = shape
+    wl = _workload(alphabet, seed=7)
+    prec = "f64" if lpp == "f64" else "f32"
+    t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision=prec,
+                lanes_per_pattern=None if lpp == "f64" else lpp, warps_per_block=warps)
+    rng = np.random.default_rng(1)
+    for n in list(t.tree.find_clades())[3:9]:
+        n.mask = (rng.random(t.data.compressed_length) < 0.6).astype(float)
+    t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=True)
+    ref = _oracle(t)
+    tol = 1e-10 if prec == "f64" else 1e-5
+    assert abs(t.tree.total_sequence_LH - ref["total_sequence_LH"]) <= (1e-10 if prec == "f64" else 1e-6) * \
+        abs(ref["total_sequence_LH"])
+    for n in t.tree.find_clades():
+        np.testing.assert_allclose(n.marginal_profile, ref["profile"][n.name], atol=tol, rtol=0)
+        if n.up is not None:
+            np.testing.assert_allclose(n.marginal_outgroup_LH, ref["outgroup_LH"][n.name], atol=tol, rtol=0)
+        prof = ref["profile"][n.name]
+        s = np.sort(prof, axis=1)
+        ok = (n._cseq == ref["cseq"][n.name]) | (s[:, -1] - s[:, -2] < (1e-9 if prec == "f64" else 1e-5))
+        assert ok.all(), n.name
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_forest_of_many_trees(precision):
+    """One launch over trees of different sizes and models equals the
+    per-tree oracle."""
+    from treetime_gb300 import GTR, engine, synth
+    from treetime_gb300.seqdata import SequenceData
+    rng = np.random.default_rng(9)
+    inputs, refs, models = [], [], []
+    for k in range(6):
+        n = int(rng.integers(5, 60))
+        L = int(rng.integers(20, 400))
+        tree = synth.coalescent_tree(n, float(rng.uniform(0.005, 0.1)), rng, prefix="t")
+        gtr = GTR.random(alphabet="nuc_nogap", rng=rng)
+        states = synth.evolve(tree, gtr, L, rng)
+        aln = synth._to_text(states, gtr.alphabet, 0.02, rng)
+        anc.prepare_tree(tree)
+        sd = SequenceData(aln, ambiguous="N")
+        layout = engine.TreeLayout(tree.root)
+        tip_row = np.array([sd.name_to_row[n.name] for n in layout.nodes[layout.n_int:]], dtype=np.int32)
+        bl = engine.branch_lengths(layout, sd.full_length)
+        inputs.append(engine.TreeInput(layout, sd.compressed_codes, tip_row, sd.multiplicity(), bl, model=k))
+        models.append(gtr)
+        refs.append(anc.marginal(tree, sd.compressed_alignment, sd.multiplicity(), gtr, sd.full_length))
+    forest = engine.Forest(inputs, 4)
+    model = engine.DeviceModel(models)
+    out = engine.marginal(forest, model, engine.Buffers(forest), precision=precision)
+    tree_lh = out["tree_lh"].cpu().numpy()
+    post = out["posterior"].cpu().numpy()
+    for k, (ti, ref) in enumerate(zip(inputs, refs)):
+        assert abs(tree_lh[k] - ref["total_sequence_LH"]) <= 1e-6 * abs(ref["total_sequence_LH"])
+        tr = forest.trees_host[k]
+        P = ti.n_patterns
+        for j, n in enumerate(ti.layout.nodes[:ti.layout.n_int]):
+            rows = post[tr["prof_base"] + j * P: tr["prof_base"] + (j + 1) * P, :4]
+            np.testing.assert_allclose(rows, ref["profile"][n.name], atol=1e-5 if precision == "f32" else 1e-10)

@@ -35,7 +35,9 @@ class TTForest(C.Structure):
                 ("n_nodes", i64), ("n_patterns", i64),
                 ("trees", vp), ("level_off", vp), ("child_off", vp), ("child_idx", vp), ("parent", vp),
                 ("tip_row", vp), ("mask_off", vp), ("masks", vp), ("bl", vp), ("tip_codes", vp), ("mult", vp),
-                ("work", vp), ("n_work", i32), ("warps_per_block", i32), ("max_blocks", i32), ("reserved", i32)]
+                ("work", vp), ("n_work", i32), ("warps_per_block", i32), ("max_blocks", i32),
+                ("lanes_per_pattern", i32), ("work_f32", vp), ("n_work_f32", i32), ("reserved", i32),
+                ("node_rec", vp), ("child_pair", vp)]
 
 
 class TTModel(C.Structure):

@@ -172,7 +172,9 @@ class GPUAncMixin:
         bl = engine.branch_lengths(layout, self.data.full_length, self.use_mutation_length)
         engine.check_exp(self.gtr, bl)
         ti = engine.TreeInput(layout, codes, tip_row, self.data.multiplicity(), bl, masks=masks)
-        forest = engine.Forest([ti], self.gtr.n_states, device=device)
+        forest = engine.Forest([ti], self.gtr.n_states, device=device,
+                               lanes_per_pattern=getattr(self, "lanes_per_pattern", None),
+                               warps_per_block=getattr(self, "warps_per_block", None))
         model = None if self.gtr.is_site_specific else engine.model_for(self.gtr, device)
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
                  root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes)

@@ -315,7 +315,10 @@ __global__ void optimal_t_profiles_kernel(ProfParams a) {
         msum = block_sum(msum, red);
         ovsum = block_sum(ovsum, red);
         __syncthreads();
-        const double hamming = 1.0 - ovsum / msum;
+        // 1 - overlap can round to a tiny negative number when the profiles agree
+        // completely (sqrt would give NaN); the distance is never negative
+        double hamming = 1.0 - ovsum / msum;
+        hamming = hamming > 0.0 ? hamming : 0.0;
         auto f = [&](double s) -> double {
             const double t = s * s;
             double e[32];

@@ -156,6 +156,74 @@ class DeviceModel:
                               _p(self.lut))
 
 
+_MODEL_CACHE = {}
+
+
+def model_key(gtr):
+    """Identity of a model's numbers: changes whenever its rates, frequencies or
+    profile map change."""
+    return (id(gtr), id(gtr.v), id(gtr.v_inv), id(gtr.eigenvals), float(np.sum(gtr.mu)), id(gtr.Pi),
+            len(gtr.profile_map))
+
+
+def model_for(gtr, device=None):
+    """Cached DeviceModel of any object with TreeTime's GTR attributes."""
+    dev = require_device(device)
+    key = (model_key(gtr), str(dev))
+    m = _MODEL_CACHE.get(id(gtr))
+    if m is None or m[0] != key:
+        m = (key, DeviceModel(gtr, dev))
+        _MODEL_CACHE[id(gtr)] = m
+    return m[1]
+
+
+def check_exp(gtr, t):
+    """TreeTime raises ValueError when some mu*lambda*t exceeds 10
+    (treetime/gtr.py:1042-1047); checked on the host before launching."""
+    t = np.asarray(t, dtype=np.float64)
+    if t.size == 0:
+        return
+    lam = np.asarray(gtr.eigenvals, dtype=np.float64)
+    mu = np.asarray(gtr.mu, dtype=np.float64)
+    top = float(np.max(mu * lam)) if lam.ndim == 1 else float(np.max(mu[None, :] * lam))
+    if getattr(gtr, "is_site_specific", False) and getattr(gtr, "approximate", False):
+        return
+    if top > 0 and top * float(np.max(t)) > 10:
+        raise ValueError("Error in computing exp(Q * t): Q has positive eigenvalues or the branch length t is too "
+                         "large. This is most likely caused by incorrect input data.")
+
+
+def site_matrices(gtr):
+    """(lambda [L, q], V [L, q, q], V^-1 [L, q, q]) of a site-specific model,
+    from TreeTime's layouts eigenvals [q, L], v [q, q, L], v_inv [q, q, L]."""
+    lam = np.ascontiguousarray(np.asarray(gtr.eigenvals).T)
+    V = np.ascontiguousarray(np.transpose(gtr.v, (2, 1, 0)))
+    Vi = np.ascontiguousarray(np.transpose(gtr.v_inv, (2, 1, 0)))
+    return lam, V, Vi
+
+
+def site_grid(gtr):
+    """Time grid of the interpolated expQt (treetime/gtr_site_specific.py:336-343)."""
+    if hasattr(gtr, "t_grid"):
+        return np.asarray(gtr.t_grid, dtype=np.float64)
+    if hasattr(gtr, "expQt_interpolator"):
+        return np.asarray(gtr.expQt_interpolator.x, dtype=np.float64)
+    rs = gtr.average_rate().mean()
+    return (1.0 / rs) * np.concatenate((np.linspace(0, 0.1, 11)[:-1], np.linspace(0.1, 1, 21)[:-1],
+                                        np.linspace(1, 5, 21)[:-1], np.linspace(5, 10, 11)))
+
+
+def prob_t_pairs_batch(q, counts, model, t):
+    """log P of every branch's pair counts at one branch length t (device)."""
+    tt = torch()
+    n = counts.shape[0]
+    d_t = tt.full((n,), float(t), dtype=tt.float64, device=counts.device)
+    out = tt.empty(n, dtype=tt.float64, device=counts.device)
+    check(_lib.load().tt_prob_t_pairs(q, n, _p(counts), None, C.byref(model.struct), _p(d_t), _p(out), _stream()),
+          "tt_prob_t_pairs")
+    return out.cpu().numpy()
+
+
 def char_state_table(gtr):
     """byte -> state index of the alphabet; TreeTime's state_pair leaves
     non-alphabet characters out for alphabets below 10 states and counts them
@@ -193,7 +261,7 @@ class Forest:
     """Device-resident schedule and inputs of a list of trees, plus the
     C-ABI struct that points at them."""
 
-    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, need_tip_rows=False):
+    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, lanes_per_pattern=None):
         dev = require_device(device)
         self.device = dev
         self.inputs = list(inputs)
@@ -209,6 +277,7 @@ class Forest:
         mask_elems = 0
         child_base = 0
         work = []
+        recs, pairs = [], []
         for t, ti in enumerate(inputs):
             L = ti.layout
             P = ti.n_patterns
@@ -217,6 +286,22 @@ class Forest:
             lev.append(L.level_off)
             coff.append(L.child_off[:-1] + child_base)
             cidx.append(L.child_idx)
+            rec = np.zeros((L.n_nodes, 4), dtype=np.int32)
+            rec[:, 0] = L.child_off[:-1] + child_base
+            rec[:, 1] = L.child_off[1:] + child_base
+            rec[:, 2] = L.parent
+            rec[:, 3] = -1
+            rec[L.n_int:, 3] = ti.tip_row
+            pair = np.full((L.n_nodes, 4), -1, dtype=np.int32)
+            binary = np.flatnonzero((L.child_off[1:] - L.child_off[:-1]) == 2)
+            c0 = L.child_idx[L.child_off[binary]]
+            c1 = L.child_idx[L.child_off[binary] + 1]
+            pair[binary, 0] = c0
+            pair[binary, 1] = rec[c0, 3]
+            pair[binary, 2] = c1
+            pair[binary, 3] = rec[c1, 3]
+            recs.append(rec)
+            pairs.append(pair)
             child_base += len(L.child_idx)
             par.append(L.parent)
             tr = np.full(L.n_nodes, -1, dtype=np.int32)
@@ -244,6 +329,23 @@ class Forest:
         child_off = np.concatenate(coff + [np.array([total_children], dtype=np.int32)]).astype(np.int32)
         work.sort(key=lambda w: -w[0])
         self.work_host = np.array([(t, p0) for _, t, p0 in work], dtype=np.int32).reshape(-1, 2)
+        sms = _lib.load().tt_device_sm_count()
+        if lanes_per_pattern is None:
+            # few 32-pattern tiles: split patterns over more lanes to get more CTAs
+            n32 = len(self.work_host)
+            lanes_per_pattern = 4 if n32 < 2 * sms else (2 if n32 < 6 * sms else 1)
+        if q >= 20:
+            lanes_per_pattern = 4
+        elif q == 5:
+            lanes_per_pattern = min(lanes_per_pattern, 2)
+        self.lanes_per_pattern = lanes_per_pattern
+        tile = TILE // lanes_per_pattern
+        wf = []
+        for t, ti in enumerate(inputs):
+            for p0 in range(0, ti.n_patterns, tile):
+                wf.append((ti.layout.n_nodes * min(tile, ti.n_patterns - p0), t, p0))
+        wf.sort(key=lambda w: -w[0])
+        self.work_f32_host = np.array([(t, p0) for _, t, p0 in wf], dtype=np.int32).reshape(-1, 2)
         self.trees_host = trees
         self.n_nodes = node_base
         self.n_patterns = pat_base
@@ -265,14 +367,18 @@ class Forest:
         self.d_mask_off = _to_dev(np.concatenate(moff), dev) if self.has_masks else None
         self.d_masks = _to_dev(np.concatenate(mvals), dev) if self.has_masks else None
         self.d_work = _to_dev(self.work_host, dev)
+        self.d_work_f32 = _to_dev(self.work_f32_host, dev)
+        self.d_node_rec = _to_dev(np.concatenate(recs), dev)
+        self.d_child_pair = _to_dev(np.concatenate(pairs), dev)
         if warps_per_block is None:
-            warps_per_block = 32 if len(self.work_host) < 2 * _lib.load().tt_device_sm_count() else 8
+            warps_per_block = 16 if len(self.work_f32_host) < 2 * sms else 8
         self.struct = TTForest(
             len(inputs), q, self.w, int(max((ti.layout.n_levels for ti in inputs), default=0)),
             self.n_nodes, self.n_patterns, _p(self.d_trees), _p(self.d_level), _p(self.d_child_off),
             _p(self.d_child_idx), _p(self.d_parent), _p(self.d_tip_row), _p(self.d_mask_off), _p(self.d_masks),
             _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
-            warps_per_block, max_blocks, 0)
+            warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host), 0,
+            _p(self.d_node_rec), _p(self.d_child_pair))
 
     def set_branch_lengths(self, bl_list):
         """Replace branch lengths (same topology) without rebuilding."""
@@ -369,15 +475,15 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
     f32 = precision == "f32"
     dt = t.float32 if f32 else t.float64
     dev = forest.device
-    key = id(gtr)
+    key = model_key(gtr)
     cache = bufs.cache.get("ss_model")
     if cache is None or cache[0] != key:
-        lam, V, Vi = gtr.site_matrices()
+        lam, V, Vi = site_matrices(gtr)
         arrs = dict(lam=_to_dev(lam, dev), V=_to_dev(V, dev), Vi=_to_dev(Vi, dev),
                     mu=_to_dev(np.asarray(gtr.mu, dtype=np.float64), dev),
                     pi=_to_dev(np.ascontiguousarray(gtr.Pi.T), dev),
                     lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev),
-                    grid=_to_dev(np.asarray(gtr.t_grid, dtype=np.float64), dev))
+                    grid=_to_dev(site_grid(gtr), dev))
         bufs.cache["ss_model"] = (key, arrs)
     arrs = bufs.cache["ss_model"][1]
     w = forest.w
@@ -400,7 +506,7 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
                       _p(out["tip_outgroup"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
                       _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
     check(lib.tt_marginal_ss(C.byref(forest.struct), _p(arrs["lam"]), _p(arrs["V"]), _p(arrs["Vi"]), _p(arrs["mu"]),
-                             _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]), len(gtr.t_grid),
+                             _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]), int(arrs["grid"].numel()),
                              float(gtr.rate_scale), int(bool(gtr.approximate)),
                              _lib.TT_PREC_F32 if f32 else _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()),
           "tt_marginal_ss")
@@ -499,7 +605,7 @@ def _mini_forest(n_nodes, q, bl, device, mult=None, parent=None, n_int=None, P=1
     keep["tip_row"] = _to_dev(np.full(n_nodes, -1, np.int32), dev)
     w = WIDTHS[q]
     f = TTForest(1, q, w, 0, n_nodes, P, _p(keep["trees"]), None, None, None, _p(keep["parent"]), _p(keep["tip_row"]),
-                 None, None, _p(keep["bl"]), None, _p(keep["mult"]), None, 0, 8, 0, 0)
+                 None, None, _p(keep["bl"]), None, _p(keep["mult"]), None, 0, 8, 0, 1, None, 0, 0, None, None)
     return f, keep
 
 
@@ -510,8 +616,8 @@ def expqt(gtr, t):
     tt = torch()
     scalar = np.ndim(t) == 0
     ts = np.atleast_1d(np.asarray(t, dtype=np.float64))
-    gtr.check_branch_lengths(ts)
-    model = gtr.device_model()
+    check_exp(gtr, ts)
+    model = model_for(gtr)
     q = gtr.n_states
     w = WIDTHS[q]
     f, keep = _mini_forest(len(ts), q, ts, model.device)
@@ -529,7 +635,7 @@ def expqt_site_specific(gtr, t):
     on the device with torch from the site eigendecompositions."""
     tt = torch()
     dev = require_device(None)
-    lam, V, Vi = gtr.site_matrices()
+    lam, V, Vi = site_matrices(gtr)
     mu = np.asarray(gtr.mu, dtype=np.float64)
     Vd, Vid = _to_dev(V, dev), _to_dev(Vi, dev)
 
@@ -538,7 +644,7 @@ def expqt_site_specific(gtr, t):
         return tt.einsum("aik,ak,akj->aij", Vd, e, Vid)
 
     if gtr.approximate and t * gtr.rate_scale < 10:
-        grid = np.asarray(gtr.t_grid)
+        grid = site_grid(gtr)
         hi = int(np.clip(np.searchsorted(grid, t), 1, len(grid) - 1))
         lo = hi - 1
         ylo, yhi = exact(grid[lo]), exact(grid[hi])
@@ -561,7 +667,7 @@ def propagate(gtr, profile, t, transpose=False, return_log=False):
         res = tt.einsum("ai,ija->aj", x, Qt)
         return (tt.log(tt.clamp(res, min=ttconf.TINY_NUMBER)) if return_log else tt.clamp(res, min=0.0)).cpu().numpy()
     P = expqt(gtr, t)
-    model = gtr.device_model()
+    model = model_for(gtr)
     dev = model.device
     q = gtr.n_states
     d_prof = _to_dev(prof.reshape(-1, q), dev)
@@ -618,7 +724,7 @@ def state_pair(gtr, seq_p, seq_ch, pattern_multiplicity=None, ignore_gaps=False)
 
 def prob_t_compressed(gtr, seq_pair, multiplicity, t, return_log=False):
     tt = torch()
-    model = gtr.device_model()
+    model = model_for(gtr)
     q = gtr.n_states
     counts = _to_dev(pairs_to_counts(q, seq_pair, multiplicity)[None], model.device)
     d_t = _to_dev(np.array([t], dtype=np.float64), model.device)
@@ -654,7 +760,7 @@ def prob_t_profiles(gtr, profile_pair, multiplicity, t, return_log=False, ignore
 
 
 def optimal_t_compressed(gtr, seq_pair, multiplicity, profiles=False, tol=1e-10):
-    model = gtr.device_model()
+    model = model_for(gtr)
     q = gtr.n_states
     if not profiles:
         counts = _to_dev(pairs_to_counts(q, seq_pair, multiplicity)[None], model.device)

@@ -201,12 +201,9 @@ class GTR:
 
     # --------------------------------------------------------- device calls
     def device_model(self, device=None):
-        """Cached FP64/FP32 device copies of V, V⁻¹, eigenvalues and pi."""
+        """Cached FP64 device copies of V, V⁻¹, eigenvalues, pi and the profile table."""
         from . import engine
-        key = str(device)
-        if self._device_cache is None or self._device_cache[0] != key:
-            self._device_cache = (key, engine.DeviceModel(self, device))
-        return self._device_cache[1]
+        return engine.model_for(self, device)
 
     def expQt(self, t):
         """P(t) = max(0, V·diag(exp(mu·lambda·t))·V⁻¹) on the GPU; ``t`` may be a

@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
     __shared__ int4 rec_s[kChunk];
     __shared__ int4 pair_s[kChunk];
     __shared__ int red[NW][32];
+    __shared__ float red_corr[NW][32];
     __shared__ unsigned diff_red[NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pl = lane / LPP, part = lane % LPP, j0 = part * S;
@@ -189,6 +190,10 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
         const int64_t nb = tr.node_base;
         const int32_t* lev = a.f.level_off + tr.level_base;
         int esum = 0;
+        // log-LH correction for masked internal children: TreeTime masks the log message of the
+        // child's sum-normalised partial and adds its prefactor unmasked; with power-of-two scaled
+        // partials that leaves (1 - m) * log(sum of the scaled partial) to add
+        float lcorr = 0.f;
 
         auto row_of = [&](int k) -> int64_t { return (tr.prof_base + (int64_t)k * P + pc) * W + j0; };
         auto tip_part = [&](int trow, float (&x)[S]) {
@@ -205,8 +210,17 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
                 const int64_t mo = __ldg(a.f.mask_off + nb + c);
                 if (mo >= 0) {
                     const float m = (float)__ldg(a.f.masks + mo + pc);
+                    // padding states (j >= Q) stay 0 so that products over children keep them 0
 #pragma unroll
-                    for (int s = 0; s < S; ++s) msg[s] = m == 0.f ? 1.f : (m == 1.f ? msg[s] : exp2f(m * log2f(msg[s])));
+                    for (int s = 0; s < S; ++s)
+                        if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : (m == 1.f ? msg[s] : exp2f(m * log2f(msg[s])));
+                    if (c < tr.n_int) {
+                        float xs = 0.f;
+#pragma unroll
+                        for (int s = 0; s < S; ++s) xs += x[s];
+                        xs = group_sum<LPP>(xs);
+                        if (m != 1.f) lcorr += (1.f - m) * logf(xs);
+                    }
                 }
             }
         };
@@ -270,12 +284,17 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
         }
         // per-pattern exponent sums: lanes of one pattern hold identical values; warps add up
         red[warp][lane] = esum;
+        red_corr[warp][lane] = lcorr;
         __syncthreads();
 
         // ---------------- root
         if (warp == 0) {
             int tot = 0;
-            for (int w = 0; w < NW; ++w) tot += red[w][lane];
+            double corr = 0.0;
+            for (int w = 0; w < NW; ++w) {
+                tot += red[w][lane];
+                corr += (double)red_corr[w][lane];
+            }
             const int kr = tr.n_int - 1;
             const double* pi = a.pi + (int64_t)tr.model * Q;
             float x[S], pr[S];
@@ -304,7 +323,7 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
             if (valid) {
                 st_part<S>(posterior + row_of(kr), pr);
                 if (part == 0) {
-                    a.o.site_lh[tr.pat_base + p] = log((double)ssum) + kLn2 * (double)tot;
+                    a.o.site_lh[tr.pat_base + p] = log((double)ssum) + kLn2 * (double)tot + corr;
                     a.o.states[tr.state_base + (int64_t)kr * P + pc] = (uint8_t)st;
                 }
                 if (a.o.outgroup) {
@@ -346,7 +365,8 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
                     }
                     if (m != 1.f) {
 #pragma unroll
-                        for (int s = 0; s < S; ++s) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
+                        for (int s = 0; s < S; ++s)
+                            if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
                     }
                     float sl = 0.f;
 #pragma unroll
@@ -371,7 +391,7 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
                     float s2 = 0.f;
 #pragma unroll
                     for (int s = 0; s < S; ++s) {
-                        if (m != 1.f) ev[s] = m * ev[s] + (1.f - m);
+                        if (m != 1.f && j0 + s < Q) ev[s] = m * ev[s] + (1.f - m);
                         x[s] *= ev[s];
                         s2 += x[s];
                     }

@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(NW * 32) marginal_ss_kernel(SSParams a) {
     constexpr bool F32 = std::is_same<T, float>::value;
     using Acc = typename std::conditional<F32, int, double>::type;
     __shared__ Acc red[NW][32];
+    __shared__ double red_corr[NW][32];
     __shared__ unsigned diff_red[NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T* partial = reinterpret_cast<T*>(a.o.partial);
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(NW * 32) marginal_ss_kernel(SSParams a) {
         const int64_t nb = tr.node_base;
         const int32_t* lev = a.f.level_off + tr.level_base;
         Acc acc = Acc(0);
+        double lcorr = 0.0;  // FP32: masked internal children, see tt_marginal_f32.cu
         for (int h = 0; h < tr.n_levels; ++h) {
             const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
             for (int k = lo + warp; k < hi; k += NW) {
@@ -172,6 +174,14 @@ __global__ void __launch_bounds__(NW * 32) marginal_ss_kernel(SSParams a) {
                     T msg[W];
                     ss_propagate<Q, W, T>(V, Vi, em1, x, msg);
                     const double m = ss_mask(a, gc, pc);
+                    if constexpr (F32) {
+                        if (m != 1.0 && c < tr.n_int) {
+                            float xs = 0.f;
+#pragma unroll
+                            for (int j = 0; j < Q; ++j) xs += x[j];
+                            lcorr += (1.0 - m) * log((double)xs);
+                        }
+                    }
 #pragma unroll
                     for (int j = 0; j < Q; ++j) {
                         if constexpr (F32) {
@@ -217,10 +227,15 @@ __global__ void __launch_bounds__(NW * 32) marginal_ss_kernel(SSParams a) {
             __syncthreads();
         }
         red[warp][lane] = acc;
+        red_corr[warp][lane] = lcorr;
         __syncthreads();
         if (warp == 0) {
             Acc tot = Acc(0);
-            for (int w = 0; w < NW; ++w) tot += red[w][lane];
+            double corr = 0.0;
+            for (int w = 0; w < NW; ++w) {
+                tot += red[w][lane];
+                corr += red_corr[w][lane];
+            }
             const int kr = tr.n_int - 1;
             T x[W], pr[W];
             load_row<W>(partial + (tr.prof_base + (int64_t)kr * P + pc) * W, x);
@@ -233,7 +248,7 @@ __global__ void __launch_bounds__(NW * 32) marginal_ss_kernel(SSParams a) {
             const T inv = (T)(1.0 / s);
 #pragma unroll
             for (int j = 0; j < Q; ++j) pr[j] *= inv;
-            const double lh = F32 ? log(s) + kLn2 * (double)tot : (double)tot + log(s);
+            const double lh = F32 ? log(s) + kLn2 * (double)tot + corr : (double)tot + log(s);
             const int st = a.o.root_uniform ? sample_cdf<Q, T, W>(pr, a.o.root_uniform[tr.pat_base + pc])
                                             : argmax_first<Q, T, W>(pr);
             if (valid) {

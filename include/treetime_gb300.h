@@ -214,6 +214,22 @@ tt_status tt_marginal_ss(const tt_forest* f, const double* lam, const double* V,
 tt_status tt_joint(const tt_forest* f, const tt_model* m, const tt_pmats* pm, const tt_joint_out* out,
                    int32_t* status, void* stream);
 
+/* Joint reconstruction that allocates nothing.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory (hosts that only hand out their own pre-sized
+ * buffers, pools that reserve all device memory at start-up, paths that cannot afford an
+ * allocation's synchronisation).  Same results as tt_branch_pmats + tt_joint; the branch matrices
+ * and the joint_Lx / joint_Cx scratch live in one fixed device array of
+ * TT_JOINT_NOALLOC_SCRATCH_BYTES inside the library (held by every GPU that loads it).
+ * `internal_rows` = sum over trees of n_int * n_patterns.  Problems needing more scratch than
+ * 2*align256(n_nodes*q*width*8) + align256(internal_rows*width*8) + align256(internal_rows*width)
+ * <= TT_JOINT_NOALLOC_SCRATCH_BYTES are rejected with TT_ERR_OOM.  The first call on each device
+ * looks the array's device address up (cudaGetSymbolAddress) and should come before any stream
+ * capture; calls share the array, so calls that overlap on the GPU race and must be serialised. */
+#define TT_JOINT_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+tt_status tt_joint_noalloc(const tt_forest* f, const tt_model* m, int64_t internal_rows, uint8_t* states,
+                           double* site_lh, double* tree_lh, unsigned long long* n_diff, const double* root_uniform,
+                           int32_t reconstruct_tips, int32_t count_diff, int32_t* status, void* stream);
+
 /* ---------------------------------------------------- a14: state pairs
  * For every non-root node k with use[k] != 0: the (parent, child) state-pair histogram
  * hist[k][i][j] = sum over patterns of mult (times the node's mask) where the parent has state i

@@ -71,6 +71,7 @@ _SIGS = {
     "tt_marginal": (i32, [P(TTForest), P(TTModel), P(TTPmats), i32, P(TTMarginalOut), vp, vp]),
     "tt_marginal_ss": (i32, [P(TTForest), vp, vp, vp, vp, vp, vp, vp, i32, f64, i32, i32, P(TTMarginalOut), vp, vp]),
     "tt_joint": (i32, [P(TTForest), P(TTModel), P(TTPmats), P(TTJointOut), vp, vp]),
+    "tt_joint_noalloc": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, vp, vp]),
     "tt_state_pairs": (i32, [P(TTForest), vp, vp, i32, i32, i32, vp, vp, vp]),
     "tt_optimal_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), f64, vp, vp, vp]),
     "tt_prob_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), vp, vp, vp]),

@@ -1,0 +1,99 @@
+// Joint reconstruction without any device allocation by the caller or the library.
+//
+// Some callers cannot call cudaMalloc: plugin hosts that hand out only their own pre-sized
+// buffers, processes whose device memory is fully reserved by a pool at start-up, and code
+// paths where the implicit synchronisation of an allocation is not acceptable.  tt_joint needs
+// scratch beyond its inputs and outputs (the branch matrices and their logs, and the per-node
+// max-product messages joint_Lx / argmax table joint_Cx); this entry point takes that scratch
+// from one fixed array in the library's device image instead of from the caller.
+//
+// The array is a file-scope __device__ object of TT_JOINT_NOALLOC_SCRATCH_BYTES bytes; every
+// GPU that loads this library holds it until the process exits.  Host code must not use the
+// symbol's host-side name as a device address: the device address is looked up once per
+// device with cudaGetSymbolAddress (on the first call made while that device is current) and
+// cached.  That first call per device therefore touches the module and should come before any
+// stream capture.  All calls share the one array and it keeps the last call's contents:
+// nothing in it has to start at zero (every scratch entry is written before it is read), but
+// calls that overlap on the GPU (different streams, or host threads) race on it and must be
+// serialised by the caller.
+#include <mutex>
+
+#include "tt_internal.cuh"
+
+static __device__ __align__(256) unsigned char tt_joint_noalloc_scratch[TT_JOINT_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_scratch_mu;
+constexpr int kMaxDevices = 256;
+void* g_scratch_dev[kMaxDevices] = {};
+
+tt_status scratch_address(void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        tt::set_error("tt_joint_noalloc: no current CUDA device (%s)", cudaGetErrorString(e));
+        return TT_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_dev[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, tt_joint_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            tt::set_error("tt_joint_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
+                          cudaGetErrorString(e));
+            return TT_ERR_CUDA;
+        }
+        g_scratch_dev[dev] = p;
+    }
+    *out = g_scratch_dev[dev];
+    return TT_OK;
+}
+
+inline uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
+
+}  // namespace
+
+extern "C" tt_status tt_joint_noalloc(const tt_forest* f, const tt_model* m, int64_t internal_rows,
+                                      uint8_t* states, double* site_lh, double* tree_lh,
+                                      unsigned long long* n_diff, const double* root_uniform,
+                                      int32_t reconstruct_tips, int32_t count_diff, int32_t* status,
+                                      void* stream) {
+    if (!f || !m || !states || !site_lh || !tree_lh || internal_rows < 0 || f->width < 1 || f->n_states < 2) {
+        tt::set_error("tt_joint_noalloc: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    const uint64_t q = (uint64_t)f->n_states, w = (uint64_t)f->width, n = (uint64_t)f->n_nodes;
+    const uint64_t pmat_bytes = align256(n * q * w * sizeof(double));
+    const uint64_t lx_bytes = align256((uint64_t)internal_rows * w * sizeof(double));
+    const uint64_t cx_bytes = align256((uint64_t)internal_rows * w);
+    const uint64_t need = 2 * pmat_bytes + lx_bytes + cx_bytes;
+    if (need > TT_JOINT_NOALLOC_SCRATCH_BYTES) {
+        tt::set_error("tt_joint_noalloc: problem needs %llu bytes of scratch, the fixed scratch holds %llu "
+                      "(%lld nodes x %d states, %lld internal-node pattern rows); use tt_joint with caller buffers",
+                      (unsigned long long)need, (unsigned long long)TT_JOINT_NOALLOC_SCRATCH_BYTES,
+                      (long long)f->n_nodes, f->n_states, (long long)internal_rows);
+        return TT_ERR_OOM;
+    }
+    void* base = nullptr;
+    tt_status st = scratch_address(&base);
+    if (st != TT_OK) return st;
+    unsigned char* b = static_cast<unsigned char*>(base);
+    tt_pmats pm;
+    pm.p64 = reinterpret_cast<double*>(b);
+    pm.p32 = nullptr;
+    pm.logp64 = reinterpret_cast<double*>(b + pmat_bytes);
+    st = tt_branch_pmats(f, m, pm, status, stream);
+    if (st != TT_OK) return st;
+    tt_joint_out jo;
+    jo.lx = reinterpret_cast<double*>(b + 2 * pmat_bytes);
+    jo.cx = b + 2 * pmat_bytes + lx_bytes;
+    jo.states = states;
+    jo.site_lh = site_lh;
+    jo.tree_lh = tree_lh;
+    jo.n_diff = n_diff;
+    jo.root_uniform = root_uniform;
+    jo.reconstruct_tips = reconstruct_tips;
+    jo.count_diff = count_diff;
+    return tt_joint(f, m, &pm, &jo, status, stream);
+}

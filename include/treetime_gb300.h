@@ -77,7 +77,9 @@ typedef struct tt_tree {
     int32_t n_levels;     /* number of height levels of internal nodes                             */
     int32_t n_patterns;
     int32_t model;        /* row of this tree's model in tt_model arrays                           */
-    int32_t reserved;
+    int32_t n_smem;       /* FP32 marginal kernel: the top n_smem internal nodes (local ids
+                             n_int-n_smem .. n_int-1, the narrow upper levels) keep their rows in
+                             shared memory for the whole pass; 0..n_int                            */
 } tt_tree;
 
 typedef struct tt_forest {
@@ -103,20 +105,28 @@ typedef struct tt_forest {
     /* Schedule of the persistent pruning kernels: tiles of consecutive patterns of one tree, given
        as (tree, first pattern) pairs, largest trees first.  One CTA walks a whole tree for a tile;
        tiles never wait on each other.  `work` holds 32-pattern tiles (one lane per pattern, used by
-       every kernel); the FP32 marginal kernel with lanes_per_pattern > 1 reads `work_f32`, whose
-       tiles hold 32 / lanes_per_pattern patterns. */
+       every kernel); the FP32 marginal kernel reads `work_f32`, whose tiles hold
+       32 / (lanes_per_pattern * nodes_per_warp) patterns, when that is below 32. */
     const int32_t* work;       /* [n_work][2]                                                      */
     int32_t n_work;
     int32_t warps_per_block;   /* 8 or >= 16 (wide CTAs) warps share the nodes of a level (0: 8)   */
     int32_t max_blocks;        /* grid size cap (0: one CTA per tile)                              */
-    int32_t lanes_per_pattern; /* 1, 2 or 4 lanes per pattern in the FP32 marginal kernel          */
+    int32_t lanes_per_pattern; /* lanes per pattern in the FP32 marginal kernel: 1 up to 5 states,
+                                  4 for 20-22 states                                               */
     const int32_t* work_f32;   /* [n_work_f32][2]                                                  */
     int32_t n_work_f32;
-    int32_t reserved;
+    int32_t smem_nodes;        /* max over trees of tt_tree.n_smem (sizes the dynamic shared memory:
+                                  smem_nodes * (32 / lanes_per_pattern) * width * 4 bytes)        */
     const int32_t* node_rec;   /* [n_nodes][4]: first child entry, end of child entries, parent
                                   local id (-1 at the root), tip row (-1 for internal nodes)      */
     const int32_t* child_pair; /* [n_nodes][4] for nodes with two children: (child 0, its tip row,
                                   child 1, its tip row); unused otherwise                          */
+    const int32_t* pair_slot;  /* [n_nodes] 2 * (global id of the parent) + (0 or 1) when the parent
+                                  has exactly two children, -1 otherwise (see tt_pmats.p32_pair)  */
+    int32_t nodes_per_warp;    /* FP32 marginal kernel: a warp works on 1, 2 or 4 nodes at once,
+                                  each with 32 / nodes_per_warp lanes; tiles of work_f32 hold
+                                  32 / (lanes_per_pattern * nodes_per_warp) patterns               */
+    int32_t reserved2;
 } tt_forest;
 
 typedef struct tt_model {
@@ -136,6 +146,10 @@ typedef struct tt_pmats {
     double* p64;               /* [n_nodes][q][width]  P(t) = max(0, V diag(exp(mu lam t)) V^-1)  */
     float*  p32;               /* [n_nodes][q][width]  FP32 copy (may be NULL)                     */
     double* logp64;            /* [n_nodes][q][width]  log(max(1e-12, P))  (may be NULL)           */
+    float*  p32_pair;          /* [n_nodes][2][q][width]: at an internal node with two children, the
+                                  FP32 matrices of its children side by side, so the FP32 marginal
+                                  kernel stages a level's matrices with one contiguous copy; needs
+                                  tt_forest.pair_slot (may be NULL)                                 */
 } tt_pmats;
 
 /* Outputs of the marginal pass.  Buffers hold float (TT_PREC_F32) or double (TT_PREC_F64). */

@@ -1,5 +1,5 @@
-"""GPU: every launch shape of the FP32 marginal kernel (lanes per pattern,
-warps per CTA) and the FP64 kernel give the oracle's results, on a tree with
+"""GPU: every launch shape of the FP32 marginal kernel (nodes per warp,
+warps per CTA, shared-memory top of the tree) and the FP64 kernel give the oracle's results, on a tree with
 polytomies, masks and missing data, for 4- and 5-state alphabets.  Also the
 multi-tree forest (one launch over several trees of different sizes and
 models) against per-tree oracle runs."""
@@ -37,15 +37,19 @@ def _oracle(t):
                         reconstruct_tip_states=True)
 
 
+@pytest.mark.parametrize("smem", [None, 0, 2048])
 @pytest.mark.parametrize("alphabet", ["nuc_nogap", "nuc"])
 @pytest.mark.parametrize("shape", [(1, 8), (1, 32), (2, 8), (2, 16), (4, 8), (4, 16), ("f64", 8), ("f64", 32)])
-def test_marginal_launch_shapes(alphabet, shape):
+def test_marginal_launch_shapes(alphabet, shape, smem):
+    """smem: None = whole tree in shared memory (small trees), 0 = none, 2048 = the top few nodes."""
     from treetime_gb300 import TreeAnc
     lpp, warps = shape
+    if lpp == "f64" and smem is not None:
+        pytest.skip("shared-memory top rows are an FP32-kernel feature")
     wl = _workload(alphabet, seed=7)
     prec = "f64" if lpp == "f64" else "f32"
     t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision=prec,
-                lanes_per_pattern=None if lpp == "f64" else lpp, warps_per_block=warps)
+                nodes_per_warp=None if lpp == "f64" else lpp, warps_per_block=warps, smem_bytes=smem)
     rng = np.random.default_rng(1)
     for n in list(t.tree.find_clades())[3:9]:
         n.mask = (rng.random(t.data.compressed_length) < 0.6).astype(float)

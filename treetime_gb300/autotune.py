@@ -1,0 +1,93 @@
+"""Autotuner for the FP32 marginal kernel's launch shape.
+
+The best shape depends on the workload: few patterns per tree want a warp to
+work on several nodes at once (narrower tiles, more CTAs); batches of many
+trees want one node per warp.  ``tune`` times every candidate
+(nodes per warp x warps per CTA x shared-memory budget for the top of the
+tree) on the actual forest with CUDA events and returns the fastest; results
+are cached in memory and in a JSON file keyed by a coarse workload signature
+(alphabet size, number of trees, node and pattern counts rounded to powers of
+two).
+"""
+
+import json
+import math
+import os
+import statistics
+
+from . import engine
+
+CANDIDATES = [(npw, nw, smem) for npw in (1, 2, 4) for nw in (8, 16) for smem in (0, 48 * 1024, 96 * 1024, 160 * 1024)]
+_CACHE = {}
+CACHE_PATH = os.environ.get("TREETIME_GB300_TUNE_CACHE",
+                            os.path.join(os.path.expanduser("~"), ".cache", "treetime_gb300", "autotune.json"))
+
+
+def signature(inputs, q):
+    nodes = sum(ti.layout.n_nodes for ti in inputs)
+    pats = sum(ti.n_patterns for ti in inputs)
+    b = lambda x: int(round(math.log2(max(1, x))))
+    return "q%d_t%d_n%d_p%d" % (q, b(len(inputs)), b(nodes), b(pats))
+
+
+def _load_file():
+    try:
+        with open(CACHE_PATH) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def _save_file(d):
+    try:
+        os.makedirs(os.path.dirname(CACHE_PATH), exist_ok=True)
+        with open(CACHE_PATH, "w") as fh:
+            json.dump(d, fh, indent=1, sort_keys=True)
+    except Exception:
+        pass
+
+
+def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True):
+    """Fastest (nodes_per_warp, warps_per_block, smem_bytes) for this forest
+    and the table of median times (ms) of all candidates."""
+    key = signature(inputs, q)
+    if use_cache:
+        if key in _CACHE:
+            return _CACHE[key]
+        disk = _load_file()
+        if key in disk:
+            _CACHE[key] = (tuple(disk[key]["best"]), disk[key]["table"])
+            return _CACHE[key]
+    t = engine.torch()
+    cands = candidates or CANDIDATES
+    if q >= 20:
+        cands = [c for c in cands if c[0] == 1]
+    elif q == 5:
+        cands = [c for c in cands if c[0] <= 2]
+    table = {}
+    for npw, nw, smem in cands:
+        try:
+            f = engine.Forest(inputs, q, device=device, nodes_per_warp=npw, warps_per_block=nw, smem_bytes=smem)
+            bufs = engine.Buffers(f)
+            for _ in range(2):
+                engine.marginal(f, model, bufs, precision="f32", sync=False)
+            t.cuda.synchronize()
+            times = []
+            for _ in range(reps):
+                a, b = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+                a.record()
+                engine.marginal(f, model, bufs, precision="f32", sync=False)
+                b.record()
+                b.synchronize()
+                times.append(a.elapsed_time(b))
+            table["%d/%d/%d" % (npw, nw, smem)] = statistics.median(times)
+        except Exception as e:  # a shape that cannot launch (e.g. too much shared memory) is skipped
+            table["%d/%d/%d" % (npw, nw, smem)] = None
+    ok = {k: v for k, v in table.items() if v is not None}
+    best = tuple(int(x) for x in min(ok, key=ok.get).split("/"))
+    _CACHE[key] = (best, table)
+    if use_cache:
+        disk = _load_file()
+        disk[key] = {"best": list(best), "table": table}
+        _save_file(disk)
+    return best, table

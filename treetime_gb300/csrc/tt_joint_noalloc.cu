@@ -79,7 +79,7 @@ extern "C" tt_status tt_joint_noalloc(const tt_forest* f, const tt_model* m, int
     tt_status st = scratch_address(&base);
     if (st != TT_OK) return st;
     unsigned char* b = static_cast<unsigned char*>(base);
-    tt_pmats pm;
+    tt_pmats pm = {};
     pm.p64 = reinterpret_cast<double*>(b);
     pm.p32 = nullptr;
     pm.logp64 = reinterpret_cast<double*>(b + pmat_bytes);

@@ -55,23 +55,24 @@ extern "C" tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt
     const int warps = f->warps_per_block ? f->warps_per_block : 8;
     tt_status st;
     if (precision == TT_PREC_F32) {
-        if (!pm->p32 || !f->node_rec || !f->child_pair) {
-            set_error("tt_marginal: FP32 needs p32, node_rec and child_pair");
+        if (!pm->p32 || !pm->p32_pair || !f->node_rec || !f->child_pair || !f->pair_slot) {
+            set_error("tt_marginal: FP32 needs p32, p32_pair, node_rec, child_pair and pair_slot");
             return TT_ERR_INVALID;
         }
         prm.pmat = pm->p32;
         int lpp = f->lanes_per_pattern > 0 ? f->lanes_per_pattern : 1;
-        if (lpp > 1) {
+        int npw = f->nodes_per_warp > 0 ? f->nodes_per_warp : 1;
+        if (lpp * npw > 1) {
             if (!f->work_f32 || f->n_work_f32 <= 0) {
-                set_error("tt_marginal: lanes_per_pattern > 1 needs work_f32");
+                set_error("tt_marginal: lanes_per_pattern or nodes_per_warp > 1 needs work_f32");
                 return TT_ERR_INVALID;
             }
             prm.items = reinterpret_cast<const WorkItem*>(f->work_f32);
             prm.n_items = f->n_work_f32;
             blocks = f->max_blocks > 0 && f->max_blocks < f->n_work_f32 ? f->max_blocks : f->n_work_f32;
         }
-        st = launch_marginal_f32(f->n_states, warps, lpp, prm, reinterpret_cast<const int4*>(f->node_rec),
-                                 reinterpret_cast<const int4*>(f->child_pair), blocks, s);
+        st = launch_marginal_f32(f->n_states, warps, lpp, npw, prm, reinterpret_cast<const int4*>(f->node_rec),
+                                 reinterpret_cast<const int4*>(f->child_pair), pm->p32_pair, blocks, s);
     } else if (precision == TT_PREC_F64) {
         prm.pmat = pm->p64;
         st = launch_marginal_f64(f->n_states, warps, prm, blocks, s);

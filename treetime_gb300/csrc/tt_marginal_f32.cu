@@ -5,12 +5,22 @@
 //   - arithmetic is FP32 in the linear domain: child messages x.P are multiplied, each node's
 //     partial is rescaled by an exact power of two and the exponents are summed per pattern in
 //     registers; the only FP64 operation is the root's log, once per pattern;
-//   - LPP lanes cooperate on one pattern (each holds S = W / LPP consecutive states), so a warp
-//     covers 32 / LPP patterns and a tree with few patterns still yields many CTAs; the matrix-
-//     vector products gather the other lanes' states with width-LPP shuffles;
+//   - a warp works on NPW nodes of a level at once (one lane per pattern, 32 / NPW patterns per
+//     tile), so a tree with few patterns still yields many CTAs without extra instructions per
+//     node-pattern; for 20+ states LPP lanes cooperate on one pattern (each holds S = W / LPP
+//     consecutive states) and the matrix-vector products gather them with width-LPP shuffles;
 //   - the tips' character -> profile table is kept in shared memory as FP32;
-//   - node records of a level are staged in shared memory in chunks, so a node costs one
-//     round trip to global memory (its children's rows) instead of three.
+//   - node records and branch matrices of a level are staged in shared memory in chunks with
+//     double-buffered cp.async copies (the next chunk is in flight while the current one is
+//     computed), the children's matrices of a two-child node lying side by side in p32_pair so
+//     that a chunk is one contiguous copy; a node then costs one round trip to global memory
+//     (its children's rows), and each warp issues those loads for D nodes before computing any
+//     of them;
+//   - the top n_smem internal nodes of the tree (its narrow upper levels, where a level has too
+//     few nodes to hide memory latency) keep their partial / posterior rows in shared memory for
+//     the whole pass: those levels run at shared-memory latency.  Their rows are still written
+//     to the global output buffers.  When the whole tree fits, the pass never reads global
+//     memory for profiles.
 #include "tt_marginal_kernels.cuh"
 
 namespace tt {
@@ -152,26 +162,107 @@ __device__ __forceinline__ int group_argmax(const float (&x)[W / LPP], int j0) {
     return bi;
 }
 
+
+// ---------------------------------------------------------------- async staging
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// msg[s] = sum_i x_i P[i][j0+s] with P in shared memory
+template <int Q, int W, int LPP>
+__device__ __forceinline__ void s_vec_mat(const float (&x)[W / LPP], const float* P, int j0, float (&msg)[W / LPP]) {
+    constexpr int S = W / LPP;
+#pragma unroll
+    for (int s = 0; s < S; ++s) msg[s] = 0.f;
+#pragma unroll
+    for (int r = 0; r < LPP; ++r) {
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+            const int i = r * S + s2;
+            if (i >= Q) continue;
+            const float xi = LPP == 1 ? x[s2] : __shfl_sync(0xffffffffu, x[s2], r, LPP);
+            float row[S];
+            ld_part<S>(P + i * W + j0, row);
+#pragma unroll
+            for (int s = 0; s < S; ++s) msg[s] = fmaf(xi, row[s], msg[s]);
+        }
+    }
+}
+
+// ev[s] = sum_j P[j0+s][j] o_j with P in shared memory
+template <int Q, int W, int LPP>
+__device__ __forceinline__ void s_mat_vec(const float* P, const float (&o)[W / LPP], int j0, float (&ev)[W / LPP]) {
+    constexpr int S = W / LPP;
+    float full[W];
+#pragma unroll
+    for (int r = 0; r < LPP; ++r) {
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) full[r * S + s2] = LPP == 1 ? o[s2] : __shfl_sync(0xffffffffu, o[s2], r, LPP);
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int i = j0 + s;
+        float acc = 0.f;
+        if (i < Q) {
+            float row[W];
+            ld_part<W>(P + i * W, row);
+#pragma unroll
+            for (int j = 0; j < Q; ++j) acc = fmaf(full[j], row[j], acc);
+        }
+        ev[s] = acc;
+    }
+}
+
 struct F32Params {
     MargParams m;
     const int4* node_rec;    // [n_nodes] (child begin, child end, parent, tip row)
     const int4* child_pair;  // [n_nodes] binary nodes: (c0, c0 tip row, c1, c1 tip row)
+    const float* p32_pair;   // [n_nodes][2][Q][W] children's matrices of binary nodes
 };
 
-template <int Q, int W, int LPP, int NW>
-__global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel(F32Params fp) {
+// Chunk of a level staged in shared memory: records, child pairs and matrices (post-order: the
+// two children's matrices; pre-order: the node's own matrix in the first half).
+template <int Q, int W>
+struct StageCfg {
+    static constexpr int kMatFloats = 2 * Q * W;
+    static constexpr int kBytesPerNode = 32 + kMatFloats * 4;
+    static constexpr int kFit = 20 * 1024 / kBytesPerNode;  // nodes per ~20 KB buffer
+    static constexpr int kChunk = kFit >= 128 ? 128 : (kFit >= 64 ? 64 : (kFit >= 32 ? 32 : (kFit >= 16 ? 16 :
+                                  (kFit >= 8 ? 8 : 4))));
+};
+
+template <int Q, int W>
+struct __align__(16) Stage {
+    int4 rec[StageCfg<Q, W>::kChunk];
+    int4 pair[StageCfg<Q, W>::kChunk];
+    float mat[StageCfg<Q, W>::kChunk][StageCfg<Q, W>::kMatFloats];
+};
+
+template <int Q, int W, int LPP, int NPW, int NW, int D>
+__global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) {
     constexpr int S = W / LPP;
-    constexpr int TP = 32 / LPP;
+    constexpr int GL = 32 / NPW;      // lanes per node group: a warp works on NPW nodes at once
+    constexpr int TP = GL / LPP;      // patterns per tile
+    constexpr int STRIDE = NW * NPW;  // nodes covered by the CTA per step
+    constexpr int CH = StageCfg<Q, W>::kChunk;
+    constexpr int QW = Q * W;
     const MargParams& a = fp.m;
     __shared__ __align__(16) float lut_s[256 * W];
-    __shared__ int4 rec_s[kChunk];
-    __shared__ int4 pair_s[kChunk];
     __shared__ int red[NW][32];
     __shared__ float red_corr[NW][32];
     __shared__ unsigned diff_red[NW];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pl = lane / LPP, part = lane % LPP, j0 = part * S;
-    for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) {
+    // dynamic shared memory: two stage buffers, then the top-of-tree rows [n_smem][TP][W]
+    extern __shared__ __align__(16) unsigned char dyn_s[];
+    Stage<Q, W>* stg = reinterpret_cast<Stage<Q, W>*>(dyn_s);
+    float* top_s = reinterpret_cast<float*>(dyn_s + 2 * sizeof(Stage<Q, W>));
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int sub = lane / GL, pl = (lane % GL) / LPP, part = lane % LPP, j0 = part * S;
+    for (int i = tid; i < 256 * W; i += blockDim.x) {
         const int c = i / W, j = i % W;
         lut_s[i] = j < Q ? (float)__ldg(a.lut + c * Q + j) : 0.f;
     }
@@ -194,111 +285,177 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
         // child's sum-normalised partial and adds its prefactor unmasked; with power-of-two scaled
         // partials that leaves (1 - m) * log(sum of the scaled partial) to add
         float lcorr = 0.f;
+        const int top = tr.n_int - tr.n_smem;  // local ids >= top live in shared memory
 
         auto row_of = [&](int k) -> int64_t { return (tr.prof_base + (int64_t)k * P + pc) * W + j0; };
-        auto tip_part = [&](int trow, float (&x)[S]) {
-            const int code = trow < 0 ? 0 : (int)__ldg(a.f.tip_codes + tr.tip_base + (int64_t)trow * P + pc);
+        auto top_row = [&](int k) -> float* { return top_s + ((int64_t)(k - top) * TP + pl) * W + j0; };
+        auto prow = [&](int k) -> float* { return k >= top ? top_row(k) : partial + row_of(k); };
+        auto qrow = [&](int k) -> float* { return k >= top ? top_row(k) : posterior + row_of(k); };
+        auto tip_code = [&](int trow) -> int {
+            return trow < 0 ? 0 : (int)__ldg(a.f.tip_codes + tr.tip_base + (int64_t)trow * P + pc);
+        };
+        auto lut_part = [&](int code, float (&x)[S]) {
 #pragma unroll
             for (int s = 0; s < S; ++s) x[s] = lut_s[code * W + j0 + s];
         };
-        auto child_msg = [&](int c, int trow, float (&msg)[S]) {
-            float x[S];
-            if (c >= tr.n_int) tip_part(trow, x);
-            else ld_part<S>(partial + row_of(c), x);
-            f_vec_mat<Q, W, LPP>(x, pm + (nb + c) * (Q * W), j0, msg);
-            if (has_masks) {
-                const int64_t mo = __ldg(a.f.mask_off + nb + c);
-                if (mo >= 0) {
-                    const float m = (float)__ldg(a.f.masks + mo + pc);
-                    // padding states (j >= Q) stay 0 so that products over children keep them 0
+        // mask of the branch above node c applied to its message; correction for internal c
+        auto apply_mask = [&](int c, const float (&x)[S], float (&msg)[S]) {
+            const int64_t mo = __ldg(a.f.mask_off + nb + c);
+            if (mo < 0) return;
+            const float m = (float)__ldg(a.f.masks + mo + pc);
+            // padding states (j >= Q) stay 0 so that products over children keep them 0
 #pragma unroll
-                    for (int s = 0; s < S; ++s)
-                        if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : (m == 1.f ? msg[s] : exp2f(m * log2f(msg[s])));
-                    if (c < tr.n_int) {
-                        float xs = 0.f;
+            for (int s = 0; s < S; ++s)
+                if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : (m == 1.f ? msg[s] : exp2f(m * log2f(msg[s])));
+            if (c < tr.n_int) {
+                float xs = 0.f;
 #pragma unroll
-                        for (int s = 0; s < S; ++s) xs += x[s];
-                        xs = group_sum<LPP>(xs);
-                        if (m != 1.f) lcorr += (1.f - m) * logf(xs);
-                    }
-                }
+                for (int s = 0; s < S; ++s) xs += x[s];
+                xs = group_sum<LPP>(xs);
+                if (m != 1.f) lcorr += (1.f - m) * logf(xs);
             }
         };
+        // stage the chunk [base, base + cnt) of a level into buffer b
+        auto stage = [&](int b, int base, int cnt, bool post) {
+            Stage<Q, W>& S_ = stg[b];
+            for (int i = tid; i < cnt; i += blockDim.x) {
+                cp_async16(&S_.rec[i], fp.node_rec + nb + base + i);
+                if (post) cp_async16(&S_.pair[i], fp.child_pair + nb + base + i);
+            }
+            const int per = post ? 2 * QW : QW;                  // floats per node
+            const float* src = post ? fp.p32_pair + (nb + base) * (2 * QW) : pm + (nb + base) * QW;
+            const int units = cnt * per / 4;
+            for (int u = tid; u < units; u += blockDim.x) {
+                const int node = (u * 4) / per, off = (u * 4) % per;
+                cp_async16(&S_.mat[node][off], src + (int64_t)u * 4);
+            }
+            cp_async_commit();
+        };
 
-        // ---------------- post-order
-        for (int h = 0; h < tr.n_levels; ++h) {
-            const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
-            for (int base = lo; base < hi; base += kChunk) {
-                const int cnt = min(kChunk, hi - base);
-                __syncthreads();
-                for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-                    rec_s[i] = __ldg(fp.node_rec + nb + base + i);
-                    pair_s[i] = __ldg(fp.child_pair + nb + base + i);
+        // ------------------------------------------------------------ post-order
+        {
+            int h = 0, base = tr.n_levels > 0 ? __ldg(lev) : 0, b = 0;
+            bool have = tr.n_levels > 0;
+            if (have) stage(0, base, min(CH, __ldg(lev + 1) - base), true);
+            while (have) {
+                const int hi = __ldg(lev + h + 1);
+                const int cnt = min(CH, hi - base);
+                int nh = h, nbase = base + CH;
+                if (nbase >= hi) { nh = h + 1; nbase = nh < tr.n_levels ? __ldg(lev + nh) : 0; }
+                const bool has_next = nh < tr.n_levels;
+                __syncthreads();  // buffer b^1 is free (its chunk was computed)
+                if (has_next) {
+                    stage(b ^ 1, nbase, min(CH, __ldg(lev + nh + 1) - nbase), true);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
                 }
-                __syncthreads();
-                for (int i = warp; i < cnt; i += NW) {
-                    const int k = base + i;
-                    const int4 rec = rec_s[i];
-                    float r[S];
+                __syncthreads();  // chunk b staged; the previous level's rows are written
+                const Stage<Q, W>& st = stg[b];
+                for (int i0 = warp * NPW + sub; i0 - sub < cnt; i0 += STRIDE * D) {
+                    // loads of D nodes first
+                    float xa[D][S], xb[D][S];
+                    int ca[D], cb[D];
+                    bool bin[D];
 #pragma unroll
-                    for (int s = 0; s < S; ++s) r[s] = (j0 + s < Q) ? 1.f : 0.f;
-                    int extra = 0;
-                    const int nch = rec.y - rec.x;
-                    if (nch == 2) {
-                        const int4 cp = pair_s[i];
-                        float m0[S], m1[S];
-                        child_msg(cp.x, cp.y, m0);
-                        child_msg(cp.z, cp.w, m1);
-#pragma unroll
-                        for (int s = 0; s < S; ++s) r[s] = m0[s] * m1[s];
-                    } else {
-                        for (int ci = rec.x; ci < rec.y; ++ci) {
-                            const int c = __ldg(a.f.child_idx + ci);
-                            const int trow = c >= tr.n_int ? __ldg(a.f.tip_row + nb + c) : -1;
-                            float m0[S];
-                            child_msg(c, trow, m0);
-#pragma unroll
-                            for (int s = 0; s < S; ++s) r[s] *= m0[s];
-                            float mx = r[0];
-#pragma unroll
-                            for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
-                            mx = group_max<LPP>(mx);
-                            if (mx < 0x1p-64f) {  // many children: keep the running product in range
-                                const int e = pow2_exponent(mx);
-                                scale_pow2<S>(r, e);
-                                extra += e;
+                    for (int d = 0; d < D; ++d) {
+                        const int i = i0 + d * STRIDE;
+                        bin[d] = false;
+                        if (i < cnt) {
+                            const int4 rec = st.rec[i];
+                            if (rec.y - rec.x == 2) {
+                                bin[d] = true;
+                                const int4 cp = st.pair[i];
+                                ca[d] = cp.x >= tr.n_int ? tip_code(cp.y) : -1;
+                                cb[d] = cp.z >= tr.n_int ? tip_code(cp.w) : -1;
+                                if (cp.x < tr.n_int) ld_part<S>(prow(cp.x), xa[d]);
+                                if (cp.z < tr.n_int) ld_part<S>(prow(cp.z), xb[d]);
                             }
                         }
                     }
-                    float mx = r[0];
 #pragma unroll
-                    for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
-                    mx = group_max<LPP>(mx);
-                    const int e = pow2_exponent(mx);
-                    scale_pow2<S>(r, e);
-                    esum += e + extra;
-                    if (valid) st_part<S>(partial + row_of(k), r);
+                    for (int d = 0; d < D; ++d) {
+                        const int i = i0 + d * STRIDE;
+                        if (i >= cnt) continue;
+                        const int k = base + i;
+                        float r[S];
+                        int extra = 0;
+                        if (bin[d]) {
+                            const int4 cp = st.pair[i];
+                            if (ca[d] >= 0) lut_part(ca[d], xa[d]);
+                            if (cb[d] >= 0) lut_part(cb[d], xb[d]);
+                            float m0[S], m1[S];
+                            s_vec_mat<Q, W, LPP>(xa[d], &st.mat[i][0], j0, m0);
+                            s_vec_mat<Q, W, LPP>(xb[d], &st.mat[i][QW], j0, m1);
+                            if (has_masks) {
+                                apply_mask(cp.x, xa[d], m0);
+                                apply_mask(cp.z, xb[d], m1);
+                            }
+#pragma unroll
+                            for (int s = 0; s < S; ++s) r[s] = m0[s] * m1[s];
+                        } else {
+                            // more (or fewer) than two children: matrices from global memory
+                            const int4 rec = st.rec[i];
+#pragma unroll
+                            for (int s = 0; s < S; ++s) r[s] = (j0 + s < Q) ? 1.f : 0.f;
+                            for (int ci = rec.x; ci < rec.y; ++ci) {
+                                const int c = __ldg(a.f.child_idx + ci);
+                                float x[S], m0[S];
+                                if (c >= tr.n_int) lut_part(tip_code(__ldg(a.f.tip_row + nb + c)), x);
+                                else ld_part<S>(prow(c), x);
+                                f_vec_mat<Q, W, LPP>(x, pm + (nb + c) * QW, j0, m0);
+                                if (has_masks) apply_mask(c, x, m0);
+#pragma unroll
+                                for (int s = 0; s < S; ++s) r[s] *= m0[s];
+                                float mx = r[0];
+#pragma unroll
+                                for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
+                                mx = group_max<LPP>(mx);
+                                if (mx < 0x1p-64f) {  // many children: keep the running product in range
+                                    const int e = pow2_exponent(mx);
+                                    scale_pow2<S>(r, e);
+                                    extra += e;
+                                }
+                            }
+                        }
+                        float mx = r[0];
+#pragma unroll
+                        for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
+                        mx = group_max<LPP>(mx);
+                        const int e = pow2_exponent(mx);
+                        scale_pow2<S>(r, e);
+                        esum += e + extra;
+                        if (k >= top) st_part<S>(top_row(k), r);
+                        if (valid) st_part<S>(partial + row_of(k), r);
+                    }
                 }
+                h = nh;
+                base = nbase;
+                b ^= 1;
+                have = has_next;
             }
-            __syncthreads();
         }
         // per-pattern exponent sums: lanes of one pattern hold identical values; warps add up
         red[warp][lane] = esum;
         red_corr[warp][lane] = lcorr;
         __syncthreads();
 
-        // ---------------- root
+        // ------------------------------------------------------------------ root
         if (warp == 0) {
             int tot = 0;
             double corr = 0.0;
+            const int gl = lane % GL;  // same pattern and state slice in every node group
             for (int w = 0; w < NW; ++w) {
-                tot += red[w][lane];
-                corr += (double)red_corr[w][lane];
+#pragma unroll
+                for (int g2 = 0; g2 < NPW; ++g2) {
+                    tot += red[w][g2 * GL + gl];
+                    corr += (double)red_corr[w][g2 * GL + gl];
+                }
             }
             const int kr = tr.n_int - 1;
             const double* pi = a.pi + (int64_t)tr.model * Q;
             float x[S], pr[S];
-            ld_part<S>(partial + row_of(kr), x);
+            ld_part<S>(prow(kr), x);
             float s_loc = 0.f;
 #pragma unroll
             for (int s = 0; s < S; ++s) {
@@ -320,7 +477,8 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
             } else {
                 st = group_argmax<Q, W, LPP>(pr, j0);
             }
-            if (valid) {
+            if (kr >= top && sub == 0) st_part<S>(top_row(kr), pr);
+            if (valid && sub == 0) {
                 st_part<S>(posterior + row_of(kr), pr);
                 if (part == 0) {
                     a.o.site_lh[tr.pat_base + p] = log((double)ssum) + kLn2 * (double)tot + corr;
@@ -334,92 +492,122 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
                 }
             }
         }
-        __syncthreads();
 
-        // ---------------- pre-order
+        // ------------------------------------------------------------- pre-order
         unsigned ndiff = 0;
         const bool do_tips = a.o.reconstruct_tips || a.o.tip_outgroup;
-        for (int h = tr.n_levels - 2; h >= (do_tips ? -1 : 0); --h) {
-            const bool tips = h < 0;
-            const int lo = tips ? tr.n_int : __ldg(lev + h);
-            const int hi = tips ? tr.n_int + tr.n_tip : __ldg(lev + h + 1);
-            for (int base = lo; base < hi; base += kChunk) {
-                const int cnt = min(kChunk, hi - base);
+        const int h_last = do_tips ? -1 : 0;
+        {
+            // levels n_levels-2 .. 0, then the tips as level -1
+            auto lv_lo = [&](int h) { return h >= 0 ? __ldg(lev + h) : tr.n_int; };
+            auto lv_hi = [&](int h) { return h >= 0 ? __ldg(lev + h + 1) : tr.n_int + tr.n_tip; };
+            int h = tr.n_levels - 2, b = 0;
+            bool have = h >= h_last;
+            int base = have ? lv_lo(h) : 0;
+            __syncthreads();  // root row written; stage buffers free
+            if (have) stage(0, base, min(CH, lv_hi(h) - base), false);
+            while (have) {
+                const int hi = lv_hi(h);
+                const int cnt = min(CH, hi - base);
+                const bool tips = h < 0;
+                int nh = h, nbase = base + CH;
+                if (nbase >= hi) { nh = h - 1; nbase = nh >= h_last ? lv_lo(nh) : 0; }
+                const bool has_next = nh >= h_last;
                 __syncthreads();
-                for (int i = threadIdx.x; i < cnt; i += blockDim.x) rec_s[i] = __ldg(fp.node_rec + nb + base + i);
+                if (has_next) {
+                    stage(b ^ 1, nbase, min(CH, lv_hi(nh) - nbase), false);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
                 __syncthreads();
-                for (int i = warp; i < cnt; i += NW) {
-                    const int k = base + i;
-                    const int4 rec = rec_s[i];
-                    const int64_t g = nb + k;
-                    float pv[S], x[S], msg[S], o[S];
-                    ld_part<S>(posterior + row_of(rec.z), pv);
-                    if (tips) tip_part(rec.w, x);
-                    else ld_part<S>(partial + row_of(k), x);
-                    const float* Pk = pm + g * (Q * W);
-                    f_vec_mat<Q, W, LPP>(x, Pk, j0, msg);
-                    float m = 1.f;
-                    if (has_masks) {
-                        const int64_t mo = __ldg(a.f.mask_off + g);
-                        if (mo >= 0) m = (float)__ldg(a.f.masks + mo + pc);
-                    }
-                    if (m != 1.f) {
+                const Stage<Q, W>& st = stg[b];
+                for (int i0 = warp * NPW + sub; i0 - sub < cnt; i0 += STRIDE * D) {
+                    float pv[D][S], x[D][S];
+                    int code[D];
 #pragma unroll
-                        for (int s = 0; s < S; ++s)
-                            if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
-                    }
-                    float sl = 0.f;
-#pragma unroll
-                    for (int s = 0; s < S; ++s) {
-                        o[s] = (j0 + s < Q) ? fmaxf(1e-12f, pv[s]) / msg[s] : 0.f;
-                        sl += o[s];
-                    }
-                    const float inv = 1.f / group_sum<LPP>(sl);
-#pragma unroll
-                    for (int s = 0; s < S; ++s) o[s] *= inv;
-                    if (valid) {
-                        float* og = reinterpret_cast<float*>(tips ? a.o.tip_outgroup : a.o.outgroup);
-                        if (og) {
-                            const int64_t row = tips ? (tr.tipprof_base + (int64_t)(k - tr.n_int) * P + pc) * W + j0
-                                                     : row_of(k);
-                            st_part<S>(og + row, o);
+                    for (int d = 0; d < D; ++d) {
+                        const int i = i0 + d * STRIDE;
+                        if (i < cnt) {
+                            const int4 rec = st.rec[i];
+                            ld_part<S>(qrow(rec.z), pv[d]);
+                            if (tips) code[d] = tip_code(rec.w);
+                            else ld_part<S>(prow(base + i), x[d]);
                         }
                     }
-                    if (tips && !a.o.reconstruct_tips) continue;
-                    float ev[S];
-                    f_mat_vec<Q, W, LPP>(Pk, o, j0, ev);
-                    float s2 = 0.f;
 #pragma unroll
-                    for (int s = 0; s < S; ++s) {
-                        if (m != 1.f && j0 + s < Q) ev[s] = m * ev[s] + (1.f - m);
-                        x[s] *= ev[s];
-                        s2 += x[s];
-                    }
-                    const float inv2 = 1.f / group_sum<LPP>(s2);
+                    for (int d = 0; d < D; ++d) {
+                        const int i = i0 + d * STRIDE;
+                        if (i >= cnt) continue;
+                        const int k = base + i;
+                        const int64_t g = nb + k;
+                        if (tips) lut_part(code[d], x[d]);
+                        const float* Pk = &st.mat[i][0];
+                        float msg[S], o[S];
+                        s_vec_mat<Q, W, LPP>(x[d], Pk, j0, msg);
+                        float m = 1.f;
+                        if (has_masks) {
+                            const int64_t mo = __ldg(a.f.mask_off + g);
+                            if (mo >= 0) m = (float)__ldg(a.f.masks + mo + pc);
+                        }
+                        if (m != 1.f) {
 #pragma unroll
-                    for (int s = 0; s < S; ++s) x[s] *= inv2;
-                    const int st = group_argmax<Q, W, LPP>(x, j0);
-                    if (valid) {
-                        float* dst = tips ? reinterpret_cast<float*>(a.o.tip_posterior) : posterior;
+                            for (int s = 0; s < S; ++s)
+                                if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
+                        }
+                        float sl = 0.f;
+#pragma unroll
+                        for (int s = 0; s < S; ++s) {
+                            o[s] = (j0 + s < Q) ? fmaxf(1e-12f, pv[d][s]) / msg[s] : 0.f;
+                            sl += o[s];
+                        }
+                        const float inv = 1.f / group_sum<LPP>(sl);
+#pragma unroll
+                        for (int s = 0; s < S; ++s) o[s] *= inv;
                         const int64_t row = tips ? (tr.tipprof_base + (int64_t)(k - tr.n_int) * P + pc) * W + j0
                                                  : row_of(k);
-                        if (dst) st_part<S>(dst + row, x);
-                        if (part == 0) {
-                            uint8_t* sp = a.o.states + tr.state_base + (int64_t)k * P + pc;
-                            if (a.o.count_diff) ndiff += (*sp != (uint8_t)st);
-                            *sp = (uint8_t)st;
+                        if (valid) {
+                            float* og = reinterpret_cast<float*>(tips ? a.o.tip_outgroup : a.o.outgroup);
+                            if (og) st_part<S>(og + row, o);
+                        }
+                        if (tips && !a.o.reconstruct_tips) continue;
+                        float ev[S];
+                        s_mat_vec<Q, W, LPP>(Pk, o, j0, ev);
+                        float s2 = 0.f;
+#pragma unroll
+                        for (int s = 0; s < S; ++s) {
+                            if (m != 1.f && j0 + s < Q) ev[s] = m * ev[s] + (1.f - m);
+                            x[d][s] *= ev[s];
+                            s2 += x[d][s];
+                        }
+                        const float inv2 = 1.f / group_sum<LPP>(s2);
+#pragma unroll
+                        for (int s = 0; s < S; ++s) x[d][s] *= inv2;
+                        const int stt = group_argmax<Q, W, LPP>(x[d], j0);
+                        if (!tips && k >= top) st_part<S>(top_row(k), x[d]);  // partial slot -> posterior
+                        if (valid) {
+                            float* dst = tips ? reinterpret_cast<float*>(a.o.tip_posterior) : posterior;
+                            if (dst) st_part<S>(dst + row, x[d]);
+                            if (part == 0) {
+                                uint8_t* sp = a.o.states + tr.state_base + (int64_t)k * P + pc;
+                                if (a.o.count_diff) ndiff += (*sp != (uint8_t)stt);
+                                *sp = (uint8_t)stt;
+                            }
                         }
                     }
                 }
+                h = nh;
+                base = nbase;
+                b ^= 1;
+                have = has_next;
             }
-            __syncthreads();
         }
         if (a.o.n_diff && a.o.count_diff) {
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) ndiff += __shfl_xor_sync(0xffffffffu, ndiff, off);
             if (lane == 0) diff_red[warp] = ndiff;
             __syncthreads();
-            if (threadIdx.x == 0) {
+            if (tid == 0) {
                 unsigned long long t = 0;
                 for (int w = 0; w < NW; ++w) t += diff_red[w];
                 if (t) atomicAdd(a.o.n_diff + wi.tree, t);
@@ -429,29 +617,41 @@ __global__ void __launch_bounds__(NW * 32, NW >= 32 ? 1 : 2) marginal_f32_kernel
     }
 }
 
-template <int Q, int LPP, int NW>
+template <int Q, int LPP, int NPW, int NW, int D>
 static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
     constexpr int W = round4(Q);
     static_assert(W % LPP == 0, "width must split over the lanes of a pattern");
-    marginal_f32_kernel<Q, W, LPP, NW><<<blocks, NW * 32, 0, s>>>(prm);
+    const size_t dyn = 2 * sizeof(Stage<Q, W>) + (size_t)prm.m.f.smem_nodes * (32 / (LPP * NPW)) * W * sizeof(float);
+    // static + dynamic shared memory passes 48 KB: opt in to the larger carve-out
+    static size_t configured = 0;
+    if (dyn > configured) {
+        cudaError_t e = cudaFuncSetAttribute(marginal_f32_kernel<Q, W, LPP, NPW, NW, D>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) {
+            set_error("tt_marginal(f32): %zu bytes of shared memory: %s", dyn, cudaGetErrorString(e));
+            return TT_ERR_INVALID;
+        }
+        configured = dyn;
+    }
+    marginal_f32_kernel<Q, W, LPP, NPW, NW, D><<<blocks, NW * 32, dyn, s>>>(prm);
     return check_launch("tt_marginal(f32)");
 }
 
-tt_status launch_marginal_f32(int q, int warps, int lpp, const MargParams& prm, const int4* node_rec,
-                              const int4* child_pair, int blocks, cudaStream_t s) {
-    F32Params fp{prm, node_rec, child_pair};
+tt_status launch_marginal_f32(int q, int warps, int lpp, int npw, const MargParams& prm, const int4* node_rec,
+                              const int4* child_pair, const float* p32_pair, int blocks, cudaStream_t s) {
+    F32Params fp{prm, node_rec, child_pair, p32_pair};
     const bool wide = warps >= 16;
     switch (q) {
         case 4:
-            if (lpp == 4) return wide ? launch_f32<4, 4, 16>(fp, blocks, s) : launch_f32<4, 4, 8>(fp, blocks, s);
-            if (lpp == 2) return wide ? launch_f32<4, 2, 16>(fp, blocks, s) : launch_f32<4, 2, 8>(fp, blocks, s);
-            return wide ? launch_f32<4, 1, 32>(fp, blocks, s) : launch_f32<4, 1, 8>(fp, blocks, s);
+            if (npw >= 4) return wide ? launch_f32<4, 1, 4, 32, 2>(fp, blocks, s) : launch_f32<4, 1, 4, 16, 2>(fp, blocks, s);
+            if (npw == 2) return wide ? launch_f32<4, 1, 2, 32, 2>(fp, blocks, s) : launch_f32<4, 1, 2, 16, 2>(fp, blocks, s);
+            return wide ? launch_f32<4, 1, 1, 32, 2>(fp, blocks, s) : launch_f32<4, 1, 1, 16, 2>(fp, blocks, s);
         case 5:
-            if (lpp >= 2) return launch_f32<5, 2, 8>(fp, blocks, s);
-            return launch_f32<5, 1, 8>(fp, blocks, s);
-        case 20: return launch_f32<20, 4, 8>(fp, blocks, s);
-        case 21: return launch_f32<21, 4, 8>(fp, blocks, s);
-        case 22: return launch_f32<22, 4, 8>(fp, blocks, s);
+            if (npw >= 2) return launch_f32<5, 1, 2, 16, 2>(fp, blocks, s);
+            return launch_f32<5, 1, 1, 16, 2>(fp, blocks, s);
+        case 20: return launch_f32<20, 4, 1, 8, 1>(fp, blocks, s);
+        case 21: return launch_f32<21, 4, 1, 8, 1>(fp, blocks, s);
+        case 22: return launch_f32<22, 4, 1, 8, 1>(fp, blocks, s);
         default:
             set_error("tt_marginal: alphabet size %d not compiled (4, 5, 20, 21, 22)", q);
             return TT_ERR_UNSUPPORTED;

@@ -393,8 +393,8 @@ tt_status launch_marginal(const MargParams& prm, int blocks, cudaStream_t s) {
 }
 
 // Instantiated in tt_marginal_f32.cu / tt_marginal_f64.cu.
-tt_status launch_marginal_f32(int q, int warps, int lpp, const MargParams& prm, const int4* node_rec,
-                              const int4* child_pair, int blocks, cudaStream_t s);
+tt_status launch_marginal_f32(int q, int warps, int lpp, int npw, const MargParams& prm, const int4* node_rec,
+                              const int4* child_pair, const float* p32_pair, int blocks, cudaStream_t s);
 tt_status launch_marginal_f64(int q, int warps, const MargParams& prm, int blocks, cudaStream_t s);
 
 }  // namespace tt

@@ -44,6 +44,10 @@ __global__ void pmats_kernel(tt_forest f, tt_model m, tt_pmats out, int32_t* sta
         }
         out.p64[g * q * w + r] = p;
         if (out.p32) out.p32[g * q * w + r] = (float)p;
+        if (out.p32_pair && f.pair_slot) {
+            const int ps = f.pair_slot[g];
+            if (ps >= 0) out.p32_pair[(int64_t)ps * q * w + r] = (float)p;
+        }
         if (out.logp64) out.logp64[g * q * w + r] = j < q ? log(p > kTiny ? p : kTiny) : 0.0;
     }
 }

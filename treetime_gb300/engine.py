@@ -261,7 +261,8 @@ class Forest:
     """Device-resident schedule and inputs of a list of trees, plus the
     C-ABI struct that points at them."""
 
-    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, lanes_per_pattern=None):
+    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, nodes_per_warp=None,
+                 smem_bytes=None):
         dev = require_device(device)
         self.device = dev
         self.inputs = list(inputs)
@@ -271,13 +272,13 @@ class Forest:
                                              ("node_base", "level_base", "pat_base", "tip_base", "prof_base",
                                               "tipprof_base", "state_base")] +
                          [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model",
-                                                   "reserved")])
+                                                   "n_smem")])
         node_base = level_base = pat_base = tip_base = prof_base = tipprof_base = state_base = 0
         lev, coff, cidx, par, trow, bl, mult, codes, moff, mvals = [], [], [], [], [], [], [], [], [], []
         mask_elems = 0
         child_base = 0
         work = []
-        recs, pairs = [], []
+        recs, pairs, pslots = [], [], []
         for t, ti in enumerate(inputs):
             L = ti.layout
             P = ti.n_patterns
@@ -302,6 +303,10 @@ class Forest:
             pair[binary, 3] = rec[c1, 3]
             recs.append(rec)
             pairs.append(pair)
+            ps = np.full(L.n_nodes, -1, dtype=np.int32)
+            ps[c0] = 2 * (node_base + binary)
+            ps[c1] = 2 * (node_base + binary) + 1
+            pslots.append(ps)
             child_base += len(L.child_idx)
             par.append(L.parent)
             tr = np.full(L.n_nodes, -1, dtype=np.int32)
@@ -330,16 +335,28 @@ class Forest:
         work.sort(key=lambda w: -w[0])
         self.work_host = np.array([(t, p0) for _, t, p0 in work], dtype=np.int32).reshape(-1, 2)
         sms = _lib.load().tt_device_sm_count()
-        if lanes_per_pattern is None:
-            # few 32-pattern tiles: split patterns over more lanes to get more CTAs
+        # FP32 kernel shape: one lane per pattern up to 5 states, four for 20+; few 32-pattern
+        # tiles -> a warp works on several nodes at once so that tiles are narrower and more
+        lanes_per_pattern = 4 if q >= 20 else 1
+        if nodes_per_warp is None:
             n32 = len(self.work_host)
-            lanes_per_pattern = 4 if n32 < 2 * sms else (2 if n32 < 6 * sms else 1)
+            nodes_per_warp = 4 if n32 < 1.5 * sms else (2 if n32 < 4 * sms else 1)
         if q >= 20:
-            lanes_per_pattern = 4
+            nodes_per_warp = 1
         elif q == 5:
-            lanes_per_pattern = min(lanes_per_pattern, 2)
+            nodes_per_warp = min(nodes_per_warp, 2)
         self.lanes_per_pattern = lanes_per_pattern
-        tile = TILE // lanes_per_pattern
+        self.nodes_per_warp = nodes_per_warp
+        tile = TILE // (lanes_per_pattern * nodes_per_warp)
+        # top of each tree kept in shared memory by the FP32 kernel: as many of the highest
+        # internal nodes as fit the budget (rows of `tile` patterns x width floats)
+        if smem_bytes is None:
+            smem_bytes = 48 * 1024
+        per_node = tile * self.w * 4
+        cap = max(1, int(smem_bytes) // per_node) if smem_bytes > 0 else 0
+        n_smem = np.minimum(trees["n_int"], cap).astype(np.int32)
+        trees["n_smem"] = n_smem
+        self.smem_nodes = int(n_smem.max()) if len(n_smem) else 0
         wf = []
         for t, ti in enumerate(inputs):
             for p0 in range(0, ti.n_patterns, tile):
@@ -370,6 +387,7 @@ class Forest:
         self.d_work_f32 = _to_dev(self.work_f32_host, dev)
         self.d_node_rec = _to_dev(np.concatenate(recs), dev)
         self.d_child_pair = _to_dev(np.concatenate(pairs), dev)
+        self.d_pair_slot = _to_dev(np.concatenate(pslots), dev)
         if warps_per_block is None:
             warps_per_block = 16 if len(self.work_f32_host) < 2 * sms else 8
         self.struct = TTForest(
@@ -377,8 +395,8 @@ class Forest:
             self.n_nodes, self.n_patterns, _p(self.d_trees), _p(self.d_level), _p(self.d_child_off),
             _p(self.d_child_idx), _p(self.d_parent), _p(self.d_tip_row), _p(self.d_mask_off), _p(self.d_masks),
             _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
-            warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host), 0,
-            _p(self.d_node_rec), _p(self.d_child_pair))
+            warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host),
+            self.smem_nodes, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), nodes_per_warp, 0)
 
     def set_branch_lengths(self, bl_list):
         """Replace branch lengths (same topology) without rebuilding."""
@@ -416,13 +434,15 @@ def branch_pmats(forest, model, bufs, need32=False, needlog=False):
     q, w = forest.q, forest.w
     p64 = bufs.get("p64", (forest.n_nodes, q, w), t.float64)
     p32 = bufs.get("p32", (forest.n_nodes, q, w), t.float32) if need32 else None
+    p32p = bufs.get("p32_pair", (forest.n_nodes, 2, q, w), t.float32) if need32 else None
     lg = bufs.get("logp", (forest.n_nodes, q, w), t.float64) if needlog else None
     status = bufs.get("status", (1,), t.int32)
     status.zero_()
     lib = _lib.load()
-    check(lib.tt_branch_pmats(C.byref(forest.struct), C.byref(model.struct), TTPmats(_p(p64), _p(p32), _p(lg)),
-                              _p(status), _stream()), "tt_branch_pmats")
-    return TTPmats(_p(p64), _p(p32), _p(lg)), status
+    pm = TTPmats(_p(p64), _p(p32), _p(lg), _p(p32p))
+    check(lib.tt_branch_pmats(C.byref(forest.struct), C.byref(model.struct), pm, _p(status), _stream()),
+          "tt_branch_pmats")
+    return pm, status
 
 
 def _check_status(status):
@@ -597,7 +617,7 @@ def _mini_forest(n_nodes, q, bl, device, mult=None, parent=None, n_int=None, P=1
     dev = require_device(device)
     tr = np.zeros(1, dtype=[(n, np.int64) for n in ("node_base", "level_base", "pat_base", "tip_base", "prof_base",
                                                     "tipprof_base", "state_base")] +
-                  [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model", "reserved")])
+                  [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model", "n_smem")])
     tr[0] = (0, 0, 0, 0, 0, 0, 0, n_nodes if n_int is None else n_int, 0, 0, P, 0, 0)
     keep = {"trees": _to_dev(tr.view(np.uint8), dev), "bl": _to_dev(np.asarray(bl, np.float64), dev)}
     keep["parent"] = _to_dev(np.asarray(parent if parent is not None else np.full(n_nodes, -1), np.int32), dev)
@@ -605,7 +625,7 @@ def _mini_forest(n_nodes, q, bl, device, mult=None, parent=None, n_int=None, P=1
     keep["tip_row"] = _to_dev(np.full(n_nodes, -1, np.int32), dev)
     w = WIDTHS[q]
     f = TTForest(1, q, w, 0, n_nodes, P, _p(keep["trees"]), None, None, None, _p(keep["parent"]), _p(keep["tip_row"]),
-                 None, None, _p(keep["bl"]), None, _p(keep["mult"]), None, 0, 8, 0, 1, None, 0, 0, None, None)
+                 None, None, _p(keep["bl"]), None, _p(keep["mult"]), None, 0, 8, 0, 1, None, 0, 0, None, None, None, 1, 0)
     return f, keep
 
 
@@ -623,8 +643,8 @@ def expqt(gtr, t):
     f, keep = _mini_forest(len(ts), q, ts, model.device)
     p64 = tt.empty((len(ts), q, w), dtype=tt.float64, device=model.device)
     status = tt.zeros(1, dtype=tt.int32, device=model.device)
-    check(_lib.load().tt_branch_pmats(C.byref(f), C.byref(model.struct), TTPmats(_p(p64), None, None), _p(status),
-                                      _stream()), "tt_branch_pmats")
+    check(_lib.load().tt_branch_pmats(C.byref(f), C.byref(model.struct), TTPmats(_p(p64), None, None, None),
+                                      _p(status), _stream()), "tt_branch_pmats")
     _check_status(status)
     res = p64[:, :, :q].cpu().numpy()
     return res[0] if scalar else res

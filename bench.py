@@ -148,7 +148,7 @@ def run_gpu(args):
     # launch shape of the FP32 kernel picked by the autotuner (outside the timed region)
     from treetime_gb300 import autotune
     best, table = autotune.tune(sess["forest"].inputs, 4, model, device=dev, use_cache=False)
-    forest = engine.Forest(sess["forest"].inputs, 4, device=dev, nodes_per_warp=best[0], warps_per_block=best[1],
+    forest = engine.Forest(sess["forest"].inputs, 4, device=dev, threads=best[0], ranges_per_sm=best[1],
                            smem_bytes=best[2])
     bufs = engine.Buffers(forest)
     P = t.data.compressed_length
@@ -245,13 +245,14 @@ def run_gpu(args):
         "rel_logLH_err_vs_fp64": rel_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NPW=%d,NW=%d>" % (
-                         forest.nodes_per_warp, 32 if forest.struct.warps_per_block >= 16 else 16),
+                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,D=2>" % forest.threads,
+                     "ranges": int(len(forest.work_f32_host)),
+                     "range_patterns": int(forest.work_f32_host[:, 2].max()),
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms},
         "e2e": {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms},
         "gpu_launches": 3 * args.steps,
-        "autotune": {"best": {"nodes_per_warp": best[0], "warps_per_block": best[1], "smem_bytes": best[2]},
+        "autotune": {"best": {"threads": best[0], "ranges_per_sm": best[1], "smem_bytes": best[2]},
                      "ms": table},
         "clocks": clocks,
     }

@@ -102,30 +102,32 @@ typedef struct tt_forest {
     const double*  bl;         /* [n_nodes] branch length above the node as used by the model       */
     const uint8_t* tip_codes;  /* tip character bytes                                              */
     const double*  mult;       /* [n_patterns] pattern multiplicities                              */
-    /* Schedule of the persistent pruning kernels: tiles of consecutive patterns of one tree, given
-       as (tree, first pattern) pairs, largest trees first.  One CTA walks a whole tree for a tile;
-       tiles never wait on each other.  `work` holds 32-pattern tiles (one lane per pattern, used by
-       every kernel); the FP32 marginal kernel reads `work_f32`, whose tiles hold
-       32 / (lanes_per_pattern * nodes_per_warp) patterns, when that is below 32. */
+    /* Schedule of the persistent pruning kernels.  `work` holds 32-pattern tiles of one tree as
+       (tree, first pattern) pairs, largest trees first; one CTA walks a whole tree for a tile and
+       tiles never wait on each other (FP64 marginal, joint).  The FP32 marginal kernel reads
+       `work_f32` instead: pattern ranges (tree, first pattern, pattern count, 0) of any width, one
+       CTA per range, sized by the host so that the ranges of the forest fill the GPU. */
     const int32_t* work;       /* [n_work][2]                                                      */
     int32_t n_work;
     int32_t warps_per_block;   /* 8 or >= 16 (wide CTAs) warps share the nodes of a level (0: 8)   */
-    int32_t max_blocks;        /* grid size cap (0: one CTA per tile)                              */
+    int32_t max_blocks;        /* grid size cap (0: one CTA per tile / range)                      */
     int32_t lanes_per_pattern; /* lanes per pattern in the FP32 marginal kernel: 1 up to 5 states,
-                                  4 for 20-22 states                                               */
-    const int32_t* work_f32;   /* [n_work_f32][2]                                                  */
+                                  4 for 20-22 states (0: whatever the kernel uses)                 */
+    const int32_t* work_f32;   /* [n_work_f32][4]: pattern count * lanes_per_pattern <= the CTA
+                                  size, and a multiple of 32 when lanes_per_pattern > 1; lanes past
+                                  the tree's last pattern compute but store nothing                */
     int32_t n_work_f32;
-    int32_t smem_nodes;        /* max over trees of tt_tree.n_smem (sizes the dynamic shared memory:
-                                  smem_nodes * (32 / lanes_per_pattern) * width * 4 bytes)        */
+    int32_t smem_top_bytes;    /* dynamic shared memory for the top-of-tree rows of the FP32
+                                  kernel: at least n_smem * pattern count * width * 4 bytes for
+                                  every range (0..200 KiB)                                         */
     const int32_t* node_rec;   /* [n_nodes][4]: first child entry, end of child entries, parent
                                   local id (-1 at the root), tip row (-1 for internal nodes)      */
     const int32_t* child_pair; /* [n_nodes][4] for nodes with two children: (child 0, its tip row,
                                   child 1, its tip row); unused otherwise                          */
     const int32_t* pair_slot;  /* [n_nodes] 2 * (global id of the parent) + (0 or 1) when the parent
                                   has exactly two children, -1 otherwise (see tt_pmats.p32_pair)  */
-    int32_t nodes_per_warp;    /* FP32 marginal kernel: a warp works on 1, 2 or 4 nodes at once,
-                                  each with 32 / nodes_per_warp lanes; tiles of work_f32 hold
-                                  32 / (lanes_per_pattern * nodes_per_warp) patterns               */
+    int32_t threads_f32;       /* CTA size of the FP32 marginal kernel for 4 states: 512 or 1024
+                                  (other values: 1024); 5 states use 1024, 20-22 states 512      */
     int32_t reserved2;
 } tt_forest;
 

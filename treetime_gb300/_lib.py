@@ -36,8 +36,8 @@ class TTForest(C.Structure):
                 ("trees", vp), ("level_off", vp), ("child_off", vp), ("child_idx", vp), ("parent", vp),
                 ("tip_row", vp), ("mask_off", vp), ("masks", vp), ("bl", vp), ("tip_codes", vp), ("mult", vp),
                 ("work", vp), ("n_work", i32), ("warps_per_block", i32), ("max_blocks", i32),
-                ("lanes_per_pattern", i32), ("work_f32", vp), ("n_work_f32", i32), ("smem_nodes", i32),
-                ("node_rec", vp), ("child_pair", vp), ("pair_slot", vp), ("nodes_per_warp", i32),
+                ("lanes_per_pattern", i32), ("work_f32", vp), ("n_work_f32", i32), ("smem_top_bytes", i32),
+                ("node_rec", vp), ("child_pair", vp), ("pair_slot", vp), ("threads_f32", i32),
                 ("reserved2", i32)]
 
 

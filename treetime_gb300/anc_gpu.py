@@ -173,9 +173,10 @@ class GPUAncMixin:
         engine.check_exp(self.gtr, bl)
         ti = engine.TreeInput(layout, codes, tip_row, self.data.multiplicity(), bl, masks=masks)
         forest = engine.Forest([ti], self.gtr.n_states, device=device,
-                               nodes_per_warp=getattr(self, "nodes_per_warp", None),
+                               threads=getattr(self, "threads", None),
                                warps_per_block=getattr(self, "warps_per_block", None),
-                               smem_bytes=getattr(self, "smem_bytes", None))
+                               smem_bytes=getattr(self, "smem_bytes", None),
+                               range_patterns=getattr(self, "range_patterns", None))
         model = None if self.gtr.is_site_specific else engine.model_for(self.gtr, device)
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
                  root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes)

@@ -60,19 +60,26 @@ extern "C" tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt
             return TT_ERR_INVALID;
         }
         prm.pmat = pm->p32;
-        int lpp = f->lanes_per_pattern > 0 ? f->lanes_per_pattern : 1;
-        int npw = f->nodes_per_warp > 0 ? f->nodes_per_warp : 1;
-        if (lpp * npw > 1) {
-            if (!f->work_f32 || f->n_work_f32 <= 0) {
-                set_error("tt_marginal: lanes_per_pattern or nodes_per_warp > 1 needs work_f32");
-                return TT_ERR_INVALID;
-            }
-            prm.items = reinterpret_cast<const WorkItem*>(f->work_f32);
-            prm.n_items = f->n_work_f32;
-            blocks = f->max_blocks > 0 && f->max_blocks < f->n_work_f32 ? f->max_blocks : f->n_work_f32;
+        if (!f->work_f32 || f->n_work_f32 <= 0) {
+            set_error("tt_marginal: FP32 needs the pattern ranges work_f32");
+            return TT_ERR_INVALID;
         }
-        st = launch_marginal_f32(f->n_states, warps, lpp, npw, prm, reinterpret_cast<const int4*>(f->node_rec),
-                                 reinterpret_cast<const int4*>(f->child_pair), pm->p32_pair, blocks, s);
+        const int lpp = marginal_f32_lanes(f->n_states);
+        if (f->lanes_per_pattern != 0 && f->lanes_per_pattern != lpp) {
+            set_error("tt_marginal: lanes_per_pattern %d, the FP32 kernel uses %d for %d states",
+                      f->lanes_per_pattern, lpp, f->n_states);
+            return TT_ERR_INVALID;
+        }
+        if (f->smem_top_bytes < 0 || f->smem_top_bytes > 200 * 1024) {
+            set_error("tt_marginal: smem_top_bytes %d outside [0, 200 KiB]", f->smem_top_bytes);
+            return TT_ERR_INVALID;
+        }
+        prm.n_items = f->n_work_f32;
+        blocks = f->max_blocks > 0 && f->max_blocks < f->n_work_f32 ? f->max_blocks : f->n_work_f32;
+        st = launch_marginal_f32(f->n_states, marginal_f32_threads(f->n_states, f->threads_f32), prm,
+                                 reinterpret_cast<const int4*>(f->work_f32), reinterpret_cast<const int4*>(f->node_rec),
+                                 reinterpret_cast<const int4*>(f->child_pair), pm->p32_pair, f->smem_top_bytes, blocks,
+                                 s);
     } else if (precision == TT_PREC_F64) {
         prm.pmat = pm->p64;
         st = launch_marginal_f64(f->n_states, warps, prm, blocks, s);

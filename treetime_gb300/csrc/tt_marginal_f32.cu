@@ -219,9 +219,11 @@ __device__ __forceinline__ void s_mat_vec(const float* P, const float (&o)[W / L
 
 struct F32Params {
     MargParams m;
+    const int4* items;       // [n_items] pattern ranges (tree, first pattern, pattern count, 0)
     const int4* node_rec;    // [n_nodes] (child begin, child end, parent, tip row)
     const int4* child_pair;  // [n_nodes] binary nodes: (c0, c0 tip row, c1, c1 tip row)
     const float* p32_pair;   // [n_nodes][2][Q][W] children's matrices of binary nodes
+    int32_t top_bytes;       // dynamic shared memory reserved for the top-of-tree rows
 };
 
 // Chunk of a level staged in shared memory: records, child pairs and matrices (post-order: the
@@ -230,9 +232,8 @@ template <int Q, int W>
 struct StageCfg {
     static constexpr int kMatFloats = 2 * Q * W;
     static constexpr int kBytesPerNode = 32 + kMatFloats * 4;
-    static constexpr int kFit = 20 * 1024 / kBytesPerNode;  // nodes per ~20 KB buffer
-    static constexpr int kChunk = kFit >= 128 ? 128 : (kFit >= 64 ? 64 : (kFit >= 32 ? 32 : (kFit >= 16 ? 16 :
-                                  (kFit >= 8 ? 8 : 4))));
+    static constexpr int kFit = 26 * 1024 / kBytesPerNode;  // nodes per ~26 KB buffer
+    static constexpr int kChunk = kFit >= 128 ? 128 : (kFit >= 4 ? kFit : 4);
 };
 
 template <int Q, int W>
@@ -242,27 +243,32 @@ struct __align__(16) Stage {
     float mat[StageCfg<Q, W>::kChunk][StageCfg<Q, W>::kMatFloats];
 };
 
-template <int Q, int W, int LPP, int NPW, int NW, int D>
-__global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) {
+// One CTA per pattern range [p0, p0 + np) of one tree.  Its NT threads form G = NT / (np * LPP)
+// node groups; thread t belongs to group t / (np * LPP) and always works on pattern
+// p0 + (t % (np * LPP)) / LPP, so per-pattern sums (scaling exponents, mask corrections) stay
+// in registers for the whole pass.  Group g handles nodes g, g + G, ... of a level, D of them
+// at a time (all loads of the D nodes are issued before any of them is computed).  The range
+// width is chosen by the host so that the ranges of the forest fill the GPU once; a pattern
+// count that is not a multiple of 32 makes warps straddle two or three nodes, which costs
+// nothing but a second shared-memory wavefront for matrix rows.
+template <int Q, int W, int LPP, int NT, int D, int MINB>
+__global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     constexpr int S = W / LPP;
-    constexpr int GL = 32 / NPW;      // lanes per node group: a warp works on NPW nodes at once
-    constexpr int TP = GL / LPP;      // patterns per tile
-    constexpr int STRIDE = NW * NPW;  // nodes covered by the CTA per step
     constexpr int CH = StageCfg<Q, W>::kChunk;
     constexpr int QW = Q * W;
     const MargParams& a = fp.m;
     __shared__ __align__(16) float lut_s[256 * W];
-    __shared__ int red[NW][32];
-    __shared__ float red_corr[NW][32];
-    __shared__ unsigned diff_red[NW];
-    // dynamic shared memory: two stage buffers, then the top-of-tree rows [n_smem][TP][W]
+    __shared__ int red[NT];
+    __shared__ float red_corr[NT];
+    __shared__ unsigned diff_red[NT / 32];
+    // dynamic shared memory: two stage buffers, then the top-of-tree rows [n_smem][np][W]
     extern __shared__ __align__(16) unsigned char dyn_s[];
     Stage<Q, W>* stg = reinterpret_cast<Stage<Q, W>*>(dyn_s);
     float* top_s = reinterpret_cast<float*>(dyn_s + 2 * sizeof(Stage<Q, W>));
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int sub = lane / GL, pl = (lane % GL) / LPP, part = lane % LPP, j0 = part * S;
-    for (int i = tid; i < 256 * W; i += blockDim.x) {
+    const int part = tid % LPP, j0 = part * S;
+    for (int i = tid; i < 256 * W; i += NT) {
         const int c = i / W, j = i % W;
         lut_s[i] = j < Q ? (float)__ldg(a.lut + c * Q + j) : 0.f;
     }
@@ -272,12 +278,24 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
     const float* pm = reinterpret_cast<const float*>(a.pmat);
 
     for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
-        const WorkItem wi = a.items[it];
-        const tt_tree tr = a.f.trees[wi.tree];
+        const int4 wi = fp.items[it];
+        const tt_tree tr = a.f.trees[wi.x];
         const int P = tr.n_patterns;
-        const int p = wi.p0 + pl;
-        const bool valid = p < P;
-        const int pc = valid ? p : P - 1;
+        const int np = wi.z;
+        const int GP = np * LPP;  // threads per node group
+        // malformed range (checked uniformly by the whole CTA): flag it and skip
+        if (np < 1 || GP > NT || (LPP > 1 && (GP & 31)) ||
+            (int64_t)tr.n_smem * np * W * (int64_t)sizeof(float) > fp.top_bytes) {
+            if (tid == 0) set_status(a.status, TT_ERR_INVALID);
+            continue;
+        }
+        const int G = NT / GP;
+        const bool active = tid < G * GP;
+        const int g = tid / GP;  // == G for the idle tail threads
+        const int pl = (tid - g * GP) / LPP;
+        const int p = wi.y + pl;
+        const bool valid = active && p < P;
+        const int pc = p < P ? p : P - 1;
         const int64_t nb = tr.node_base;
         const int32_t* lev = a.f.level_off + tr.level_base;
         int esum = 0;
@@ -287,16 +305,26 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
         float lcorr = 0.f;
         const int top = tr.n_int - tr.n_smem;  // local ids >= top live in shared memory
 
-        auto row_of = [&](int k) -> int64_t { return (tr.prof_base + (int64_t)k * P + pc) * W + j0; };
-        auto top_row = [&](int k) -> float* { return top_s + ((int64_t)(k - top) * TP + pl) * W + j0; };
-        auto prow = [&](int k) -> float* { return k >= top ? top_row(k) : partial + row_of(k); };
-        auto qrow = [&](int k) -> float* { return k >= top ? top_row(k) : posterior + row_of(k); };
-        auto tip_code = [&](int trow) -> int {
-            return trow < 0 ? 0 : (int)__ldg(a.f.tip_codes + tr.tip_base + (int64_t)trow * P + pc);
-        };
+        // row k of this thread's pattern: base + k * (P * W) floats
+        const int PW = P * W;
+        float* const part0 = partial + (tr.prof_base + pc) * W + j0;
+        float* const post0 = posterior + (tr.prof_base + pc) * W + j0;
+        const int top_lane = pl * W + j0;
+        const int NPWs = np * W;
+        const uint8_t* const codes0 = a.f.tip_codes + tr.tip_base + pc;
+        uint8_t* const states0 = a.o.states + tr.state_base + pc;
+        auto top_row = [&](int k) -> float* { return top_s + (k - top) * NPWs + top_lane; };
+        auto prow = [&](int k) -> float* { return k >= top ? top_row(k) : part0 + (int64_t)k * PW; };
+        auto qrow = [&](int k) -> float* { return k >= top ? top_row(k) : post0 + (int64_t)k * PW; };
+        auto tip_code = [&](int trow) -> int { return trow < 0 ? 0 : (int)__ldg(codes0 + (int64_t)trow * P); };
         auto lut_part = [&](int code, float (&x)[S]) {
+            if constexpr (S == 4) {
+                const float4 v = *reinterpret_cast<const float4*>(lut_s + code * W + j0);
+                x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+            } else {
 #pragma unroll
-            for (int s = 0; s < S; ++s) x[s] = lut_s[code * W + j0 + s];
+                for (int s = 0; s < S; ++s) x[s] = lut_s[code * W + j0 + s];
+            }
         };
         // mask of the branch above node c applied to its message; correction for internal c
         auto apply_mask = [&](int c, const float (&x)[S], float (&msg)[S]) {
@@ -318,19 +346,29 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
         // stage the chunk [base, base + cnt) of a level into buffer b
         auto stage = [&](int b, int base, int cnt, bool post) {
             Stage<Q, W>& S_ = stg[b];
-            for (int i = tid; i < cnt; i += blockDim.x) {
+            for (int i = tid; i < cnt; i += NT) {
                 cp_async16(&S_.rec[i], fp.node_rec + nb + base + i);
                 if (post) cp_async16(&S_.pair[i], fp.child_pair + nb + base + i);
             }
-            const int per = post ? 2 * QW : QW;                  // floats per node
-            const float* src = post ? fp.p32_pair + (nb + base) * (2 * QW) : pm + (nb + base) * QW;
-            const int units = cnt * per / 4;
-            for (int u = tid; u < units; u += blockDim.x) {
-                const int node = (u * 4) / per, off = (u * 4) % per;
-                cp_async16(&S_.mat[node][off], src + (int64_t)u * 4);
+            if (post) {
+                constexpr int U = 2 * QW / 4;  // 16-byte units per node
+                const float* src = fp.p32_pair + (nb + base) * (2 * QW);
+                for (int u = tid; u < cnt * U; u += NT) {
+                    const int node = u / U, off = (u - node * U) * 4;
+                    cp_async16(&S_.mat[node][off], src + (int64_t)u * 4);
+                }
+            } else {
+                constexpr int U = QW / 4;
+                const float* src = pm + (nb + base) * QW;
+                for (int u = tid; u < cnt * U; u += NT) {
+                    const int node = u / U, off = (u - node * U) * 4;
+                    cp_async16(&S_.mat[node][off], src + (int64_t)u * 4);
+                }
             }
             cp_async_commit();
         };
+        const int GD = G * D;
+        const int first = active ? g : 0x7fffffff;
 
         // ------------------------------------------------------------ post-order
         {
@@ -352,14 +390,14 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                 }
                 __syncthreads();  // chunk b staged; the previous level's rows are written
                 const Stage<Q, W>& st = stg[b];
-                for (int i0 = warp * NPW + sub; i0 - sub < cnt; i0 += STRIDE * D) {
+                for (int i0 = first; i0 < cnt; i0 += GD) {
                     // loads of D nodes first
                     float xa[D][S], xb[D][S];
                     int ca[D], cb[D];
                     bool bin[D];
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
-                        const int i = i0 + d * STRIDE;
+                        const int i = i0 + d * G;
                         bin[d] = false;
                         if (i < cnt) {
                             const int4 rec = st.rec[i];
@@ -375,19 +413,19 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                     }
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
-                        const int i = i0 + d * STRIDE;
+                        const int i = i0 + d * G;
                         if (i >= cnt) continue;
                         const int k = base + i;
                         float r[S];
                         int extra = 0;
                         if (bin[d]) {
-                            const int4 cp = st.pair[i];
                             if (ca[d] >= 0) lut_part(ca[d], xa[d]);
                             if (cb[d] >= 0) lut_part(cb[d], xb[d]);
                             float m0[S], m1[S];
                             s_vec_mat<Q, W, LPP>(xa[d], &st.mat[i][0], j0, m0);
                             s_vec_mat<Q, W, LPP>(xb[d], &st.mat[i][QW], j0, m1);
                             if (has_masks) {
+                                const int4 cp = st.pair[i];
                                 apply_mask(cp.x, xa[d], m0);
                                 apply_mask(cp.z, xb[d], m1);
                             }
@@ -426,7 +464,7 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                         scale_pow2<S>(r, e);
                         esum += e + extra;
                         if (k >= top) st_part<S>(top_row(k), r);
-                        if (valid) st_part<S>(partial + row_of(k), r);
+                        if (valid) st_part<S>(part0 + (int64_t)k * PW, r);
                     }
                 }
                 h = nh;
@@ -435,22 +473,18 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                 have = has_next;
             }
         }
-        // per-pattern exponent sums: lanes of one pattern hold identical values; warps add up
-        red[warp][lane] = esum;
-        red_corr[warp][lane] = lcorr;
+        // per-pattern exponent sums: lanes of one pattern hold identical values; groups add up
+        red[tid] = esum;
+        red_corr[tid] = lcorr;
         __syncthreads();
 
         // ------------------------------------------------------------------ root
-        if (warp == 0) {
+        if (tid < GP) {  // group 0 (whole warps when LPP > 1)
             int tot = 0;
             double corr = 0.0;
-            const int gl = lane % GL;  // same pattern and state slice in every node group
-            for (int w = 0; w < NW; ++w) {
-#pragma unroll
-                for (int g2 = 0; g2 < NPW; ++g2) {
-                    tot += red[w][g2 * GL + gl];
-                    corr += (double)red_corr[w][g2 * GL + gl];
-                }
+            for (int gg = 0; gg < G; ++gg) {
+                tot += red[gg * GP + tid];
+                corr += (double)red_corr[gg * GP + tid];
             }
             const int kr = tr.n_int - 1;
             const double* pi = a.pi + (int64_t)tr.model * Q;
@@ -477,18 +511,19 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
             } else {
                 st = group_argmax<Q, W, LPP>(pr, j0);
             }
-            if (kr >= top && sub == 0) st_part<S>(top_row(kr), pr);
-            if (valid && sub == 0) {
-                st_part<S>(posterior + row_of(kr), pr);
+            if (kr >= top) st_part<S>(top_row(kr), pr);
+            if (valid) {
+                st_part<S>(post0 + (int64_t)kr * PW, pr);
                 if (part == 0) {
                     a.o.site_lh[tr.pat_base + p] = log((double)ssum) + kLn2 * (double)tot + corr;
-                    a.o.states[tr.state_base + (int64_t)kr * P + pc] = (uint8_t)st;
+                    states0[(int64_t)kr * P] = (uint8_t)st;
                 }
                 if (a.o.outgroup) {
                     float o[S];
 #pragma unroll
                     for (int s = 0; s < S; ++s) o[s] = (j0 + s < Q) ? (float)__ldg(pi + j0 + s) : 0.f;
-                    st_part<S>(reinterpret_cast<float*>(a.o.outgroup) + row_of(kr), o);
+                    st_part<S>(reinterpret_cast<float*>(a.o.outgroup) + (tr.prof_base + pc) * W + j0 +
+                                   (int64_t)kr * PW, o);
                 }
             }
         }
@@ -496,6 +531,7 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
         // ------------------------------------------------------------- pre-order
         unsigned ndiff = 0;
         const bool do_tips = a.o.reconstruct_tips || a.o.tip_outgroup;
+        const bool count_diff = a.o.count_diff != 0;
         const int h_last = do_tips ? -1 : 0;
         {
             // levels n_levels-2 .. 0, then the tips as level -1
@@ -522,32 +558,35 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                 }
                 __syncthreads();
                 const Stage<Q, W>& st = stg[b];
-                for (int i0 = warp * NPW + sub; i0 - sub < cnt; i0 += STRIDE * D) {
+                for (int i0 = first; i0 < cnt; i0 += GD) {
                     float pv[D][S], x[D][S];
                     int code[D];
+                    unsigned old[D];
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
-                        const int i = i0 + d * STRIDE;
+                        const int i = i0 + d * G;
+                        old[d] = 0;
                         if (i < cnt) {
                             const int4 rec = st.rec[i];
                             ld_part<S>(qrow(rec.z), pv[d]);
                             if (tips) code[d] = tip_code(rec.w);
                             else ld_part<S>(prow(base + i), x[d]);
+                            if (count_diff && valid && part == 0) old[d] = states0[(int64_t)(base + i) * P];
                         }
                     }
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
-                        const int i = i0 + d * STRIDE;
+                        const int i = i0 + d * G;
                         if (i >= cnt) continue;
                         const int k = base + i;
-                        const int64_t g = nb + k;
+                        const int64_t gk = nb + k;
                         if (tips) lut_part(code[d], x[d]);
                         const float* Pk = &st.mat[i][0];
                         float msg[S], o[S];
                         s_vec_mat<Q, W, LPP>(x[d], Pk, j0, msg);
                         float m = 1.f;
                         if (has_masks) {
-                            const int64_t mo = __ldg(a.f.mask_off + g);
+                            const int64_t mo = __ldg(a.f.mask_off + gk);
                             if (mo >= 0) m = (float)__ldg(a.f.masks + mo + pc);
                         }
                         if (m != 1.f) {
@@ -555,17 +594,19 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                             for (int s = 0; s < S; ++s)
                                 if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
                         }
+                        // outgroup message: parent's posterior divided by this node's message
+                        // (fast division, <= 2 ulp; the result is renormalised right away)
                         float sl = 0.f;
 #pragma unroll
                         for (int s = 0; s < S; ++s) {
-                            o[s] = (j0 + s < Q) ? fmaxf(1e-12f, pv[d][s]) / msg[s] : 0.f;
+                            o[s] = (j0 + s < Q) ? __fdividef(fmaxf(1e-12f, pv[d][s]), msg[s]) : 0.f;
                             sl += o[s];
                         }
-                        const float inv = 1.f / group_sum<LPP>(sl);
+                        const float inv = __fdividef(1.f, group_sum<LPP>(sl));
 #pragma unroll
                         for (int s = 0; s < S; ++s) o[s] *= inv;
                         const int64_t row = tips ? (tr.tipprof_base + (int64_t)(k - tr.n_int) * P + pc) * W + j0
-                                                 : row_of(k);
+                                                 : (tr.prof_base + (int64_t)k * P + pc) * W + j0;
                         if (valid) {
                             float* og = reinterpret_cast<float*>(tips ? a.o.tip_outgroup : a.o.outgroup);
                             if (og) st_part<S>(og + row, o);
@@ -580,7 +621,7 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                             x[d][s] *= ev[s];
                             s2 += x[d][s];
                         }
-                        const float inv2 = 1.f / group_sum<LPP>(s2);
+                        const float inv2 = __fdividef(1.f, group_sum<LPP>(s2));
 #pragma unroll
                         for (int s = 0; s < S; ++s) x[d][s] *= inv2;
                         const int stt = group_argmax<Q, W, LPP>(x[d], j0);
@@ -589,9 +630,8 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                             float* dst = tips ? reinterpret_cast<float*>(a.o.tip_posterior) : posterior;
                             if (dst) st_part<S>(dst + row, x[d]);
                             if (part == 0) {
-                                uint8_t* sp = a.o.states + tr.state_base + (int64_t)k * P + pc;
-                                if (a.o.count_diff) ndiff += (*sp != (uint8_t)stt);
-                                *sp = (uint8_t)stt;
+                                if (count_diff) ndiff += (old[d] != (unsigned)stt);
+                                states0[(int64_t)k * P] = (uint8_t)stt;
                             }
                         }
                     }
@@ -602,60 +642,66 @@ __global__ void __launch_bounds__(NW * 32, 1) marginal_f32_kernel(F32Params fp) 
                 have = has_next;
             }
         }
-        if (a.o.n_diff && a.o.count_diff) {
+        if (a.o.n_diff && count_diff) {
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) ndiff += __shfl_xor_sync(0xffffffffu, ndiff, off);
             if (lane == 0) diff_red[warp] = ndiff;
             __syncthreads();
             if (tid == 0) {
                 unsigned long long t = 0;
-                for (int w = 0; w < NW; ++w) t += diff_red[w];
-                if (t) atomicAdd(a.o.n_diff + wi.tree, t);
+                for (int w = 0; w < NT / 32; ++w) t += diff_red[w];
+                if (t) atomicAdd(a.o.n_diff + wi.x, t);
             }
         }
         __syncthreads();
     }
 }
 
-template <int Q, int LPP, int NPW, int NW, int D>
+template <int Q, int LPP, int NT, int D, int MINB>
 static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
     constexpr int W = round4(Q);
     static_assert(W % LPP == 0, "width must split over the lanes of a pattern");
-    const size_t dyn = 2 * sizeof(Stage<Q, W>) + (size_t)prm.m.f.smem_nodes * (32 / (LPP * NPW)) * W * sizeof(float);
-    // static + dynamic shared memory passes 48 KB: opt in to the larger carve-out
-    static size_t configured = 0;
-    if (dyn > configured) {
-        cudaError_t e = cudaFuncSetAttribute(marginal_f32_kernel<Q, W, LPP, NPW, NW, D>,
+    const size_t dyn = 2 * sizeof(Stage<Q, W>) + (size_t)prm.top_bytes;
+    // static + dynamic shared memory past 48 KB needs the opt-in, once per device
+    static size_t configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || dyn > configured[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(marginal_f32_kernel<Q, W, LPP, NT, D, MINB>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
         if (e != cudaSuccess) {
             set_error("tt_marginal(f32): %zu bytes of shared memory: %s", dyn, cudaGetErrorString(e));
             return TT_ERR_INVALID;
         }
-        configured = dyn;
+        if (dev >= 0 && dev < 64) configured[dev] = dyn;
     }
-    marginal_f32_kernel<Q, W, LPP, NPW, NW, D><<<blocks, NW * 32, dyn, s>>>(prm);
+    marginal_f32_kernel<Q, W, LPP, NT, D, MINB><<<blocks, NT, dyn, s>>>(prm);
     return check_launch("tt_marginal(f32)");
 }
 
-tt_status launch_marginal_f32(int q, int warps, int lpp, int npw, const MargParams& prm, const int4* node_rec,
-                              const int4* child_pair, const float* p32_pair, int blocks, cudaStream_t s) {
-    F32Params fp{prm, node_rec, child_pair, p32_pair};
-    const bool wide = warps >= 16;
+tt_status launch_marginal_f32(int q, int threads, const MargParams& prm, const int4* items, const int4* node_rec,
+                              const int4* child_pair, const float* p32_pair, int top_bytes, int blocks,
+                              cudaStream_t s) {
+    F32Params fp{prm, items, node_rec, child_pair, p32_pair, top_bytes};
     switch (q) {
         case 4:
-            if (npw >= 4) return wide ? launch_f32<4, 1, 4, 32, 2>(fp, blocks, s) : launch_f32<4, 1, 4, 16, 2>(fp, blocks, s);
-            if (npw == 2) return wide ? launch_f32<4, 1, 2, 32, 2>(fp, blocks, s) : launch_f32<4, 1, 2, 16, 2>(fp, blocks, s);
-            return wide ? launch_f32<4, 1, 1, 32, 2>(fp, blocks, s) : launch_f32<4, 1, 1, 16, 2>(fp, blocks, s);
-        case 5:
-            if (npw >= 2) return launch_f32<5, 1, 2, 16, 2>(fp, blocks, s);
-            return launch_f32<5, 1, 1, 16, 2>(fp, blocks, s);
-        case 20: return launch_f32<20, 4, 1, 8, 1>(fp, blocks, s);
-        case 21: return launch_f32<21, 4, 1, 8, 1>(fp, blocks, s);
-        case 22: return launch_f32<22, 4, 1, 8, 1>(fp, blocks, s);
+            return threads == 512 ? launch_f32<4, 1, 512, 2, 1>(fp, blocks, s) : launch_f32<4, 1, 1024, 1, 1>(fp, blocks, s);
+        case 5: return launch_f32<5, 1, 1024, 1, 1>(fp, blocks, s);
+        case 20: return launch_f32<20, 4, 512, 1, 1>(fp, blocks, s);
+        case 21: return launch_f32<21, 4, 512, 1, 1>(fp, blocks, s);
+        case 22: return launch_f32<22, 4, 512, 1, 1>(fp, blocks, s);
         default:
             set_error("tt_marginal: alphabet size %d not compiled (4, 5, 20, 21, 22)", q);
             return TT_ERR_UNSUPPORTED;
     }
 }
+
+int marginal_f32_threads(int q, int requested) {
+    if (q == 4) return requested == 512 ? 512 : 1024;
+    if (q == 5) return 1024;
+    return 512;
+}
+
+int marginal_f32_lanes(int q) { return q >= 20 ? 4 : 1; }
 
 }  // namespace tt

@@ -15,6 +15,8 @@ Layout of a forest in device memory (see include/treetime_gb300.h):
 
 import ctypes as C
 
+import math
+
 import numpy as np
 
 from . import _lib
@@ -261,8 +263,8 @@ class Forest:
     """Device-resident schedule and inputs of a list of trees, plus the
     C-ABI struct that points at them."""
 
-    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, nodes_per_warp=None,
-                 smem_bytes=None):
+    def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, threads=None,
+                 smem_bytes=None, range_patterns=None, ranges_per_sm=1):
         dev = require_device(device)
         self.device = dev
         self.inputs = list(inputs)
@@ -335,34 +337,56 @@ class Forest:
         work.sort(key=lambda w: -w[0])
         self.work_host = np.array([(t, p0) for _, t, p0 in work], dtype=np.int32).reshape(-1, 2)
         sms = _lib.load().tt_device_sm_count()
-        # FP32 kernel shape: one lane per pattern up to 5 states, four for 20+; few 32-pattern
-        # tiles -> a warp works on several nodes at once so that tiles are narrower and more
+        # FP32 kernel: one CTA per pattern range, one lane per pattern up to 5 states, four for
+        # 20+.  Range widths make the ranges of the forest fill the GPU once (ranges_per_sm
+        # CTAs per SM): each tree gets the width whose node x pattern work is one CTA's share.
         lanes_per_pattern = 4 if q >= 20 else 1
-        if nodes_per_warp is None:
-            n32 = len(self.work_host)
-            nodes_per_warp = 4 if n32 < 1.5 * sms else (2 if n32 < 4 * sms else 1)
         if q >= 20:
-            nodes_per_warp = 1
-        elif q == 5:
-            nodes_per_warp = min(nodes_per_warp, 2)
+            threads = 512
+        elif q == 5 or threads is None:
+            threads = 1024
+        if threads not in (512, 1024):
+            raise ValueError("threads must be 512 or 1024")
         self.lanes_per_pattern = lanes_per_pattern
-        self.nodes_per_warp = nodes_per_warp
-        tile = TILE // (lanes_per_pattern * nodes_per_warp)
+        self.threads = threads
+        max_np = threads // lanes_per_pattern
+        unit = 32 // lanes_per_pattern if lanes_per_pattern > 1 else 1
+        slots = max(1, sms * max(1, int(ranges_per_sm)))
+        total = sum(ti.layout.n_nodes * ti.n_patterns for ti in inputs)
+        ranges, widths = [], []
+        for t, ti in enumerate(inputs):
+            P, N = ti.n_patterns, ti.layout.n_nodes
+            if range_patterns:
+                want = int(range_patterns)
+            else:
+                want = int(math.ceil(total / slots / max(1, N)))
+            want = max(1, min(want, P, max_np))
+            if unit > 1:
+                want = min(max_np, -(-want // unit) * unit)
+                starts = list(range(0, P, want))
+                ws = [want] * len(starts)
+            else:
+                n_r = -(-P // want)
+                base_w, extra = divmod(P, n_r)
+                ws = [base_w + (1 if r < extra else 0) for r in range(n_r)]
+                starts = list(np.cumsum([0] + ws[:-1]))
+            widths.append(max(ws))
+            for p0, w_ in zip(starts, ws):
+                ranges.append((N * min(w_, P - p0), t, int(p0), int(w_)))
+        ranges.sort(key=lambda r: -r[0])
+        self.work_f32_host = np.array([(t, p0, w_, 0) for _, t, p0, w_ in ranges], dtype=np.int32).reshape(-1, 4)
         # top of each tree kept in shared memory by the FP32 kernel: as many of the highest
-        # internal nodes as fit the budget (rows of `tile` patterns x width floats)
+        # internal nodes as fit the budget (rows of range-width patterns x width floats)
         if smem_bytes is None:
             smem_bytes = 48 * 1024
-        per_node = tile * self.w * 4
-        cap = max(1, int(smem_bytes) // per_node) if smem_bytes > 0 else 0
-        n_smem = np.minimum(trees["n_int"], cap).astype(np.int32)
+        top_bytes = 0
+        n_smem = np.zeros(len(inputs), dtype=np.int32)
+        for t in range(len(inputs)):
+            per_node = widths[t] * self.w * 4
+            n_smem[t] = min(int(trees["n_int"][t]), int(smem_bytes) // per_node) if smem_bytes > 0 else 0
+            top_bytes = max(top_bytes, int(n_smem[t]) * per_node)
         trees["n_smem"] = n_smem
-        self.smem_nodes = int(n_smem.max()) if len(n_smem) else 0
-        wf = []
-        for t, ti in enumerate(inputs):
-            for p0 in range(0, ti.n_patterns, tile):
-                wf.append((ti.layout.n_nodes * min(tile, ti.n_patterns - p0), t, p0))
-        wf.sort(key=lambda w: -w[0])
-        self.work_f32_host = np.array([(t, p0) for _, t, p0 in wf], dtype=np.int32).reshape(-1, 2)
+        self.smem_top_bytes = top_bytes
         self.trees_host = trees
         self.n_nodes = node_base
         self.n_patterns = pat_base
@@ -389,14 +413,14 @@ class Forest:
         self.d_child_pair = _to_dev(np.concatenate(pairs), dev)
         self.d_pair_slot = _to_dev(np.concatenate(pslots), dev)
         if warps_per_block is None:
-            warps_per_block = 16 if len(self.work_f32_host) < 2 * sms else 8
+            warps_per_block = 16 if len(self.work_host) < 2 * sms else 8
         self.struct = TTForest(
             len(inputs), q, self.w, int(max((ti.layout.n_levels for ti in inputs), default=0)),
             self.n_nodes, self.n_patterns, _p(self.d_trees), _p(self.d_level), _p(self.d_child_off),
             _p(self.d_child_idx), _p(self.d_parent), _p(self.d_tip_row), _p(self.d_mask_off), _p(self.d_masks),
             _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
             warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host),
-            self.smem_nodes, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), nodes_per_warp, 0)
+            self.smem_top_bytes, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), threads, 0)
 
     def set_branch_lengths(self, bl_list):
         """Replace branch lengths (same topology) without rebuilding."""

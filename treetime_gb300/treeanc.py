@@ -67,7 +67,7 @@ class TreeAnc(GPUAncMixin):
     def __init__(self, tree=None, aln=None, gtr=None, fill_overhangs=True, ref=None, verbose=ttconf.VERBOSE,
                  ignore_gaps=True, convert_upper=True, seq_multiplicity=None, log=None, compress=True, seq_len=None,
                  ignore_missing_alns=False, keep_node_order=False, rng_seed=None, precision="f64", device=None,
-                 nodes_per_warp=None, warps_per_block=None, smem_bytes=None, **kwargs):
+                 threads=None, warps_per_block=None, smem_bytes=None, range_patterns=None, **kwargs):
         if tree is None:
             raise TypeError("TreeAnc requires a tree!")
         if precision not in ("f64", "f32"):
@@ -90,9 +90,10 @@ class TreeAnc(GPUAncMixin):
         self.rng = np.random.default_rng(seed=rng_seed)
         self.precision = precision
         self.device = device
-        self.nodes_per_warp = nodes_per_warp
+        self.threads = threads
         self.warps_per_block = warps_per_block
         self.smem_bytes = smem_bytes
+        self.range_patterns = range_patterns
         self._session = None
         self._topology_version = 0
         self._tree = None

@@ -77,9 +77,7 @@ typedef struct tt_tree {
     int32_t n_levels;     /* number of height levels of internal nodes                             */
     int32_t n_patterns;
     int32_t model;        /* row of this tree's model in tt_model arrays                           */
-    int32_t n_smem;       /* FP32 marginal kernel: the top n_smem internal nodes (local ids
-                             n_int-n_smem .. n_int-1, the narrow upper levels) keep their rows in
-                             shared memory for the whole pass; 0..n_int                            */
+    int32_t reserved;     /* 0                                                                      */
 } tt_tree;
 
 typedef struct tt_forest {
@@ -117,9 +115,7 @@ typedef struct tt_forest {
                                   size, and a multiple of 32 when lanes_per_pattern > 1; lanes past
                                   the tree's last pattern compute but store nothing                */
     int32_t n_work_f32;
-    int32_t smem_top_bytes;    /* dynamic shared memory for the top-of-tree rows of the FP32
-                                  kernel: at least n_smem * pattern count * width * 4 bytes for
-                                  every range (0..200 KiB)                                         */
+    int32_t reserved1;         /* 0                                                                */
     const int32_t* node_rec;   /* [n_nodes][4]: first child entry, end of child entries, parent
                                   local id (-1 at the root), tip row (-1 for internal nodes)      */
     const int32_t* child_pair; /* [n_nodes][4] for nodes with two children: (child 0, its tip row,
@@ -127,7 +123,7 @@ typedef struct tt_forest {
     const int32_t* pair_slot;  /* [n_nodes] 2 * (global id of the parent) + (0 or 1) when the parent
                                   has exactly two children, -1 otherwise (see tt_pmats.p32_pair)  */
     int32_t threads_f32;       /* CTA size of the FP32 marginal kernel for 4 states: 512 or 1024
-                                  (other values: 1024); 5 states use 1024, 20-22 states 512      */
+                                  (other values: 1024); 5 and 20-22 states always use 512         */
     int32_t reserved2;
 } tt_forest;
 

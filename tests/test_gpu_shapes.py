@@ -1,5 +1,5 @@
 """GPU: every launch shape of the FP32 marginal kernel (CTA size, pattern-range
-width, shared-memory top of the tree) and the FP64 kernel give the oracle's
+width) and the FP64 kernel give the oracle's
 results, on a tree with polytomies, masks and missing data, for 4-, 5-, 20- and
 21-state alphabets.  Also the multi-tree forest (one launch over several trees
 of different sizes and models) against per-tree oracle runs."""
@@ -41,24 +41,20 @@ SHAPES = [(1024, None), (512, None), (1024, 1), (1024, 7), (512, 19), (1024, 32)
           ("f64", 8), ("f64", 32)]
 
 
-@pytest.mark.parametrize("smem", [None, 0, 2048])
 @pytest.mark.parametrize("alphabet", ["nuc_nogap", "nuc", "aa_nogap", "aa"])
 @pytest.mark.parametrize("shape", SHAPES)
-def test_marginal_launch_shapes(alphabet, shape, smem):
+def test_marginal_launch_shapes(alphabet, shape):
     """shape = (CTA threads, patterns per range; None = sized to fill the GPU)
-    or ("f64", warps per CTA).  smem: None = default top-of-tree budget, 0 =
-    none, 2048 = the top few nodes.  Range widths that do not divide the
+    or ("f64", warps per CTA).  Range widths that do not divide the
     pattern count, one-pattern ranges and ranges wider than the alignment are
     all covered."""
     from treetime_gb300 import TreeAnc
     threads, rp = shape
-    if threads == "f64" and smem is not None:
-        pytest.skip("shared-memory top rows are an FP32-kernel feature")
     if alphabet.startswith("aa") and (threads == 1024 or (threads == "f64" and rp == 32)):
         pytest.skip("20+ states run 512-thread CTAs (ranges rounded up to multiples of 8 patterns)")
     wl = _workload(alphabet, seed=7, L=300 if not alphabet.startswith("aa") else 120)
     prec = "f64" if threads == "f64" else "f32"
-    kw = dict(warps_per_block=rp) if prec == "f64" else dict(threads=threads, range_patterns=rp, smem_bytes=smem)
+    kw = dict(warps_per_block=rp) if prec == "f64" else dict(threads=threads, range_patterns=rp)
     t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision=prec, **kw)
     rng = np.random.default_rng(1)
     for n in list(t.tree.find_clades())[3:9]:

@@ -27,7 +27,7 @@ class TTTree(C.Structure):
     _fields_ = [("node_base", i64), ("level_base", i64), ("pat_base", i64), ("tip_base", i64),
                 ("prof_base", i64), ("tipprof_base", i64), ("state_base", i64),
                 ("n_int", i32), ("n_tip", i32), ("n_levels", i32), ("n_patterns", i32),
-                ("model", i32), ("n_smem", i32)]
+                ("model", i32), ("reserved", i32)]
 
 
 class TTForest(C.Structure):
@@ -36,7 +36,7 @@ class TTForest(C.Structure):
                 ("trees", vp), ("level_off", vp), ("child_off", vp), ("child_idx", vp), ("parent", vp),
                 ("tip_row", vp), ("mask_off", vp), ("masks", vp), ("bl", vp), ("tip_codes", vp), ("mult", vp),
                 ("work", vp), ("n_work", i32), ("warps_per_block", i32), ("max_blocks", i32),
-                ("lanes_per_pattern", i32), ("work_f32", vp), ("n_work_f32", i32), ("smem_top_bytes", i32),
+                ("lanes_per_pattern", i32), ("work_f32", vp), ("n_work_f32", i32), ("reserved1", i32),
                 ("node_rec", vp), ("child_pair", vp), ("pair_slot", vp), ("threads_f32", i32),
                 ("reserved2", i32)]
 

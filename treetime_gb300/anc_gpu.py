@@ -175,7 +175,6 @@ class GPUAncMixin:
         forest = engine.Forest([ti], self.gtr.n_states, device=device,
                                threads=getattr(self, "threads", None),
                                warps_per_block=getattr(self, "warps_per_block", None),
-                               smem_bytes=getattr(self, "smem_bytes", None),
                                range_patterns=getattr(self, "range_patterns", None))
         model = None if self.gtr.is_site_specific else engine.model_for(self.gtr, device)
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,

@@ -1,9 +1,8 @@
 """Autotuner for the FP32 marginal kernel's launch shape.
 
-The best shape depends on the workload: the CTA size (512 or 1024 threads), how
-many pattern ranges the forest is cut into per SM (one wide range per SM, or
-two narrower ones so that two CTAs share an SM) and the shared-memory budget
-for the top of the tree.  ``tune`` times every candidate on the actual forest
+The best shape depends on the workload: the CTA size (512 or 1024 threads) and
+how many pattern ranges the forest is cut into per SM (one wide range per SM,
+or two narrower ones queued behind each other).  ``tune`` times every candidate on the actual forest
 with CUDA events and returns the fastest; results are cached in memory and in
 a JSON file keyed by a coarse workload signature (alphabet size, number of
 trees, node and pattern counts rounded to powers of two).
@@ -16,8 +15,7 @@ import statistics
 
 from . import engine
 
-CANDIDATES = [(threads, rps, smem) for threads in (512, 1024) for rps in (1, 2)
-              for smem in (0, 48 * 1024, 96 * 1024, 160 * 1024)]
+CANDIDATES = [(threads, rps) for threads in (512, 1024) for rps in (1, 2)]
 _CACHE = {}
 CACHE_PATH = os.environ.get("TREETIME_GB300_TUNE_CACHE",
                             os.path.join(os.path.expanduser("~"), ".cache", "treetime_gb300", "autotune.json"))
@@ -48,8 +46,8 @@ def _save_file(d):
 
 
 def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True):
-    """Fastest (threads, ranges_per_sm, smem_bytes) for this forest and the
-    table of median times (ms) of all candidates."""
+    """Fastest (threads, ranges_per_sm) for this forest and the table of
+    median times (ms) of all candidates."""
     key = signature(inputs, q)
     if use_cache:
         if key in _CACHE:
@@ -60,14 +58,12 @@ def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True)
             return _CACHE[key]
     t = engine.torch()
     cands = candidates or CANDIDATES
-    if q >= 20:
+    if q != 4:
         cands = [c for c in cands if c[0] == 512]
-    elif q != 4:
-        cands = [c for c in cands if c[0] == 1024]
     table = {}
-    for threads, rps, smem in cands:
+    for threads, rps in cands:
         try:
-            f = engine.Forest(inputs, q, device=device, threads=threads, ranges_per_sm=rps, smem_bytes=smem)
+            f = engine.Forest(inputs, q, device=device, threads=threads, ranges_per_sm=rps)
             bufs = engine.Buffers(f)
             for _ in range(2):
                 engine.marginal(f, model, bufs, precision="f32", sync=False)
@@ -80,9 +76,9 @@ def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True)
                 b.record()
                 b.synchronize()
                 times.append(a.elapsed_time(b))
-            table["%d/%d/%d" % (threads, rps, smem)] = statistics.median(times)
+            table["%d/%d" % (threads, rps)] = statistics.median(times)
         except Exception as e:  # a shape that cannot launch (e.g. too much shared memory) is skipped
-            table["%d/%d/%d" % (threads, rps, smem)] = None
+            table["%d/%d" % (threads, rps)] = None
     ok = {k: v for k, v in table.items() if v is not None}
     best = tuple(int(x) for x in min(ok, key=ok.get).split("/"))
     _CACHE[key] = (best, table)

@@ -70,16 +70,11 @@ extern "C" tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt
                       f->lanes_per_pattern, lpp, f->n_states);
             return TT_ERR_INVALID;
         }
-        if (f->smem_top_bytes < 0 || f->smem_top_bytes > 200 * 1024) {
-            set_error("tt_marginal: smem_top_bytes %d outside [0, 200 KiB]", f->smem_top_bytes);
-            return TT_ERR_INVALID;
-        }
         prm.n_items = f->n_work_f32;
         blocks = f->max_blocks > 0 && f->max_blocks < f->n_work_f32 ? f->max_blocks : f->n_work_f32;
         st = launch_marginal_f32(f->n_states, marginal_f32_threads(f->n_states, f->threads_f32), prm,
                                  reinterpret_cast<const int4*>(f->work_f32), reinterpret_cast<const int4*>(f->node_rec),
-                                 reinterpret_cast<const int4*>(f->child_pair), pm->p32_pair, f->smem_top_bytes, blocks,
-                                 s);
+                                 reinterpret_cast<const int4*>(f->child_pair), pm->p32_pair, blocks, s);
     } else if (precision == TT_PREC_F64) {
         prm.pmat = pm->p64;
         st = launch_marginal_f64(f->n_states, warps, prm, blocks, s);

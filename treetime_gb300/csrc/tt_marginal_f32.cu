@@ -1,26 +1,25 @@
 // FP32-scaled marginal reconstruction kernel (the fast path of tt_marginal).
 //
-// Same algorithm and schedule as the FP64 kernel (tt_marginal_kernels.cuh): one CTA walks a
-// whole tree for one tile of patterns, warps share the nodes of a height level.  What differs:
-//   - arithmetic is FP32 in the linear domain: child messages x.P are multiplied, each node's
-//     partial is rescaled by an exact power of two and the exponents are summed per pattern in
-//     registers; the only FP64 operation is the root's log, once per pattern;
-//   - a warp works on NPW nodes of a level at once (one lane per pattern, 32 / NPW patterns per
-//     tile), so a tree with few patterns still yields many CTAs without extra instructions per
-//     node-pattern; for 20+ states LPP lanes cooperate on one pattern (each holds S = W / LPP
-//     consecutive states) and the matrix-vector products gather them with width-LPP shuffles;
+// Same algorithm as the FP64 kernel (tt_marginal_kernels.cuh): a CTA walks a whole tree level by
+// level for a set of patterns, post-order then pre-order.  What differs:
+//   - arithmetic is FP32 in the linear domain: child messages x.P are multiplied and a node's
+//     partial is rescaled by an exact power of two only when its largest entry falls below
+//     2^-16 (messages never exceed the largest entry of the child's partial, so partials stay in
+//     (2^-16 * tiny message, 1]); the exponents are summed per pattern in registers and the only
+//     FP64 operation is the root's log, once per pattern.  Power-of-two scaling is exact, so when
+//     and how often it happens does not change any result;
+//   - one CTA per pattern range of any width: the host cuts the forest's patterns into about one
+//     range per SM and the CTA's threads form node groups of (range width x lanes per pattern)
+//     threads, so every SM has work whatever the pattern count;
+//   - for 20+ states LPP = 4 lanes cooperate on one pattern (each holds S = W / LPP consecutive
+//     states) and the matrix-vector products gather them with width-LPP shuffles;
 //   - the tips' character -> profile table is kept in shared memory as FP32;
 //   - node records and branch matrices of a level are staged in shared memory in chunks with
-//     double-buffered cp.async copies (the next chunk is in flight while the current one is
-//     computed), the children's matrices of a two-child node lying side by side in p32_pair so
-//     that a chunk is one contiguous copy; a node then costs one round trip to global memory
-//     (its children's rows), and each warp issues those loads for D nodes before computing any
-//     of them;
-//   - the top n_smem internal nodes of the tree (its narrow upper levels, where a level has too
-//     few nodes to hide memory latency) keep their partial / posterior rows in shared memory for
-//     the whole pass: those levels run at shared-memory latency.  Their rows are still written
-//     to the global output buffers.  When the whole tree fits, the pass never reads global
-//     memory for profiles.
+//     double-buffered cp.async copies; a chunk costs one CTA barrier (each thread first waits for
+//     its own copies of the chunk, the barrier then publishes everybody's copies and the rows the
+//     previous chunk wrote, and the next chunk's copies are issued right after it).  The
+//     children's matrices of a two-child node lie side by side in p32_pair so that a chunk is one
+//     contiguous copy.
 #include "tt_marginal_kernels.cuh"
 
 namespace tt {
@@ -221,9 +220,8 @@ struct F32Params {
     MargParams m;
     const int4* items;       // [n_items] pattern ranges (tree, first pattern, pattern count, 0)
     const int4* node_rec;    // [n_nodes] (child begin, child end, parent, tip row)
-    const int4* child_pair;  // [n_nodes] binary nodes: (c0, c0 tip row, c1, c1 tip row)
+    const int4* child_pair;  // [n_nodes] binary nodes: (c0, c0 tip row, c1, c1 tip row); else c0 = -1
     const float* p32_pair;   // [n_nodes][2][Q][W] children's matrices of binary nodes
-    int32_t top_bytes;       // dynamic shared memory reserved for the top-of-tree rows
 };
 
 // Chunk of a level staged in shared memory: records, child pairs and matrices (post-order: the
@@ -232,8 +230,8 @@ template <int Q, int W>
 struct StageCfg {
     static constexpr int kMatFloats = 2 * Q * W;
     static constexpr int kBytesPerNode = 32 + kMatFloats * 4;
-    static constexpr int kFit = 26 * 1024 / kBytesPerNode;  // nodes per ~26 KB buffer
-    static constexpr int kChunk = kFit >= 128 ? 128 : (kFit >= 4 ? kFit : 4);
+    static constexpr int kFit = 48 * 1024 / kBytesPerNode;  // nodes per ~48 KB buffer
+    static constexpr int kChunk = kFit >= 256 ? 256 : (kFit >= 4 ? kFit : 4);
 };
 
 template <int Q, int W>
@@ -243,14 +241,16 @@ struct __align__(16) Stage {
     float mat[StageCfg<Q, W>::kChunk][StageCfg<Q, W>::kMatFloats];
 };
 
+// Partials are rescaled (by an exact power of two) only below this largest entry.
+constexpr float kRescaleBelow = 0x1p-16f;
+
 // One CTA per pattern range [p0, p0 + np) of one tree.  Its NT threads form G = NT / (np * LPP)
 // node groups; thread t belongs to group t / (np * LPP) and always works on pattern
 // p0 + (t % (np * LPP)) / LPP, so per-pattern sums (scaling exponents, mask corrections) stay
 // in registers for the whole pass.  Group g handles nodes g, g + G, ... of a level, D of them
-// at a time (all loads of the D nodes are issued before any of them is computed).  The range
-// width is chosen by the host so that the ranges of the forest fill the GPU once; a pattern
-// count that is not a multiple of 32 makes warps straddle two or three nodes, which costs
-// nothing but a second shared-memory wavefront for matrix rows.
+// at a time (all loads of the D nodes are issued before any of them is computed).  A pattern
+// count that is not a multiple of 32 makes warps straddle two or three nodes, which costs a
+// second shared-memory wavefront for matrix rows and nothing else.
 template <int Q, int W, int LPP, int NT, int D, int MINB>
 __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     constexpr int S = W / LPP;
@@ -261,10 +261,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     __shared__ int red[NT];
     __shared__ float red_corr[NT];
     __shared__ unsigned diff_red[NT / 32];
-    // dynamic shared memory: two stage buffers, then the top-of-tree rows [n_smem][np][W]
-    extern __shared__ __align__(16) unsigned char dyn_s[];
+    extern __shared__ __align__(16) unsigned char dyn_s[];  // two stage buffers
     Stage<Q, W>* stg = reinterpret_cast<Stage<Q, W>*>(dyn_s);
-    float* top_s = reinterpret_cast<float*>(dyn_s + 2 * sizeof(Stage<Q, W>));
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int part = tid % LPP, j0 = part * S;
@@ -283,9 +281,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         const int P = tr.n_patterns;
         const int np = wi.z;
         const int GP = np * LPP;  // threads per node group
-        // malformed range (checked uniformly by the whole CTA): flag it and skip
-        if (np < 1 || GP > NT || (LPP > 1 && (GP & 31)) ||
-            (int64_t)tr.n_smem * np * W * (int64_t)sizeof(float) > fp.top_bytes) {
+        // malformed range (the same for the whole CTA): flag it and skip
+        if (np < 1 || GP > NT || (LPP > 1 && (GP & 31))) {
             if (tid == 0) set_status(a.status, TT_ERR_INVALID);
             continue;
         }
@@ -297,25 +294,20 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         const bool valid = active && p < P;
         const int pc = p < P ? p : P - 1;
         const int64_t nb = tr.node_base;
+        const int n_int = tr.n_int;
         const int32_t* lev = a.f.level_off + tr.level_base;
         int esum = 0;
         // log-LH correction for masked internal children: TreeTime masks the log message of the
         // child's sum-normalised partial and adds its prefactor unmasked; with power-of-two scaled
         // partials that leaves (1 - m) * log(sum of the scaled partial) to add
         float lcorr = 0.f;
-        const int top = tr.n_int - tr.n_smem;  // local ids >= top live in shared memory
 
         // row k of this thread's pattern: base + k * (P * W) floats
         const int PW = P * W;
         float* const part0 = partial + (tr.prof_base + pc) * W + j0;
         float* const post0 = posterior + (tr.prof_base + pc) * W + j0;
-        const int top_lane = pl * W + j0;
-        const int NPWs = np * W;
         const uint8_t* const codes0 = a.f.tip_codes + tr.tip_base + pc;
         uint8_t* const states0 = a.o.states + tr.state_base + pc;
-        auto top_row = [&](int k) -> float* { return top_s + (k - top) * NPWs + top_lane; };
-        auto prow = [&](int k) -> float* { return k >= top ? top_row(k) : part0 + (int64_t)k * PW; };
-        auto qrow = [&](int k) -> float* { return k >= top ? top_row(k) : post0 + (int64_t)k * PW; };
         auto tip_code = [&](int trow) -> int { return trow < 0 ? 0 : (int)__ldg(codes0 + (int64_t)trow * P); };
         auto lut_part = [&](int code, float (&x)[S]) {
             if constexpr (S == 4) {
@@ -335,7 +327,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 #pragma unroll
             for (int s = 0; s < S; ++s)
                 if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : (m == 1.f ? msg[s] : exp2f(m * log2f(msg[s])));
-            if (c < tr.n_int) {
+            if (c < n_int) {
                 float xs = 0.f;
 #pragma unroll
                 for (int s = 0; s < S; ++s) xs += x[s];
@@ -381,14 +373,10 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                 int nh = h, nbase = base + CH;
                 if (nbase >= hi) { nh = h + 1; nbase = nh < tr.n_levels ? __ldg(lev + nh) : 0; }
                 const bool has_next = nh < tr.n_levels;
-                __syncthreads();  // buffer b^1 is free (its chunk was computed)
-                if (has_next) {
-                    stage(b ^ 1, nbase, min(CH, __ldg(lev + nh + 1) - nbase), true);
-                    cp_async_wait<1>();
-                } else {
-                    cp_async_wait<0>();
-                }
-                __syncthreads();  // chunk b staged; the previous level's rows are written
+                cp_async_wait<0>();  // this thread's copies of the chunk have landed
+                __syncthreads();     // everybody's copies and the previous chunk's rows are visible;
+                                     // buffer b^1 (the previous chunk's) is free
+                if (has_next) stage(b ^ 1, nbase, min(CH, __ldg(lev + nh + 1) - nbase), true);
                 const Stage<Q, W>& st = stg[b];
                 for (int i0 = first; i0 < cnt; i0 += GD) {
                     // loads of D nodes first
@@ -400,14 +388,13 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         const int i = i0 + d * G;
                         bin[d] = false;
                         if (i < cnt) {
-                            const int4 rec = st.rec[i];
-                            if (rec.y - rec.x == 2) {
+                            const int4 cp = st.pair[i];
+                            if (cp.x >= 0) {
                                 bin[d] = true;
-                                const int4 cp = st.pair[i];
-                                ca[d] = cp.x >= tr.n_int ? tip_code(cp.y) : -1;
-                                cb[d] = cp.z >= tr.n_int ? tip_code(cp.w) : -1;
-                                if (cp.x < tr.n_int) ld_part<S>(prow(cp.x), xa[d]);
-                                if (cp.z < tr.n_int) ld_part<S>(prow(cp.z), xb[d]);
+                                ca[d] = cp.x >= n_int ? tip_code(cp.y) : -1;
+                                cb[d] = cp.z >= n_int ? tip_code(cp.w) : -1;
+                                if (cp.x < n_int) ld_part<S>(part0 + (int64_t)cp.x * PW, xa[d]);
+                                if (cp.z < n_int) ld_part<S>(part0 + (int64_t)cp.z * PW, xb[d]);
                             }
                         }
                     }
@@ -417,7 +404,6 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         if (i >= cnt) continue;
                         const int k = base + i;
                         float r[S];
-                        int extra = 0;
                         if (bin[d]) {
                             if (ca[d] >= 0) lut_part(ca[d], xa[d]);
                             if (cb[d] >= 0) lut_part(cb[d], xb[d]);
@@ -439,8 +425,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                             for (int ci = rec.x; ci < rec.y; ++ci) {
                                 const int c = __ldg(a.f.child_idx + ci);
                                 float x[S], m0[S];
-                                if (c >= tr.n_int) lut_part(tip_code(__ldg(a.f.tip_row + nb + c)), x);
-                                else ld_part<S>(prow(c), x);
+                                if (c >= n_int) lut_part(tip_code(__ldg(a.f.tip_row + nb + c)), x);
+                                else ld_part<S>(part0 + (int64_t)c * PW, x);
                                 f_vec_mat<Q, W, LPP>(x, pm + (nb + c) * QW, j0, m0);
                                 if (has_masks) apply_mask(c, x, m0);
 #pragma unroll
@@ -449,10 +435,10 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 #pragma unroll
                                 for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
                                 mx = group_max<LPP>(mx);
-                                if (mx < 0x1p-64f) {  // many children: keep the running product in range
+                                if (mx < kRescaleBelow) {  // many children: keep the running product in range
                                     const int e = pow2_exponent(mx);
                                     scale_pow2<S>(r, e);
-                                    extra += e;
+                                    esum += e;
                                 }
                             }
                         }
@@ -460,10 +446,11 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 #pragma unroll
                         for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
                         mx = group_max<LPP>(mx);
-                        const int e = pow2_exponent(mx);
-                        scale_pow2<S>(r, e);
-                        esum += e + extra;
-                        if (k >= top) st_part<S>(top_row(k), r);
+                        if (mx < kRescaleBelow) {
+                            const int e = pow2_exponent(mx);
+                            scale_pow2<S>(r, e);
+                            esum += e;
+                        }
                         if (valid) st_part<S>(part0 + (int64_t)k * PW, r);
                     }
                 }
@@ -476,7 +463,21 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         // per-pattern exponent sums: lanes of one pattern hold identical values; groups add up
         red[tid] = esum;
         red_corr[tid] = lcorr;
-        __syncthreads();
+        __syncthreads();  // also: every thread is done with the post-order stage buffers
+
+        // pre-order levels n_levels-2 .. 0, then the tips as level -1; the first chunk's copies
+        // overlap the root step
+        unsigned ndiff = 0;
+        const bool do_tips = a.o.reconstruct_tips || a.o.tip_outgroup;
+        const bool count_diff = a.o.count_diff != 0;
+        const bool keep_outgroup = a.o.outgroup != nullptr || a.o.tip_outgroup != nullptr;
+        const int h_last = do_tips ? -1 : 0;
+        auto lv_lo = [&](int h) { return h >= 0 ? __ldg(lev + h) : n_int; };
+        auto lv_hi = [&](int h) { return h >= 0 ? __ldg(lev + h + 1) : n_int + tr.n_tip; };
+        int h = tr.n_levels - 2;
+        bool have = h >= h_last;
+        int base = have ? lv_lo(h) : 0;
+        if (have) stage(0, base, min(CH, lv_hi(h) - base), false);
 
         // ------------------------------------------------------------------ root
         if (tid < GP) {  // group 0 (whole warps when LPP > 1)
@@ -486,10 +487,10 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                 tot += red[gg * GP + tid];
                 corr += (double)red_corr[gg * GP + tid];
             }
-            const int kr = tr.n_int - 1;
+            const int kr = n_int - 1;
             const double* pi = a.pi + (int64_t)tr.model * Q;
             float x[S], pr[S];
-            ld_part<S>(prow(kr), x);
+            ld_part<S>(part0 + (int64_t)kr * PW, x);
             float s_loc = 0.f;
 #pragma unroll
             for (int s = 0; s < S; ++s) {
@@ -511,7 +512,6 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
             } else {
                 st = group_argmax<Q, W, LPP>(pr, j0);
             }
-            if (kr >= top) st_part<S>(top_row(kr), pr);
             if (valid) {
                 st_part<S>(post0 + (int64_t)kr * PW, pr);
                 if (part == 0) {
@@ -529,19 +529,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         }
 
         // ------------------------------------------------------------- pre-order
-        unsigned ndiff = 0;
-        const bool do_tips = a.o.reconstruct_tips || a.o.tip_outgroup;
-        const bool count_diff = a.o.count_diff != 0;
-        const int h_last = do_tips ? -1 : 0;
         {
-            // levels n_levels-2 .. 0, then the tips as level -1
-            auto lv_lo = [&](int h) { return h >= 0 ? __ldg(lev + h) : tr.n_int; };
-            auto lv_hi = [&](int h) { return h >= 0 ? __ldg(lev + h + 1) : tr.n_int + tr.n_tip; };
-            int h = tr.n_levels - 2, b = 0;
-            bool have = h >= h_last;
-            int base = have ? lv_lo(h) : 0;
-            __syncthreads();  // root row written; stage buffers free
-            if (have) stage(0, base, min(CH, lv_hi(h) - base), false);
+            int b = 0;
             while (have) {
                 const int hi = lv_hi(h);
                 const int cnt = min(CH, hi - base);
@@ -549,14 +538,9 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                 int nh = h, nbase = base + CH;
                 if (nbase >= hi) { nh = h - 1; nbase = nh >= h_last ? lv_lo(nh) : 0; }
                 const bool has_next = nh >= h_last;
-                __syncthreads();
-                if (has_next) {
-                    stage(b ^ 1, nbase, min(CH, lv_hi(nh) - nbase), false);
-                    cp_async_wait<1>();
-                } else {
-                    cp_async_wait<0>();
-                }
-                __syncthreads();
+                cp_async_wait<0>();
+                __syncthreads();  // chunk staged; the parents' rows (and the root's) are written
+                if (has_next) stage(b ^ 1, nbase, min(CH, lv_hi(nh) - nbase), false);
                 const Stage<Q, W>& st = stg[b];
                 for (int i0 = first; i0 < cnt; i0 += GD) {
                     float pv[D][S], x[D][S];
@@ -568,9 +552,9 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         old[d] = 0;
                         if (i < cnt) {
                             const int4 rec = st.rec[i];
-                            ld_part<S>(qrow(rec.z), pv[d]);
+                            ld_part<S>(post0 + (int64_t)rec.z * PW, pv[d]);
                             if (tips) code[d] = tip_code(rec.w);
-                            else ld_part<S>(prow(base + i), x[d]);
+                            else ld_part<S>(part0 + (int64_t)(base + i) * PW, x[d]);
                             if (count_diff && valid && part == 0) old[d] = states0[(int64_t)(base + i) * P];
                         }
                     }
@@ -579,14 +563,13 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         const int i = i0 + d * G;
                         if (i >= cnt) continue;
                         const int k = base + i;
-                        const int64_t gk = nb + k;
                         if (tips) lut_part(code[d], x[d]);
                         const float* Pk = &st.mat[i][0];
                         float msg[S], o[S];
                         s_vec_mat<Q, W, LPP>(x[d], Pk, j0, msg);
                         float m = 1.f;
                         if (has_masks) {
-                            const int64_t mo = __ldg(a.f.mask_off + gk);
+                            const int64_t mo = __ldg(a.f.mask_off + nb + k);
                             if (mo >= 0) m = (float)__ldg(a.f.masks + mo + pc);
                         }
                         if (m != 1.f) {
@@ -595,21 +578,24 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                                 if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
                         }
                         // outgroup message: parent's posterior divided by this node's message
-                        // (fast division, <= 2 ulp; the result is renormalised right away)
-                        float sl = 0.f;
+                        // (fast division, <= 2 ulp).  Its scale cancels in the posterior, so it is
+                        // normalised only when it is stored.
 #pragma unroll
-                        for (int s = 0; s < S; ++s) {
+                        for (int s = 0; s < S; ++s)
                             o[s] = (j0 + s < Q) ? __fdividef(fmaxf(1e-12f, pv[d][s]), msg[s]) : 0.f;
-                            sl += o[s];
-                        }
-                        const float inv = __fdividef(1.f, group_sum<LPP>(sl));
+                        if (keep_outgroup) {
+                            float sl = 0.f;
 #pragma unroll
-                        for (int s = 0; s < S; ++s) o[s] *= inv;
-                        const int64_t row = tips ? (tr.tipprof_base + (int64_t)(k - tr.n_int) * P + pc) * W + j0
-                                                 : (tr.prof_base + (int64_t)k * P + pc) * W + j0;
-                        if (valid) {
-                            float* og = reinterpret_cast<float*>(tips ? a.o.tip_outgroup : a.o.outgroup);
-                            if (og) st_part<S>(og + row, o);
+                            for (int s = 0; s < S; ++s) sl += o[s];
+                            const float inv = __fdividef(1.f, group_sum<LPP>(sl));
+#pragma unroll
+                            for (int s = 0; s < S; ++s) o[s] *= inv;
+                            if (valid) {
+                                float* og = reinterpret_cast<float*>(tips ? a.o.tip_outgroup : a.o.outgroup);
+                                const int64_t row = tips ? (tr.tipprof_base + (int64_t)(k - n_int) * P + pc) * W + j0
+                                                         : (tr.prof_base + (int64_t)k * P + pc) * W + j0;
+                                if (og) st_part<S>(og + row, o);
+                            }
                         }
                         if (tips && !a.o.reconstruct_tips) continue;
                         float ev[S];
@@ -625,10 +611,13 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 #pragma unroll
                         for (int s = 0; s < S; ++s) x[d][s] *= inv2;
                         const int stt = group_argmax<Q, W, LPP>(x[d], j0);
-                        if (!tips && k >= top) st_part<S>(top_row(k), x[d]);  // partial slot -> posterior
                         if (valid) {
-                            float* dst = tips ? reinterpret_cast<float*>(a.o.tip_posterior) : posterior;
-                            if (dst) st_part<S>(dst + row, x[d]);
+                            if (tips) {
+                                st_part<S>(reinterpret_cast<float*>(a.o.tip_posterior) +
+                                               (tr.tipprof_base + (int64_t)(k - n_int) * P + pc) * W + j0, x[d]);
+                            } else {
+                                st_part<S>(post0 + (int64_t)k * PW, x[d]);
+                            }
                             if (part == 0) {
                                 if (count_diff) ndiff += (old[d] != (unsigned)stt);
                                 states0[(int64_t)k * P] = (uint8_t)stt;
@@ -661,7 +650,7 @@ template <int Q, int LPP, int NT, int D, int MINB>
 static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
     constexpr int W = round4(Q);
     static_assert(W % LPP == 0, "width must split over the lanes of a pattern");
-    const size_t dyn = 2 * sizeof(Stage<Q, W>) + (size_t)prm.top_bytes;
+    const size_t dyn = 2 * sizeof(Stage<Q, W>);
     // static + dynamic shared memory past 48 KB needs the opt-in, once per device
     static size_t configured[64] = {};
     int dev = 0;
@@ -680,13 +669,12 @@ static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
 }
 
 tt_status launch_marginal_f32(int q, int threads, const MargParams& prm, const int4* items, const int4* node_rec,
-                              const int4* child_pair, const float* p32_pair, int top_bytes, int blocks,
-                              cudaStream_t s) {
-    F32Params fp{prm, items, node_rec, child_pair, p32_pair, top_bytes};
+                              const int4* child_pair, const float* p32_pair, int blocks, cudaStream_t s) {
+    F32Params fp{prm, items, node_rec, child_pair, p32_pair};
     switch (q) {
         case 4:
             return threads == 512 ? launch_f32<4, 1, 512, 2, 1>(fp, blocks, s) : launch_f32<4, 1, 1024, 1, 1>(fp, blocks, s);
-        case 5: return launch_f32<5, 1, 1024, 1, 1>(fp, blocks, s);
+        case 5: return launch_f32<5, 1, 512, 2, 1>(fp, blocks, s);
         case 20: return launch_f32<20, 4, 512, 1, 1>(fp, blocks, s);
         case 21: return launch_f32<21, 4, 512, 1, 1>(fp, blocks, s);
         case 22: return launch_f32<22, 4, 512, 1, 1>(fp, blocks, s);
@@ -698,7 +686,7 @@ tt_status launch_marginal_f32(int q, int threads, const MargParams& prm, const i
 
 int marginal_f32_threads(int q, int requested) {
     if (q == 4) return requested == 512 ? 512 : 1024;
-    if (q == 5) return 1024;
+    if (q == 5) return 512;
     return 512;
 }
 

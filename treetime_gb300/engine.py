@@ -264,7 +264,7 @@ class Forest:
     C-ABI struct that points at them."""
 
     def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, threads=None,
-                 smem_bytes=None, range_patterns=None, ranges_per_sm=1):
+                 range_patterns=None, ranges_per_sm=1):
         dev = require_device(device)
         self.device = dev
         self.inputs = list(inputs)
@@ -274,7 +274,7 @@ class Forest:
                                              ("node_base", "level_base", "pat_base", "tip_base", "prof_base",
                                               "tipprof_base", "state_base")] +
                          [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model",
-                                                   "n_smem")])
+                                                   "reserved")])
         node_base = level_base = pat_base = tip_base = prof_base = tipprof_base = state_base = 0
         lev, coff, cidx, par, trow, bl, mult, codes, moff, mvals = [], [], [], [], [], [], [], [], [], []
         mask_elems = 0
@@ -341,9 +341,9 @@ class Forest:
         # 20+.  Range widths make the ranges of the forest fill the GPU once (ranges_per_sm
         # CTAs per SM): each tree gets the width whose node x pattern work is one CTA's share.
         lanes_per_pattern = 4 if q >= 20 else 1
-        if q >= 20:
-            threads = 512
-        elif q == 5 or threads is None:
+        if q != 4:
+            threads = 512  # the only shape compiled for 5 and 20+ states
+        elif threads is None:
             threads = 1024
         if threads not in (512, 1024):
             raise ValueError("threads must be 512 or 1024")
@@ -375,18 +375,6 @@ class Forest:
                 ranges.append((N * min(w_, P - p0), t, int(p0), int(w_)))
         ranges.sort(key=lambda r: -r[0])
         self.work_f32_host = np.array([(t, p0, w_, 0) for _, t, p0, w_ in ranges], dtype=np.int32).reshape(-1, 4)
-        # top of each tree kept in shared memory by the FP32 kernel: as many of the highest
-        # internal nodes as fit the budget (rows of range-width patterns x width floats)
-        if smem_bytes is None:
-            smem_bytes = 48 * 1024
-        top_bytes = 0
-        n_smem = np.zeros(len(inputs), dtype=np.int32)
-        for t in range(len(inputs)):
-            per_node = widths[t] * self.w * 4
-            n_smem[t] = min(int(trees["n_int"][t]), int(smem_bytes) // per_node) if smem_bytes > 0 else 0
-            top_bytes = max(top_bytes, int(n_smem[t]) * per_node)
-        trees["n_smem"] = n_smem
-        self.smem_top_bytes = top_bytes
         self.trees_host = trees
         self.n_nodes = node_base
         self.n_patterns = pat_base
@@ -420,7 +408,7 @@ class Forest:
             _p(self.d_child_idx), _p(self.d_parent), _p(self.d_tip_row), _p(self.d_mask_off), _p(self.d_masks),
             _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
             warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host),
-            self.smem_top_bytes, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), threads, 0)
+            0, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), threads, 0)
 
     def set_branch_lengths(self, bl_list):
         """Replace branch lengths (same topology) without rebuilding."""
@@ -641,7 +629,7 @@ def _mini_forest(n_nodes, q, bl, device, mult=None, parent=None, n_int=None, P=1
     dev = require_device(device)
     tr = np.zeros(1, dtype=[(n, np.int64) for n in ("node_base", "level_base", "pat_base", "tip_base", "prof_base",
                                                     "tipprof_base", "state_base")] +
-                  [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model", "n_smem")])
+                  [(n, np.int32) for n in ("n_int", "n_tip", "n_levels", "n_patterns", "model", "reserved")])
     tr[0] = (0, 0, 0, 0, 0, 0, 0, n_nodes if n_int is None else n_int, 0, 0, P, 0, 0)
     keep = {"trees": _to_dev(tr.view(np.uint8), dev), "bl": _to_dev(np.asarray(bl, np.float64), dev)}
     keep["parent"] = _to_dev(np.asarray(parent if parent is not None else np.full(n_nodes, -1), np.int32), dev)

@@ -148,7 +148,8 @@ def run_gpu(args):
     # launch shape of the FP32 kernel picked by the autotuner (outside the timed region)
     from treetime_gb300 import autotune
     best, table = autotune.tune(sess["forest"].inputs, 4, model, device=dev, use_cache=False)
-    forest = engine.Forest(sess["forest"].inputs, 4, device=dev, threads=best[0], ranges_per_sm=best[1])
+    forest = engine.Forest(sess["forest"].inputs, 4, device=dev, threads=best[0], ctas_per_sm=best[1],
+                           ranges_per_sm=best[2])
     bufs = engine.Buffers(forest)
     P = t.data.compressed_length
     N = layout.n_nodes
@@ -244,14 +245,15 @@ def run_gpu(args):
         "rel_logLH_err_vs_fp64": rel_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,D=%d>" % (forest.threads, 2 if forest.threads == 512 else 1),
+                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d,PIPE=%d>" % (
+                         forest.threads, forest.ctas_per_sm, int(forest.threads == 512 and forest.ctas_per_sm == 1)),
                      "ranges": int(len(forest.work_f32_host)),
                      "range_patterns": int(forest.work_f32_host[:, 2].max()),
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms},
         "e2e": {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms},
         "gpu_launches": 3 * args.steps,
-        "autotune": {"best": {"threads": best[0], "ranges_per_sm": best[1]},
+        "autotune": {"best": {"threads": best[0], "ctas_per_sm": best[1], "ranges_per_sm": best[2]},
                      "ms": table},
         "clocks": clocks,
     }

@@ -124,7 +124,9 @@ typedef struct tt_forest {
                                   has exactly two children, -1 otherwise (see tt_pmats.p32_pair)  */
     int32_t threads_f32;       /* CTA size of the FP32 marginal kernel for 4 states: 512 or 1024
                                   (other values: 1024); 5 and 20-22 states always use 512         */
-    int32_t reserved2;
+    int32_t ctas_per_sm_f32;   /* 4 states with 512 threads: 2 = two CTAs share an SM (64 registers
+                                  per thread), otherwise one CTA per SM with software-pipelined
+                                  node loads (128 registers per thread)                            */
 } tt_forest;
 
 typedef struct tt_model {

@@ -37,24 +37,30 @@ def _oracle(t):
                         reconstruct_tip_states=True)
 
 
-SHAPES = [(1024, None), (512, None), (1024, 1), (1024, 7), (512, 19), (1024, 32), (1024, 100), (512, 512),
-          ("f64", 8), ("f64", 32)]
+SHAPES = [(1024, None), (512, None), ("512x2", None), (1024, 1), (1024, 7), (512, 19), ("512x2", 19), (1024, 32),
+          ("512x2", 32), (1024, 100), (512, 512), ("f64", 8), ("f64", 32)]
 
 
 @pytest.mark.parametrize("alphabet", ["nuc_nogap", "nuc", "aa_nogap", "aa"])
 @pytest.mark.parametrize("shape", SHAPES)
 def test_marginal_launch_shapes(alphabet, shape):
-    """shape = (CTA threads, patterns per range; None = sized to fill the GPU)
+    """shape = (CTA threads, or "512x2" for two 512-thread CTAs per SM;
+    patterns per range, None = sized to fill the GPU)
     or ("f64", warps per CTA).  Range widths that do not divide the
     pattern count, one-pattern ranges and ranges wider than the alignment are
     all covered."""
     from treetime_gb300 import TreeAnc
     threads, rp = shape
-    if alphabet.startswith("aa") and (threads == 1024 or (threads == "f64" and rp == 32)):
+    if alphabet.startswith("aa") and (threads in (1024, "512x2") or (threads == "f64" and rp == 32)):
         pytest.skip("20+ states run 512-thread CTAs (ranges rounded up to multiples of 8 patterns)")
     wl = _workload(alphabet, seed=7, L=300 if not alphabet.startswith("aa") else 120)
     prec = "f64" if threads == "f64" else "f32"
-    kw = dict(warps_per_block=rp) if prec == "f64" else dict(threads=threads, range_patterns=rp)
+    if prec == "f64":
+        kw = dict(warps_per_block=rp)
+    elif threads == "512x2":
+        kw = dict(threads=512, ctas_per_sm=2, range_patterns=rp)
+    else:
+        kw = dict(threads=threads, range_patterns=rp)
     t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision=prec, **kw)
     rng = np.random.default_rng(1)
     for n in list(t.tree.find_clades())[3:9]:

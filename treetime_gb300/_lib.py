@@ -38,7 +38,7 @@ class TTForest(C.Structure):
                 ("work", vp), ("n_work", i32), ("warps_per_block", i32), ("max_blocks", i32),
                 ("lanes_per_pattern", i32), ("work_f32", vp), ("n_work_f32", i32), ("reserved1", i32),
                 ("node_rec", vp), ("child_pair", vp), ("pair_slot", vp), ("threads_f32", i32),
-                ("reserved2", i32)]
+                ("ctas_per_sm_f32", i32)]
 
 
 class TTModel(C.Structure):

@@ -175,6 +175,7 @@ class GPUAncMixin:
         forest = engine.Forest([ti], self.gtr.n_states, device=device,
                                threads=getattr(self, "threads", None),
                                warps_per_block=getattr(self, "warps_per_block", None),
+                               ctas_per_sm=getattr(self, "ctas_per_sm", None) or 1,
                                range_patterns=getattr(self, "range_patterns", None))
         model = None if self.gtr.is_site_specific else engine.model_for(self.gtr, device)
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,

@@ -1,8 +1,9 @@
 """Autotuner for the FP32 marginal kernel's launch shape.
 
-The best shape depends on the workload: the CTA size (512 or 1024 threads) and
-how many pattern ranges the forest is cut into per SM (one wide range per SM,
-or two narrower ones queued behind each other).  ``tune`` times every candidate on the actual forest
+The best shape depends on the workload: the CTA size and residency (1024
+threads, one CTA per SM; 512 threads, two CTAs per SM; 512 threads, one CTA
+per SM with software-pipelined loads) and how many pattern ranges the forest
+is cut into per SM (one wide range per SM, or two narrower ones).  ``tune`` times every candidate on the actual forest
 with CUDA events and returns the fastest; results are cached in memory and in
 a JSON file keyed by a coarse workload signature (alphabet size, number of
 trees, node and pattern counts rounded to powers of two).
@@ -15,7 +16,7 @@ import statistics
 
 from . import engine
 
-CANDIDATES = [(threads, rps) for threads in (512, 1024) for rps in (1, 2)]
+CANDIDATES = [(threads, ctas, rps) for threads, ctas in ((1024, 1), (512, 2), (512, 1)) for rps in (1, 2)]
 _CACHE = {}
 CACHE_PATH = os.environ.get("TREETIME_GB300_TUNE_CACHE",
                             os.path.join(os.path.expanduser("~"), ".cache", "treetime_gb300", "autotune.json"))
@@ -46,8 +47,8 @@ def _save_file(d):
 
 
 def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True):
-    """Fastest (threads, ranges_per_sm) for this forest and the table of
-    median times (ms) of all candidates."""
+    """Fastest (threads, ctas_per_sm, ranges_per_sm) for this forest and the
+    table of median times (ms) of all candidates."""
     key = signature(inputs, q)
     if use_cache:
         if key in _CACHE:
@@ -59,11 +60,11 @@ def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True)
     t = engine.torch()
     cands = candidates or CANDIDATES
     if q != 4:
-        cands = [c for c in cands if c[0] == 512]
+        cands = [c for c in cands if c[:2] == (512, 1)]
     table = {}
-    for threads, rps in cands:
+    for threads, ctas, rps in cands:
         try:
-            f = engine.Forest(inputs, q, device=device, threads=threads, ranges_per_sm=rps)
+            f = engine.Forest(inputs, q, device=device, threads=threads, ctas_per_sm=ctas, ranges_per_sm=rps)
             bufs = engine.Buffers(f)
             for _ in range(2):
                 engine.marginal(f, model, bufs, precision="f32", sync=False)
@@ -76,9 +77,9 @@ def tune(inputs, q, model, device=None, candidates=None, reps=7, use_cache=True)
                 b.record()
                 b.synchronize()
                 times.append(a.elapsed_time(b))
-            table["%d/%d" % (threads, rps)] = statistics.median(times)
+            table["%d/%d/%d" % (threads, ctas, rps)] = statistics.median(times)
         except Exception as e:  # a shape that cannot launch (e.g. too much shared memory) is skipped
-            table["%d/%d" % (threads, rps)] = None
+            table["%d/%d/%d" % (threads, ctas, rps)] = None
     ok = {k: v for k, v in table.items() if v is not None}
     best = tuple(int(x) for x in min(ok, key=ok.get).split("/"))
     _CACHE[key] = (best, table)

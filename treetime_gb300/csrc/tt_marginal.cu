@@ -72,7 +72,7 @@ extern "C" tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt
         }
         prm.n_items = f->n_work_f32;
         blocks = f->max_blocks > 0 && f->max_blocks < f->n_work_f32 ? f->max_blocks : f->n_work_f32;
-        st = launch_marginal_f32(f->n_states, marginal_f32_threads(f->n_states, f->threads_f32), prm,
+        st = launch_marginal_f32(f->n_states, marginal_f32_threads(f->n_states, f->threads_f32), f->ctas_per_sm_f32, prm,
                                  reinterpret_cast<const int4*>(f->work_f32), reinterpret_cast<const int4*>(f->node_rec),
                                  reinterpret_cast<const int4*>(f->child_pair), pm->p32_pair, blocks, s);
     } else if (precision == TT_PREC_F64) {

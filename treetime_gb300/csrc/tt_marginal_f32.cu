@@ -24,7 +24,6 @@
 
 namespace tt {
 
-constexpr int kChunk = 256;
 
 template <int S>
 __device__ __forceinline__ void ld_part(const float* __restrict__ p, float (&r)[S]) {
@@ -668,12 +667,17 @@ static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
     return check_launch("tt_marginal(f32)");
 }
 
-tt_status launch_marginal_f32(int q, int threads, const MargParams& prm, const int4* items, const int4* node_rec,
-                              const int4* child_pair, const float* p32_pair, int blocks, cudaStream_t s) {
+tt_status launch_marginal_f32(int q, int threads, int ctas_per_sm, const MargParams& prm, const int4* items,
+                              const int4* node_rec, const int4* child_pair, const float* p32_pair, int blocks,
+                              cudaStream_t s) {
     F32Params fp{prm, items, node_rec, child_pair, p32_pair};
     switch (q) {
         case 4:
-            return threads == 512 ? launch_f32<4, 1, 512, 2, 1>(fp, blocks, s) : launch_f32<4, 1, 1024, 1, 1>(fp, blocks, s);
+            // 1024 threads, one CTA per SM; 512 threads, two CTAs per SM (64 registers each); or
+            // 512 threads, one CTA per SM, two nodes per group at a time (128 registers)
+            if (threads == 512)
+                return ctas_per_sm == 2 ? launch_f32<4, 1, 512, 1, 2>(fp, blocks, s) : launch_f32<4, 1, 512, 2, 1>(fp, blocks, s);
+            return launch_f32<4, 1, 1024, 1, 1>(fp, blocks, s);
         case 5: return launch_f32<5, 1, 512, 2, 1>(fp, blocks, s);
         case 20: return launch_f32<20, 4, 512, 1, 1>(fp, blocks, s);
         case 21: return launch_f32<21, 4, 512, 1, 1>(fp, blocks, s);

@@ -393,8 +393,9 @@ tt_status launch_marginal(const MargParams& prm, int blocks, cudaStream_t s) {
 }
 
 // Instantiated in tt_marginal_f32.cu / tt_marginal_f64.cu.
-tt_status launch_marginal_f32(int q, int threads, const MargParams& prm, const int4* items, const int4* node_rec,
-                              const int4* child_pair, const float* p32_pair, int blocks, cudaStream_t s);
+tt_status launch_marginal_f32(int q, int threads, int ctas_per_sm, const MargParams& prm, const int4* items,
+                              const int4* node_rec, const int4* child_pair, const float* p32_pair, int blocks,
+                              cudaStream_t s);
 int marginal_f32_threads(int q, int requested);  // CTA size the FP32 kernel uses for q states
 int marginal_f32_lanes(int q);                   // lanes per pattern of the FP32 kernel
 tt_status launch_marginal_f64(int q, int warps, const MargParams& prm, int blocks, cudaStream_t s);

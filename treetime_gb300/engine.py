@@ -264,7 +264,7 @@ class Forest:
     C-ABI struct that points at them."""
 
     def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, threads=None,
-                 range_patterns=None, ranges_per_sm=1):
+                 ctas_per_sm=1, range_patterns=None, ranges_per_sm=1):
         dev = require_device(device)
         self.device = dev
         self.inputs = list(inputs)
@@ -347,8 +347,11 @@ class Forest:
             threads = 1024
         if threads not in (512, 1024):
             raise ValueError("threads must be 512 or 1024")
+        if ctas_per_sm not in (1, 2):
+            raise ValueError("ctas_per_sm must be 1 or 2")
         self.lanes_per_pattern = lanes_per_pattern
         self.threads = threads
+        self.ctas_per_sm = ctas_per_sm if (q == 4 and threads == 512) else 1
         max_np = threads // lanes_per_pattern
         unit = 32 // lanes_per_pattern if lanes_per_pattern > 1 else 1
         slots = max(1, sms * max(1, int(ranges_per_sm)))
@@ -408,7 +411,7 @@ class Forest:
             _p(self.d_child_idx), _p(self.d_parent), _p(self.d_tip_row), _p(self.d_mask_off), _p(self.d_masks),
             _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
             warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host),
-            0, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), threads, 0)
+            0, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), threads, self.ctas_per_sm)
 
     def set_branch_lengths(self, bl_list):
         """Replace branch lengths (same topology) without rebuilding."""

@@ -67,7 +67,7 @@ class TreeAnc(GPUAncMixin):
     def __init__(self, tree=None, aln=None, gtr=None, fill_overhangs=True, ref=None, verbose=ttconf.VERBOSE,
                  ignore_gaps=True, convert_upper=True, seq_multiplicity=None, log=None, compress=True, seq_len=None,
                  ignore_missing_alns=False, keep_node_order=False, rng_seed=None, precision="f64", device=None,
-                 threads=None, warps_per_block=None, range_patterns=None, **kwargs):
+                 threads=None, ctas_per_sm=None, warps_per_block=None, range_patterns=None, **kwargs):
         if tree is None:
             raise TypeError("TreeAnc requires a tree!")
         if precision not in ("f64", "f32"):
@@ -93,6 +93,7 @@ class TreeAnc(GPUAncMixin):
         self.threads = threads
         self.warps_per_block = warps_per_block
         self.range_patterns = range_patterns
+        self.ctas_per_sm = ctas_per_sm
         self._session = None
         self._topology_version = 0
         self._tree = None

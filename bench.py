@@ -75,7 +75,7 @@ class ClockSampler:
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -245,8 +245,7 @@ def run_gpu(args):
         "rel_logLH_err_vs_fp64": rel_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d,PIPE=%d>" % (
-                         forest.threads, forest.ctas_per_sm, int(forest.threads == 512 and forest.ctas_per_sm == 1)),
+                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d>" % (forest.threads, forest.ctas_per_sm),
                      "ranges": int(len(forest.work_f32_host)),
                      "range_patterns": int(forest.work_f32_host[:, 2].max()),
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms},
@@ -402,7 +401,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

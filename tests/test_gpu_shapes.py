@@ -52,7 +52,7 @@ def test_marginal_launch_shapes(alphabet, shape):
     from treetime_gb300 import TreeAnc
     threads, rp = shape
     if alphabet.startswith("aa") and (threads in (1024, "512x2") or (threads == "f64" and rp == 32)):
-        pytest.skip("20+ states run 512-thread CTAs (ranges rounded up to multiples of 8 patterns)")
+        pytest.skip("20+ states run 512-thread CTAs, one pattern per 4 lanes (ranges rounded up to 8 patterns)")
     wl = _workload(alphabet, seed=7, L=300 if not alphabet.startswith("aa") else 120)
     prec = "f64" if threads == "f64" else "f32"
     if prec == "f64":

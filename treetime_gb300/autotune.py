@@ -2,8 +2,8 @@
 
 The best shape depends on the workload: the CTA size and residency (1024
 threads, one CTA per SM; 512 threads, two CTAs per SM; 512 threads, one CTA
-per SM with software-pipelined loads) and how many pattern ranges the forest
-is cut into per SM (one wide range per SM, or two narrower ones).  ``tune`` times every candidate on the actual forest
+per SM with two nodes per group at a time) and how many pattern ranges the
+forest is cut into per SM (one wide range per SM, or two narrower ones).  ``tune`` times every candidate on the actual forest
 with CUDA events and returns the fastest; results are cached in memory and in
 a JSON file keyed by a coarse workload signature (alphabet size, number of
 trees, node and pattern counts rounded to powers of two).

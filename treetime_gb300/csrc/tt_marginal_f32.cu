@@ -20,228 +20,9 @@
 //     previous chunk wrote, and the next chunk's copies are issued right after it).  The
 //     children's matrices of a two-child node lie side by side in p32_pair so that a chunk is one
 //     contiguous copy.
-#include "tt_marginal_kernels.cuh"
+#include "tt_marginal_f32.cuh"
 
 namespace tt {
-
-
-template <int S>
-__device__ __forceinline__ void ld_part(const float* __restrict__ p, float (&r)[S]) {
-    if constexpr (S == 4) {
-        float4 v = *reinterpret_cast<const float4*>(p);
-        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
-    } else if constexpr (S == 2) {
-        float2 v = *reinterpret_cast<const float2*>(p);
-        r[0] = v.x; r[1] = v.y;
-    } else if constexpr (S % 4 == 0) {
-#pragma unroll
-        for (int k = 0; k < S; k += 4) {
-            float4 v = *reinterpret_cast<const float4*>(p + k);
-            r[k] = v.x; r[k + 1] = v.y; r[k + 2] = v.z; r[k + 3] = v.w;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < S; ++k) r[k] = p[k];
-    }
-}
-
-template <int S>
-__device__ __forceinline__ void ld_part_ro(const float* __restrict__ p, float (&r)[S]) {
-    if constexpr (S == 4) {
-        float4 v = __ldg(reinterpret_cast<const float4*>(p));
-        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
-    } else if constexpr (S == 2) {
-        float2 v = __ldg(reinterpret_cast<const float2*>(p));
-        r[0] = v.x; r[1] = v.y;
-    } else if constexpr (S % 4 == 0) {
-#pragma unroll
-        for (int k = 0; k < S; k += 4) {
-            float4 v = __ldg(reinterpret_cast<const float4*>(p + k));
-            r[k] = v.x; r[k + 1] = v.y; r[k + 2] = v.z; r[k + 3] = v.w;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < S; ++k) r[k] = __ldg(p + k);
-    }
-}
-
-template <int S>
-__device__ __forceinline__ void st_part(float* __restrict__ p, const float (&r)[S]) {
-    if constexpr (S == 4) {
-        *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
-    } else if constexpr (S == 2) {
-        *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
-    } else if constexpr (S % 4 == 0) {
-#pragma unroll
-        for (int k = 0; k < S; k += 4) *reinterpret_cast<float4*>(p + k) = make_float4(r[k], r[k + 1], r[k + 2], r[k + 3]);
-    } else {
-#pragma unroll
-        for (int k = 0; k < S; ++k) p[k] = r[k];
-    }
-}
-
-template <int LPP>
-__device__ __forceinline__ float group_max(float v) {
-#pragma unroll
-    for (int o = LPP / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-template <int LPP>
-__device__ __forceinline__ float group_sum(float v) {
-#pragma unroll
-    for (int o = LPP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// msg[s] = sum_i x_i P[i][j0+s]: lane holds x for states j0..j0+S-1 of its pattern
-template <int Q, int W, int LPP>
-__device__ __forceinline__ void f_vec_mat(const float (&x)[W / LPP], const float* __restrict__ P, int j0,
-                                          float (&msg)[W / LPP]) {
-    constexpr int S = W / LPP;
-#pragma unroll
-    for (int s = 0; s < S; ++s) msg[s] = 0.f;
-#pragma unroll
-    for (int r = 0; r < LPP; ++r) {
-#pragma unroll
-        for (int s2 = 0; s2 < S; ++s2) {
-            const int i = r * S + s2;
-            if (i >= Q) continue;
-            const float xi = LPP == 1 ? x[s2] : __shfl_sync(0xffffffffu, x[s2], r, LPP);
-            float row[S];
-            ld_part_ro<S>(P + i * W + j0, row);
-#pragma unroll
-            for (int s = 0; s < S; ++s) msg[s] = fmaf(xi, row[s], msg[s]);
-        }
-    }
-}
-
-// ev[s] = sum_j P[j0+s][j] o_j
-template <int Q, int W, int LPP>
-__device__ __forceinline__ void f_mat_vec(const float* __restrict__ P, const float (&o)[W / LPP], int j0,
-                                          float (&ev)[W / LPP]) {
-    constexpr int S = W / LPP;
-    float full[W];
-#pragma unroll
-    for (int r = 0; r < LPP; ++r) {
-#pragma unroll
-        for (int s2 = 0; s2 < S; ++s2) full[r * S + s2] = LPP == 1 ? o[s2] : __shfl_sync(0xffffffffu, o[s2], r, LPP);
-    }
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const int i = j0 + s;
-        float acc = 0.f;
-        if (i < Q) {
-            float row[W];
-            ld_part_ro<W>(P + i * W, row);
-#pragma unroll
-            for (int j = 0; j < Q; ++j) acc = fmaf(full[j], row[j], acc);
-        }
-        ev[s] = acc;
-    }
-}
-
-// first argmax over the pattern's states (ties -> lowest index), across the LPP lanes
-template <int Q, int W, int LPP>
-__device__ __forceinline__ int group_argmax(const float (&x)[W / LPP], int j0) {
-    constexpr int S = W / LPP;
-    float bv = -INFINITY;
-    int bi = Q;
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const int j = j0 + s;
-        if (j < Q && (x[s] > bv || bi == Q)) { bv = x[s]; bi = j; }
-    }
-#pragma unroll
-    for (int o = LPP / 2; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-    }
-    return bi;
-}
-
-
-// ---------------------------------------------------------------- async staging
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// msg[s] = sum_i x_i P[i][j0+s] with P in shared memory
-template <int Q, int W, int LPP>
-__device__ __forceinline__ void s_vec_mat(const float (&x)[W / LPP], const float* P, int j0, float (&msg)[W / LPP]) {
-    constexpr int S = W / LPP;
-#pragma unroll
-    for (int s = 0; s < S; ++s) msg[s] = 0.f;
-#pragma unroll
-    for (int r = 0; r < LPP; ++r) {
-#pragma unroll
-        for (int s2 = 0; s2 < S; ++s2) {
-            const int i = r * S + s2;
-            if (i >= Q) continue;
-            const float xi = LPP == 1 ? x[s2] : __shfl_sync(0xffffffffu, x[s2], r, LPP);
-            float row[S];
-            ld_part<S>(P + i * W + j0, row);
-#pragma unroll
-            for (int s = 0; s < S; ++s) msg[s] = fmaf(xi, row[s], msg[s]);
-        }
-    }
-}
-
-// ev[s] = sum_j P[j0+s][j] o_j with P in shared memory
-template <int Q, int W, int LPP>
-__device__ __forceinline__ void s_mat_vec(const float* P, const float (&o)[W / LPP], int j0, float (&ev)[W / LPP]) {
-    constexpr int S = W / LPP;
-    float full[W];
-#pragma unroll
-    for (int r = 0; r < LPP; ++r) {
-#pragma unroll
-        for (int s2 = 0; s2 < S; ++s2) full[r * S + s2] = LPP == 1 ? o[s2] : __shfl_sync(0xffffffffu, o[s2], r, LPP);
-    }
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const int i = j0 + s;
-        float acc = 0.f;
-        if (i < Q) {
-            float row[W];
-            ld_part<W>(P + i * W, row);
-#pragma unroll
-            for (int j = 0; j < Q; ++j) acc = fmaf(full[j], row[j], acc);
-        }
-        ev[s] = acc;
-    }
-}
-
-struct F32Params {
-    MargParams m;
-    const int4* items;       // [n_items] pattern ranges (tree, first pattern, pattern count, 0)
-    const int4* node_rec;    // [n_nodes] (child begin, child end, parent, tip row)
-    const int4* child_pair;  // [n_nodes] binary nodes: (c0, c0 tip row, c1, c1 tip row); else c0 = -1
-    const float* p32_pair;   // [n_nodes][2][Q][W] children's matrices of binary nodes
-};
-
-// Chunk of a level staged in shared memory: records, child pairs and matrices (post-order: the
-// two children's matrices; pre-order: the node's own matrix in the first half).
-template <int Q, int W>
-struct StageCfg {
-    static constexpr int kMatFloats = 2 * Q * W;
-    static constexpr int kBytesPerNode = 32 + kMatFloats * 4;
-    static constexpr int kFit = 48 * 1024 / kBytesPerNode;  // nodes per ~48 KB buffer
-    static constexpr int kChunk = kFit >= 256 ? 256 : (kFit >= 4 ? kFit : 4);
-};
-
-template <int Q, int W>
-struct __align__(16) Stage {
-    int4 rec[StageCfg<Q, W>::kChunk];
-    int4 pair[StageCfg<Q, W>::kChunk];
-    float mat[StageCfg<Q, W>::kChunk][StageCfg<Q, W>::kMatFloats];
-};
-
-// Partials are rescaled (by an exact power of two) only below this largest entry.
-constexpr float kRescaleBelow = 0x1p-16f;
 
 // One CTA per pattern range [p0, p0 + np) of one tree.  Its NT threads form G = NT / (np * LPP)
 // node groups; thread t belongs to group t / (np * LPP) and always works on pattern
@@ -260,6 +41,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     __shared__ int red[NT];
     __shared__ float red_corr[NT];
     __shared__ unsigned diff_red[NT / 32];
+    __shared__ int lev_s[kLevCap];
     extern __shared__ __align__(16) unsigned char dyn_s[];  // two stage buffers
     Stage<Q, W>* stg = reinterpret_cast<Stage<Q, W>*>(dyn_s);
     const int tid = threadIdx.x;
@@ -295,6 +77,12 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         const int64_t nb = tr.node_base;
         const int n_int = tr.n_int;
         const int32_t* lev = a.f.level_off + tr.level_base;
+        const int nlev = tr.n_levels;
+        const bool lev_sm = nlev < kLevCap;
+        if (lev_sm)
+            for (int i = tid; i <= nlev; i += NT) lev_s[i] = __ldg(lev + i);
+        __syncthreads();
+        auto LV = [&](int i) -> int { return lev_sm ? lev_s[i] : __ldg(lev + i); };
         int esum = 0;
         // log-LH correction for masked internal children: TreeTime masks the log message of the
         // child's sum-normalised partial and adds its prefactor unmasked; with power-of-two scaled
@@ -359,25 +147,40 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
             cp_async_commit();
         };
         const int GD = G * D;
-        const int first = active ? g : 0x7fffffff;
 
         // ------------------------------------------------------------ post-order
+        // A chunk is a slice of CH nodes of a wide level, or several whole narrow levels together
+        // (up to CH nodes, staged with one copy); the levels inside a chunk are separated by a
+        // CTA barrier only.  post_chunk returns the end of the chunk starting at node `base` of
+        // level h and its last level.
+        auto post_chunk = [&](int h, int base, int& he) -> int {
+            if (LV(h + 1) - base > CH) { he = h; return base + CH; }
+            int e = h + 1;
+            while (e < nlev && LV(e + 1) - base <= CH) ++e;
+            he = e - 1;
+            return LV(e);
+        };
         {
-            int h = 0, base = tr.n_levels > 0 ? __ldg(lev) : 0, b = 0;
-            bool have = tr.n_levels > 0;
-            if (have) stage(0, base, min(CH, __ldg(lev + 1) - base), true);
+            int b = 0, h = 0, base = nlev > 0 ? LV(0) : 0, he = 0, end = 0;
+            bool have = nlev > 0;
+            if (have) {
+                end = post_chunk(0, base, he);
+                stage(0, base, end - base, true);
+            }
             while (have) {
-                const int hi = __ldg(lev + h + 1);
-                const int cnt = min(CH, hi - base);
-                int nh = h, nbase = base + CH;
-                if (nbase >= hi) { nh = h + 1; nbase = nh < tr.n_levels ? __ldg(lev + nh) : 0; }
-                const bool has_next = nh < tr.n_levels;
+                const int nh = end < LV(he + 1) ? he : he + 1;
+                const bool has_next = nh < nlev;
+                int nhe = 0, nend = 0;
+                if (has_next) nend = post_chunk(nh, end, nhe);
                 cp_async_wait<0>();  // this thread's copies of the chunk have landed
                 __syncthreads();     // everybody's copies and the previous chunk's rows are visible;
                                      // buffer b^1 (the previous chunk's) is free
-                if (has_next) stage(b ^ 1, nbase, min(CH, __ldg(lev + nh + 1) - nbase), true);
+                if (has_next) stage(b ^ 1, end, nend - end, true);
                 const Stage<Q, W>& st = stg[b];
-                for (int i0 = first; i0 < cnt; i0 += GD) {
+                for (int lv = h; lv <= he; ++lv) {
+                if (lv > h) __syncthreads();  // the previous level's rows are written
+                const int s0 = max(base, LV(lv)) - base, s1 = min(end, LV(lv + 1)) - base;
+                for (int i0 = active ? s0 + g : s1; i0 < s1; i0 += GD) {
                     // loads of D nodes first
                     float xa[D][S], xb[D][S];
                     int ca[D], cb[D];
@@ -386,7 +189,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                     for (int d = 0; d < D; ++d) {
                         const int i = i0 + d * G;
                         bin[d] = false;
-                        if (i < cnt) {
+                        if (i < s1) {
                             const int4 cp = st.pair[i];
                             if (cp.x >= 0) {
                                 bin[d] = true;
@@ -400,7 +203,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
                         const int i = i0 + d * G;
-                        if (i >= cnt) continue;
+                        if (i >= s1) continue;
                         const int k = base + i;
                         float r[S];
                         if (bin[d]) {
@@ -453,8 +256,11 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         if (valid) st_part<S>(part0 + (int64_t)k * PW, r);
                     }
                 }
+                }
                 h = nh;
-                base = nbase;
+                base = end;
+                end = nend;
+                he = nhe;
                 b ^= 1;
                 have = has_next;
             }
@@ -471,12 +277,42 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         const bool count_diff = a.o.count_diff != 0;
         const bool keep_outgroup = a.o.outgroup != nullptr || a.o.tip_outgroup != nullptr;
         const int h_last = do_tips ? -1 : 0;
-        auto lv_lo = [&](int h) { return h >= 0 ? __ldg(lev + h) : n_int; };
-        auto lv_hi = [&](int h) { return h >= 0 ? __ldg(lev + h + 1) : n_int + tr.n_tip; };
-        int h = tr.n_levels - 2;
-        bool have = h >= h_last;
-        int base = have ? lv_lo(h) : 0;
-        if (have) stage(0, base, min(CH, lv_hi(h) - base), false);
+        // Chunks go down the tree: a slice of CH nodes of a wide level, or several whole narrow
+        // levels (top level first); then, when requested, the tips in slices of CH.  State
+        // (h, cur): h >= 0 -> level h's nodes below cur are left; h == -1 -> tips from cur on.
+        // pre_chunk gives the chunk [lo, hi) of a state, its lowest level hb and the next state.
+        auto pre_chunk = [&](int h, int cur, int& lo, int& hi, int& hb, int& nh, int& ncur) {
+            if (h < 0) {
+                lo = cur;
+                hi = min(cur + CH, n_int + tr.n_tip);
+                hb = -1;
+                nh = hi < n_int + tr.n_tip ? -1 : -2;
+                ncur = hi;
+                return;
+            }
+            hi = cur;
+            if (cur - LV(h) > CH) {
+                lo = cur - CH;
+                hb = h;
+                nh = h;
+                ncur = lo;
+                return;
+            }
+            int e = h - 1;
+            while (e >= 0 && cur - LV(e) <= CH) --e;
+            hb = e + 1;
+            lo = LV(hb);
+            nh = e;
+            ncur = e >= 0 ? LV(e + 1) : n_int;
+        };
+        int ph = nlev - 2, pcur = ph >= 0 ? LV(ph + 1) : n_int;
+        if (ph < 0) ph = -1;  // a tree whose root is its only internal node: tips only
+        bool have = ph >= h_last;
+        int plo = 0, phi = 0, phb = 0, pnh = 0, pncur = 0;
+        if (have) {
+            pre_chunk(ph, pcur, plo, phi, phb, pnh, pncur);
+            stage(0, plo, phi - plo, false);
+        }
 
         // ------------------------------------------------------------------ root
         if (tid < GP) {  // group 0 (whole warps when LPP > 1)
@@ -531,17 +367,20 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         {
             int b = 0;
             while (have) {
-                const int hi = lv_hi(h);
-                const int cnt = min(CH, hi - base);
-                const bool tips = h < 0;
-                int nh = h, nbase = base + CH;
-                if (nbase >= hi) { nh = h - 1; nbase = nh >= h_last ? lv_lo(nh) : 0; }
+                const int base = plo, hi = phi, htop = ph, hbot = phb;
+                const bool tips = htop < 0;
+                const int nh = pnh, ncur = pncur;
                 const bool has_next = nh >= h_last;
+                if (has_next) pre_chunk(nh, ncur, plo, phi, phb, pnh, pncur);
                 cp_async_wait<0>();
                 __syncthreads();  // chunk staged; the parents' rows (and the root's) are written
-                if (has_next) stage(b ^ 1, nbase, min(CH, lv_hi(nh) - nbase), false);
+                if (has_next) stage(b ^ 1, plo, phi - plo, false);
                 const Stage<Q, W>& st = stg[b];
-                for (int i0 = first; i0 < cnt; i0 += GD) {
+                for (int lv = htop; lv >= hbot; --lv) {
+                if (lv < htop) __syncthreads();  // the parents' level is written
+                const int s0 = tips ? 0 : max(base, LV(lv)) - base;
+                const int s1 = tips ? hi - base : min(hi, LV(lv + 1)) - base;
+                for (int i0 = active ? s0 + g : s1; i0 < s1; i0 += GD) {
                     float pv[D][S], x[D][S];
                     int code[D];
                     unsigned old[D];
@@ -549,7 +388,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                     for (int d = 0; d < D; ++d) {
                         const int i = i0 + d * G;
                         old[d] = 0;
-                        if (i < cnt) {
+                        if (i < s1) {
                             const int4 rec = st.rec[i];
                             ld_part<S>(post0 + (int64_t)rec.z * PW, pv[d]);
                             if (tips) code[d] = tip_code(rec.w);
@@ -560,7 +399,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
                         const int i = i0 + d * G;
-                        if (i >= cnt) continue;
+                        if (i >= s1) continue;
                         const int k = base + i;
                         if (tips) lut_part(code[d], x[d]);
                         const float* Pk = &st.mat[i][0];
@@ -624,8 +463,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         }
                     }
                 }
-                h = nh;
-                base = nbase;
+                }
+                ph = nh;
                 b ^= 1;
                 have = has_next;
             }

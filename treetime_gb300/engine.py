@@ -342,7 +342,7 @@ class Forest:
         # CTAs per SM): each tree gets the width whose node x pattern work is one CTA's share.
         lanes_per_pattern = 4 if q >= 20 else 1
         if q != 4:
-            threads = 512  # the only shape compiled for 5 and 20+ states
+            threads = 512  # the only CTA size compiled for 5 and 20+ states
         elif threads is None:
             threads = 1024
         if threads not in (512, 1024):

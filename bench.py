@@ -29,6 +29,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
+REFERENCE_BUDGET_S = 90.0
 METRIC = "node-pattern updates/s (marginal reconstruction, FP32-scaled; FP64 plain beside it)"
 UNIT = "node-pattern updates/s"
 WORKLOAD = "c1: 2000-tip coalescent tree x 30000 nucleotide sites (90% invariant), GTR kappa=3, marginal"
@@ -156,8 +157,12 @@ def run_gpu(args):
     units = N * P
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
+    # one step = one marginal reconstruction, replayed from a captured CUDA graph (the buffer
+    # clears and the three launches, no host work between kernels)
+    graphs = {prec: engine.CapturedMarginal(forest, model, bufs, precision=prec) for prec in ("f32", "f64")}
+
     def step(prec):
-        return engine.marginal(forest, model, bufs, precision=prec, sync=False)
+        return graphs[prec].replay()
 
     def timed(prec, k, w):
         for _ in range(w):
@@ -175,10 +180,8 @@ def run_gpu(args):
         return times
 
     # parity of the measured path against the FP64 kernel on this workload
-    out64 = engine.marginal(forest, model, bufs, precision="f64")
-    lh64 = float(out64["tree_lh"][0].item())
-    out32 = engine.marginal(forest, model, bufs, precision="f32")
-    lh32 = float(out32["tree_lh"][0].item())
+    lh64 = float(graphs["f64"].replay(sync=True)["tree_lh"][0].item())
+    lh32 = float(graphs["f32"].replay(sync=True)["tree_lh"][0].item())
     rel_err = abs(lh32 - lh64) / abs(lh64)
 
     # FP64 plain kernel (reported beside the measured path)
@@ -196,7 +199,7 @@ def run_gpu(args):
         pm, status = engine.branch_pmats(forest, model, bufs, need32=True)
         for _ in range(min(args.steps, 50)):
             flush.zero_()
-            out = engine.marginal(forest, model, bufs, precision="f32", sync=False)  # warm buffers
+            graphs["f32"].replay()  # fresh inputs for the kernel timed alone
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             flush.zero_()
@@ -214,7 +217,7 @@ def run_gpu(args):
         ms32 = float(x.item())
 
     # end-to-end through host buffers (pinned), copies inside the timed region
-    e2e_ms, h2d, d2h = _e2e(engine, t, forest, model, bufs, args.steps, args.warmup, flush)
+    e2e_ms, h2d, d2h = _e2e(engine, t, forest, graphs["f32"], args.steps, args.warmup, flush)
 
     if rank != 0:
         return None
@@ -261,6 +264,169 @@ def run_gpu(args):
     return res
 
 
+C3_WORKLOAD = ("c3: 256 independent coalescent trees, tips log-uniform in [50, 5000], sites log-uniform in "
+               "[1k, 30k], branch means log-uniform in [1e-4, 0.05], a random GTR per tree; the whole batch is "
+               "one forest, one captured launch sequence per step")
+
+
+def run_c3(args):
+    """--workload c3: the batched workload.  Every rank builds its own batch
+    (replicas; seeds differ by rank) and runs the marginal pass over the whole
+    forest as one captured CUDA graph per step.  Inputs (tens of GB) are far
+    larger than L2, so no flush is needed between steps."""
+    import torch
+    from treetime_gb300 import engine, synth
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    inputs, gtrs = synth.forest_c3(seed=3 + rank)
+    build_s = time.perf_counter() - t0
+    model = engine.DeviceModel(gtrs, device=dev)
+    forest = engine.Forest(inputs, 4, device=dev)
+    bufs = engine.Buffers(forest)
+    units = sum(ti.layout.n_nodes * ti.n_patterns for ti in inputs)
+    cap = engine.CapturedMarginal(forest, model, bufs, precision="f32")
+    lh32 = cap.replay(sync=True)["tree_lh"].cpu().numpy().copy()
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return ts
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t32 = timed(cap.replay, args.steps, args.warmup)
+        pm, _ = engine.branch_pmats(forest, model, bufs, need32=True)
+        kt = timed(lambda: _marginal_only(engine, forest, model, bufs, pm, "f32"), min(args.steps, 10), 1)
+    ms32 = sum(t32) / len(t32)
+    if world > 1:
+        import torch.distributed as dist
+        x = torch.tensor([ms32], device=dev)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        ms32 = float(x.item())
+
+    # end to end: every tree's tip codes, branch lengths and multiplicities from pinned host
+    # memory, states and site log-likelihoods back, every step
+    codes_h = torch.from_numpy(np.concatenate([ti.tip_codes.reshape(-1) for ti in inputs])).pin_memory()
+    bl_h = torch.from_numpy(forest.bl_host.copy()).pin_memory()
+    mult_h = torch.from_numpy(np.concatenate([ti.mult for ti in inputs])).pin_memory()
+    states_h = torch.empty(forest.state_rows, dtype=torch.uint8).pin_memory()
+    lh_h = torch.empty(forest.n_patterns, dtype=torch.float64).pin_memory()
+
+    def one_e2e():
+        forest.d_codes[: codes_h.numel()].copy_(codes_h, non_blocking=True)
+        forest.d_bl.copy_(bl_h, non_blocking=True)
+        forest.d_mult.copy_(mult_h, non_blocking=True)
+        out = cap.replay()
+        states_h.copy_(out["states"], non_blocking=True)
+        lh_h.copy_(out["site_lh"], non_blocking=True)
+        return float(out["tree_lh"].sum().item())
+
+    te = timed(one_e2e, min(args.steps, 10), 1)
+    e2e_ms = sum(te) / len(te)
+    h2d = codes_h.numel() + bl_h.numel() * 8 + mult_h.numel() * 8
+    d2h = states_h.numel() + lh_h.numel() * 8 + 8
+
+    # FP64 plain kernel on the same forest when its buffers fit beside the FP32 ones
+    fp64 = None
+    free, _ = torch.cuda.mem_get_info(dev)
+    need64 = forest.prof_rows * forest.w * 8 * 2 + forest.n_nodes * forest.q * forest.w * 8 * 2
+    if free > 1.15 * need64:
+        cap64 = engine.CapturedMarginal(forest, model, bufs, precision="f64")
+        lh64 = cap64.replay(sync=True)["tree_lh"].cpu().numpy().copy()
+        t64 = timed(cap64.replay, 3, 1)
+        rel = np.abs(lh32 - lh64) / np.abs(lh64)
+        w = int(np.argmax(rel))
+        tw = inputs[w]
+        fp64 = {"value": units / (sum(t64) / len(t64) * 1e-3), "ms_per_step": sum(t64) / len(t64),
+                "max_rel_logLH_err_fp32_vs_fp64": float(rel.max()),
+                "median_rel_logLH_err_fp32_vs_fp64": float(np.median(rel)),
+                "trees_over_1e-6": int((rel > 1e-6).sum()), "trees": len(inputs),
+                "worst_tree": {"tips": tw.layout.n_tip, "patterns": tw.n_patterns, "sites": int(round(tw.mult.sum())),
+                               "mean_branch_length": float(np.mean(tw.bl)), "logLH_fp64": float(lh64[w]),
+                               "abs_err": float(abs(lh32[w] - lh64[w]))}}
+    else:
+        fp64 = {"skipped": "FP64 buffers (%.0f GB) do not fit beside the FP32 ones (%.0f GB free)"
+                % (need64 / 1e9, free / 1e9)}
+
+    if rank != 0:
+        return None
+    peak, peak_kind = _peaks()
+    ab = sum(algorithmic_bytes(ti.layout, ti.n_patterns) for ti in inputs)
+    k_ms = sum(kt) / len(kt)
+    res = {
+        "metric": METRIC, "value": world * units / (ms32 * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded coalescent trees, GTR-evolved alignments)",
+        "config": {"workload": C3_WORKLOAD, "trees": len(inputs), "nodes": forest.n_nodes,
+                   "patterns": forest.n_patterns, "node_patterns_per_step": units,
+                   "l2": "inputs (%.0f GB of profile rows) far larger than L2; no flush" % (forest.prof_rows * 32 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU", "build_seconds": build_s,
+                   "ranges": int(len(forest.work_f32_host))},
+        "fp64_plain": fp64,
+        "roofline": {"bound": "hbm", "achieved": ab / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": ab / (k_ms * 1e-3) / 1e9 / peak, "traffic": _traffic("marginal_f32_q4/c3"),
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms,
+                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d>" % (forest.threads, forest.ctas_per_sm)},
+        "e2e": {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        res["cpu_baseline"] = cpu_baseline_forest(inputs, gtrs)
+    return res
+
+
+def cpu_baseline_forest(inputs, gtrs, budget_node_patterns=4e7, seed=0):
+    """The oracle marginal on a seeded random sample of the batch's trees (one
+    process), bounded to about ``budget_node_patterns`` node-pattern updates."""
+    from oracle import anc
+    from treetime_gb300.tree import Tree
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(len(inputs))
+    done_units, secs, used = 0, 0.0, 0
+    for k in order:
+        ti = inputs[k]
+        u = ti.layout.n_nodes * ti.n_patterns
+        if done_units + u > budget_node_patterns and used > 0:
+            continue
+        root = ti.layout.nodes[ti.layout.n_int - 1]
+        tree = anc.prepare_tree(Tree(root=root))
+        tips = ti.layout.nodes[ti.layout.n_int:]
+        chars = ti.tip_codes.view("S1").astype("U1")
+        aln = {t.name: chars[r] for t, r in zip(tips, ti.tip_row)}
+        L = int(round(ti.mult.sum()))
+        t0 = time.perf_counter()
+        anc.marginal(tree, aln, ti.mult, _model_state(gtrs[k]), L)
+        secs += time.perf_counter() - t0
+        done_units += u
+        used += 1
+        if done_units >= budget_node_patterns:
+            break
+    return {"value": done_units / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d trees of the batch (seeded random), %.2e node-pattern updates, numpy restatement of "
+                      "TreeTime, 1 process" % (used, done_units), "seconds": secs}
+
+
 def _marginal_only(engine, forest, model, bufs, pm, prec):
     """Launch only the marginal pruning kernel (branch matrices already made)."""
     import ctypes as C
@@ -280,11 +446,12 @@ def _marginal_only(engine, forest, model, bufs, pm, prec):
                                engine._stream()), "tt_marginal")
 
 
-def _e2e(engine, t, forest, model, bufs, steps, warmup, flush):
+def _e2e(engine, t, forest, graph, steps, warmup, flush):
     """Host buffers in, host buffers out: tip codes, branch lengths and
-    multiplicities are copied from pinned host memory, the reconstruction runs,
-    and the states and per-pattern log-likelihoods come back to pinned host
-    memory, every step."""
+    multiplicities are copied from pinned host memory, the reconstruction runs
+    (the captured graph, which reads the forest's input buffers in place), and
+    the states and per-pattern log-likelihoods come back to pinned host memory,
+    every step."""
     import torch
     codes_h = torch.from_numpy(np.ascontiguousarray(t.data.compressed_codes).reshape(-1)).pin_memory()
     bl_h = torch.from_numpy(forest.bl_host.copy()).pin_memory()
@@ -298,7 +465,7 @@ def _e2e(engine, t, forest, model, bufs, steps, warmup, flush):
         forest.d_codes[: codes_h.numel()].copy_(codes_h, non_blocking=True)
         forest.d_bl.copy_(bl_h, non_blocking=True)
         forest.d_mult.copy_(mult_h, non_blocking=True)
-        out = engine.marginal(forest, model, bufs, precision="f32", sync=False)
+        out = graph.replay()
         states_h.copy_(out["states"], non_blocking=True)
         lh_h.copy_(out["site_lh"], non_blocking=True)
         return float(out["tree_lh"][0].item())
@@ -378,18 +545,24 @@ def run_reference(args):
     chunks = [slice(i * P // cores, (i + 1) * P // cores) for i in range(cores)]
     inputs = _oracle_inputs(t, chunks)
     ctx = mp.get_context("spawn")
+    # one step is the whole workload on all cores (smaller samples would be dominated by the
+    # per-node Python overhead); the timed steps stop after REFERENCE_BUDGET_S seconds
     with ctx.Pool(cores) as pool:
-        for _ in range(args.warmup):
+        for _ in range(min(args.warmup, 3)):
             pool.map(_oracle_chunk, inputs)
         times = []
+        t_start = time.perf_counter()
         for _ in range(args.steps):
             t0 = time.perf_counter()
             pool.map(_oracle_chunk, inputs)
             times.append(time.perf_counter() - t0)
+            if time.perf_counter() - t_start > REFERENCE_BUDGET_S and len(times) >= 3:
+                break
     sec = sum(times) / len(times)
     v = N * P / sec
-    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(times),
+            "steps_requested": args.steps, "warmup": min(args.warmup, 3), "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "patterns": P, "nodes": N},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -405,6 +578,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3"],
+                    help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -412,7 +587,7 @@ def main():
     else:
         from treetime_gb300 import build
         build.build()
-        res = run_gpu(args)
+        res = run_c3(args) if args.workload == "c3" else run_gpu(args)
     if res is not None:
         print(json.dumps(res))
 

@@ -3,23 +3,28 @@
 
 namespace tt {
 
-// Per-tree multiplicity-weighted sum of the site log-likelihoods, fixed summation order.
-__global__ void tree_sum_kernel(const tt_tree* trees, const double* site_lh, const double* mult, double* tree_lh) {
-    __shared__ double red[256];
+// Per-tree multiplicity-weighted sum of the site log-likelihoods in a fixed order (strided
+// per-thread sums, then warp shuffles, then the 32 warp sums): deterministic from run to run.
+__global__ void __launch_bounds__(1024) tree_sum_kernel(const tt_tree* trees, const double* site_lh,
+                                                         const double* mult, double* tree_lh) {
+    __shared__ double red[32];
     const tt_tree tr = trees[blockIdx.x];
     double s = 0.0;
     for (int p = threadIdx.x; p < tr.n_patterns; p += blockDim.x) s += site_lh[tr.pat_base + p] * mult[tr.pat_base + p];
-    red[threadIdx.x] = s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-        __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) tree_lh[blockIdx.x] = s;
     }
-    if (threadIdx.x == 0) tree_lh[blockIdx.x] = red[0];
 }
 
 tt_status tree_sums(const tt_forest* f, const double* site_lh, double* tree_lh, cudaStream_t s) {
-    tree_sum_kernel<<<f->n_trees, 256, 0, s>>>(f->trees, site_lh, f->mult, tree_lh);
+    tree_sum_kernel<<<f->n_trees, 1024, 0, s>>>(f->trees, site_lh, f->mult, tree_lh);
     return check_launch("tree_sum");
 }
 

@@ -17,38 +17,43 @@ __device__ __forceinline__ int tree_of_node(const tt_tree* trees, int n_trees, i
     return lo;
 }
 
+// One thread per matrix row (node g, child state i): the q factors exp(mu*lambda_k*t) are computed
+// once per row (FP64 exp is slow on this GPU) and the row's w entries summed over k in order.
 __global__ void pmats_kernel(tt_forest f, tt_model m, tt_pmats out, int32_t* status) {
+    constexpr int kMaxQ = 32;
     const int q = f.n_states, w = f.width;
-    const int64_t total = f.n_nodes * q * w;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+    const int64_t rows = f.n_nodes * q;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t g = idx / (q * w);
-        const int r = (int)(idx % (q * w));
-        const int i = r / w, j = r % w;
-        double p = 0.0;
-        if (j < q) {
-            const int t = tree_of_node(f.trees, f.n_trees, g);
-            const int mi = f.trees[t].model;
-            const double* V = m.V + (int64_t)mi * q * q;
-            const double* Vi = m.Vinv + (int64_t)mi * q * q;
-            const double* lam = m.lam + (int64_t)mi * q;
-            const double mu = m.mu[mi];
-            const double bl = f.bl[g];
-            double acc = 0.0;
-            for (int k = 0; k < q; ++k) {
-                const double lv = mu * bl * lam[k];
-                if (lv > 10.0) set_status(status, TT_ERR_NUMERIC);
-                acc = fma(V[i * q + k], exp(lv) * Vi[k * q + j], acc);
+        const int64_t g = idx / q;
+        const int i = (int)(idx - g * q);
+        const int t = tree_of_node(f.trees, f.n_trees, g);
+        const int mi = f.trees[t].model;
+        const double* V = m.V + (int64_t)mi * q * q;
+        const double* Vi = m.Vinv + (int64_t)mi * q * q;
+        const double* lam = m.lam + (int64_t)mi * q;
+        const double mu = m.mu[mi];
+        const double bl = f.bl[g];
+        double ex[kMaxQ];
+        for (int k = 0; k < q; ++k) {
+            const double lv = mu * bl * lam[k];
+            if (lv > 10.0) set_status(status, TT_ERR_NUMERIC);
+            ex[k] = exp(lv);
+        }
+        const int ps = (out.p32_pair && f.pair_slot) ? f.pair_slot[g] : -1;
+        const int64_t o = g * q * w + (int64_t)i * w;
+        for (int j = 0; j < w; ++j) {
+            double p = 0.0;
+            if (j < q) {
+                double acc = 0.0;
+                for (int k = 0; k < q; ++k) acc = fma(V[i * q + k], ex[k] * Vi[k * q + j], acc);
+                p = acc > 0.0 ? acc : 0.0;
             }
-            p = acc > 0.0 ? acc : 0.0;
+            out.p64[o + j] = p;
+            if (out.p32) out.p32[o + j] = (float)p;
+            if (ps >= 0) out.p32_pair[(int64_t)ps * q * w + (int64_t)i * w + j] = (float)p;
+            if (out.logp64) out.logp64[o + j] = j < q ? log(p > kTiny ? p : kTiny) : 0.0;
         }
-        out.p64[g * q * w + r] = p;
-        if (out.p32) out.p32[g * q * w + r] = (float)p;
-        if (out.p32_pair && f.pair_slot) {
-            const int ps = f.pair_slot[g];
-            if (ps >= 0) out.p32_pair[(int64_t)ps * q * w + r] = (float)p;
-        }
-        if (out.logp64) out.logp64[g * q * w + r] = j < q ? log(p > kTiny ? p : kTiny) : 0.0;
     }
 }
 
@@ -77,9 +82,9 @@ extern "C" tt_status tt_branch_pmats(const tt_forest* f, const tt_model* m, tt_p
         set_error("tt_branch_pmats: invalid arguments");
         return TT_ERR_INVALID;
     }
-    const int64_t total = f->n_nodes * f->n_states * f->width;
+    const int64_t total = f->n_nodes * f->n_states;  // one thread per matrix row
     if (total == 0) return TT_OK;
-    const int threads = 256;
+    const int threads = 128;
     int64_t blocks = (total + threads - 1) / threads;
     if (blocks > 65535LL * 8) blocks = 65535LL * 8;
     pmats_kernel<<<(unsigned)blocks, threads, 0, as_stream(stream)>>>(*f, *m, out, status);

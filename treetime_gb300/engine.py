@@ -428,7 +428,8 @@ class Forest:
 # kernels
 # ----------------------------------------------------------------------------
 class Buffers:
-    """Device outputs of the pruning passes for a forest (reused across calls)."""
+    """Device outputs of the pruning passes for a forest (reused across calls;
+    one buffer per name and dtype, so FP32 and FP64 passes keep their own)."""
 
     def __init__(self, forest):
         self.f = forest
@@ -436,7 +437,7 @@ class Buffers:
 
     def get(self, name, shape, dtype):
         t = torch()
-        key = name
+        key = (name, dtype)
         buf = self.cache.get(key)
         if buf is None or tuple(buf.shape) != tuple(shape) or buf.dtype != dtype:
             buf = t.empty(shape, dtype=dtype, device=self.f.device)
@@ -500,6 +501,38 @@ def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_
         _check_status(status)
     out["_keep"] = ru
     return out
+
+
+class CapturedMarginal:
+    """One marginal pass over a forest captured as a CUDA graph: the buffer
+    clears and the three launches (branch matrices, the pass, the per-tree
+    sums) replay with a single host call and no gaps between kernels.  The
+    forest's device inputs (tip codes, branch lengths, multiplicities) may be
+    overwritten in place between replays; the outputs are the same device
+    buffers every time (``self.out``).  Root sampling is not captured (its
+    uniform draws are a per-call host input)."""
+
+    def __init__(self, forest, model, bufs, precision="f32", reconstruct_tips=False, keep_outgroup=False,
+                 tip_outgroup=False, count_diff=False):
+        t = torch()
+        kw = dict(precision=precision, reconstruct_tips=reconstruct_tips, keep_outgroup=keep_outgroup,
+                  tip_outgroup=tip_outgroup, count_diff=count_diff)
+        marginal(forest, model, bufs, sync=True, **kw)  # allocates every buffer, configures the kernels
+        side = t.cuda.Stream(device=forest.device)
+        side.wait_stream(t.cuda.current_stream(forest.device))
+        with t.cuda.stream(side):
+            marginal(forest, model, bufs, sync=False, **kw)
+        t.cuda.current_stream(forest.device).wait_stream(side)
+        self.graph = t.cuda.CUDAGraph()
+        with t.cuda.graph(self.graph):
+            self.out = marginal(forest, model, bufs, sync=False, **kw)
+        self.status = bufs.get("status", (1,), t.int32)
+
+    def replay(self, sync=False):
+        self.graph.replay()
+        if sync:
+            _check_status(self.status)
+        return self.out
 
 
 def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=False, keep_outgroup=False,
@@ -584,7 +617,7 @@ def state_pairs(forest, bufs, char_state, gap_state, ignore_gaps, tips_use_state
     hist = bufs.get("hist", (forest.n_nodes, q, q), t.float64)
     hist.zero_()
     cs = _to_dev(char_state, forest.device)
-    check(lib.tt_state_pairs(C.byref(forest.struct), _p(bufs.cache["states"]), _p(cs), int(bool(tips_use_states)),
+    check(lib.tt_state_pairs(C.byref(forest.struct), _p(bufs.cache[("states", t.uint8)]), _p(cs), int(bool(tips_use_states)),
                              -1 if gap_state is None else int(gap_state), int(bool(ignore_gaps)), None, _p(hist),
                              _stream()), "tt_state_pairs")
     return hist, cs

@@ -108,6 +108,70 @@ def evolve(tree, gtr, L, rng, invariant_frac=0.0, root_states=None):
     return out
 
 
+def evolve_sparse(tree, gtr, L, rng):
+    """The same substitution process as ``evolve`` (uniform root), sampled per
+    branch as "keep the parent state with probability P(s -> s), otherwise draw
+    the new state from P(. | s) restricted to the other states": one uniform
+    draw per site plus one per changed site, so short branches are cheap.
+    Returns {tip name: uint8 state indices}."""
+    q = gtr.n_states
+    root = tree.root
+    states = {id(root): rng.integers(q, size=L).astype(np.uint8)}
+    out = {}
+    stack = [root]
+    while stack:
+        node = stack.pop()
+        s = states.pop(id(node))
+        if not node.clades:
+            out[node.name] = s
+            continue
+        for ch in node.clades:
+            P = _pmat(gtr, ch.branch_length)               # P[child, parent]
+            stay = np.diag(P).astype(np.float32)
+            off = P.T.copy()                               # rows: parent state
+            np.fill_diagonal(off, 0.0)
+            tot = off.sum(axis=1, keepdims=True)
+            cdf = np.cumsum(off / np.where(tot > 0, tot, 1.0), axis=1)
+            u = rng.random(L, dtype=np.float32)
+            moved = np.flatnonzero(u > stay[s])
+            child = s.copy()
+            if moved.size:
+                v = rng.random(moved.size)
+                child[moved] = np.minimum((v[:, None] > cdf[s[moved]]).sum(axis=1), q - 1).astype(np.uint8)
+            states[id(ch)] = child
+            stack.append(ch)
+    return out
+
+
+def forest_c3(n_trees=256, seed=3, n_range=(50, 5000), L_range=(1000, 30000), bl_range=(1e-4, 0.05)):
+    """The batched workload as device-ready inputs: ``n_trees`` independent
+    coalescent trees with tip counts, site counts and mean branch lengths
+    log-uniform in the given ranges, each with its own random nucleotide GTR
+    (model index = tree index), alignments compressed to patterns.  Built from
+    state codes directly (no alignment text).  Returns (inputs, gtrs)."""
+    from . import engine
+    from .seqdata import compress_codes
+    rng = np.random.default_rng(seed)
+    lu = lambda lo, hi: float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+    alpha = np.frombuffer("".join(alphabets["nuc_nogap"]).encode(), dtype=np.uint8)
+    inputs, gtrs = [], []
+    for k in range(n_trees):
+        n = int(lu(*n_range))
+        L = int(lu(*L_range))
+        bl = lu(*bl_range)
+        tree = coalescent_tree(n, bl, rng)
+        gtr = GTR.random(mu=1.0, alphabet="nuc_nogap", rng=rng)
+        st = evolve_sparse(tree, gtr, L, rng)
+        layout = engine.TreeLayout(tree.root)
+        tips = layout.nodes[layout.n_int:]
+        codes = alpha[np.stack([st[t.name] for t in tips])]
+        pc, mult, _, _ = compress_codes(codes, ord("N"))
+        inputs.append(engine.TreeInput(layout, pc, np.arange(len(tips), dtype=np.int32), mult,
+                                       engine.branch_lengths(layout, L), model=k))
+        gtrs.append(gtr)
+    return inputs, gtrs
+
+
 def _to_text(states, alphabet, gap_frac, rng):
     alpha = np.asarray(alphabet)
     aln = {}

@@ -284,7 +284,7 @@ def run_c3(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     t0 = time.perf_counter()
-    inputs, gtrs = synth.forest_c3(seed=3 + rank)
+    inputs, gtrs = synth.forest_c3(n_trees=args.c3_trees, seed=3 + rank)
     build_s = time.perf_counter() - t0
     model = engine.DeviceModel(gtrs, device=dev)
     forest = engine.Forest(inputs, 4, device=dev)
@@ -348,7 +348,9 @@ def run_c3(args):
     fp64 = None
     free, _ = torch.cuda.mem_get_info(dev)
     need64 = forest.prof_rows * forest.w * 8 * 2 + forest.n_nodes * forest.q * forest.w * 8 * 2
-    if free > 1.15 * need64:
+    if getattr(args, "no_fp64", False):
+        fp64 = {"skipped": "--no-fp64"}
+    elif free > 1.15 * need64:
         cap64 = engine.CapturedMarginal(forest, model, bufs, precision="f64")
         lh64 = cap64.replay(sync=True)["tree_lh"].cpu().numpy().copy()
         t64 = timed(cap64.replay, 3, 1)
@@ -376,7 +378,8 @@ def run_c3(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded coalescent trees, GTR-evolved alignments)",
-        "config": {"workload": C3_WORKLOAD, "trees": len(inputs), "nodes": forest.n_nodes,
+        "config": {"workload": C3_WORKLOAD if args.c3_trees == 256 else C3_WORKLOAD + " (first %d trees)" % args.c3_trees,
+                   "trees": len(inputs), "nodes": forest.n_nodes,
                    "patterns": forest.n_patterns, "node_patterns_per_step": units,
                    "l2": "inputs (%.0f GB of profile rows) far larger than L2; no flush" % (forest.prof_rows * 32 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU", "build_seconds": build_s,
@@ -580,6 +583,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c1", choices=["c1", "c3"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
+    ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
+    ap.add_argument("--c3-trees", type=int, default=256,
+                    help="trees in the c3 batch (fewer: the first trees of the same seeded draw, for profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

@@ -148,7 +148,10 @@ def run_gpu(args):
     layout, model = sess["layout"], sess["model"]
     # launch shape of the FP32 kernel picked by the autotuner (outside the timed region)
     from treetime_gb300 import autotune
-    best, table = autotune.tune(sess["forest"].inputs, 4, model, device=dev, use_cache=False)
+    if args.shape:  # fixed launch shape (profiling runs: timings under a profiler would mislead the tuner)
+        best, table = tuple(int(x) for x in args.shape.split("/")), {}
+    else:
+        best, table = autotune.tune(sess["forest"].inputs, 4, model, device=dev, use_cache=False)
     forest = engine.Forest(sess["forest"].inputs, 4, device=dev, threads=best[0], ctas_per_sm=best[1],
                            ranges_per_sm=best[2])
     bufs = engine.Buffers(forest)
@@ -261,6 +264,91 @@ def run_gpu(args):
     }
     if not args.no_cpu_baseline and world == 1:
         res["cpu_baseline"] = cpu_baseline(t)
+    return res
+
+
+C2_WORKLOAD = ("c2: 500-tip Yule tree x 1500 amino-acid sites (21 states incl. gap, no compression), "
+               "site-specific GTR (per-site pi ~ Dirichlet(0.5), shared W ~ U(0.1, 5)), TreeTime's interpolated P(t)")
+
+
+def run_c2(args):
+    """--workload c2: marginal reconstruction under GTR_site_specific (each
+    site its own eigenbasis), FP32 beside FP64, L2 flushed before every step."""
+    import torch
+    from treetime_gb300 import TreeAnc, engine, synth
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl = synth.make_workload("c2", seed=2 + rank)
+    t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], compress=False, verbose=0, precision="f32",
+                device=dev)
+    sess = t._get_session()
+    forest, bufs, layout, gtr = sess["forest"], sess["bufs"], sess["layout"], t.gtr
+    P, N = t.data.compressed_length, layout.n_nodes
+    units = N * P
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def timed(prec, k, w):
+        for _ in range(w):
+            engine.marginal_site_specific(forest, gtr, bufs, precision=prec, sync=False)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            engine.marginal_site_specific(forest, gtr, bufs, precision=prec, sync=False)
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return ts
+
+    lh64 = float(engine.marginal_site_specific(forest, gtr, bufs, precision="f64")["tree_lh"][0].item())
+    lh32 = float(engine.marginal_site_specific(forest, gtr, bufs, precision="f32")["tree_lh"][0].item())
+    t64 = timed("f64", max(3, min(20, args.steps // 10)), 1)
+    with ClockSampler(local) as clk:
+        t32 = timed("f32", args.steps, args.warmup)
+    ms32, ms64 = sum(t32) / len(t32), sum(t64) / len(t64)
+    if rank != 0:
+        return None
+    q, w = gtr.n_states, forest.w
+    # profile traffic as for c1 (w = 24 floats per row), plus each site's eigensystem read once
+    ab = P * (layout.n_int * (5 * w * 4 + 3 * 4 + 1) + layout.n_tip) + P * 12 + P * (2 * q * q + 2 * q + 1) * 8
+    peak, peak_kind = _peaks()
+    res = {
+        "metric": METRIC, "value": world * units / (ms32 * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Yule tree, site-specific-model alignment)",
+        "config": {"workload": C2_WORKLOAD, "tips": layout.n_tip, "nodes": N, "patterns": P,
+                   "node_patterns_per_step": units, "approximate": bool(gtr.approximate),
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU"},
+        "fp64_plain": {"value": units / (ms64 * 1e-3), "ms_per_step": ms64},
+        "fp32_over_fp64": ms64 / ms32, "rel_logLH_err_vs_fp64": abs(lh32 - lh64) / abs(lh64),
+        "roofline": {"bound": "hbm", "achieved": ab / (ms32 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": ab / (ms32 * 1e-3) / 1e9 / peak, "traffic": _traffic("marginal_ss_f32/c2"),
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": ab,
+                     "note": "step time (eigen-basis transport per node and site, two launches)"},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        # TreeTime's site-specific path interpolates every site's matrix on every branch (about
+        # 2 s per branch here), so the whole tree would take tens of minutes: time a 6-tip tree
+        # drawn the same way (1,500 sites, same model family) instead
+        from oracle import anc
+        from treetime_gb300.tree import parse_newick, to_newick
+        ws = synth.make_workload("c2", seed=20, n=6)
+        ts = TreeAnc(tree=ws["tree"], aln=ws["aln"], gtr=ws["gtr"], compress=False, verbose=0, device=dev)
+        tree = anc.prepare_tree(parse_newick(to_newick(ts.tree)))
+        aln = dict(zip(ts.data.sequence_names, ts.data.compressed_codes.view("S1").astype("U1")))
+        t0 = time.perf_counter()
+        anc.marginal(tree, aln, ts.data.multiplicity(), ts.gtr, ts.data.full_length)
+        secs = time.perf_counter() - t0
+        su = (2 * 6 - 1) * ts.data.compressed_length
+        res["cpu_baseline"] = {"value": su / secs, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "one marginal reconstruction of a 6-tip tree x 1500 sites drawn like "
+                                         "the workload (numpy restatement of TreeTime, 1 process)", "seconds": secs}
     return res
 
 
@@ -581,9 +669,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
+    ap.add_argument("--shape", default="", help="c1: fixed FP32 launch shape threads/ctas_per_sm/ranges_per_sm "
+                                                 "instead of the autotuner (profiling runs)")
     ap.add_argument("--c3-trees", type=int, default=256,
                     help="trees in the c3 batch (fewer: the first trees of the same seeded draw, for profiling)")
     args = ap.parse_args()
@@ -593,7 +683,7 @@ def main():
     else:
         from treetime_gb300 import build
         build.build()
-        res = run_c3(args) if args.workload == "c3" else run_gpu(args)
+        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

@@ -518,6 +518,72 @@ def cpu_baseline_forest(inputs, gtrs, budget_node_patterns=4e7, seed=0):
                       "TreeTime, 1 process" % (used, done_units), "seconds": secs}
 
 
+C4_WORKLOAD = ("c4: serving loop, Poisson arrivals at 200 req/s; 90% nucleotide jobs drawn from the c3 size "
+               "distribution (half reconstruction, half branch-length optimisation), 10% protein jobs of c2 shape "
+               "(site-specific model); 3 ancestral/branch-length iterations per job, device-resident state, "
+               "admission by free HBM, one stream per admitted job")
+
+
+def run_c4(args):
+    """--workload c4: the serving loop under Poisson arrivals.  The request
+    pool (64 distinct nucleotide jobs from the batch's size distribution, 2
+    protein jobs) is generated before the timed window; requests sample it."""
+    import torch
+    from treetime_gb300 import TreeAnc, serving, synth
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(40 + rank)
+    nuc, nuc_gtrs = synth.forest_c3(n_trees=64, seed=41 + rank)
+    prot = []
+    for s in range(2):
+        wl = synth.make_workload("c2", seed=50 + s + 10 * rank)
+        t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], compress=False, verbose=0, device=dev)
+        prot.append((t._get_session()["forest"].inputs[0], t.gtr))
+    rate, window = 200.0, args.c4_seconds
+    n = int(rng.poisson(rate * window))
+    arrivals = np.sort(rng.uniform(0.0, window, size=n))
+    jobs = []
+    for i in range(n):
+        if rng.random() < 0.1:
+            ti, g = prot[int(rng.integers(len(prot)))]
+            jobs.append(serving.Job(ti, g, kind="marginal", iterations=3))
+        else:
+            k = int(rng.integers(len(nuc)))
+            jobs.append(serving.Job(nuc[k], nuc_gtrs[k], kind="marginal" if rng.random() < 0.5 else "optimize",
+                                    iterations=3))
+    # warm: one job of each kind (kernels configured, allocator and pinned pools primed)
+    warm = [serving.Job(nuc[0], nuc_gtrs[0], "marginal"), serving.Job(nuc[1], nuc_gtrs[1], "optimize"),
+            serving.Job(prot[0][0], prot[0][1], "marginal")]
+    serving.Server(device=dev, max_slots=args.c4_slots).serve(warm, [0.0, 0.0, 0.0])
+    srv = serving.Server(device=dev, max_slots=args.c4_slots)
+    with ClockSampler(local) as clk:
+        done, wall = srv.serve(jobs, arrivals)
+    st = serving.latency_stats(done)
+    if rank != 0:
+        return None
+    return {
+        "metric": METRIC, "value": world * st["node_pattern_updates"] / wall, "unit": UNIT, "n_gpus": world,
+        "steps": len(done), "warmup": len(warm), "ms_per_step": wall * 1e3 / max(1, len(done)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded request pool: c3-distribution nucleotide trees, c2-shape protein trees)",
+        "config": {"workload": C4_WORKLOAD, "arrival_rate_per_s": rate, "window_s": window, "requests": n,
+                   "slots": args.c4_slots, "pool": {"nucleotide": len(nuc), "protein": len(prot)},
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "latency_s": {"p50": st["p50"], "p99": st["p99"], "max": st["max"]},
+        "served": {"jobs": len(done), "wall_s": wall, "jobs_per_s": len(done) / wall,
+                   "node_pattern_updates": st["node_pattern_updates"], "peak_concurrent_jobs": srv.peak_active,
+                   "kinds": {"nucleotide_marginal": sum(1 for j in done if j.kind == "marginal" and not j.site_specific),
+                             "nucleotide_optimize": sum(1 for j in done if j.kind == "optimize"),
+                             "protein_marginal": sum(1 for j in done if j.site_specific)}},
+        # library kernels per iteration: protein 2 (pass, tree sums); nucleotide 3 (branch matrices,
+        # pass, tree sums) plus 2 Brent launches for branch-length jobs
+        "gpu_launches": int(sum(j.iterations * (2 if j.site_specific else 3 + (2 if j.kind == "optimize" else 0))
+                                for j in done)),
+        "clocks": clk.summary(),
+    }
+
+
 def _marginal_only(engine, forest, model, bufs, pm, prec):
     """Launch only the marginal pruning kernel (branch matrices already made)."""
     import ctypes as C
@@ -669,9 +735,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
+    ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
+    ap.add_argument("--c4-slots", type=int, default=16, help="c4: jobs admitted at the same time")
     ap.add_argument("--shape", default="", help="c1: fixed FP32 launch shape threads/ctas_per_sm/ranges_per_sm "
                                                  "instead of the autotuner (profiling runs)")
     ap.add_argument("--c3-trees", type=int, default=256,
@@ -683,7 +751,7 @@ def main():
     else:
         from treetime_gb300 import build
         build.build()
-        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3}[args.workload](args)
+        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

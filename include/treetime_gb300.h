@@ -9,6 +9,7 @@
  *                        pre-order passes                        treetime/treeanc.py:762-932
  *                        (normalize_profile, prof2seq argmax     treetime/seq_utils.py:232-307)
  *   tt_marginal_ss       the same for GTR_site_specific models   treetime/gtr_site_specific.py:331-437
+ *   tt_marginal_ss_f32   its FP32 fast path
  *   tt_joint             TreeAnc._ml_anc_joint                   treetime/treeanc.py:934-1080
  *   tt_state_pairs       GTR.state_pair + TreeAnc.add_branch_state
  *                                                                treetime/gtr.py:631-712, treetime/treeanc.py:1148-1163
@@ -215,11 +216,39 @@ tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt_pmats* pm,
  * equilibrium frequencies; P_a(t) evaluated in the eigenbasis, with TreeTime's linear
  * interpolation on the time grid `t_grid` (n_grid points) when `approximate` is set and
  * t * rate_scale < 10 (treetime/gtr_site_specific.py:331-437).  Single-tree forests only.
- *   lam [P][q], V [P][q][q], Vinv [P][q][q], mu [P], pi [P][q]  (FP64, per pattern) */
+ *   lam [P][q], V [P][q][q], Vinv [P][q][q], mu [P], pi [P][q]  (FP64, per pattern)
+ * FP64 log-domain kernel (precision must be TT_PREC_F64); the FP32 path is tt_marginal_ss_f32. */
 tt_status tt_marginal_ss(const tt_forest* f, const double* lam, const double* V, const double* Vinv,
                          const double* mu, const double* pi, const double* lut, const double* t_grid,
                          int32_t n_grid, double rate_scale, int32_t approximate, int32_t precision,
                          const tt_marginal_out* out, int32_t* status, void* stream);
+
+/* Site-specific model in FP32 layouts for tt_marginal_ss_f32.  V and Vinv are interleaved by site
+ * (element e of site a at [e * n_sites + a], consecutive sites are consecutive words): V_a[i][k] at
+ * e = i*q + k and V_a^-1[k][j] at e = k*q + j (the transposes of GTR_site_specific.v / v_inv per
+ * site).  The per-site vectors are rows of `width` floats (q padded with zeros to the forest's
+ * row width) so that a thread reads its site's row with vector loads. */
+typedef struct tt_ss_f32 {
+    int32_t n_sites;        /* = the forest's n_patterns (one tree, compress=False)                */
+    int32_t n_grid;         /* points of the interpolation grid; 0: exact exponentials everywhere */
+    const float* V;         /* [q*q][n_sites]                                                      */
+    const float* Vinv;      /* [q*q][n_sites]                                                      */
+    const float* mulam;     /* [n_sites][width]: mu_a * lambda_a,k                                 */
+    const float* pi;        /* [n_sites][width]: equilibrium frequencies (root prior)              */
+    const float* em1_grid;  /* [n_grid][n_sites][width]: expm1(grid_g * mu_a * lambda_a,k), computed in
+                               FP64: TreeTime's interpolated P(t) (approximate=True) interpolates
+                               matrices that share V_a, i.e. it interpolates d - 1 linearly      */
+    const double* grid;     /* [n_grid] time grid of the interpolated P(t)                         */
+    const double* lut;      /* [256][q] character -> profile table                                 */
+    double rate_scale;      /* branches with t * rate_scale >= 10 use exact exponentials           */
+} tt_ss_f32;
+
+/* FP32 marginal reconstruction under a site-specific model: one CTA per range of at most 32
+ * sites ([n_ranges][4] = (0, first site, site count, 0)), the range's V and V^-1 in shared memory.
+ * Replaces TreeAnc._ml_anc_marginal with GTR_site_specific (treetime/treeanc.py:762-932,
+ * treetime/gtr_site_specific.py:331-437) like tt_marginal_ss, in FP32 with power-of-two scaling. */
+tt_status tt_marginal_ss_f32(const tt_forest* f, const tt_ss_f32* m, const int32_t* ranges, int32_t n_ranges,
+                             const tt_marginal_out* out, int32_t* status, void* stream);
 
 /* ------------------------------------------------------------ a13: joint
  * Max-product reconstruction in FP64 (log domain), root argmax/sampling, pre-order backtrack.

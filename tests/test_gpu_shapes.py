@@ -115,3 +115,26 @@ def test_forest_of_many_trees(precision):
         for j, n in enumerate(ti.layout.nodes[:ti.layout.n_int]):
             rows = post[tr["prof_base"] + j * P: tr["prof_base"] + (j + 1) * P, :4]
             np.testing.assert_allclose(rows, ref["profile"][n.name], atol=1e-5 if precision == "f32" else 1e-10)
+
+
+@pytest.mark.parametrize("width", [1, 7, 32, None])
+@pytest.mark.parametrize("approximate", [True, False])
+def test_site_specific_f32_range_widths(width, approximate):
+    """The FP32 site-specific kernel (site ranges of 1..32 sites with their
+    eigenvectors in shared memory) against the FP64 kernel, with masks and
+    tips reconstructed."""
+    from treetime_gb300 import TreeAnc, engine, synth
+    wl = synth.make_workload("c2", seed=4, n=30, L=70, approximate=approximate)
+    t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], compress=False, verbose=0, precision="f64")
+    rng = np.random.default_rng(3)
+    for n in list(t.tree.find_clades())[2:7]:
+        n.mask = (rng.random(t.data.compressed_length) < 0.5).astype(float)
+    s = t._get_session()
+    kw = dict(reconstruct_tips=True, keep_outgroup=True, tip_outgroup=True)
+    r64 = engine.marginal_site_specific(s["forest"], t.gtr, engine.Buffers(s["forest"]), precision="f64", **kw)
+    r32 = engine.marginal_site_specific(s["forest"], t.gtr, engine.Buffers(s["forest"]), precision="f32",
+                                        range_width=width, **kw)
+    lh64, lh32 = float(r64["tree_lh"][0]), float(r32["tree_lh"][0])
+    assert abs(lh32 - lh64) <= 1e-6 * abs(lh64)
+    for k in ("posterior", "tip_posterior", "outgroup", "tip_outgroup"):
+        np.testing.assert_allclose(r32[k].cpu().numpy(), r64[k].cpu().numpy(), atol=1e-5, rtol=0)

@@ -50,6 +50,11 @@ class TTPmats(C.Structure):
     _fields_ = [("p64", vp), ("p32", vp), ("logp64", vp), ("p32_pair", vp)]
 
 
+class TTSSF32(C.Structure):
+    _fields_ = [("n_sites", i32), ("n_grid", i32), ("V", vp), ("Vinv", vp), ("mulam", vp), ("pi", vp),
+                ("em1_grid", vp), ("grid", vp), ("lut", vp), ("rate_scale", C.c_double)]
+
+
 class TTMarginalOut(C.Structure):
     _fields_ = [("partial", vp), ("posterior", vp), ("outgroup", vp), ("tip_posterior", vp),
                 ("tip_outgroup", vp), ("states", vp), ("site_lh", vp), ("tree_lh", vp), ("n_diff", vp),
@@ -71,6 +76,7 @@ _SIGS = {
     "tt_propagate": (i32, [i32, i64, vp, vp, vp, i32, i32, vp, vp]),
     "tt_marginal": (i32, [P(TTForest), P(TTModel), P(TTPmats), i32, P(TTMarginalOut), vp, vp]),
     "tt_marginal_ss": (i32, [P(TTForest), vp, vp, vp, vp, vp, vp, vp, i32, f64, i32, i32, P(TTMarginalOut), vp, vp]),
+    "tt_marginal_ss_f32": (i32, [P(TTForest), P(TTSSF32), vp, i32, P(TTMarginalOut), vp, vp]),
     "tt_joint": (i32, [P(TTForest), P(TTModel), P(TTPmats), P(TTJointOut), vp, vp]),
     "tt_joint_noalloc": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, vp, vp]),
     "tt_state_pairs": (i32, [P(TTForest), vp, vp, i32, i32, i32, vp, vp, vp]),

@@ -400,12 +400,15 @@ extern "C" tt_status tt_marginal_ss(const tt_forest* f, const double* lam, const
     cudaStream_t s = as_stream(stream);
     int blocks = f->max_blocks > 0 && f->max_blocks < f->n_work ? f->max_blocks : f->n_work;
     tt_status st;
-    const bool f32 = precision == TT_PREC_F32;
+    if (precision != TT_PREC_F64) {
+        set_error("tt_marginal_ss: FP64 only; the FP32 path is tt_marginal_ss_f32");
+        return TT_ERR_UNSUPPORTED;
+    }
     switch (f->n_states) {
-        case 4: st = f32 ? launch_ss<float, 4>(prm, blocks, s) : launch_ss<double, 4>(prm, blocks, s); break;
-        case 20: st = f32 ? launch_ss<float, 20>(prm, blocks, s) : launch_ss<double, 20>(prm, blocks, s); break;
-        case 21: st = f32 ? launch_ss<float, 21>(prm, blocks, s) : launch_ss<double, 21>(prm, blocks, s); break;
-        case 22: st = f32 ? launch_ss<float, 22>(prm, blocks, s) : launch_ss<double, 22>(prm, blocks, s); break;
+        case 4: st = launch_ss<double, 4>(prm, blocks, s); break;
+        case 20: st = launch_ss<double, 20>(prm, blocks, s); break;
+        case 21: st = launch_ss<double, 21>(prm, blocks, s); break;
+        case 22: st = launch_ss<double, 22>(prm, blocks, s); break;
         default:
             set_error("tt_marginal_ss: alphabet size %d not compiled (4, 20, 21, 22)", f->n_states);
             return TT_ERR_UNSUPPORTED;

@@ -535,25 +535,63 @@ class CapturedMarginal:
         return self.out
 
 
+def _ss_f32_model(forest, gtr, bufs, dev, range_width=None):
+    """FP32 site-interleaved model arrays and site ranges for tt_marginal_ss_f32
+    (cached per model, forest and range width)."""
+    key = (model_key(gtr), range_width)
+    cache = bufs.cache.get("ss_f32")
+    if cache is not None and cache[0] == key:
+        return cache[1]
+    t = torch()
+    lam, V, Vi = site_matrices(gtr)                    # [P][q], [P][q][q], [P][q][q] (FP64)
+    P, q = lam.shape
+    w = forest.w
+    mu = np.asarray(gtr.mu, dtype=np.float64).reshape(-1)
+    mulam = mu[:, None] * lam                          # [P][q]
+
+    def rows(x):                                       # [..., q] -> [..., w] float32, zero padded
+        out = np.zeros(x.shape[:-1] + (w,), dtype=np.float32)
+        out[..., :q] = x
+        return out
+
+    arrs = dict(
+        V=_to_dev(np.ascontiguousarray(V.transpose(1, 2, 0).reshape(q * q, P)).astype(np.float32), dev),
+        Vi=_to_dev(np.ascontiguousarray(Vi.transpose(1, 2, 0).reshape(q * q, P)).astype(np.float32), dev),
+        mulam=_to_dev(rows(mulam), dev),
+        pi=_to_dev(rows(np.asarray(gtr.Pi, dtype=np.float64).T), dev),
+        lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev))
+    n_grid = 0
+    if gtr.approximate:
+        grid = site_grid(gtr)
+        n_grid = len(grid)
+        em1 = np.expm1(grid[:, None, None] * mulam[None, :, :])  # [n_grid][P][q]
+        arrs["grid"] = _to_dev(grid, dev)
+        arrs["em1"] = _to_dev(rows(em1), dev)
+    # site ranges: about one per SM, at most 32 sites
+    sms = _lib.load().tt_device_sm_count()
+    width = int(min(32, max(1, range_width or math.ceil(P / max(1, sms)))))
+    starts = np.arange(0, P, width)
+    ranges = np.zeros((len(starts), 4), dtype=np.int32)
+    ranges[:, 1] = starts
+    ranges[:, 2] = np.minimum(width, P - starts)
+    arrs["ranges"] = _to_dev(ranges, dev)
+    arrs["struct"] = _lib.TTSSF32(P, n_grid, _p(arrs["V"]), _p(arrs["Vi"]), _p(arrs["mulam"]), _p(arrs["pi"]),
+                                  _p(arrs.get("em1")), _p(arrs.get("grid")), _p(arrs["lut"]),
+                                  float(gtr.rate_scale))
+    bufs.cache["ss_f32"] = (key, arrs)
+    return arrs
+
+
 def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=False, keep_outgroup=False,
-                           tip_outgroup=False, count_diff=False, root_uniform=None, sync=True):
-    """Marginal pass for a GTR_site_specific model (single tree)."""
+                           tip_outgroup=False, count_diff=False, root_uniform=None, sync=True, range_width=None):
+    """Marginal pass for a GTR_site_specific model (single tree): FP64 log-domain
+    kernel, or the FP32 kernel with each site range's eigenvectors in shared
+    memory."""
     t = torch()
     lib = _lib.load()
     f32 = precision == "f32"
     dt = t.float32 if f32 else t.float64
     dev = forest.device
-    key = model_key(gtr)
-    cache = bufs.cache.get("ss_model")
-    if cache is None or cache[0] != key:
-        lam, V, Vi = site_matrices(gtr)
-        arrs = dict(lam=_to_dev(lam, dev), V=_to_dev(V, dev), Vi=_to_dev(Vi, dev),
-                    mu=_to_dev(np.asarray(gtr.mu, dtype=np.float64), dev),
-                    pi=_to_dev(np.ascontiguousarray(gtr.Pi.T), dev),
-                    lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev),
-                    grid=_to_dev(site_grid(gtr), dev))
-        bufs.cache["ss_model"] = (key, arrs)
-    arrs = bufs.cache["ss_model"][1]
     w = forest.w
     out = {
         "partial": bufs.get("partial", (forest.prof_rows, w), dt),
@@ -573,11 +611,27 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
     o = TTMarginalOut(_p(out["partial"]), _p(out["posterior"]), _p(out["outgroup"]), _p(out["tip_posterior"]),
                       _p(out["tip_outgroup"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
                       _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
-    check(lib.tt_marginal_ss(C.byref(forest.struct), _p(arrs["lam"]), _p(arrs["V"]), _p(arrs["Vi"]), _p(arrs["mu"]),
-                             _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]), int(arrs["grid"].numel()),
-                             float(gtr.rate_scale), int(bool(gtr.approximate)),
-                             _lib.TT_PREC_F32 if f32 else _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()),
-          "tt_marginal_ss")
+    if f32:
+        arrs = _ss_f32_model(forest, gtr, bufs, dev, range_width)
+        check(lib.tt_marginal_ss_f32(C.byref(forest.struct), C.byref(arrs["struct"]), _p(arrs["ranges"]),
+                                     int(arrs["ranges"].shape[0]), C.byref(o), _p(status), _stream()),
+              "tt_marginal_ss_f32")
+    else:
+        key = model_key(gtr)
+        cache = bufs.cache.get("ss_model")
+        if cache is None or cache[0] != key:
+            lam, V, Vi = site_matrices(gtr)
+            arrs = dict(lam=_to_dev(lam, dev), V=_to_dev(V, dev), Vi=_to_dev(Vi, dev),
+                        mu=_to_dev(np.asarray(gtr.mu, dtype=np.float64), dev),
+                        pi=_to_dev(np.ascontiguousarray(gtr.Pi.T), dev),
+                        lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev),
+                        grid=_to_dev(site_grid(gtr), dev))
+            bufs.cache["ss_model"] = (key, arrs)
+        arrs = bufs.cache["ss_model"][1]
+        check(lib.tt_marginal_ss(C.byref(forest.struct), _p(arrs["lam"]), _p(arrs["V"]), _p(arrs["Vi"]),
+                                 _p(arrs["mu"]), _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]),
+                                 int(arrs["grid"].numel()), float(gtr.rate_scale), int(bool(gtr.approximate)),
+                                 _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()), "tt_marginal_ss")
     if sync:
         _check_status(status)
     out["_keep"] = ru
@@ -640,13 +694,20 @@ def optimal_t_pairs(q, counts, model, model_of=None, tol=1e-10):
 
 def optimal_t_profiles(forest, model, node_of, pp, pp_row, pc, pc_row, precision, gap_state, ignore_gaps,
                        tol=1e-10):
+    dev = forest.device
+    return optimal_t_profiles_dev(forest, model, _to_dev(np.asarray(node_of, np.int32), dev), pp,
+                                  _to_dev(np.asarray(pp_row, np.int64), dev), pc,
+                                  _to_dev(np.asarray(pc_row, np.int64), dev), precision, gap_state, ignore_gaps, tol)
+
+
+def optimal_t_profiles_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, precision, gap_state, ignore_gaps,
+                           tol=1e-10):
+    """optimal_t_profiles with the branch list (int32 node ids) and the row
+    offsets (int64) already on the device: enqueues only, no host copy."""
     t = torch()
     lib = _lib.load()
     dev = forest.device
-    n = len(node_of)
-    d_node = _to_dev(np.asarray(node_of, np.int32), dev)
-    d_pp_row = _to_dev(np.asarray(pp_row, np.int64), dev)
-    d_pc_row = _to_dev(np.asarray(pc_row, np.int64), dev)
+    n = int(d_node.numel())
     tout = t.empty(n, dtype=t.float64, device=dev)
     info = t.empty(n, dtype=t.int32, device=dev)
     check(lib.tt_optimal_t_profiles(C.byref(forest.struct), C.byref(model.struct), n, _p(d_node), _p(pp),

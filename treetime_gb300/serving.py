@@ -1,0 +1,316 @@
+"""Request loop: continuous batching of reconstruction and branch-length jobs on one GPU.
+
+A job is one tree with its alignment and model and a number of iterations of
+TreeTime's ancestral / branch-length cycle:
+
+  * ``"marginal"``: marginal ancestral reconstruction, repeated (FP32 kernel;
+    the site-specific kernel for ``GTR_site_specific`` models);
+  * ``"optimize"``: marginal reconstruction, then profile-mode Brent on every
+    branch below the root from the outgroup and subtree profiles
+    (``optimal_marginal_branch_length``, treetime/treeanc.py:1272-1295) and the
+    damped update of ``optimize_tree_marginal`` (treetime/treeanc.py:1297-1360,
+    damping 0.75; the root's two children are optimised independently rather
+    than as one combined branch), repeated on the new branch lengths.
+
+The scheduler runs on the calling thread.  Jobs are admitted in arrival order
+while a slot is free and the job's device footprint fits the memory budget
+(admission by free HBM); an admitted job keeps its schedule, inputs and
+profile buffers resident on the device for all its iterations and runs on its
+own CUDA stream, so the kernels of every admitted job overlap on the GPU.  The
+scheduler polls the jobs' events: a job whose iteration has finished gets its
+next iteration enqueued at once (iteration-level scheduling), a finished job
+has its results copied back and leaves, and its slot and memory go to the next
+job in the queue.  A job's numbers do not depend on which other jobs share the
+GPU with it (each kernel reads only its own job's buffers)."""
+
+import collections
+import threading
+import time
+
+import numpy as np
+
+from . import engine
+
+KINDS = ("marginal", "optimize")
+
+
+class Job:
+    """One request: ``inputs`` (an ``engine.TreeInput``), ``gtr`` (GTR or
+    GTR_site_specific), ``kind`` and ``iterations``.  After completion
+    ``result`` holds ``tree_lh`` (per iteration), ``states`` (the internal
+    nodes' reconstructed state indices, [n_int, P]) and ``branch_lengths``
+    (the final ones, per node), and ``t_submit`` / ``t_admit`` / ``t_done``
+    the host clock at those events (seconds)."""
+
+    _next_id = 0
+
+    def __init__(self, inputs, gtr, kind="marginal", iterations=3, job_id=None):
+        if kind not in KINDS:
+            raise ValueError("kind must be one of %s" % (KINDS,))
+        if kind == "optimize" and getattr(gtr, "is_site_specific", False):
+            raise NotImplementedError("branch-length jobs need a standard GTR model")
+        self.inputs = inputs
+        self.gtr = gtr
+        self.kind = kind
+        self.iterations = int(iterations)
+        self.site_specific = bool(getattr(gtr, "is_site_specific", False))
+        if job_id is None:
+            job_id = Job._next_id
+            Job._next_id += 1
+        self.id = job_id
+        self.t_submit = self.t_admit = self.t_done = None
+        self.result = None
+        self.footprint = footprint(inputs, gtr.n_states, kind)
+
+    @property
+    def node_patterns(self):
+        """Node-pattern updates of one iteration."""
+        return self.inputs.layout.n_nodes * self.inputs.n_patterns
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_submit
+
+
+def footprint(inputs, q, kind):
+    """Upper estimate of the device bytes a job holds while admitted: FP32
+    partial / posterior / outgroup rows, states, tip codes, branch matrices
+    (FP64, FP32 and the paired FP32 copy), schedule arrays."""
+    lay, P = inputs.layout, inputs.n_patterns
+    w = engine.WIDTHS[q]
+    rows = lay.n_int * P * w * 4
+    prof = rows * (3 if kind == "optimize" else 2) + (lay.n_tip * P * w * 4 if kind == "optimize" else 0)
+    mats = lay.n_nodes * q * w * (8 + 4 + 8)
+    other = lay.n_nodes * P + inputs.tip_codes.size + lay.n_nodes * 64 + P * 24
+    return int((prof + mats + other) * 1.1) + (1 << 20)
+
+
+def plan_admissions(queue, free_slots, free_bytes):
+    """Jobs to admit now, in arrival order: each while a slot is free and its
+    footprint fits the free bytes.  A job that does not fit waits at the head
+    of the queue (later, smaller jobs do not overtake it, so none starves)."""
+    out = []
+    for job in queue:
+        if free_slots <= 0 or job.footprint > free_bytes:
+            break
+        out.append(job)
+        free_slots -= 1
+        free_bytes -= job.footprint
+    return out
+
+
+class _Active:
+    """Device state of an admitted job."""
+
+    def __init__(self, job, server):
+        t = engine.torch()
+        self.job = job
+        self.stream = server._stream_pool.pop() if server._stream_pool else t.cuda.Stream(device=server.device)
+        dev = server.device
+        with t.cuda.stream(self.stream):
+            self.forest = engine.Forest([job.inputs], job.gtr.n_states, device=dev)
+            self.bufs = engine.Buffers(self.forest)
+            self.model = None if job.site_specific else engine.model_for(job.gtr, dev)
+            self.lh = t.zeros(job.iterations, dtype=t.float64, device=dev)
+            self.status = t.zeros(1, dtype=t.int32, device=dev)
+            if job.kind == "optimize":
+                self._prepare_optimize(dev)
+        self.it = 0
+        self.event = t.cuda.Event()
+        self.done_event = None
+        self.host = None
+
+    def _prepare_optimize(self, dev):
+        t = engine.torch()
+        lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
+        nodes = [k for k in range(lay.n_nodes) if lay.parent[k] >= 0]
+        internal = [k for k in nodes if k < lay.n_int]
+        tips = [k for k in nodes if k >= lay.n_int]
+        up = lambda x, dt: t.as_tensor(np.asarray(x), dtype=dt, device=dev)
+        self.opt = dict(internal=internal, tips=tips,
+                        n_int32=up(internal, t.int32), n_tip32=up(tips, t.int32),
+                        int_rows=up([k * P for k in internal], t.int64),
+                        tip_rows=up([(k - lay.n_int) * P for k in tips], t.int64),
+                        no_rows=up([-1] * len(tips), t.int64),
+                        d_int=up(internal, t.int64), d_tip=up(tips, t.int64),
+                        floor=engine.ttconf.MIN_BRANCH_LENGTH / float(self.job.inputs.mult.sum()),
+                        bl=up(self.job.inputs.bl, t.float64))
+
+    def enqueue_iteration(self):
+        """Queue one iteration on the job's stream (no host synchronisation)."""
+        t = engine.torch()
+        job = self.job
+        with t.cuda.stream(self.stream):
+            if job.site_specific:
+                out = engine.marginal_site_specific(self.forest, job.gtr, self.bufs, precision="f32", sync=False)
+            else:
+                keep = job.kind == "optimize"
+                out = engine.marginal(self.forest, self.model, self.bufs, precision="f32", keep_outgroup=keep,
+                                      tip_outgroup=keep, sync=False)
+            self.lh[self.it].copy_(out["tree_lh"][0])
+            self.status.copy_(t.maximum(self.status, self.bufs.get("status", (1,), t.int32)))
+            if job.kind == "optimize":
+                self._branch_lengths(out)
+            self.out = out
+            self.event.record(self.stream)
+        self.it += 1
+
+    def _branch_lengths(self, out):
+        t = engine.torch()
+        o = self.opt
+        damp = 0.75 ** (self.it + 1)      # iteration i damps with 0.75^(i+1) ...
+        new = o["bl"].clone()
+        tol = 1e-8 + 0.01 ** (self.it + 1)  # ... and optimises to 1e-8 + 0.01^(i+1)
+        gap = self.job.gtr.gap_index
+        if o["internal"]:
+            ti, _ = engine.optimal_t_profiles_dev(self.forest, self.model, o["n_int32"], out["outgroup"],
+                                                  o["int_rows"], out["partial"], o["int_rows"], "f32", gap, True, tol)
+            new[o["d_int"]] = ti * (1 - damp) + o["bl"][o["d_int"]] * damp
+        if o["tips"]:
+            tt, _ = engine.optimal_t_profiles_dev(self.forest, self.model, o["n_tip32"], out["tip_outgroup"],
+                                                  o["tip_rows"], out["partial"], o["no_rows"], "f32", gap, True, tol)
+            new[o["d_tip"]] = tt * (1 - damp) + o["bl"][o["d_tip"]] * damp
+        o["bl"] = new
+        self.forest.d_bl.copy_(t.clamp(new, min=o["floor"]))
+
+    def enqueue_results(self):
+        """Copy the results to pinned host memory on the job's stream."""
+        t = engine.torch()
+        lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
+        with t.cuda.stream(self.stream):
+            states = self.out["states"][: lay.n_int * P]
+            self.host = dict(tree_lh=t.empty(self.lh.shape, dtype=t.float64, pin_memory=True),
+                             states=t.empty(states.shape, dtype=t.uint8, pin_memory=True),
+                             bl=t.empty(self.forest.d_bl.shape, dtype=t.float64, pin_memory=True),
+                             status=t.empty(1, dtype=t.int32, pin_memory=True))
+            self.host["tree_lh"].copy_(self.lh, non_blocking=True)
+            self.host["states"].copy_(states, non_blocking=True)
+            self.host["bl"].copy_(self.forest.d_bl, non_blocking=True)
+            self.host["status"].copy_(self.status, non_blocking=True)
+            self.done_event = t.cuda.Event()
+            self.done_event.record(self.stream)
+
+    def collect(self):
+        lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
+        st = int(self.host["status"][0])
+        if st:
+            engine.check(st, "serving job %s" % self.job.id)
+        self.job.result = dict(tree_lh=self.host["tree_lh"].numpy().copy(),
+                               states=self.host["states"].numpy().reshape(lay.n_int, P).copy(),
+                               branch_lengths=self.host["bl"].numpy().copy())
+
+
+class Server:
+    """Continuous-batching scheduler for one GPU.
+
+    ``max_slots``: jobs admitted at the same time (each gets a CUDA stream);
+    ``hbm_bytes``: device-memory budget for admitted jobs (default: 80% of the
+    free memory when the server starts)."""
+
+    def __init__(self, device=None, max_slots=16, hbm_bytes=None, poll_s=2e-5):
+        t = engine.torch()
+        self.device = engine.require_device(device)
+        if hbm_bytes is None:
+            free, _ = t.cuda.mem_get_info(self.device)
+            hbm_bytes = int(free * 0.8)
+        self.max_slots = int(max_slots)
+        self.hbm_bytes = int(hbm_bytes)
+        self.poll_s = poll_s
+        self._queue = collections.deque()
+        self._lock = threading.Lock()
+        self._active = []
+        self._stream_pool = []
+        self.done = []
+        self.peak_active = 0
+
+    def submit(self, job):
+        """Queue a job (thread-safe); it is admitted by the scheduler loop."""
+        job.t_submit = time.perf_counter()
+        with self._lock:
+            self._queue.append(job)
+
+    def _used_bytes(self):
+        return sum(a.job.footprint for a in self._active)
+
+    def step(self):
+        """One scheduler pass; returns True when something happened."""
+        busy = False
+        # finished jobs leave first: their slots and memory go to the queue
+        still = []
+        for a in self._active:
+            if a.done_event is not None and a.done_event.query():
+                a.collect()
+                a.job.t_done = time.perf_counter()
+                self.done.append(a.job)
+                self._stream_pool.append(a.stream)
+                busy = True
+            else:
+                still.append(a)
+        self._active = still
+        with self._lock:
+            plan = plan_admissions(self._queue, self.max_slots - len(self._active),
+                                   self.hbm_bytes - self._used_bytes())
+            for _ in plan:
+                self._queue.popleft()
+        for job in plan:
+            job.t_admit = time.perf_counter()
+            a = _Active(job, self)
+            a.enqueue_iteration()
+            self._active.append(a)
+            busy = True
+        self.peak_active = max(self.peak_active, len(self._active))
+        # iteration-level scheduling: a job whose iteration finished gets the next one now
+        for a in self._active:
+            if a.done_event is None and a.event.query():
+                if a.it < a.job.iterations:
+                    a.enqueue_iteration()
+                else:
+                    a.enqueue_results()
+                busy = True
+        return busy
+
+    def pending(self):
+        with self._lock:
+            return len(self._queue) + len(self._active)
+
+    def run(self, until=None):
+        """Scheduler loop until the queue and the GPU are empty (and, when
+        given, until() is true)."""
+        while True:
+            busy = self.step()
+            if not busy:
+                if self.pending() == 0 and (until is None or until()):
+                    return
+                time.sleep(self.poll_s)
+
+    def serve(self, jobs, arrival_times):
+        """Submit ``jobs`` at ``arrival_times`` (seconds from now, from a feeder
+        thread) and run the loop until all are done.  Returns the finished jobs
+        and the wall time."""
+        order = np.argsort(arrival_times)
+        t0 = time.perf_counter()
+        fed = threading.Event()
+
+        def feeder():
+            for i in order:
+                delay = t0 + arrival_times[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                self.submit(jobs[i])
+            fed.set()
+
+        th = threading.Thread(target=feeder, daemon=True)
+        th.start()
+        self.run(until=fed.is_set)
+        th.join()
+        return list(jobs), time.perf_counter() - t0
+
+
+def latency_stats(jobs):
+    """p50 / p99 / max latency (s) and node-pattern updates of finished jobs."""
+    lat = np.array([j.latency for j in jobs if j.latency is not None])
+    units = sum(j.node_patterns * j.iterations for j in jobs if j.t_done is not None)
+    if lat.size == 0:
+        return dict(p50=None, p99=None, max=None, node_pattern_updates=units)
+    return dict(p50=float(np.percentile(lat, 50)), p99=float(np.percentile(lat, 99)), max=float(lat.max()),
+                node_pattern_updates=int(units))

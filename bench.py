@@ -573,6 +573,7 @@ def run_c4(args):
         "latency_s": {"p50": st["p50"], "p99": st["p99"], "max": st["max"]},
         "served": {"jobs": len(done), "wall_s": wall, "jobs_per_s": len(done) / wall,
                    "node_pattern_updates": st["node_pattern_updates"], "peak_concurrent_jobs": srv.peak_active,
+                   "scheduler_host_s": {k: round(v, 3) for k, v in srv.host_s.items()},
                    "kinds": {"nucleotide_marginal": sum(1 for j in done if j.kind == "marginal" and not j.site_specific),
                              "nucleotide_optimize": sum(1 for j in done if j.kind == "optimize"),
                              "protein_marginal": sum(1 for j in done if j.site_specific)}},

@@ -14,6 +14,7 @@ Layout of a forest in device memory (see include/treetime_gb300.h):
 """
 
 import ctypes as C
+import time
 
 import math
 
@@ -54,6 +55,41 @@ def _p(t):
 
 def _stream():
     return C.c_void_p(torch().cuda.current_stream().cuda_stream)
+
+
+class Uploader:
+    """Packs host arrays into one page-locked staging buffer and copies them
+    to the device with a single non-blocking copy on the current stream;
+    ``finish`` returns typed device views (each at a 256-byte aligned offset
+    of one device buffer).  One asynchronous copy instead of one synchronous
+    pageable copy per array: the latter stalls the host for milliseconds per
+    array while other streams keep the GPU busy."""
+
+    def __init__(self):
+        self.items = []
+        self.size = 0
+
+    def add(self, name, arr):
+        a = np.ascontiguousarray(arr)
+        off = (self.size + 255) & ~255
+        self.items.append((name, a, off))
+        self.size = off + a.nbytes
+        return self
+
+    def finish(self, device):
+        t = torch()
+        stage = t.empty(max(1, self.size), dtype=t.uint8, pin_memory=True)
+        host = stage.numpy()
+        for _, a, off in self.items:
+            host[off:off + a.nbytes] = a.view(np.uint8).reshape(-1)
+        dbuf = stage.to(device, non_blocking=True)
+        out = {}
+        for name, a, off in self.items:
+            tdt = t.from_numpy(a[:0]).dtype if a.size else t.uint8
+            view = dbuf[off:off + a.nbytes].view(tdt)
+            out[name] = view.view(a.shape) if a.size else view
+        out["_buffer"] = dbuf
+        return out
 
 
 def _to_dev(arr, device, dtype=None):
@@ -265,6 +301,7 @@ class Forest:
 
     def __init__(self, inputs, q, device=None, warps_per_block=None, max_blocks=0, threads=None,
                  ctas_per_sm=1, range_patterns=None, ranges_per_sm=1):
+        t_build = time.perf_counter()
         dev = require_device(device)
         self.device = dev
         self.inputs = list(inputs)
@@ -379,30 +416,36 @@ class Forest:
         ranges.sort(key=lambda r: -r[0])
         self.work_f32_host = np.array([(t, p0, w_, 0) for _, t, p0, w_ in ranges], dtype=np.int32).reshape(-1, 4)
         self.trees_host = trees
+        self.max_model = int(max((ti.model for ti in inputs), default=0))
+        t_up = time.perf_counter()
         self.n_nodes = node_base
         self.n_patterns = pat_base
         self.prof_rows = prof_base
         self.tip_rows = tipprof_base
         self.state_rows = state_base
-        self.d_trees = _to_dev(trees.view(np.uint8), dev)
-        self.d_level = _to_dev(np.concatenate(lev).astype(np.int32), dev)
-        self.d_child_off = _to_dev(child_off, dev)
-        self.d_child_idx = _to_dev(np.concatenate(cidx).astype(np.int32) if total_children else
-                                   np.zeros(1, np.int32), dev)
-        self.d_parent = _to_dev(np.concatenate(par), dev)
-        self.d_tip_row = _to_dev(np.concatenate(trow), dev)
+        up = Uploader()
+        up.add("trees", trees.view(np.uint8)).add("level", np.concatenate(lev).astype(np.int32))
+        up.add("child_off", child_off)
+        up.add("child_idx", np.concatenate(cidx).astype(np.int32) if total_children else np.zeros(1, np.int32))
+        up.add("parent", np.concatenate(par)).add("tip_row", np.concatenate(trow))
         self.bl_host = np.concatenate(bl)
-        self.d_bl = _to_dev(self.bl_host, dev)
-        self.d_mult = _to_dev(np.concatenate(mult), dev)
-        self.d_codes = _to_dev(np.concatenate(codes) if codes else np.zeros(1, np.uint8), dev)
+        up.add("bl", self.bl_host).add("mult", np.concatenate(mult))
+        up.add("codes", np.concatenate(codes) if codes else np.zeros(1, np.uint8))
         self.has_masks = mask_elems > 0
-        self.d_mask_off = _to_dev(np.concatenate(moff), dev) if self.has_masks else None
-        self.d_masks = _to_dev(np.concatenate(mvals), dev) if self.has_masks else None
-        self.d_work = _to_dev(self.work_host, dev)
-        self.d_work_f32 = _to_dev(self.work_f32_host, dev)
-        self.d_node_rec = _to_dev(np.concatenate(recs), dev)
-        self.d_child_pair = _to_dev(np.concatenate(pairs), dev)
-        self.d_pair_slot = _to_dev(np.concatenate(pslots), dev)
+        if self.has_masks:
+            up.add("mask_off", np.concatenate(moff)).add("masks", np.concatenate(mvals))
+        up.add("work", self.work_host).add("work_f32", self.work_f32_host)
+        up.add("node_rec", np.concatenate(recs)).add("child_pair", np.concatenate(pairs))
+        up.add("pair_slot", np.concatenate(pslots))
+        d = up.finish(dev)
+        self._dev_buffer = d["_buffer"]
+        self.d_trees, self.d_level, self.d_child_off = d["trees"], d["level"], d["child_off"]
+        self.d_child_idx, self.d_parent, self.d_tip_row = d["child_idx"], d["parent"], d["tip_row"]
+        self.d_bl, self.d_mult, self.d_codes = d["bl"], d["mult"], d["codes"]
+        self.d_mask_off = d.get("mask_off")
+        self.d_masks = d.get("masks")
+        self.d_work, self.d_work_f32 = d["work"], d["work_f32"]
+        self.d_node_rec, self.d_child_pair, self.d_pair_slot = d["node_rec"], d["child_pair"], d["pair_slot"]
         if warps_per_block is None:
             warps_per_block = 16 if len(self.work_host) < 2 * sms else 8
         self.struct = TTForest(
@@ -412,6 +455,7 @@ class Forest:
             _p(self.d_bl), _p(self.d_codes), _p(self.d_mult), _p(self.d_work), len(self.work_host),
             warps_per_block, max_blocks, lanes_per_pattern, _p(self.d_work_f32), len(self.work_f32_host),
             0, _p(self.d_node_rec), _p(self.d_child_pair), _p(self.d_pair_slot), threads, self.ctas_per_sm)
+        self.build_s = (t_up - t_build, time.perf_counter() - t_up)  # host preparation, device uploads
 
     def set_branch_lengths(self, bl_list):
         """Replace branch lengths (same topology) without rebuilding."""
@@ -461,6 +505,12 @@ def branch_pmats(forest, model, bufs, need32=False, needlog=False):
     return pm, status
 
 
+def _check_models(forest, model):
+    if forest.max_model >= model.struct.n_models:
+        raise ValueError("a tree of the forest uses model %d, the DeviceModel holds %d"
+                         % (forest.max_model, model.struct.n_models))
+
+
 def _check_status(status):
     s = int(status.item())
     if s:
@@ -476,6 +526,7 @@ def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_
     lib = _lib.load()
     f32 = precision == "f32"
     dt = t.float32 if f32 else t.float64
+    _check_models(forest, model)
     pm, status = branch_pmats(forest, model, bufs, need32=f32)
     w = forest.w
     out = {
@@ -535,13 +586,16 @@ class CapturedMarginal:
         return self.out
 
 
+_SS_F32_CACHE = {}
+
+
 def _ss_f32_model(forest, gtr, bufs, dev, range_width=None):
     """FP32 site-interleaved model arrays and site ranges for tt_marginal_ss_f32
-    (cached per model, forest and range width)."""
-    key = (model_key(gtr), range_width)
-    cache = bufs.cache.get("ss_f32")
-    if cache is not None and cache[0] == key:
-        return cache[1]
+    (cached per model, row width, device and range width)."""
+    key = (model_key(gtr), forest.w, str(dev), range_width)
+    hit = _SS_F32_CACHE.get(key)
+    if hit is not None:
+        return hit
     t = torch()
     lam, V, Vi = site_matrices(gtr)                    # [P][q], [P][q][q], [P][q][q] (FP64)
     P, q = lam.shape
@@ -578,7 +632,9 @@ def _ss_f32_model(forest, gtr, bufs, dev, range_width=None):
     arrs["struct"] = _lib.TTSSF32(P, n_grid, _p(arrs["V"]), _p(arrs["Vi"]), _p(arrs["mulam"]), _p(arrs["pi"]),
                                   _p(arrs.get("em1")), _p(arrs.get("grid")), _p(arrs["lut"]),
                                   float(gtr.rate_scale))
-    bufs.cache["ss_f32"] = (key, arrs)
+    if len(_SS_F32_CACHE) > 16:
+        _SS_F32_CACHE.clear()
+    _SS_F32_CACHE[key] = arrs
     return arrs
 
 
@@ -641,6 +697,7 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
 def joint(forest, model, bufs, reconstruct_tips=False, count_diff=False, root_uniform=None, sync=True):
     t = torch()
     lib = _lib.load()
+    _check_models(forest, model)
     pm, status = branch_pmats(forest, model, bufs, needlog=True)
     w = forest.w
     out = {

@@ -24,6 +24,7 @@ job in the queue.  A job's numbers do not depend on which other jobs share the
 GPU with it (each kernel reads only its own job's buffers)."""
 
 import collections
+import copy
 import threading
 import time
 
@@ -99,22 +100,56 @@ def plan_admissions(queue, free_slots, free_bytes):
     return out
 
 
+class _PinnedPool:
+    """Reusable page-locked host buffers by power-of-two size class (a fresh
+    page-locked allocation of a large job's results costs milliseconds)."""
+
+    def __init__(self):
+        self.free = collections.defaultdict(list)
+
+    def take(self, nbytes):
+        t = engine.torch()
+        cls = max(1 << 12, 1 << int(np.ceil(np.log2(max(1, nbytes)))))
+        if self.free[cls]:
+            return self.free[cls].pop()
+        return t.empty(cls, dtype=t.uint8, pin_memory=True)
+
+    def give(self, buf):
+        self.free[buf.numel()].append(buf)
+
+
+def _view(buf, shape, dtype):
+    t = engine.torch()
+    n = int(np.prod(shape)) * t.empty((), dtype=dtype).element_size()
+    return buf[:n].view(dtype).view(shape)
+
+
 class _Active:
     """Device state of an admitted job."""
 
     def __init__(self, job, server):
         t = engine.torch()
         self.job = job
+        self.pool = server._pinned
         self.stream = server._stream_pool.pop() if server._stream_pool else t.cuda.Stream(device=server.device)
         dev = server.device
+        ti = copy.copy(job.inputs)
+        ti.model = 0  # the job's own one-model DeviceModel
+        hs = server.host_s
         with t.cuda.stream(self.stream):
-            self.forest = engine.Forest([job.inputs], job.gtr.n_states, device=dev)
+            self.forest = engine.Forest([ti], job.gtr.n_states, device=dev)
+            hs["admit.forest_host"] += self.forest.build_s[0]
+            hs["admit.forest_upload"] += self.forest.build_s[1]
+            t0 = time.perf_counter()
             self.bufs = engine.Buffers(self.forest)
             self.model = None if job.site_specific else engine.model_for(job.gtr, dev)
             self.lh = t.zeros(job.iterations, dtype=t.float64, device=dev)
             self.status = t.zeros(1, dtype=t.int32, device=dev)
+            t1 = time.perf_counter()
+            hs["admit.model"] += t1 - t0
             if job.kind == "optimize":
                 self._prepare_optimize(dev)
+                hs["admit.optimize_setup"] += time.perf_counter() - t1
         self.it = 0
         self.event = t.cuda.Event()
         self.done_event = None
@@ -123,18 +158,19 @@ class _Active:
     def _prepare_optimize(self, dev):
         t = engine.torch()
         lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
-        nodes = [k for k in range(lay.n_nodes) if lay.parent[k] >= 0]
-        internal = [k for k in nodes if k < lay.n_int]
-        tips = [k for k in nodes if k >= lay.n_int]
-        up = lambda x, dt: t.as_tensor(np.asarray(x), dtype=dt, device=dev)
-        self.opt = dict(internal=internal, tips=tips,
-                        n_int32=up(internal, t.int32), n_tip32=up(tips, t.int32),
-                        int_rows=up([k * P for k in internal], t.int64),
-                        tip_rows=up([(k - lay.n_int) * P for k in tips], t.int64),
-                        no_rows=up([-1] * len(tips), t.int64),
-                        d_int=up(internal, t.int64), d_tip=up(tips, t.int64),
-                        floor=engine.ttconf.MIN_BRANCH_LENGTH / float(self.job.inputs.mult.sum()),
-                        bl=up(self.job.inputs.bl, t.float64))
+        k = np.arange(lay.n_nodes)
+        has_parent = np.asarray(lay.parent) >= 0
+        internal = k[has_parent & (k < lay.n_int)]
+        tips = k[has_parent & (k >= lay.n_int)]
+        up = engine.Uploader()
+        up.add("n_int32", internal.astype(np.int32)).add("n_tip32", tips.astype(np.int32))
+        up.add("int_rows", internal.astype(np.int64) * P).add("tip_rows", (tips - lay.n_int).astype(np.int64) * P)
+        up.add("no_rows", np.full(len(tips), -1, np.int64))
+        up.add("d_int", internal.astype(np.int64)).add("d_tip", tips.astype(np.int64))
+        up.add("bl", np.asarray(self.job.inputs.bl, np.float64))
+        d = up.finish(dev)
+        self.opt = dict(d, internal=len(internal) > 0, tips=len(tips) > 0,
+                        floor=engine.ttconf.MIN_BRANCH_LENGTH / float(self.job.inputs.mult.sum()))
 
     def enqueue_iteration(self):
         """Queue one iteration on the job's stream (no host synchronisation)."""
@@ -159,17 +195,18 @@ class _Active:
         t = engine.torch()
         o = self.opt
         damp = 0.75 ** (self.it + 1)      # iteration i damps with 0.75^(i+1) ...
-        new = o["bl"].clone()
+        old = o["bl"]
+        new = old.clone()
         tol = 1e-8 + 0.01 ** (self.it + 1)  # ... and optimises to 1e-8 + 0.01^(i+1)
         gap = self.job.gtr.gap_index
         if o["internal"]:
             ti, _ = engine.optimal_t_profiles_dev(self.forest, self.model, o["n_int32"], out["outgroup"],
                                                   o["int_rows"], out["partial"], o["int_rows"], "f32", gap, True, tol)
-            new[o["d_int"]] = ti * (1 - damp) + o["bl"][o["d_int"]] * damp
+            new[o["d_int"]] = ti * (1 - damp) + old[o["d_int"]] * damp
         if o["tips"]:
             tt, _ = engine.optimal_t_profiles_dev(self.forest, self.model, o["n_tip32"], out["tip_outgroup"],
                                                   o["tip_rows"], out["partial"], o["no_rows"], "f32", gap, True, tol)
-            new[o["d_tip"]] = tt * (1 - damp) + o["bl"][o["d_tip"]] * damp
+            new[o["d_tip"]] = tt * (1 - damp) + old[o["d_tip"]] * damp
         o["bl"] = new
         self.forest.d_bl.copy_(t.clamp(new, min=o["floor"]))
 
@@ -177,12 +214,15 @@ class _Active:
         """Copy the results to pinned host memory on the job's stream."""
         t = engine.torch()
         lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
+        pool = self.pool
         with t.cuda.stream(self.stream):
             states = self.out["states"][: lay.n_int * P]
-            self.host = dict(tree_lh=t.empty(self.lh.shape, dtype=t.float64, pin_memory=True),
-                             states=t.empty(states.shape, dtype=t.uint8, pin_memory=True),
-                             bl=t.empty(self.forest.d_bl.shape, dtype=t.float64, pin_memory=True),
-                             status=t.empty(1, dtype=t.int32, pin_memory=True))
+            self._bufs = [pool.take(self.lh.numel() * 8), pool.take(states.numel()),
+                          pool.take(self.forest.d_bl.numel() * 8), pool.take(4)]
+            self.host = dict(tree_lh=_view(self._bufs[0], self.lh.shape, t.float64),
+                             states=_view(self._bufs[1], states.shape, t.uint8),
+                             bl=_view(self._bufs[2], self.forest.d_bl.shape, t.float64),
+                             status=_view(self._bufs[3], (1,), t.int32))
             self.host["tree_lh"].copy_(self.lh, non_blocking=True)
             self.host["states"].copy_(states, non_blocking=True)
             self.host["bl"].copy_(self.forest.d_bl, non_blocking=True)
@@ -198,6 +238,8 @@ class _Active:
         self.job.result = dict(tree_lh=self.host["tree_lh"].numpy().copy(),
                                states=self.host["states"].numpy().reshape(lay.n_int, P).copy(),
                                branch_lengths=self.host["bl"].numpy().copy())
+        for b in self._bufs:
+            self.pool.give(b)
 
 
 class Server:
@@ -220,8 +262,12 @@ class Server:
         self._lock = threading.Lock()
         self._active = []
         self._stream_pool = []
+        self._pinned = _PinnedPool()
         self.done = []
         self.peak_active = 0
+        self.peak_bytes = 0
+        # host seconds spent per scheduler phase (admission, enqueueing, result copies, collection)
+        self.host_s = collections.Counter()
 
     def submit(self, job):
         """Queue a job (thread-safe); it is admitted by the scheduler loop."""
@@ -239,7 +285,9 @@ class Server:
         still = []
         for a in self._active:
             if a.done_event is not None and a.done_event.query():
+                t0 = time.perf_counter()
                 a.collect()
+                self.host_s["collect"] += time.perf_counter() - t0
                 a.job.t_done = time.perf_counter()
                 self.done.append(a.job)
                 self._stream_pool.append(a.stream)
@@ -255,17 +303,24 @@ class Server:
         for job in plan:
             job.t_admit = time.perf_counter()
             a = _Active(job, self)
+            t1 = time.perf_counter()
             a.enqueue_iteration()
+            self.host_s["admit"] += t1 - job.t_admit
+            self.host_s["enqueue"] += time.perf_counter() - t1
             self._active.append(a)
             busy = True
         self.peak_active = max(self.peak_active, len(self._active))
+        self.peak_bytes = max(self.peak_bytes, self._used_bytes())
         # iteration-level scheduling: a job whose iteration finished gets the next one now
         for a in self._active:
             if a.done_event is None and a.event.query():
+                t0 = time.perf_counter()
                 if a.it < a.job.iterations:
                     a.enqueue_iteration()
+                    self.host_s["enqueue"] += time.perf_counter() - t0
                 else:
                     a.enqueue_results()
+                    self.host_s["results"] += time.perf_counter() - t0
                 busy = True
         return busy
 

@@ -42,6 +42,18 @@ def _dist():
     return world, rank, local
 
 
+def _reduce_max(x, device, world):
+    """Max of a per-rank float over all ranks (the job time is the slowest
+    rank's); identity on one process."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    v = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(v, op=dist.ReduceOp.MAX)
+    return float(v.item())
+
+
 def _peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
@@ -212,12 +224,7 @@ def run_gpu(args):
             b.synchronize()
             kt.append(a.elapsed_time(b))
     torch.cuda.synchronize()
-    ms32 = sum(t32) / len(t32)
-    if world > 1:
-        import torch.distributed as dist
-        x = torch.tensor([ms32], device=dev)
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        ms32 = float(x.item())
+    ms32 = _reduce_max(sum(t32) / len(t32), dev, world)
 
     # end-to-end through host buffers (pinned), copies inside the timed region
     e2e_ms, h2d, d2h = _e2e(engine, t, forest, graphs["f32"], args.steps, args.warmup, flush)
@@ -403,12 +410,7 @@ def run_c3(args):
         t32 = timed(cap.replay, args.steps, args.warmup)
         pm, _ = engine.branch_pmats(forest, model, bufs, need32=True)
         kt = timed(lambda: _marginal_only(engine, forest, model, bufs, pm, "f32"), min(args.steps, 10), 1)
-    ms32 = sum(t32) / len(t32)
-    if world > 1:
-        import torch.distributed as dist
-        x = torch.tensor([ms32], device=dev)
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        ms32 = float(x.item())
+    ms32 = _reduce_max(sum(t32) / len(t32), dev, world)
 
     # end to end: every tree's tip codes, branch lengths and multiplicities from pinned host
     # memory, states and site log-likelihoods back, every step

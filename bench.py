@@ -520,7 +520,7 @@ def cpu_baseline_forest(inputs, gtrs, budget_node_patterns=4e7, seed=0):
                       "TreeTime, 1 process" % (used, done_units), "seconds": secs}
 
 
-C4_WORKLOAD = ("c4: serving loop, Poisson arrivals at 200 req/s; 90% nucleotide jobs drawn from the c3 size "
+C4_WORKLOAD = ("c4: serving loop, Poisson arrivals (200 req/s unless --c4-rate); 90% nucleotide jobs drawn from the c3 size "
                "distribution (half reconstruction, half branch-length optimisation), 10% protein jobs of c2 shape "
                "(site-specific model); 3 ancestral/branch-length iterations per job, device-resident state, "
                "admission by free HBM, one stream per admitted job")
@@ -542,7 +542,7 @@ def run_c4(args):
         wl = synth.make_workload("c2", seed=50 + s + 10 * rank)
         t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], compress=False, verbose=0, device=dev)
         prot.append((t._get_session()["forest"].inputs[0], t.gtr))
-    rate, window = 200.0, args.c4_seconds
+    rate, window = args.c4_rate, args.c4_seconds
     n = int(rng.poisson(rate * window))
     arrivals = np.sort(rng.uniform(0.0, window, size=n))
     jobs = []
@@ -742,6 +742,7 @@ def main():
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
+    ap.add_argument("--c4-rate", type=float, default=200.0, help="c4: mean arrival rate (requests/s)")
     ap.add_argument("--c4-slots", type=int, default=16, help="c4: jobs admitted at the same time")
     ap.add_argument("--shape", default="", help="c1: fixed FP32 launch shape threads/ctas_per_sm/ranges_per_sm "
                                                  "instead of the autotuner (profiling runs)")

@@ -305,13 +305,17 @@ tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts, const int3
  * outgroup) and child-side profiles pc (subtree) as rows of `width` elements at row offsets
  * pp_row[b], pc_row[b] (+ pattern), tips' child profiles from their codes when pc_row[b] < 0;
  * minimises -sum mult*mask*log(pc.P(s^2).pp + 1e-24)*non_gap + exp(s^4/1e4) with Brent.
- * `prec` says whether the profile buffers hold float or double.
- * Replaces GTR.optimal_t_compressed(profiles=True) with GTR.prob_t_profiles
- * (treetime/gtr.py:816-963). */
+ * `prec` says whether the profile buffers hold float or double.  Per branch the per-pattern
+ * eigen coefficients are computed once; those that do not fit in shared memory (about 200 KB /
+ * ((q + 1) * 8) patterns) go to `workspace` (device FP64, per persistent CTA: min(n, SM count)
+ * CTAs each need (P - that) * (q + 1) doubles) or, when it is NULL or too small, are recomputed
+ * at every objective evaluation.  Replaces GTR.optimal_t_compressed(profiles=True) with
+ * GTR.prob_t_profiles (treetime/gtr.py:816-963). */
 tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
                                 const void* pp, const int64_t* pp_row, const void* pc, const int64_t* pc_row,
                                 int32_t prec, int32_t gap_state, int32_t ignore_gaps, double tol,
-                                double* t_out, int32_t* info, void* stream);
+                                double* t_out, int32_t* info, double* workspace, int64_t workspace_bytes,
+                                void* stream);
 
 /* -------------------------------------------------- a1: compression
  * Column classes of a tips x sites byte matrix (row-major, n_rows x n_cols): key[c] = the letter

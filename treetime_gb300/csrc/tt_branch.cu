@@ -222,7 +222,9 @@ struct ProfParams {
     double tol;
     double* t_out;
     int32_t* info;
-    int cap;  // patterns staged in shared memory
+    int cap;            // patterns whose coefficients sit in shared memory
+    double* work;       // per-CTA coefficients of the patterns past `cap` (nullptr: recompute)
+    int64_t work_cta;   // doubles per CTA in `work`
 };
 
 __device__ double block_sum(double v, double* red) {
@@ -279,10 +281,50 @@ __device__ __forceinline__ void pattern_coeffs(const ProfParams& a, const tt_tre
     }
 }
 
-__global__ void optimal_t_profiles_kernel(ProfParams a) {
+// Natural log by the table-driven method of P. T. P. Tang ("Table-driven implementation of the
+// logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990): x = 2^e * m with
+// m in [1, 2); F = 1 + j/128 is the table point nearest m, so r = (m - F) / F has |r| <= 2^-8 (m - F
+// is exact) and log x = e ln2 + log F + log(1 + r), the last from its Taylor series to r^7
+// (truncation below 1e-20).  About 11 FP64 operations against the library log's longer sequence:
+// the profile objective takes one log per pattern per evaluation and GB300's FP64 rate is low.
+// logF / invF are the 129 table values log(F_j), 1/F_j.  x must be positive and normal.
+__device__ __forceinline__ double log_tang(double x, const double* logF, const double* invF) {
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    const int e = ((hi >> 20) & 0x7ff) - 1023;
+    const int mant = hi & 0x000fffff;
+    const double m = __hiloint2double(mant | 0x3ff00000, lo);  // in [1, 2)
+    const int j = (mant + (1 << 12)) >> 13;                      // nearest 1/128 step, 0..128
+    const double f = m - (1.0 + j * (1.0 / 128.0));              // exact
+    const double r = f * invF[j];
+    double p = 1.0 / 7.0;
+    p = fma(p, r, -1.0 / 6.0);
+    p = fma(p, r, 1.0 / 5.0);
+    p = fma(p, r, -1.0 / 4.0);
+    p = fma(p, r, 1.0 / 3.0);
+    p = fma(p, r, -0.5);
+    p = fma(p, r, 1.0);
+    return fma((double)e, kLn2, fma(p, r, logF[j]));
+}
+
+// One persistent CTA per SM loops over branches.  Per branch the per-pattern eigen coefficients
+// u (q of them) and the weight are computed once: the first `cap` patterns' in shared memory, the
+// rest in the CTA's slice of the workspace (or, without a workspace, recomputed at every
+// evaluation); each Brent evaluation is then a q-term sum, one log and one multiply-add per
+// pattern.  QT > 0: the alphabet size is a compile-time constant (arrays in registers).
+template <int QT>
+__global__ void __launch_bounds__(256) optimal_t_profiles_kernel(ProfParams a) {
+    constexpr int QA = QT > 0 ? QT : 32;  // array bound
     extern __shared__ double sm[];
     __shared__ double red[32];
-    const int q = a.f.n_states;
+    __shared__ double log_tab[129], inv_tab[129];
+    for (int j = threadIdx.x; j < 129; j += blockDim.x) {
+        const double F = 1.0 + j / 128.0;
+        log_tab[j] = log(F);
+        inv_tab[j] = 1.0 / F;
+    }
+    __syncthreads();
+    const int q = QT > 0 ? QT : a.f.n_states;
+    double* const work = a.work ? a.work + (int64_t)blockIdx.x * a.work_cta : nullptr;
     for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
         const int64_t g = a.node_of[b];
         const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
@@ -294,11 +336,12 @@ __global__ void optimal_t_profiles_kernel(ProfParams a) {
         const double* lam = a.m.lam + (int64_t)mi * q;
         const double mu = a.m.mu[mi];
         const int staged = P < a.cap ? P : a.cap;
+        const bool spill = work != nullptr && (int64_t)(P - staged) * (q + 1) <= a.work_cta;
         double* us = sm;                       // [staged][q]
         double* ws = sm + (int64_t)staged * q;  // [staged]
         double msum = 0.0, ovsum = 0.0;
         for (int p = threadIdx.x; p < P; p += blockDim.x) {
-            double u[32], wgt, ov;
+            double u[QA], wgt, ov;
             pattern_coeffs(a, tr, g, k, b, p, V, Vi, u, wgt, ov);
             double m = a.f.mult[tr.pat_base + p];
             if (a.f.mask_off) {
@@ -308,33 +351,52 @@ __global__ void optimal_t_profiles_kernel(ProfParams a) {
             msum += m;
             ovsum += ov;
             if (p < staged) {
-                for (int kk = 0; kk < q; ++kk) us[p * q + kk] = u[kk];
+#pragma unroll
+                for (int kk = 0; kk < QA; ++kk)
+                    if (kk < q) us[p * q + kk] = u[kk];
                 ws[p] = wgt;
+            } else if (spill) {
+                double* o = work + (int64_t)(p - staged) * (q + 1);
+#pragma unroll
+                for (int kk = 0; kk < QA; ++kk)
+                    if (kk < q) o[kk] = u[kk];
+                o[q] = wgt;
             }
         }
         msum = block_sum(msum, red);
         ovsum = block_sum(ovsum, red);
-        __syncthreads();
+        __syncthreads();  // (block_sum ends with a barrier; the workspace writes are this thread's own)
         // 1 - overlap can round to a tiny negative number when the profiles agree
         // completely (sqrt would give NaN); the distance is never negative
         double hamming = 1.0 - ovsum / msum;
         hamming = hamming > 0.0 ? hamming : 0.0;
         auto f = [&](double s) -> double {
             const double t = s * s;
-            double e[32];
-            for (int kk = 0; kk < q; ++kk) e[kk] = exp(mu * lam[kk] * t);
+            double e[QA];
+#pragma unroll
+            for (int kk = 0; kk < QA; ++kk) e[kk] = kk < q ? exp(mu * lam[kk] * t) : 0.0;
             double acc = 0.0;
             for (int p = threadIdx.x; p < P; p += blockDim.x) {
                 double res = 0.0, wgt;
                 if (p < staged) {
-                    for (int kk = 0; kk < q; ++kk) res = fma(us[p * q + kk], e[kk], res);
+#pragma unroll
+                    for (int kk = 0; kk < QA; ++kk)
+                        if (kk < q) res = fma(us[p * q + kk], e[kk], res);
                     wgt = ws[p];
+                } else if (spill) {
+                    const double* o = work + (int64_t)(p - staged) * (q + 1);
+#pragma unroll
+                    for (int kk = 0; kk < QA; ++kk)
+                        if (kk < q) res = fma(o[kk], e[kk], res);
+                    wgt = o[q];
                 } else {
-                    double u[32], ov;
+                    double u[QA], ov;
                     pattern_coeffs(a, tr, g, k, b, p, V, Vi, u, wgt, ov);
-                    for (int kk = 0; kk < q; ++kk) res = fma(u[kk], e[kk], res);
+#pragma unroll
+                    for (int kk = 0; kk < QA; ++kk)
+                        if (kk < q) res = fma(u[kk], e[kk], res);
                 }
-                acc += wgt * log(res + kSuperTiny);
+                acc += wgt * log_tang(res + kSuperTiny, log_tab, inv_tab);
             }
             const double tot = block_sum(acc, red);
             return -tot + exp(t * t / 10000.0);
@@ -398,23 +460,30 @@ extern "C" tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts,
     return check_launch("tt_prob_t_pairs");
 }
 
+template <int QT>
+static void launch_t_profiles(const ProfParams& a, int blocks, size_t smem, cudaStream_t s) {
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        cudaFuncSetAttribute(optimal_t_profiles_kernel<QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
+    optimal_t_profiles_kernel<QT><<<blocks, 256, smem, s>>>(a);
+}
+
 extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
                                            const void* pp, const int64_t* pp_row, const void* pc,
                                            const int64_t* pc_row, int32_t prec, int32_t gap_state,
                                            int32_t ignore_gaps, double tol, double* t_out, int32_t* info,
-                                           void* stream) {
+                                           double* workspace, int64_t workspace_bytes, void* stream) {
     if (!f || !m || n < 0 || (n > 0 && (!node_of || !pp || !pp_row || !pc_row || !t_out)) || f->n_states > 32) {
         set_error("tt_optimal_t_profiles: invalid arguments");
         return TT_ERR_INVALID;
     }
     if (n == 0) return TT_OK;
-    static bool configured = false;
     const int q = f->n_states;
     const size_t smem_max = 200 * 1024;
-    if (!configured) {
-        cudaFuncSetAttribute(optimal_t_profiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-        configured = true;
-    }
     ProfParams a;
     a.f = *f;
     a.m = *m;
@@ -431,7 +500,20 @@ extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m
     a.t_out = t_out;
     a.info = info;
     a.cap = (int)(smem_max / ((q + 1) * sizeof(double)));
-    int64_t blocks = n < 65535 * 4 ? n : 65535 * 4;
-    optimal_t_profiles_kernel<<<(unsigned)blocks, 256, smem_max, as_stream(stream)>>>(a);
+    // one persistent CTA per SM (200 KB of shared memory each)
+    const int64_t sms = sm_count();
+    const int blocks = (int)(n < sms ? n : sms);
+    a.work = workspace;
+    a.work_cta = workspace && workspace_bytes > 0 ? workspace_bytes / (int64_t)sizeof(double) / blocks : 0;
+    if (a.work_cta <= 0) a.work = nullptr;
+    cudaStream_t s = as_stream(stream);
+    switch (q) {
+        case 4: launch_t_profiles<4>(a, blocks, smem_max, s); break;
+        case 5: launch_t_profiles<5>(a, blocks, smem_max, s); break;
+        case 20: launch_t_profiles<20>(a, blocks, smem_max, s); break;
+        case 21: launch_t_profiles<21>(a, blocks, smem_max, s); break;
+        case 22: launch_t_profiles<22>(a, blocks, smem_max, s); break;
+        default: launch_t_profiles<0>(a, blocks, smem_max, s); break;
+    }
     return check_launch("tt_optimal_t_profiles");
 }

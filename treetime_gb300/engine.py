@@ -767,12 +767,37 @@ def optimal_t_profiles_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, pr
     n = int(d_node.numel())
     tout = t.empty(n, dtype=t.float64, device=dev)
     info = t.empty(n, dtype=t.int32, device=dev)
+    ws, ws_bytes = _profile_workspace(forest, n, dev)
     check(lib.tt_optimal_t_profiles(C.byref(forest.struct), C.byref(model.struct), n, _p(d_node), _p(pp),
                                     _p(d_pp_row), _p(pc), _p(d_pc_row),
                                     _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64,
                                     -1 if gap_state is None else int(gap_state), int(bool(ignore_gaps)), float(tol),
-                                    _p(tout), _p(info), _stream()), "tt_optimal_t_profiles")
+                                    _p(tout), _p(info), _p(ws), ws_bytes, _stream()), "tt_optimal_t_profiles")
     return tout, info
+
+
+_PROFILE_WS = {}
+
+
+def _profile_workspace(forest, n, dev):
+    """Device FP64 workspace for the per-pattern coefficients that do not fit
+    in the profile-Brent kernel's shared memory (one slice per persistent
+    CTA); one buffer per device and stream, grown when a call needs more."""
+    t = torch()
+    q = forest.q
+    cap = (200 * 1024) // ((q + 1) * 8)
+    p_max = int(np.max(forest.trees_host["n_patterns"])) if len(forest.trees_host) else 0
+    over = max(0, p_max - cap)
+    if over == 0 or n == 0:
+        return None, 0
+    blocks = min(n, _lib.load().tt_device_sm_count())
+    need = blocks * over * (q + 1) * 8
+    key = (str(dev), t.cuda.current_stream(dev).cuda_stream)
+    buf = _PROFILE_WS.get(key)
+    if buf is None or buf.numel() < need // 8:
+        buf = t.empty(need // 8, dtype=t.float64, device=dev)
+        _PROFILE_WS[key] = buf
+    return buf, int(buf.numel() * 8)
 
 
 # ----------------------------------------------------------------------------
@@ -960,17 +985,22 @@ def optimal_t_compressed(gtr, seq_pair, multiplicity, profiles=False, tol=1e-10)
         pad = lambda a: np.pad(a, ((0, 0), (0, w - q)))
         d_pp = _to_dev(pad(pp), dev)
         d_pc = _to_dev(pad(pc), dev)
-        tout, info = optimal_t_profiles(_ForestView(f, dev), model, [1], d_pp, [0], d_pc, [0], "f64", gtr.gap_index,
-                                        True, tol)
+        tout, info = optimal_t_profiles(_ForestView(f, dev, q, P), model, [1], d_pp, [0], d_pc, [0], "f64",
+                                        gtr.gap_index, True, tol)
     if int(info[0].item()) == -1:
         check(_lib.TT_ERR_BRACKET, "optimal_t_compressed")
     return float(tout[0].item())
 
 
 class _ForestView:
-    def __init__(self, struct, device):
+    """The parts of a Forest the per-branch calls read: the C struct, the
+    device, the alphabet size and the pattern count of its one tree."""
+
+    def __init__(self, struct, device, q, n_patterns):
         self.struct = struct
         self.device = device
+        self.q = q
+        self.trees_host = np.array([(n_patterns,)], dtype=[("n_patterns", np.int32)])
 
 
 # ----------------------------------------------------------------------------

@@ -17,6 +17,9 @@
  *                                                                treetime/gtr.py:717-749, :816-920
  *   tt_optimal_t_profiles GTR.optimal_t_compressed(profiles=True) with GTR.prob_t_profiles
  *                                                                treetime/gtr.py:816-963
+ *   tt_prob_t_profiles_grid, tt_prob_t_pairs_grid
+ *                        the log-likelihood grids of BranchLenInterpolator ('marginal', 'joint')
+ *                                                                treetime/branch_len_interpolator.py:96-125
  *   tt_compress_columns  SequenceData.make_compressed_alignment  treetime/sequence_data.py:325-464
  *
  * Conventions
@@ -316,6 +319,26 @@ tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n
                                 int32_t prec, int32_t gap_state, int32_t ignore_gaps, double tol,
                                 double* t_out, int32_t* info, double* workspace, int64_t workspace_bytes,
                                 void* stream);
+
+/* ------------------------------------- branch-length likelihood grids
+ * log P(data | t) of each of n branches at n_grid branch lengths per branch, grid[b][g] (row-major,
+ * device FP64) into logp_out[b][g]; a negative entry gives -1e10 (TreeTime's value for t < 0), so
+ * rows of branches with shorter grids are padded with -1.
+ * tt_prob_t_profiles_grid: the profile objective of tt_optimal_t_profiles (same arguments and
+ * workspace rule) without the Brent search, sum mult*mask*log(pc.P(t).pp + 1e-24)*non_gap: the
+ * values BranchLenInterpolator takes in 'marginal' mode (treetime/branch_len_interpolator.py:
+ * 96-105, GTR.prob_t_profiles treetime/gtr.py:922-963).
+ * tt_prob_t_pairs_grid: sum count*log(max(P(t)[child][parent], 1e-24)) over [n][q][q] counts
+ * (model row model_of[b], or 0 when model_of is NULL): 'joint' mode (treetime/
+ * branch_len_interpolator.py:107-118, GTR.prob_t_compressed treetime/gtr.py:717-748). */
+tt_status tt_prob_t_profiles_grid(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
+                                  const void* pp, const int64_t* pp_row, const void* pc, const int64_t* pc_row,
+                                  int32_t prec, int32_t gap_state, int32_t ignore_gaps, const double* grid,
+                                  int32_t n_grid, double* logp_out, double* workspace, int64_t workspace_bytes,
+                                  void* stream);
+tt_status tt_prob_t_pairs_grid(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
+                               const tt_model* m, const double* grid, int32_t n_grid, double* logp_out,
+                               void* stream);
 
 /* -------------------------------------------------- a1: compression
  * Column classes of a tips x sites byte matrix (row-major, n_rows x n_cols): key[c] = the letter

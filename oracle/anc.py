@@ -110,6 +110,15 @@ def expQt(model, t):
     return np.maximum(0, Qs)
 
 
+def expQt_expm1(model, t):
+    """exp(Qt) as I + V diag(expm1(mu lam t)) V^-1, clipped at 0: the same
+    matrix as expQt (standard models), but with the small off-diagonal entries
+    of short times accurate to rounding relative to their own size instead of
+    set by the rounding of V diag(exp) V^-1 (exactly 0 at t = 0)."""
+    em1 = np.expm1(model.mu * t * model.eigenvals)
+    return np.maximum(0, np.eye(len(em1)) + model.v.dot(np.diag(em1).dot(model.v_inv)))
+
+
 def _site_expQt_exact(model, t):
     """gtr_site_specific.py:350-365 (no clamp)."""
     e = np.exp(t * model.mu * model.eigenvals)
@@ -411,6 +420,48 @@ def optimal_t_compressed(model, seq_pair, multiplicity, profiles=False, tol=1e-1
     if opt["success"] is not True:
         new_len = hamming
     return new_len, opt
+
+
+def branch_len_grid(mutation_length, one_mutation, n_grid_points=125):
+    """BranchLenInterpolator's grid, branch_len_interpolator.py:36-62."""
+    if mutation_length < np.min((1e-5, 0.1 * one_mutation)):
+        short_range = 10 * one_mutation
+        return np.concatenate([short_range * (np.linspace(0, 1.0, n_grid_points // 2)[:-1]),
+                               short_range + (MAX_BRANCH_LENGTH - short_range)
+                               * (np.linspace(0, 1.0, n_grid_points // 2 + 1) ** 2)])
+    sigma = mutation_length
+    grid_left = mutation_length * (1 - np.linspace(1, 0.0, n_grid_points // 3) ** 2.0)
+    grid_zero = grid_left[1] * np.logspace(-20, 0, 6)[:5]
+    grid_zero2 = grid_left[1] * np.linspace(0, 1, 10)[1:-1]
+    grid_right = mutation_length + (3 * sigma * (np.linspace(0, 1, n_grid_points // 3) ** 2))
+    far_grid = grid_right.max() + MAX_BRANCH_LENGTH * np.linspace(0, 1, n_grid_points // 3) ** 2
+    grid = np.concatenate((grid_zero, grid_zero2, grid_left, grid_right[1:], far_grid[1:]))
+    grid.sort()
+    return grid
+
+
+def branch_len_log_prob(model, grid, mode, profile_pair=None, multiplicity=None, seq_pair=None,
+                        pair_multiplicity=None, expm1_form=False):
+    """-log P on the grid, branch_len_interpolator.py:103-118 ('marginal':
+    prob_t_profiles of the branch's profile pair; 'joint': prob_t_compressed
+    of its state pairs).  ``expm1_form``: 'joint' values from expQt_expm1."""
+    if mode == "marginal":
+        return np.array([-prob_t_profiles(model, profile_pair, multiplicity, k, return_log=True) for k in grid])
+    if expm1_form:
+        out = []
+        for k in grid:
+            logQt = np.log(np.maximum(expQt_expm1(model, k), SUPERTINY_NUMBER))
+            out.append(BIG_NUMBER if k < 0 else -np.sum(logQt[seq_pair[:, 1], seq_pair[:, 0]] * pair_multiplicity))
+        return np.array(out)
+    return np.array([-prob_t_compressed(model, seq_pair, pair_multiplicity, k, return_log=True) for k in grid])
+
+
+def pair_resolution(model, grid, seq_pair):
+    """Per grid point, the smallest exp(Qt) entry (expQt_expm1) over the
+    observed state pairs: where it is below ~1e-6 the reference's own value
+    is dominated by the rounding of V diag(exp) V^-1."""
+    return np.array([np.min(expQt_expm1(model, k)[seq_pair[:, 1], seq_pair[:, 0]]) if len(seq_pair) else 1.0
+                     for k in grid])
 
 
 def optimize_branch_lengths_joint(tree, cseq_of, mult, model, ignore_gaps=True):

@@ -142,6 +142,78 @@ def run_case(name, newick, aln, kind, params, compress=True, masks=None, reconst
     return out
 
 
+def run_blgrid(name, newick, aln, kind, params, n_grid_points=125):
+    """BranchLenInterpolator grids and values of every branch, in 'marginal'
+    mode (after a marginal reconstruction) and in 'joint' mode (after a joint
+    one), as ClockTree.init_date_constraints builds them."""
+    from treetime import TreeAnc
+    from treetime.branch_len_interpolator import BranchLenInterpolator
+    out = {"case": name, "newick": newick, "kind": kind, "n_grid_points": n_grid_points,
+           "aln_names": np.array(list(aln.keys())), "aln_seqs": np.array(list(aln.values()))}
+    for k, v in params.items():
+        out["param_" + k] = np.asarray(v)
+    for mode in ("marginal", "joint"):
+        tree, recs = _bio_inputs(newick, aln)
+        t = TreeAnc(tree=tree, aln=recs, gtr=_ref_gtr(kind, params), compress=True, verbose=0)
+        t.infer_ancestral_sequences(marginal=mode == "marginal")
+        nodes = [n for n in t.tree.find_clades() if n.up is not None]
+        xs, ys, peaks, ml = [], [], [], []
+        for n in nodes:
+            if mode == "marginal":
+                n.profile_pair = t.marginal_branch_profile(n)
+            else:
+                t.add_branch_state(n)
+            bi = BranchLenInterpolator(n, t.gtr, pattern_multiplicity=t.data.multiplicity(mask=n.mask),
+                                       one_mutation=t.one_mutation, branch_length_mode=mode,
+                                       n_grid_points=n_grid_points)
+            xs.append(np.asarray(bi._func.x))
+            ys.append(np.asarray(bi._func.y))
+            peaks.append(bi._peak_val)
+            ml.append(n.mutation_length)
+        G = max(len(x) for x in xs)
+        out[mode + "_names"] = np.array([n.name for n in nodes])
+        out[mode + "_mutation_length"] = np.array(ml)
+        out[mode + "_len"] = np.array([len(x) for x in xs])
+        out[mode + "_x"] = np.stack([np.pad(x, (0, G - len(x)), constant_values=-1.0) for x in xs])
+        out[mode + "_y"] = np.stack([np.pad(y, (0, G - len(y))) for y in ys])
+        out[mode + "_peak"] = np.array(peaks)
+        out["one_mutation"] = t.one_mutation
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
+
+
+def blgrid_cases():
+    """Nucleotide tree with a few zero-length branches (both grid shapes) and
+    a 5-state alphabet with gaps."""
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    rng = np.random.default_rng(21)
+    tree = synth.coalescent_tree(20, 0.03, rng)
+    pi = rng.dirichlet(np.ones(4))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(4, 4)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap")
+    states = synth.evolve(tree, g, 150, rng)
+    aln = synth._to_text(states, g.alphabet, 0.02, rng)
+    for i, c in enumerate(c for c in tree.find_clades() if c is not tree.root):
+        if i % 7 == 3:
+            c.branch_length = 0.0
+    run_blgrid("blgrid_nuc", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "nuc_nogap", "mu": 1.0})
+    rng = np.random.default_rng(22)
+    tree = synth.coalescent_tree(14, 0.06, rng)
+    pi = rng.dirichlet(np.ones(5))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(5, 5)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc")
+    states = synth.evolve(tree, g, 120, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    for k in list(aln)[:4]:
+        aln[k] = "-" * 6 + aln[k][6:]
+    run_blgrid("blgrid_nuc5", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "nuc", "mu": 1.0},
+               n_grid_points=75)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -280,4 +352,10 @@ def main(ref_path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else "/root/reference"
+    if "--blgrid" in sys.argv:
+        _setup(ref)
+        blgrid_cases()
+    else:
+        main(ref)

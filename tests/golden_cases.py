@@ -13,7 +13,14 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def case_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """Reconstruction cases (every fixture but the branch-length grids)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith("blgrid_"))
+
+
+def blgrid_names():
+    """BranchLenInterpolator fixtures."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "blgrid_*.npz")))
 
 
 def load(name):
@@ -57,6 +64,50 @@ def compressed_from(g, model):
     aln = {k: chars[i] for i, k in enumerate(names)}
     extend_profile(model, list(aln.values()))
     return aln
+
+
+def compress_inputs(aln, model):
+    """(name -> compressed char array, multiplicities, full length) of a raw
+    alignment, by the host compression (pinned bit-exact to TreeTime's)."""
+    from treetime_gb300.seqdata import SequenceData
+    sd = SequenceData(aln, compress=True, ambiguous=model.ambiguous)
+    chars = np.asarray(sd.compressed_codes).view("S1").astype("U1")
+    caln = {k: chars[i] for i, k in enumerate(sd.sequence_names)}
+    extend_profile(model, list(caln.values()))
+    return caln, sd.multiplicity(), len(sd.full_to_compressed_sequence_map)
+
+
+def blgrid_oracle(g, mode, expm1_form=False):
+    """name -> (-log P on the fixture's grid, per-point resolution) by the
+    oracle, from the oracle's own reconstruction of the fixture's inputs.
+    Resolution: the smallest P(t) entry of the observed state pairs ('joint'),
+    1 for 'marginal'."""
+    from oracle import anc
+    tree, aln, model, _ = inputs_from(g)
+    anc.prepare_tree(tree)
+    caln, mult, full = compress_inputs(aln, model)
+    nodes = {n.name: n for n in anc.preorder(tree.root)}
+    out = {}
+    if mode == "marginal":
+        res = anc.marginal(tree, caln, mult, model, full)
+    else:
+        res = anc.joint(tree, caln, mult, model, full)
+        cseq = dict(res["cseq"])
+        cseq.update(caln)
+    for i, name in enumerate(g[mode + "_names"].tolist()):
+        x = g[mode + "_x"][i, :int(g[mode + "_len"][i])]
+        if mode == "marginal":
+            v = anc.branch_len_log_prob(model, x, "marginal", profile_pair=(
+                res["outgroup_LH"][name], res["subtree_LH"][name]), multiplicity=mult)
+            out[name] = (v, np.ones(len(x)))
+        else:
+            node = nodes[name]
+            pairs, pm = anc.state_pair(model, cseq[node.up.name], cseq[name], pattern_multiplicity=mult,
+                                       ignore_gaps=True)
+            v = anc.branch_len_log_prob(model, x, "joint", seq_pair=pairs, pair_multiplicity=pm,
+                                        expm1_form=expm1_form)
+            out[name] = (v, anc.pair_resolution(model, x, pairs))
+    return out
 
 
 def codes_of(arr):

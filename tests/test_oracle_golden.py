@@ -148,3 +148,42 @@ def test_oracle_marginal_branch_lengths_match_treetime(case):
                                         profiles=True)
         v = want[n.name]
         assert abs(t - v) <= 1e-6 * abs(v) + 1e-10, (n.name, t, v)
+
+
+# ------------------------------------------------ branch-length interpolator grids
+BLGRID = gc.blgrid_names()
+
+
+@pytest.mark.parametrize("case", BLGRID)
+def test_branch_len_grids_match_treetime(case):
+    """The oracle's and the product's grid builders give TreeTime's grids
+    bit for bit (both shapes: zero-length and finite branches)."""
+    from treetime_gb300 import engine
+    g = gc.load(case)
+    n, om = int(g["n_grid_points"]), float(g["one_mutation"])
+    for mode in ("marginal", "joint"):
+        for i, ml in enumerate(g[mode + "_mutation_length"]):
+            want = g[mode + "_x"][i, :int(g[mode + "_len"][i])]
+            np.testing.assert_array_equal(anc.branch_len_grid(float(ml), om, n), want)
+            np.testing.assert_array_equal(engine.branch_len_grid(float(ml), om, n), want)
+
+
+@pytest.mark.parametrize("mode", ["marginal", "joint"])
+@pytest.mark.parametrize("case", BLGRID)
+def test_oracle_branch_len_values_match_treetime(case, mode):
+    g = gc.load(case)
+    got = gc.blgrid_oracle(g, mode)
+    got_e = gc.blgrid_oracle(g, mode, expm1_form=True)
+    n_noise = 0
+    for i, name in enumerate(g[mode + "_names"].tolist()):
+        L = int(g[mode + "_len"][i])
+        want = g[mode + "_y"][i, :L] + g[mode + "_peak"][i]
+        np.testing.assert_allclose(got[name][0], want, rtol=1e-11, atol=1e-9, err_msg=name)
+        # the expm1 form agrees wherever the observed pairs' P(t) is resolved
+        ok = got_e[name][1] >= 1e-6
+        n_noise += int((~ok).sum())
+        np.testing.assert_allclose(got_e[name][0][ok], want[ok], rtol=1e-9, atol=1e-8, err_msg=name)
+    if mode == "marginal":
+        assert n_noise == 0
+    elif case == "blgrid_nuc":
+        assert n_noise > 0  # the fixture does reach the rounding-dominated points

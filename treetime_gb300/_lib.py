@@ -84,6 +84,9 @@ _SIGS = {
     "tt_prob_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), vp, vp, vp]),
     "tt_optimal_t_profiles": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, i32, f64, vp, vp,
                                     vp, i64, vp]),
+    "tt_prob_t_profiles_grid": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, i32, vp, i32, vp,
+                                      vp, i64, vp]),
+    "tt_prob_t_pairs_grid": (i32, [i32, i64, vp, vp, P(TTModel), vp, i32, vp, vp]),
     "tt_compress_columns": (i32, [vp, i64, i64, i32, vp, vp, vp]),
 }
 

@@ -376,19 +376,19 @@ class GPUAncMixin:
         node.branch_state = {"pair": pairs, "multiplicity": mult}
         return engine.optimal_t_compressed(self.gtr, pairs, mult)
 
-    def _marginal_branch_lengths(self, nodes, tol):
-        """Profile-mode Brent for the given nodes in one device pass, from the
-        outgroup and subtree profiles of the last marginal reconstruction."""
+    def _profile_branch_groups(self, nodes):
+        """The profile-pair arguments of the given branches, from the outgroup
+        and subtree profiles of the last marginal reconstruction: one group for
+        internal nodes (child rows in the partials) and one for tips (child
+        profiles from their codes), as (positions in `nodes`, node ids,
+        outgroup buffer, parent rows, child rows, partials buffer)."""
         last = getattr(self, "_last", None)
         if last is None or last[0] != "marginal" or last[1].get("outgroup") is None:
             raise Exception("marginal ancestral inference needs to be performed first!")
         out = last[1]
-        sess = self._get_session()
-        layout = sess["layout"]
+        layout = self._get_session()["layout"]
         P = self.data.compressed_length
         ks = [layout.local[id(n)] for n in nodes]
-        res = np.zeros(len(nodes))
-        info = np.zeros(len(nodes), dtype=np.int32)
         groups = (([i for i, k in enumerate(ks) if k < layout.n_int], out["outgroup"], False),
                   ([i for i, k in enumerate(ks) if k >= layout.n_int], out["tip_outgroup"], True))
         for idx, pp, tips in groups:
@@ -397,14 +397,70 @@ class GPUAncMixin:
             kk = [ks[i] for i in idx]
             pp_row = [((k - layout.n_int) if tips else k) * P for k in kk]
             pc_row = [-1 if tips else k * P for k in kk]
-            t, inf = engine.optimal_t_profiles(sess["forest"], engine.model_for(self.gtr, getattr(self, "device", None)),
-                                               kk, pp, pp_row, out["partial"], pc_row, self._gpu_precision(),
-                                               self.gtr.gap_index, True, tol)
+            yield idx, kk, pp, pp_row, pc_row, out["partial"]
+
+    def _marginal_branch_lengths(self, nodes, tol):
+        """Profile-mode Brent for the given nodes in one device pass, from the
+        outgroup and subtree profiles of the last marginal reconstruction."""
+        sess = self._get_session()
+        model = engine.model_for(self.gtr, getattr(self, "device", None))
+        res = np.zeros(len(nodes))
+        info = np.zeros(len(nodes), dtype=np.int32)
+        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
+            t, inf = engine.optimal_t_profiles(sess["forest"], model, kk, pp, pp_row, pc, pc_row,
+                                               self._gpu_precision(), self.gtr.gap_index, True, tol)
             res[idx] = t.cpu().numpy()
             info[idx] = inf.cpu().numpy()
         if (info == -1).any():
             engine.check(engine._lib.TT_ERR_BRACKET, "optimal_marginal_branch_length")
         return res
+
+    def branch_length_grids(self, nodes=None, branch_length_mode="marginal", n_grid_points=None,
+                            one_mutation=None):
+        """For each branch, the grid of branch lengths and -log P(data | t) on
+        it: the two arrays TreeTime's BranchLenInterpolator tabulates per node
+        in ClockTree.init_date_constraints (treetime/branch_len_interpolator.py:
+        36-125, treetime/clock_tree.py:343-368), for all branches in one device
+        launch.  'marginal' evaluates the profile pairs of the last marginal
+        reconstruction (GTR.prob_t_profiles with the node's mask), 'joint' the
+        state-pair counts of the last reconstruction (GTR.prob_t_compressed).
+        Returns {node: (grid, neg_log_p)}; grid points follow the node's
+        mutation_length and `one_mutation` (default self.one_mutation)."""
+        if branch_length_mode not in ("marginal", "joint"):
+            raise Exception("unknown branch length mode! " + str(branch_length_mode))
+        n_grid_points = ttconf.BRANCH_GRID_SIZE if n_grid_points is None else n_grid_points
+        one_mutation = self.one_mutation if one_mutation is None else one_mutation
+        if nodes is None:
+            nodes = [n for n in self.tree.find_clades() if n.up is not None]
+        for n in nodes:
+            if n.up is None:
+                raise Exception("Cannot create branch length interpolator for the root node.")
+        if not nodes:
+            return {}
+        grids = [engine.branch_len_grid(n.mutation_length, one_mutation, n_grid_points) for n in nodes]
+        padded = engine.pad_grids(grids)
+        sess = self._get_session()
+        dev = sess["forest"].device
+        logp = np.empty(padded.shape)
+        if branch_length_mode == "marginal":
+            model = engine.model_for(self.gtr, getattr(self, "device", None))
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
+                d = engine._to_dev
+                v = engine.prob_t_profiles_grid_dev(sess["forest"], model, d(np.asarray(kk, np.int32), dev), pp,
+                                                    d(np.asarray(pp_row, np.int64), dev), pc,
+                                                    d(np.asarray(pc_row, np.int64), dev), self._gpu_precision(),
+                                                    self.gtr.gap_index, True, d(padded[idx], dev))
+                logp[idx] = v.cpu().numpy()
+        else:
+            if not self.sequence_reconstruction:
+                raise Exception("branch state pairs need to be assigned to nodes")
+            sess, hist = self._pair_histograms()
+            layout = sess["layout"]
+            ks = engine._to_dev(np.asarray([layout.local[id(n)] for n in nodes], np.int64), dev)
+            counts = engine.torch().trunc(hist)[ks].contiguous()  # TreeTime casts pair counts to int
+            logp = engine.prob_t_pairs_grid(self.gtr.n_states, counts, sess["model"],
+                                            engine._to_dev(padded, dev)).cpu().numpy()
+        return {n: (grids[i], -logp[i, :len(grids[i])]) for i, n in enumerate(nodes)}
 
     def optimal_marginal_branch_length(self, node, tol=1e-10):
         if node.up is None:

@@ -8,6 +8,7 @@ SUPERTINY_NUMBER = 1e-24
 MIN_LOG = -1e8
 MIN_BRANCH_LENGTH = 1e-3  # fraction of one mutation used as lower cut-off for branch lengths
 MAX_BRANCH_LENGTH = 4.0
+BRANCH_GRID_SIZE = 125  # grid points of a branch-length interpolator
 VERBOSE = 3
 SUCCESS = "success"
 ERROR = "error"

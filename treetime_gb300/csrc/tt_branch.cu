@@ -200,6 +200,56 @@ __global__ void prob_t_pairs_kernel(int q, int64_t n, const double* __restrict__
     }
 }
 
+// log P(pairs | t) of each branch on a grid of branch lengths (TreeTime's BranchLenInterpolator in
+// 'joint' mode, treetime/branch_len_interpolator.py:107-118, each one GTR.prob_t_compressed
+// (return_log=True), treetime/gtr.py:717-748): sum over the (parent, child) pairs of
+// count * log(max(P(t)[child, parent], 1e-24)), P(t) clipped at zero as expQt does.  The grid
+// reaches down to t = 0, where the off-diagonal entries of V diag(exp(mu lam t)) V^-1 are rounding
+// noise of order 1e-16 (its log then depends on the summation order); P(t) is therefore formed as
+// I + V diag(expm1(mu lam t)) V^-1, whose off-diagonal entries are accurate to rounding relative
+// to their own size (exactly 0 at t = 0).  One CTA per branch stages the q*q counts; each warp
+// takes grid points, writes expm1(mu lam_k t) to its row of shared memory and its lanes split the
+// nonzero pairs.
+__global__ void __launch_bounds__(256) prob_t_pairs_grid_kernel(int q, int64_t n, const double* __restrict__ counts,
+                                                                const int32_t* __restrict__ model_of, tt_model m,
+                                                                const double* __restrict__ grid, int n_grid,
+                                                                double* __restrict__ out) {
+    __shared__ double cnt[32 * 32];
+    __shared__ double ex[8][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int64_t b = blockIdx.x; b < n; b += gridDim.x) {
+        for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) cnt[idx] = counts[b * q * q + idx];
+        __syncthreads();
+        const int mi = model_of ? model_of[b] : 0;
+        const double* V = m.V + (int64_t)mi * q * q;
+        const double* Vi = m.Vinv + (int64_t)mi * q * q;
+        const double* lam = m.lam + (int64_t)mi * q;
+        const double mu = m.mu[mi];
+        for (int gi = warp; gi < n_grid; gi += nw) {
+            const double t = grid[b * n_grid + gi];
+            double acc = 0.0;
+            if (t >= 0.0) {
+                if (lane < q) ex[warp][lane] = expm1(mu * lam[lane] * t);
+                __syncwarp();
+                for (int idx = lane; idx < q * q; idx += 32) {
+                    const double c = cnt[idx];
+                    if (c == 0.0) continue;
+                    const int ip = idx / q, jc = idx % q;  // parent state, child state
+                    double pv = 0.0;
+                    for (int k = 0; k < q; ++k) pv = fma(V[jc * q + k], ex[warp][k] * Vi[k * q + ip], pv);
+                    if (ip == jc) pv += 1.0;
+                    pv = pv > 0.0 ? pv : 0.0;
+                    acc += log(pv > kSuperTiny ? pv : kSuperTiny) * c;
+                }
+                acc = warp_sum(acc);
+            }
+            if (lane == 0) out[b * n_grid + gi] = t >= 0.0 ? acc : -kBig;
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------ profile pairs
 template <typename T>
 __device__ __forceinline__ void read_prof(const void* base, int64_t row, int w, int q, double* x) {
@@ -225,6 +275,9 @@ struct ProfParams {
     int cap;            // patterns whose coefficients sit in shared memory
     double* work;       // per-CTA coefficients of the patterns past `cap` (nullptr: recompute)
     int64_t work_cta;   // doubles per CTA in `work`
+    const double* grid;  // grid mode: [n][n_grid] branch lengths (negative: unused slot)
+    int n_grid;
+    double* grid_out;    // grid mode: [n][n_grid] log P(data | t)
 };
 
 __device__ double block_sum(double v, double* red) {
@@ -460,6 +513,121 @@ extern "C" tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts,
     return check_launch("tt_prob_t_pairs");
 }
 
+extern "C" tt_status tt_prob_t_pairs_grid(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
+                                          const tt_model* m, const double* grid, int32_t n_grid, double* logp_out,
+                                          void* stream) {
+    if (!m || q < 2 || q > 32 || m->n_states != q || n < 0 || n_grid < 0 ||
+        (n > 0 && n_grid > 0 && (!counts || !grid || !logp_out))) {
+        set_error("tt_prob_t_pairs_grid: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n == 0 || n_grid == 0) return TT_OK;
+    const int64_t cap = 8 * (int64_t)sm_count();
+    const int64_t blocks = n < cap ? n : cap;
+    prob_t_pairs_grid_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(q, n, counts, model_of, *m, grid,
+                                                                              n_grid, logp_out);
+    return check_launch("tt_prob_t_pairs_grid");
+}
+
+// log P(data | t) of each branch on a grid of branch lengths (the evaluations behind TreeTime's
+// BranchLenInterpolator in 'marginal' mode, treetime/branch_len_interpolator.py:96-105, each one
+// GTR.prob_t_profiles(return_log=True), treetime/gtr.py:922-963): per branch the per-pattern
+// eigen coefficients are staged once as in optimal_t_profiles_kernel, then each warp takes grid
+// points and its lanes sum sum_a w_a log(pc_a.P(t).pp_a + 1e-24) over the patterns.
+template <int QT>
+__global__ void __launch_bounds__(256) prob_t_profiles_grid_kernel(ProfParams a) {
+    constexpr int QA = QT > 0 ? QT : 32;
+    extern __shared__ double sm[];
+    __shared__ double log_tab[129], inv_tab[129];
+    for (int j = threadIdx.x; j < 129; j += blockDim.x) {
+        const double F = 1.0 + j / 128.0;
+        log_tab[j] = log(F);
+        inv_tab[j] = 1.0 / F;
+    }
+    __syncthreads();
+    const int q = QT > 0 ? QT : a.f.n_states;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double* const work = a.work ? a.work + (int64_t)blockIdx.x * a.work_cta : nullptr;
+    for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
+        const int64_t g = a.node_of[b];
+        const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
+        const int k = (int)(g - tr.node_base);
+        const int P = tr.n_patterns;
+        const int mi = tr.model;
+        const double* V = a.m.V + (int64_t)mi * q * q;
+        const double* Vi = a.m.Vinv + (int64_t)mi * q * q;
+        const double* lam = a.m.lam + (int64_t)mi * q;
+        const double mu = a.m.mu[mi];
+        const int staged = P < a.cap ? P : a.cap;
+        const bool spill = work != nullptr && (int64_t)(P - staged) * (q + 1) <= a.work_cta;
+        double* us = sm;
+        double* ws = sm + (int64_t)staged * q;
+        for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            double u[QA], wgt, ov;
+            pattern_coeffs(a, tr, g, k, b, p, V, Vi, u, wgt, ov);
+            if (p < staged) {
+#pragma unroll
+                for (int kk = 0; kk < QA; ++kk)
+                    if (kk < q) us[p * q + kk] = u[kk];
+                ws[p] = wgt;
+            } else if (spill) {
+                double* o = work + (int64_t)(p - staged) * (q + 1);
+#pragma unroll
+                for (int kk = 0; kk < QA; ++kk)
+                    if (kk < q) o[kk] = u[kk];
+                o[q] = wgt;
+            }
+        }
+        __syncthreads();
+        for (int gi = warp; gi < a.n_grid; gi += nw) {
+            const double t = a.grid[b * a.n_grid + gi];
+            double acc = 0.0;
+            if (t >= 0.0) {
+                double e[QA];
+#pragma unroll
+                for (int kk = 0; kk < QA; ++kk) e[kk] = kk < q ? exp(mu * lam[kk] * t) : 0.0;
+                for (int p = lane; p < P; p += 32) {
+                    double res = 0.0, wgt;
+                    if (p < staged) {
+#pragma unroll
+                        for (int kk = 0; kk < QA; ++kk)
+                            if (kk < q) res = fma(us[p * q + kk], e[kk], res);
+                        wgt = ws[p];
+                    } else if (spill) {
+                        const double* o = work + (int64_t)(p - staged) * (q + 1);
+#pragma unroll
+                        for (int kk = 0; kk < QA; ++kk)
+                            if (kk < q) res = fma(o[kk], e[kk], res);
+                        wgt = o[q];
+                    } else {
+                        double u[QA], ov;
+                        pattern_coeffs(a, tr, g, k, b, p, V, Vi, u, wgt, ov);
+#pragma unroll
+                        for (int kk = 0; kk < QA; ++kk)
+                            if (kk < q) res = fma(u[kk], e[kk], res);
+                    }
+                    acc += wgt * log_tang(res + kSuperTiny, log_tab, inv_tab);
+                }
+                acc = warp_sum(acc);
+            }
+            if (lane == 0) a.grid_out[b * a.n_grid + gi] = t >= 0.0 ? acc : -kBig;
+        }
+        __syncthreads();
+    }
+}
+
+template <int QT>
+static void launch_t_grid(const ProfParams& a, int blocks, size_t smem, cudaStream_t s) {
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        cudaFuncSetAttribute(prob_t_profiles_grid_kernel<QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
+    prob_t_profiles_grid_kernel<QT><<<blocks, 256, smem, s>>>(a);
+}
+
 template <int QT>
 static void launch_t_profiles(const ProfParams& a, int blocks, size_t smem, cudaStream_t s) {
     static bool configured[64] = {};
@@ -470,6 +638,29 @@ static void launch_t_profiles(const ProfParams& a, int blocks, size_t smem, cuda
         if (dev >= 0 && dev < 64) configured[dev] = true;
     }
     optimal_t_profiles_kernel<QT><<<blocks, 256, smem, s>>>(a);
+}
+
+static ProfParams prof_params(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
+                              const void* pp, const int64_t* pp_row, const void* pc, const int64_t* pc_row,
+                              int32_t prec, int32_t gap_state, int32_t ignore_gaps, double* workspace,
+                              int64_t workspace_bytes, size_t smem, int blocks) {
+    ProfParams a{};
+    a.f = *f;
+    a.m = *m;
+    a.n = n;
+    a.node_of = node_of;
+    a.pp = pp;
+    a.pp_row = pp_row;
+    a.pc = pc;
+    a.pc_row = pc_row;
+    a.prec = prec;
+    a.gap = gap_state;
+    a.ignore_gaps = ignore_gaps;
+    a.cap = (int)(smem / ((f->n_states + 1) * sizeof(double)));
+    a.work = workspace;
+    a.work_cta = workspace && workspace_bytes > 0 ? workspace_bytes / (int64_t)sizeof(double) / blocks : 0;
+    if (a.work_cta <= 0) a.work = nullptr;
+    return a;
 }
 
 extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
@@ -484,28 +675,14 @@ extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m
     if (n == 0) return TT_OK;
     const int q = f->n_states;
     const size_t smem_max = 200 * 1024;
-    ProfParams a;
-    a.f = *f;
-    a.m = *m;
-    a.n = n;
-    a.node_of = node_of;
-    a.pp = pp;
-    a.pp_row = pp_row;
-    a.pc = pc;
-    a.pc_row = pc_row;
-    a.prec = prec;
-    a.gap = gap_state;
-    a.ignore_gaps = ignore_gaps;
-    a.tol = tol;
-    a.t_out = t_out;
-    a.info = info;
-    a.cap = (int)(smem_max / ((q + 1) * sizeof(double)));
     // one persistent CTA per SM (200 KB of shared memory each)
     const int64_t sms = sm_count();
     const int blocks = (int)(n < sms ? n : sms);
-    a.work = workspace;
-    a.work_cta = workspace && workspace_bytes > 0 ? workspace_bytes / (int64_t)sizeof(double) / blocks : 0;
-    if (a.work_cta <= 0) a.work = nullptr;
+    ProfParams a = prof_params(f, m, n, node_of, pp, pp_row, pc, pc_row, prec, gap_state, ignore_gaps, workspace,
+                               workspace_bytes, smem_max, blocks);
+    a.tol = tol;
+    a.t_out = t_out;
+    a.info = info;
     cudaStream_t s = as_stream(stream);
     switch (q) {
         case 4: launch_t_profiles<4>(a, blocks, smem_max, s); break;
@@ -516,4 +693,37 @@ extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m
         default: launch_t_profiles<0>(a, blocks, smem_max, s); break;
     }
     return check_launch("tt_optimal_t_profiles");
+}
+
+extern "C" tt_status tt_prob_t_profiles_grid(const tt_forest* f, const tt_model* m, int64_t n,
+                                             const int32_t* node_of, const void* pp, const int64_t* pp_row,
+                                             const void* pc, const int64_t* pc_row, int32_t prec, int32_t gap_state,
+                                             int32_t ignore_gaps, const double* grid, int32_t n_grid,
+                                             double* logp_out, double* workspace, int64_t workspace_bytes,
+                                             void* stream) {
+    if (!f || !m || n < 0 || n_grid < 0 || f->n_states > 32 ||
+        (n > 0 && n_grid > 0 && (!node_of || !pp || !pp_row || !pc_row || !grid || !logp_out))) {
+        set_error("tt_prob_t_profiles_grid: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n == 0 || n_grid == 0) return TT_OK;
+    const int q = f->n_states;
+    const size_t smem_max = 200 * 1024;
+    const int64_t sms = sm_count();
+    const int blocks = (int)(n < sms ? n : sms);
+    ProfParams a = prof_params(f, m, n, node_of, pp, pp_row, pc, pc_row, prec, gap_state, ignore_gaps, workspace,
+                               workspace_bytes, smem_max, blocks);
+    a.grid = grid;
+    a.n_grid = n_grid;
+    a.grid_out = logp_out;
+    cudaStream_t s = as_stream(stream);
+    switch (q) {
+        case 4: launch_t_grid<4>(a, blocks, smem_max, s); break;
+        case 5: launch_t_grid<5>(a, blocks, smem_max, s); break;
+        case 20: launch_t_grid<20>(a, blocks, smem_max, s); break;
+        case 21: launch_t_grid<21>(a, blocks, smem_max, s); break;
+        case 22: launch_t_grid<22>(a, blocks, smem_max, s); break;
+        default: launch_t_grid<0>(a, blocks, smem_max, s); break;
+    }
+    return check_launch("tt_prob_t_profiles_grid");
 }

@@ -803,6 +803,83 @@ def _profile_workspace(forest, n, dev):
 # ----------------------------------------------------------------------------
 # single-call GTR API (device computations behind GTR methods)
 # ----------------------------------------------------------------------------
+def branch_len_grid(mutation_length, one_mutation, n_grid_points=ttconf.BRANCH_GRID_SIZE):
+    """The branch lengths at which BranchLenInterpolator tabulates a branch's
+    likelihood (treetime/branch_len_interpolator.py:36-62), built with the same
+    numpy expressions so that the grid is identical to TreeTime's: for an
+    effectively zero branch (mutation_length < min(1e-5, one_mutation / 10))
+    a linear ramp to 10 mutations then a quadratic one to MAX_BRANCH_LENGTH;
+    otherwise points clustered at zero, a quadratic approach to the branch
+    length, a quadratic tail to 4x it and a sparse tail to MAX_BRANCH_LENGTH."""
+    ml = float(mutation_length)
+    n = int(n_grid_points)
+    if ml < np.min((1e-5, 0.1 * one_mutation)):
+        short = 10 * one_mutation
+        ramp = short * (np.linspace(0, 1.0, n // 2)[:-1])
+        rest = short + (ttconf.MAX_BRANCH_LENGTH - short) * (np.linspace(0, 1.0, n // 2 + 1) ** 2)
+        return np.concatenate([ramp, rest])
+    sigma = ml
+    left = ml * (1 - np.linspace(1, 0.0, n // 3) ** 2.0)
+    near_zero = left[1] * np.logspace(-20, 0, 6)[:5]
+    near_zero2 = left[1] * np.linspace(0, 1, 10)[1:-1]
+    right = ml + (3 * sigma * (np.linspace(0, 1, n // 3) ** 2))
+    far = right.max() + ttconf.MAX_BRANCH_LENGTH * np.linspace(0, 1, n // 3) ** 2
+    grid = np.concatenate((near_zero, near_zero2, left, right[1:], far[1:]))
+    grid.sort()
+    return grid
+
+
+def pad_grids(grids):
+    """[n][G] FP64 array of ragged per-branch grids, short rows padded with -1
+    (the grid kernels return -1e10 there)."""
+    G = max((len(g) for g in grids), default=0)
+    out = np.full((len(grids), G), -1.0)
+    for i, g in enumerate(grids):
+        out[i, :len(g)] = g
+    return out
+
+
+def prob_t_profiles_grid_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, precision, gap_state, ignore_gaps,
+                             d_grid):
+    """log P(profiles | t) of each listed branch at each point of its row of
+    d_grid ([n][G] device FP64): the 'marginal' BranchLenInterpolator values
+    (treetime/branch_len_interpolator.py:96-105), enqueued in one launch."""
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    n = int(d_node.numel())
+    G = int(d_grid.shape[1]) if d_grid.dim() == 2 else 0
+    if d_grid.shape[0] != n:
+        raise ValueError("prob_t_profiles_grid: %d grid rows for %d branches" % (d_grid.shape[0], n))
+    out = t.empty((n, G), dtype=t.float64, device=dev)
+    ws, ws_bytes = _profile_workspace(forest, n, dev)
+    check(lib.tt_prob_t_profiles_grid(C.byref(forest.struct), C.byref(model.struct), n, _p(d_node), _p(pp),
+                                      _p(d_pp_row), _p(pc), _p(d_pc_row),
+                                      _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64,
+                                      -1 if gap_state is None else int(gap_state), int(bool(ignore_gaps)),
+                                      _p(d_grid), G, _p(out), _p(ws), ws_bytes, _stream()), "tt_prob_t_profiles_grid")
+    return out
+
+
+def prob_t_pairs_grid(q, counts, model, d_grid, model_of=None):
+    """log P(state pairs | t) of [n, q, q] device counts at each point of the
+    branch's row of d_grid: the 'joint' BranchLenInterpolator values
+    (treetime/branch_len_interpolator.py:107-118)."""
+    t = torch()
+    lib = _lib.load()
+    n = counts.shape[0]
+    G = int(d_grid.shape[1])
+    if d_grid.shape[0] != n:
+        raise ValueError("prob_t_pairs_grid: %d grid rows for %d branches" % (d_grid.shape[0], n))
+    out = t.empty((n, G), dtype=t.float64, device=counts.device)
+    mo = None
+    if model_of is not None:
+        mo = model_of if hasattr(model_of, "data_ptr") else _to_dev(np.asarray(model_of, np.int32), counts.device)
+    check(lib.tt_prob_t_pairs_grid(q, n, _p(counts), _p(mo), C.byref(model.struct), _p(d_grid), G, _p(out),
+                                   _stream()), "tt_prob_t_pairs_grid")
+    return out
+
+
 def _mini_forest(n_nodes, q, bl, device, mult=None, parent=None, n_int=None, P=1):
     """A one-tree forest struct for standalone per-branch calls."""
     dev = require_device(device)

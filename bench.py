@@ -396,6 +396,137 @@ def run_c2(args):
     return res
 
 
+BLGRID_WORKLOAD = ("blgrid: BranchLenInterpolator likelihood grids ('marginal' mode, TreeTime's 125-point grids) "
+                   "of every branch of the 2000-tip x 30000-site tree, from its FP32 reconstruction's profiles")
+BLGRID_METRIC = "branch-length grid evaluations/s (log P of one pattern at one grid point of one branch)"
+BLGRID_UNIT = "evaluations/s"
+
+
+def _fp64_fma_rate(engine, dev):
+    """Measured FP64 FMA issue rate of this GPU (FMAs/s), from the library's
+    probe kernel: best of 3 launches of SMs x 8 CTAs x 256 threads x 8
+    independent chains x 4096 FMAs, CUDA events on the launching stream."""
+    import torch
+    lib = engine._lib.load()
+    blocks = int(lib.tt_device_sm_count()) * 8
+    sink = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
+    iters = 4096
+    engine.check(lib.tt_fp64_fma_probe(64, blocks, engine._p(sink), engine._stream()), "tt_fp64_fma_probe")
+    best = float("inf")
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        engine.check(lib.tt_fp64_fma_probe(iters, blocks, engine._p(sink), engine._stream()), "tt_fp64_fma_probe")
+        b.record()
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return blocks * 256 * 8 * iters / (best * 1e-3)
+
+
+def run_blgrid(args):
+    """--workload blgrid: the likelihood grids of every branch (TreeTime's
+    BranchLenInterpolator values in 'marginal' mode) from the profiles of a
+    marginal reconstruction, one launch per branch group (internal nodes,
+    tips); FP64 arithmetic (per-pattern eigen sums and a table-driven log)."""
+    import torch
+    from treetime_gb300 import engine
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t, wl = build_workload()
+    t.device = dev
+    t.infer_ancestral_sequences(marginal=True)
+    nodes = [n for n in t.tree.find_clades() if n.up is not None]
+    sess = t._get_session()
+    forest = sess["forest"]
+    model = engine.model_for(t.gtr, dev)
+    padded, lengths = engine.branch_len_grids([n.mutation_length for n in nodes], t.one_mutation)
+    P, q = t.data.compressed_length, t.gtr.n_states
+    evals = int(lengths.sum()) * P
+    prec = t._gpu_precision()
+    groups = []
+    for idx, kk, pp, pp_row, pc_row, pc in t._profile_branch_groups(nodes):
+        groups.append((engine._to_dev(np.asarray(kk, np.int32), dev), pp,
+                       engine._to_dev(np.asarray(pp_row, np.int64), dev), pc,
+                       engine._to_dev(np.asarray(pc_row, np.int64), dev), engine._to_dev(padded[idx], dev), idx))
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def step():
+        return [engine.prob_t_profiles_grid_dev(forest, model, dn, pp, dpr, pc, dcr, prec, t.gtr.gap_index, True, dg)
+                for dn, pp, dpr, pc, dcr, dg, _ in groups]
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ts = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            step()
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+    ms = _reduce_max(sum(ts) / len(ts), dev, world)
+    # end to end through the public call: host grids, uploads, the launches, the results back
+    e2e = []
+    for i in range(max(3, min(args.steps, 10))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = t.branch_length_grids(nodes)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = statistics.median(e2e) * 1e3
+    fma_rate = _fp64_fma_rate(engine, dev)
+    if rank != 0:
+        return None
+    # FP64 instructions per evaluation: q FMAs of the eigen sum, 1 add of the 1e-24 floor, the table log
+    # (1 subtract for the reduced argument, 1 multiply by 1/F, 6 polynomial FMAs, 2 FMAs to assemble)
+    # and 1 FMA to accumulate weight * log: q + 12
+    ops = evals * (q + 12)
+    achieved = ops / (ms * 1e-3)
+    out = {
+        "metric": BLGRID_METRIC, "value": world * evals / (ms * 1e-3), "unit": BLGRID_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
+        "config": {"workload": BLGRID_WORKLOAD, "branches": len(nodes), "patterns": P,
+                   "grid_points": int(lengths.sum()), "evaluations_per_step": evals, "profiles": prec,
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU"},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fma_rate / 1e12,
+                     "unit": "T FP64 instructions/s", "frac": achieved / fma_rate, "traffic": None,
+                     "peak_source": "measured live (FP64 FMA probe kernel)",
+                     "ops_per_evaluation": q + 12},
+        "e2e": {"value": evals / (e2e_ms * 1e-3), "unit": BLGRID_UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(padded.nbytes + sum(len(g[6]) * 20 for g in groups)),
+                "d2h_bytes_per_step": int(padded.nbytes)},
+        "gpu_launches": len(groups) * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        # TreeTime's own evaluation (numpy, per grid point) for a sample of branches
+        from oracle import anc
+        mult = t.data.multiplicity()
+        chosen = nodes[::max(1, len(nodes) // 400)]
+        errs, done, secs = [], 0, 0.0
+        for n in chosen:
+            grid, y = res[n]
+            pp, pc = np.asarray(n.marginal_outgroup_LH, np.float64), np.asarray(n.marginal_subtree_LH, np.float64)
+            t0 = time.perf_counter()
+            want = anc.branch_len_log_prob(t.gtr, grid, "marginal", profile_pair=(pp, pc), multiplicity=mult)
+            secs += time.perf_counter() - t0
+            done += len(grid) * P
+            errs.append(float(np.max(np.abs(y - want) / np.maximum(np.abs(want), 1.0))))
+            if secs > 20.0:
+                break
+        out["cpu_baseline"] = {"value": done / secs, "unit": BLGRID_UNIT, "cores": 1, "kind": "port",
+                               "sample": "%d branches' grids (every %d-th branch) by the numpy restatement of "
+                                         "TreeTime's BranchLenInterpolator evaluation, 1 process"
+                                         % (len(errs), max(1, len(nodes) // 400)), "seconds": secs}
+        out["max_rel_err_vs_oracle"] = max(errs)
+    return out
+
+
 C3_WORKLOAD = ("c3: 256 independent coalescent trees, tips log-uniform in [50, 5000], sites log-uniform in "
                "[1k, 30k], branch means log-uniform in [1e-4, 0.05], a random GTR per tree; the whole batch is "
                "one forest, one captured launch sequence per step")
@@ -775,7 +906,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "blgrid"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
@@ -793,7 +924,7 @@ def main():
     else:
         from treetime_gb300 import build
         build.build()
-        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4}[args.workload](args)
+        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4, "blgrid": run_blgrid}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

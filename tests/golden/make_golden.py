@@ -4,6 +4,7 @@ Run in a container where the TreeTime sources are available (they are not
 shipped with this repository and are not needed to run the tests):
 
     python tests/golden/make_golden.py /path/to/treetime-source
+    python tests/golden/make_golden.py /path/to/treetime-source --blgrid   (interpolator grids only)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from

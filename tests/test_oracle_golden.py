@@ -162,10 +162,14 @@ def test_branch_len_grids_match_treetime(case):
     g = gc.load(case)
     n, om = int(g["n_grid_points"]), float(g["one_mutation"])
     for mode in ("marginal", "joint"):
+        grids, lengths = engine.branch_len_grids(g[mode + "_mutation_length"], om, n)
+        np.testing.assert_array_equal(lengths, g[mode + "_len"])
         for i, ml in enumerate(g[mode + "_mutation_length"]):
             want = g[mode + "_x"][i, :int(g[mode + "_len"][i])]
             np.testing.assert_array_equal(anc.branch_len_grid(float(ml), om, n), want)
             np.testing.assert_array_equal(engine.branch_len_grid(float(ml), om, n), want)
+            np.testing.assert_array_equal(grids[i, :lengths[i]], want)
+            assert (grids[i, lengths[i]:] == -1.0).all()
 
 
 @pytest.mark.parametrize("mode", ["marginal", "joint"])

@@ -87,6 +87,7 @@ _SIGS = {
     "tt_prob_t_profiles_grid": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, i32, vp, i32, vp,
                                       vp, i64, vp]),
     "tt_prob_t_pairs_grid": (i32, [i32, i64, vp, vp, P(TTModel), vp, i32, vp, vp]),
+    "tt_fp64_fma_probe": (i32, [i64, i32, vp, vp]),
     "tt_compress_columns": (i32, [vp, i64, i64, i32, vp, vp, vp]),
 }
 

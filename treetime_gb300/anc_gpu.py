@@ -76,7 +76,8 @@ class ResultStore:
             if is_tip:
                 return self.tt._tip_profile(node)
             x = self._rows("partial", k)
-            if self.precision == "f32":  # FP32 partials are power-of-two scaled
+            if self.precision == "f32":  # FP32 partials are power-of-two scaled: normalise in FP64
+                x = x.astype(np.float64)
                 x = x / x.sum(axis=1, keepdims=True)
             return x
         if name == "marginal_outgroup_LH":
@@ -437,8 +438,7 @@ class GPUAncMixin:
                 raise Exception("Cannot create branch length interpolator for the root node.")
         if not nodes:
             return {}
-        grids = [engine.branch_len_grid(n.mutation_length, one_mutation, n_grid_points) for n in nodes]
-        padded = engine.pad_grids(grids)
+        padded, lengths = engine.branch_len_grids([n.mutation_length for n in nodes], one_mutation, n_grid_points)
         sess = self._get_session()
         dev = sess["forest"].device
         logp = np.empty(padded.shape)
@@ -460,7 +460,7 @@ class GPUAncMixin:
             counts = engine.torch().trunc(hist)[ks].contiguous()  # TreeTime casts pair counts to int
             logp = engine.prob_t_pairs_grid(self.gtr.n_states, counts, sess["model"],
                                             engine._to_dev(padded, dev)).cpu().numpy()
-        return {n: (grids[i], -logp[i, :len(grids[i])]) for i, n in enumerate(nodes)}
+        return {n: (padded[i, :lengths[i]], -logp[i, :lengths[i]]) for i, n in enumerate(nodes)}
 
     def optimal_marginal_branch_length(self, node, tol=1e-10):
         if node.up is None:

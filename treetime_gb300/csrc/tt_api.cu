@@ -30,9 +30,34 @@ int sm_count() {
     return n > 0 ? n : 1;
 }
 
+// FP64 FMA issue-rate probe: 8 independent dependency chains per thread, so that the FP64 pipe,
+// not latency, sets the time.  Every thread writes its sum (nothing is dead code).
+__global__ void __launch_bounds__(256) fp64_fma_probe_kernel(int64_t iters, double a, double b, double* sink) {
+    double x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c;
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += x[c];
+    sink[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace tt
 
 extern "C" {
+
+tt_status tt_fp64_fma_probe(int64_t iters, int32_t blocks, double* sink, void* stream) {
+    if (iters < 0 || blocks <= 0 || !sink) {
+        tt::set_error("tt_fp64_fma_probe: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    tt::fp64_fma_probe_kernel<<<blocks, 256, 0, tt::as_stream(stream)>>>(iters, 0.9999999, 1e-7, sink);
+    return tt::check_launch("tt_fp64_fma_probe");
+}
 
 int32_t tt_abi_version(void) { return TT_ABI_VERSION; }
 

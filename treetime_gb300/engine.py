@@ -803,40 +803,44 @@ def _profile_workspace(forest, n, dev):
 # ----------------------------------------------------------------------------
 # single-call GTR API (device computations behind GTR methods)
 # ----------------------------------------------------------------------------
-def branch_len_grid(mutation_length, one_mutation, n_grid_points=ttconf.BRANCH_GRID_SIZE):
-    """The branch lengths at which BranchLenInterpolator tabulates a branch's
-    likelihood (treetime/branch_len_interpolator.py:36-62), built with the same
-    numpy expressions so that the grid is identical to TreeTime's: for an
+def branch_len_grids(mutation_lengths, one_mutation, n_grid_points=ttconf.BRANCH_GRID_SIZE):
+    """The branch lengths at which BranchLenInterpolator tabulates each
+    branch's likelihood (treetime/branch_len_interpolator.py:36-62), for many
+    branches at once: ([n, G] grids padded with -1, [n] lengths).  The numpy
+    expressions are TreeTime's, applied row-wise (elementwise IEEE operations
+    and a row sort), so every row is identical to TreeTime's grid: for an
     effectively zero branch (mutation_length < min(1e-5, one_mutation / 10))
     a linear ramp to 10 mutations then a quadratic one to MAX_BRANCH_LENGTH;
     otherwise points clustered at zero, a quadratic approach to the branch
     length, a quadratic tail to 4x it and a sparse tail to MAX_BRANCH_LENGTH."""
-    ml = float(mutation_length)
+    ml = np.asarray(mutation_lengths, dtype=np.float64).reshape(-1)
     n = int(n_grid_points)
-    if ml < np.min((1e-5, 0.1 * one_mutation)):
-        short = 10 * one_mutation
-        ramp = short * (np.linspace(0, 1.0, n // 2)[:-1])
-        rest = short + (ttconf.MAX_BRANCH_LENGTH - short) * (np.linspace(0, 1.0, n // 2 + 1) ** 2)
-        return np.concatenate([ramp, rest])
-    sigma = ml
-    left = ml * (1 - np.linspace(1, 0.0, n // 3) ** 2.0)
-    near_zero = left[1] * np.logspace(-20, 0, 6)[:5]
-    near_zero2 = left[1] * np.linspace(0, 1, 10)[1:-1]
-    right = ml + (3 * sigma * (np.linspace(0, 1, n // 3) ** 2))
-    far = right.max() + ttconf.MAX_BRANCH_LENGTH * np.linspace(0, 1, n // 3) ** 2
-    grid = np.concatenate((near_zero, near_zero2, left, right[1:], far[1:]))
-    grid.sort()
-    return grid
+    zero = ml < np.min((1e-5, 0.1 * one_mutation))
+    short = 10 * one_mutation
+    zgrid = np.concatenate([short * (np.linspace(0, 1.0, n // 2)[:-1]),
+                            short + (ttconf.MAX_BRANCH_LENGTH - short) * (np.linspace(0, 1.0, n // 2 + 1) ** 2)])
+    m = ml[~zero][:, None]
+    left = m * (1 - np.linspace(1, 0.0, n // 3) ** 2.0)
+    near_zero = left[:, 1:2] * np.logspace(-20, 0, 6)[:5]
+    near_zero2 = left[:, 1:2] * np.linspace(0, 1, 10)[1:-1]
+    right = m + (3 * m * (np.linspace(0, 1, n // 3) ** 2))
+    far = right.max(axis=1, keepdims=True) + ttconf.MAX_BRANCH_LENGTH * np.linspace(0, 1, n // 3) ** 2
+    fgrid = np.concatenate((near_zero, near_zero2, left, right[:, 1:], far[:, 1:]), axis=1)
+    fgrid.sort(axis=1)
+    G = max(len(zgrid) if zero.any() else 0, fgrid.shape[1] if len(m) else 0)
+    out = np.full((len(ml), G), -1.0)
+    lengths = np.where(zero, len(zgrid), fgrid.shape[1]).astype(np.int64)
+    if zero.any():
+        out[zero, :len(zgrid)] = zgrid
+    if len(m):
+        out[~zero, :fgrid.shape[1]] = fgrid
+    return out, lengths
 
 
-def pad_grids(grids):
-    """[n][G] FP64 array of ragged per-branch grids, short rows padded with -1
-    (the grid kernels return -1e10 there)."""
-    G = max((len(g) for g in grids), default=0)
-    out = np.full((len(grids), G), -1.0)
-    for i, g in enumerate(grids):
-        out[i, :len(g)] = g
-    return out
+def branch_len_grid(mutation_length, one_mutation, n_grid_points=ttconf.BRANCH_GRID_SIZE):
+    """One branch's grid (see branch_len_grids)."""
+    g, n = branch_len_grids([mutation_length], one_mutation, n_grid_points)
+    return g[0, :n[0]]
 
 
 def prob_t_profiles_grid_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, precision, gap_state, ignore_gaps,

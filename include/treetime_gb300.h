@@ -20,6 +20,9 @@
  *   tt_prob_t_profiles_grid, tt_prob_t_pairs_grid
  *                        the log-likelihood grids of BranchLenInterpolator ('marginal', 'joint')
  *                                                                treetime/branch_len_interpolator.py:96-125
+ *   tt_mutation_counts, tt_mutation_counts_joint
+ *                        the substitution counting of TreeAnc.infer_gtr   treetime/treeanc.py:1544-1584
+ *   tt_branch_mutation_matrix  TreeAnc.get_branch_mutation_matrix     treetime/treeanc.py:1085-1120
  *   tt_compress_columns  SequenceData.make_compressed_alignment  treetime/sequence_data.py:325-464
  *
  * Conventions
@@ -343,6 +346,41 @@ tt_status tt_prob_t_profiles_grid(const tt_forest* f, const tt_model* m, int64_t
 tt_status tt_prob_t_pairs_grid(int32_t q, int64_t n, const double* counts, const int32_t* model_of,
                                const tt_model* m, const double* grid, int32_t n_grid, double* logp_out,
                                void* stream);
+
+/* ------------------------------------------ substitution counts (GTR inference)
+ * Counts for tree `tree` of the forest (n_patterns = its pattern count) over n branches
+ * (node ids node_of[b] of that tree, any order): n_ija[i][j][a] (derived state i, ancestral
+ * state j, pattern a; [q][q][n_patterns]) and T_ia[i][a] ([q][n_patterns]), both overwritten.
+ * Accumulation is deterministic: branches are split into contiguous chunks, each summed in order
+ * into its own slice of `workspace` (device FP64) and the slices added in order; the workspace
+ * must hold at least rows * n_patterns doubles (rows = 2*q*q marginal, q*q + q joint), more
+ * allows up to 64 chunks.
+ * tt_mutation_counts ('marginal'): profiles as for tt_optimal_t_profiles, p64 the FP64 branch
+ * matrices of tt_branch_pmats; per branch and pattern M = pc_i pp_j (P(t)_ij + 1e-24) normalised,
+ * n_ija += M * mult * mask, T_ia += 0.5 t (row and column sums of M) * mult * mask.
+ * tt_mutation_counts_joint: parent states from `states` (tt_joint / tt_marginal layout), child
+ * states from `states` or, for tips when tips_use_states = 0, from their codes through
+ * char_state (byte -> state, 255 = not a state of the alphabet); where both are states, differ and
+ * the mask is positive, the pattern's positions (mult minus tip_mismatch[tip row][a], the
+ * positions where the tip's raw character differs from its compressed one; may be NULL) are
+ * added to n_ija[child][parent][a] with 0.5 t each moved in T from the child to the parent
+ * state; every branch adds t * mult * mask to T[child state][a].
+ * Replaces the counting loop of TreeAnc.infer_gtr (treetime/treeanc.py:1544-1584). */
+tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, int32_t tree, int32_t n_patterns, int64_t n,
+                             const int32_t* node_of, const void* pp, const int64_t* pp_row, const void* pc,
+                             const int64_t* pc_row, int32_t prec, const double* p64, double* n_ija,
+                             double* T_ia, double* workspace, int64_t workspace_bytes, void* stream);
+tt_status tt_mutation_counts_joint(const tt_forest* f, int32_t tree, int32_t n_patterns, int64_t n,
+                                   const int32_t* node_of, const uint8_t* states, const uint8_t* char_state,
+                                   int32_t tips_use_states, const int32_t* tip_mismatch, double* n_ija,
+                                   double* T_ia, double* workspace, int64_t workspace_bytes, void* stream);
+/* The normalised joint distribution of the states at both ends of one branch (node[0] on the
+ * device), out[a][i][j] for every pattern a (i child, j parent): TreeAnc.get_branch_mutation_matrix
+ * (treetime/treeanc.py:1085-1120). */
+tt_status tt_branch_mutation_matrix(const tt_forest* f, const tt_model* m, int32_t tree, int32_t n_patterns,
+                                    const int32_t* node, const void* pp, const int64_t* pp_row, const void* pc,
+                                    const int64_t* pc_row, int32_t prec, const double* p64, double* out,
+                                    void* stream);
 
 /* -------------------------------------------------- a1: compression
  * Column classes of a tips x sites byte matrix (row-major, n_rows x n_cols): key[c] = the letter

@@ -464,6 +464,72 @@ def pair_resolution(model, grid, seq_pair):
                      for k in grid])
 
 
+def branch_mutation_matrix(model, pp, pc, t):
+    """treeanc.py:1085-1120 (standard models): normalised
+    pc_i pp_j (expQt(t)_ij + 1e-24) per pattern, [L, q, q]."""
+    Qt = expQt(model, t) + SUPERTINY_NUMBER
+    M = np.einsum("ai,aj,ij->aij", pc, pp, Qt)
+    norm = M.sum(axis=2).sum(axis=1)
+    return np.einsum("aij,a->aij", M, 1.0 / norm)
+
+
+def substitution_counts_marginal(tree, res, mult, model, full_length):
+    """The 'marginal' counting loop of TreeAnc.infer_gtr (treeanc.py:1544-1563)
+    from an oracle marginal reconstruction ``res``: (n_ija, T_ia)."""
+    q = len(model.alphabet)
+    L = len(mult)
+    n_ija = np.zeros((q, q, L))
+    T_ia = np.zeros((q, L))
+    for node in preorder(tree.root):
+        if not node.clades:
+            continue
+        for c in node.clades:
+            t = branch_length_to_gtr(c, full_length)
+            mut = np.transpose(branch_mutation_matrix(model, res["outgroup_LH"][c.name], res["subtree_LH"][c.name],
+                                                      t), (1, 2, 0))
+            m = mult if getattr(c, "mask", None) is None else mult * c.mask
+            T_ia += 0.5 * t * mut.sum(axis=0) * m
+            T_ia += 0.5 * t * mut.sum(axis=1) * m
+            n_ija += mut * m
+    return n_ija, T_ia
+
+
+def substitution_counts_joint(tree, cseq, raw_of, f2c, mult, model, full_length):
+    """The 'joint' counting loop of TreeAnc.infer_gtr (treeanc.py:1564-1582):
+    mutations on the full-length sequences (a tip's raw characters when
+    ``raw_of(name)`` gives them, else its compressed sequence), skipped where a
+    character is not a state; ``cseq`` name -> compressed characters."""
+    q = len(model.alphabet)
+    L = len(mult)
+    index = {s: i for i, s in enumerate(np.asarray(model.alphabet).tolist())}
+    n_ija = np.zeros((q, q, L))
+    T_ia = np.zeros((q, L))
+    for node in preorder(tree.root):
+        if not node.clades:
+            continue
+        for c in node.clades:
+            t = branch_length_to_gtr(c, full_length)
+            parent = cseq[node.name][f2c]
+            raw = raw_of(c.name)
+            child = raw if raw is not None else (cseq[c.name][f2c] if c.name in cseq else None)
+            if child is not None:
+                for pos in np.where(parent != child)[0]:
+                    a, d = parent[pos], child[pos]
+                    if a not in index or d not in index:
+                        continue
+                    i, j = index[d], index[a]
+                    cpos = f2c[pos]
+                    n_ija[i, j, cpos] += 1
+                    T_ia[j, cpos] += 0.5 * t
+                    T_ia[i, cpos] -= 0.5 * t
+            if c.name in cseq:
+                m = mult if getattr(c, "mask", None) is None else mult * c.mask
+                for i, nuc in enumerate(model.alphabet):
+                    ind = cseq[c.name] == nuc
+                    T_ia[i, ind] += t * m[ind]
+    return n_ija, T_ia
+
+
 def optimize_branch_lengths_joint(tree, cseq_of, mult, model, ignore_gaps=True):
     """TreeAnc.optimize_branch_lengths_joint (treeanc.py:1176-1242) with
     optimal_branch_length (:1244-1270) and add_branch_state (:1148-1163).

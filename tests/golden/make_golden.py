@@ -5,6 +5,7 @@ shipped with this repository and are not needed to run the tests):
 
     python tests/golden/make_golden.py /path/to/treetime-source
     python tests/golden/make_golden.py /path/to/treetime-source --blgrid   (interpolator grids only)
+    python tests/golden/make_golden.py /path/to/treetime-source --infer-gtr   (GTR inference only)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -215,6 +216,110 @@ def blgrid_cases():
                n_grid_points=75)
 
 
+def run_infer_gtr(name, newick, aln, kind, params, compress=True, masks=None, site_specific=False, pc=5.0):
+    """TreeAnc.infer_gtr in 'marginal' and 'joint' mode: the counts TreeTime
+    hands to GTR.infer / GTR_site_specific.infer (captured at the call) and the
+    inferred model."""
+    from treetime import TreeAnc, GTR, GTR_site_specific
+    out = {"case": name, "newick": newick, "kind": kind, "compress": compress, "site_specific": site_specific,
+           "pc": pc, "aln_names": np.array(list(aln.keys())), "aln_seqs": np.array(list(aln.values()))}
+    for k, v in params.items():
+        out["param_" + k] = np.asarray(v)
+    if masks:
+        out["mask_names"] = np.array(list(masks.keys()))
+        out["mask_rows"] = np.stack([masks[k] for k in masks])
+    cls = GTR_site_specific if site_specific else GTR
+    captured = {}
+    orig = cls.__dict__["infer"].__func__
+
+    def capture(klass, *args, **kwargs):
+        captured["args"] = [np.array(a, copy=True) for a in args]
+        captured["root_state"] = np.array(kwargs.get("root_state", args[2] if len(args) > 2 else None), copy=True)
+        return orig(klass, *args, **kwargs)
+
+    modes = ("marginal",) if site_specific or masks else ("marginal", "joint")
+    for mode in modes:
+        tree, recs = _bio_inputs(newick, aln)
+        t = TreeAnc(tree=tree, aln=recs, gtr=_ref_gtr(kind, params), compress=compress, verbose=0)
+        if masks:
+            for n in t.tree.find_clades():
+                if n.name in masks:
+                    n.mask = masks[n.name]
+        t.infer_ancestral_sequences(marginal=mode == "marginal")
+        cls.infer = classmethod(capture)
+        try:
+            g = t.infer_gtr(marginal=mode == "marginal", site_specific=site_specific, pc=pc)
+        finally:
+            cls.infer = classmethod(orig)
+        a = captured["args"]
+        out[mode + "_nij"] = a[0]
+        out[mode + "_Ti"] = a[1]
+        out[mode + "_root_state"] = captured["root_state"]
+        out[mode + "_W"], out[mode + "_Pi"], out[mode + "_mu"] = np.asarray(g.W), np.asarray(g.Pi), np.asarray(g.mu)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
+
+
+def infer_gtr_cases():
+    """Nucleotides (4 states), 5 states with gaps and ambiguity codes, masks
+    (marginal mode) and a site-specific inference from an uncompressed
+    protein alignment."""
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    rng = np.random.default_rng(31)
+    tree = synth.coalescent_tree(24, 0.04, rng)
+    pi = rng.dirichlet(np.ones(4))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(4, 4)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap")
+    states = synth.evolve(tree, g, 300, rng)
+    aln = synth._to_text(states, g.alphabet, 0.02, rng)
+    nwk = to_newick(tree)
+    prm = {"pi": pi, "W": W, "alphabet": "nuc_nogap", "mu": 1.0}
+    run_infer_gtr("gtrinf_nuc", nwk, aln, "gtr", prm)
+    from treetime_gb300.seqdata import SequenceData
+    P = SequenceData(aln, compress=True, ambiguous="N").compressed_length
+    names = [c.name for c in tree.find_clades() if c.name][:5]
+    masks = {k: (rng.random(P) < 0.7).astype(float) for k in names}
+    run_infer_gtr("gtrinf_nuc_masked", nwk, aln, "gtr", prm, masks=masks)
+
+    rng = np.random.default_rng(32)
+    tree = synth.coalescent_tree(18, 0.05, rng)
+    pi = rng.dirichlet(np.ones(5))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(5, 5)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc")
+    states = synth.evolve(tree, g, 250, rng, invariant_frac=0.4)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    for k in list(aln):
+        s = np.array(list(aln[k]))
+        r = rng.random(len(s))
+        s[r < 0.04] = "N"
+        s[(r > 0.04) & (r < 0.06)] = rng.choice(list("RYKM"))
+        if rng.random() < 0.3:
+            s[: rng.integers(1, 8)] = "-"
+        aln[k] = "".join(s)
+    run_infer_gtr("gtrinf_nuc5", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "nuc", "mu": 1.0})
+
+    rng = np.random.default_rng(33)
+    L = 60
+    tree = synth.yule_tree(12, 0.08, rng)
+    from treetime_gb300.gtr import GTR_site_specific
+    pi_s = rng.dirichlet(np.full(21, 0.5), size=L).T
+    W_s = np.triu(rng.uniform(0.1, 5.0, size=(21, 21)), 1)
+    W_s = W_s + W_s.T
+    gs = GTR_site_specific(seq_len=L, approximate=False, alphabet=synth.AA21)
+    gs.assign_rates(mu=1.0, pi=pi_s, W=W_s)
+    states = synth.evolve_site_specific(tree, gs, L, rng)
+    aln = synth._to_text(states, gs.alphabet, 0.0, rng)
+    pi0 = rng.dirichlet(np.ones(21))
+    W0 = rng.uniform(0.5, 2.0, size=(21, 21))
+    W0 = W0 + W0.T
+    run_infer_gtr("gtrinf_aa_ss", to_newick(tree), aln, "gtr",
+                  {"pi": pi0, "W": W0, "alphabet": synth.AA21, "mu": 1.0}, compress=False, site_specific=True)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -358,5 +463,8 @@ if __name__ == "__main__":
     if "--blgrid" in sys.argv:
         _setup(ref)
         blgrid_cases()
+    elif "--infer-gtr" in sys.argv:
+        _setup(ref)
+        infer_gtr_cases()
     else:
         main(ref)

@@ -13,9 +13,46 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def case_names():
-    """Reconstruction cases (every fixture but the branch-length grids)."""
+    """Reconstruction cases (every fixture but the branch-length grids and the
+    GTR inference cases)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("blgrid_"))
+                  if not os.path.basename(p).startswith(("blgrid_", "gtrinf_")))
+
+
+def gtrinf_names():
+    """TreeAnc.infer_gtr fixtures."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "gtrinf_*.npz")))
+
+
+def gtrinf_oracle(g, mode):
+    """(n_ija, T_ia, root cseq) of the oracle's counting on the fixture's
+    inputs after its own reconstruction in `mode`."""
+    from oracle import anc
+    tree, aln, model, masks = inputs_from(g)
+    anc.prepare_tree(tree)
+    if masks:
+        for n in anc.preorder(tree.root):
+            if n.name in masks:
+                n.mask = masks[n.name]
+    if bool(g["compress"]):
+        caln, mult, full = compress_inputs(aln, model)
+    else:
+        arrays = {k: anc.seq2array(v, fill_overhangs=True, ambiguous=model.ambiguous) for k, v in aln.items()}
+        caln, mult, f2c, _ = anc.compress_alignment(list(arrays), arrays, model.ambiguous)
+        extend_profile(model, list(caln.values()))
+        full = len(f2c)
+    arrays = {k: anc.seq2array(v, fill_overhangs=True, ambiguous=model.ambiguous) for k, v in aln.items()}
+    _, _, f2c, _ = anc.compress_alignment(list(arrays), arrays, model.ambiguous)
+    if mode == "marginal":
+        res = anc.marginal(tree, caln, mult, model, full)
+        n_ija, T_ia = anc.substitution_counts_marginal(tree, res, mult, model, full)
+        return n_ija, T_ia, res
+    res = anc.joint(tree, caln, mult, model, full)
+    cseq = dict(res["cseq"])
+    cseq.update(caln)
+    n_ija, T_ia = anc.substitution_counts_joint(tree, cseq, lambda k: arrays.get(k), np.asarray(f2c), mult, model,
+                                                full)
+    return n_ija, T_ia, res
 
 
 def blgrid_names():

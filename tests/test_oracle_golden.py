@@ -191,3 +191,46 @@ def test_oracle_branch_len_values_match_treetime(case, mode):
         assert n_noise == 0
     elif case == "blgrid_nuc":
         assert n_noise > 0  # the fixture does reach the rounding-dominated points
+
+
+# ------------------------------------------------------------------ GTR inference
+GTRINF = gc.gtrinf_names()
+
+
+def _gtrinf_modes(g):
+    return [m for m in ("marginal", "joint") if m + "_nij" in g]
+
+
+@pytest.mark.parametrize("case", GTRINF)
+def test_host_gtr_infer_matches_treetime(case):
+    """The host fit (GTR.infer / GTR_site_specific.infer) on TreeTime's own
+    counts gives TreeTime's model."""
+    from treetime_gb300.gtr import GTR, GTR_site_specific
+    g = gc.load(case)
+    model = gc.model_from(g)
+    for mode in _gtrinf_modes(g):
+        if bool(g["site_specific"]):
+            m = GTR_site_specific.infer(np.copy(g[mode + "_nij"]), np.copy(g[mode + "_Ti"]),
+                                        root_state=np.copy(g[mode + "_root_state"]), pc=float(g["pc"]),
+                                        alphabet=model.alphabet, prof_map=model.profile_map)
+            m.mu /= m.average_rate().mean()
+        else:
+            m = GTR.infer(np.copy(g[mode + "_nij"]), np.copy(g[mode + "_Ti"]), np.copy(g[mode + "_root_state"]),
+                          pc=float(g["pc"]), alphabet=model.alphabet, prof_map=model.profile_map)
+            m.mu = 1.0
+        np.testing.assert_allclose(m.W, g[mode + "_W"], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(m.Pi, g[mode + "_Pi"], rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(m.mu, g[mode + "_mu"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("case", GTRINF)
+def test_oracle_substitution_counts_match_treetime(case):
+    g = gc.load(case)
+    for mode in _gtrinf_modes(g):
+        n_ija, T_ia, _ = gc.gtrinf_oracle(g, mode)
+        if bool(g["site_specific"]):
+            np.testing.assert_allclose(n_ija, g[mode + "_nij"], rtol=1e-11, atol=1e-11)
+            np.testing.assert_allclose(T_ia, g[mode + "_Ti"], rtol=1e-11, atol=1e-11)
+        else:
+            np.testing.assert_allclose(n_ija.sum(axis=-1), g[mode + "_nij"], rtol=1e-11, atol=1e-11)
+            np.testing.assert_allclose(T_ia.sum(axis=-1), g[mode + "_Ti"], rtol=1e-11, atol=1e-11)

@@ -88,6 +88,10 @@ _SIGS = {
                                       vp, i64, vp]),
     "tt_prob_t_pairs_grid": (i32, [i32, i64, vp, vp, P(TTModel), vp, i32, vp, vp]),
     "tt_fp64_fma_probe": (i32, [i64, i32, vp, vp]),
+    "tt_mutation_counts": (i32, [P(TTForest), P(TTModel), i32, i32, i64, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp,
+                                 i64, vp]),
+    "tt_mutation_counts_joint": (i32, [P(TTForest), i32, i32, i64, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp]),
+    "tt_branch_mutation_matrix": (i32, [P(TTForest), P(TTModel), i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp]),
     "tt_compress_columns": (i32, [vp, i64, i64, i32, vp, vp, vp]),
 }
 

@@ -467,19 +467,156 @@ class GPUAncMixin:
             return self.one_mutation
         return float(self._marginal_branch_lengths([node], tol)[0])
 
+    # ------------------------------------------------------------ GTR inference
+    def _tip_mismatch(self):
+        """[tip rows, P] int32: alignment positions of each pattern where a
+        tip's character differs from its compressed character (compression
+        rewrites the ambiguous character in columns of one state; TreeTime
+        counts a tip's mutations on its raw characters), or None."""
+        d = self.data
+        name_to_row, ccodes = self._aln_index()
+        f2c = np.asarray(d.full_to_compressed_sequence_map)
+        if hasattr(d, "codes") and getattr(d, "sequence_names", None) is not None:
+            raw = np.asarray(d.codes)
+            rows = [name_to_row[k] for k in d.sequence_names]
+        else:
+            names = list(name_to_row)
+            raw = np.stack([chars_to_codes(np.asarray(d.aln[k])) for k in names])
+            rows = [name_to_row[k] for k in names]
+        P = ccodes.shape[1]
+        out = np.zeros((ccodes.shape[0], P), dtype=np.int64)
+        for i, r in enumerate(rows):
+            mm = raw[i] != ccodes[r][f2c]
+            if mm.any():
+                out[r] = np.bincount(f2c[mm], minlength=P)
+        return out.astype(np.int32) if out.any() else None
+
+    def _counting_branches(self):
+        """Branches in TreeTime's counting order: children of the internal
+        nodes in get_nonterminals() order (treetime/treeanc.py:1545-1546)."""
+        return [c for n in self.tree.get_nonterminals() for c in n.clades]
+
+    def get_branch_mutation_matrix(self, node, full_sequence=False):
+        """[L, q, q] joint distribution of the states at both ends of the branch
+        above `node` from the last marginal reconstruction (i child, j parent),
+        computed on the device (treetime/treeanc.py:1085-1120)."""
+        if self.gtr.is_site_specific:
+            raise NotImplementedError("mutation matrices with site-specific models are not supported on the GPU")
+        sess = self._get_session()
+        model = engine.model_for(self.gtr, getattr(self, "device", None))
+        engine.branch_pmats(sess["forest"], model, sess["bufs"])
+        p64 = sess["bufs"].cache[("p64", engine.torch().float64)]
+        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups([node]):
+            m = engine.branch_mutation_matrix(sess["forest"], model, p64, 0, kk[0], pp, pp_row[0], pc, pc_row[0],
+                                              self._gpu_precision()).cpu().numpy()
+        if full_sequence:
+            return m[self.data.full_to_compressed_sequence_map]
+        return m
+
+    def _substitution_counts(self, marginal):
+        """(n_ija [q, q, P], T_ia [q, P]) over all branches, on the device."""
+        sess = self._get_session()
+        layout, forest = sess["layout"], sess["forest"]
+        nodes = self._counting_branches()
+        t = engine.torch()
+        if marginal:
+            if self.gtr.is_site_specific:
+                raise NotImplementedError("marginal GTR inference from a site-specific model is not supported "
+                                          "on the GPU")
+            model = engine.model_for(self.gtr, getattr(self, "device", None))
+            engine.branch_pmats(forest, model, sess["bufs"])
+            p64 = sess["bufs"].cache[("p64", t.float64)]
+            n_ija = T_ia = None
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
+                d = engine._to_dev
+                dev = forest.device
+                n1, T1 = engine.mutation_counts(forest, model, p64, 0, d(np.asarray(kk, np.int32), dev), pp,
+                                                d(np.asarray(pp_row, np.int64), dev), pc,
+                                                d(np.asarray(pc_row, np.int64), dev), self._gpu_precision())
+                n_ija = n1 if n_ija is None else n_ija + n1
+                T_ia = T1 if T_ia is None else T_ia + T1
+            return n_ija, T_ia
+        states = sess["bufs"].cache.get(("states", t.uint8))
+        if states is None:
+            raise ValueError("Ancestral sequences are not yet inferred")
+        ks = np.asarray([layout.local[id(n)] for n in nodes], np.int32)
+        tips_states = bool(self.reconstructed_tip_sequences)
+        return engine.mutation_counts_joint(forest, 0, engine._to_dev(ks, forest.device), states,
+                                            engine.char_state_table(self.gtr, strict=True), tips_states,
+                                            None if tips_states else self._tip_mismatch())
+
+    def infer_gtr(self, marginal=False, site_specific=False, normalized_rate=True, fixed_pi=None, pc=5.0,
+                  **kwargs):
+        """GTR inference (treetime/treeanc.py:1500-1632): the substitution
+        counts n_ija and times T_ia of all branches in one device launch, then
+        TreeTime's fixed-point fit of the model on the host (GTR.infer or
+        GTR_site_specific.infer)."""
+        from .gtr import GTR, GTR_site_specific
+        if site_specific and self.data.compress:
+            raise TypeError("TreeAnc.infer_gtr(): sequence compression and site specific GTR models are "
+                            "incompatible!")
+        if not self.ok:
+            raise MissingDataError("TreeAnc.infer_gtr: ERROR, sequences or tree are missing", 0)
+        if marginal and self.sequence_reconstruction != "marginal":
+            self._ml_anc_marginal(**kwargs)
+        elif not self.sequence_reconstruction:
+            self._ml_anc_joint(**kwargs)
+        self.logger("TreeAnc.infer_gtr: counting mutations...", 2)
+        n_ija, T_ia = self._substitution_counts(marginal)
+        self.logger("TreeAnc.infer_gtr: counting mutations...done", 3)
+        root = self.tree.root
+        if site_specific:
+            n_ija, T_ia = n_ija.cpu().numpy(), T_ia.cpu().numpy()
+            if marginal:
+                root_state = root.marginal_profile.T
+            else:
+                root_state = np.array([self.gtr.profile_map[c] for c in root.cseq]).T
+            self._gtr = GTR_site_specific.infer(n_ija, T_ia, pc=pc, root_state=root_state, logger=self.logger,
+                                                alphabet=self.gtr.alphabet, prof_map=self.gtr.profile_map)
+        else:
+            mult = self.data.multiplicity(mask=getattr(root, "mask", None))
+            root_state = np.array([np.sum((root.cseq == nuc) * mult) for nuc in self.gtr.alphabet])
+            self._gtr = GTR.infer(n_ija.sum(dim=-1).cpu().numpy(), T_ia.sum(dim=-1).cpu().numpy(), root_state,
+                                  fixed_pi=fixed_pi, pc=pc, alphabet=self.gtr.alphabet, logger=self.logger,
+                                  prof_map=self.gtr.profile_map)
+        if normalized_rate:
+            self.logger("TreeAnc.infer_gtr: setting overall rate to 1.0...", 2)
+            if site_specific:
+                self._gtr.mu /= self._gtr.average_rate().mean()
+            else:
+                self._gtr.mu = 1.0
+        return self._gtr
+
+    def infer_gtr_iterative(self, max_iter=10, site_specific=False, LHtol=0.1, pc=1.0, normalized_rate=False):
+        """Alternate GTR inference and marginal reconstruction until the
+        likelihood gain falls below LHtol (treetime/treeanc.py:1633-1676)."""
+        self.infer_ancestral_sequences(marginal=True)
+        old_p = np.copy(self.gtr.Pi)
+        old_LH = self.sequence_LH()
+        for i in range(max_iter):
+            self.infer_gtr(site_specific=site_specific, marginal=True, normalized_rate=normalized_rate, pc=pc)
+            self.infer_ancestral_sequences(marginal=True)
+            dp = np.abs(self.gtr.Pi - old_p).mean() if self.gtr.Pi.shape == old_p.shape else np.nan
+            deltaLH = self.sequence_LH() - old_LH
+            old_p = np.copy(self.gtr.Pi)
+            old_LH = self.sequence_LH()
+            self.logger("TreeAnc.infer_gtr_iterative: iteration %d, LH=%1.2f (%1.2f), deltaP=%1.4f"
+                        % (i, old_LH, deltaLH, dp), 2)
+            if deltaLH < LHtol:
+                self.logger("TreeAnc.infer_gtr_iterative: deltaLH=%f, stopping iteration." % deltaLH, 1)
+                break
+        return ttconf.SUCCESS
+
     def optimize_tree_marginal(self, max_iter=10, infer_gtr=False, pc=1.0, damping=0.75, LHtol=0.1,
                                site_specific_gtr=False, **kwargs):
         """treetime/treeanc.py:1297-1360, with the branches of an iteration
         optimised in one device pass."""
-        if infer_gtr:
-            parent = super()
-            if hasattr(parent, "optimize_tree_marginal"):
-                return parent.optimize_tree_marginal(max_iter=max_iter, infer_gtr=infer_gtr, pc=pc, damping=damping,
-                                                     LHtol=LHtol, site_specific_gtr=site_specific_gtr, **kwargs)
-            raise NotImplementedError("GTR inference is not part of the GPU hot path")
         self.infer_ancestral_sequences(marginal=True, **kwargs)
         oldLH = self.sequence_LH()
         for i in range(max_iter):
+            if infer_gtr:
+                self.infer_gtr(site_specific=site_specific_gtr, marginal=True, normalized_rate=True, pc=pc)
+                self.infer_ancestral_sequences(marginal=True, **kwargs)
             old_bl = self.tree.total_branch_length()
             tol = 1e-8 + 0.01 ** (i + 1)
             root = self.tree.root

@@ -262,12 +262,14 @@ def prob_t_pairs_batch(q, counts, model, t):
     return out.cpu().numpy()
 
 
-def char_state_table(gtr):
+def char_state_table(gtr, strict=False):
     """byte -> state index of the alphabet; TreeTime's state_pair leaves
     non-alphabet characters out for alphabets below 10 states and counts them
-    as state 1 for larger ones (treetime/gtr.py:674-707)."""
+    as state 1 for larger ones (treetime/gtr.py:674-707).  strict: every
+    non-alphabet character is 255 (GTR.state_index lookups, as in
+    TreeAnc.infer_gtr)."""
     tab = np.full(256, 255, dtype=np.uint8)
-    if len(gtr.alphabet) >= 10:
+    if len(gtr.alphabet) >= 10 and not strict:
         tab[:] = 1
     for i, c in enumerate(gtr.alphabet):
         tab[ord(str(c))] = i
@@ -881,6 +883,85 @@ def prob_t_pairs_grid(q, counts, model, d_grid, model_of=None):
         mo = model_of if hasattr(model_of, "data_ptr") else _to_dev(np.asarray(model_of, np.int32), counts.device)
     check(lib.tt_prob_t_pairs_grid(q, n, _p(counts), _p(mo), C.byref(model.struct), _p(d_grid), G, _p(out),
                                    _stream()), "tt_prob_t_pairs_grid")
+    return out
+
+
+_MUT_WS = {}
+
+
+def _mutation_workspace(dev, rows, P, n, threads_per_pattern):
+    """Device FP64 workspace of the counting kernels: one [rows][P] slice per
+    chunk of branches, as many chunks (<= 64) as fill the GPU; cached per
+    device and stream, grown when a call needs more."""
+    t = torch()
+    sms = _lib.load().tt_device_sm_count()
+    want = max(1, min(64, n, -(-(sms * 2048) // max(1, P * threads_per_pattern))))
+    need = want * rows * P
+    key = (str(dev), t.cuda.current_stream(dev).cuda_stream)
+    buf = _MUT_WS.get(key)
+    if buf is None or buf.numel() < need:
+        buf = t.empty(max(need, 1), dtype=t.float64, device=dev)
+        _MUT_WS[key] = buf
+    return buf, int(buf.numel() * 8)
+
+
+def mutation_counts(forest, model, p64, tree, d_node, pp, d_pp_row, pc, d_pc_row, precision):
+    """Substitution counts of the 'marginal' GTR inference over the listed
+    branches of one tree: (n_ija [q, q, P], T_ia [q, P]) device FP64
+    (treetime/treeanc.py:1546-1563)."""
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    q = forest.q
+    P = int(forest.trees_host["n_patterns"][tree])
+    n = int(d_node.numel())
+    n_ija = t.empty((q, q, P), dtype=t.float64, device=dev)
+    T_ia = t.empty((q, P), dtype=t.float64, device=dev)
+    ws, ws_bytes = _mutation_workspace(dev, 2 * q * q, P, n, 1 if q <= 5 else 32)
+    check(lib.tt_mutation_counts(C.byref(forest.struct), C.byref(model.struct), int(tree), P, n, _p(d_node), _p(pp),
+                                 _p(d_pp_row), _p(pc), _p(d_pc_row),
+                                 _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(p64), _p(n_ija),
+                                 _p(T_ia), _p(ws), ws_bytes, _stream()), "tt_mutation_counts")
+    return n_ija, T_ia
+
+
+def mutation_counts_joint(forest, tree, d_node, states, char_state, tips_use_states, tip_mismatch=None):
+    """Substitution counts of the 'joint' GTR inference from the states of the
+    last reconstruction: (n_ija [q, q, P], T_ia [q, P]) device FP64
+    (treetime/treeanc.py:1564-1582)."""
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    q = forest.q
+    P = int(forest.trees_host["n_patterns"][tree])
+    n = int(d_node.numel())
+    n_ija = t.empty((q, q, P), dtype=t.float64, device=dev)
+    T_ia = t.empty((q, P), dtype=t.float64, device=dev)
+    ws, ws_bytes = _mutation_workspace(dev, q * q + q, P, n, 1)
+    cs = _to_dev(np.asarray(char_state, np.uint8), dev)
+    mm = None if tip_mismatch is None else _to_dev(np.asarray(tip_mismatch, np.int32), dev)
+    check(lib.tt_mutation_counts_joint(C.byref(forest.struct), int(tree), P, n, _p(d_node), _p(states), _p(cs),
+                                       int(bool(tips_use_states)), _p(mm), _p(n_ija), _p(T_ia), _p(ws), ws_bytes,
+                                       _stream()), "tt_mutation_counts_joint")
+    return n_ija, T_ia
+
+
+def branch_mutation_matrix(forest, model, p64, tree, node, pp, pp_row, pc, pc_row, precision):
+    """[P, q, q] normalised joint distribution of the states at both ends of
+    one branch (treetime/treeanc.py:1085-1120)."""
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    q = forest.q
+    P = int(forest.trees_host["n_patterns"][tree])
+    out = t.empty((P, q, q), dtype=t.float64, device=dev)
+    d_node = _to_dev(np.array([node], np.int32), dev)
+    d_pp = _to_dev(np.array([pp_row], np.int64), dev)
+    d_pc = _to_dev(np.array([pc_row], np.int64), dev)
+    check(lib.tt_branch_mutation_matrix(C.byref(forest.struct), C.byref(model.struct), int(tree), P, _p(d_node),
+                                        _p(pp), _p(d_pp), _p(pc), _p(d_pc),
+                                        _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(p64),
+                                        _p(out), _stream()), "tt_branch_mutation_matrix")
     return out
 
 

@@ -149,6 +149,61 @@ class GTR:
         return gtr
 
     @classmethod
+    def infer(cls, nij, Ti, root_state, fixed_pi=None, pc=1.0, gap_limit=0.01, **kwargs):
+        """Fit mu, pi and W to substitution counts n_ij (i derived, j ancestral),
+        times T_i spent in each state and root state counts by TreeTime's fixed
+        point iteration of n_ij + pc = pi_i W_ij (T_j + pc + root_state)
+        (treetime/gtr.py:492-599): at most 40 rounds until |pi - pi_old| <= 1e-5,
+        then the gap frequency set to gap_limit.  Host work on q x q arrays; the
+        counts come from the GPU (TreeAnc.infer_gtr)."""
+        gtr = cls(**kwargs)
+        gtr.logger("GTR: model inference ", 1)
+        dp, n_iter_max = 1e-5, 40
+        nij = np.array(nij, dtype=float)
+        Ti = np.asarray(Ti, dtype=float)
+        pc_mat = pc * np.ones_like(nij)
+        np.fill_diagonal(pc_mat, 0.0)
+        np.fill_diagonal(nij, 0.0)
+        count = 0
+        pi_old = np.zeros_like(Ti)
+        pi = np.ones_like(Ti) if fixed_pi is None else np.copy(fixed_pi)
+        pi /= pi.sum()
+        W_ij = np.ones_like(nij)
+        mu = (nij.sum() + pc) / (Ti.sum() + pc)
+        while np.linalg.norm(pi_old - pi) > dp and count < n_iter_max:
+            gtr.logger(" ".join(map(str, ["GTR inference iteration", count, "change:",
+                                          np.linalg.norm(pi_old - pi)])), 3)
+            count += 1
+            pi_old = np.copy(pi)
+            W_ij = ((nij + nij.T + 2 * pc_mat) / mu
+                    / (np.outer(pi, Ti) + np.outer(Ti, pi) + ttconf.TINY_NUMBER + 2 * pc_mat))
+            np.fill_diagonal(W_ij, 0)
+            W_ij = W_ij / avg_transition(W_ij, pi, gap_index=gtr.gap_index)
+            if fixed_pi is None:
+                pi = (np.sum(nij + pc_mat, axis=1) + root_state) / (
+                    ttconf.TINY_NUMBER + mu * np.dot(W_ij, Ti) + root_state.sum() + np.sum(pc_mat, axis=1))
+                pi /= pi.sum()
+                mu = (nij.sum() + pc) / (np.sum(pi * (W_ij.dot(Ti))) + pc)
+            else:
+                mu = (nij.sum() + pc) / (np.sum(pi * (W_ij.dot(pi))) * Ti.sum() + pc)
+        if count >= n_iter_max:
+            gtr.logger("WARNING: maximum number of iterations has been reached in GTR inference", 3, warn=True)
+            if np.linalg.norm(pi_old - pi) > dp:
+                gtr.logger("the iterative scheme has not converged", 3, warn=True)
+            elif np.abs(1 - np.max(pi.sum(axis=0))) > dp:
+                gtr.logger("the iterative scheme has converged, but proper normalization was not reached", 3,
+                           warn=True)
+        if gtr.gap_index is not None:
+            if pi[gtr.gap_index] < gap_limit:
+                gtr.logger("The model allows for gaps which are estimated to occur at a low fraction of %1.3e"
+                           % pi[gtr.gap_index] + " this can potentially result in artificats."
+                           + " gap fraction will be set to %1.4f" % gap_limit, 2, warn=True)
+            pi[gtr.gap_index] = gap_limit
+            pi /= pi.sum()
+        gtr.assign_rates(mu=mu, W=W_ij, pi=pi)
+        return gtr
+
+    @classmethod
     def random(cls, mu=1.0, alphabet="nuc", rng=None):
         """Random model: pi and W uniform on [0,1) from ``rng`` in the order
         pi then W (treetime/gtr.py:463-489)."""
@@ -372,6 +427,57 @@ class GTR_site_specific(GTR):
         if self.Pi.shape[1] > 1:
             return np.einsum("a,ia,ij,ja->a", self.mu, self.Pi, self.W, self.Pi)
         return self.mu * np.einsum("ia,ij,ja->a", self.Pi, self.W, self.Pi)
+
+    @classmethod
+    def infer(cls, sub_ija, T_ia, root_state, pc=1.0, gap_limit=0.01, Nit=30, dp=1e-5, **kwargs):
+        """Per-site fit of pi_ia and mu_a with a shared W to per-site counts
+        n_ija and times T_ia (treetime/gtr_site_specific.py:208-310): at most
+        Nit rounds of the fixed point iteration until |p - p_old| <= dp, gap
+        frequencies set to gap_limit per site.  Host work; the counts come from
+        the GPU (TreeAnc.infer_gtr)."""
+        gtr = cls(**kwargs)
+        gtr.logger("GTR: model inference ", 1)
+        q = len(gtr.alphabet)
+        L = sub_ija.shape[-1]
+        n_iter = 0
+        n_ija = np.copy(sub_ija)
+        n_ija[range(q), range(q), :] = 0
+        n_ij = n_ija.sum(axis=-1)
+        m_ia = np.sum(n_ija, axis=1) + root_state + pc
+        n_a = n_ija.sum(axis=1).sum(axis=0) + pc
+        Lambda = np.sum(root_state, axis=0) + q * pc
+        p_ia_old = np.zeros((q, L))
+        p_ia = np.ones((q, L)) / q
+        mu_a = np.ones(L)
+        W_ij = np.ones((q, q)) - np.eye(q)
+        while (np.linalg.norm(p_ia_old - p_ia) > dp) and n_iter < Nit:
+            gtr.logger(" ".join(map(str, ["GTR inference iteration", n_iter, "change:",
+                                          np.linalg.norm(p_ia_old - p_ia)])), 3)
+            n_iter += 1
+            p_ia_old = np.copy(p_ia)
+            S_ij = np.einsum("a,ia,ja", mu_a, p_ia, T_ia)
+            W_ij = (n_ij + n_ij.T + pc) / (S_ij + S_ij.T + pc)
+            avg_pi = p_ia.mean(axis=-1)
+            average_rate = W_ij.dot(avg_pi).dot(avg_pi)
+            W_ij = W_ij / average_rate
+            mu_a *= average_rate
+            p_ia = m_ia / (mu_a * np.dot(W_ij, T_ia) + Lambda)
+            p_ia = p_ia / p_ia.sum(axis=0)
+            mu_a = n_a / (pc + np.einsum("ia,ij,ja->a", p_ia, W_ij, T_ia))
+        if n_iter >= Nit:
+            gtr.logger("WARNING: maximum number of iterations has been reached in GTR inference", 3, warn=True)
+            if np.linalg.norm(p_ia_old - p_ia) > dp:
+                gtr.logger("the iterative scheme has not converged", 3, warn=True)
+        if gtr.gap_index is not None:
+            for p in range(p_ia.shape[-1]):
+                if p_ia[gtr.gap_index, p] < gap_limit:
+                    gtr.logger("The model allows for gaps which are estimated to occur at a low fraction of %1.3e"
+                               % p_ia[gtr.gap_index, p] + "\n\t\tthis can potentially result in artifacts."
+                               + "\n\t\tgap fraction will be set to %1.4f" % gap_limit, 4, warn=True)
+                p_ia[gtr.gap_index, p] = gap_limit
+                p_ia[:, p] /= p_ia[:, p].sum()
+        gtr.assign_rates(mu=mu_a, W=W_ij, pi=p_ia)
+        return gtr
 
     @classmethod
     def random(cls, L=1, avg_mu=1.0, alphabet="nuc", pi_dirichlet_alpha=1, W_dirichlet_alpha=3.0,

@@ -20,8 +20,12 @@ states and likelihoods.  ``precision='f32'`` selects the FP32 power-of-two
 scaled kernels (FP64 per-pattern log-likelihoods); the default 'f64' follows
 TreeTime's FP64 log-domain arithmetic.
 
-Out of scope (raise NotImplementedError): Fitch parsimony, GTR inference,
-sparse (VCF) alignments.
+GTR inference (``infer_gtr``, ``infer_gtr_iterative``,
+``get_branch_mutation_matrix``) counts substitutions on the GPU and fits the
+model on the host as TreeTime does.
+
+Out of scope (raise NotImplementedError): Fitch parsimony, sparse (VCF)
+alignments.
 """
 
 import gc
@@ -300,7 +304,7 @@ class TreeAnc(GPUAncMixin):
             raise UnknownMethodError("Reconstruction method needs to be in ['ml', 'probabilistic', 'fitch', "
                                      "'parsimony'], got '{}'".format(method))
         if infer_gtr:
-            raise NotImplementedError("GTR inference is not part of the GPU hot path")
+            self.infer_gtr(marginal=marginal, **kwargs)
         return fn(reconstruct_tip_states=reconstruct_tip_states, **kwargs)
 
     # ------------------------------------------------------------ likelihoods

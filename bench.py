@@ -527,6 +527,118 @@ def run_blgrid(args):
     return out
 
 
+GTRINF_WORKLOAD = ("gtrinf: substitution counts of 'marginal' GTR inference (TreeAnc.infer_gtr) over every branch of "
+                   "the 2000-tip x 30000-site tree, from its FP32 reconstruction's profiles")
+GTRINF_METRIC = "branch-pattern mutation matrices/s (q x q joint state distribution of one pattern on one branch)"
+GTRINF_UNIT = "branch-patterns/s"
+
+
+def run_gtrinf(args):
+    """--workload gtrinf: the counting step of TreeAnc.infer_gtr(marginal=True)
+    -- per branch and pattern the normalised q x q joint distribution of the
+    states at both ends, summed into n_ija and T_ia -- for all branches: one
+    counting launch and one chunk-reduction launch per branch group (internal
+    nodes, tips); L2 flushed before every step."""
+    import torch
+    from treetime_gb300 import engine
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t, wl = build_workload()
+    t.device = dev
+    t.infer_ancestral_sequences(marginal=True)
+    sess = t._get_session()
+    forest = sess["forest"]
+    model = engine.model_for(t.gtr, dev)
+    nodes = t._counting_branches()
+    P, q, w = t.data.compressed_length, t.gtr.n_states, forest.w
+    units = len(nodes) * P
+    prec = t._gpu_precision()
+    engine.branch_pmats(forest, model, sess["bufs"])
+    p64 = sess["bufs"].cache[("p64", torch.float64)]
+    groups = []
+    for idx, kk, pp, pp_row, pc_row, pc in t._profile_branch_groups(nodes):
+        groups.append((engine._to_dev(np.asarray(kk, np.int32), dev), pp,
+                       engine._to_dev(np.asarray(pp_row, np.int64), dev), pc,
+                       engine._to_dev(np.asarray(pc_row, np.int64), dev), len(kk), pc_row[0] < 0))
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def step():
+        return [engine.mutation_counts(forest, model, p64, 0, dn, pp, dpr, pc, dcr, prec)
+                for dn, pp, dpr, pc, dcr, _, _ in groups]
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ts = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            step()
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+    ms = _reduce_max(sum(ts) / len(ts), dev, world)
+    e2e = []
+    for _ in range(max(3, min(args.steps, 20))):
+        t0 = time.perf_counter()
+        t._substitution_counts(True)[0].sum().item()
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = statistics.median(e2e) * 1e3
+    if rank != 0:
+        return None
+    # algorithmic bytes: each branch reads the two profile rows of every pattern (a tip's child
+    # row is its 1-byte code), the offset branch matrices are written once, the chunk slices are
+    # written and read back once, the counts written
+    sms = engine._lib.load().tt_device_sm_count()
+    ab = 0
+    es = 4 if prec == "f32" else 8
+    for _, _, _, _, _, nb, tips in groups:
+        ab += nb * P * (w * es + (1 if tips else w * es))
+        chunks = max(1, min(64, nb, -(-(sms * 2048) // P)))
+        ab += forest.n_nodes * q * (w * 8 + q * es) + 2 * chunks * (q * q + q) * P * 8 + (q * q + q) * P * 8
+    peak, peak_kind = _peaks()
+    achieved = ab / (ms * 1e-3) / 1e9
+    out = {
+        "metric": GTRINF_METRIC, "value": world * units / (ms * 1e-3), "unit": GTRINF_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == "f32" else "f64",
+        "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
+        "config": {"workload": GTRINF_WORKLOAD, "branches": len(nodes), "patterns": P, "profiles": prec,
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_kind, "algorithmic_bytes_per_step": ab,
+                     "note": "both groups' offset, counting and reduction launches per step"},
+        "e2e": {"value": units / (e2e_ms * 1e-3), "unit": GTRINF_UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(sum(g[5] * 20 for g in groups)),
+                "d2h_bytes_per_step": int((q * q + q) * P * 8)},
+        "gpu_launches": 3 * len(groups) * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import anc
+        mult = t.data.multiplicity()
+        L = t.data.full_length
+        done, secs = 0, 0.0
+        chosen = nodes[::max(1, len(nodes) // 2000)]
+        for n in chosen:
+            pp, pc = np.asarray(n.marginal_outgroup_LH, np.float64), np.asarray(n.marginal_subtree_LH, np.float64)
+            t0 = time.perf_counter()
+            mut = np.transpose(anc.branch_mutation_matrix(t.gtr, pp, pc, anc.branch_length_to_gtr(n, L)), (1, 2, 0))
+            _ = 0.5 * mut.sum(axis=0) * mult + 0.5 * mut.sum(axis=1) * mult, mut * mult
+            secs += time.perf_counter() - t0
+            done += P
+            if secs > 20.0:
+                break
+        out["cpu_baseline"] = {"value": done / secs, "unit": GTRINF_UNIT, "cores": 1, "kind": "port",
+                               "sample": "%d branches (every %d-th) through the numpy restatement of TreeTime's "
+                                         "counting step, 1 process" % (done // P, max(1, len(nodes) // 2000)),
+                               "seconds": secs}
+    return out
+
+
 C3_WORKLOAD = ("c3: 256 independent coalescent trees, tips log-uniform in [50, 5000], sites log-uniform in "
                "[1k, 30k], branch means log-uniform in [1e-4, 0.05], a random GTR per tree; the whole batch is "
                "one forest, one captured launch sequence per step")
@@ -906,7 +1018,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "blgrid"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
@@ -924,7 +1036,8 @@ def main():
     else:
         from treetime_gb300 import build
         build.build()
-        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4, "blgrid": run_blgrid}[args.workload](args)
+        res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4, "blgrid": run_blgrid,
+               "gtrinf": run_gtrinf}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

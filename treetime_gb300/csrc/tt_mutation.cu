@@ -3,7 +3,8 @@
 //
 // Marginal mode: per branch and pattern a the joint distribution of the states at both ends,
 // M[a,i,j] = pc[a,i] pp[a,j] (P(t)[i,j] + 1e-24) / sum_ij(...) (i child, j parent), summed over
-// branches as n_ija += M * mult and T_ia += 0.5 t (sum_i M[i,.] + sum_j M[.,j]) * mult.
+// branches as n_ija += M * mult and T_ia += 0.5 t (sum_i M[i,.] + sum_j M[.,j]) * mult; the row
+// and column sums come from R.pp and pc.R, so no q x q time-weighted matrix is kept.
 // Joint mode: per branch and pattern the parent/child states; a difference adds the number of
 // alignment positions of the pattern to n_ija[child, parent, a] and moves 0.5 t per position of
 // time from the child state to the parent state; every branch adds t * mult to T[child state].
@@ -53,18 +54,18 @@ __device__ __forceinline__ double ld(const void* base, int64_t idx) {
     return (double)reinterpret_cast<const T*>(base)[idx];
 }
 
-// profile value j of the parent side (pp) and child side (pc) of branch b at pattern p
+// profile value j of the parent side (pp) and child side (pc) of branch b at pattern p, for
+// get_branch_mutation_matrix
 struct BranchRows {
     const void* pp;
     const void* pc;
     int64_t ppo, pco;  // element offsets of the rows (pco < 0: tip, from its code)
     const double* lut;  // tip: profile row of the tip's character
-    double pcs;         // 1 / sum of the child row (FP32 partials are power-of-two scaled)
     bool f32;
     __device__ double parent(int j) const { return f32 ? ld<float>(pp, ppo + j) : ld<double>(pp, ppo + j); }
     __device__ double child(int i) const {
         if (lut) return lut[i];
-        return f32 ? ld<float>(pc, pco + i) * pcs : ld<double>(pc, pco + i);
+        return f32 ? ld<float>(pc, pco + i) : ld<double>(pc, pco + i);
     }
 };
 
@@ -76,7 +77,6 @@ __device__ __forceinline__ BranchRows branch_rows(const MutParams& a, const tt_t
     r.f32 = a.prec == TT_PREC_F32;
     r.ppo = (a.pp_row[b] + p) * w;
     r.lut = nullptr;
-    r.pcs = 1.0;
     if (a.pc_row[b] < 0) {
         const int64_t g = a.node_of[b];
         const int row = a.f.tip_row[g];
@@ -85,11 +85,6 @@ __device__ __forceinline__ BranchRows branch_rows(const MutParams& a, const tt_t
         r.pco = -1;
     } else {
         r.pco = (a.pc_row[b] + p) * w;
-        if (r.f32) {
-            double s = 0.0;
-            for (int i = 0; i < q; ++i) s += ld<float>(a.pc, r.pco + i);
-            r.pcs = 1.0 / s;
-        }
     }
     return r;
 }
@@ -103,59 +98,103 @@ __device__ __forceinline__ double branch_weight(const MutParams& a, const tt_tre
     return m;
 }
 
-// Marginal mode, q <= 5: one thread per (pattern, chunk), the q*q sums in registers.
-// Rows of the slice: [0, q*q) sum of M*mult, [q*q, 2*q*q) sum of 0.5*t*M*mult.
-template <int Q>
-__global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a) {
+// R[g][i][j] = P(t)_ij + 1e-24 for every node, in the counting kernels' arithmetic type.
+template <typename Tc>
+__global__ void mut_offset_kernel(const double* __restrict__ p64, int64_t n_nodes, int q, int w, Tc* __restrict__ R) {
+    const int qq = q * q;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n_nodes * qq;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = idx / qq;
+        const int e = (int)(idx - g * qq), i = e / q, j = e - (e / q) * q;
+        R[idx] = (Tc)(p64[g * q * w + (int64_t)i * w + j] + kSuperTiny);
+    }
+}
+
+// Marginal counting.  Per branch and pattern, with a = pc (child side; the normalisation of M
+// makes its scale irrelevant, so FP32 partials are used as stored), b = pp and R = P(t) + 1e-24:
+// Rb = R.b, aR = a.R, tot = a.Rb, c = mult*mask / tot; then n_ij += c a_i b_j R_ij and
+// T_k += 0.5 t c (b_k aR_k + a_k Rb_k) (the row and column sums of the normalised M).  Tc is the
+// arithmetic type: double for FP64 profiles, float for FP32 profiles (sums over a chunk of at
+// most a few dozen branches; the chunk sums are added in FP64).
+// Rows of the chunk slice: [0, q*q) n, [q*q, q*q + q) T.
+
+// q <= 5: one thread per (pattern, chunk), all sums in registers.
+template <int Q, typename Tin, typename Tc>
+__global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a, const Tc* __restrict__ R) {
     const tt_tree tr = a.f.trees[a.tree];
     const int P = a.P;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     if (p >= P) return;
     const int w = a.f.width;
-    double N[Q * Q], S[Q * Q];
+    const Tin* pp = reinterpret_cast<const Tin*>(a.pp);
+    const Tin* pc = reinterpret_cast<const Tin*>(a.pc);
+    Tc N[Q * Q], T[Q];
 #pragma unroll
-    for (int e = 0; e < Q * Q; ++e) N[e] = S[e] = 0.0;
+    for (int e = 0; e < Q * Q; ++e) N[e] = Tc(0);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) T[k] = Tc(0);
     const int64_t b0 = c * a.chunk_len;
     const int64_t b1 = b0 + a.chunk_len < a.n ? b0 + a.chunk_len : a.n;
     for (int64_t b = b0; b < b1; ++b) {
         const int64_t g = a.node_of[b];
-        const BranchRows r = branch_rows(a, tr, b, p);
-        double pcv[Q], ppv[Q];
+        const int64_t pcr = a.pc_row[b];
+        Tc av[Q], bv[Q];
+        const Tin* prow = pp + (a.pp_row[b] + p) * w;
+#pragma unroll
+        for (int j = 0; j < Q; ++j) bv[j] = (Tc)prow[j];
+        if (pcr < 0) {
+            const int row = a.f.tip_row[g];
+            const int code = row < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)row * tr.n_patterns + p];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) av[i] = (Tc)a.m.lut[code * Q + i];
+        } else {
+            const Tin* crow = pc + (pcr + p) * w;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) av[i] = (Tc)crow[i];
+        }
+        const Tc* Rg = R + g * Q * Q;
+        Tc Rm[Q * Q];
+#pragma unroll
+        for (int e = 0; e < Q * Q; ++e) Rm[e] = __ldg(Rg + e);
+        Tc Rb[Q], aR[Q], tot = Tc(0);
 #pragma unroll
         for (int i = 0; i < Q; ++i) {
-            pcv[i] = r.child(i);
-            ppv[i] = r.parent(i);
+            Tc s = Tc(0);
+#pragma unroll
+            for (int j = 0; j < Q; ++j) s = fma(Rm[i * Q + j], bv[j], s);
+            Rb[i] = s;
+            tot = fma(av[i], s, tot);
         }
-        const double* Pm = a.p64 + g * Q * w;
-        double M[Q * Q], tot = 0.0;
 #pragma unroll
-        for (int i = 0; i < Q; ++i)
+        for (int j = 0; j < Q; ++j) {
+            Tc s = Tc(0);
 #pragma unroll
-            for (int j = 0; j < Q; ++j) {
-                M[i * Q + j] = pcv[i] * ppv[j] * (__ldg(Pm + i * w + j) + kSuperTiny);
-                tot += M[i * Q + j];
-            }
-        const double mw = branch_weight(a, tr, g, p);
-        const double wn = mw / tot, ws = 0.5 * a.f.bl[g] * mw / tot;
-#pragma unroll
-        for (int e = 0; e < Q * Q; ++e) {
-            N[e] = fma(M[e], wn, N[e]);
-            S[e] = fma(M[e], ws, S[e]);
+            for (int i = 0; i < Q; ++i) s = fma(av[i], Rm[i * Q + j], s);
+            aR[j] = s;
         }
+        const Tc cw = (Tc)branch_weight(a, tr, g, p) / tot;
+        const Tc h = (Tc)(0.5 * a.f.bl[g]) * cw;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const Tc cai = cw * av[i];
+#pragma unroll
+            for (int j = 0; j < Q; ++j) N[i * Q + j] = fma(cai * bv[j], Rm[i * Q + j], N[i * Q + j]);
+        }
+#pragma unroll
+        for (int k = 0; k < Q; ++k) T[k] = fma(h, fma(av[k], Rb[k], bv[k] * aR[k]), T[k]);
     }
     double* out = a.part + (int64_t)c * a.rows * P;
 #pragma unroll
-    for (int e = 0; e < Q * Q; ++e) {
-        out[(int64_t)e * P + p] = N[e];
-        out[(int64_t)(Q * Q + e) * P + p] = S[e];
-    }
+    for (int e = 0; e < Q * Q; ++e) out[(int64_t)e * P + p] = (double)N[e];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) out[(int64_t)(Q * Q + k) * P + p] = (double)T[k];
 }
 
-// Marginal mode, larger alphabets: one warp per (pattern, chunk); lane l holds the entries
-// e = l, l + 32, ... of the q*q matrix.
-template <int EPL>
-__global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a) {
+// Larger alphabets: one warp per (pattern, chunk); lane l < q holds a_l, b_l, (R.b)_l, (a.R)_l and
+// T_l, and the matrix entries e = l, l + 32, ... of n.
+template <int EPL, typename Tin, typename Tc>
+__global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a, const Tc* __restrict__ R) {
     const tt_tree tr = a.f.trees[a.tree];
     const int P = a.P;
     const int lane = threadIdx.x & 31;
@@ -163,45 +202,64 @@ __global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a) {
     const int c = blockIdx.y;
     if (p >= P) return;
     const int q = a.f.n_states, w = a.f.width, qq = q * q;
-    double N[EPL], S[EPL];
+    const Tin* pp = reinterpret_cast<const Tin*>(a.pp);
+    const Tin* pc = reinterpret_cast<const Tin*>(a.pc);
+    int ei[EPL], ej[EPL];
 #pragma unroll
-    for (int r = 0; r < EPL; ++r) N[r] = S[r] = 0.0;
+    for (int r = 0; r < EPL; ++r) {
+        const int e = lane + 32 * r;
+        ei[r] = e < qq ? e / q : 0;
+        ej[r] = e < qq ? e - (e / q) * q : 0;
+    }
+    Tc N[EPL], T = Tc(0);
+#pragma unroll
+    for (int r = 0; r < EPL; ++r) N[r] = Tc(0);
     const int64_t b0 = c * a.chunk_len;
     const int64_t b1 = b0 + a.chunk_len < a.n ? b0 + a.chunk_len : a.n;
     for (int64_t b = b0; b < b1; ++b) {
         const int64_t g = a.node_of[b];
-        const BranchRows rw = branch_rows(a, tr, b, p);
-        const double pcl = lane < q ? rw.child(lane) : 0.0;
-        const double ppl = lane < q ? rw.parent(lane) : 0.0;
-        const double* Pm = a.p64 + g * q * w;
-        double M[EPL], tot = 0.0;
+        const int64_t pcr = a.pc_row[b];
+        Tc al = Tc(0), bl = Tc(0);
+        if (lane < q) {
+            bl = (Tc)pp[(a.pp_row[b] + p) * w + lane];
+            if (pcr < 0) {
+                const int row = a.f.tip_row[g];
+                const int code = row < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)row * tr.n_patterns + p];
+                al = (Tc)a.m.lut[code * q + lane];
+            } else {
+                al = (Tc)pc[(pcr + p) * w + lane];
+            }
+        }
+        const Tc* Rg = R + g * qq;
+        Tc Rb = Tc(0), aR = Tc(0);
+        for (int k = 0; k < q; ++k) {
+            const Tc bk = __shfl_sync(0xffffffffu, bl, k);
+            const Tc ak = __shfl_sync(0xffffffffu, al, k);
+            if (lane < q) {
+                Rb = fma(__ldg(Rg + lane * q + k), bk, Rb);
+                aR = fma(ak, __ldg(Rg + k * q + lane), aR);
+            }
+        }
+        Tc tot = al * Rb;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, off);
+        const Tc cw = (Tc)branch_weight(a, tr, g, p) / tot;
+        const Tc cal = cw * al;
 #pragma unroll
         for (int r = 0; r < EPL; ++r) {
-            const int e = lane + 32 * r;
-            const int i = e < qq ? e / q : 0, j = e < qq ? e - (e / q) * q : 0;
-            const double ci = __shfl_sync(0xffffffffu, pcl, i);
-            const double pj = __shfl_sync(0xffffffffu, ppl, j);
-            M[r] = e < qq ? ci * pj * (__ldg(Pm + i * w + j) + kSuperTiny) : 0.0;
-            tot += M[r];
+            const Tc ci = __shfl_sync(0xffffffffu, cal, ei[r]);
+            const Tc bj = __shfl_sync(0xffffffffu, bl, ej[r]);
+            if (lane + 32 * r < qq) N[r] = fma(ci * bj, __ldg(Rg + ei[r] * q + ej[r]), N[r]);
         }
-        tot = warp_total(tot);
-        const double mw = branch_weight(a, tr, g, p);
-        const double wn = mw / tot, ws = 0.5 * a.f.bl[g] * mw / tot;
-#pragma unroll
-        for (int r = 0; r < EPL; ++r) {
-            N[r] = fma(M[r], wn, N[r]);
-            S[r] = fma(M[r], ws, S[r]);
-        }
+        T = fma((Tc)(0.5 * a.f.bl[g]) * cw, fma(al, Rb, bl * aR), T);
     }
     double* out = a.part + (int64_t)c * a.rows * P;
 #pragma unroll
     for (int r = 0; r < EPL; ++r) {
         const int e = lane + 32 * r;
-        if (e < qq) {
-            out[(int64_t)e * P + p] = N[r];
-            out[(int64_t)(qq + e) * P + p] = S[r];
-        }
+        if (e < qq) out[(int64_t)e * P + p] = (double)N[r];
     }
+    if (lane < q) out[(int64_t)(qq + lane) * P + p] = (double)T;
 }
 
 // Joint mode: one thread per (pattern, chunk); updates are sparse (one matrix entry per branch),
@@ -253,33 +311,18 @@ __global__ void __launch_bounds__(256) mut_joint_kernel(MutParams a) {
     }
 }
 
-// Sum of the chunk slices in chunk order; marginal mode turns the time-weighted matrix S into
-// T[k] = sum_i S[i][k] + sum_j S[k][j].
-__global__ void mut_reduce_kernel(const double* __restrict__ part, int chunks, int rows, int P, int q, int marginal,
+// Sum of the chunk slices in chunk order: n_ija from rows [0, q*q), T_ia from rows [q*q, q*q + q).
+__global__ void mut_reduce_kernel(const double* __restrict__ part, int chunks, int rows, int P, int q,
                                   double* __restrict__ n_ija, double* __restrict__ T_ia) {
     const int qq = q * q;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)rows * P;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int r = (int)(idx / P);
         const int p = (int)(idx - (int64_t)r * P);
-        if (r < qq) {
-            double s = 0.0;
-            for (int c = 0; c < chunks; ++c) s += part[((int64_t)c * rows + r) * P + p];
-            n_ija[(int64_t)r * P + p] = s;
-        } else if (!marginal) {
-            double s = 0.0;
-            for (int c = 0; c < chunks; ++c) s += part[((int64_t)c * rows + r) * P + p];
-            T_ia[(int64_t)(r - qq) * P + p] = s;
-        } else if (r < qq + q) {
-            const int kk = r - qq;
-            double s = 0.0;
-            for (int c = 0; c < chunks; ++c) {
-                const double* S = part + ((int64_t)c * rows + qq) * P + p;
-                for (int i = 0; i < q; ++i) s += S[(int64_t)(i * q + kk) * P];
-                for (int j = 0; j < q; ++j) s += S[(int64_t)(kk * q + j) * P];
-            }
-            T_ia[(int64_t)kk * P + p] = s;
-        }
+        double s = 0.0;
+        for (int c = 0; c < chunks; ++c) s += part[((int64_t)c * rows + r) * P + p];
+        if (r < qq) n_ija[(int64_t)r * P + p] = s;
+        else T_ia[(int64_t)(r - qq) * P + p] = s;
     }
 }
 
@@ -332,24 +375,27 @@ int want_chunks(int64_t n, int P, int threads_per_pattern) {
 using namespace tt;
 
 extern "C" tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, int32_t tree, int32_t n_patterns,
-                                        int64_t n,
-                                        const int32_t* node_of, const void* pp, const int64_t* pp_row,
+                                        int64_t n, const int32_t* node_of, const void* pp, const int64_t* pp_row,
                                         const void* pc, const int64_t* pc_row, int32_t prec, const double* p64,
                                         double* n_ija, double* T_ia, double* workspace, int64_t workspace_bytes,
                                         void* stream) {
     if (!valid_tree(f, tree) || !m || n < 0 || n_patterns < 0 || !p64 || !n_ija || !T_ia || f->n_states < 2 ||
-        f->n_states > 32 ||
-        (n > 0 && (!node_of || !pp || !pp_row || !pc_row))) {
+        f->n_states > 32 || (n > 0 && (!node_of || !pp || !pp_row || !pc_row))) {
         set_error("tt_mutation_counts: invalid arguments");
         return TT_ERR_INVALID;
     }
     const int q = f->n_states, P = n_patterns;
     if (P == 0) return TT_OK;
-    const int rows = 2 * q * q;
+    const bool f32 = prec == TT_PREC_F32;
+    const int rows = q * q + q;
     const bool small = q <= 5;
-    int chunks = fit_chunks(workspace_bytes, rows, P, want_chunks(n > 0 ? n : 1, P, small ? 1 : 32));
-    if (!workspace || chunks < 1) {
-        set_error("tt_mutation_counts: workspace smaller than 2*q*q*patterns doubles");
+    // workspace: the offset branch matrices R, then the chunk slices
+    const int64_t r_bytes = ((f->n_nodes * q * q * (f32 ? 4 : 8) + 255) / 256) * 256;
+    const int chunks = workspace && workspace_bytes > r_bytes
+                           ? fit_chunks(workspace_bytes - r_bytes, rows, P, want_chunks(n > 0 ? n : 1, P, small ? 1 : 32))
+                           : 0;
+    if (chunks < 1) {
+        set_error("tt_mutation_counts: workspace smaller than n_nodes*q*q + (q*q+q)*patterns doubles");
         return TT_ERR_OOM;
     }
     MutParams a{};
@@ -365,38 +411,53 @@ extern "C" tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, i
     a.pc_row = pc_row;
     a.prec = prec;
     a.p64 = p64;
-    a.part = workspace;
+    a.part = reinterpret_cast<double*>(reinterpret_cast<char*>(workspace) + r_bytes);
     a.rows = rows;
     a.chunks = chunks;
     a.chunk_len = n > 0 ? (n + chunks - 1) / chunks : 0;
     cudaStream_t s = as_stream(stream);
     if (n > 0) {
+        const int64_t rn = f->n_nodes * q * q;
+        int rblocks = (int)((rn + 255) / 256);
+        if (rblocks > sm_count() * 8) rblocks = sm_count() * 8;
+        float* R32 = reinterpret_cast<float*>(workspace);
+        double* R64 = workspace;
+        if (f32) mut_offset_kernel<float><<<rblocks, 256, 0, s>>>(p64, f->n_nodes, q, f->width, R32);
+        else mut_offset_kernel<double><<<rblocks, 256, 0, s>>>(p64, f->n_nodes, q, f->width, R64);
         if (small) {
             dim3 grid((P + 255) / 256, chunks);
+#define TT_MUT_SMALL(QV)                                                                                    \
+    if (f32) mut_marginal_small_kernel<QV, float, float><<<grid, 256, 0, s>>>(a, R32);                     \
+    else mut_marginal_small_kernel<QV, double, double><<<grid, 256, 0, s>>>(a, R64);
             switch (q) {
-                case 2: mut_marginal_small_kernel<2><<<grid, 256, 0, s>>>(a); break;
-                case 3: mut_marginal_small_kernel<3><<<grid, 256, 0, s>>>(a); break;
-                case 4: mut_marginal_small_kernel<4><<<grid, 256, 0, s>>>(a); break;
-                default: mut_marginal_small_kernel<5><<<grid, 256, 0, s>>>(a); break;
+                case 2: TT_MUT_SMALL(2) break;
+                case 3: TT_MUT_SMALL(3) break;
+                case 4: TT_MUT_SMALL(4) break;
+                default: TT_MUT_SMALL(5) break;
             }
+#undef TT_MUT_SMALL
         } else {
             dim3 grid((P + 7) / 8, chunks);
             const int epl = (q * q + 31) / 32;
-            if (epl <= 4) mut_marginal_warp_kernel<4><<<grid, 256, 0, s>>>(a);
-            else if (epl <= 8) mut_marginal_warp_kernel<8><<<grid, 256, 0, s>>>(a);
-            else if (epl <= 16) mut_marginal_warp_kernel<16><<<grid, 256, 0, s>>>(a);
-            else mut_marginal_warp_kernel<32><<<grid, 256, 0, s>>>(a);
+#define TT_MUT_WARP(E)                                                                                      \
+    if (f32) mut_marginal_warp_kernel<E, float, float><<<grid, 256, 0, s>>>(a, R32);                        \
+    else mut_marginal_warp_kernel<E, double, double><<<grid, 256, 0, s>>>(a, R64);
+            if (epl <= 4) { TT_MUT_WARP(4) }
+            else if (epl <= 8) { TT_MUT_WARP(8) }
+            else if (epl <= 16) { TT_MUT_WARP(16) }
+            else { TT_MUT_WARP(32) }
+#undef TT_MUT_WARP
         }
         tt_status st = check_launch("tt_mutation_counts");
         if (st != TT_OK) return st;
     } else {
-        cudaMemsetAsync(workspace, 0, (size_t)rows * P * sizeof(double), s);
+        cudaMemsetAsync(a.part, 0, (size_t)rows * P * sizeof(double), s);
         a.chunks = 1;
     }
     const int64_t total = (int64_t)rows * P;
     int blocks = (int)((total + 255) / 256);
     if (blocks > sm_count() * 16) blocks = sm_count() * 16;
-    mut_reduce_kernel<<<blocks, 256, 0, s>>>(workspace, a.chunks, rows, P, q, 1, n_ija, T_ia);
+    mut_reduce_kernel<<<blocks, 256, 0, s>>>(a.part, a.chunks, rows, P, q, n_ija, T_ia);
     return check_launch("tt_mutation_counts (reduce)");
 }
 
@@ -447,7 +508,7 @@ extern "C" tt_status tt_mutation_counts_joint(const tt_forest* f, int32_t tree, 
     const int64_t total = (int64_t)rows * P;
     int blocks = (int)((total + 255) / 256);
     if (blocks > sm_count() * 16) blocks = sm_count() * 16;
-    mut_reduce_kernel<<<blocks, 256, 0, s>>>(workspace, a.chunks, rows, P, q, 0, n_ija, T_ia);
+    mut_reduce_kernel<<<blocks, 256, 0, s>>>(workspace, a.chunks, rows, P, q, n_ija, T_ia);
     return check_launch("tt_mutation_counts_joint (reduce)");
 }
 

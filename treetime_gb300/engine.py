@@ -889,14 +889,15 @@ def prob_t_pairs_grid(q, counts, model, d_grid, model_of=None):
 _MUT_WS = {}
 
 
-def _mutation_workspace(dev, rows, P, n, threads_per_pattern):
-    """Device FP64 workspace of the counting kernels: one [rows][P] slice per
+def _mutation_workspace(dev, rows, P, n, threads_per_pattern, extra_bytes=0):
+    """Device FP64 workspace of the counting kernels: `extra_bytes` (rounded
+    up to 256) for the offset branch matrices, then one [rows][P] slice per
     chunk of branches, as many chunks (<= 64) as fill the GPU; cached per
     device and stream, grown when a call needs more."""
     t = torch()
     sms = _lib.load().tt_device_sm_count()
     want = max(1, min(64, n, -(-(sms * 2048) // max(1, P * threads_per_pattern))))
-    need = want * rows * P
+    need = want * rows * P + -(-extra_bytes // 256) * 32
     key = (str(dev), t.cuda.current_stream(dev).cuda_stream)
     buf = _MUT_WS.get(key)
     if buf is None or buf.numel() < need:
@@ -917,7 +918,8 @@ def mutation_counts(forest, model, p64, tree, d_node, pp, d_pp_row, pc, d_pc_row
     n = int(d_node.numel())
     n_ija = t.empty((q, q, P), dtype=t.float64, device=dev)
     T_ia = t.empty((q, P), dtype=t.float64, device=dev)
-    ws, ws_bytes = _mutation_workspace(dev, 2 * q * q, P, n, 1 if q <= 5 else 32)
+    ws, ws_bytes = _mutation_workspace(dev, q * q + q, P, n, 1 if q <= 5 else 32,
+                                       extra_bytes=forest.n_nodes * q * q * (4 if precision == "f32" else 8))
     check(lib.tt_mutation_counts(C.byref(forest.struct), C.byref(model.struct), int(tree), P, n, _p(d_node), _p(pp),
                                  _p(d_pp_row), _p(pc), _p(d_pc_row),
                                  _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(p64), _p(n_ija),

@@ -402,21 +402,23 @@ BLGRID_METRIC = "branch-length grid evaluations/s (log P of one pattern at one g
 BLGRID_UNIT = "evaluations/s"
 
 
-def _fp64_fma_rate(engine, dev):
-    """Measured FP64 FMA issue rate of this GPU (FMAs/s), from the library's
-    probe kernel: best of 3 launches of SMs x 8 CTAs x 256 threads x 8
-    independent chains x 4096 FMAs, CUDA events on the launching stream."""
+def _fma_rate(engine, dev, prec="f64"):
+    """Measured FMA issue rate of this GPU (FMAs/s, FP64 or FP32), from the
+    library's probe kernel: best of 3 launches of SMs x 8 CTAs x 256 threads x
+    8 independent chains x `iters` FMAs, CUDA events on the launching stream."""
     import torch
     lib = engine._lib.load()
     blocks = int(lib.tt_device_sm_count()) * 8
-    sink = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
-    iters = 4096
-    engine.check(lib.tt_fp64_fma_probe(64, blocks, engine._p(sink), engine._stream()), "tt_fp64_fma_probe")
+    f32 = prec == "f32"
+    sink = torch.empty(blocks * 256, dtype=torch.float32 if f32 else torch.float64, device=dev)
+    iters = 4096 * (32 if f32 else 1)
+    pr = engine._lib.TT_PREC_F32 if f32 else engine._lib.TT_PREC_F64
+    engine.check(lib.tt_fma_probe(64, blocks, pr, engine._p(sink), engine._stream()), "tt_fma_probe")
     best = float("inf")
     for _ in range(3):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        engine.check(lib.tt_fp64_fma_probe(iters, blocks, engine._p(sink), engine._stream()), "tt_fp64_fma_probe")
+        engine.check(lib.tt_fma_probe(iters, blocks, pr, engine._p(sink), engine._stream()), "tt_fma_probe")
         b.record()
         b.synchronize()
         best = min(best, a.elapsed_time(b))
@@ -477,26 +479,74 @@ def run_blgrid(args):
         res = t.branch_length_grids(nodes)
         e2e.append(time.perf_counter() - t0)
     e2e_ms = statistics.median(e2e) * 1e3
-    fma_rate = _fp64_fma_rate(engine, dev)
+    f32_kernel = prec == "f32" and q <= 5
+    # the FP64 kernel on the profiles of an FP64 reconstruction of the same tree, beside it
+    fp64 = None
+    if f32_kernel:
+        from treetime_gb300 import TreeAnc
+        from treetime_gb300.tree import parse_newick, to_newick
+        # its own copy of the tree: the nodes of `t` keep their FP32 results
+        t64 = TreeAnc(tree=parse_newick(to_newick(t.tree)), aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision="f64",
+                      device=dev)
+        t64.infer_ancestral_sequences(marginal=True)
+        n64 = [n for n in t64.tree.find_clades() if n.up is not None]
+        t64.branch_length_grids(n64)
+        torch.cuda.synchronize()
+        k64 = []
+        for _ in range(3):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            t64.branch_length_grids(n64)
+            b.record()
+            b.synchronize()
+            k64.append(a.elapsed_time(b))
+        ms64 = min(k64)
+        r64 = _fma_rate(engine, dev, "f64")
+        # accuracy of the FP32 path (FP32 reconstruction, FP32 grid kernel) against the FP64 path
+        g64 = {n.name: v for n, v in t64.branch_length_grids(n64).items()}
+        dabs = max(float(np.max(np.abs(res[n][1] - g64[n.name][1]))) for n in nodes)
+        drel = max(float(np.max(np.abs(res[n][1] - g64[n.name][1]) / np.maximum(np.abs(g64[n.name][1]), 1.0)))
+                   for n in nodes)
+        # FP64 instructions per evaluation: q FMAs of the eigen sum, 1 add of the 1e-24 floor, the
+        # table log (1 subtract for the reduced argument, 1 multiply by 1/F, 6 polynomial FMAs, 2 FMAs
+        # to assemble) and 1 FMA to accumulate weight * log: q + 12
+        fp64 = {"ms_per_step": ms64, "value": evals / (ms64 * 1e-3),
+                "note": "FP64 kernel (eigenbasis sums, table-driven FP64 log) on an FP64 reconstruction's "
+                        "profiles, timed through TreeAnc.branch_length_grids (host grids and copies included)",
+                "roofline": {"bound": "fp64", "achieved": evals * (q + 12) / (ms64 * 1e-3) / 1e12,
+                             "peak": r64 / 1e12, "unit": "T FP64 instructions/s",
+                             "frac": evals * (q + 12) / (ms64 * 1e-3) / r64},
+                "f32_path_vs_f64_path": {"max_abs_diff": dabs, "max_rel_diff": drel,
+                                         "note": "-log P on every grid point of every branch; relative to "
+                                                 "max(|value|, 1)"}}
     if rank != 0:
         return None
-    # FP64 instructions per evaluation: q FMAs of the eigen sum, 1 add of the 1e-24 floor, the table log
-    # (1 subtract for the reduced argument, 1 multiply by 1/F, 6 polynomial FMAs, 2 FMAs to assemble)
-    # and 1 FMA to accumulate weight * log: q + 12
-    ops = evals * (q + 12)
-    achieved = ops / (ms * 1e-3)
+    if f32_kernel:
+        # FP32 arithmetic per evaluation: q*q + q FMAs of pc.P(t).pp, the 1e-24 offset, the weight
+        # multiply, 4 of the compensated sum and one logf (counted as one operation)
+        opq = q * q + q + 7
+        rate = _fma_rate(engine, dev, "f32")
+        roof = {"bound": "fp32", "achieved": evals * opq / (ms * 1e-3) / 1e12, "peak": rate / 1e12,
+                "unit": "T FP32 operations/s", "frac": evals * opq / (ms * 1e-3) / rate, "traffic": None,
+                "peak_source": "measured live (FP32 FMA probe kernel)", "ops_per_evaluation": opq,
+                "kernel": "prob_t_profiles_grid_f32_kernel<%d>" % q}
+    else:
+        rate = _fma_rate(engine, dev, "f64")
+        roof = {"bound": "fp64", "achieved": evals * (q + 12) / (ms * 1e-3) / 1e12, "peak": rate / 1e12,
+                "unit": "T FP64 instructions/s", "frac": evals * (q + 12) / (ms * 1e-3) / rate, "traffic": None,
+                "peak_source": "measured live (FP64 FMA probe kernel)", "ops_per_evaluation": q + 12,
+                "kernel": "prob_t_profiles_grid_kernel<%d>" % q}
     out = {
         "metric": BLGRID_METRIC, "value": world * evals / (ms * 1e-3), "unit": BLGRID_UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if f32_kernel else "f64",
         "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
         "config": {"workload": BLGRID_WORKLOAD, "branches": len(nodes), "patterns": P,
                    "grid_points": int(lengths.sum()), "evaluations_per_step": evals, "profiles": prec,
                    "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU"},
-        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fma_rate / 1e12,
-                     "unit": "T FP64 instructions/s", "frac": achieved / fma_rate, "traffic": None,
-                     "peak_source": "measured live (FP64 FMA probe kernel)",
-                     "ops_per_evaluation": q + 12},
+        "roofline": roof,
+        "fp64_kernel": fp64,
         "e2e": {"value": evals / (e2e_ms * 1e-3), "unit": BLGRID_UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(padded.nbytes + sum(len(g[6]) * 20 for g in groups)),
                 "d2h_bytes_per_step": int(padded.nbytes)},
@@ -508,7 +558,7 @@ def run_blgrid(args):
         from oracle import anc
         mult = t.data.multiplicity()
         chosen = nodes[::max(1, len(nodes) // 400)]
-        errs, done, secs = [], 0, 0.0
+        errs, aerrs, done, secs = [], [], 0, 0.0
         for n in chosen:
             grid, y = res[n]
             pp, pc = np.asarray(n.marginal_outgroup_LH, np.float64), np.asarray(n.marginal_subtree_LH, np.float64)
@@ -517,6 +567,7 @@ def run_blgrid(args):
             secs += time.perf_counter() - t0
             done += len(grid) * P
             errs.append(float(np.max(np.abs(y - want) / np.maximum(np.abs(want), 1.0))))
+            aerrs.append(float(np.max(np.abs(y - want))))
             if secs > 20.0:
                 break
         out["cpu_baseline"] = {"value": done / secs, "unit": BLGRID_UNIT, "cores": 1, "kind": "port",
@@ -524,6 +575,7 @@ def run_blgrid(args):
                                          "TreeTime's BranchLenInterpolator evaluation, 1 process"
                                          % (len(errs), max(1, len(nodes) // 400)), "seconds": secs}
         out["max_rel_err_vs_oracle"] = max(errs)
+        out["max_abs_err_vs_oracle"] = max(aerrs)
     return out
 
 

@@ -195,10 +195,11 @@ const char* tt_status_string(tt_status s);
 size_t      tt_last_error(char* buf, size_t n);
 /* Number of streaming multiprocessors of the current device (host query, no launch). */
 int32_t     tt_device_sm_count(void);
-/* FP64 FMA throughput probe (measurement of the FP64 roofline of the branch-length kernels):
- * `blocks` CTAs of 256 threads, each thread 8 independent chains of `iters` FMAs; writes one
- * double per thread to sink[blocks * 256].  FMAs issued: blocks * 256 * 8 * iters. */
-tt_status   tt_fp64_fma_probe(int64_t iters, int32_t blocks, double* sink, void* stream);
+/* FMA throughput probe (measurement of the FP64 / FP32 rooflines of the branch-length kernels):
+ * `blocks` CTAs of 256 threads, each thread 8 independent chains of `iters` FMAs in FP64
+ * (prec = TT_PREC_F64) or FP32 (TT_PREC_F32); writes one value per thread to sink[blocks * 256].
+ * FMAs issued: blocks * 256 * 8 * iters. */
+tt_status   tt_fma_probe(int64_t iters, int32_t blocks, int32_t prec, void* sink, void* stream);
 
 /* -------------------------------------------------------------- a4: P(t)
  * P(t) for the branch above every node of the forest (FP64 + optional FP32 / log copies).

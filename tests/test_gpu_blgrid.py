@@ -4,7 +4,7 @@ grids and values (golden fixtures) and the CPU oracle.
 
 Tolerances: grids bit-exact (host-built); -log P on the grid 1e-9 relative +
 1e-8 absolute from FP64 profiles / pair counts, 1e-4 relative + 1e-3
-absolute from FP32-scaled profiles.  'joint' values are compared with
+absolute from FP32-scaled profiles (FP32 arithmetic for up to 5 states).  'joint' values are compared with
 TreeTime's at the grid points where every observed state pair has
 P(t) >= 1e-6; below that (t near 0) TreeTime's value is set by the rounding
 of V diag(exp(Qt)) V^-1, and the kernel's (formed with expm1) is compared
@@ -63,12 +63,14 @@ def _masked_tree(g, precision, rng):
     return t, masks
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
 @pytest.mark.parametrize("case", CASES)
-def test_branch_length_grids_with_masks_match_oracle(case):
+def test_branch_length_grids_with_masks_match_oracle(case, precision):
     """Per-node masks weight the patterns (data.multiplicity(mask=node.mask))."""
     g = gc.load(case)
     rng = np.random.default_rng(5)
-    t, masks = _masked_tree(g, "f64", rng)
+    t, masks = _masked_tree(g, precision, rng)
+    rtol, atol = (1e-9, 1e-8) if precision == "f64" else (1e-4, 1e-3)
     t.infer_ancestral_sequences(marginal=True)
     res = {n.name: v for n, v in t.branch_length_grids(branch_length_mode="marginal").items()}
     tree, aln, model, _ = gc.inputs_from(g)
@@ -86,7 +88,7 @@ def test_branch_length_grids_with_masks_match_oracle(case):
         want = anc.branch_len_log_prob(model, grid, "marginal",
                                        profile_pair=(o["outgroup_LH"][n.name], o["subtree_LH"][n.name]),
                                        multiplicity=m)
-        np.testing.assert_allclose(y, want, rtol=1e-9, atol=1e-8, err_msg=n.name)
+        np.testing.assert_allclose(y, want, rtol=rtol, atol=atol, err_msg=n.name)
 
 
 def test_branch_length_grids_protein_beyond_shared_memory():
@@ -119,3 +121,27 @@ def test_branch_length_grids_protein_beyond_shared_memory():
                                        profile_pair=(o["outgroup_LH"][n.name], o["subtree_LH"][n.name]),
                                        multiplicity=mult)
         np.testing.assert_allclose(y, want, rtol=1e-9, atol=1e-8, err_msg=n.name)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_branch_length_grids_odd_grid_length(precision):
+    """n_grid_points = 200 gives 209-point grids (an odd row length, so the
+    FP32 kernel's pattern rows start after a padded shared-memory table)."""
+    g = gc.load("blgrid_nuc")
+    t = _tree_anc(g, precision)
+    t.infer_ancestral_sequences(marginal=True)
+    res = {n.name: v for n, v in t.branch_length_grids(branch_length_mode="marginal", n_grid_points=200).items()}
+    assert max(len(v[0]) for v in res.values()) % 2 == 1
+    tree, aln, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    caln, mult, full = gc.compress_inputs(aln, model)
+    o = anc.marginal(tree, caln, mult, model, full)
+    rtol, atol = (1e-9, 1e-8) if precision == "f64" else (1e-4, 1e-3)
+    for n in anc.preorder(tree.root):
+        if n.up is None:
+            continue
+        grid, y = res[n.name]
+        want = anc.branch_len_log_prob(model, grid, "marginal",
+                                       profile_pair=(o["outgroup_LH"][n.name], o["subtree_LH"][n.name]),
+                                       multiplicity=mult)
+        np.testing.assert_allclose(y, want, rtol=rtol, atol=atol, err_msg=n.name)

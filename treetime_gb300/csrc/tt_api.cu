@@ -30,17 +30,18 @@ int sm_count() {
     return n > 0 ? n : 1;
 }
 
-// FP64 FMA issue-rate probe: 8 independent dependency chains per thread, so that the FP64 pipe,
-// not latency, sets the time.  Every thread writes its sum (nothing is dead code).
-__global__ void __launch_bounds__(256) fp64_fma_probe_kernel(int64_t iters, double a, double b, double* sink) {
-    double x[8];
+// FMA issue-rate probe: 8 independent dependency chains per thread, so that the FP64 (or FP32)
+// pipe, not latency, sets the time.  Every thread writes its sum (nothing is dead code).
+template <typename T>
+__global__ void __launch_bounds__(256) fma_probe_kernel(int64_t iters, T a, T b, T* sink) {
+    T x[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c;
+    for (int c = 0; c < 8; ++c) x[c] = T(threadIdx.x * 1e-3 + c);
     for (int64_t i = 0; i < iters; ++i) {
 #pragma unroll
         for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
     }
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int c = 0; c < 8; ++c) s += x[c];
     sink[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
@@ -50,13 +51,18 @@ __global__ void __launch_bounds__(256) fp64_fma_probe_kernel(int64_t iters, doub
 
 extern "C" {
 
-tt_status tt_fp64_fma_probe(int64_t iters, int32_t blocks, double* sink, void* stream) {
+tt_status tt_fma_probe(int64_t iters, int32_t blocks, int32_t prec, void* sink, void* stream) {
     if (iters < 0 || blocks <= 0 || !sink) {
-        tt::set_error("tt_fp64_fma_probe: invalid arguments");
+        tt::set_error("tt_fma_probe: invalid arguments");
         return TT_ERR_INVALID;
     }
-    tt::fp64_fma_probe_kernel<<<blocks, 256, 0, tt::as_stream(stream)>>>(iters, 0.9999999, 1e-7, sink);
-    return tt::check_launch("tt_fp64_fma_probe");
+    if (prec == TT_PREC_F32)
+        tt::fma_probe_kernel<float><<<blocks, 256, 0, tt::as_stream(stream)>>>(iters, 0.9999999f, 1e-7f,
+                                                                              static_cast<float*>(sink));
+    else
+        tt::fma_probe_kernel<double><<<blocks, 256, 0, tt::as_stream(stream)>>>(iters, 0.9999999, 1e-7,
+                                                                               static_cast<double*>(sink));
+    return tt::check_launch("tt_fma_probe");
 }
 
 int32_t tt_abi_version(void) { return TT_ABI_VERSION; }

@@ -616,6 +616,227 @@ __global__ void __launch_bounds__(256) prob_t_profiles_grid_kernel(ProfParams a)
     }
 }
 
+// The same values from FP32-scaled profiles in FP32 arithmetic (alphabets of up to 5 states).  Per
+// branch the CTA forms P(t) = max(0, V diag(exp(mu lam t)) V^-1) for every grid point in FP64 (the
+// arithmetic of expQt) and keeps it as FP32 in shared memory; it then stages the patterns in
+// tiles (child profile normalised, parent profile, weight mult*mask*non_gap as FP32 rows), and
+// each warp takes grid points, its lanes summing w log(pc.P(t).pp + 1e-24) over the tile's
+// patterns with compensated (Kahan) FP32 sums; the warp's total is added in FP64.  The terms
+// pc_i P_ij pp_j are all non-negative, so FP32 loses no accuracy to cancellation (the eigenbasis
+// sum of the FP64 kernel would).  Patterns of weight above kHeavyWeight (the invariant columns of a
+// compressed alignment, thousands of sites each) would carry FP32's relative error times their
+// weight into the sum: the first kHeavyMax of them per tile, in pattern order, are evaluated in FP64
+// instead (eigenbasis coefficients, the table-driven FP64 log), the CTA's threads taking grid points.
+constexpr float kHeavyWeight = 16.0f;
+constexpr int kHeavyMax = 64;
+
+template <int Q>
+__global__ void __launch_bounds__(256) prob_t_profiles_grid_f32_kernel(ProfParams a, int tile) {
+    extern __shared__ double sm[];
+    __shared__ double log_tab[129], inv_tab[129];
+    __shared__ double hu[kHeavyMax][Q], hw[kHeavyMax];
+    __shared__ int hidx[kHeavyMax];
+    __shared__ int hcount;
+    const int G = a.n_grid;
+    double* E = sm;                                            // [G][Q]
+    double* hsum = E + (int64_t)G * Q;                         // [G] FP64 sums of the heavy patterns
+    float* Pt = reinterpret_cast<float*>(hsum + G);            // [G][Q*Q]
+    // pattern rows from the next 16-byte boundary (float4 rows for Q = 4)
+    const int64_t fixed = ((int64_t)G * (Q + 1) * 8 + (int64_t)G * Q * Q * 4 + 15) / 16 * 16;
+    float* pcS = reinterpret_cast<float*>(reinterpret_cast<char*>(sm) + fixed);  // [Q][tile] ([tile][4] for Q = 4)
+    float* ppS = pcS + Q * tile;                               // [Q][tile] ([tile][4] for Q = 4)
+    float* wS = ppS + Q * tile;                                // [tile]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int w = a.f.width;
+    for (int j = threadIdx.x; j < 129; j += blockDim.x) {
+        const double F = 1.0 + j / 128.0;
+        log_tab[j] = log(F);
+        inv_tab[j] = 1.0 / F;
+    }
+    for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
+        const int64_t g = a.node_of[b];
+        const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
+        const int P = tr.n_patterns;
+        const int mi = tr.model;
+        const double* V = a.m.V + (int64_t)mi * Q * Q;
+        const double* Vi = a.m.Vinv + (int64_t)mi * Q * Q;
+        const double* lam = a.m.lam + (int64_t)mi * Q;
+        const double mu = a.m.mu[mi];
+        const double* tg = a.grid + b * G;
+        for (int idx = threadIdx.x; idx < G * Q; idx += blockDim.x) {
+            const double t = tg[idx / Q];
+            E[idx] = t >= 0.0 ? exp(mu * lam[idx % Q] * t) : 0.0;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < G * Q * Q; idx += blockDim.x) {
+            const int gi = idx / (Q * Q), e = idx - gi * (Q * Q), i = e / Q, j = e - (e / Q) * Q;
+            double s = 0.0;
+#pragma unroll
+            for (int k = 0; k < Q; ++k) s = fma(V[i * Q + k], E[gi * Q + k] * Vi[k * Q + j], s);
+            Pt[idx] = (float)(s > 0.0 ? s : 0.0);
+        }
+        const bool tipb = a.pc_row[b] < 0;
+        const int trow = tipb ? a.f.tip_row[g] : -1;
+        const int64_t mo = a.f.mask_off ? a.f.mask_off[g] : -1;
+        for (int p0 = 0; p0 < P; p0 += tile) {
+            const int np = P - p0 < tile ? P - p0 : tile;
+            __syncthreads();  // P(t) written; the previous tile's readers are done
+            for (int pi = threadIdx.x; pi < np; pi += blockDim.x) {
+                const int p = p0 + pi;
+                float ppv[Q], pcv[Q];
+                const int64_t pr = (a.pp_row[b] + p) * w;
+#pragma unroll
+                for (int j = 0; j < Q; ++j)
+                    ppv[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
+                                                   : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
+                if (tipb) {
+                    const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) pcv[i] = (float)a.m.lut[code * Q + i];
+                } else {
+                    const int64_t cr = (a.pc_row[b] + p) * w;
+                    float s = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        pcv[i] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pc)[cr + i]
+                                                       : (float)reinterpret_cast<const double*>(a.pc)[cr + i];
+                        s += pcv[i];
+                    }
+                    if (a.prec == TT_PREC_F32) {  // FP32 partials are power-of-two scaled: normalise
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) pcv[i] /= s;
+                    }
+                }
+                float m = (float)a.f.mult[tr.pat_base + p];
+                if (mo >= 0) m *= (float)a.f.masks[mo + p];
+                if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) m *= (1.0f - ppv[a.gap]) * (1.0f - pcv[a.gap]);
+                if constexpr (Q == 4) {
+                    reinterpret_cast<float4*>(pcS)[pi] = make_float4(pcv[0], pcv[1], pcv[2], pcv[3]);
+                    reinterpret_cast<float4*>(ppS)[pi] = make_float4(ppv[0], ppv[1], ppv[2], ppv[3]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        pcS[i * tile + pi] = pcv[i];
+                        ppS[i * tile + pi] = ppv[i];
+                    }
+                }
+                wS[pi] = m;
+            }
+            __syncthreads();
+            // heavy patterns of the tile, in pattern order
+            if (warp == 0) {
+                int count = 0;
+                for (int base = 0; base < np; base += 32) {
+                    const int pi = base + lane;
+                    const bool heavy = pi < np && wS[pi] > kHeavyWeight;
+                    const unsigned bal = __ballot_sync(0xffffffffu, heavy);
+                    const int pos = count + __popc(bal & ((1u << lane) - 1u));
+                    if (heavy && pos < kHeavyMax) hidx[pos] = pi;
+                    count += __popc(bal);
+                }
+                if (lane == 0) hcount = count < kHeavyMax ? count : kHeavyMax;
+            }
+            __syncthreads();
+            const int H = hcount;
+            for (int idx = threadIdx.x; idx < H * Q; idx += blockDim.x) {
+                const int h = idx / Q, k = idx - (idx / Q) * Q, pi = hidx[h];
+                // the child profile again from its stored row, normalised in FP64 (an FP32
+                // normalisation would add up to one FP32 rounding, times the pattern's weight)
+                double pcd[Q], sc = 0.0;
+                if (tipb) {
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) pcd[i] = Q == 4 ? (double)pcS[pi * 4 + i] : (double)pcS[i * tile + pi];
+                    sc = 1.0;
+                } else {
+                    const int64_t cr = (a.pc_row[b] + p0 + pi) * w;
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        pcd[i] = a.prec == TT_PREC_F32 ? (double)reinterpret_cast<const float*>(a.pc)[cr + i]
+                                                       : reinterpret_cast<const double*>(a.pc)[cr + i];
+                        sc += pcd[i];
+                    }
+                    if (a.prec != TT_PREC_F32) sc = 1.0;
+                }
+                double x = 0.0, y = 0.0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    const double ppi = Q == 4 ? (double)ppS[pi * 4 + i] : (double)ppS[i * tile + pi];
+                    x = fma(pcd[i], V[i * Q + k], x);
+                    y = fma(Vi[k * Q + i], ppi, y);
+                }
+                hu[h][k] = x / sc * y;
+            }
+            for (int h = threadIdx.x; h < H; h += blockDim.x) {
+                const int pi = hidx[h], p = p0 + pi;
+                double m = a.f.mult[tr.pat_base + p];
+                if (mo >= 0) m *= a.f.masks[mo + p];
+                if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) {
+                    const double pcg = Q == 4 ? (double)pcS[pi * 4 + a.gap] : (double)pcS[a.gap * tile + pi];
+                    const double ppg = Q == 4 ? (double)ppS[pi * 4 + a.gap] : (double)ppS[a.gap * tile + pi];
+                    m *= (1.0 - ppg) * (1.0 - pcg);
+                }
+                hw[h] = m;
+            }
+            __syncthreads();
+            for (int h = threadIdx.x; h < H; h += blockDim.x) wS[hidx[h]] = 0.0f;
+            for (int gi = threadIdx.x; gi < G; gi += blockDim.x) {
+                double acc = 0.0;
+                for (int h = 0; h < H; ++h) {
+                    double res = 0.0;
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) res = fma(hu[h][k], E[gi * Q + k], res);
+                    acc = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), acc);
+                }
+                hsum[gi] = acc;
+            }
+            __syncthreads();
+            for (int gi = warp; gi < G; gi += nw) {
+                if (tg[gi] < 0.0) {
+                    if (lane == 0) a.grid_out[b * G + gi] = -kBig;
+                    continue;
+                }
+                float Pm[Q * Q];
+#pragma unroll
+                for (int e = 0; e < Q * Q; ++e) Pm[e] = Pt[gi * Q * Q + e];
+                float s = 0.0f, c = 0.0f;
+#pragma unroll 2
+                for (int pi = lane; pi < np; pi += 32) {
+                    float pb[Q], pa[Q];
+                    if constexpr (Q == 4) {
+                        const float4 b4 = reinterpret_cast<const float4*>(ppS)[pi];
+                        const float4 a4 = reinterpret_cast<const float4*>(pcS)[pi];
+                        pb[0] = b4.x; pb[1] = b4.y; pb[2] = b4.z; pb[3] = b4.w;
+                        pa[0] = a4.x; pa[1] = a4.y; pa[2] = a4.z; pa[3] = a4.w;
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < Q; ++j) {
+                            pb[j] = ppS[j * tile + pi];
+                            pa[j] = pcS[j * tile + pi];
+                        }
+                    }
+                    float res = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        float v = 0.0f;
+#pragma unroll
+                        for (int j = 0; j < Q; ++j) v = fmaf(Pm[i * Q + j], pb[j], v);
+                        res = fmaf(pa[i], v, res);
+                    }
+                    const float y = wS[pi] * logf(res + 1e-24f) - c;
+                    const float tsum = s + y;
+                    c = (tsum - s) - y;
+                    s = tsum;
+                }
+                double tot = (double)s - (double)c;
+                tot = warp_sum(tot);
+                if (lane == 0)
+                    a.grid_out[b * G + gi] = (p0 == 0 ? 0.0 : a.grid_out[b * G + gi]) + (tot + hsum[gi]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <int QT>
 static void launch_t_grid(const ProfParams& a, int blocks, size_t smem, cudaStream_t s) {
     static bool configured[64] = {};
@@ -717,6 +938,35 @@ extern "C" tt_status tt_prob_t_profiles_grid(const tt_forest* f, const tt_model*
     a.n_grid = n_grid;
     a.grid_out = logp_out;
     cudaStream_t s = as_stream(stream);
+    if (prec == TT_PREC_F32 && (q == 4 || q == 5)) {
+        // FP32 profiles, small alphabets: FP32 kernel, three CTAs per SM (64 KB of dynamic shared
+        // memory each: exp table, heavy-pattern sums, P(t) table, pattern tiles; 5 KB static)
+        const int64_t fixed = ((int64_t)n_grid * (q + 1) * 8 + (int64_t)n_grid * q * q * 4 + 15) / 16 * 16;
+        const int64_t budget = 64 * 1024;
+        int64_t tile = (budget - fixed) / ((2 * q + 1) * 4);
+        tile = (tile / 32) * 32;
+        if (tile >= 256) {
+            const size_t smem = (size_t)(fixed + tile * (2 * q + 1) * 4 + 16);
+            const int64_t cap = 3 * sms;
+            const int fb = (int)(n < cap ? n : cap);
+            static bool configured[2][64] = {};
+            int dev = 0;
+            cudaGetDevice(&dev);
+            const int qi = q == 4 ? 0 : 1;
+            if (dev < 0 || dev >= 64 || !configured[qi][dev]) {
+                if (q == 4)
+                    cudaFuncSetAttribute(prob_t_profiles_grid_f32_kernel<4>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+                else
+                    cudaFuncSetAttribute(prob_t_profiles_grid_f32_kernel<5>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+                if (dev >= 0 && dev < 64) configured[qi][dev] = true;
+            }
+            if (q == 4) prob_t_profiles_grid_f32_kernel<4><<<fb, 256, smem, s>>>(a, (int)tile);
+            else prob_t_profiles_grid_f32_kernel<5><<<fb, 256, smem, s>>>(a, (int)tile);
+            return check_launch("tt_prob_t_profiles_grid");
+        }
+    }
     switch (q) {
         case 4: launch_t_grid<4>(a, blocks, smem_max, s); break;
         case 5: launch_t_grid<5>(a, blocks, smem_max, s); break;

@@ -23,6 +23,7 @@
  *   tt_mutation_counts, tt_mutation_counts_joint
  *                        the substitution counting of TreeAnc.infer_gtr   treetime/treeanc.py:1544-1584
  *   tt_branch_mutation_matrix  TreeAnc.get_branch_mutation_matrix     treetime/treeanc.py:1085-1120
+ *   tt_fitch_up, tt_fitch_down  TreeAnc._fitch_anc (Fitch parsimony)   treetime/treeanc.py:575-686
  *   tt_compress_columns  SequenceData.make_compressed_alignment  treetime/sequence_data.py:325-464
  *
  * Conventions
@@ -384,6 +385,29 @@ tt_status tt_branch_mutation_matrix(const tt_forest* f, const tt_model* m, int32
                                     const int32_t* node, const void* pp, const int64_t* pp_row, const void* pc,
                                     const int64_t* pc_row, int32_t prec, const double* p64, double* out,
                                     void* stream);
+
+/* ------------------------------------------------------------ Fitch parsimony
+ * TreeAnc._fitch_anc (treetime/treeanc.py:575-686) with TreeTime's list semantics: a node's list
+ * of characters is its last child's list filtered by the other children's lists (order and
+ * repeats of the last child's list), or the children's lists concatenated when that is empty;
+ * characters are compared as bytes (ambiguity codes and gaps are characters like any other).
+ * tt_fitch_up: the lists of every internal node, `lists` = 16 bytes per profile row of the forest
+ * (row prof_base + k*P + p: up to 15 characters, byte 15 = length); *status = TT_ERR_UNSUPPORTED
+ * when a list would exceed 15 characters, TT_ERR_INVALID when a tip has no sequence.  With
+ * tip_chars (state layout, may be NULL) a tip's character is read from its row there -- the
+ * reconstructed tip sequences TreeTime's cseq returns after a reconstruction with tip states --
+ * instead of from its code.
+ * tt_fitch_down: given the root characters root_chars[pattern] (chosen by the caller from the
+ * root's lists: the first entry, or a random one where the list is longer), a node keeps its
+ * parent's character when it is in its list, else takes the first entry; characters to `chars`
+ * (state layout, internal nodes), optionally state indices through char_state (255 for
+ * characters outside the alphabet) to `states`, and, with `prev` (the previous characters,
+ * state layout), per-tree counts of changed characters of the non-root internal nodes added to
+ * n_diff[tree]. */
+tt_status tt_fitch_up(const tt_forest* f, void* lists, const uint8_t* tip_chars, int32_t* status, void* stream);
+tt_status tt_fitch_down(const tt_forest* f, const void* lists, const uint8_t* root_chars, uint8_t* chars,
+                        uint8_t* states, const uint8_t* char_state, const uint8_t* prev, int64_t* n_diff,
+                        void* stream);
 
 /* -------------------------------------------------- a1: compression
  * Column classes of a tips x sites byte matrix (row-major, n_rows x n_cols): key[c] = the letter

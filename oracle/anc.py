@@ -317,6 +317,46 @@ def joint(tree, aln, mult, model, full_length, sample_from_profile=False, recons
                 root_Lx=root_lx, sequence_LH=seq_lh, sequence_joint_LH=total, N_diff=n_diff)
 
 
+def fitch(tree, tip_cseq, L, rng, prev_cseq=None):
+    """TreeAnc._fitch_anc (treeanc.py:575-643) with _fitch_state (:645-664)
+    and _fitch_intersect (:666-686): Python lists of characters per node and
+    position.  ``tip_cseq`` name -> compressed characters; returns (name ->
+    characters of every internal node, N_diff)."""
+    state = {}
+    for leaf in (n for n in preorder(tree.root) if not n.clades):
+        state[leaf.name] = [[k] for k in tip_cseq[leaf.name]]
+
+    def intersect(arrays):
+        arrays = list(arrays)
+        while len(arrays) > 1:
+            arr1 = arrays.pop()
+            s2 = set(arrays.pop())
+            arrays.append([v for v in arr1 if v in s2])
+        return arrays[0]
+
+    for node in (n for n in postorder(tree.root) if n.clades):
+        st = []
+        for pos in range(L):
+            s = intersect([state[c.name][pos] for c in node.clades])
+            if len(s) == 0:
+                s = list(np.concatenate([state[c.name][pos] for c in node.clades]))
+            st.append(s)
+        state[node.name] = st
+    cseq = {tree.root.name: np.array([k[rng.integers(len(k)) if len(k) > 1 else 0] for k in state[tree.root.name]])}
+    n_diff = 0
+    for node in preorder(tree.root):
+        if not node.clades or node is tree.root:
+            continue
+        par = cseq[node.up.name]
+        seq = np.array([par[i] if par[i] in state[node.name][i] else state[node.name][i][0] for i in range(L)])
+        if prev_cseq is not None:
+            n_diff += int((seq != prev_cseq[node.name]).sum())
+        else:
+            n_diff += L
+        cseq[node.name] = seq
+    return cseq, n_diff
+
+
 def ancestral_likelihood(tree, cseq, mult, model, full_length):
     """TreeAnc.ancestral_likelihood (treeanc.py:714-750): per-pattern log-LH
     of a full assignment of sequences."""

@@ -6,6 +6,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source
     python tests/golden/make_golden.py /path/to/treetime-source --blgrid   (interpolator grids only)
     python tests/golden/make_golden.py /path/to/treetime-source --infer-gtr   (GTR inference only)
+    python tests/golden/make_golden.py /path/to/treetime-source --fitch   (Fitch parsimony only)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -320,6 +321,79 @@ def infer_gtr_cases():
                   {"pi": pi0, "W": W0, "alphabet": synth.AA21, "mu": 1.0}, compress=False, site_specific=True)
 
 
+def run_fitch(name, newick, aln, kind, params, rng_seed=7):
+    """TreeAnc.infer_ancestral_sequences(method='fitch'): the characters of
+    every internal node and N_diff, then a second call (N_diff against the
+    first) and a marginal reconstruction followed by Fitch (N_diff against
+    the marginal sequences)."""
+    from treetime import TreeAnc
+    out = {"case": name, "newick": newick, "kind": kind, "rng_seed": rng_seed,
+           "aln_names": np.array(list(aln.keys())), "aln_seqs": np.array(list(aln.values()))}
+    for k, v in params.items():
+        out["param_" + k] = np.asarray(v)
+    tree, recs = _bio_inputs(newick, aln)
+    t = TreeAnc(tree=tree, aln=recs, gtr=_ref_gtr(kind, params), compress=True, verbose=0, rng_seed=rng_seed)
+    out["fitch_N_diff"] = t.infer_ancestral_sequences(method="fitch")
+    inner = [n for n in t.tree.find_clades() if not n.is_terminal()]
+    out["fitch_names"] = np.array([n.name for n in inner])
+    out["fitch_cseq"] = np.stack([_codes(n._cseq) for n in inner])
+    out["fitch_N_diff_again"] = t.infer_ancestral_sequences(method="fitch")
+    out["fitch_cseq_again"] = np.stack([_codes(n._cseq) for n in inner])
+    tree, recs = _bio_inputs(newick, aln)
+    t = TreeAnc(tree=tree, aln=recs, gtr=_ref_gtr(kind, params), compress=True, verbose=0, rng_seed=rng_seed)
+    t.infer_ancestral_sequences(marginal=True)
+    out["fitch_after_marginal_N_diff"] = t.infer_ancestral_sequences(method="fitch")
+    out["fitch_after_marginal_cseq"] = np.stack([_codes(n._cseq) for n in t.tree.find_clades()
+                                                 if not n.is_terminal()])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
+
+
+def fitch_cases():
+    """Binary nucleotide tree; polytomies with ambiguity codes, N and gaps
+    (characters outside the alphabet, repeated union entries); amino acids."""
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    rng = np.random.default_rng(41)
+    tree = synth.coalescent_tree(30, 0.05, rng)
+    g = GTR.custom(mu=1.0, pi=np.ones(4), W=np.ones((4, 4)), alphabet="nuc_nogap")
+    states = synth.evolve(tree, g, 200, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    run_fitch("fitch_nuc", to_newick(tree), aln, "gtr", {"pi": np.ones(4), "W": np.ones((4, 4)),
+                                                          "alphabet": "nuc_nogap", "mu": 1.0})
+    rng = np.random.default_rng(42)
+    tree = synth.coalescent_tree(22, 0.08, rng)
+    inner = [c for c in tree.find_clades(order="postorder") if c.clades and c is not tree.root]
+    for c in inner[:4]:
+        for par in tree.find_clades():
+            if c in par.clades:
+                i = par.clades.index(c)
+                par.clades[i:i + 1] = c.clades
+                break
+    pi = rng.dirichlet(np.ones(5))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(5, 5)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc")
+    states = synth.evolve(tree, g, 150, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    for k in list(aln):
+        s = np.array(list(aln[k]))
+        r = rng.random(len(s))
+        s[r < 0.05] = "N"
+        s[(r > 0.05) & (r < 0.08)] = rng.choice(list("RYKMSW"))
+        aln[k] = "".join(s)
+    run_fitch("fitch_poly", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "nuc", "mu": 1.0})
+    rng = np.random.default_rng(43)
+    tree = synth.coalescent_tree(16, 0.2, rng)
+    pi = rng.random(20)
+    W = rng.random((20, 20))
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="aa_nogap")
+    states = synth.evolve(tree, g, 100, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    run_fitch("fitch_aa", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "aa_nogap", "mu": 1.0})
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -466,5 +540,8 @@ if __name__ == "__main__":
     elif "--infer-gtr" in sys.argv:
         _setup(ref)
         infer_gtr_cases()
+    elif "--fitch" in sys.argv:
+        _setup(ref)
+        fitch_cases()
     else:
         main(ref)

@@ -234,3 +234,30 @@ def test_oracle_substitution_counts_match_treetime(case):
         else:
             np.testing.assert_allclose(n_ija.sum(axis=-1), g[mode + "_nij"], rtol=1e-11, atol=1e-11)
             np.testing.assert_allclose(T_ia.sum(axis=-1), g[mode + "_Ti"], rtol=1e-11, atol=1e-11)
+
+
+# ------------------------------------------------------------------ Fitch parsimony
+FITCH = gc.fitch_names()
+
+
+@pytest.mark.parametrize("case", FITCH)
+def test_oracle_fitch_matches_treetime(case):
+    g = gc.load(case)
+    tree, aln, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    caln, mult, full = gc.compress_inputs(aln, model)
+    rng = np.random.default_rng(int(g["rng_seed"]))
+    cseq, nd = anc.fitch(tree, caln, len(mult), rng)
+    assert nd == int(g["fitch_N_diff"])
+    for i, k in enumerate(g["fitch_names"].tolist()):
+        np.testing.assert_array_equal(gc.codes_of(cseq[k]), g["fitch_cseq"][i], err_msg=k)
+    cseq2, nd2 = anc.fitch(tree, caln, len(mult), rng, prev_cseq=cseq)
+    assert nd2 == int(g["fitch_N_diff_again"])
+    for i, k in enumerate(g["fitch_names"].tolist()):
+        np.testing.assert_array_equal(gc.codes_of(cseq2[k]), g["fitch_cseq_again"][i], err_msg=k)
+    res = anc.marginal(tree, caln, mult, model, full)
+    cseq3, nd3 = anc.fitch(tree, caln, len(mult), np.random.default_rng(int(g["rng_seed"])),
+                           prev_cseq=res["cseq"])
+    assert nd3 == int(g["fitch_after_marginal_N_diff"])
+    for i, k in enumerate(g["fitch_names"].tolist()):
+        np.testing.assert_array_equal(gc.codes_of(cseq3[k]), g["fitch_after_marginal_cseq"][i], err_msg=k)

@@ -88,6 +88,8 @@ _SIGS = {
                                       vp, i64, vp]),
     "tt_prob_t_pairs_grid": (i32, [i32, i64, vp, vp, P(TTModel), vp, i32, vp, vp]),
     "tt_fma_probe": (i32, [i64, i32, i32, vp, vp]),
+    "tt_fitch_up": (i32, [P(TTForest), vp, vp, vp, vp]),
+    "tt_fitch_down": (i32, [P(TTForest), vp, vp, vp, vp, vp, vp, vp, vp]),
     "tt_mutation_counts": (i32, [P(TTForest), P(TTModel), i32, i32, i64, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp,
                                  i64, vp]),
     "tt_mutation_counts_joint": (i32, [P(TTForest), i32, i32, i64, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp]),

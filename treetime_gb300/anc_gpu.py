@@ -67,6 +67,9 @@ class ResultStore:
         if name == "_cseq":
             if is_tip and not self.reconstruct_tips:
                 return None
+            if self.kind == "parsimony":  # characters, possibly outside the alphabet
+                chars = self._fetch_buf("chars")
+                return chars[k * self.P:(k + 1) * self.P].view("S1").astype("U1")
             return self.tt.gtr.alphabet[self.states[k]]
         if self.kind != "marginal":
             return None
@@ -295,6 +298,77 @@ class GPUAncMixin:
         self.reconstructed_tip_sequences = reconstruct_tip_states
         self.sequence_reconstruction = "joint"
         self._last = ("joint", out)
+        return N_diff
+
+    def _previous_chars(self, sess):
+        """Characters of the last reconstruction in the state layout (device),
+        or None when there is none."""
+        t = engine.torch()
+        last = getattr(self, "_last", None)
+        if not self.sequence_reconstruction or last is None:
+            return None
+        if last[0] == "parsimony":
+            return last[1]["chars"].clone()
+        states = sess["bufs"].cache.get(("states", t.uint8))
+        if states is None:
+            return None
+        alpha = np.zeros(256, dtype=np.uint8)
+        alpha[:len(self.gtr.alphabet)] = np.frombuffer("".join(self.gtr.alphabet.tolist()).encode(), np.uint8)
+        return engine._to_dev(alpha, states.device)[states.long()]
+
+    def _fitch_anc(self, **kwargs):
+        """Fitch parsimony (treetime/treeanc.py:575-643) on the GPU: the lists
+        of all internal nodes in one pass up the tree, the root's characters on
+        the host (a random entry of a longer list from TreeTime's generator, in
+        position order), one pass down."""
+        t = engine.torch()
+        lib = engine._lib.load()
+        sess = self._get_session()
+        layout, forest, bufs = sess["layout"], sess["forest"], sess["bufs"]
+        P = self.data.compressed_length
+        tip_chars = None
+        if self.reconstructed_tip_sequences:
+            tip_chars = self._previous_chars(sess)
+        else:
+            name_to_row, _ = self._aln_index()
+            for n in layout.nodes[layout.n_int:]:
+                if n.name not in name_to_row:
+                    raise MissingDataError("TreeAnc._fitch_anc: terminal node alignments required; sequence is "
+                                           "missing for leaf: '%s'." % n.name)
+        prev = self._previous_chars(sess)
+        lists = bufs.get("fitch_lists", (forest.prof_rows, 16), t.uint8)
+        status = bufs.get("status", (1,), t.int32)
+        status.zero_()
+        engine.check(lib.tt_fitch_up(C.byref(forest.struct), engine._p(lists), engine._p(tip_chars),
+                                     engine._p(status), engine._stream()), "tt_fitch_up")
+        engine._check_status(status)
+        self.logger("TreeAnc._fitch_anc: Walking up the tree, creating the Fitch profiles", 2)
+        root = lists[(layout.n_int - 1) * P:layout.n_int * P].cpu().numpy()
+        lens = root[:, 15].astype(np.int64)
+        root_chars = root[:, 0].copy()
+        for i in np.nonzero(lens > 1)[0]:
+            choices = root[i, :lens[i]].tobytes().decode("latin-1")
+            self.logger("Ambiguous state of the root sequence in the position %d: %s, choosing %s"
+                        % (i, str(list(choices)), choices[0]), 4)
+            root_chars[i] = root[i, self.rng.integers(lens[i])]
+        self.logger("TreeAnc._fitch_anc: Walking down the self.tree, generating sequences from the Fitch profiles.", 2)
+        chars = bufs.get("fitch_chars", (forest.state_rows,), t.uint8)
+        states = bufs.get("states", (forest.state_rows,), t.uint8)
+        if tip_chars is not None:
+            chars[layout.n_int * P:].copy_(tip_chars[layout.n_int * P:])
+        n_diff = t.zeros(1, dtype=t.int64, device=forest.device)
+        d_root = engine._to_dev(root_chars, forest.device)
+        cs = engine._to_dev(engine.char_state_table(self.gtr, strict=True), forest.device)
+        engine.check(lib.tt_fitch_down(C.byref(forest.struct), engine._p(lists), engine._p(d_root), engine._p(chars),
+                                       engine._p(states), engine._p(cs), engine._p(prev), engine._p(n_diff),
+                                       engine._stream()), "tt_fitch_down")
+        N_diff = int(n_diff.item()) if prev is not None else (layout.n_int - 1) * P
+        self._clear_results(layout)
+        out = {"states": states, "chars": chars}
+        self._install(ResultStore(self, layout, "parsimony", out, "f64", self.reconstructed_tip_sequences), layout)
+        self.sequence_reconstruction = "parsimony"
+        self._last = ("parsimony", out)
+        self.logger("Done ancestral state reconstruction", 3)
         return N_diff
 
     # --------------------------------------------------------- branch lengths

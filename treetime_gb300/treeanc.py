@@ -22,10 +22,10 @@ TreeTime's FP64 log-domain arithmetic.
 
 GTR inference (``infer_gtr``, ``infer_gtr_iterative``,
 ``get_branch_mutation_matrix``) counts substitutions on the GPU and fits the
-model on the host as TreeTime does.
+model on the host as TreeTime does; Fitch parsimony (``method='fitch'``) runs
+its passes up and down the tree on the GPU.
 
-Out of scope (raise NotImplementedError): Fitch parsimony, sparse (VCF)
-alignments.
+Out of scope (raise NotImplementedError): sparse (VCF) alignments.
 """
 
 import gc
@@ -299,7 +299,7 @@ class TreeAnc(GPUAncMixin):
         if method.lower() in ["ml", "probabilistic"]:
             fn = self._ml_anc_marginal if marginal else self._ml_anc_joint
         elif method.lower() in ["fitch", "parsimony"]:
-            raise NotImplementedError("Fitch parsimony is not part of the GPU hot path")
+            fn = self._fitch_anc
         else:
             raise UnknownMethodError("Reconstruction method needs to be in ['ml', 'probabilistic', 'fitch', "
                                      "'parsimony'], got '{}'".format(method))

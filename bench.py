@@ -691,6 +691,101 @@ def run_gtrinf(args):
     return out
 
 
+FITCH_WORKLOAD = ("fitch: Fitch parsimony reconstruction (TreeAnc.infer_ancestral_sequences(method='fitch')) of the "
+                  "2000-tip x 30000-site tree")
+
+
+def run_fitch(args):
+    """--workload fitch: one Fitch reconstruction per step through the public
+    call (pass up, root lists to the host and TreeTime's random choices, pass
+    down, N_diff against the previous reconstruction); the device passes are
+    also timed alone.  L2 flushed before every step."""
+    import torch
+    from treetime_gb300 import engine
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t, wl = build_workload()
+    t.device = dev
+    P = t.data.compressed_length
+    layout = t._get_session()["layout"]
+    units = layout.n_nodes * P
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        t.infer_ancestral_sequences(method="fitch")
+    torch.cuda.synchronize()
+    ts = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            t.infer_ancestral_sequences(method="fitch")
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+    ms = _reduce_max(statistics.median(ts) * 1e3, dev, world)
+    # the two device passes alone (CUDA events), as the library's C entries run them
+    sess = t._get_session()
+    forest, bufs = sess["forest"], sess["bufs"]
+    lib = engine._lib.load()
+    lists = bufs.get("fitch_lists", (forest.prof_rows, 16), torch.uint8)
+    status = bufs.get("status", (1,), torch.int32)
+    chars = bufs.get("fitch_chars", (forest.state_rows,), torch.uint8)
+    root_chars = engine._to_dev(np.full(P, ord("A"), np.uint8), dev)
+    kt = []
+    for _ in range(min(args.steps, 20)):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        engine.check(lib.tt_fitch_up(engine.C.byref(forest.struct), engine._p(lists), None, engine._p(status),
+                                     engine._stream()), "tt_fitch_up")
+        engine.check(lib.tt_fitch_down(engine.C.byref(forest.struct), engine._p(lists), engine._p(root_chars),
+                                       engine._p(chars), None, None, None, None, engine._stream()), "tt_fitch_down")
+        b.record()
+        b.synchronize()
+        kt.append(a.elapsed_time(b))
+    k_ms = statistics.median(kt)
+    if rank != 0:
+        return None
+    # algorithmic bytes of the two passes: per internal node and pattern a 16-byte list written
+    # and read back by the parent, read again going down, one character written; per tip a code
+    ab = P * (layout.n_int * (16 * 3 + 1) + layout.n_tip)
+    peak, peak_kind = _peaks()
+    out = {
+        "metric": "node-patterns/s (Fitch parsimony reconstruction)", "value": world * units / (ms * 1e-3),
+        "unit": "node-patterns/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
+        "config": {"workload": FITCH_WORKLOAD, "nodes": layout.n_nodes, "patterns": P,
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU",
+                   "timing": "host clock around the public call (it reads the root lists back and makes "
+                             "TreeTime's random choices on the host)"},
+        "device_passes": {"ms": k_ms, "value": units / (k_ms * 1e-3)},
+        "roofline": {"bound": "hbm", "achieved": ab / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": ab / (k_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                     "note": "both passes; one thread per pattern walks the tree (latency bound)"},
+        "e2e": {"value": units / (ms * 1e-3), "unit": "node-patterns/s", "ms_per_step": ms,
+                "h2d_bytes_per_step": P, "d2h_bytes_per_step": 16 * P + 8},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import anc
+        from treetime_gb300.tree import parse_newick, to_newick
+        tree = anc.prepare_tree(parse_newick(to_newick(t.tree)))
+        chars = np.asarray(t.data.compressed_codes).view("S1").astype("U1")
+        caln = {k: chars[i] for i, k in enumerate(t.data.sequence_names)}
+        Ps = max(1, min(P, 200))
+        t0 = time.perf_counter()
+        anc.fitch(tree, {k: v[:Ps] for k, v in caln.items()}, Ps, np.random.default_rng(0))
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": layout.n_nodes * Ps / secs, "unit": "node-patterns/s", "cores": 1,
+                               "kind": "port", "sample": "the first %d patterns of the workload through the "
+                               "Python restatement of TreeTime's Fitch (lists per node and position), 1 process"
+                               % Ps, "seconds": secs}
+    return out
+
+
 C3_WORKLOAD = ("c3: 256 independent coalescent trees, tips log-uniform in [50, 5000], sites log-uniform in "
                "[1k, 30k], branch means log-uniform in [1e-4, 0.05], a random GTR per tree; the whole batch is "
                "one forest, one captured launch sequence per step")
@@ -1070,7 +1165,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf", "fitch"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
@@ -1089,7 +1184,7 @@ def main():
         from treetime_gb300 import build
         build.build()
         res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4, "blgrid": run_blgrid,
-               "gtrinf": run_gtrinf}[args.workload](args)
+               "gtrinf": run_gtrinf, "fitch": run_fitch}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

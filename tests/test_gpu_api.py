@@ -158,3 +158,88 @@ def test_joint_lh_is_max_by_brute_force():
     t2.reconstructed_tip_sequences = True
     ref = t2.ancestral_likelihood()
     assert abs(ref.max() - real[0]) < 1e-10
+
+
+def _bl_pair(n_tips, L, mean_bl, seed):
+    """(FP32 lengths, FP64 lengths, FP64 objective) of every branch of one
+    synthetic nucleotide tree, from profile-mode Brent."""
+    from treetime_gb300 import TreeAnc, synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import parse_newick, to_newick
+    rng = np.random.default_rng(seed)
+    tree = synth.coalescent_tree(n_tips, mean_bl, rng)
+    g = GTR.custom(mu=1.0, pi=rng.dirichlet(np.ones(4)), W=np.ones((4, 4)), alphabet="nuc_nogap")
+    aln = synth._to_text(synth.evolve(tree, g, L, rng), g.alphabet, 0.0, rng)
+    nwk = to_newick(tree)
+    out = {}
+    for prec in ("f32", "f64"):
+        t = TreeAnc(tree=parse_newick(nwk), aln=aln, gtr=g, verbose=0, precision=prec)
+        t.infer_ancestral_sequences(marginal=True)
+        nodes = [n for n in t.tree.find_clades() if n.up is not None]
+        out[prec] = (t, {n.name: x for n, x in zip(nodes, t._marginal_branch_lengths(nodes, 1e-10))})
+    return out, g
+
+
+def _heavy_pair():
+    """The same comparison through the engine with every pattern's
+    multiplicity scaled by 20 (TreeTime's compression only merges constant
+    columns, so a TreeAnc never has more than a handful of heavy patterns)."""
+    from treetime_gb300 import TreeAnc, engine, synth
+    from treetime_gb300.gtr import GTR
+    rng = np.random.default_rng(12)
+    tree = synth.coalescent_tree(16, 0.05, rng)
+    g = GTR.custom(mu=1.0, pi=rng.dirichlet(np.ones(4)), W=np.ones((4, 4)), alphabet="nuc_nogap")
+    aln = synth._to_text(synth.evolve(tree, g, 400, rng), g.alphabet, 0.0, rng)
+    t = TreeAnc(tree=tree, aln=aln, gtr=g, verbose=0)
+    ti = t._get_session()["forest"].inputs[0]
+    heavy = engine.TreeInput(ti.layout, ti.tip_codes, ti.tip_row, ti.mult * 20.0, ti.bl)
+    assert (heavy.mult > 16).sum() > 64
+    lay = ti.layout
+    ks = np.arange(lay.n_nodes)
+    ks = ks[ks != lay.n_int - 1]
+    out = {}
+    for prec in ("f32", "f64"):
+        forest = engine.Forest([heavy], 4)
+        model = engine.model_for(g)
+        bufs = engine.Buffers(forest)
+        res = engine.marginal(forest, model, bufs, precision=prec, keep_outgroup=True, tip_outgroup=True)
+        P = int(forest.trees_host["n_patterns"][0])
+        vals = {}
+        for grp, pp in ((ks[ks < lay.n_int], res["outgroup"]), (ks[ks >= lay.n_int], res["tip_outgroup"])):
+            tips = grp[0] >= lay.n_int
+            pp_row = [((k - lay.n_int) if tips else k) * P for k in grp]
+            pc_row = [-1 if tips else k * P for k in grp]
+            tt, _ = engine.optimal_t_profiles(forest, model, grp, pp, pp_row, res["partial"], pc_row, prec, None,
+                                              True, 1e-10)
+            vals.update({lay.nodes[k].name: x for k, x in zip(grp, tt.cpu().numpy())})
+        out[prec] = (t, vals)
+    # the FP64 objective uses the FP64 reconstruction's profiles with the scaled multiplicities
+    t.infer_ancestral_sequences(marginal=True)
+    t.data._multiplicity = t.data.multiplicity() * 20.0
+    return out, g
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", ["many_patterns", "many_heavy"])
+def test_fp32_profile_brent_matches_fp64(shape):
+    """FP32-profile Brent (FP32 objective) against the FP64 path: patterns
+    beyond the shared-memory rows (read from the stored profiles at every
+    evaluation), and more than 64 heavy patterns (the first 64 in FP64).
+    Lengths agree to 2e-3 relative, or the FP64 objective agrees to 1e-6."""
+    from oracle import anc as oanc
+    if shape == "many_patterns":
+        out, g = _bl_pair(40, 6000, 0.2, 11)
+        assert out["f32"][0].data.compressed_length > (100 * 1024) // 36
+    else:
+        out, g = _heavy_pair()
+    t64 = out["f64"][0]
+    nodes = {n.name: n for n in t64.tree.find_clades()}
+    mult = t64.data.multiplicity()
+    for name, x32 in out["f32"][1].items():
+        x64 = out["f64"][1][name]
+        if abs(x32 - x64) <= 2e-3 * abs(x64) + 1e-10:
+            continue
+        n = nodes[name]
+        pp, pc = n.marginal_outgroup_LH, n.marginal_subtree_LH
+        f = lambda tt: -oanc.prob_t_profiles(g, (pp, pc), mult, tt, return_log=True) + np.exp(tt * tt / 1e4)
+        assert abs(f(x32) - f(x64)) <= 1e-6 * abs(f(x64)) + 1e-12, (name, x32, x64)

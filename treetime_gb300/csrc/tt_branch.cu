@@ -837,6 +837,256 @@ __global__ void __launch_bounds__(256) prob_t_profiles_grid_f32_kernel(ProfParam
     }
 }
 
+// Profile-mode Brent from FP32-scaled profiles (alphabets of up to 5 states): the objective of
+// optimal_t_profiles_kernel evaluated as in prob_t_profiles_grid_f32_kernel -- per evaluation
+// warp 0 forms P(t) in FP64 (kept as FP32) and the heavy patterns' FP64 terms, then every thread
+// sums w logf(pc.P(t).pp + 1e-24) over its patterns with compensated FP32 sums, added across the
+// CTA in FP64.  Patterns are staged in shared memory (FP32 rows: normalised child profile, parent
+// profile, weight) when the tree has at most `cap` of them, else read from their stored rows at
+// every evaluation.  The search, bracket, Hamming distance and results are those of the FP64
+// kernel (the Hamming distance is summed in FP64).
+template <int Q>
+__global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams a) {
+    extern __shared__ float smf[];
+    __shared__ double red[32];
+    __shared__ double log_tab[129], inv_tab[129];
+    __shared__ double hu[kHeavyMax][Q], hw[kHeavyMax];
+    __shared__ int hidx[kHeavyMax];
+    __shared__ int hcount, hall;
+    __shared__ float Pt[Q * Q];
+    __shared__ double Ed[Q];
+    __shared__ double hsum_s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int w = a.f.width;
+    for (int j = threadIdx.x; j < 129; j += blockDim.x) {
+        const double F = 1.0 + j / 128.0;
+        log_tab[j] = log(F);
+        inv_tab[j] = 1.0 / F;
+    }
+    const int cap = a.cap;
+    float* pcS = smf;             // [cap][Q] (float4 rows for Q = 4)
+    float* ppS = smf + cap * Q;   // [cap][Q]
+    float* wS = smf + 2 * cap * Q;  // [cap]
+    for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
+        const int64_t g = a.node_of[b];
+        const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
+        const int P = tr.n_patterns;
+        const int mi = tr.model;
+        const double* V = a.m.V + (int64_t)mi * Q * Q;
+        const double* Vi = a.m.Vinv + (int64_t)mi * Q * Q;
+        const double* lam = a.m.lam + (int64_t)mi * Q;
+        const double mu = a.m.mu[mi];
+        const bool staged = P <= cap;
+        const bool tipb = a.pc_row[b] < 0;
+        const int trow = tipb ? a.f.tip_row[g] : -1;
+        const int64_t mo = a.f.mask_off ? a.f.mask_off[g] : -1;
+        // one pattern's FP32 rows and weights from the stored profiles
+        auto fetch = [&](int p, float* pa, float* pb, float& wgt, double& m64, double& ov64) {
+            const int64_t pr = (a.pp_row[b] + p) * w;
+#pragma unroll
+            for (int j = 0; j < Q; ++j)
+                pb[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
+                                              : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
+            double pcd[Q];
+            if (tipb) {
+                const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) pcd[i] = a.m.lut[code * Q + i];
+            } else {
+                const int64_t cr = (a.pc_row[b] + p) * w;
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    pcd[i] = a.prec == TT_PREC_F32 ? (double)reinterpret_cast<const float*>(a.pc)[cr + i]
+                                                   : reinterpret_cast<const double*>(a.pc)[cr + i];
+                    s += pcd[i];
+                }
+                if (a.prec == TT_PREC_F32)
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) pcd[i] /= s;
+            }
+            double m = a.f.mult[tr.pat_base + p];
+            if (mo >= 0) m *= a.f.masks[mo + p];
+            double ov = 0.0;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) ov += (double)pb[i] * pcd[i];
+            m64 = m;
+            ov64 = m * ov;
+            if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) m *= (1.0 - (double)pb[a.gap]) * (1.0 - pcd[a.gap]);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) pa[i] = (float)pcd[i];
+            wgt = (float)m;
+            return m;
+        };
+        // staging (or just the sums), Hamming distance in FP64
+        double msum = 0.0, ovsum = 0.0;
+        for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            float pa[Q], pb[Q], wgt;
+            double m64, ov64;
+            fetch(p, pa, pb, wgt, m64, ov64);
+            msum += m64;
+            ovsum += ov64;
+            if (staged) {
+                if constexpr (Q == 4) {
+                    reinterpret_cast<float4*>(pcS)[p] = make_float4(pa[0], pa[1], pa[2], pa[3]);
+                    reinterpret_cast<float4*>(ppS)[p] = make_float4(pb[0], pb[1], pb[2], pb[3]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        pcS[p * Q + i] = pa[i];
+                        ppS[p * Q + i] = pb[i];
+                    }
+                }
+                wS[p] = wgt;
+            }
+        }
+        msum = block_sum(msum, red);
+        ovsum = block_sum(ovsum, red);
+        // heavy patterns (weight above kHeavyWeight), the first kHeavyMax in pattern order
+        if (warp == 0) {
+            int count = 0;
+            for (int base = 0; base < P; base += 32) {
+                const int p = base + lane;
+                float wgt = 0.0f;
+                if (p < P) {
+                    if (staged) {
+                        wgt = wS[p];
+                    } else {
+                        float pa[Q], pb[Q];
+                        double m64, ov64;
+                        fetch(p, pa, pb, wgt, m64, ov64);
+                    }
+                }
+                const bool heavy = p < P && wgt > kHeavyWeight;
+                const unsigned bal = __ballot_sync(0xffffffffu, heavy);
+                const int pos = count + __popc(bal & ((1u << lane) - 1u));
+                if (heavy && pos < kHeavyMax) hidx[pos] = p;
+                count += __popc(bal);
+            }
+            if (lane == 0) {
+                hcount = count < kHeavyMax ? count : kHeavyMax;
+                hall = count;
+            }
+        }
+        __syncthreads();
+        const int H = hcount;
+        const int hlast = H > 0 ? hidx[H - 1] : -1;
+        const bool all_heavy_listed = hall <= kHeavyMax;
+        for (int h = threadIdx.x; h < H; h += blockDim.x) {
+            float pa[Q], pb[Q], wgt;
+            double m64, ov64;
+            const int p = hidx[h];
+            const double m = fetch(p, pa, pb, wgt, m64, ov64);
+            // FP64 child profile again (fetch rounds it to FP32)
+            double pcd[Q];
+            if (tipb) {
+                const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) pcd[i] = a.m.lut[code * Q + i];
+            } else {
+                const int64_t cr = (a.pc_row[b] + p) * w;
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    pcd[i] = a.prec == TT_PREC_F32 ? (double)reinterpret_cast<const float*>(a.pc)[cr + i]
+                                                   : reinterpret_cast<const double*>(a.pc)[cr + i];
+                    s += pcd[i];
+                }
+                if (a.prec != TT_PREC_F32) s = 1.0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) pcd[i] /= s;
+            }
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                double x = 0.0, y = 0.0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    x = fma(pcd[i], V[i * Q + k], x);
+                    y = fma(Vi[k * Q + i], (double)pb[i], y);
+                }
+                hu[h][k] = x * y;
+            }
+            hw[h] = m;
+        }
+        __syncthreads();
+        double hamming = 1.0 - ovsum / msum;
+        hamming = hamming > 0.0 ? hamming : 0.0;
+        auto f = [&](double s) -> double {
+            const double t = s * s;
+            if (warp == 0) {
+                if (lane < Q) Ed[lane] = exp(mu * lam[lane] * t);
+                __syncwarp();
+                if (lane < Q * Q) {
+                    const int i = lane / Q, j = lane - (lane / Q) * Q;
+                    double v = 0.0;
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) v = fma(V[i * Q + k], Ed[k] * Vi[k * Q + j], v);
+                    Pt[lane] = (float)(v > 0.0 ? v : 0.0);
+                }
+                double hs = 0.0;
+                for (int h = lane; h < H; h += 32) {
+                    double res = 0.0;
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) res = fma(hu[h][k], Ed[k], res);
+                    hs = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), hs);
+                }
+                hs = warp_sum(hs);
+                if (lane == 0) hsum_s = hs;
+            }
+            __syncthreads();
+            // read before the CTA-wide sum: warp 0 rewrites these for the next evaluation as soon
+            // as that sum's barriers have been passed
+            const double hs = hsum_s;
+            float Pm[Q * Q];
+#pragma unroll
+            for (int e = 0; e < Q * Q; ++e) Pm[e] = Pt[e];
+            float sacc = 0.0f, c = 0.0f;
+            for (int p = threadIdx.x; p < P; p += blockDim.x) {
+                float pa[Q], pb[Q], wgt;
+                if (staged) {
+                    if constexpr (Q == 4) {
+                        const float4 b4 = reinterpret_cast<const float4*>(ppS)[p];
+                        const float4 a4 = reinterpret_cast<const float4*>(pcS)[p];
+                        pb[0] = b4.x; pb[1] = b4.y; pb[2] = b4.z; pb[3] = b4.w;
+                        pa[0] = a4.x; pa[1] = a4.y; pa[2] = a4.z; pa[3] = a4.w;
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) {
+                            pb[i] = ppS[p * Q + i];
+                            pa[i] = pcS[p * Q + i];
+                        }
+                    }
+                    wgt = wS[p];
+                } else {
+                    double m64, ov64;
+                    fetch(p, pa, pb, wgt, m64, ov64);
+                }
+                if (wgt > kHeavyWeight && (all_heavy_listed || p <= hlast)) continue;  // evaluated in FP64
+                float res = 0.0f;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    float v = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < Q; ++j) v = fmaf(Pm[i * Q + j], pb[j], v);
+                    res = fmaf(pa[i], v, res);
+                }
+                const float y = wgt * logf(res + 1e-24f) - c;
+                const float tsum = sacc + y;
+                c = (tsum - sacc) - y;
+                sacc = tsum;
+            }
+            const double tot = block_sum((double)sacc - (double)c, red);
+            return -(tot + hs) + exp(t * t / 10000.0);
+        };
+        BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
+        if (threadIdx.x == 0) {
+            a.t_out[b] = r.state == 0 ? r.x * r.x : hamming;
+            if (a.info) a.info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
+        }
+        __syncthreads();
+    }
+}
+
 template <int QT>
 static void launch_t_grid(const ProfParams& a, int blocks, size_t smem, cudaStream_t s) {
     static bool configured[64] = {};
@@ -905,6 +1155,30 @@ extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m
     a.t_out = t_out;
     a.info = info;
     cudaStream_t s = as_stream(stream);
+    if (prec == TT_PREC_F32 && (q == 4 || q == 5)) {
+        // FP32 profiles, small alphabets: FP32 objective, two CTAs per SM with 100 KB of pattern rows
+        const size_t smem = 100 * 1024;
+        ProfParams b32 = a;
+        b32.cap = (int)(smem / ((2 * q + 1) * sizeof(float)));
+        const int64_t cap2 = 2 * sms;
+        const int fb = (int)(n < cap2 ? n : cap2);
+        static bool configured[2][64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const int qi = q == 4 ? 0 : 1;
+        if (dev < 0 || dev >= 64 || !configured[qi][dev]) {
+            if (q == 4)
+                cudaFuncSetAttribute(optimal_t_profiles_f32_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+            else
+                cudaFuncSetAttribute(optimal_t_profiles_f32_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+            if (dev >= 0 && dev < 64) configured[qi][dev] = true;
+        }
+        if (q == 4) optimal_t_profiles_f32_kernel<4><<<fb, 256, smem, s>>>(b32);
+        else optimal_t_profiles_f32_kernel<5><<<fb, 256, smem, s>>>(b32);
+        return check_launch("tt_optimal_t_profiles");
+    }
     switch (q) {
         case 4: launch_t_profiles<4>(a, blocks, smem_max, s); break;
         case 5: launch_t_profiles<5>(a, blocks, smem_max, s); break;

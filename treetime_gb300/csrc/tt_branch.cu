@@ -841,10 +841,11 @@ __global__ void __launch_bounds__(256) prob_t_profiles_grid_f32_kernel(ProfParam
 // optimal_t_profiles_kernel evaluated as in prob_t_profiles_grid_f32_kernel -- per evaluation
 // warp 0 forms P(t) in FP64 (kept as FP32) and the heavy patterns' FP64 terms, then every thread
 // sums w logf(pc.P(t).pp + 1e-24) over its patterns with compensated FP32 sums, added across the
-// CTA in FP64.  Patterns are staged in shared memory (FP32 rows: normalised child profile, parent
-// profile, weight) when the tree has at most `cap` of them, else read from their stored rows at
-// every evaluation.  The search, bracket, Hamming distance and results are those of the FP64
-// kernel (the Hamming distance is summed in FP64).
+// CTA in FP64.  Patterns are staged as FP32 rows (normalised child profile, parent profile,
+// weight) in shared memory when the tree has at most `cap` of them, else in the CTA's slice of the
+// workspace when it is large enough, else read from their stored rows at every evaluation.  The
+// search, bracket, Hamming distance and results are those of the FP64 kernel (the Hamming
+// distance is summed in FP64).
 template <int Q>
 __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams a) {
     extern __shared__ float smf[];
@@ -864,9 +865,6 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
         inv_tab[j] = 1.0 / F;
     }
     const int cap = a.cap;
-    float* pcS = smf;             // [cap][Q] (float4 rows for Q = 4)
-    float* ppS = smf + cap * Q;   // [cap][Q]
-    float* wS = smf + 2 * cap * Q;  // [cap]
     for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
         const int64_t g = a.node_of[b];
         const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
@@ -876,7 +874,20 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
         const double* Vi = a.m.Vinv + (int64_t)mi * Q * Q;
         const double* lam = a.m.lam + (int64_t)mi * Q;
         const double mu = a.m.mu[mi];
-        const bool staged = P <= cap;
+        // FP32 rows: [stride][Q] child, [stride][Q] parent (float4 rows for Q = 4), [stride] weight
+        float* rows = nullptr;
+        int stride = 0;
+        if (P <= cap) {
+            rows = smf;
+            stride = cap;
+        } else if (a.work && a.work_cta * 8 >= (int64_t)((P + 3) & ~3) * (2 * Q + 1) * 4) {
+            rows = reinterpret_cast<float*>(a.work + (int64_t)blockIdx.x * a.work_cta);
+            stride = (P + 3) & ~3;
+        }
+        const bool staged = rows != nullptr;
+        float* pcS = rows;
+        float* ppS = staged ? rows + (int64_t)stride * Q : nullptr;
+        float* wS = staged ? rows + (int64_t)stride * Q * 2 : nullptr;
         const bool tipb = a.pc_row[b] < 0;
         const int trow = tipb ? a.f.tip_row[g] : -1;
         const int64_t mo = a.f.mask_off ? a.f.mask_off[g] : -1;
@@ -970,8 +981,8 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
         }
         __syncthreads();
         const int H = hcount;
-        const int hlast = H > 0 ? hidx[H - 1] : -1;
         const bool all_heavy_listed = hall <= kHeavyMax;
+        // (rows: the listed patterns' FP32 weights are zeroed below, after their FP64 terms)
         for (int h = threadIdx.x; h < H; h += blockDim.x) {
             float pa[Q], pb[Q], wgt;
             double m64, ov64;
@@ -1009,6 +1020,19 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
             hw[h] = m;
         }
         __syncthreads();
+        if (staged)
+            for (int h = threadIdx.x; h < H; h += blockDim.x) wS[hidx[h]] = 0.0f;
+        // whether pattern p is one of the listed heavy patterns (the list is in pattern order)
+        auto listed = [&](int p) -> bool {
+            if (all_heavy_listed) return true;
+            int lo = 0, hi = H - 1;
+            while (lo <= hi) {
+                const int mid = (lo + hi) >> 1;
+                if (hidx[mid] == p) return true;
+                if (hidx[mid] < p) lo = mid + 1; else hi = mid - 1;
+            }
+            return false;
+        };
         double hamming = 1.0 - ovsum / msum;
         hamming = hamming > 0.0 ? hamming : 0.0;
         auto f = [&](double s) -> double {
@@ -1057,11 +1081,36 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                         }
                     }
                     wgt = wS[p];
-                } else {
-                    double m64, ov64;
-                    fetch(p, pa, pb, wgt, m64, ov64);
+                } else {  // from the stored rows, FP32 only
+                    const int64_t pr = (a.pp_row[b] + p) * w;
+#pragma unroll
+                    for (int j = 0; j < Q; ++j)
+                        pb[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
+                                                      : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
+                    if (tipb) {
+                        const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) pa[i] = (float)a.m.lut[code * Q + i];
+                    } else {
+                        const int64_t cr = (a.pc_row[b] + p) * w;
+                        float sc = 0.0f;
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) {
+                            pa[i] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pc)[cr + i]
+                                                          : (float)reinterpret_cast<const double*>(a.pc)[cr + i];
+                            sc += pa[i];
+                        }
+                        if (a.prec == TT_PREC_F32) {
+                            const float inv = 1.0f / sc;
+#pragma unroll
+                            for (int i = 0; i < Q; ++i) pa[i] *= inv;
+                        }
+                    }
+                    wgt = (float)a.f.mult[tr.pat_base + p];
+                    if (mo >= 0) wgt *= (float)a.f.masks[mo + p];
+                    if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) wgt *= (1.0f - pb[a.gap]) * (1.0f - pa[a.gap]);
+                    if (wgt > 0.5f * kHeavyWeight && H > 0 && listed(p)) continue;  // evaluated in FP64
                 }
-                if (wgt > kHeavyWeight && (all_heavy_listed || p <= hlast)) continue;  // evaluated in FP64
                 float res = 0.0f;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
@@ -1162,6 +1211,11 @@ extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m
         b32.cap = (int)(smem / ((2 * q + 1) * sizeof(float)));
         const int64_t cap2 = 2 * sms;
         const int fb = (int)(n < cap2 ? n : cap2);
+        // workspace slices for trees with more patterns than shared memory holds (even, so that
+        // every slice starts on a 16-byte boundary)
+        b32.work = workspace;
+        b32.work_cta = workspace && workspace_bytes > 0 ? (workspace_bytes / (int64_t)sizeof(double) / fb) & ~1LL : 0;
+        if (b32.work_cta <= 0) b32.work = nullptr;
         static bool configured[2][64] = {};
         int dev = 0;
         cudaGetDevice(&dev);

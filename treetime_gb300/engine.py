@@ -769,7 +769,7 @@ def optimal_t_profiles_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, pr
     n = int(d_node.numel())
     tout = t.empty(n, dtype=t.float64, device=dev)
     info = t.empty(n, dtype=t.int32, device=dev)
-    ws, ws_bytes = _profile_workspace(forest, n, dev)
+    ws, ws_bytes = _profile_workspace(forest, n, dev, precision)
     check(lib.tt_optimal_t_profiles(C.byref(forest.struct), C.byref(model.struct), n, _p(d_node), _p(pp),
                                     _p(d_pp_row), _p(pc), _p(d_pc_row),
                                     _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64,
@@ -781,19 +781,30 @@ def optimal_t_profiles_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, pr
 _PROFILE_WS = {}
 
 
-def _profile_workspace(forest, n, dev):
-    """Device FP64 workspace for the per-pattern coefficients that do not fit
-    in the profile-Brent kernel's shared memory (one slice per persistent
-    CTA); one buffer per device and stream, grown when a call needs more."""
+def _profile_workspace(forest, n, dev, precision="f64"):
+    """Device workspace of the profile-Brent and grid kernels (one slice per
+    persistent CTA): FP64 kernels, the per-pattern coefficients that do not fit
+    in shared memory; the FP32 Brent kernel (FP32 profiles, up to 5 states),
+    the FP32 pattern rows of trees with more patterns than its shared memory
+    holds.  One buffer per device and stream, grown when a call needs more."""
     t = torch()
     q = forest.q
-    cap = (200 * 1024) // ((q + 1) * 8)
     p_max = int(np.max(forest.trees_host["n_patterns"])) if len(forest.trees_host) else 0
-    over = max(0, p_max - cap)
-    if over == 0 or n == 0:
-        return None, 0
-    blocks = min(n, _lib.load().tt_device_sm_count())
-    need = blocks * over * (q + 1) * 8
+    sms = _lib.load().tt_device_sm_count()
+    if precision == "f32" and q <= 5 and q >= 4:
+        cap = (100 * 1024) // ((2 * q + 1) * 4)
+        if p_max <= cap or n == 0:
+            return None, 0
+        blocks = min(n, 2 * sms)
+        per = -(-(((p_max + 3) & ~3) * (2 * q + 1) * 4) // 16) * 16
+        need = blocks * per
+    else:
+        cap = (200 * 1024) // ((q + 1) * 8)
+        over = max(0, p_max - cap)
+        if over == 0 or n == 0:
+            return None, 0
+        blocks = min(n, sms)
+        need = blocks * over * (q + 1) * 8
     key = (str(dev), t.cuda.current_stream(dev).cuda_stream)
     buf = _PROFILE_WS.get(key)
     if buf is None or buf.numel() < need // 8:

@@ -2,10 +2,13 @@
 implemented on the GPU.
 
 The mixin replaces exactly the hot-path methods of treetime/treeanc.py:
-``_ml_anc_marginal`` (:762), ``_ml_anc_joint`` (:934),
+``_ml_anc_marginal`` (:762), ``_ml_anc_joint`` (:934), ``_fitch_anc`` (:575),
 ``optimize_branch_lengths_joint`` (:1176), ``optimal_branch_length`` (:1244),
 ``optimal_marginal_branch_length`` (:1272), ``optimize_tree_marginal``
-(:1297) and ``prune_short_branches`` (:1475).  It reads only the state
+(:1297), ``prune_short_branches`` (:1475), ``get_branch_mutation_matrix``
+(:1085), ``infer_gtr`` (:1500) and ``infer_gtr_iterative`` (:1633), and adds
+``branch_length_grids`` (the values of BranchLenInterpolator,
+treetime/branch_len_interpolator.py:36-125).  It reads only the state
 TreeTime's own classes keep (``tree``, ``data``, ``gtr``, ``rng``,
 ``sequence_reconstruction``, ``reconstructed_tip_sequences``,
 ``use_mutation_length``, ``ignore_gaps``, ``logger``), so it composes with

@@ -786,6 +786,91 @@ def run_fitch(args):
     return out
 
 
+BRENT_WORKLOAD = ("brent: profile-mode Brent (optimal_marginal_branch_length, scipy's Brent parameters, tol 1e-10) "
+                  "on every branch of the 2000-tip x 30000-site tree from its FP32 reconstruction's profiles")
+
+
+def run_brent(args):
+    """--workload brent: the branch-length optimiser of optimize_tree_marginal
+    -- profile-mode Brent on all 3,998 branches in one launch per branch group
+    (internal nodes, tips) -- from the FP32 reconstruction (FP32 objective);
+    the FP64 kernel on an FP64 reconstruction beside it.  L2 flushed before
+    every step."""
+    import torch
+    from treetime_gb300 import TreeAnc, engine
+    from treetime_gb300.tree import parse_newick, to_newick
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t, wl = build_workload()
+    t.device = dev
+    t.infer_ancestral_sequences(marginal=True)
+    nodes = [n for n in t.tree.find_clades() if n.up is not None]
+    P = t.data.compressed_length
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def timed(tt, nn, k, w):
+        for _ in range(w):
+            tt._marginal_branch_lengths(nn, 1e-10)
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = tt._marginal_branch_lengths(nn, 1e-10)
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts) * 1e3, res
+
+    with ClockSampler(local) as clk:
+        ms, r32 = timed(t, nodes, args.steps, args.warmup)
+    ms = _reduce_max(ms, dev, world)
+    t64 = TreeAnc(tree=parse_newick(to_newick(t.tree)), aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision="f64",
+                  device=dev)
+    t64.infer_ancestral_sequences(marginal=True)
+    n64 = [n for n in t64.tree.find_clades() if n.up is not None]
+    ms64, r64 = timed(t64, n64, 3, 1)
+    if rank != 0:
+        return None
+    rel = np.abs(r32 - r64) / np.maximum(np.abs(r64), 1e-12)
+    out = {
+        "metric": "branches optimised/s (profile-mode Brent, all branches of one tree)",
+        "value": world * len(nodes) / (ms * 1e-3), "unit": "branches/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
+        "config": {"workload": BRENT_WORKLOAD, "branches": len(nodes), "patterns": P,
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU",
+                   "timing": "host clock around TreeAnc._marginal_branch_lengths (uploads of the branch lists, "
+                             "two launches, the lengths back)"},
+        "fp64_path": {"ms_per_step": ms64, "value": len(n64) / (ms64 * 1e-3),
+                      "note": "FP64 reconstruction, FP64 objective (optimal_t_profiles_kernel)"},
+        "f32_vs_f64_lengths": {"median_rel": float(np.median(rel)), "p99_rel": float(np.percentile(rel, 99)),
+                               "max_rel": float(rel.max())},
+        "roofline": {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                     "traffic": None, "note": "~30 dependent objective evaluations per branch, each a CTA-wide sum"},
+        "e2e": {"value": len(nodes) / (ms * 1e-3), "unit": "branches/s", "ms_per_step": ms,
+                "h2d_bytes_per_step": len(nodes) * 20, "d2h_bytes_per_step": len(nodes) * 12},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import anc
+        mult = t.data.multiplicity()
+        done, secs = 0, 0.0
+        for n in n64[::50]:
+            pp, pc = np.asarray(n.marginal_outgroup_LH), np.asarray(n.marginal_subtree_LH)
+            t0 = time.perf_counter()
+            anc.optimal_t_compressed(t64.gtr, (pp, pc), mult, profiles=True, tol=1e-10)
+            secs += time.perf_counter() - t0
+            done += 1
+            if secs > 20.0:
+                break
+        out["cpu_baseline"] = {"value": done / secs, "unit": "branches/s", "cores": 1, "kind": "port",
+                               "sample": "%d branches (every 50th) through the numpy restatement of TreeTime's "
+                                         "optimal_t_compressed(profiles=True) with scipy's Brent, 1 process" % done,
+                               "seconds": secs}
+    return out
+
+
 C3_WORKLOAD = ("c3: 256 independent coalescent trees, tips log-uniform in [50, 5000], sites log-uniform in "
                "[1k, 30k], branch means log-uniform in [1e-4, 0.05], a random GTR per tree; the whole batch is "
                "one forest, one captured launch sequence per step")
@@ -1165,7 +1250,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf", "fitch"],
+    ap.add_argument("--workload", default="c1",
+                    choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf", "fitch", "brent"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
@@ -1184,7 +1270,7 @@ def main():
         from treetime_gb300 import build
         build.build()
         res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4, "blgrid": run_blgrid,
-               "gtrinf": run_gtrinf, "fitch": run_fitch}[args.workload](args)
+               "gtrinf": run_gtrinf, "fitch": run_fitch, "brent": run_brent}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

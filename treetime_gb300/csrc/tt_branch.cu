@@ -846,6 +846,10 @@ __global__ void __launch_bounds__(256) prob_t_profiles_grid_f32_kernel(ProfParam
 // workspace when it is large enough, else read from their stored rows at every evaluation.  The
 // search, bracket, Hamming distance and results are those of the FP64 kernel (the Hamming
 // distance is summed in FP64).
+// Barrier 1 over all threads of the CTA, for code where warps reach it from different places (the
+// non-aligned form: a warp may arrive from another instruction than the others).
+__device__ __forceinline__ void role_barrier() { asm volatile("barrier.sync 1, %0;" ::"r"(blockDim.x) : "memory"); }
+
 template <int Q>
 __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams a) {
     extern __shared__ float smf[];
@@ -856,7 +860,8 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
     __shared__ int hcount, hall;
     __shared__ float Pt[Q * Q];
     __shared__ double Ed[Q];
-    __shared__ double hsum_s;
+    __shared__ double red_total;
+    __shared__ int go;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int w = a.f.width;
     for (int j = threadIdx.x; j < 129; j += blockDim.x) {
@@ -929,14 +934,55 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
             wgt = (float)m;
             return m;
         };
-        // staging (or just the sums), Hamming distance in FP64
-        double msum = 0.0, ovsum = 0.0;
+        // one pattern's FP32 rows and weight (mult*mask*non_gap) and its mult*mask, FP32 only
+        auto fetch32 = [&](int p, float* pa, float* pb, float& wgt, float& m32) {
+            const int64_t pr = (a.pp_row[b] + p) * w;
+#pragma unroll
+            for (int j = 0; j < Q; ++j)
+                pb[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
+                                              : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
+            if (tipb) {
+                const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) pa[i] = (float)a.m.lut[code * Q + i];
+            } else {
+                const int64_t cr = (a.pc_row[b] + p) * w;
+                float sc = 0.0f;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    pa[i] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pc)[cr + i]
+                                                  : (float)reinterpret_cast<const double*>(a.pc)[cr + i];
+                    sc += pa[i];
+                }
+                if (a.prec == TT_PREC_F32) {
+                    const float inv = 1.0f / sc;
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) pa[i] *= inv;
+                }
+            }
+            m32 = (float)a.f.mult[tr.pat_base + p];
+            if (mo >= 0) m32 *= (float)a.f.masks[mo + p];
+            wgt = m32;
+            if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) wgt *= (1.0f - pb[a.gap]) * (1.0f - pa[a.gap]);
+        };
+        // staging and the Hamming distance (compensated FP32 sums, added across the CTA in FP64)
+        float ms = 0.0f, msc = 0.0f, os = 0.0f, osc = 0.0f;
         for (int p = threadIdx.x; p < P; p += blockDim.x) {
-            float pa[Q], pb[Q], wgt;
-            double m64, ov64;
-            fetch(p, pa, pb, wgt, m64, ov64);
-            msum += m64;
-            ovsum += ov64;
+            float pa[Q], pb[Q], wgt, m32;
+            fetch32(p, pa, pb, wgt, m32);
+            float ov = 0.0f;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) ov = fmaf(pb[i], pa[i], ov);
+            {
+                const float y = m32 - msc, t2 = ms + y;
+                msc = (t2 - ms) - y;
+                ms = t2;
+            }
+            {
+                const float y = m32 * ov - osc, t2 = os + y;
+                osc = (t2 - os) - y;
+                os = t2;
+            }
             if (staged) {
                 if constexpr (Q == 4) {
                     reinterpret_cast<float4*>(pcS)[p] = make_float4(pa[0], pa[1], pa[2], pa[3]);
@@ -951,8 +997,8 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                 wS[p] = wgt;
             }
         }
-        msum = block_sum(msum, red);
-        ovsum = block_sum(ovsum, red);
+        const double msum = block_sum((double)ms - (double)msc, red);
+        const double ovsum = block_sum((double)os - (double)osc, red);
         // heavy patterns (weight above kHeavyWeight), the first kHeavyMax in pattern order
         if (warp == 0) {
             int count = 0;
@@ -963,9 +1009,8 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                     if (staged) {
                         wgt = wS[p];
                     } else {
-                        float pa[Q], pb[Q];
-                        double m64, ov64;
-                        fetch(p, pa, pb, wgt, m64, ov64);
+                        float pa[Q], pb[Q], m32;
+                        fetch32(p, pa, pb, wgt, m32);
                     }
                 }
                 const bool heavy = p < P && wgt > kHeavyWeight;
@@ -982,13 +1027,12 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
         __syncthreads();
         const int H = hcount;
         const bool all_heavy_listed = hall <= kHeavyMax;
-        // (rows: the listed patterns' FP32 weights are zeroed below, after their FP64 terms)
+        // FP64 coefficients and weights of the listed heavy patterns, from their stored rows
         for (int h = threadIdx.x; h < H; h += blockDim.x) {
             float pa[Q], pb[Q], wgt;
             double m64, ov64;
             const int p = hidx[h];
             const double m = fetch(p, pa, pb, wgt, m64, ov64);
-            // FP64 child profile again (fetch rounds it to FP32)
             double pcd[Q];
             if (tipb) {
                 const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
@@ -996,16 +1040,16 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                 for (int i = 0; i < Q; ++i) pcd[i] = a.m.lut[code * Q + i];
             } else {
                 const int64_t cr = (a.pc_row[b] + p) * w;
-                double s = 0.0;
+                double sc = 0.0;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
                     pcd[i] = a.prec == TT_PREC_F32 ? (double)reinterpret_cast<const float*>(a.pc)[cr + i]
                                                    : reinterpret_cast<const double*>(a.pc)[cr + i];
-                    s += pcd[i];
+                    sc += pcd[i];
                 }
-                if (a.prec != TT_PREC_F32) s = 1.0;
+                if (a.prec != TT_PREC_F32) sc = 1.0;
 #pragma unroll
-                for (int i = 0; i < Q; ++i) pcd[i] /= s;
+                for (int i = 0; i < Q; ++i) pcd[i] /= sc;
             }
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
@@ -1033,34 +1077,8 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
             }
             return false;
         };
-        double hamming = 1.0 - ovsum / msum;
-        hamming = hamming > 0.0 ? hamming : 0.0;
-        auto f = [&](double s) -> double {
-            const double t = s * s;
-            if (warp == 0) {
-                if (lane < Q) Ed[lane] = exp(mu * lam[lane] * t);
-                __syncwarp();
-                if (lane < Q * Q) {
-                    const int i = lane / Q, j = lane - (lane / Q) * Q;
-                    double v = 0.0;
-#pragma unroll
-                    for (int k = 0; k < Q; ++k) v = fma(V[i * Q + k], Ed[k] * Vi[k * Q + j], v);
-                    Pt[lane] = (float)(v > 0.0 ? v : 0.0);
-                }
-                double hs = 0.0;
-                for (int h = lane; h < H; h += 32) {
-                    double res = 0.0;
-#pragma unroll
-                    for (int k = 0; k < Q; ++k) res = fma(hu[h][k], Ed[k], res);
-                    hs = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), hs);
-                }
-                hs = warp_sum(hs);
-                if (lane == 0) hsum_s = hs;
-            }
-            __syncthreads();
-            // read before the CTA-wide sum: warp 0 rewrites these for the next evaluation as soon
-            // as that sum's barriers have been passed
-            const double hs = hsum_s;
+        // this thread's compensated sum of w log(pc.P(t).pp + 1e-24) over its patterns
+        auto pattern_sum = [&]() -> double {
             float Pm[Q * Q];
 #pragma unroll
             for (int e = 0; e < Q * Q; ++e) Pm[e] = Pt[e];
@@ -1081,34 +1099,9 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                         }
                     }
                     wgt = wS[p];
-                } else {  // from the stored rows, FP32 only
-                    const int64_t pr = (a.pp_row[b] + p) * w;
-#pragma unroll
-                    for (int j = 0; j < Q; ++j)
-                        pb[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
-                                                      : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
-                    if (tipb) {
-                        const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
-#pragma unroll
-                        for (int i = 0; i < Q; ++i) pa[i] = (float)a.m.lut[code * Q + i];
-                    } else {
-                        const int64_t cr = (a.pc_row[b] + p) * w;
-                        float sc = 0.0f;
-#pragma unroll
-                        for (int i = 0; i < Q; ++i) {
-                            pa[i] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pc)[cr + i]
-                                                          : (float)reinterpret_cast<const double*>(a.pc)[cr + i];
-                            sc += pa[i];
-                        }
-                        if (a.prec == TT_PREC_F32) {
-                            const float inv = 1.0f / sc;
-#pragma unroll
-                            for (int i = 0; i < Q; ++i) pa[i] *= inv;
-                        }
-                    }
-                    wgt = (float)a.f.mult[tr.pat_base + p];
-                    if (mo >= 0) wgt *= (float)a.f.masks[mo + p];
-                    if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) wgt *= (1.0f - pb[a.gap]) * (1.0f - pa[a.gap]);
+                } else {
+                    float m32;
+                    fetch32(p, pa, pb, wgt, m32);
                     if (wgt > 0.5f * kHeavyWeight && H > 0 && listed(p)) continue;  // evaluated in FP64
                 }
                 float res = 0.0f;
@@ -1124,13 +1117,65 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                 c = (tsum - sacc) - y;
                 sacc = tsum;
             }
-            const double tot = block_sum((double)sacc - (double)c, red);
-            return -(tot + hs) + exp(t * t / 10000.0);
+            return (double)sacc - (double)c;
         };
-        BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
-        if (threadIdx.x == 0) {
-            a.t_out[b] = r.state == 0 ? r.x * r.x : hamming;
-            if (a.info) a.info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
+        // the CTA-wide sum: every warp's total in red[], added by thread 0 (its result is needed
+        // by warp 0 only)
+        auto cta_sum = [&](double v) -> double {
+            v = warp_sum(v);
+            if (lane == 0) red[warp] = v;
+            role_barrier();
+            if (threadIdx.x == 0) {
+                double s2 = 0.0;
+                for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) s2 += red[w2];
+                red_total = s2;
+            }
+            role_barrier();
+            return red_total;
+        };
+        // Warp 0 runs the search; the other warps only take part in each evaluation's pattern sum.
+        // Per evaluation every thread passes three barriers: P(t) published, warp totals
+        // written, CTA total written; after the search one more releases the other warps.
+        if (warp == 0) {
+            double hamming = 1.0 - ovsum / msum;
+            hamming = hamming > 0.0 ? hamming : 0.0;
+            auto f = [&](double s) -> double {
+                const double t = s * s;
+                if (lane < Q) Ed[lane] = exp(mu * lam[lane] * t);
+                __syncwarp();
+                if (lane < Q * Q) {
+                    const int i = lane / Q, j = lane - (lane / Q) * Q;
+                    double v = 0.0;
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) v = fma(V[i * Q + k], Ed[k] * Vi[k * Q + j], v);
+                    Pt[lane] = (float)(v > 0.0 ? v : 0.0);
+                }
+                double hs = 0.0;
+                for (int h = lane; h < H; h += 32) {
+                    double res = 0.0;
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) res = fma(hu[h][k], Ed[k], res);
+                    hs = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), hs);
+                }
+                hs = warp_sum(hs);
+                if (lane == 0) go = 1;
+                role_barrier();
+                const double tot = cta_sum(pattern_sum());
+                return -(tot + hs) + exp(t * t / 10000.0);
+            };
+            BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
+            if (lane == 0) {
+                a.t_out[b] = r.state == 0 ? r.x * r.x : hamming;
+                if (a.info) a.info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
+                go = 0;
+            }
+            role_barrier();
+        } else {
+            while (true) {
+                role_barrier();
+                if (!go) break;
+                cta_sum(pattern_sum());
+            }
         }
         __syncthreads();
     }

@@ -355,9 +355,9 @@ tt_status tt_prob_t_pairs_grid(int32_t q, int64_t n, const double* counts, const
  * state j, pattern a; [q][q][n_patterns]) and T_ia[i][a] ([q][n_patterns]), both overwritten.
  * Accumulation is deterministic: branches are split into contiguous chunks, each summed in order
  * into its own slice of `workspace` (device FP64) and the slices added in order; the workspace
- * must hold at least (q*q + q) * n_patterns doubles (marginal mode: after n_nodes*q*q values of
- * the arithmetic type, rounded up to 256 bytes, for the offset branch matrices), more allows up
- * to 64 chunks.
+ * must hold at least (q*q + q) * n_patterns doubles (marginal mode: after n_nodes*(q*q + 1) values
+ * of the arithmetic type, rounded up to 256 bytes, for the offset branch matrices and half branch
+ * lengths), more allows up to 64 chunks.
  * tt_mutation_counts ('marginal'): profiles as for tt_optimal_t_profiles, p64 the FP64 branch
  * matrices of tt_branch_pmats; per branch and pattern M = pc_i pp_j (P(t)_ij + 1e-24) normalised,
  * n_ija += M * mult * mask, T_ia += 0.5 t (row and column sums of M) * mult * mask.  FP64 profiles

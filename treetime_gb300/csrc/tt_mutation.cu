@@ -98,15 +98,18 @@ __device__ __forceinline__ double branch_weight(const MutParams& a, const tt_tre
     return m;
 }
 
-// R[g][i][j] = P(t)_ij + 1e-24 for every node, in the counting kernels' arithmetic type.
+// R[g][i][j] = P(t)_ij + 1e-24 for every node and half[g] = t/2, in the counting kernels'
+// arithmetic type (conversions from FP64 cost FP64 issue slots; done once per node here).
 template <typename Tc>
-__global__ void mut_offset_kernel(const double* __restrict__ p64, int64_t n_nodes, int q, int w, Tc* __restrict__ R) {
+__global__ void mut_offset_kernel(const double* __restrict__ p64, const double* __restrict__ bl, int64_t n_nodes,
+                                  int q, int w, Tc* __restrict__ R, Tc* __restrict__ half) {
     const int qq = q * q;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n_nodes * qq;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t g = idx / qq;
         const int e = (int)(idx - g * qq), i = e / q, j = e - (e / q) * q;
         R[idx] = (Tc)(p64[g * q * w + (int64_t)i * w + j] + kSuperTiny);
+        if (e == 0) half[g] = (Tc)(0.5 * bl[g]);
     }
 }
 
@@ -120,7 +123,8 @@ __global__ void mut_offset_kernel(const double* __restrict__ p64, int64_t n_node
 
 // q <= 5: one thread per (pattern, chunk), all sums in registers.
 template <int Q, typename Tin, typename Tc>
-__global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a, const Tc* __restrict__ R) {
+__global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a, const Tc* __restrict__ R,
+                                                                 const Tc* __restrict__ half) {
     const tt_tree tr = a.f.trees[a.tree];
     const int P = a.P;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -134,6 +138,7 @@ __global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a, co
     for (int e = 0; e < Q * Q; ++e) N[e] = Tc(0);
 #pragma unroll
     for (int k = 0; k < Q; ++k) T[k] = Tc(0);
+    const Tc mult = (Tc)a.f.mult[tr.pat_base + p];
     const int64_t b0 = c * a.chunk_len;
     const int64_t b1 = b0 + a.chunk_len < a.n ? b0 + a.chunk_len : a.n;
     for (int64_t b = b0; b < b1; ++b) {
@@ -173,8 +178,13 @@ __global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a, co
             for (int i = 0; i < Q; ++i) s = fma(av[i], Rm[i * Q + j], s);
             aR[j] = s;
         }
-        const Tc cw = (Tc)branch_weight(a, tr, g, p) / tot;
-        const Tc h = (Tc)(0.5 * a.f.bl[g]) * cw;
+        Tc mw = mult;
+        if (a.f.mask_off) {
+            const int64_t mo = a.f.mask_off[g];
+            if (mo >= 0) mw *= (Tc)a.f.masks[mo + p];
+        }
+        const Tc cw = mw / tot;
+        const Tc h = __ldg(half + g) * cw;
 #pragma unroll
         for (int i = 0; i < Q; ++i) {
             const Tc cai = cw * av[i];
@@ -194,7 +204,8 @@ __global__ void __launch_bounds__(256) mut_marginal_small_kernel(MutParams a, co
 // Larger alphabets: one warp per (pattern, chunk); lane l < q holds a_l, b_l, (R.b)_l, (a.R)_l and
 // T_l, and the matrix entries e = l, l + 32, ... of n.
 template <int EPL, typename Tin, typename Tc>
-__global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a, const Tc* __restrict__ R) {
+__global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a, const Tc* __restrict__ R,
+                                                                const Tc* __restrict__ half) {
     const tt_tree tr = a.f.trees[a.tree];
     const int P = a.P;
     const int lane = threadIdx.x & 31;
@@ -243,7 +254,7 @@ __global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a, con
         Tc tot = al * Rb;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, off);
-        const Tc cw = (Tc)branch_weight(a, tr, g, p) / tot;
+        const Tc cw = (Tc)branch_weight(a, tr, g, p) / tot;  // (one per warp and branch)
         const Tc cal = cw * al;
 #pragma unroll
         for (int r = 0; r < EPL; ++r) {
@@ -251,7 +262,7 @@ __global__ void __launch_bounds__(256) mut_marginal_warp_kernel(MutParams a, con
             const Tc bj = __shfl_sync(0xffffffffu, bl, ej[r]);
             if (lane + 32 * r < qq) N[r] = fma(ci * bj, __ldg(Rg + ei[r] * q + ej[r]), N[r]);
         }
-        T = fma((Tc)(0.5 * a.f.bl[g]) * cw, fma(al, Rb, bl * aR), T);
+        T = fma(__ldg(half + g) * cw, fma(al, Rb, bl * aR), T);
     }
     double* out = a.part + (int64_t)c * a.rows * P;
 #pragma unroll
@@ -389,8 +400,8 @@ extern "C" tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, i
     const bool f32 = prec == TT_PREC_F32;
     const int rows = q * q + q;
     const bool small = q <= 5;
-    // workspace: the offset branch matrices R, then the chunk slices
-    const int64_t r_bytes = ((f->n_nodes * q * q * (f32 ? 4 : 8) + 255) / 256) * 256;
+    // workspace: the offset branch matrices R and half branch lengths, then the chunk slices
+    const int64_t r_bytes = ((f->n_nodes * (q * q + 1) * (f32 ? 4 : 8) + 255) / 256) * 256;
     const int chunks = workspace && workspace_bytes > r_bytes
                            ? fit_chunks(workspace_bytes - r_bytes, rows, P, want_chunks(n > 0 ? n : 1, P, small ? 1 : 32))
                            : 0;
@@ -422,13 +433,15 @@ extern "C" tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, i
         if (rblocks > sm_count() * 8) rblocks = sm_count() * 8;
         float* R32 = reinterpret_cast<float*>(workspace);
         double* R64 = workspace;
-        if (f32) mut_offset_kernel<float><<<rblocks, 256, 0, s>>>(p64, f->n_nodes, q, f->width, R32);
-        else mut_offset_kernel<double><<<rblocks, 256, 0, s>>>(p64, f->n_nodes, q, f->width, R64);
+        float* H32 = R32 + f->n_nodes * q * q;
+        double* H64 = R64 + f->n_nodes * q * q;
+        if (f32) mut_offset_kernel<float><<<rblocks, 256, 0, s>>>(p64, f->bl, f->n_nodes, q, f->width, R32, H32);
+        else mut_offset_kernel<double><<<rblocks, 256, 0, s>>>(p64, f->bl, f->n_nodes, q, f->width, R64, H64);
         if (small) {
             dim3 grid((P + 255) / 256, chunks);
 #define TT_MUT_SMALL(QV)                                                                                    \
-    if (f32) mut_marginal_small_kernel<QV, float, float><<<grid, 256, 0, s>>>(a, R32);                     \
-    else mut_marginal_small_kernel<QV, double, double><<<grid, 256, 0, s>>>(a, R64);
+    if (f32) mut_marginal_small_kernel<QV, float, float><<<grid, 256, 0, s>>>(a, R32, H32);                \
+    else mut_marginal_small_kernel<QV, double, double><<<grid, 256, 0, s>>>(a, R64, H64);
             switch (q) {
                 case 2: TT_MUT_SMALL(2) break;
                 case 3: TT_MUT_SMALL(3) break;
@@ -440,8 +453,8 @@ extern "C" tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, i
             dim3 grid((P + 7) / 8, chunks);
             const int epl = (q * q + 31) / 32;
 #define TT_MUT_WARP(E)                                                                                      \
-    if (f32) mut_marginal_warp_kernel<E, float, float><<<grid, 256, 0, s>>>(a, R32);                        \
-    else mut_marginal_warp_kernel<E, double, double><<<grid, 256, 0, s>>>(a, R64);
+    if (f32) mut_marginal_warp_kernel<E, float, float><<<grid, 256, 0, s>>>(a, R32, H32);                   \
+    else mut_marginal_warp_kernel<E, double, double><<<grid, 256, 0, s>>>(a, R64, H64);
             if (epl <= 4) { TT_MUT_WARP(4) }
             else if (epl <= 8) { TT_MUT_WARP(8) }
             else if (epl <= 16) { TT_MUT_WARP(16) }

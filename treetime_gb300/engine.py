@@ -930,7 +930,7 @@ def mutation_counts(forest, model, p64, tree, d_node, pp, d_pp_row, pc, d_pc_row
     n_ija = t.empty((q, q, P), dtype=t.float64, device=dev)
     T_ia = t.empty((q, P), dtype=t.float64, device=dev)
     ws, ws_bytes = _mutation_workspace(dev, q * q + q, P, n, 1 if q <= 5 else 32,
-                                       extra_bytes=forest.n_nodes * q * q * (4 if precision == "f32" else 8))
+                                       extra_bytes=forest.n_nodes * (q * q + 1) * (4 if precision == "f32" else 8))
     check(lib.tt_mutation_counts(C.byref(forest.struct), C.byref(model.struct), int(tree), P, n, _p(d_node), _p(pp),
                                  _p(d_pp_row), _p(pc), _p(d_pc_row),
                                  _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(p64), _p(n_ija),

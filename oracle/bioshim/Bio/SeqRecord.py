@@ -10,3 +10,7 @@ class SeqRecord:
 
     def __len__(self):
         return len(self.seq)
+
+    def upper(self):
+        """A copy with the sequence in upper case (Biopython's SeqRecord.upper)."""
+        return SeqRecord(self.seq.upper(), id=self.id, name=self.name, description=self.description)

@@ -7,6 +7,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source --blgrid   (interpolator grids only)
     python tests/golden/make_golden.py /path/to/treetime-source --infer-gtr   (GTR inference only)
     python tests/golden/make_golden.py /path/to/treetime-source --fitch   (Fitch parsimony only)
+    python tests/golden/make_golden.py /path/to/treetime-source --vcf   (VCF reading and sparse alignments)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -394,6 +395,150 @@ def fitch_cases():
     run_fitch("fitch_aa", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "aa_nogap", "mu": 1.0})
 
 
+def _vcf_haploid(path, ref, aln, rng):
+    """A haploid VCF of an alignment's differences from `ref`: one line per
+    variable column, ALT alleles in order of appearance, deletions of runs of
+    gaps after a reference base written as REF/ALT indels, N as no-calls."""
+    names = list(aln)
+    L = len(ref)
+    lines = ["##fileformat=VCFv4.2", "##source=synthetic",
+             "#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT\t" + "\t".join(names)]
+    pos = 0
+    while pos < L:
+        col = [aln[k][pos] for k in names]
+        dels = [k for k in names if aln[k][pos] == "-"]
+        if dels and pos > 0 and pos + 1 < L and all(aln[k][pos - 1] == ref[pos - 1] for k in dels) \
+                and rng.random() < 0.5:
+            # a one-base deletion written against the previous reference base
+            r = ref[pos - 1:pos + 1]
+            calls = ["1" if aln[k][pos] == "-" else "0" for k in names]
+            lines.append("chr1\t%d\t.\t%s\t%s\t.\tPASS\t.\tGT\t%s" % (pos, r, r[0], "\t".join(calls)))
+            pos += 1
+            continue
+        alts = []
+        calls = []
+        for c in col:
+            if c == ref[pos]:
+                calls.append("0")
+            elif c == "N":
+                calls.append(".")
+            else:
+                a = "*" if c == "-" else c
+                if a not in alts:
+                    alts.append(a)
+                calls.append(str(alts.index(a) + 1))
+        if alts or "." in calls:
+            lines.append("chr1\t%d\t.\t%s\t%s\t.\tPASS\t.\tGT\t%s" % (pos + 1, ref[pos], ",".join(alts) or ".",
+                                                                        "\t".join(calls)))
+        pos += 1
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+
+
+def _vcf_diploid(path):
+    """A diploid VCF with every kind of call TreeTime's reader distinguishes:
+    homozygous and heterozygous substitutions, no-calls, deletions,
+    insertions (with and without a first-base change), insertion plus
+    deletion, '*' and '.' alleles, an invalid allele and a non-GT line."""
+    samples = ["s1", "s2", "s3", "s4"]
+    rows = [
+        (3, "A", "G", ["1/1", "0/1", "./.", "0/0"]),
+        (6, "C", "T,G", ["2/2", "1|1", "0/2", "./."]),
+        (10, "GTA", "G", ["1/1", "0/1", "./.", "0/0"]),
+        (15, "T", "TAC", ["1/1", "0/1", "0/0", "./."]),
+        (18, "A", "GCC", ["1/1", "0/0", "0/0", "0/0"]),
+        (22, "GC", "GCC,G", ["1/1", "2/2", "0/1", "0/0"]),
+        (25, "T", "*", ["1/1", "0/0", "0/0", "0/0"]),
+        (27, "C", ".", ["1/1", "0/0", "0/0", "0/0"]),
+        (29, "A", "<DEL>", ["1/1", "0/0", "0/0", "0/0"]),
+        (31, "G", "a", ["1/1", "0/0", "1/1", "0/0"]),
+        (33, "T", "C", ["0/0", "0/0", "1/1", "1/1"]),
+        (35, "CA", "C,CTT", ["./.", "0/2", "2/2", "1/1"]),
+    ]
+    lines = ["##fileformat=VCFv4.2", "#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT\t" +
+             "\t".join(samples)]
+    for pos, r, a, calls in rows:
+        lines.append("chr1\t%d\t.\t%s\t%s\t.\tPASS\t.\tGT:DP\t%s" % (pos, r, a,
+                                                                       "\t".join(c + ":7" for c in calls)))
+    lines.append("chr1\t37\t.\tA\tT\t.\tPASS\t.\tDP\t3\t3\t3\t3")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+
+
+def vcf_cases(ref_path):
+    """read_vcf on a diploid file exercising every call type and on a haploid
+    file derived from a simulated alignment; for the latter also the sparse
+    compression of SequenceData and a marginal reconstruction by TreeAnc."""
+    import tempfile
+    from treetime import TreeAnc
+    from treetime.vcf_utils import read_vcf
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+
+    def flat(d):
+        keys = sorted((k, p) for k, v in d.items() for p in v)
+        return (np.array([k for k, _ in keys]), np.array([p for _, p in keys], dtype=np.int64),
+                np.array([d[k][p] for k, p in keys]))
+
+    tmp = tempfile.mkdtemp()
+    out = {}
+    # diploid
+    vcf = os.path.join(tmp, "d.vcf")
+    _vcf_diploid(vcf)
+    res = read_vcf(vcf)
+    out["d_vcf_text"] = np.array(open(vcf).read())
+    out["d_seq_name"], out["d_seq_pos"], out["d_seq_chr"] = flat(res["sequences"])
+    out["d_ins_name"], out["d_ins_pos"], out["d_ins_str"] = flat(res["insertions"])
+    out["d_ins_keys"] = np.array(sorted(res["insertions"].keys()))
+    out["d_positions"] = np.array(res["positions"], dtype=np.int64)
+    out["d_ploidy"] = res["metadata"]["ploidy"]
+    out["d_chrom"] = res["metadata"]["chrom"]
+    # haploid, from a simulated alignment
+    rng = np.random.default_rng(51)
+    tree = synth.coalescent_tree(20, 0.02, rng)
+    g = GTR.custom(mu=1.0, pi=np.ones(5), W=np.ones((5, 5)), alphabet="nuc")
+    L = 400
+    states = synth.evolve(tree, g, L, rng)
+    aln = synth._to_text(states, g.alphabet, 0.0, rng)
+    ref = "".join(rng.choice(list("ACGT"), size=L))
+    ref = "".join(max("ACGT", key=lambda c: sum(aln[k][i] == c for k in aln)) if rng.random() < 0.9 else ref[i]
+                  for i in range(L))
+    ref = ref[:100] + "NN" + ref[102:]
+    for k in list(aln):
+        s = np.array(list(aln[k]))
+        r = rng.random(L)
+        s[r < 0.02] = "N"
+        aln[k] = "".join(s)
+    vcf = os.path.join(tmp, "h.vcf")
+    _vcf_haploid(vcf, ref, aln, rng)
+    fa = os.path.join(tmp, "ref.fasta")
+    with open(fa, "w") as fh:
+        fh.write(">ref\n" + ref + "\n")
+    res = read_vcf(vcf, fa)
+    out["h_vcf_text"] = np.array(open(vcf).read())
+    out["h_ref"] = np.array(res["reference"])
+    out["h_seq_name"], out["h_seq_pos"], out["h_seq_chr"] = flat(res["sequences"])
+    out["h_names"] = np.array(list(res["sequences"].keys()))
+    out["h_positions"] = np.array(res["positions"], dtype=np.int64)
+    nwk = to_newick(tree)
+    out["h_newick"] = np.array(nwk)
+    from Bio import Phylo
+    gtr_nuc = _ref_gtr("gtr", {"pi": np.ones(5), "W": np.ones((5, 5)), "alphabet": "nuc", "mu": 1.0})
+    t = TreeAnc(tree=Phylo.read(io.StringIO(nwk), "newick"), aln=res["sequences"], ref=res["reference"],
+                gtr=gtr_nuc, verbose=0)
+    d = t.data
+    out["h_comp_names"] = np.array(list(d.compressed_alignment.keys()))
+    out["h_comp_codes"] = np.stack([_codes(d.compressed_alignment[k]) for k in d.compressed_alignment])
+    out["h_mult"] = d.multiplicity()
+    out["h_f2c"] = d.full_to_compressed_sequence_map
+    out["h_const_amb"] = np.array(sorted(d.inferred_const_sites), dtype=np.int64)
+    t.infer_ancestral_sequences(marginal=True)
+    out["h_marg_total_LH"] = t.tree.total_sequence_LH
+    out["h_marg_sequence_LH"] = t.tree.sequence_LH
+    np.savez_compressed(os.path.join(HERE, "vcf_cases.npz"), **out)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -543,5 +688,8 @@ if __name__ == "__main__":
     elif "--fitch" in sys.argv:
         _setup(ref)
         fitch_cases()
+    elif "--vcf" in sys.argv:
+        _setup(ref)
+        vcf_cases(ref)
     else:
         main(ref)

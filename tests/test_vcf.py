@@ -1,0 +1,91 @@
+"""VCF reading and sparse alignments against TreeTime's own results
+(tests/golden/vcf_cases.npz, made by running TreeTime's read_vcf, its
+SequenceData on the sparse alignment and a marginal reconstruction).  CPU
+only, except the reconstruction."""
+
+import os
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from treetime_gb300.vcf import read_vcf
+
+G = gc.load("vcf_cases")
+
+
+def _write(tmp_path, name, text):
+    p = os.path.join(str(tmp_path), name)
+    with open(p, "w") as fh:
+        fh.write(str(text))
+    return p
+
+
+def _flat(d):
+    keys = sorted((k, p) for k, v in d.items() for p in v)
+    return ([k for k, _ in keys], [p for _, p in keys], [d[k][p] for k, p in keys])
+
+
+def test_read_vcf_diploid_calls_match_treetime(tmp_path, capsys):
+    res = read_vcf(_write(tmp_path, "d.vcf", G["d_vcf_text"]))
+    names, pos, chars = _flat(res["sequences"])
+    assert names == G["d_seq_name"].tolist()
+    assert pos == G["d_seq_pos"].tolist()
+    assert chars == G["d_seq_chr"].tolist()
+    names, pos, strs = _flat(res["insertions"])
+    assert names == G["d_ins_name"].tolist() and pos == G["d_ins_pos"].tolist() and strs == G["d_ins_str"].tolist()
+    assert sorted(res["insertions"].keys()) == G["d_ins_keys"].tolist()
+    assert res["positions"] == G["d_positions"].tolist()
+    assert res["metadata"]["ploidy"] == int(G["d_ploidy"])
+    assert res["metadata"]["chrom"] == str(G["d_chrom"])
+    assert "invalid allele" in capsys.readouterr().out
+
+
+def test_read_vcf_haploid_with_reference_matches_treetime(tmp_path):
+    ref = _write(tmp_path, "ref.fasta", ">ref\n" + str(G["h_ref"]) + "\n")
+    res = read_vcf(_write(tmp_path, "h.vcf", G["h_vcf_text"]), ref)
+    assert res["reference"] == str(G["h_ref"])
+    names, pos, chars = _flat(res["sequences"])
+    assert names == G["h_seq_name"].tolist()
+    assert pos == G["h_seq_pos"].tolist()
+    assert chars == G["h_seq_chr"].tolist()
+    assert list(res["sequences"].keys()) == G["h_names"].tolist()
+    assert res["positions"] == G["h_positions"].tolist()
+
+
+def test_sparse_compression_matches_treetime(tmp_path):
+    from treetime_gb300.seqdata import SequenceData
+    ref = _write(tmp_path, "ref.fasta", ">ref\n" + str(G["h_ref"]) + "\n")
+    res = read_vcf(_write(tmp_path, "h.vcf", G["h_vcf_text"]), ref)
+    sd = SequenceData(res["sequences"], ref=res["reference"], ambiguous="N")
+    assert sd.is_sparse
+    assert list(sd.compressed_alignment.keys()) == G["h_comp_names"].tolist()
+    np.testing.assert_array_equal(sd.compressed_codes, G["h_comp_codes"])
+    np.testing.assert_array_equal(sd.multiplicity(), G["h_mult"])
+    np.testing.assert_array_equal(sd.full_to_compressed_sequence_map, G["h_f2c"])
+    assert sorted(sd.inferred_const_sites) == G["h_const_amb"].tolist()
+    # the reference may also come as a FASTA file name
+    sd2 = SequenceData(res["sequences"], ref=ref, ambiguous="N")
+    np.testing.assert_array_equal(sd2.compressed_codes, G["h_comp_codes"])
+
+
+def test_vcf_file_as_alignment(tmp_path):
+    from treetime_gb300.seqdata import SequenceData
+    sd = SequenceData(_write(tmp_path, "h.vcf", G["h_vcf_text"]), ref=str(G["h_ref"]), ambiguous="N")
+    np.testing.assert_array_equal(sd.compressed_codes, G["h_comp_codes"])
+
+
+@pytest.mark.gpu
+def test_marginal_reconstruction_of_sparse_alignment_matches_treetime(tmp_path):
+    from treetime_gb300 import TreeAnc
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import parse_newick
+    ref = _write(tmp_path, "ref.fasta", ">ref\n" + str(G["h_ref"]) + "\n")
+    res = read_vcf(_write(tmp_path, "h.vcf", G["h_vcf_text"]), ref)
+    for precision, rel in (("f64", 1e-10), ("f32", 1e-6)):
+        t = TreeAnc(tree=parse_newick(str(G["h_newick"])), aln=res["sequences"], ref=res["reference"],
+                    gtr=GTR.custom(mu=1.0, pi=np.ones(5), W=np.ones((5, 5)), alphabet="nuc"), verbose=0,
+                    precision=precision)
+        t.infer_ancestral_sequences(marginal=True)
+        want = float(G["h_marg_total_LH"])
+        assert abs(t.tree.total_sequence_LH - want) <= rel * abs(want)

@@ -551,6 +551,8 @@ class GPUAncMixin:
         rewrites the ambiguous character in columns of one state; TreeTime
         counts a tip's mutations on its raw characters), or None."""
         d = self.data
+        if getattr(d, "is_sparse", False):
+            raise NotImplementedError("joint-mode GTR inference from a sparse alignment is not supported")
         name_to_row, ccodes = self._aln_index()
         f2c = np.asarray(d.full_to_compressed_sequence_map)
         if hasattr(d, "codes") and getattr(d, "sequence_names", None) is not None:

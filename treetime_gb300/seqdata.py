@@ -172,7 +172,13 @@ class SequenceData:
         if in_aln is None:
             return
         if isinstance(in_aln, str) and os.path.isfile(in_aln):
-            in_aln = read_fasta(in_aln)
+            if in_aln.lower().endswith((".vcf", ".vcf.gz")) and self.ref is not None:
+                from .vcf import read_vcf
+                in_aln = read_vcf(in_aln)["sequences"]
+            else:
+                in_aln = read_fasta(in_aln)
+        if isinstance(in_aln, dict) and in_aln and all(isinstance(v, dict) for v in in_aln.values()):
+            return self._set_sparse(in_aln)
         if isinstance(in_aln, dict):
             raw = [(k, v) for k, v in in_aln.items()]
         else:
@@ -215,6 +221,118 @@ class SequenceData:
         self._aln = _LazyCharRows(self.sequence_names, self.codes)
         self.make_compressed_alignment()
 
+    def _set_sparse(self, in_aln):
+        """A sparse alignment {name: {position: character}} of differences from
+        the reference `ref` (e.g. from a VCF file), compressed as TreeTime does
+        (treetime/sequence_data.py:325-464 with
+        treetime/vcf_utils.py:653-749): positions that differ in no sequence,
+        or are constant up to the ambiguous character, or carry one non-reference
+        state in every sequence, become constant patterns, one per state in
+        sorted order; the other positions are taken in the order in which they
+        first appear in the sequences' dictionaries, a column with one state
+        after replacing the ambiguous character joins that state's constant
+        pattern, any other column gets a pattern of its own."""
+        if self.ref is None:
+            raise MissingDataError("SequenceData: a sparse alignment needs a reference sequence")
+        if not self.compress:
+            raise NotImplementedError("sparse alignments are always compressed")
+        ref = self.ref
+        if isinstance(ref, str) and os.path.isfile(ref):
+            recs = read_fasta(ref)
+            if len(recs) != 1:
+                raise TypeError("SequenceData.ref: reference sequence file %s could not be parsed" % ref)
+            ref = next(iter(recs.values()))
+        if hasattr(ref, "seq"):
+            ref = str(ref.seq)
+        ref = ref if isinstance(ref, str) else "".join(np.asarray(ref).astype("U").tolist())
+        ref = ref.upper() if self.convert_upper else ref
+        ref_codes = np.frombuffer(ref.encode("latin-1"), dtype=np.uint8).copy()
+        self.ref = ref_codes.view("S1").astype("U1")  # the reference as a character array, as TreeTime keeps it
+        sample = ref_codes[:20000]
+        nucish = np.isin(sample, np.frombuffer(b"acgtACGT-N", dtype=np.uint8)).sum()
+        self.likely_alphabet = "nuc" if nucish > 0.9 * len(sample) else "aa"
+        if self.ambiguous is None:
+            self.ambiguous = "N" if self.likely_alphabet == "nuc" else "X"
+        amb = ord(self.ambiguous)
+        L = len(ref_codes)
+        if self._full_length and self._full_length != L:
+            self.logger("SequenceData.aln: specified sequence length doesn't match reference length, ignoring "
+                        "sequence length.", 1, warn=True)
+        self._full_length = L
+        self.is_sparse = True
+        self.codes = None
+        self.sequence_names = list(in_aln.keys())
+        names = self.sequence_names
+        nseq = len(names)
+        conv = (lambda c: c.upper()) if self.convert_upper else (lambda c: c)
+        seqs = {k: {int(p): ord(conv(str(c))) for p, c in v.items()} for k, v in in_aln.items()}
+        # positions with at least one difference, in order of first appearance
+        inv = {}
+        for k in names:
+            for p, c in seqs[k].items():
+                inv.setdefault(p, []).append(c)
+        ref_mod = ref_codes.copy()
+        variable, nonref_pos, nonref_allele, up_to_amb = [], [], [], []
+        for p, bs in inv.items():
+            bases = sorted(set(bs))
+            if len(bs) == nseq:
+                if len(bases) == 1 or (len(bases) <= 2 and amb in bases):
+                    nonref_pos.append(p)
+                    nonref_allele.append(bases[0] if len(bases) == 1 else [x for x in bases if x != amb][0])
+                    if amb in bases:
+                        up_to_amb.append(p)
+                else:
+                    variable.append(p)
+            elif len(bases) == 1 and bases[0] == amb:
+                up_to_amb.append(p)
+            else:
+                variable.append(p)
+        if nonref_pos:
+            ref_mod[np.asarray(nonref_pos)] = np.asarray(nonref_allele, dtype=np.uint8)
+        states = np.unique(ref_mod)
+        if variable:
+            ref_mod[np.asarray(variable)] = ord(".")
+        columns, patterns, positions = [], {}, []
+        for base in states:
+            if base == amb:
+                continue
+            pos = np.flatnonzero(ref_mod == base)
+            if len(pos):
+                patterns[bytes([base]) * nseq] = len(columns)
+                columns.append(np.full(nseq, base, dtype=np.uint8))
+                positions.append(list(pos))
+        for p in variable:
+            col = np.array([seqs[k].get(p, ref_codes[p]) for k in names], dtype=np.uint8)
+            letters = np.unique(col)
+            if len(letters) == 2 and amb in letters:
+                col[col == amb] = letters[letters != amb][0]
+                letters = letters[letters != amb]
+            key = col.tobytes()
+            if len(letters) > 1:
+                key += b"_%d" % p
+            if key not in patterns:
+                patterns[key] = len(columns)
+                columns.append(col)
+                positions.append([p])
+            else:
+                positions[patterns[key]].append(p)
+        mult = np.array([len(x) for x in positions], dtype=float)
+        f2c = np.zeros(L, dtype=int)
+        c2f = {}
+        for i, pos in enumerate(positions):
+            f2c[np.asarray(pos, dtype=int)] = i
+            c2f[i] = np.asarray(pos, dtype=int)
+        self.inferred_const_sites = up_to_amb
+        self.nonref_positions = np.sort(np.asarray(list(inv.keys()), dtype=int))
+        self._aln = in_aln
+        self.compressed_codes = np.stack(columns, axis=1) if columns else np.zeros((nseq, 0), np.uint8)
+        self._multiplicity = mult
+        self.full_to_compressed_sequence_map = f2c
+        self.compressed_to_full_sequence_map = c2f
+        self._compressed_length = len(mult)
+        self._compressed_alignment = None
+        self.name_to_row = {k: i for i, k in enumerate(names)}
+
     def _to_codes(self, v):
         if isinstance(v, np.ndarray) and v.dtype == np.uint8:
             return v.copy()
@@ -237,6 +355,8 @@ class SequenceData:
         return self._compressed_length
 
     def make_compressed_alignment(self, device=None):
+        if self.is_sparse:
+            return ttconf.SUCCESS
         amb = ord(self.ambiguous) if self.ambiguous else None
         if device is not None and self.compress:
             from . import engine

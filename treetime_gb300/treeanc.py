@@ -25,7 +25,10 @@ GTR inference (``infer_gtr``, ``infer_gtr_iterative``,
 model on the host as TreeTime does; Fitch parsimony (``method='fitch'``) runs
 its passes up and down the tree on the GPU.
 
-Out of scope (raise NotImplementedError): sparse (VCF) alignments.
+Sparse alignments ({name: {position: character}} with ``ref``, e.g. from a
+VCF file through ``treetime_gb300.vcf.read_vcf``) are compressed as TreeTime
+does and reconstructed like dense ones; joint-mode GTR inference from them is
+not supported.
 """
 
 import gc
@@ -76,8 +79,6 @@ class TreeAnc(GPUAncMixin):
             raise TypeError("TreeAnc requires a tree!")
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
-        if ref is not None:
-            raise NotImplementedError("sparse (VCF) alignments are not supported")
         self.t_start = time.time()
         self.verbose = verbose
         self.log = log
@@ -229,7 +230,8 @@ class TreeAnc(GPUAncMixin):
                     raise MissingDataError("TreeAnc._check_alignment_tree_gtr_consistency: At least 30\\% terminal "
                                            "nodes cannot be assigned a sequence!\nAre you sure the alignment belongs "
                                            "to the tree?")
-        extend_profile(self.gtr, self.data.aln.values(), logger=self.logger)
+        extend_profile(self.gtr, [self.data.ref] if getattr(self.data, "is_sparse", False) else self.data.aln.values(),
+                       logger=self.logger)
         self.gtr._device_cache = None
         self._session = None
         self.ok = True

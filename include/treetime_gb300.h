@@ -175,6 +175,8 @@ typedef struct tt_marginal_out {
     const double* root_uniform;/* [n_patterns] draws for sampling the root state, or NULL (argmax) */
     int32_t  reconstruct_tips; /* also run the pre-order step at tips                              */
     int32_t  count_diff;       /* compare with the states already in `states` to count n_diff      */
+    const double* node_uniform;/* draws for sampling the other nodes' states (state layout: node k,
+                                  pattern p at state_base + k*n_patterns + p), or NULL (argmax)    */
 } tt_marginal_out;
 
 typedef struct tt_joint_out {

@@ -8,6 +8,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source --infer-gtr   (GTR inference only)
     python tests/golden/make_golden.py /path/to/treetime-source --fitch   (Fitch parsimony only)
     python tests/golden/make_golden.py /path/to/treetime-source --vcf   (VCF reading and sparse alignments)
+    python tests/golden/make_golden.py /path/to/treetime-source --sample   (states drawn at every node)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -539,6 +540,45 @@ def vcf_cases(ref_path):
     np.savez_compressed(os.path.join(HERE, "vcf_cases.npz"), **out)
 
 
+def run_sample(name, newick, aln, kind, params, rng_seed=5):
+    """Marginal reconstruction with sample_from_profile=True (every node's
+    state drawn from its profile with TreeTime's generator), without and with
+    tip states, and a second call (N_diff against the first)."""
+    from treetime import TreeAnc
+    out = {"case": name, "newick": newick, "kind": kind, "rng_seed": rng_seed,
+           "aln_names": np.array(list(aln.keys())), "aln_seqs": np.array(list(aln.values()))}
+    for k, v in params.items():
+        out["param_" + k] = np.asarray(v)
+    for tips in (False, True):
+        tree, recs = _bio_inputs(newick, aln)
+        t = TreeAnc(tree=tree, aln=recs, gtr=_ref_gtr(kind, params), compress=True, verbose=0, rng_seed=rng_seed)
+        tag = "tips" if tips else "inner"
+        out[tag + "_N_diff"] = t.infer_ancestral_sequences(marginal=True, sample_from_profile=True,
+                                                            reconstruct_tip_states=tips)
+        nodes = [n for n in t.tree.find_clades() if hasattr(n, "_cseq") and n._cseq is not None]
+        out[tag + "_names"] = np.array([n.name for n in nodes])
+        out[tag + "_cseq"] = np.stack([_codes(n._cseq) for n in nodes])
+        out[tag + "_N_diff_again"] = t.infer_ancestral_sequences(marginal=True, sample_from_profile=True,
+                                                                  reconstruct_tip_states=tips)
+        out[tag + "_cseq_again"] = np.stack([_codes(n._cseq) for n in nodes])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def sample_cases():
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    rng = np.random.default_rng(61)
+    tree = synth.coalescent_tree(24, 0.08, rng)
+    pi = rng.dirichlet(np.ones(5))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(5, 5)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc")
+    states = synth.evolve(tree, g, 150, rng)
+    aln = synth._to_text(states, g.alphabet, 0.02, rng)
+    run_sample("sample_nuc5", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "nuc", "mu": 1.0})
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -691,5 +731,8 @@ if __name__ == "__main__":
     elif "--vcf" in sys.argv:
         _setup(ref)
         vcf_cases(ref)
+    elif "--sample" in sys.argv:
+        _setup(ref)
+        sample_cases()
     else:
         main(ref)

@@ -183,3 +183,33 @@ def test_marginal_branch_lengths_match_treetime(case, precision):
         f = lambda tt: -anc.prob_t_profiles(model_o, (pp, pc), g["multiplicity"], tt, return_log=True) \
             + np.exp(tt * tt / 1e4)
         assert abs(f(x) - f(v)) <= obj_rel * abs(f(v)) + 1e-12, (name, x, v, f(x), f(v))
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("tips", [False, True])
+def test_sampling_at_every_node_matches_treetime(tips, precision):
+    """sample_from_profile=True: every node's state drawn from its profile with
+    TreeTime's generator (one rng.random(L) per node in preorder after the
+    root's).  FP64: bit-exact; FP32: a draw within 1e-5 of a cumulative
+    boundary may fall on the other side (at most 0.2% of the states)."""
+    from treetime_gb300 import TreeAnc
+    g = gc.load("sample_nuc5")
+    tree, aln, model, _ = gc.inputs_from(g)
+    t = TreeAnc(tree=tree, aln=aln, gtr=model, compress=True, verbose=0, rng_seed=int(g["rng_seed"]),
+                precision=precision)
+    tag = "tips" if tips else "inner"
+    nd = t.infer_ancestral_sequences(marginal=True, sample_from_profile=True, reconstruct_tip_states=tips)
+    assert nd == int(g[tag + "_N_diff"])
+    nodes = _by_name(t)
+    bad = total = 0
+    for i, k in enumerate(g[tag + "_names"].tolist()):
+        got = gc.codes_of(nodes[k].cseq)
+        bad += int((got != g[tag + "_cseq"][i]).sum())
+        total += got.size
+    if precision == "f64":
+        assert bad == 0
+    else:
+        assert bad <= 0.002 * total
+    nd2 = t.infer_ancestral_sequences(marginal=True, sample_from_profile=True, reconstruct_tip_states=tips)
+    if precision == "f64":
+        assert nd2 == int(g[tag + "_N_diff_again"])

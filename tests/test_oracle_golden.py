@@ -261,3 +261,21 @@ def test_oracle_fitch_matches_treetime(case):
     assert nd3 == int(g["fitch_after_marginal_N_diff"])
     for i, k in enumerate(g["fitch_names"].tolist()):
         np.testing.assert_array_equal(gc.codes_of(cseq3[k]), g["fitch_after_marginal_cseq"][i], err_msg=k)
+
+
+# ------------------------------------------------------- states drawn at every node
+@pytest.mark.parametrize("tips", [False, True])
+def test_oracle_sampling_at_every_node_matches_treetime(tips):
+    g = gc.load("sample_nuc5")
+    tree, aln, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    caln, mult, full = gc.compress_inputs(aln, model)
+    rng = np.random.default_rng(int(g["rng_seed"]))
+    tag = "tips" if tips else "inner"
+    res = anc.marginal(tree, caln, mult, model, full, sample_from_profile=True, reconstruct_tip_states=tips, rng=rng)
+    assert res["N_diff"] == int(g[tag + "_N_diff"])
+    for i, k in enumerate(g[tag + "_names"].tolist()):
+        np.testing.assert_array_equal(gc.codes_of(res["cseq"][k]), g[tag + "_cseq"][i], err_msg=k)
+    res2 = anc.marginal(tree, caln, mult, model, full, sample_from_profile=True, reconstruct_tip_states=tips,
+                        rng=rng, prev_cseq=res["cseq"])
+    assert res2["N_diff"] == int(g[tag + "_N_diff_again"])

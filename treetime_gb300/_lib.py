@@ -58,7 +58,7 @@ class TTSSF32(C.Structure):
 class TTMarginalOut(C.Structure):
     _fields_ = [("partial", vp), ("posterior", vp), ("outgroup", vp), ("tip_posterior", vp),
                 ("tip_outgroup", vp), ("states", vp), ("site_lh", vp), ("tree_lh", vp), ("n_diff", vp),
-                ("root_uniform", vp), ("reconstruct_tips", i32), ("count_diff", i32)]
+                ("root_uniform", vp), ("reconstruct_tips", i32), ("count_diff", i32), ("node_uniform", vp)]
 
 
 class TTJointOut(C.Structure):

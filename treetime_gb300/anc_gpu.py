@@ -241,11 +241,25 @@ class GPUAncMixin:
                         setattr(n, a, v)
 
     def _root_draws(self, sample_from_profile):
-        if sample_from_profile is True:
-            raise NotImplementedError("sampling states at every node is not supported; use 'root' or False")
-        if sample_from_profile == "root":
+        """The root's uniform draws (sample_from_profile 'root' or True), one
+        rng.random(L) as TreeTime's prof2seq (treetime/seq_utils.py:265-269)."""
+        if sample_from_profile == "root" or sample_from_profile is True:
             return self.rng.random(size=self.data.compressed_length)
         return None
+
+    def _node_draws(self, layout, reconstruct_tip_states):
+        """sample_from_profile=True: one rng.random(L) per node whose state is
+        drawn, in preorder after the root's (treetime/treeanc.py:880-932): the
+        internal nodes, and the tips when their states are reconstructed; laid
+        out by node id like the states (the other rows are not read)."""
+        P = self.data.compressed_length
+        out = np.zeros(layout.n_nodes * P)
+        for n in self.tree.find_clades(order="preorder"):
+            if n.up is None or (not n.clades and not reconstruct_tip_states):
+                continue
+            k = layout.local[id(n)]
+            out[k * P:(k + 1) * P] = self.rng.random(size=P)
+        return out
 
     # --------------------------------------------------------- reconstruction
     def _ml_anc_marginal(self, sample_from_profile=False, reconstruct_tip_states=False, debug=False,
@@ -258,9 +272,10 @@ class GPUAncMixin:
         if reconstruct_tip_states and count_diff and not self.reconstructed_tip_sequences:
             self._seed_tip_states(sess)
         draws = self._root_draws(sample_from_profile)
+        node_draws = self._node_draws(layout, reconstruct_tip_states) if sample_from_profile is True else None
         prec = self._gpu_precision()
         kw = dict(precision=prec, reconstruct_tips=reconstruct_tip_states, keep_outgroup=keep_outgroup,
-                  tip_outgroup=keep_outgroup, count_diff=count_diff, root_uniform=draws)
+                  tip_outgroup=keep_outgroup, count_diff=count_diff, root_uniform=draws, node_uniform=node_draws)
         if self.gtr.is_site_specific:
             out = engine.marginal_site_specific(sess["forest"], self.gtr, sess["bufs"], **kw)
         else:

@@ -448,7 +448,18 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         const float inv2 = __fdividef(1.f, group_sum<LPP>(s2));
 #pragma unroll
                         for (int s = 0; s < S; ++s) x[d][s] *= inv2;
-                        const int stt = group_argmax<Q, W, LPP>(x[d], j0);
+                        int stt;
+                        if (a.o.node_uniform) {
+                            float full[W];
+#pragma unroll
+                            for (int r = 0; r < LPP; ++r)
+#pragma unroll
+                                for (int s3 = 0; s3 < S; ++s3)
+                                    full[r * S + s3] = LPP == 1 ? x[d][s3] : __shfl_sync(0xffffffffu, x[d][s3], r, LPP);
+                            stt = sample_cdf<Q, float, W>(full, a.o.node_uniform[tr.state_base + (int64_t)k * P + pc]);
+                        } else {
+                            stt = group_argmax<Q, W, LPP>(x[d], j0);
+                        }
                         if (valid) {
                             if (tips) {
                                 st_part<S>(reinterpret_cast<float*>(a.o.tip_posterior) +

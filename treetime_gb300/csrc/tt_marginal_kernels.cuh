@@ -275,7 +275,8 @@ __device__ __forceinline__ unsigned pre_node(const MargParams& a, const tt_tree&
     const T inv = T(1) / s;
 #pragma unroll
     for (int i = 0; i < Q; ++i) x[i] *= inv;
-    const int st = argmax_first<Q, T, W>(x);
+    const int st = a.o.node_uniform ? sample_cdf<Q, T, W>(x, a.o.node_uniform[tr.state_base + (int64_t)k * P + pc])
+                                    : argmax_first<Q, T, W>(x);
     unsigned changed = 0;
     if (valid) {
         const int64_t row = is_tip ? tr.tipprof_base + (int64_t)(k - tr.n_int) * P + pc

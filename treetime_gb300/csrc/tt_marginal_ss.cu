@@ -330,7 +330,9 @@ __global__ void __launch_bounds__(NW * 32) marginal_ss_kernel(SSParams a) {
                 const T inv = T(1) / s;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) x[i] *= inv;
-                const int st = argmax_first<Q, T, W>(x);
+                const int st = a.o.node_uniform
+                                   ? sample_cdf<Q, T, W>(x, a.o.node_uniform[tr.state_base + (int64_t)k * P + pc])
+                                   : argmax_first<Q, T, W>(x);
                 if (valid) {
                     T* dst = is_tip ? reinterpret_cast<T*>(a.o.tip_posterior) : posterior;
                     if (dst) store_row<W>(dst + row * W, x);

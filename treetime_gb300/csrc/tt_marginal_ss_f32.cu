@@ -290,7 +290,9 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
                 const float inv = __fdividef(1.f, s);
 #pragma unroll
                 for (int i = 0; i < Q; ++i) x[i] *= inv;
-                const int st = argmax_first<Q, float, W>(x);
+                const int st = a.o.node_uniform
+                                   ? sample_cdf<Q, float, W>(x, a.o.node_uniform[tr.state_base + (int64_t)k * P + pc])
+                                   : argmax_first<Q, float, W>(x);
                 if (valid) {
                     const int64_t prow = is_tip ? tr.tipprof_base + (int64_t)(k - n_int) * P + pc
                                                 : tr.prof_base + (int64_t)k * P + pc;

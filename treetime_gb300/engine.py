@@ -520,7 +520,7 @@ def _check_status(status):
 
 
 def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_outgroup=False,
-             tip_outgroup=False, count_diff=False, root_uniform=None, sync=True):
+             tip_outgroup=False, count_diff=False, root_uniform=None, sync=True, node_uniform=None):
     """Run the marginal pass over the forest.  Returns the dict of device
     buffers (partial, posterior, outgroup, tip_posterior, tip_outgroup, states,
     site_lh, tree_lh, n_diff)."""
@@ -544,15 +544,16 @@ def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_
     }
     out["n_diff"].zero_()
     ru = _to_dev(root_uniform, forest.device, t.float64) if root_uniform is not None else None
+    nu = _to_dev(node_uniform, forest.device, t.float64) if node_uniform is not None else None
     o = TTMarginalOut(_p(out["partial"]), _p(out["posterior"]), _p(out["outgroup"]), _p(out["tip_posterior"]),
                       _p(out["tip_outgroup"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
-                      _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
+                      _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)), _p(nu))
     check(lib.tt_marginal(C.byref(forest.struct), C.byref(model.struct), C.byref(pm),
                           _lib.TT_PREC_F32 if f32 else _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()),
           "tt_marginal")
     if sync:
         _check_status(status)
-    out["_keep"] = ru
+    out["_keep"] = (ru, nu)
     return out
 
 
@@ -641,7 +642,8 @@ def _ss_f32_model(forest, gtr, bufs, dev, range_width=None):
 
 
 def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=False, keep_outgroup=False,
-                           tip_outgroup=False, count_diff=False, root_uniform=None, sync=True, range_width=None):
+                           tip_outgroup=False, count_diff=False, root_uniform=None, sync=True, range_width=None,
+                           node_uniform=None):
     """Marginal pass for a GTR_site_specific model (single tree): FP64 log-domain
     kernel, or the FP32 kernel with each site range's eigenvectors in shared
     memory."""
@@ -666,9 +668,10 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
     status = bufs.get("status", (1,), t.int32)
     status.zero_()
     ru = _to_dev(root_uniform, dev, t.float64) if root_uniform is not None else None
+    nu = _to_dev(node_uniform, dev, t.float64) if node_uniform is not None else None
     o = TTMarginalOut(_p(out["partial"]), _p(out["posterior"]), _p(out["outgroup"]), _p(out["tip_posterior"]),
                       _p(out["tip_outgroup"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
-                      _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
+                      _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)), _p(nu))
     if f32:
         arrs = _ss_f32_model(forest, gtr, bufs, dev, range_width)
         check(lib.tt_marginal_ss_f32(C.byref(forest.struct), C.byref(arrs["struct"]), _p(arrs["ranges"]),
@@ -692,7 +695,7 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
                                  _lib.TT_PREC_F64, C.byref(o), _p(status), _stream()), "tt_marginal_ss")
     if sync:
         _check_status(status)
-    out["_keep"] = ru
+    out["_keep"] = (ru, nu)
     return out
 
 

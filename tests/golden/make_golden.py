@@ -9,6 +9,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source --fitch   (Fitch parsimony only)
     python tests/golden/make_golden.py /path/to/treetime-source --vcf   (VCF reading and sparse alignments)
     python tests/golden/make_golden.py /path/to/treetime-source --sample   (states drawn at every node)
+    python tests/golden/make_golden.py /path/to/treetime-source --extra-sites   (constant sites beyond the alignment)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -579,6 +580,43 @@ def sample_cases():
     run_sample("sample_nuc5", to_newick(tree), aln, "gtr", {"pi": pi, "W": W, "alphabet": "nuc", "mu": 1.0})
 
 
+def extra_sites_cases():
+    """seq_len beyond the alignment (additional constant sites): TreeTime's
+    compressed alignment and marginal log-likelihood, nucleotides and amino
+    acids."""
+    from treetime import TreeAnc
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    out = {}
+    for tag, alphabet, q, seed, extra in (("nuc", "nuc", 5, 71, 1234), ("aa", "aa", 21, 72, 77)):
+        rng = np.random.default_rng(seed)
+        tree = synth.coalescent_tree(14, 0.05, rng)
+        pi = rng.dirichlet(np.ones(q))
+        W = np.triu(rng.uniform(0.5, 2.0, size=(q, q)), 1)
+        W = W + W.T
+        g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet=alphabet)
+        aln = synth._to_text(synth.evolve(tree, g, 90, rng), g.alphabet, 0.03, rng)
+        nwk = to_newick(tree)
+        params = {"pi": pi, "W": W, "alphabet": alphabet, "mu": 1.0}
+        tr, recs = _bio_inputs(nwk, aln)
+        t = TreeAnc(tree=tr, aln=recs, gtr=_ref_gtr("gtr", params), verbose=0, seq_len=90 + extra)
+        d = t.data
+        out[tag + "_newick"] = np.array(nwk)
+        out[tag + "_aln_names"] = np.array(list(aln.keys()))
+        out[tag + "_aln_seqs"] = np.array(list(aln.values()))
+        for k, v in params.items():
+            out[tag + "_param_" + k] = np.asarray(v)
+        out[tag + "_seq_len"] = 90 + extra
+        out[tag + "_comp_names"] = np.array(list(d.compressed_alignment.keys()))
+        out[tag + "_comp_codes"] = np.stack([_codes(d.compressed_alignment[k]) for k in d.compressed_alignment])
+        out[tag + "_mult"] = d.multiplicity()
+        out[tag + "_f2c"] = d.full_to_compressed_sequence_map
+        t.infer_ancestral_sequences(marginal=True)
+        out[tag + "_marg_total_LH"] = t.tree.total_sequence_LH
+    np.savez_compressed(os.path.join(HERE, "extra_sites.npz"), **out)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -734,5 +772,8 @@ if __name__ == "__main__":
     elif "--sample" in sys.argv:
         _setup(ref)
         sample_cases()
+    elif "--extra-sites" in sys.argv:
+        _setup(ref)
+        extra_sites_cases()
     else:
         main(ref)

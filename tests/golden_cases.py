@@ -16,7 +16,8 @@ def case_names():
     """Reconstruction cases (every fixture but the branch-length grids and the
     GTR inference cases)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("blgrid_", "gtrinf_", "fitch_", "vcf_", "sample_")))
+                  if not os.path.basename(p).startswith(("blgrid_", "gtrinf_", "fitch_", "vcf_", "sample_",
+                                                          "extra_")))
 
 
 def fitch_names():

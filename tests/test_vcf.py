@@ -89,3 +89,35 @@ def test_marginal_reconstruction_of_sparse_alignment_matches_treetime(tmp_path):
         t.infer_ancestral_sequences(marginal=True)
         want = float(G["h_marg_total_LH"])
         assert abs(t.tree.total_sequence_LH - want) <= rel * abs(want)
+
+
+# ------------------------------------------------- constant sites beyond the alignment
+E = gc.load("extra_sites")
+
+
+@pytest.mark.parametrize("tag", ["nuc", "aa"])
+def test_additional_constant_sites_match_treetime(tag):
+    from treetime_gb300.seqdata import SequenceData
+    aln = dict(zip(E[tag + "_aln_names"].tolist(), E[tag + "_aln_seqs"].tolist()))
+    sd = SequenceData(aln, sequence_length=int(E[tag + "_seq_len"]), ambiguous="N" if tag == "nuc" else "X")
+    assert sd.full_length == int(E[tag + "_seq_len"])
+    assert list(sd.compressed_alignment.keys()) == E[tag + "_comp_names"].tolist()
+    np.testing.assert_array_equal(sd.compressed_codes, E[tag + "_comp_codes"])
+    np.testing.assert_array_equal(sd.multiplicity(), E[tag + "_mult"])
+    np.testing.assert_array_equal(sd.full_to_compressed_sequence_map, E[tag + "_f2c"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", ["nuc", "aa"])
+def test_additional_constant_sites_reconstruction_matches_treetime(tag):
+    from treetime_gb300 import TreeAnc
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import parse_newick
+    aln = dict(zip(E[tag + "_aln_names"].tolist(), E[tag + "_aln_seqs"].tolist()))
+    alphabet = str(E[tag + "_param_alphabet"])
+    g = GTR.custom(mu=1.0, pi=E[tag + "_param_pi"], W=E[tag + "_param_W"], alphabet=alphabet)
+    t = TreeAnc(tree=parse_newick(str(E[tag + "_newick"])), aln=aln, gtr=g, verbose=0,
+                seq_len=int(E[tag + "_seq_len"]))
+    t.infer_ancestral_sequences(marginal=True)
+    want = float(E[tag + "_marg_total_LH"])
+    assert abs(t.tree.total_sequence_LH - want) <= 1e-10 * abs(want)

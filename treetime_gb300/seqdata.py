@@ -211,9 +211,10 @@ class SequenceData:
         if self._full_length:
             if self._full_length < L:
                 raise AttributeError("SequenceData.aln: specified sequence length is smaller than alignment length!")
+            if self._full_length > L:
+                self.logger("SequenceData.aln: specified sequence length doesn't match alignment length. Treating "
+                            "difference as constant sites.", 2, warn=True)
             self.additional_constant_sites = max(0, self._full_length - L)
-            if self.additional_constant_sites:
-                raise NotImplementedError("additional constant sites are not supported")
         else:
             self._full_length = L
         self.sequence_names = [k for k, _ in raw]
@@ -363,6 +364,8 @@ class SequenceData:
             pc, mult, f2c, c2f = engine.compress_columns(self.codes, amb, device)
         else:
             pc, mult, f2c, c2f = compress_codes(self.codes, amb, self.compress)
+        if self.additional_constant_sites and self.compress:
+            pc, mult, f2c, c2f = self._add_constant_sites(pc, mult, f2c, c2f)
         self.compressed_codes = pc
         self._multiplicity = mult
         self.full_to_compressed_sequence_map = f2c
@@ -371,6 +374,50 @@ class SequenceData:
         self._compressed_alignment = None
         self.name_to_row = {k: i for i, k in enumerate(self.sequence_names)}
         return ttconf.SUCCESS
+
+    def _add_constant_sites(self, pc, mult, f2c, c2f):
+        """Constant columns for the sites beyond the alignment
+        (treetime/sequence_data.py:418-441): shared among the alphabet's states
+        (without gap and ambiguous character) in proportion to their counts in
+        the alignment, rounded, the last state taking the remainder; each
+        state's columns join its constant pattern or start one, at positions
+        after the alignment."""
+        from .alphabets import alphabets
+        extra = int(self.additional_constant_sites)
+        states = [c for c in alphabets[self.likely_alphabet + "_nogap"].tolist() if c not in (self.ambiguous, "-")]
+        counts = [(c, int(np.sum(self.codes == ord(c)))) for c in states]
+        total = np.sum([n for _, n in counts])
+        shares = [(c, int(np.round(extra * n / total))) for c, n in counts]
+        left = extra
+        pi = self.codes.shape[1]
+        nseq = pc.shape[0]
+        cols = [pc[:, i] for i in range(pc.shape[1])]
+        mult = list(mult)
+        f2c = np.concatenate([f2c, np.zeros(extra, dtype=f2c.dtype)])
+        const = {}
+        for i, col in enumerate(cols):
+            if (col == col[0]).all() and col[0] not in const:
+                const[int(col[0])] = i
+        c2f = dict(c2f)
+        for c, n in shares:
+            if c == shares[-1][0]:
+                n = left
+            if n:
+                code = ord(c)
+                if code in const:
+                    p = const[code]
+                    mult[p] += n
+                    c2f[p] = np.concatenate([c2f[p], np.arange(pi, pi + n)])
+                else:
+                    p = len(cols)
+                    cols.append(np.full(nseq, code, dtype=np.uint8))
+                    mult.append(float(n))
+                    const[code] = p
+                    c2f[p] = np.arange(pi, pi + n)
+                f2c[pi:pi + n] = p
+                pi += n
+                left -= n
+        return np.ascontiguousarray(np.stack(cols, axis=1)), np.asarray(mult, dtype=float), f2c, c2f
 
     @property
     def compressed_alignment(self):
@@ -390,7 +437,11 @@ class SequenceData:
 
     # ------------------------------------------------------ sequence maps
     def compressed_to_full_sequence(self, sequence, include_additional_constant_sites=False, as_string=False):
-        tmp = sequence[self.full_to_compressed_sequence_map[: self.full_length]]
+        """treetime/sequence_data.py:513-539: the sites beyond the alignment only
+        when asked for."""
+        L = self.full_length if include_additional_constant_sites else \
+            self.full_length - int(self.additional_constant_sites or 0)
+        tmp = sequence[self.full_to_compressed_sequence_map[:L]]
         if as_string:
             return "".join(tmp.astype("U"))
         return tmp

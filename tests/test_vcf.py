@@ -121,3 +121,26 @@ def test_additional_constant_sites_reconstruction_matches_treetime(tag):
     t.infer_ancestral_sequences(marginal=True)
     want = float(E[tag + "_marg_total_LH"])
     assert abs(t.tree.total_sequence_LH - want) <= 1e-10 * abs(want)
+
+
+def test_treetime_vcf_reader_suite_passes_with_this_reader(tmp_path):
+    """TreeTime's own read_vcf tests (its test/test_vcf.py: malformed files,
+    multiple chromosomes, simple files, no-calls and missing alleles, the VCF
+    specification's examples, mutation plus insertion, metadata) run against
+    this package's reader.  The writing tests (write_vcf) are not part of it.
+    Skipped where the TreeTime sources are not present."""
+    import subprocess
+    import sys
+    src = os.environ.get("TREETIME_SOURCE", "/root/reference")
+    suite = os.path.join(src, "test", "test_vcf.py")
+    if not os.path.isfile(suite):
+        pytest.skip("TreeTime sources not present")
+    here = os.path.dirname(os.path.abspath(__file__))
+    repo = os.path.dirname(here)
+    env = dict(os.environ)
+    env["PYTHONPATH"] = os.pathsep.join([os.path.join(repo, "oracle", "bioshim"), src, repo,
+                                         os.path.join(here, "golden"), env.get("PYTHONPATH", "")])
+    r = subprocess.run([sys.executable, "-m", "pytest", suite, "-q", "-p", "vcf_reader_plugin", "-p",
+                        "no:cacheprovider", "-k", "not TestWriting and not roundtrip", "--rootdir", str(tmp_path)],
+                       env=env, cwd=str(tmp_path), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]

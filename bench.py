@@ -871,6 +871,96 @@ def run_brent(args):
     return out
 
 
+COMPRESS_WORKLOAD = ("compress: pattern compression (SequenceData.make_compressed_alignment) of the 2000-tip x "
+                     "30000-site alignment (2000 x 30000 bytes)")
+
+
+def run_compress(args):
+    """--workload compress: column classification on the device
+    (tt_compress_columns over the alignment resident in HBM, timed alone), and
+    the public call engine.compress_columns (alignment copied in, keys back,
+    patterns assembled on the host) beside the vectorised host compression and
+    TreeTime's per-column loop (the oracle) on a sample of columns."""
+    import torch
+    from treetime_gb300 import engine, synth
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl = synth.make_workload("c1", seed=1)
+    from treetime_gb300.seqdata import SequenceData, compress_codes
+    sd = SequenceData(wl["aln"], compress=False, ambiguous="N")
+    codes = np.ascontiguousarray(sd.codes)
+    n, L = codes.shape
+    amb = ord("N")
+    lib = engine._lib.load()
+    d = engine._to_dev(codes, dev)
+    key = torch.empty(L, dtype=torch.int64, device=dev)
+    fixed = torch.empty(L, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def kernel():
+        engine.check(lib.tt_compress_columns(engine._p(d), n, L, amb, engine._p(key), engine._p(fixed),
+                                             engine._stream()), "tt_compress_columns")
+
+    for _ in range(args.warmup):
+        kernel()
+    torch.cuda.synchronize()
+    kt = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            kernel()
+            b.record()
+            b.synchronize()
+            kt.append(a.elapsed_time(b))
+    k_ms = _reduce_max(sum(kt) / len(kt), dev, world)
+    e2e = []
+    for _ in range(max(3, min(args.steps, 10))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pc, mult, f2c, c2f = engine.compress_columns(codes, amb, dev)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = statistics.median(e2e) * 1e3
+    t0 = time.perf_counter()
+    hpc, hmult, hf2c, _ = compress_codes(codes, amb)
+    host_ms = (time.perf_counter() - t0) * 1e3
+    same = bool(np.array_equal(pc, hpc) and np.array_equal(mult, hmult) and np.array_equal(f2c, hf2c))
+    if rank != 0:
+        return None
+    ab = n * L + L * 12
+    peak, peak_kind = _peaks()
+    out = {
+        "metric": "alignment sites compressed/s", "value": world * L / (k_ms * 1e-3), "unit": "sites/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": k_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded c1 alignment)",
+        "config": {"workload": COMPRESS_WORKLOAD, "sequences": n, "sites": L, "patterns": int(len(mult)),
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": ab / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": ab / (k_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": ab},
+        "e2e": {"value": L / (e2e_ms * 1e-3), "unit": "sites/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": n * L,
+                "d2h_bytes_per_step": L * 12,
+                "note": "engine.compress_columns: alignment up, keys down, patterns assembled on the host"},
+        "host_vectorised_ms": host_ms, "identical_to_host": same,
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import anc
+        names = sd.sequence_names
+        m = 2000
+        arrays = {k: codes[i, :m].view("S1").astype("U1") for i, k in enumerate(names)}
+        t0 = time.perf_counter()
+        anc.compress_alignment(names, arrays, "N")
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": m / secs, "unit": "sites/s", "cores": 1, "kind": "port",
+                               "sample": "the first %d columns through the restatement of TreeTime's per-column "
+                                         "loop, 1 process" % m, "seconds": secs}
+    return out
+
+
 C3_WORKLOAD = ("c3: 256 independent coalescent trees, tips log-uniform in [50, 5000], sites log-uniform in "
                "[1k, 30k], branch means log-uniform in [1e-4, 0.05], a random GTR per tree; the whole batch is "
                "one forest, one captured launch sequence per step")
@@ -1251,7 +1341,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c1",
-                    choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf", "fitch", "brent"],
+                    choices=["c1", "c2", "c3", "c4", "blgrid", "gtrinf", "fitch", "brent", "compress"],
                     help="c1: the 2,000-tip x 30k-site tree (the headline line); c3: the batch of 256 trees")
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
@@ -1270,7 +1360,8 @@ def main():
         from treetime_gb300 import build
         build.build()
         res = {"c1": run_gpu, "c2": run_c2, "c3": run_c3, "c4": run_c4, "blgrid": run_blgrid,
-               "gtrinf": run_gtrinf, "fitch": run_fitch, "brent": run_brent}[args.workload](args)
+               "gtrinf": run_gtrinf, "fitch": run_fitch, "brent": run_brent,
+               "compress": run_compress}[args.workload](args)
     if res is not None:
         print(json.dumps(res))
 

@@ -10,12 +10,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_compress_columns_equals_host(seed):
+@pytest.mark.parametrize("seed,n,L", [(0, 37, 2000), (1, 37, 2003), (2, 5, 1001), (3, 3, 1000), (4, 211, 4096)])
+def test_compress_columns_equals_host(seed, n, L):
+    """Row lengths that are (tiled kernel) and are not (column kernel)
+    multiples of 4, fewer rows than the tiled kernel's warps, ragged tiles."""
     from treetime_gb300 import engine
     from treetime_gb300.seqdata import compress_codes
     rng = np.random.default_rng(seed)
-    n, L = 37, 2000
     alpha = np.frombuffer(b"ACGT", dtype=np.uint8)
     root = rng.integers(4, size=L)
     codes = alpha[np.where(rng.random((n, L)) < 0.08, rng.integers(4, size=(n, L)), root[None, :])]

@@ -1205,11 +1205,15 @@ def compress_columns(codes, ambiguous_code, device=None):
     f2c = rank[inverse].astype(np.int64)
     mult = counts[order].astype(float)
     cols = first[order]
-    pc = np.ascontiguousarray(codes[:, cols])
+    # the pattern columns gathered on the device (one strided pass over the alignment)
+    pc = d[:, _to_dev(cols.astype(np.int64), dev)].cpu().numpy()
     fx = fixed_h[cols]
-    for j in np.flatnonzero(fx >= 0):
-        col = pc[:, j]
-        col[col == ambiguous_code] = fx[j]
+    js = np.flatnonzero(fx >= 0)
+    if len(js):
+        sub = pc[:, js]
+        hit = sub == ambiguous_code
+        sub[hit] = np.broadcast_to(fx[js].astype(np.uint8), sub.shape)[hit]
+        pc[:, js] = sub
     pos_sorted = np.argsort(f2c, kind="stable")
     bounds = np.concatenate(([0], np.cumsum(counts[order])))
     c2f = {p: pos_sorted[bounds[p]:bounds[p + 1]].astype(int) for p in range(len(order))}

@@ -265,6 +265,7 @@ def run_gpu(args):
                    "note": "the same alignment %d times, each with its own profile buffers, one forest, one "
                            "captured launch sequence per step; L2 flushed before every step" % k}
 
+    pipeline = _config_pipeline(t)
     if rank != 0:
         return None
     peak, peak_kind = _peaks()
@@ -302,6 +303,7 @@ def run_gpu(args):
                 "ms_per_step": e2e_ms},
         "gpu_launches": 3 * args.steps,
         "batched": batched,
+        "config_pipeline": pipeline,
         "autotune": {"best": {"threads": best[0], "ctas_per_sm": best[1], "ranges_per_sm": best[2]},
                      "ms": table},
         "clocks": clocks,
@@ -309,6 +311,38 @@ def run_gpu(args):
     if not args.no_cpu_baseline and world == 1:
         res["cpu_baseline"] = cpu_baseline(t)
     return res
+
+
+def _config_pipeline(t, repeats=3):
+    """The configuration's whole step through the public TreeAnc calls:
+    marginal reconstruction (FP32-scaled), joint reconstruction (FP64) and
+    optimal_t_compressed on every branch (optimize_branch_lengths_joint), host
+    clock, median of `repeats`; the tree's branch lengths are restored
+    afterwards."""
+    import torch
+    nodes = list(t.tree.find_clades())
+    saved = [(n.branch_length, getattr(n, "mutation_length", n.branch_length)) for n in nodes]
+    parts = {"marginal": [], "joint": [], "branch_lengths": []}
+    for _ in range(repeats + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t.infer_ancestral_sequences(marginal=True)
+        t1 = time.perf_counter()
+        t.infer_ancestral_sequences(marginal=False)
+        t2 = time.perf_counter()
+        t.optimize_branch_lengths_joint()
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        for n, (bl, ml) in zip(nodes, saved):
+            n.branch_length, n.mutation_length = bl, ml
+        parts["marginal"].append(t1 - t0)
+        parts["joint"].append(t2 - t1)
+        parts["branch_lengths"].append(t3 - t2)
+    out = {k: statistics.median(v[1:]) * 1e3 for k, v in parts.items()}
+    out["total_ms"] = sum(out.values())
+    out["note"] = ("one TreeTime step of this configuration through TreeAnc: infer_ancestral_sequences(marginal=True), "
+                   "(marginal=False), optimize_branch_lengths_joint; host clock, per-call set-up and copies included")
+    return out
 
 
 C2_WORKLOAD = ("c2: 500-tip Yule tree x 1500 amino-acid sites (21 states incl. gap, no compression), "

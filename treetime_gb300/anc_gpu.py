@@ -32,6 +32,16 @@ from .errors import MissingDataError
 from .tree import LAZY_ATTRS, Clade
 
 
+def _count_clades(root):
+    """Number of clades below and including `root` (one iterative walk)."""
+    n, stack = 0, [root]
+    while stack:
+        c = stack.pop()
+        n += 1
+        stack.extend(c.clades)
+    return n
+
+
 class ResultStore:
     """Host view of one reconstruction's device results; node attributes are
     built from it on first access."""
@@ -156,7 +166,7 @@ class GPUAncMixin:
         s = getattr(self, "_session", None)
         gtr_key = engine.model_key(self.gtr)
         if s is not None and s["root"] is self.tree.root and s["data"] is self.data and s["gtr_key"] == gtr_key \
-                and s["n_nodes"] == self.tree.count_terminals() + len(self.tree.get_nonterminals()) \
+                and s["n_nodes"] == _count_clades(self.tree.root) \
                 and not self._masks_changed(s):
             bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
             engine.check_exp(self.gtr, bl)
@@ -222,13 +232,12 @@ class GPUAncMixin:
         states[layout.n_int * P:].copy_(engine.torch().from_numpy(tip.reshape(-1)))
 
     def _clear_results(self, layout):
+        rm = frozenset(LAZY_ATTRS + ("_anc_src", "joint_Lx", "joint_Cx", "seq_idx", "marginal_log_Lx",
+                                     "marginal_subtree_LH_prefactor"))
         for n in layout.nodes:
             d = n.__dict__
-            for a in LAZY_ATTRS:
-                d.pop(a, None)
-            d.pop("_anc_src", None)
-            for a in ("joint_Lx", "joint_Cx", "seq_idx", "marginal_log_Lx", "marginal_subtree_LH_prefactor"):
-                d.pop(a, None)
+            for a in rm.intersection(d):
+                del d[a]
 
     def _install(self, src, layout):
         for n in layout.nodes:

@@ -136,8 +136,9 @@ struct PairObjective {
     double mu;
     const double* cnt;   // [q][q] truncated counts, parent-major
     int lane;
-    __device__ double operator()(double s) const {
-        const double t = s * s;
+    __device__ double operator()(double s) const { return at_t(s * s); }
+    // the objective at branch length t itself (prob_t_compressed takes t, the search s = sqrt(t))
+    __device__ double at_t(double t) const {
         double acc = 0.0;
         for (int idx = lane; idx < q * q; idx += 32) {
             const double c = cnt[idx];
@@ -194,7 +195,7 @@ __global__ void prob_t_pairs_kernel(int q, int64_t n, const double* __restrict__
         const int mi = model_of ? model_of[b] : 0;
         PairObjective f{q, m.V + (int64_t)mi * q * q, m.Vinv + (int64_t)mi * q * q, m.lam + (int64_t)mi * q,
                         m.mu[mi], cnt, lane};
-        const double v = t[b] < 0 ? kBig : f(sqrt(t[b]));
+        const double v = t[b] < 0 ? kBig : f.at_t(t[b]);
         if (lane == 0) out[b] = -v;
         __syncwarp();
     }

@@ -76,3 +76,24 @@ def test_tree_layout_caterpillar_and_polytomy():
     assert L.n_levels == 300
     L = _check_layout(parse_newick("((a,b,c,d)x,(e,f)y,g,h)r;"))
     assert L.n_levels == 2
+
+
+def test_uncompiled_alphabet_size_fails_before_launch():
+    """A custom alphabet whose size the tree kernels were not compiled for
+    raises NotImplementedError at the public call, before any device work; the
+    serving front end refuses such a job when it is created."""
+    from treetime_gb300 import GTR, TreeAnc
+    from treetime_gb300.engine import check_alphabet
+    from treetime_gb300.serving import Job
+    g = GTR.custom(pi=np.ones(7) / 7, W=np.ones((7, 7)), alphabet=np.array(list("ABCDEFG")))
+    aln = {"a": "ABCDEFG", "b": "ABCDEFF", "c": "ABCDEGG", "d": "GBCDEFG"}
+    t = TreeAnc(tree="((a:0.1,b:0.2):0.05,c:0.3,d:0.1);", aln=aln, gtr=g, verbose=0)
+    for marginal in (False, True):
+        with pytest.raises(NotImplementedError, match="alphabet size 7"):
+            t.infer_ancestral_sequences(marginal=marginal)
+    with pytest.raises(NotImplementedError, match="alphabet size 7"):
+        Job(None, g)
+    for q in (4, 5, 20, 21, 22):
+        check_alphabet(q)
+    with pytest.raises(NotImplementedError):
+        check_alphabet(5, site_specific=True)

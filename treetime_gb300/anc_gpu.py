@@ -172,6 +172,7 @@ class GPUAncMixin:
             engine.check_exp(self.gtr, bl)
             s["forest"].set_branch_lengths([bl])
             return s
+        engine.check_alphabet(self.gtr.n_states, self.gtr.is_site_specific)
         device = getattr(self, "device", None)
         layout = engine.TreeLayout(self.tree.root)
         name_to_row, codes = self._aln_index()

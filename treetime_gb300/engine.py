@@ -28,6 +28,20 @@ from .alphabets import MISSING_CODE, profile_lut
 TILE = 32
 WIDTHS = {q: (q + 3) // 4 * 4 for q in range(1, 33)}
 
+# Alphabet sizes the tree kernels (marginal, joint, site-specific marginal) are compiled for:
+# nucleotides without / with gap, amino acids without / with gap, and 22 (aa + gap + X style).
+COMPILED_ALPHABETS = (4, 5, 20, 21, 22)
+
+
+def check_alphabet(q, site_specific=False):
+    """Raise NotImplementedError for an alphabet size the tree kernels were not
+    compiled for (the FP64 and FP32 site-specific kernels have no 5-state
+    instance)."""
+    sizes = (4, 20, 21, 22) if site_specific else COMPILED_ALPHABETS
+    if q not in sizes:
+        raise NotImplementedError(f"alphabet size {q} is not compiled into the tree kernels "
+                                  f"(sizes {', '.join(map(str, sizes))})")
+
 _torch = None
 
 

@@ -50,6 +50,7 @@ class Job:
             raise ValueError("kind must be one of %s" % (KINDS,))
         if kind == "optimize" and getattr(gtr, "is_site_specific", False):
             raise NotImplementedError("branch-length jobs need a standard GTR model")
+        engine.check_alphabet(gtr.n_states, getattr(gtr, "is_site_specific", False))
         self.inputs = inputs
         self.gtr = gtr
         self.kind = kind

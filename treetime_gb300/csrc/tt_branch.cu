@@ -851,6 +851,45 @@ __global__ void __launch_bounds__(256) prob_t_profiles_grid_f32_kernel(ProfParam
 // non-aligned form: a warp may arrive from another instruction than the others).
 __device__ __forceinline__ void role_barrier() { asm volatile("barrier.sync 1, %0;" ::"r"(blockDim.x) : "memory"); }
 
+// Error-free addition (Knuth's TwoSum): s + e == a + b exactly, s = fl(a + b).  The result does not
+// depend on the order of a and b.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Sum of (hi, lo) float pairs over the warp, every lane receiving the same pair: TwoSum of the high
+// parts at each butterfly step, the low parts and the step's rounding error added in FP32.  Keeps
+// the compensated sums' accuracy (relative error ~1e-14) without FP64 instructions.
+__device__ __forceinline__ void warp_sum_pair(float& hi, float& lo) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, off), l2 = __shfl_xor_sync(0xffffffffu, lo, off);
+        float s, e;
+        two_sum(hi, h2, s, e);
+        hi = s;
+        lo = (lo + l2) + e;
+    }
+}
+
+// Per-SM launch tickets: the CTAs resident on one SM take consecutive tickets, from which each
+// picks the scheduler partition (warp slot mod 4) of its search warp and of its helper warp, so that
+// the serial FP64 chains of two CTAs do not share one partition's FP64 unit.
+__device__ unsigned int g_sm_ticket[256];
+
+__device__ __forceinline__ unsigned int warp_slot() {
+    unsigned int w;
+    asm volatile("mov.u32 %0, %%warpid;" : "=r"(w));
+    return w;
+}
+
+__device__ __forceinline__ unsigned int sm_id() {
+    unsigned int s;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(s));
+    return s;
+}
+
 template <int Q>
 __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams a) {
     extern __shared__ float smf[];
@@ -861,15 +900,35 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
     __shared__ int hcount, hall;
     __shared__ float Pt[Q * Q];
     __shared__ double Ed[Q];
-    __shared__ double red_total;
-    __shared__ int go;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ float2 redp[32];
+    __shared__ double hs_total;
+    __shared__ unsigned int slots[32];
+    __shared__ int go, lead_w, help_w;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int w = a.f.width;
     for (int j = threadIdx.x; j < 129; j += blockDim.x) {
         const double F = 1.0 + j / 128.0;
         log_tab[j] = log(F);
         inv_tab[j] = 1.0 / F;
     }
+    // roles: the search warp and the heavy-pattern helper on the partitions this CTA's ticket names
+    if (lane == 0) slots[warp] = warp_slot();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int ticket = atomicAdd(&g_sm_ticket[sm_id() & 255u], 1u);
+        const unsigned int want_lead = (2u * ticket) & 3u, want_help = (2u * ticket + 1u) & 3u;
+        int lw = -1, hw2 = -1;
+        for (int k = 0; k < nw; ++k)
+            if (lw < 0 && (slots[k] & 3u) == want_lead) lw = k;
+        if (lw < 0) lw = 0;
+        for (int k = 0; k < nw; ++k)
+            if (hw2 < 0 && k != lw && (slots[k] & 3u) == want_help) hw2 = k;
+        if (hw2 < 0) hw2 = (lw + 1) % nw;
+        lead_w = lw;
+        help_w = hw2;
+    }
+    __syncthreads();
+    const int lead = lead_w, help = help_w;
     const int cap = a.cap;
     for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
         const int64_t g = a.node_of[b];
@@ -1078,13 +1137,19 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
             }
             return false;
         };
-        // this thread's compensated sum of w log(pc.P(t).pp + 1e-24) over its patterns
-        auto pattern_sum = [&]() -> double {
+        // Patterns are summed by every warp but the helper (by every warp when there are no heavy
+        // patterns); this thread's rank among them and their number.
+        const bool helper_busy = H > 0;
+        const int rank = helper_busy ? (warp - (warp > help ? 1 : 0)) * 32 + lane : (int)threadIdx.x;
+        const int n_sum = helper_busy ? (nw - 1) * 32 : (int)blockDim.x;
+        // this thread's compensated sum of w log(pc.P(t).pp + 1e-24) over its patterns, as the pair
+        // (hi, lo) with value hi + lo
+        auto pattern_sum = [&](float& hi, float& lo) {
             float Pm[Q * Q];
 #pragma unroll
             for (int e = 0; e < Q * Q; ++e) Pm[e] = Pt[e];
             float sacc = 0.0f, c = 0.0f;
-            for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            for (int p = rank; p < P; p += n_sum) {
                 float pa[Q], pb[Q], wgt;
                 if (staged) {
                     if constexpr (Q == 4) {
@@ -1118,51 +1183,72 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                 c = (tsum - sacc) - y;
                 sacc = tsum;
             }
-            return (double)sacc - (double)c;
+            hi = sacc;
+            lo = -c;
         };
-        // the CTA-wide sum: every warp's total in red[], added by thread 0 (its result is needed
-        // by warp 0 only)
-        auto cta_sum = [&](double v) -> double {
-            v = warp_sum(v);
-            if (lane == 0) red[warp] = v;
-            role_barrier();
-            if (threadIdx.x == 0) {
-                double s2 = 0.0;
-                for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) s2 += red[w2];
-                red_total = s2;
+        // the warp's pair into redp[warp] (the helper, when busy, stores a zero pair)
+        auto warp_part = [&]() {
+            float hi = 0.0f, lo = 0.0f;
+            if (!(helper_busy && warp == help)) pattern_sum(hi, lo);
+            warp_sum_pair(hi, lo);
+            if (lane == 0) redp[warp] = make_float2(hi, lo);
+        };
+        // the helper's FP64 sum over the listed heavy patterns at the published exponentials
+        auto heavy_part = [&]() {
+            double hs = 0.0;
+            for (int h = lane; h < H; h += 32) {
+                double res = 0.0;
+#pragma unroll
+                for (int k = 0; k < Q; ++k) res = fma(hu[h][k], Ed[k], res);
+                hs = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), hs);
             }
-            role_barrier();
-            return red_total;
+            hs = warp_sum(hs);
+            if (lane == 0) hs_total = hs;
         };
-        // Warp 0 runs the search; the other warps only take part in each evaluation's pattern sum.
-        // Per evaluation every thread passes three barriers: P(t) published, warp totals
-        // written, CTA total written; after the search one more releases the other warps.
-        if (warp == 0) {
+        // The search warp runs Brent; per evaluation it publishes exp(mu lam t) and P(t) (barrier 1),
+        // every warp then adds its patterns (the helper its heavy patterns instead) and writes its
+        // part (barrier 2), after which the search warp combines the parts alone: the other warps
+        // write again only after the next barrier 1.  After the search one more barrier 1 releases
+        // the other warps.
+        if (warp == lead) {
             double hamming = 1.0 - ovsum / msum;
             hamming = hamming > 0.0 ? hamming : 0.0;
+            // this lane's P(t) entry as sum_k W[k] exp(mu lam_k t), W[k] = V[i][k] V^-1[k][j]
+            double Wk[Q];
+            const double mulam = lane < Q ? mu * lam[lane] : 0.0;
+            {
+                const int i = lane < Q * Q ? lane / Q : 0, j = lane < Q * Q ? lane - (lane / Q) * Q : 0;
+#pragma unroll
+                for (int k = 0; k < Q; ++k) Wk[k] = V[i * Q + k] * Vi[k * Q + j];
+            }
             auto f = [&](double s) -> double {
                 const double t = s * s;
-                if (lane < Q) Ed[lane] = exp(mu * lam[lane] * t);
+                if (lane < Q) Ed[lane] = exp(mulam * t);
                 __syncwarp();
                 if (lane < Q * Q) {
-                    const int i = lane / Q, j = lane - (lane / Q) * Q;
-                    double v = 0.0;
+                    double v = Wk[0] * Ed[0];
 #pragma unroll
-                    for (int k = 0; k < Q; ++k) v = fma(V[i * Q + k], Ed[k] * Vi[k * Q + j], v);
-                    Pt[lane] = (float)(v > 0.0 ? v : 0.0);
+                    for (int k = 1; k < Q; ++k) v = fma(Wk[k], Ed[k], v);
+                    Pt[lane] = fmaxf((float)v, 0.0f);
                 }
-                double hs = 0.0;
-                for (int h = lane; h < H; h += 32) {
-                    double res = 0.0;
-#pragma unroll
-                    for (int k = 0; k < Q; ++k) res = fma(hu[h][k], Ed[k], res);
-                    hs = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), hs);
-                }
-                hs = warp_sum(hs);
+                // exp(t^2 / 1e4) - 1 in FP32: t <= 4 on the search interval, so the term is below
+                // 1.6e-3 and FP32 leaves an absolute error under 1e-10
+                const float tf = (float)t;
+                const float pen = expm1f(tf * tf * 1e-4f);
                 if (lane == 0) go = 1;
                 role_barrier();
-                const double tot = cta_sum(pattern_sum());
-                return -(tot + hs) + exp(t * t / 10000.0);
+                warp_part();
+                role_barrier();
+                float hi = 0.0f, lo = 0.0f;
+                for (int k = 0; k < nw; ++k) {
+                    const float2 r2 = redp[k];
+                    float sn, en;
+                    two_sum(hi, r2.x, sn, en);
+                    hi = sn;
+                    lo = (lo + r2.y) + en;
+                }
+                const double tot = (double)hi + (double)lo + (helper_busy ? hs_total : 0.0);
+                return -tot + (1.0 + (double)pen);
             };
             BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
             if (lane == 0) {
@@ -1175,7 +1261,9 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
             while (true) {
                 role_barrier();
                 if (!go) break;
-                cta_sum(pattern_sum());
+                if (helper_busy && warp == help) heavy_part();
+                warp_part();
+                role_barrier();
             }
         }
         __syncthreads();

@@ -17,6 +17,7 @@ collective on the data path; rank 0 prints the max-over-ranks timing.
 """
 
 import argparse
+import collections
 import json
 import os
 import statistics
@@ -1206,6 +1207,24 @@ def run_c4(args):
     with ClockSampler(local) as clk:
         done, wall = srv.serve(jobs, arrivals)
     st = serving.latency_stats(done)
+    # device time of each kind of job run alone (one slot, events between phases), on a sample of
+    # the pool, and what the served mix would take at those times back to back
+    solo = {}
+    sample = {"nucleotide_marginal": [serving.Job(nuc[k], nuc_gtrs[k], "marginal") for k in range(16)],
+              "nucleotide_optimize": [serving.Job(nuc[k], nuc_gtrs[k], "optimize") for k in range(16)],
+              "protein_marginal": [serving.Job(prot[k % len(prot)][0], prot[k % len(prot)][1], "marginal")
+                                   for k in range(4)]}
+    for kind, js in sample.items():
+        serving.Server(device=dev, max_slots=1, phase_events=True).serve(js, [0.0] * len(js))
+        ph = collections.Counter()
+        for j in js:
+            ph.update(j.phase_ms)
+        solo[kind] = {k: round(v / len(js), 3) for k, v in ph.items()}
+        solo[kind]["node_patterns_per_iteration"] = float(np.mean([j.node_patterns for j in js]))
+    served_kind = lambda j: ("protein_marginal" if j.site_specific else
+                             "nucleotide_optimize" if j.kind == "optimize" else "nucleotide_marginal")
+    solo_s = sum(sum(v for k, v in solo[served_kind(j)].items() if k != "node_patterns_per_iteration")
+                 for j in done) / 1e3
     if rank != 0:
         return None
     return {
@@ -1228,6 +1247,8 @@ def run_c4(args):
         "gpu_launches": int(sum(j.iterations * (2 if j.site_specific else 3 + (2 if j.kind == "optimize" else 0))
                                 for j in done)),
         "clocks": clk.summary(),
+        "solo_device_ms_per_job": solo,
+        "solo_device_s_for_the_served_mix": round(solo_s, 3),
     }
 
 

@@ -891,7 +891,7 @@ __device__ __forceinline__ unsigned int sm_id() {
 }
 
 template <int Q>
-__global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams a) {
+__global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfParams a) {
     extern __shared__ float smf[];
     __shared__ double red[32];
     __shared__ double log_tab[129], inv_tab[129];
@@ -903,6 +903,7 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
     __shared__ float2 redp[32];
     __shared__ double hs_total;
     __shared__ unsigned int slots[32];
+    __shared__ int hwarp[32];
     __shared__ int go, lead_w, help_w;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int w = a.f.width;
@@ -1059,11 +1060,14 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
         }
         const double msum = block_sum((double)ms - (double)msc, red);
         const double ovsum = block_sum((double)os - (double)osc, red);
-        // heavy patterns (weight above kHeavyWeight), the first kHeavyMax in pattern order
-        if (warp == 0) {
-            int count = 0;
-            for (int base = 0; base < P; base += 32) {
-                const int p = base + lane;
+        // heavy patterns (weight above kHeavyWeight), the first kHeavyMax in pattern order: each warp
+        // counts those of a contiguous run of 32-pattern blocks, the counts give each warp its first
+        // list position, and the warps whose runs start within the list write their entries
+        {
+            const int nblk = (P + 31) >> 5, per = (nblk + nw - 1) / nw;
+            const int b0 = warp * per, b1 = min(nblk, b0 + per);
+            auto heavy_mask = [&](int blk) -> unsigned {
+                const int p = blk * 32 + lane;
                 float wgt = 0.0f;
                 if (p < P) {
                     if (staged) {
@@ -1073,15 +1077,27 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                         fetch32(p, pa, pb, wgt, m32);
                     }
                 }
-                const bool heavy = p < P && wgt > kHeavyWeight;
-                const unsigned bal = __ballot_sync(0xffffffffu, heavy);
-                const int pos = count + __popc(bal & ((1u << lane) - 1u));
-                if (heavy && pos < kHeavyMax) hidx[pos] = p;
-                count += __popc(bal);
+                return __ballot_sync(0xffffffffu, p < P && wgt > kHeavyWeight);
+            };
+            int count = 0;
+#pragma unroll 4
+            for (int blk = b0; blk < b1; ++blk) count += __popc(heavy_mask(blk));
+            if (lane == 0) hwarp[warp] = count;
+            __syncthreads();
+            int off = 0, total = 0;
+            for (int k = 0; k < nw; ++k) {
+                off += k < warp ? hwarp[k] : 0;
+                total += hwarp[k];
             }
-            if (lane == 0) {
-                hcount = count < kHeavyMax ? count : kHeavyMax;
-                hall = count;
+            for (int blk = b0; blk < b1 && off < kHeavyMax && count > 0; ++blk) {
+                const unsigned bal = heavy_mask(blk);
+                const int pos = off + __popc(bal & ((1u << lane) - 1u));
+                if (((bal >> lane) & 1u) && pos < kHeavyMax) hidx[pos] = blk * 32 + lane;
+                off += __popc(bal);
+            }
+            if (threadIdx.x == 0) {
+                hcount = total < kHeavyMax ? total : kHeavyMax;
+                hall = total;
             }
         }
         __syncthreads();
@@ -1149,27 +1165,7 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
 #pragma unroll
             for (int e = 0; e < Q * Q; ++e) Pm[e] = Pt[e];
             float sacc = 0.0f, c = 0.0f;
-            for (int p = rank; p < P; p += n_sum) {
-                float pa[Q], pb[Q], wgt;
-                if (staged) {
-                    if constexpr (Q == 4) {
-                        const float4 b4 = reinterpret_cast<const float4*>(ppS)[p];
-                        const float4 a4 = reinterpret_cast<const float4*>(pcS)[p];
-                        pb[0] = b4.x; pb[1] = b4.y; pb[2] = b4.z; pb[3] = b4.w;
-                        pa[0] = a4.x; pa[1] = a4.y; pa[2] = a4.z; pa[3] = a4.w;
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < Q; ++i) {
-                            pb[i] = ppS[p * Q + i];
-                            pa[i] = pcS[p * Q + i];
-                        }
-                    }
-                    wgt = wS[p];
-                } else {
-                    float m32;
-                    fetch32(p, pa, pb, wgt, m32);
-                    if (wgt > 0.5f * kHeavyWeight && H > 0 && listed(p)) continue;  // evaluated in FP64
-                }
+            auto add = [&](const float* pa, const float* pb, float wgt) {
                 float res = 0.0f;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
@@ -1182,6 +1178,46 @@ __global__ void __launch_bounds__(256) optimal_t_profiles_f32_kernel(ProfParams 
                 const float tsum = sacc + y;
                 c = (tsum - sacc) - y;
                 sacc = tsum;
+            };
+            auto load = [&](int p, float* pa, float* pb, float& wgt) {
+                if constexpr (Q == 4) {
+                    const float4 b4 = reinterpret_cast<const float4*>(ppS)[p];
+                    const float4 a4 = reinterpret_cast<const float4*>(pcS)[p];
+                    pb[0] = b4.x; pb[1] = b4.y; pb[2] = b4.z; pb[3] = b4.w;
+                    pa[0] = a4.x; pa[1] = a4.y; pa[2] = a4.z; pa[3] = a4.w;
+                } else {
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        pb[i] = ppS[p * Q + i];
+                        pa[i] = pcS[p * Q + i];
+                    }
+                }
+                wgt = wS[p];
+            };
+            if (staged) {
+                // kBatch patterns' rows loaded before any is used: the loads of the workspace slice
+                // (L2) overlap instead of each waiting for the previous pattern's sum
+                constexpr int kBatch = 4;
+                int p = rank;
+                for (; p + (kBatch - 1) * n_sum < P; p += kBatch * n_sum) {
+                    float pa[kBatch][Q], pb[kBatch][Q], wgt[kBatch];
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) load(p + u * n_sum, pa[u], pb[u], wgt[u]);
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) add(pa[u], pb[u], wgt[u]);
+                }
+                for (; p < P; p += n_sum) {
+                    float pa[Q], pb[Q], wgt;
+                    load(p, pa, pb, wgt);
+                    add(pa, pb, wgt);
+                }
+            } else {
+                for (int p = rank; p < P; p += n_sum) {
+                    float pa[Q], pb[Q], wgt, m32;
+                    fetch32(p, pa, pb, wgt, m32);
+                    if (wgt > 0.5f * kHeavyWeight && H > 0 && listed(p)) continue;  // evaluated in FP64
+                    add(pa, pb, wgt);
+                }
             }
             hi = sacc;
             lo = -c;

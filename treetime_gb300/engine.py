@@ -446,7 +446,12 @@ class Forest:
         up.add("parent", np.concatenate(par)).add("tip_row", np.concatenate(trow))
         self.bl_host = np.concatenate(bl)
         up.add("bl", self.bl_host).add("mult", np.concatenate(mult))
-        up.add("codes", np.concatenate(codes) if codes else np.zeros(1, np.uint8))
+        # a single tree's tip codes already in page-locked memory (TreeInput.tip_codes_pinned, a torch
+        # uint8 tensor) are copied on their own; otherwise they join the staging buffer
+        pinned = getattr(inputs[0], "tip_codes_pinned", None) if len(inputs) == 1 else None
+        if pinned is None:
+            up.add("codes", codes[0] if len(codes) == 1 else (np.concatenate(codes) if codes
+                                                               else np.zeros(1, np.uint8)))
         self.has_masks = mask_elems > 0
         if self.has_masks:
             up.add("mask_off", np.concatenate(moff)).add("masks", np.concatenate(mvals))
@@ -457,7 +462,12 @@ class Forest:
         self._dev_buffer = d["_buffer"]
         self.d_trees, self.d_level, self.d_child_off = d["trees"], d["level"], d["child_off"]
         self.d_child_idx, self.d_parent, self.d_tip_row = d["child_idx"], d["parent"], d["tip_row"]
-        self.d_bl, self.d_mult, self.d_codes = d["bl"], d["mult"], d["codes"]
+        if pinned is None:
+            self.d_codes = d["codes"]
+        else:
+            self.d_codes = torch().empty(max(1, pinned.numel()), dtype=torch().uint8, device=dev)
+            self.d_codes[:pinned.numel()].copy_(pinned, non_blocking=True)
+        self.d_bl, self.d_mult = d["bl"], d["mult"]
         self.d_mask_off = d.get("mask_off")
         self.d_masks = d.get("masks")
         self.d_work, self.d_work_f32 = d["work"], d["work_f32"]

@@ -16,15 +16,19 @@ The scheduler runs on the calling thread.  Jobs are admitted in arrival order
 while a slot is free and the job's device footprint fits the memory budget
 (admission by free HBM); an admitted job keeps its schedule, inputs and
 profile buffers resident on the device for all its iterations and runs on its
-own CUDA stream, so the kernels of every admitted job overlap on the GPU.  The
-scheduler polls the jobs' events: a job whose iteration has finished gets its
-next iteration enqueued at once (iteration-level scheduling), a finished job
-has its results copied back and leaves, and its slot and memory go to the next
-job in the queue.  A job's numbers do not depend on which other jobs share the
-GPU with it (each kernel reads only its own job's buffers)."""
+own CUDA stream, so the kernels of every admitted job overlap on the GPU.  At
+admission all of a job's iterations and the copy of its results to pinned host
+memory are queued on its stream at once (the iterations need no host decision
+in between), so the host does no per-iteration round trip.  Submitting a job
+stages its tip codes into page-locked memory on the submitting thread, so the
+scheduler's upload is one asynchronous copy; a collector thread turns the
+finished jobs' pinned results into arrays.  A job's numbers do not depend on
+which other jobs share the GPU with it (each kernel reads only its own job's
+buffers)."""
 
 import collections
 import copy
+import queue
 import threading
 import time
 
@@ -55,6 +59,8 @@ class Job:
         self.gtr = gtr
         self.kind = kind
         self.iterations = int(iterations)
+        if self.iterations < 1:
+            raise ValueError("a job runs at least one iteration")
         self.site_specific = bool(getattr(gtr, "is_site_specific", False))
         if job_id is None:
             job_id = Job._next_id
@@ -62,7 +68,17 @@ class Job:
         self.id = job_id
         self.t_submit = self.t_admit = self.t_done = None
         self.result = None
+        self.error = None
         self.footprint = footprint(inputs, gtr.n_states, kind)
+        self._codes_buf = None
+
+    def stage(self, pool):
+        """Copy the tip codes into a page-locked buffer of `pool` (done by the
+        submitting thread; the admission's upload then copies from it)."""
+        codes = self.inputs.tip_codes.reshape(-1)
+        buf = pool.take(codes.nbytes)
+        np.copyto(buf[:codes.nbytes].numpy(), codes)
+        self._codes_buf = buf
 
     @property
     def node_patterns(self):
@@ -103,20 +119,36 @@ def plan_admissions(queue, free_slots, free_bytes):
 
 class _PinnedPool:
     """Reusable page-locked host buffers by power-of-two size class (a fresh
-    page-locked allocation of a large job's results costs milliseconds)."""
+    page-locked allocation of a large job's results costs milliseconds); shared
+    by the submitting, scheduling and collecting threads."""
 
     def __init__(self):
         self.free = collections.defaultdict(list)
+        self.lock = threading.Lock()
 
     def take(self, nbytes):
         t = engine.torch()
         cls = max(1 << 12, 1 << int(np.ceil(np.log2(max(1, nbytes)))))
-        if self.free[cls]:
-            return self.free[cls].pop()
+        with self.lock:
+            if self.free[cls]:
+                return self.free[cls].pop()
         return t.empty(cls, dtype=t.uint8, pin_memory=True)
 
     def give(self, buf):
-        self.free[buf.numel()].append(buf)
+        with self.lock:
+            self.free[buf.numel()].append(buf)
+
+
+_POOL = None
+
+
+def pinned_pool():
+    """The process's pinned-buffer pool (one per process, so that warm-up runs
+    prime it for later servers)."""
+    global _POOL
+    if _POOL is None:
+        _POOL = _PinnedPool()
+    return _POOL
 
 
 def _view(buf, shape, dtype):
@@ -136,6 +168,8 @@ class _Active:
         dev = server.device
         ti = copy.copy(job.inputs)
         ti.model = 0  # the job's own one-model DeviceModel
+        if job._codes_buf is not None:
+            ti.tip_codes_pinned = job._codes_buf[:ti.tip_codes.size]
         hs = server.host_s
         with t.cuda.stream(self.stream):
             self.forest = engine.Forest([ti], job.gtr.n_states, device=dev)
@@ -152,9 +186,9 @@ class _Active:
                 self._prepare_optimize(dev)
                 hs["admit.optimize_setup"] += time.perf_counter() - t1
         self.it = 0
-        self.event = t.cuda.Event()
         self.done_event = None
         self.host = None
+        self.phase_events = [] if server.phase_events else None
 
     def _prepare_optimize(self, dev):
         t = engine.torch()
@@ -177,7 +211,10 @@ class _Active:
         """Queue one iteration on the job's stream (no host synchronisation)."""
         t = engine.torch()
         job = self.job
+        ev = self.phase_events
         with t.cuda.stream(self.stream):
+            if ev is not None:
+                ev.append(("start", self._event()))
             if job.site_specific:
                 out = engine.marginal_site_specific(self.forest, job.gtr, self.bufs, precision="f32", sync=False)
             else:
@@ -186,11 +223,31 @@ class _Active:
                                       tip_outgroup=keep, sync=False)
             self.lh[self.it].copy_(out["tree_lh"][0])
             self.status.copy_(t.maximum(self.status, self.bufs.get("status", (1,), t.int32)))
+            if ev is not None:
+                ev.append(("marginal", self._event()))
             if job.kind == "optimize":
                 self._branch_lengths(out)
+                if ev is not None:
+                    ev.append(("branch_lengths", self._event()))
             self.out = out
-            self.event.record(self.stream)
         self.it += 1
+
+    def _event(self):
+        e = engine.torch().cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+    def phase_ms(self):
+        """Device milliseconds per phase (marginal, branch_lengths) summed over
+        the iterations, from the events recorded when the server was created
+        with ``phase_events=True`` (meaningful for a job that ran alone)."""
+        out = collections.Counter()
+        prev = None
+        for name, e in self.phase_events or ():
+            if prev is not None and name != "start":
+                out[name] += prev.elapsed_time(e)
+            prev = e
+        return out
 
     def _branch_lengths(self, out):
         t = engine.torch()
@@ -232,15 +289,25 @@ class _Active:
             self.done_event.record(self.stream)
 
     def collect(self):
+        """Arrays from the pinned results (the job's stream has finished); a
+        device error status becomes the job's ``error``, raised as
+        ``engine.check`` raises it.  Returns the pinned buffers to the pool."""
         lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
-        st = int(self.host["status"][0])
-        if st:
-            engine.check(st, "serving job %s" % self.job.id)
-        self.job.result = dict(tree_lh=self.host["tree_lh"].numpy().copy(),
-                               states=self.host["states"].numpy().reshape(lay.n_int, P).copy(),
-                               branch_lengths=self.host["bl"].numpy().copy())
-        for b in self._bufs:
-            self.pool.give(b)
+        try:
+            st = int(self.host["status"][0])
+            if st:
+                engine.check(st, "serving job %s" % self.job.id)
+            self.job.result = dict(tree_lh=self.host["tree_lh"].numpy().copy(),
+                                   states=self.host["states"].numpy().reshape(lay.n_int, P).copy(),
+                                   branch_lengths=self.host["bl"].numpy().copy())
+        except Exception as e:  # noqa: BLE001 -- handed to the caller of run()
+            self.job.error = e
+        finally:
+            for b in self._bufs:
+                self.pool.give(b)
+            if self.job._codes_buf is not None:
+                self.pool.give(self.job._codes_buf)
+                self.job._codes_buf = None
 
 
 class Server:
@@ -250,7 +317,7 @@ class Server:
     ``hbm_bytes``: device-memory budget for admitted jobs (default: 80% of the
     free memory when the server starts)."""
 
-    def __init__(self, device=None, max_slots=16, hbm_bytes=None, poll_s=2e-5):
+    def __init__(self, device=None, max_slots=16, hbm_bytes=None, poll_s=2e-5, phase_events=False):
         t = engine.torch()
         self.device = engine.require_device(device)
         if hbm_bytes is None:
@@ -259,20 +326,28 @@ class Server:
         self.max_slots = int(max_slots)
         self.hbm_bytes = int(hbm_bytes)
         self.poll_s = poll_s
+        # per-phase device times of each job (job.phase_ms), for jobs run alone
+        self.phase_events = bool(phase_events)
         self._queue = collections.deque()
         self._lock = threading.Lock()
         self._active = []
         self._stream_pool = []
-        self._pinned = _PinnedPool()
+        self._pinned = pinned_pool()
+        self._finished = queue.Queue()
+        self._collecting = 0
+        self._errors = []
         self.done = []
         self.peak_active = 0
         self.peak_bytes = 0
-        # host seconds spent per scheduler phase (admission, enqueueing, result copies, collection)
+        # host seconds spent per phase (admission, enqueueing, result copies; collection on the
+        # collector thread)
         self.host_s = collections.Counter()
 
     def submit(self, job):
-        """Queue a job (thread-safe); it is admitted by the scheduler loop."""
+        """Queue a job (thread-safe): its tip codes are staged into pinned
+        memory on the calling thread; the scheduler loop admits it."""
         job.t_submit = time.perf_counter()
+        job.stage(self._pinned)
         with self._lock:
             self._queue.append(job)
 
@@ -282,16 +357,15 @@ class Server:
     def step(self):
         """One scheduler pass; returns True when something happened."""
         busy = False
-        # finished jobs leave first: their slots and memory go to the queue
+        # finished jobs leave first: their slots and memory go to the queue, their results to the
+        # collector thread
         still = []
         for a in self._active:
-            if a.done_event is not None and a.done_event.query():
-                t0 = time.perf_counter()
-                a.collect()
-                self.host_s["collect"] += time.perf_counter() - t0
-                a.job.t_done = time.perf_counter()
-                self.done.append(a.job)
+            if a.done_event.query():
                 self._stream_pool.append(a.stream)
+                with self._lock:
+                    self._collecting += 1
+                self._finished.put(a)
                 busy = True
             else:
                 still.append(a)
@@ -305,39 +379,60 @@ class Server:
             job.t_admit = time.perf_counter()
             a = _Active(job, self)
             t1 = time.perf_counter()
-            a.enqueue_iteration()
+            while a.it < job.iterations:
+                a.enqueue_iteration()
+            t2 = time.perf_counter()
+            a.enqueue_results()
             self.host_s["admit"] += t1 - job.t_admit
-            self.host_s["enqueue"] += time.perf_counter() - t1
+            self.host_s["enqueue"] += t2 - t1
+            self.host_s["results"] += time.perf_counter() - t2
             self._active.append(a)
             busy = True
         self.peak_active = max(self.peak_active, len(self._active))
         self.peak_bytes = max(self.peak_bytes, self._used_bytes())
-        # iteration-level scheduling: a job whose iteration finished gets the next one now
-        for a in self._active:
-            if a.done_event is None and a.event.query():
-                t0 = time.perf_counter()
-                if a.it < a.job.iterations:
-                    a.enqueue_iteration()
-                    self.host_s["enqueue"] += time.perf_counter() - t0
-                else:
-                    a.enqueue_results()
-                    self.host_s["results"] += time.perf_counter() - t0
-                busy = True
         return busy
+
+    def _collect_loop(self):
+        while True:
+            a = self._finished.get()
+            if a is None:
+                return
+            t0 = time.perf_counter()
+            a.collect()
+            if a.phase_events is not None:
+                a.job.phase_ms = dict(a.phase_ms())
+            a.job.t_done = time.perf_counter()
+            with self._lock:
+                self.host_s["collect"] += a.job.t_done - t0
+                self.done.append(a.job)
+                if a.job.error is not None:
+                    self._errors.append(a.job.error)
+                self._collecting -= 1
 
     def pending(self):
         with self._lock:
-            return len(self._queue) + len(self._active)
+            return len(self._queue) + len(self._active) + self._collecting
 
     def run(self, until=None):
         """Scheduler loop until the queue and the GPU are empty (and, when
-        given, until() is true)."""
-        while True:
-            busy = self.step()
-            if not busy:
-                if self.pending() == 0 and (until is None or until()):
-                    return
-                time.sleep(self.poll_s)
+        given, until() is true).  Raises the first device error of a job
+        finished in this run, after the others have finished."""
+        collector = threading.Thread(target=self._collect_loop, daemon=True)
+        collector.start()
+        try:
+            while True:
+                busy = self.step()
+                if not busy:
+                    if self.pending() == 0 and (until is None or until()):
+                        break
+                    time.sleep(self.poll_s)
+        finally:
+            self._finished.put(None)
+            collector.join()
+        with self._lock:
+            errors, self._errors = self._errors, []
+        if errors:
+            raise errors[0]
 
     def serve(self, jobs, arrival_times):
         """Submit ``jobs`` at ``arrival_times`` (seconds from now, from a feeder

@@ -135,9 +135,9 @@ class ClockSampler:
         return out
 
 
-def build_workload(seed=1):
+def build_workload(seed=1, **over):
     from treetime_gb300 import TreeAnc, synth
-    wl = synth.make_workload("c1", seed=seed)
+    wl = synth.make_workload("c1", seed=seed, **over)
     t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision="f32")
     return t, wl
 
@@ -845,27 +845,37 @@ def run_brent(args):
     world, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    t, wl = build_workload()
+    over = {} if args.brent_invariant is None else {"invariant_frac": args.brent_invariant}
+    t, wl = build_workload(**over)
     t.device = dev
     t.infer_ancestral_sequences(marginal=True)
     nodes = [n for n in t.tree.find_clades() if n.up is not None]
     P = t.data.compressed_length
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
+    dev_ms = []
+
     def timed(tt, nn, k, w):
         for _ in range(w):
             tt._marginal_branch_lengths(nn, 1e-10)
         ts = []
+        dev_ms.clear()
         for _ in range(k):
             flush.zero_()
             torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             t0 = time.perf_counter()
+            e0.record()
             res = tt._marginal_branch_lengths(nn, 1e-10)
+            e1.record()
             ts.append(time.perf_counter() - t0)
+            e1.synchronize()
+            dev_ms.append(e0.elapsed_time(e1))
         return statistics.median(ts) * 1e3, res
 
     with ClockSampler(local) as clk:
         ms, r32 = timed(t, nodes, args.steps, args.warmup)
+    device_ms = statistics.median(dev_ms)
     ms = _reduce_max(ms, dev, world)
     t64 = TreeAnc(tree=parse_newick(to_newick(t.tree)), aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision="f64",
                   device=dev)
@@ -881,9 +891,11 @@ def run_brent(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
         "config": {"workload": BRENT_WORKLOAD, "branches": len(nodes), "patterns": P,
+                   "invariant_frac": 0.9 if args.brent_invariant is None else args.brent_invariant,
                    "l2": "flushed (512 MiB write) before every timed step", "parallelism": "single GPU",
                    "timing": "host clock around TreeAnc._marginal_branch_lengths (uploads of the branch lists, "
                              "two launches, the lengths back)"},
+        "device_ms_per_step": device_ms,
         "fp64_path": {"ms_per_step": ms64, "value": len(n64) / (ms64 * 1e-3),
                       "note": "FP64 reconstruction, FP64 objective (optimal_t_profiles_kernel)"},
         "f32_vs_f64_lengths": {"median_rel": float(np.median(rel)), "p99_rel": float(np.percentile(rel, 99)),
@@ -1409,6 +1421,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="c3: skip the FP64 arm (profiling runs)")
     ap.add_argument("--c4-seconds", type=float, default=10.0, help="c4: arrival window (s)")
     ap.add_argument("--c4-rate", type=float, default=200.0, help="c4: mean arrival rate (requests/s)")
+    ap.add_argument("--brent-invariant", type=float, default=None,
+                    help="brent: invariant-site fraction of the 2,000-tip alignment (default 0.9; lower values "
+                         "give more patterns than the kernel's shared memory holds)")
     ap.add_argument("--c1-batch", type=int, default=8, help="c1: reconstructions in the batched measurement (1: none)")
     ap.add_argument("--c4-slots", type=int, default=16, help="c4: jobs admitted at the same time")
     ap.add_argument("--shape", default="", help="c1: fixed FP32 launch shape threads/ctas_per_sm/ranges_per_sm "

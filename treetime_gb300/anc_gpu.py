@@ -509,9 +509,13 @@ class GPUAncMixin:
         model = engine.model_for(self.gtr, getattr(self, "device", None))
         res = np.zeros(len(nodes))
         info = np.zeros(len(nodes), dtype=np.int32)
+        # both branch groups are queued before either result is read back
+        pending = []
         for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
             t, inf = engine.optimal_t_profiles(sess["forest"], model, kk, pp, pp_row, pc, pc_row,
                                                self._gpu_precision(), self.gtr.gap_index, True, tol)
+            pending.append((idx, t, inf))
+        for idx, t, inf in pending:
             res[idx] = t.cpu().numpy()
             info[idx] = inf.cpu().numpy()
         if (info == -1).any():

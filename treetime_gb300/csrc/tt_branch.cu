@@ -904,6 +904,7 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
     __shared__ double hs_total;
     __shared__ unsigned int slots[32];
     __shared__ int hwarp[32];
+    __shared__ float lutS[256 * Q];
     __shared__ int go, lead_w, help_w;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int w = a.f.width;
@@ -931,6 +932,11 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
     __syncthreads();
     const int lead = lead_w, help = help_w;
     const int cap = a.cap;
+    // tip profiles as FP32, and whether profile rows can be read as float4
+    for (int j = threadIdx.x; j < 256 * Q; j += blockDim.x) lutS[j] = (float)a.m.lut[j];
+    const bool vec_rows = a.prec == TT_PREC_F32 && (w & 3) == 0 && (reinterpret_cast<uintptr_t>(a.pp) & 15) == 0 &&
+                          (a.pc == nullptr || (reinterpret_cast<uintptr_t>(a.pc) & 15) == 0);
+    __syncthreads();
     for (int64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
         const int64_t g = a.node_of[b];
         const tt_tree tr = a.f.trees[tree_of(a.f.trees, a.f.n_trees, g)];
@@ -957,65 +963,40 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
         const bool tipb = a.pc_row[b] < 0;
         const int trow = tipb ? a.f.tip_row[g] : -1;
         const int64_t mo = a.f.mask_off ? a.f.mask_off[g] : -1;
-        // one pattern's FP32 rows and weights from the stored profiles
-        auto fetch = [&](int p, float* pa, float* pb, float& wgt, double& m64, double& ov64) {
-            const int64_t pr = (a.pp_row[b] + p) * w;
-#pragma unroll
-            for (int j = 0; j < Q; ++j)
-                pb[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
-                                              : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
-            double pcd[Q];
-            if (tipb) {
-                const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
-#pragma unroll
-                for (int i = 0; i < Q; ++i) pcd[i] = a.m.lut[code * Q + i];
-            } else {
-                const int64_t cr = (a.pc_row[b] + p) * w;
-                double s = 0.0;
-#pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    pcd[i] = a.prec == TT_PREC_F32 ? (double)reinterpret_cast<const float*>(a.pc)[cr + i]
-                                                   : reinterpret_cast<const double*>(a.pc)[cr + i];
-                    s += pcd[i];
+        // one pattern's FP32 rows and weight (mult*mask*non_gap) and its mult*mask, FP32 only; rows
+        // of FP32 profiles are read 16 bytes at a time when the buffers allow it
+        const int64_t pp_base = a.pp_row[b], pc_base = a.pc_row[b];
+        auto row32 = [&](const void* base, int64_t off, float* out) {
+            if (vec_rows) {
+                const float4* r4 = reinterpret_cast<const float4*>(static_cast<const float*>(base) + off);
+                const float4 x = __ldg(r4);
+                out[0] = x.x;
+                if (Q > 1) out[1] = x.y;
+                if (Q > 2) out[2] = x.z;
+                if (Q > 3) out[3] = x.w;
+                if constexpr (Q > 4) {
+                    const float4 y = __ldg(r4 + 1);
+                    out[4] = y.x;
                 }
-                if (a.prec == TT_PREC_F32)
+            } else {
 #pragma unroll
-                    for (int i = 0; i < Q; ++i) pcd[i] /= s;
+                for (int j = 0; j < Q; ++j)
+                    out[j] = a.prec == TT_PREC_F32 ? static_cast<const float*>(base)[off + j]
+                                                   : (float)static_cast<const double*>(base)[off + j];
             }
-            double m = a.f.mult[tr.pat_base + p];
-            if (mo >= 0) m *= a.f.masks[mo + p];
-            double ov = 0.0;
-#pragma unroll
-            for (int i = 0; i < Q; ++i) ov += (double)pb[i] * pcd[i];
-            m64 = m;
-            ov64 = m * ov;
-            if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) m *= (1.0 - (double)pb[a.gap]) * (1.0 - pcd[a.gap]);
-#pragma unroll
-            for (int i = 0; i < Q; ++i) pa[i] = (float)pcd[i];
-            wgt = (float)m;
-            return m;
         };
-        // one pattern's FP32 rows and weight (mult*mask*non_gap) and its mult*mask, FP32 only
         auto fetch32 = [&](int p, float* pa, float* pb, float& wgt, float& m32) {
-            const int64_t pr = (a.pp_row[b] + p) * w;
-#pragma unroll
-            for (int j = 0; j < Q; ++j)
-                pb[j] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pp)[pr + j]
-                                              : (float)reinterpret_cast<const double*>(a.pp)[pr + j];
+            row32(a.pp, (pp_base + p) * w, pb);
             if (tipb) {
                 const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) pa[i] = (float)a.m.lut[code * Q + i];
+                for (int i = 0; i < Q; ++i) pa[i] = lutS[code * Q + i];
             } else {
-                const int64_t cr = (a.pc_row[b] + p) * w;
-                float sc = 0.0f;
+                row32(a.pc, (pc_base + p) * w, pa);
+                if (a.prec == TT_PREC_F32) {  // FP32 partials are power-of-two scaled: normalise
+                    float sc = 0.0f;
 #pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    pa[i] = a.prec == TT_PREC_F32 ? reinterpret_cast<const float*>(a.pc)[cr + i]
-                                                  : (float)reinterpret_cast<const double*>(a.pc)[cr + i];
-                    sc += pa[i];
-                }
-                if (a.prec == TT_PREC_F32) {
+                    for (int i = 0; i < Q; ++i) sc += pa[i];
                     const float inv = 1.0f / sc;
 #pragma unroll
                     for (int i = 0; i < Q; ++i) pa[i] *= inv;
@@ -1026,45 +1007,88 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
             wgt = m32;
             if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) wgt *= (1.0f - pb[a.gap]) * (1.0f - pa[a.gap]);
         };
-        // staging and the Hamming distance (compensated FP32 sums, added across the CTA in FP64)
+        // heavy-pattern bit masks (one word per 32-pattern block): after the rows when they are in
+        // shared memory, else at the start of the dynamic shared memory the rows do not use
+        const int nblk = (P + 31) >> 5;
+        const int64_t dyn_words = ((int64_t)cap * (2 * Q + 1) * 4 + (int64_t)((cap + 31) / 32) * 4) / 4;
+        uint32_t* hmask = P <= cap ? reinterpret_cast<uint32_t*>(smf + (int64_t)cap * (2 * Q + 1))
+                                   : reinterpret_cast<uint32_t*>(smf);
+        const bool masks = nblk <= (P <= cap ? (cap + 31) / 32 : dyn_words);
+        // staging and the Hamming distance (compensated FP32 sums, added across the CTA in FP64); each
+        // warp takes 32-pattern blocks and records which of its patterns are heavy
         float ms = 0.0f, msc = 0.0f, os = 0.0f, osc = 0.0f;
-        for (int p = threadIdx.x; p < P; p += blockDim.x) {
-            float pa[Q], pb[Q], wgt, m32;
-            fetch32(p, pa, pb, wgt, m32);
-            float ov = 0.0f;
+#pragma unroll 2
+        for (int p0 = warp * 32; p0 < P; p0 += blockDim.x) {
+            const int p = p0 + lane;
+            float wgt = 0.0f;
+            if (p < P) {
+                float pa[Q], pb[Q], m32;
+                fetch32(p, pa, pb, wgt, m32);
+                float ov = 0.0f;
 #pragma unroll
-            for (int i = 0; i < Q; ++i) ov = fmaf(pb[i], pa[i], ov);
-            {
-                const float y = m32 - msc, t2 = ms + y;
-                msc = (t2 - ms) - y;
-                ms = t2;
-            }
-            {
-                const float y = m32 * ov - osc, t2 = os + y;
-                osc = (t2 - os) - y;
-                os = t2;
-            }
-            if (staged) {
-                if constexpr (Q == 4) {
-                    reinterpret_cast<float4*>(pcS)[p] = make_float4(pa[0], pa[1], pa[2], pa[3]);
-                    reinterpret_cast<float4*>(ppS)[p] = make_float4(pb[0], pb[1], pb[2], pb[3]);
-                } else {
-#pragma unroll
-                    for (int i = 0; i < Q; ++i) {
-                        pcS[p * Q + i] = pa[i];
-                        ppS[p * Q + i] = pb[i];
-                    }
+                for (int i = 0; i < Q; ++i) ov = fmaf(pb[i], pa[i], ov);
+                {
+                    const float y = m32 - msc, t2 = ms + y;
+                    msc = (t2 - ms) - y;
+                    ms = t2;
                 }
-                wS[p] = wgt;
+                {
+                    const float y = m32 * ov - osc, t2 = os + y;
+                    osc = (t2 - os) - y;
+                    os = t2;
+                }
+                if (staged) {
+                    if constexpr (Q == 4) {
+                        reinterpret_cast<float4*>(pcS)[p] = make_float4(pa[0], pa[1], pa[2], pa[3]);
+                        reinterpret_cast<float4*>(ppS)[p] = make_float4(pb[0], pb[1], pb[2], pb[3]);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) {
+                            pcS[p * Q + i] = pa[i];
+                            ppS[p * Q + i] = pb[i];
+                        }
+                    }
+                    wS[p] = wgt;
+                }
             }
+            const unsigned bal = __ballot_sync(0xffffffffu, p < P && wgt > kHeavyWeight);
+            if (masks && lane == 0) hmask[p0 >> 5] = bal;
         }
         const double msum = block_sum((double)ms - (double)msc, red);
         const double ovsum = block_sum((double)os - (double)osc, red);
-        // heavy patterns (weight above kHeavyWeight), the first kHeavyMax in pattern order: each warp
-        // counts those of a contiguous run of 32-pattern blocks, the counts give each warp its first
-        // list position, and the warps whose runs start within the list write their entries
-        {
-            const int nblk = (P + 31) >> 5, per = (nblk + nw - 1) / nw;
+        // heavy patterns (weight above kHeavyWeight), the first kHeavyMax in pattern order
+        if (masks) {
+            // warp 0 walks the block masks 32 at a time: a lane's first list position is the number
+            // of heavy patterns in the blocks before its own
+            if (warp == 0) {
+                int count = 0;
+                for (int base = 0; base < nblk; base += 32) {
+                    const int blk = base + lane;
+                    unsigned mm = blk < nblk ? hmask[blk] : 0u;
+                    const int c = __popc(mm);
+                    int incl = c;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    int pos = count + incl - c;
+                    while (mm != 0u && pos < kHeavyMax) {
+                        hidx[pos++] = blk * 32 + (__ffs(mm) - 1);
+                        mm &= mm - 1u;
+                    }
+                    count += __shfl_sync(0xffffffffu, incl, 31);
+                }
+                if (lane == 0) {
+                    hcount = count < kHeavyMax ? count : kHeavyMax;
+                    hall = count;
+                }
+            }
+        } else {
+            // more blocks than the masks' space: each warp counts the heavy patterns of a contiguous
+            // run of blocks, the counts give each warp its first list position, and the warps whose
+            // runs start within the list write their entries
+            const int per = (nblk + nw - 1) / nw;
             const int b0 = warp * per, b1 = min(nblk, b0 + per);
             auto heavy_mask = [&](int blk) -> unsigned {
                 const int p = blk * 32 + lane;
@@ -1103,19 +1127,22 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
         __syncthreads();
         const int H = hcount;
         const bool all_heavy_listed = hall <= kHeavyMax;
-        // FP64 coefficients and weights of the listed heavy patterns, from their stored rows
+        // FP64 coefficients and weights of the listed heavy patterns, from their stored rows (the
+        // child profile normalised in FP64)
         for (int h = threadIdx.x; h < H; h += blockDim.x) {
-            float pa[Q], pb[Q], wgt;
-            double m64, ov64;
             const int p = hidx[h];
-            const double m = fetch(p, pa, pb, wgt, m64, ov64);
-            double pcd[Q];
+            double pbd[Q], pcd[Q];
+            const int64_t pr = (pp_base + p) * w;
+#pragma unroll
+            for (int j = 0; j < Q; ++j)
+                pbd[j] = a.prec == TT_PREC_F32 ? (double)reinterpret_cast<const float*>(a.pp)[pr + j]
+                                               : reinterpret_cast<const double*>(a.pp)[pr + j];
             if (tipb) {
                 const int code = trow < 0 ? 0 : a.f.tip_codes[tr.tip_base + (int64_t)trow * P + p];
 #pragma unroll
                 for (int i = 0; i < Q; ++i) pcd[i] = a.m.lut[code * Q + i];
             } else {
-                const int64_t cr = (a.pc_row[b] + p) * w;
+                const int64_t cr = (pc_base + p) * w;
                 double sc = 0.0;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
@@ -1123,17 +1150,22 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
                                                    : reinterpret_cast<const double*>(a.pc)[cr + i];
                     sc += pcd[i];
                 }
-                if (a.prec != TT_PREC_F32) sc = 1.0;
+                if (a.prec == TT_PREC_F32) {
+                    const double inv = 1.0 / sc;
 #pragma unroll
-                for (int i = 0; i < Q; ++i) pcd[i] /= sc;
+                    for (int i = 0; i < Q; ++i) pcd[i] *= inv;
+                }
             }
+            double m = a.f.mult[tr.pat_base + p];
+            if (mo >= 0) m *= a.f.masks[mo + p];
+            if (a.ignore_gaps && a.gap >= 0 && a.gap < Q) m *= (1.0 - pbd[a.gap]) * (1.0 - pcd[a.gap]);
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
                 double x = 0.0, y = 0.0;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
                     x = fma(pcd[i], V[i * Q + k], x);
-                    y = fma(Vi[k * Q + i], (double)pb[i], y);
+                    y = fma(Vi[k * Q + i], pbd[i], y);
                 }
                 hu[h][k] = x * y;
             }
@@ -1378,7 +1410,10 @@ extern "C" tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m
         // FP32 profiles, small alphabets: FP32 objective, two CTAs per SM with 100 KB of pattern rows
         const size_t smem = 100 * 1024;
         ProfParams b32 = a;
-        b32.cap = (int)(smem / ((2 * q + 1) * sizeof(float)));
+        // pattern rows plus one heavy-pattern mask word per 32 patterns
+        int cap32 = (int)(smem / ((2 * q + 1) * sizeof(float)));
+        while ((size_t)cap32 * (2 * q + 1) * 4 + (size_t)((cap32 + 31) / 32) * 4 > smem) --cap32;
+        b32.cap = cap32;
         const int64_t cap2 = 2 * sms;
         const int fb = (int)(n < cap2 ? n : cap2);
         // workspace slices for trees with more patterns than shared memory holds (even, so that

@@ -819,7 +819,10 @@ def _profile_workspace(forest, n, dev, precision="f64"):
     p_max = int(np.max(forest.trees_host["n_patterns"])) if len(forest.trees_host) else 0
     sms = _lib.load().tt_device_sm_count()
     if precision == "f32" and q <= 5 and q >= 4:
+        # the kernel's shared memory: pattern rows plus one heavy-pattern mask word per 32 patterns
         cap = (100 * 1024) // ((2 * q + 1) * 4)
+        while cap * (2 * q + 1) * 4 + (cap + 31) // 32 * 4 > 100 * 1024:
+            cap -= 1
         if p_max <= cap or n == 0:
             return None, 0
         blocks = min(n, 2 * sms)

@@ -479,28 +479,30 @@ class GPUAncMixin:
         node.branch_state = {"pair": pairs, "multiplicity": mult}
         return engine.optimal_t_compressed(self.gtr, pairs, mult)
 
-    def _profile_branch_groups(self, nodes):
+    def _profile_branch_groups(self, nodes, sess=None):
         """The profile-pair arguments of the given branches, from the outgroup
         and subtree profiles of the last marginal reconstruction: one group for
         internal nodes (child rows in the partials) and one for tips (child
         profiles from their codes), as (positions in `nodes`, node ids,
-        outgroup buffer, parent rows, child rows, partials buffer)."""
+        outgroup buffer, parent rows, child rows, partials buffer); the ids and
+        rows are numpy arrays (int32, int64, int64)."""
         last = getattr(self, "_last", None)
         if last is None or last[0] != "marginal" or last[1].get("outgroup") is None:
             raise Exception("marginal ancestral inference needs to be performed first!")
         out = last[1]
-        layout = self._get_session()["layout"]
+        layout = (sess or self._get_session())["layout"]
         P = self.data.compressed_length
-        ks = [layout.local[id(n)] for n in nodes]
-        groups = (([i for i, k in enumerate(ks) if k < layout.n_int], out["outgroup"], False),
-                  ([i for i, k in enumerate(ks) if k >= layout.n_int], out["tip_outgroup"], True))
-        for idx, pp, tips in groups:
-            if not idx:
+        local = layout.local
+        ks = np.fromiter((local[id(n)] for n in nodes), dtype=np.int64, count=len(nodes))
+        tip = ks >= layout.n_int
+        for sel, pp, tips in ((~tip, out["outgroup"], False), (tip, out["tip_outgroup"], True)):
+            idx = np.flatnonzero(sel)
+            if idx.size == 0:
                 continue
-            kk = [ks[i] for i in idx]
-            pp_row = [((k - layout.n_int) if tips else k) * P for k in kk]
-            pc_row = [-1 if tips else k * P for k in kk]
-            yield idx, kk, pp, pp_row, pc_row, out["partial"]
+            kk = ks[idx]
+            pp_row = ((kk - layout.n_int) if tips else kk) * P
+            pc_row = np.full(idx.size, -1, np.int64) if tips else kk * P
+            yield idx, kk.astype(np.int32), pp, pp_row, pc_row, out["partial"]
 
     def _marginal_branch_lengths(self, nodes, tol):
         """Profile-mode Brent for the given nodes in one device pass, from the
@@ -511,7 +513,7 @@ class GPUAncMixin:
         info = np.zeros(len(nodes), dtype=np.int32)
         # both branch groups are queued before either result is read back
         pending = []
-        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
+        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
             t, inf = engine.optimal_t_profiles(sess["forest"], model, kk, pp, pp_row, pc, pc_row,
                                                self._gpu_precision(), self.gtr.gap_index, True, tol)
             pending.append((idx, t, inf))
@@ -550,7 +552,7 @@ class GPUAncMixin:
         logp = np.empty(padded.shape)
         if branch_length_mode == "marginal":
             model = engine.model_for(self.gtr, getattr(self, "device", None))
-            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
                 d = engine._to_dev
                 v = engine.prob_t_profiles_grid_dev(sess["forest"], model, d(np.asarray(kk, np.int32), dev), pp,
                                                     d(np.asarray(pp_row, np.int64), dev), pc,
@@ -614,9 +616,9 @@ class GPUAncMixin:
         model = engine.model_for(self.gtr, getattr(self, "device", None))
         engine.branch_pmats(sess["forest"], model, sess["bufs"])
         p64 = sess["bufs"].cache[("p64", engine.torch().float64)]
-        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups([node]):
-            m = engine.branch_mutation_matrix(sess["forest"], model, p64, 0, kk[0], pp, pp_row[0], pc, pc_row[0],
-                                              self._gpu_precision()).cpu().numpy()
+        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups([node], sess):
+            m = engine.branch_mutation_matrix(sess["forest"], model, p64, 0, int(kk[0]), pp, int(pp_row[0]), pc,
+                                              int(pc_row[0]), self._gpu_precision()).cpu().numpy()
         if full_sequence:
             return m[self.data.full_to_compressed_sequence_map]
         return m
@@ -635,7 +637,7 @@ class GPUAncMixin:
             engine.branch_pmats(forest, model, sess["bufs"])
             p64 = sess["bufs"].cache[("p64", t.float64)]
             n_ija = T_ia = None
-            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes):
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
                 d = engine._to_dev
                 dev = forest.device
                 n1, T1 = engine.mutation_counts(forest, model, p64, 0, d(np.asarray(kk, np.int32), dev), pp,

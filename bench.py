@@ -1143,6 +1143,7 @@ def run_c3(args):
     }
     if not args.no_cpu_baseline and world == 1:
         res["cpu_baseline"] = cpu_baseline_forest(inputs, gtrs)
+        res["cpu_baseline_all_cores"] = cpu_baseline_forest_pool(inputs, gtrs)
     return res
 
 
@@ -1175,6 +1176,54 @@ def cpu_baseline_forest(inputs, gtrs, budget_node_patterns=4e7, seed=0):
     return {"value": done_units / secs, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": "%d trees of the batch (seeded random), %.2e node-pattern updates, numpy restatement of "
                       "TreeTime, 1 process" % (used, done_units), "seconds": secs}
+
+
+def _forest_tree_job(job):
+    """One tree of the batch through the oracle marginal (pool worker):
+    (newick, {tip: characters}, multiplicities, model state, L) -> seconds."""
+    from oracle import anc
+    from treetime_gb300.tree import Tree, parse_newick
+    nwk, aln, mult, model, L = job
+    tree = anc.prepare_tree(Tree(root=parse_newick(nwk).root))
+    t0 = time.perf_counter()
+    anc.marginal(tree, aln, mult, model, L)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline_forest_pool(inputs, gtrs, budget_node_patterns_per_core=3e7, seed=0):
+    """The oracle marginal on a seeded random sample of the batch's trees, the
+    trees spread over a spawn-started pool of os.cpu_count() processes (the
+    trees are independent), bounded to about ``budget_node_patterns_per_core``
+    node-pattern updates per process; wall clock around the pool's map."""
+    import multiprocessing as mp
+    from treetime_gb300.tree import Tree, to_newick
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    jobs, units = [], 0
+    for k in rng.permutation(len(inputs)):
+        ti = inputs[k]
+        u = ti.layout.n_nodes * ti.n_patterns
+        if units + u > budget_node_patterns_per_core * cores and jobs:
+            continue
+        root = ti.layout.nodes[ti.layout.n_int - 1]
+        tips = ti.layout.nodes[ti.layout.n_int:]
+        chars = ti.tip_codes.view("S1").astype("U1")
+        aln = {t.name: chars[r] for t, r in zip(tips, ti.tip_row)}
+        jobs.append((to_newick(Tree(root=root)), aln, ti.mult, _model_state(gtrs[k]), int(round(ti.mult.sum()))))
+        units += u
+        if units >= budget_node_patterns_per_core * cores:
+            break
+    jobs.sort(key=lambda j: -len(j[2]) * len(j[1]))  # largest first: better balance over the pool
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_forest_tree_job, jobs[-1:] * cores)  # workers started and modules imported
+        t0 = time.perf_counter()
+        pool.map(_forest_tree_job, jobs, chunksize=1)
+        wall = time.perf_counter() - t0
+    return {"value": units / wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d trees of the batch (seeded random), %.2e node-pattern updates, numpy restatement of "
+                      "TreeTime, trees over a pool of %d processes" % (len(jobs), units, cores),
+            "seconds": wall}
 
 
 C4_WORKLOAD = ("c4: serving loop, Poisson arrivals (200 req/s unless --c4-rate); 90% nucleotide jobs drawn from the c3 size "

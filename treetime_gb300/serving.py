@@ -20,8 +20,9 @@ own CUDA stream, so the kernels of every admitted job overlap on the GPU.  At
 admission all of a job's iterations and the copy of its results to pinned host
 memory are queued on its stream at once (the iterations need no host decision
 in between), so the host does no per-iteration round trip.  Submitting a job
-stages its tip codes into page-locked memory on the submitting thread, so the
-scheduler's upload is one asynchronous copy; a collector thread turns the
+stages its tip codes into page-locked memory on the submitting thread (for up
+to 2 x max_slots waiting jobs), so the scheduler's upload is one asynchronous
+copy; a collector thread turns the
 finished jobs' pinned results into arrays.  A job's numbers do not depend on
 which other jobs share the GPU with it (each kernel reads only its own job's
 buffers)."""
@@ -335,6 +336,7 @@ class Server:
         self._pinned = pinned_pool()
         self._finished = queue.Queue()
         self._collecting = 0
+        self._staged_waiting = 0
         self._errors = []
         self.done = []
         self.peak_active = 0
@@ -344,10 +346,18 @@ class Server:
         self.host_s = collections.Counter()
 
     def submit(self, job):
-        """Queue a job (thread-safe): its tip codes are staged into pinned
-        memory on the calling thread; the scheduler loop admits it."""
+        """Queue a job (thread-safe); the scheduler loop admits it.  While
+        fewer than ``2 * max_slots`` queued jobs hold staged codes, the job's
+        tip codes are staged into pinned memory on the calling thread (a long
+        queue does not pin the host memory of every waiting job; the others
+        are packed at admission)."""
         job.t_submit = time.perf_counter()
-        job.stage(self._pinned)
+        with self._lock:
+            stage = self._staged_waiting < 2 * self.max_slots
+            if stage:
+                self._staged_waiting += 1
+        if stage:
+            job.stage(self._pinned)
         with self._lock:
             self._queue.append(job)
 
@@ -373,8 +383,10 @@ class Server:
         with self._lock:
             plan = plan_admissions(self._queue, self.max_slots - len(self._active),
                                    self.hbm_bytes - self._used_bytes())
-            for _ in plan:
+            for job in plan:
                 self._queue.popleft()
+                if job._codes_buf is not None:
+                    self._staged_waiting -= 1
         for job in plan:
             job.t_admit = time.perf_counter()
             a = _Active(job, self)

@@ -243,3 +243,20 @@ def test_fp32_profile_brent_matches_fp64(shape):
         pp, pc = n.marginal_outgroup_LH, n.marginal_subtree_LH
         f = lambda tt: -oanc.prob_t_profiles(g, (pp, pc), mult, tt, return_log=True) + np.exp(tt * tt / 1e4)
         assert abs(f(x32) - f(x64)) <= 1e-6 * abs(f(x64)) + 1e-12, (name, x32, x64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("invariant_frac", [0.0, 0.9])
+def test_fp32_profile_brent_is_deterministic(invariant_frac):
+    """Repeated launches of the FP32 profile Brent kernel give bit-identical
+    lengths: the warps' roles move between launches (they follow the CTAs'
+    placement), the patterns each thread sums do not.  With invariant sites
+    the constant columns are heavy patterns (the helper warp's FP64 terms)."""
+    from treetime_gb300 import TreeAnc, synth
+    wl = synth.make_workload("c0", seed=5, n=60, L=3000, invariant_frac=invariant_frac, gap_frac=0.0)
+    t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], verbose=0, precision="f32")
+    t.infer_ancestral_sequences(marginal=True)
+    nodes = [n for n in t.tree.find_clades() if n.up is not None]
+    first = t._marginal_branch_lengths(nodes, 1e-10)
+    for _ in range(4):
+        np.testing.assert_array_equal(t._marginal_branch_lengths(nodes, 1e-10), first)

@@ -874,8 +874,9 @@ __device__ __forceinline__ void warp_sum_pair(float& hi, float& lo) {
 }
 
 // Per-SM launch tickets: the CTAs resident on one SM take consecutive tickets, from which each
-// picks the scheduler partition (warp slot mod 4) of its search warp and of its helper warp, so that
-// the serial FP64 chains of two CTAs do not share one partition's FP64 unit.
+// picks the scheduler partition (warp slot mod 4) of its search warp, so that the serial FP64
+// chains of two CTAs do not share one partition's FP64 unit.  Roles never change which patterns a
+// thread sums: the results do not depend on the placement.
 __device__ unsigned int g_sm_ticket[256];
 
 __device__ __forceinline__ unsigned int warp_slot() {
@@ -902,6 +903,7 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
     __shared__ double Ed[Q];
     __shared__ float2 redp[32];
     __shared__ double hs_total;
+    __shared__ float pen_s;
     __shared__ unsigned int slots[32];
     __shared__ int hwarp[32];
     __shared__ float lutS[256 * Q];
@@ -913,20 +915,21 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
         log_tab[j] = log(F);
         inv_tab[j] = 1.0 / F;
     }
-    // roles: the search warp and the heavy-pattern helper on the partitions this CTA's ticket names
+    // roles: the heavy-pattern helper is the last warp (a fixed index, so that the patterns each
+    // thread sums, and hence the results, do not depend on where the CTA runs); the search warp is
+    // the first other warp on the scheduler partition this CTA's ticket names among the three
+    // partitions other than the helper's
     if (lane == 0) slots[warp] = warp_slot();
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned int ticket = atomicAdd(&g_sm_ticket[sm_id() & 255u], 1u);
-        const unsigned int want_lead = (2u * ticket) & 3u, want_help = (2u * ticket + 1u) & 3u;
-        int lw = -1, hw2 = -1;
-        for (int k = 0; k < nw; ++k)
-            if (lw < 0 && (slots[k] & 3u) == want_lead) lw = k;
-        if (lw < 0) lw = 0;
-        for (int k = 0; k < nw; ++k)
-            if (hw2 < 0 && k != lw && (slots[k] & 3u) == want_help) hw2 = k;
-        if (hw2 < 0) hw2 = (lw + 1) % nw;
-        lead_w = lw;
+        const int hw2 = nw - 1;
+        const unsigned int hpart = slots[hw2] & 3u;
+        const unsigned int want = (hpart + 1u + ticket % 3u) & 3u;
+        int lw = -1;
+        for (int k = 0; k < hw2; ++k)
+            if (lw < 0 && (slots[k] & 3u) == want) lw = k;
+        lead_w = lw < 0 ? 0 : lw;
         help_w = hw2;
     }
     __syncthreads();
@@ -1185,10 +1188,10 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
             }
             return false;
         };
-        // Patterns are summed by every warp but the helper (by every warp when there are no heavy
-        // patterns); this thread's rank among them and their number.
+        // Patterns are summed by every warp but the helper (the last warp; by every warp when there
+        // are no heavy patterns); this thread's rank among them and their number.
         const bool helper_busy = H > 0;
-        const int rank = helper_busy ? (warp - (warp > help ? 1 : 0)) * 32 + lane : (int)threadIdx.x;
+        const int rank = (int)threadIdx.x;
         const int n_sum = helper_busy ? (nw - 1) * 32 : (int)blockDim.x;
         // this thread's compensated sum of w log(pc.P(t).pp + 1e-24) over its patterns, as the pair
         // (hi, lo) with value hi + lo
@@ -1271,7 +1274,7 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
                 hs = fma(hw[h], log_tang(res + kSuperTiny, log_tab, inv_tab), hs);
             }
             hs = warp_sum(hs);
-            if (lane == 0) hs_total = hs;
+            if (lane == 0) hs_total = (1.0 + (double)pen_s) - hs;  // the penalty minus the heavy sum
         };
         // The search warp runs Brent; per evaluation it publishes exp(mu lam t) and P(t) (barrier 1),
         // every warp then adds its patterns (the helper its heavy patterns instead) and writes its
@@ -1303,20 +1306,24 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
                 // 1.6e-3 and FP32 leaves an absolute error under 1e-10
                 const float tf = (float)t;
                 const float pen = expm1f(tf * tf * 1e-4f);
-                if (lane == 0) go = 1;
+                if (lane == 0) {
+                    pen_s = pen;
+                    go = 1;
+                }
                 role_barrier();
                 warp_part();
                 role_barrier();
+                // the warps' pairs summed across lanes 0..nw-1; the helper, when busy, has combined
+                // the penalty and its FP64 heavy-pattern sum (hs_total = 1 + penalty - heavy sum)
                 float hi = 0.0f, lo = 0.0f;
-                for (int k = 0; k < nw; ++k) {
-                    const float2 r2 = redp[k];
-                    float sn, en;
-                    two_sum(hi, r2.x, sn, en);
-                    hi = sn;
-                    lo = (lo + r2.y) + en;
+                if (lane < nw) {
+                    const float2 r2 = redp[lane];
+                    hi = r2.x;
+                    lo = r2.y;
                 }
-                const double tot = (double)hi + (double)lo + (helper_busy ? hs_total : 0.0);
-                return -tot + (1.0 + (double)pen);
+                warp_sum_pair(hi, lo);
+                const double tail = helper_busy ? hs_total : 1.0 + (double)pen;
+                return tail - ((double)hi + (double)lo);
             };
             BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
             if (lane == 0) {

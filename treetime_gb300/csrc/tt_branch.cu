@@ -839,12 +839,15 @@ __global__ void __launch_bounds__(256) prob_t_profiles_grid_f32_kernel(ProfParam
 }
 
 // Profile-mode Brent from FP32-scaled profiles (alphabets of up to 5 states): the objective of
-// optimal_t_profiles_kernel evaluated as in prob_t_profiles_grid_f32_kernel -- per evaluation
-// warp 0 forms P(t) in FP64 (kept as FP32) and the heavy patterns' FP64 terms, then every thread
-// sums w logf(pc.P(t).pp + 1e-24) over its patterns with compensated FP32 sums, added across the
-// CTA in FP64.  Patterns are staged as FP32 rows (normalised child profile, parent profile,
-// weight) in shared memory when the tree has at most `cap` of them, else in the CTA's slice of the
-// workspace when it is large enough, else read from their stored rows at every evaluation.  The
+// optimal_t_profiles_kernel evaluated as in prob_t_profiles_grid_f32_kernel.  Two CTAs per SM,
+// one branch at a time per CTA.  Per evaluation the search warp forms exp(mu lam t) and P(t) in
+// FP64 (P kept as FP32); the helper warp (the CTA's last) evaluates the heavy patterns' terms in
+// FP64; the other warps sum w logf(pc.P(t).pp + 1e-24) over their patterns with compensated FP32
+// sums, reduced across lanes and warps as error-free FP32 pairs; the search warp adds the parts
+// in FP64.  Patterns are staged once per branch as FP32 rows (normalised child profile, parent
+// profile, weight) in shared memory when the tree has at most `cap` of them, else in the CTA's
+// slice of the workspace when it is large enough, else read from their stored rows at every
+// evaluation; the heavy patterns are found from per-block masks recorded while staging.  The
 // search, bracket, Hamming distance and results are those of the FP64 kernel (the Hamming
 // distance is summed in FP64).
 // Barrier 1 over all threads of the CTA, for code where warps reach it from different places (the

@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -74,12 +75,15 @@ def _traffic(kernel_key):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region; the raw
+    samples go to ``clocks_<gpu>.csv`` in $TT_BENCH_OUT (default: the system's
+    temporary directory)."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(HERE, "gpurun_out", "clocks_%d.csv" % index)
+        out = os.environ.get("TT_BENCH_OUT") or tempfile.gettempdir()
+        self.path = os.path.join(out, "clocks_%d.csv" % index)
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)

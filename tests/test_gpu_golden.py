@@ -168,7 +168,7 @@ def test_marginal_branch_lengths_match_treetime(case, precision):
     nodes = _by_name(t)
     names = g["mbl_names"].tolist()
     got = t._marginal_branch_lengths([nodes[n] for n in names], 1e-10)
-    # reference profiles (oracle, FP64) to judge flat objectives
+    # reference profiles (oracle, FP64) to assess flat objectives
     tree_o, _, model_o, _ = gc.inputs_from(g)
     anc.prepare_tree(tree_o)
     ores = anc.marginal(tree_o, gc.compressed_from(g, model_o), g["multiplicity"], model_o,

@@ -323,8 +323,14 @@ tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts, const int3
  * eigen coefficients are computed once; those that do not fit in shared memory (about 200 KB /
  * ((q + 1) * 8) patterns) go to `workspace` (device FP64, per persistent CTA: min(n, SM count)
  * CTAs each need (P - that) * (q + 1) doubles) or, when it is NULL or too small, are recomputed
- * at every objective evaluation.  Replaces GTR.optimal_t_compressed(profiles=True) with
- * GTR.prob_t_profiles (treetime/gtr.py:816-963). */
+ * at every objective evaluation.  FP32 profiles (`prec` TT_PREC_F32) of 4- or 5-state alphabets
+ * take an FP32 objective instead (pattern sums in compensated FP32, patterns of weight above 16
+ * in FP64): per branch the patterns' FP32 rows are staged in shared memory when there are at
+ * most 2,834 (q = 4) / 2,320 (q = 5) of them, else in the workspace, where each of the
+ * min(n, 2 x SM count) CTAs needs ((P + 3) & ~3) * (2q + 1) floats; rows are read 16 bytes at a
+ * time when pp and pc are 16-byte aligned.  Results are bit-identical from launch to launch.
+ * Replaces GTR.optimal_t_compressed(profiles=True) with GTR.prob_t_profiles
+ * (treetime/gtr.py:816-963). */
 tt_status tt_optimal_t_profiles(const tt_forest* f, const tt_model* m, int64_t n, const int32_t* node_of,
                                 const void* pp, const int64_t* pp_row, const void* pc, const int64_t* pc_row,
                                 int32_t prec, int32_t gap_state, int32_t ignore_gaps, double tol,

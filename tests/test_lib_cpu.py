@@ -97,3 +97,34 @@ def test_uncompiled_alphabet_size_fails_before_launch():
         check_alphabet(q)
     with pytest.raises(NotImplementedError):
         check_alphabet(5, site_specific=True)
+
+
+def test_profile_branch_groups_rows():
+    """The branch lists of the profile-mode calls (host logic): internal
+    branches read their child rows from the partials, tips from their codes
+    (child row -1, parent row in the tip outgroup buffer); positions refer to
+    the caller's node order."""
+    from types import SimpleNamespace
+    from treetime_gb300.anc_gpu import GPUAncMixin
+    tree = synth.coalescent_tree(40, 0.01, np.random.default_rng(3))
+    L = TreeLayout(tree.root)
+    P = 17
+    out = {"outgroup": "OUT", "tip_outgroup": "TIPOUT", "partial": "PART"}
+    host = SimpleNamespace(_last=("marginal", out), data=SimpleNamespace(compressed_length=P))
+    root = L.nodes[L.n_int - 1]
+    nodes = [n for n in L.nodes if n is not root]
+    order = np.random.default_rng(4).permutation(len(nodes))
+    nodes = [nodes[i] for i in order]
+    seen = np.zeros(len(nodes), bool)
+    groups = list(GPUAncMixin._profile_branch_groups(host, nodes, {"layout": L}))
+    assert [g[2] for g in groups] == ["OUT", "TIPOUT"]
+    for idx, kk, pp, pp_row, pc_row, pc in groups:
+        assert pc == "PART" and kk.dtype == np.int32 and pp_row.dtype == np.int64 and pc_row.dtype == np.int64
+        for i, k, r, c in zip(idx, kk, pp_row, pc_row):
+            assert L.local[id(nodes[i])] == k
+            seen[i] = True
+            if k < L.n_int:
+                assert pp == "OUT" and r == k * P and c == k * P
+            else:
+                assert pp == "TIPOUT" and r == (k - L.n_int) * P and c == -1
+    assert seen.all()

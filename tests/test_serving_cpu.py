@@ -35,3 +35,35 @@ def test_footprint_grows_with_size_and_kind():
     assert footprint(big, 4, "marginal") < footprint(big, 4, "optimize")
     rows = big.layout.n_int * big.n_patterns * 4 * 4
     assert footprint(big, 4, "marginal") >= 2 * rows
+
+
+def test_submit_stages_codes_for_a_bounded_number_of_waiting_jobs():
+    """Submitting copies a job's tip codes into a (here: ordinary) host buffer
+    of the pool while fewer than 2 x max_slots waiting jobs hold one; later
+    jobs are packed at admission instead."""
+    import collections
+    import threading
+    import torch
+    from treetime_gb300 import engine, synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.serving import Job, Server
+
+    class Pool:
+        def take(self, n):
+            return torch.zeros(max(n, 1), dtype=torch.uint8)
+
+    tree = synth.coalescent_tree(12, 0.01, np.random.default_rng(0))
+    lay = engine.TreeLayout(tree.root)
+    rng = np.random.default_rng(1)
+    codes = rng.choice(np.frombuffer(b"ACGT", np.uint8), size=(lay.n_tip, 50))
+    ti = engine.TreeInput(lay, codes, np.arange(lay.n_tip, dtype=np.int32), np.ones(50), np.full(lay.n_nodes, 0.01))
+    g = GTR.standard("JC69", alphabet="nuc_nogap")
+    srv = object.__new__(Server)  # the queueing half of the server, without a device
+    srv.max_slots, srv._lock, srv._queue = 2, threading.Lock(), collections.deque()
+    srv._staged_waiting, srv._pinned = 0, Pool()
+    jobs = [Job(ti, g) for _ in range(6)]
+    for j in jobs:
+        srv.submit(j)
+    staged = [j._codes_buf is not None for j in jobs]
+    assert staged == [True] * 4 + [False] * 2 and srv._staged_waiting == 4 and len(srv._queue) == 6
+    np.testing.assert_array_equal(jobs[0]._codes_buf[:codes.size].numpy(), codes.reshape(-1))

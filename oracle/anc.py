@@ -586,6 +586,57 @@ def optimize_branch_lengths_joint(tree, cseq_of, mult, model, ignore_gaps=True):
     return out
 
 
+def optimize_tree_marginal(tree, aln, mult, model, full_length, max_iter=10, damping=0.75, LHtol=0.1):
+    """TreeAnc.optimize_tree_marginal (treeanc.py:1297-1360) without GTR
+    inference: marginal reconstruction, then per iteration i every branch's
+    profile-mode Brent (tolerance 1e-8 + 0.01^(i+1)) with the damped update
+    new*(1 - damping^(i+1)) + old*damping^(i+1), in TreeTime's preorder visit;
+    the two children of a bifurcating root form one branch (parent profile
+    normalize(subtree(n2) * outgroup(root))), updated at the visit of each
+    child (:1318-1341).  Stops when the log-likelihood gains less than LHtol.
+    Branch (and mutation) lengths of ``tree`` are updated in place.  Returns
+    (last marginal result, per-iteration total log-likelihoods)."""
+    res = marginal(tree, aln, mult, model, full_length)
+    old_lh = res["total_sequence_LH"]
+    history = []
+    root = tree.root
+    for i in range(max_iter):
+        tol = 1e-8 + 0.01 ** (i + 1)
+        d = damping ** (i + 1)
+        for n in preorder(root):
+            if n is root:
+                continue
+            if n.up is root and len(root.clades) == 2:
+                n1, n2 = root.clades
+                total_bl = n1.branch_length + n2.branch_length
+                bl_ratio = n1.branch_length / total_bl
+                prof_c = res["subtree_LH"][n1.name]
+                prof_p = normalize_profile(res["subtree_LH"][n2.name] * res["outgroup_LH"][root.name])[0]
+                m1, m2 = getattr(n1, "mask", None), getattr(n2, "mask", None)
+                m = mult if m1 is None or m2 is None else mult * (m1 * m2)
+                new_bl, _ = optimal_t_compressed(model, (prof_p, prof_c), m, profiles=True, tol=tol)
+                update = new_bl * (1 - d) + total_bl * d
+                n1.branch_length = update * bl_ratio
+                n2.branch_length = update * (1 - bl_ratio)
+                n1.mutation_length = n1.branch_length
+                n2.mutation_length = n2.branch_length
+            else:
+                mask = getattr(n, "mask", None)
+                m = mult if mask is None else mult * mask
+                new_val, _ = optimal_t_compressed(model, (res["outgroup_LH"][n.name], res["subtree_LH"][n.name]), m,
+                                                  profiles=True, tol=tol)
+                n.branch_length = new_val * (1 - d) + n.branch_length * d
+                n.mutation_length = n.branch_length
+        res = marginal(tree, aln, mult, model, full_length)
+        lh = res["total_sequence_LH"]
+        history.append(lh)
+        delta = lh - old_lh
+        old_lh = lh
+        if delta < LHtol:
+            break
+    return res, history
+
+
 # --------------------------------------------------------------- compression
 def seq2array(seq, fill_overhangs=False, ambiguous="N", convert_upper=True):
     """seq_utils.py:152-204 for word length 1."""

@@ -10,6 +10,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source --vcf   (VCF reading and sparse alignments)
     python tests/golden/make_golden.py /path/to/treetime-source --sample   (states drawn at every node)
     python tests/golden/make_golden.py /path/to/treetime-source --extra-sites   (constant sites beyond the alignment)
+    python tests/golden/make_golden.py /path/to/treetime-source --optimize   (optimize_tree_marginal iterations)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -617,6 +618,48 @@ def extra_sites_cases():
     np.savez_compressed(os.path.join(HERE, "extra_sites.npz"), **out)
 
 
+def optimize_cases():
+    """TreeAnc.optimize_tree_marginal: the branch lengths, log-likelihood and
+    sequences after TreeTime's damped marginal iterations, on a tree with a
+    bifurcating root (its two children optimised as one branch) and on one
+    with a trifurcating root."""
+    from treetime import TreeAnc
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    out = {}
+    for tag, seed, collapse in (("bif", 81, False), ("tri", 82, True)):
+        rng = np.random.default_rng(seed)
+        tree = synth.coalescent_tree(20, 0.05, rng)
+        if collapse:  # merge the root's first internal child into the root
+            first = next(c for c in tree.root.clades if c.clades)
+            tree.root.clades = [c for c in tree.root.clades if c is not first] + first.clades
+        pi = rng.dirichlet(np.ones(4))
+        W = np.triu(rng.uniform(0.5, 2.0, size=(4, 4)), 1)
+        W = W + W.T
+        g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap")
+        aln = synth._to_text(synth.evolve(tree, g, 300, rng), g.alphabet, 0.0, rng)
+        nwk = to_newick(tree)
+        params = {"pi": pi, "W": W, "alphabet": "nuc_nogap", "mu": 1.0}
+        tr, recs = _bio_inputs(nwk, aln)
+        t = TreeAnc(tree=tr, aln=recs, gtr=_ref_gtr("gtr", params), verbose=0)
+        t.optimize_tree_marginal(max_iter=4)
+        nodes = list(t.tree.find_clades())
+        out[tag + "_newick"] = np.array(nwk)
+        out[tag + "_aln_names"] = np.array(list(aln.keys()))
+        out[tag + "_aln_seqs"] = np.array(list(aln.values()))
+        for k, v in params.items():
+            out[tag + "_param_" + k] = np.asarray(v)
+        out[tag + "_root_children"] = len(t.tree.root.clades)
+        out[tag + "_node_names"] = np.array([n.name for n in nodes])
+        out[tag + "_node_bl"] = np.array([n.branch_length for n in nodes], dtype=float)
+        out[tag + "_total_LH"] = t.tree.total_sequence_LH
+        inner = [n for n in nodes if n.clades]
+        out[tag + "_cseq_names"] = np.array([n.name for n in inner])
+        out[tag + "_cseq"] = np.stack([_codes(n._cseq) for n in inner])
+    np.savez_compressed(os.path.join(HERE, "optimize_marginal.npz"), **out)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -775,5 +818,8 @@ if __name__ == "__main__":
     elif "--extra-sites" in sys.argv:
         _setup(ref)
         extra_sites_cases()
+    elif "--optimize" in sys.argv:
+        _setup(ref)
+        optimize_cases()
     else:
         main(ref)

@@ -17,7 +17,16 @@ def case_names():
     GTR inference cases)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                   if not os.path.basename(p).startswith(("blgrid_", "gtrinf_", "fitch_", "vcf_", "sample_",
-                                                          "extra_")))
+                                                          "extra_", "optimize_")))
+
+
+def optimize_cases():
+    """(tag, fixture view) of the optimize_tree_marginal fixture: each tree's
+    arrays under the unprefixed keys the other fixtures use."""
+    g = load("optimize_marginal")
+    tags = sorted({k.split("_", 1)[0] for k in g})
+    return [(tag, {k[len(tag) + 1:]: v for k, v in g.items() if k.startswith(tag + "_")} | {"kind": "gtr"})
+            for tag in tags]
 
 
 def fitch_names():

@@ -279,3 +279,26 @@ def test_oracle_sampling_at_every_node_matches_treetime(tips):
     res2 = anc.marginal(tree, caln, mult, model, full, sample_from_profile=True, reconstruct_tip_states=tips,
                         rng=rng, prev_cseq=res["cseq"])
     assert res2["N_diff"] == int(g[tag + "_N_diff_again"])
+
+
+# ------------------------------------------------ optimize_tree_marginal iterations
+@pytest.mark.parametrize("tag,g", gc.optimize_cases(), ids=lambda x: x if isinstance(x, str) else "")
+def test_oracle_optimize_tree_marginal_matches_treetime(tag, g):
+    """The oracle's restatement of TreeTime's damped marginal branch-length
+    iterations (bifurcating root: the two children as one branch, updated at
+    the visit of each child; trifurcating root: every branch on its own)
+    against TreeTime's own run: branch lengths, log-likelihood, sequences."""
+    tree, aln, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    assert len(tree.root.clades) == int(g["root_children"])
+    caln, mult, L = gc.compress_inputs(aln, model)
+    res, history = anc.optimize_tree_marginal(tree, caln, mult, model, L, max_iter=4)
+    want = _names_map(g["node_names"], g["node_bl"])
+    for n in anc.preorder(tree.root):
+        v = want[n.name]
+        assert abs(n.branch_length - v) <= 1e-9 * abs(v) + 1e-12, (tag, n.name, n.branch_length, v)
+    assert abs(res["total_sequence_LH"] - float(g["total_LH"])) <= 1e-9 * abs(float(g["total_LH"]))
+    cseq = _names_map(g["cseq_names"], g["cseq"])
+    for name, codes in cseq.items():
+        np.testing.assert_array_equal(np.frombuffer(np.asarray(res["cseq"][name]).astype("S1").tobytes(), np.uint8),
+                                      codes)

@@ -735,19 +735,22 @@ class GPUAncMixin:
             new = dict(zip([id(n) for n in nodes], self._marginal_branch_lengths(nodes, tol))) if nodes else {}
             if special:
                 n1, n2 = root.clades
-                total_bl = n1.branch_length + n2.branch_length
-                bl_ratio = n1.branch_length / total_bl
                 prof_c = n1.marginal_subtree_LH
                 tmp = n2.marginal_subtree_LH * root.marginal_outgroup_LH
                 prof_p = np.einsum("ai,a->ai", tmp, 1.0 / tmp.sum(axis=1))
                 m1, m2 = getattr(n1, "mask", None), getattr(n2, "mask", None)
                 mult = self.data.multiplicity() if m1 is None or m2 is None else self.data.multiplicity(mask=m1 * m2)
                 new_bl = engine.optimal_t_compressed(self.gtr, (prof_p, prof_c), mult, profiles=True, tol=tol)
-                update = new_bl * (1 - damping ** (i + 1)) + total_bl * damping ** (i + 1)
-                n1.branch_length = update * bl_ratio
-                n2.branch_length = update * (1 - bl_ratio)
-                n1.mutation_length = n1.branch_length
-                n2.mutation_length = n2.branch_length
+                # TreeTime's loop meets the pair at both children (treetime/treeanc.py:1318-1341) and
+                # applies the damped update at each visit, the second from the first's lengths
+                for _visit in range(2):
+                    total_bl = n1.branch_length + n2.branch_length
+                    bl_ratio = n1.branch_length / total_bl
+                    update = new_bl * (1 - damping ** (i + 1)) + total_bl * damping ** (i + 1)
+                    n1.branch_length = update * bl_ratio
+                    n2.branch_length = update * (1 - bl_ratio)
+                    n1.mutation_length = n1.branch_length
+                    n2.mutation_length = n2.branch_length
             for n in nodes:
                 update = new[id(n)] * (1 - damping ** (i + 1)) + n.branch_length * damping ** (i + 1)
                 n.branch_length = update

@@ -637,6 +637,30 @@ def optimize_tree_marginal(tree, aln, mult, model, full_length, max_iter=10, dam
     return res, history
 
 
+def prune_short_branches(tree, cseq_of, mult, model, one_mutation):
+    """TreeAnc.prune_short_branches (treeanc.py:1475-1497): in preorder, an
+    internal branch shorter than 0.1 * one_mutation whose parent and child
+    sequences have probability > 0.1 at distance zero (GTR.prob_t: state
+    pairs with gaps ignored, the node's mask on the multiplicities) is
+    collapsed, its children re-attached to its parent; a node visited after
+    its parent was collapsed is compared with its new parent.  Modifies
+    ``tree``; returns the names of the collapsed nodes."""
+    out = []
+    for node in preorder(tree.root):
+        if node.up is None or not node.clades:
+            continue
+        if node.branch_length < 0.1 * one_mutation:
+            mask = getattr(node, "mask", None)
+            m = mult if mask is None else mult * mask
+            pairs, pm = state_pair(model, cseq_of(node.up), cseq_of(node), pattern_multiplicity=m, ignore_gaps=True)
+            if prob_t_compressed(model, pairs, pm, 0.0) > 0.1:
+                node.up.clades = [k for k in node.up.clades if k != node] + node.clades
+                for clade in node.clades:
+                    clade.up = node.up
+                out.append(node.name)
+    return out
+
+
 # --------------------------------------------------------------- compression
 def seq2array(seq, fill_overhangs=False, ambiguous="N", convert_upper=True):
     """seq_utils.py:152-204 for word length 1."""

@@ -11,6 +11,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source --sample   (states drawn at every node)
     python tests/golden/make_golden.py /path/to/treetime-source --extra-sites   (constant sites beyond the alignment)
     python tests/golden/make_golden.py /path/to/treetime-source --optimize   (optimize_tree_marginal iterations)
+    python tests/golden/make_golden.py /path/to/treetime-source --prune   (short-branch pruning with a gap)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -660,6 +661,45 @@ def optimize_cases():
     np.savez_compressed(os.path.join(HERE, "optimize_marginal.npz"), **out)
 
 
+def prune_cases():
+    """TreeAnc.prune_short_branches on a tree with two consecutive short
+    internal branches (P -> X -> G) whose reconstructed sequences are set so
+    that X equals P except for a gap, and G equals X except where X has the
+    gap: X is collapsed (the gap is ignored), after which TreeTime compares G
+    with its new parent P, where they differ, and keeps G."""
+    from treetime import TreeAnc, GTR
+    nwk = "((((t1:0.1,t2:0.1)G:0.0001,t3:0.1)X:0.0001,t4:0.1)P:0.1,(t5:0.1,t6:0.1)Q:0.1)R;"
+    rng = np.random.default_rng(91)
+    L = 40
+    base = rng.choice(list("ACGT"), size=L)
+    aln = {}
+    for k in range(1, 7):
+        seq = base.copy()
+        seq[rng.integers(L, size=2)] = rng.choice(list("ACGT"), size=2)
+        aln["t%d" % k] = "".join(seq)
+    tr, recs = _bio_inputs(nwk, aln)
+    t = TreeAnc(tree=tr, aln=recs, gtr=GTR.standard("JC69", alphabet="nuc"), verbose=0)
+    t.infer_ancestral_sequences(marginal=False)
+    nodes = {n.name: n for n in t.tree.find_clades()}
+    p_seq = np.array(list("A" * t.data.compressed_length))
+    x_seq = p_seq.copy()
+    x_seq[0] = "-"
+    g_seq = x_seq.copy()
+    g_seq[0] = "C"
+    nodes["P"]._cseq, nodes["X"]._cseq, nodes["G"]._cseq = p_seq, x_seq, g_seq
+    inner = [n for n in t.tree.find_clades() if n.clades]
+    out = {"newick": np.array(nwk), "aln_names": np.array(list(aln.keys())),
+           "aln_seqs": np.array(list(aln.values())), "one_mutation": t.one_mutation,
+           "multiplicity": t.data.multiplicity(),
+           "cseq_names": np.array([n.name for n in inner]),
+           "cseq": np.stack([_codes(n._cseq) for n in inner])}
+    t.prune_short_branches()
+    after = list(t.tree.find_clades())
+    out["node_names"] = np.array([n.name for n in after])
+    out["parent_names"] = np.array([n.up.name if n.up is not None else "" for n in after])
+    np.savez_compressed(os.path.join(HERE, "prune_gaps.npz"), **out)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -821,5 +861,8 @@ if __name__ == "__main__":
     elif "--optimize" in sys.argv:
         _setup(ref)
         optimize_cases()
+    elif "--prune" in sys.argv:
+        _setup(ref)
+        prune_cases()
     else:
         main(ref)

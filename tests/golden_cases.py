@@ -17,7 +17,7 @@ def case_names():
     GTR inference cases)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                   if not os.path.basename(p).startswith(("blgrid_", "gtrinf_", "fitch_", "vcf_", "sample_",
-                                                          "extra_", "optimize_")))
+                                                          "extra_", "optimize_", "prune_")))
 
 
 def optimize_cases():

@@ -128,3 +128,26 @@ def test_profile_branch_groups_rows():
             else:
                 assert pp == "TIPOUT" and r == (k - L.n_int) * P and c == -1
     assert seen.all()
+
+
+@pytest.mark.parametrize("alphabet,ignore_gaps", [("nuc", True), ("nuc", False), ("nuc_nogap", True), ("aa", True)])
+def test_pair_counts_equal_state_pair(alphabet, ignore_gaps):
+    """The host pair counts used for a re-parented node when pruning equal
+    TreeTime's GTR.state_pair (the oracle's restatement, both alphabet-size
+    branches) after its cast to integers, with masked multiplicities."""
+    from oracle import anc
+    from treetime_gb300.anc_gpu import pair_counts
+    from treetime_gb300.gtr import GTR
+    g = GTR.standard("JC69", alphabet=alphabet)
+    q = g.n_states
+    rng = np.random.default_rng(q + ignore_gaps)
+    L = 500
+    a = rng.integers(q, size=L)
+    b = np.where(rng.random(L) < 0.2, rng.integers(q, size=L), a)
+    mult = rng.integers(1, 5, size=L) * np.where(rng.random(L) < 0.3, 0.5, 1.0)
+    got = np.trunc(pair_counts(a, b, mult, q, g.gap_index, ignore_gaps))
+    pairs, cnt = anc.state_pair(g, g.alphabet[a], g.alphabet[b], pattern_multiplicity=mult, ignore_gaps=ignore_gaps)
+    want = np.zeros((q, q))
+    for (i, j), c in zip(pairs, cnt):
+        want[i, j] = c
+    np.testing.assert_array_equal(got, want)

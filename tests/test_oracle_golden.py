@@ -302,3 +302,22 @@ def test_oracle_optimize_tree_marginal_matches_treetime(tag, g):
     for name, codes in cseq.items():
         np.testing.assert_array_equal(np.frombuffer(np.asarray(res["cseq"][name]).astype("S1").tobytes(), np.uint8),
                                       codes)
+
+
+def test_oracle_prune_short_branches_matches_treetime():
+    """Short-branch pruning with a collapsed parent: TreeTime compares the
+    next node with its new parent (where a gap no longer hides a mismatch)
+    and keeps it; the oracle's restatement gives TreeTime's topology."""
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import parse_newick
+    g = gc.load("prune_gaps")
+    tree = parse_newick(str(g["newick"]))
+    anc.prepare_tree(tree)
+    model = GTR.standard("JC69", alphabet="nuc")
+    chars = g["cseq"].view("S1").astype("U1")
+    cseq = {str(k): chars[i] for i, k in enumerate(g["cseq_names"])}
+    collapsed = anc.prune_short_branches(tree, lambda n: cseq[n.name], g["multiplicity"], model,
+                                         float(g["one_mutation"]))
+    assert collapsed == ["X"]
+    got = {n.name: (n.up.name if n.up is not None else "") for n in anc.preorder(tree.root)}
+    assert got == dict(zip(g["node_names"].tolist(), g["parent_names"].tolist()))

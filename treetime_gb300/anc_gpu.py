@@ -42,6 +42,19 @@ def _count_clades(root):
     return n
 
 
+def pair_counts(seq_p, seq_ch, mult, q, gap_index, ignore_gaps):
+    """[q, q] multiplicity-weighted counts of (parent state, child state) over
+    the patterns of two state-index sequences, positions with a gap on either
+    side left out when `ignore_gaps` (GTR.state_pair, treetime/gtr.py:631-712,
+    before its cast to integers)."""
+    w = np.asarray(mult, dtype=float)
+    a = np.asarray(seq_p, dtype=np.int64)
+    b = np.asarray(seq_ch, dtype=np.int64)
+    if ignore_gaps and gap_index is not None:
+        w = np.where((a == gap_index) | (b == gap_index), 0.0, w)
+    return np.bincount(a * q + b, weights=w, minlength=q * q).reshape(q, q)
+
+
 class ResultStore:
     """Host view of one reconstruction's device results; node attributes are
     built from it on first access."""
@@ -400,7 +413,10 @@ class GPUAncMixin:
         return N_diff
 
     # --------------------------------------------------------- branch lengths
-    def _pair_histograms(self):
+    def _pair_histograms(self, ignore_gaps=None):
+        """(session, [n_nodes, q, q] device histograms of (parent, child) states
+        per branch), gaps excluded when `ignore_gaps` (default: the instance's
+        setting)."""
         sess = self._get_session()
         layout = sess["layout"]
         name_to_row, _ = self._aln_index()
@@ -411,8 +427,9 @@ class GPUAncMixin:
                         "TreeAnc.optimal_branch_length: terminal node alignments required; sequence is missing for "
                         "leaf: '%s'. Missing terminal sequences can be inferred from sister nodes by rerunning with "
                         "`reconstruct_tip_states=True` or `--reconstruct-tip-states`" % n.name)
+        ig = self.ignore_gaps if ignore_gaps is None else ignore_gaps
         hist, _ = engine.state_pairs(sess["forest"], sess["bufs"], engine.char_state_table(self.gtr),
-                                     self.gtr.gap_index, self.ignore_gaps, self.reconstructed_tip_sequences)
+                                     self.gtr.gap_index, ig, self.reconstructed_tip_sequences)
         return sess, hist
 
     def optimize_branch_lengths_joint(self, **kwargs):
@@ -765,16 +782,40 @@ class GPUAncMixin:
                 break
         return ttconf.SUCCESS
 
+    def _prob_zero_reparented(self, sess, node, states):
+        """Probability at distance zero of `node`'s states given its current
+        parent's (a parent that replaced a collapsed one): the pair counts of
+        the two reconstructed sequences (gaps ignored, node mask applied,
+        truncated to integers as GTR.state_pair does), evaluated on the device.
+        `states` caches the host copy of the states between calls."""
+        layout = sess["layout"]
+        t = engine.torch()
+        if not states:
+            P = self.data.compressed_length
+            st = sess["bufs"].cache[("states", t.uint8)][: layout.n_nodes * P].cpu().numpy()
+            states.append(st.reshape(layout.n_nodes, P))
+        st = states[0]
+        a = st[layout.local[id(node.up)]]
+        b = st[layout.local[id(node)]]
+        mask = getattr(node, "mask", None)
+        mult = self.data.multiplicity() if mask is None else self.data.multiplicity(mask=mask)
+        c = pair_counts(a, b, mult, self.gtr.n_states, self.gtr.gap_index, True)
+        d = t.as_tensor(np.trunc(c)[None], dtype=t.float64, device=sess["forest"].device)
+        return float(np.exp(engine.prob_t_pairs_batch(self.gtr.n_states, d, sess["model"], 0.0))[0])
+
     def prune_short_branches(self):
         """Collapse internal branches shorter than 0.1 / L whose sequences have
-        probability > 0.1 at distance zero (treetime/treeanc.py:1475-1497); the
-        histograms and zero-length likelihoods of all branches come from one
-        device pass."""
+        probability > 0.1 at distance zero (treetime/treeanc.py:1475-1497);
+        the histograms and zero-length likelihoods of all branches come from
+        one device pass.  As in TreeTime, the pairs are counted with gaps
+        ignored (GTR.prob_t's default), and a node whose parent was collapsed
+        earlier in the same pass is compared with its new parent."""
         self.logger("TreeAnc.prune_short_branches: pruning short branches (max prob at zero)...", 1)
-        sess, hist = self._pair_histograms()
+        sess, hist = self._pair_histograms(ignore_gaps=True)
         layout = sess["layout"]
         counts = engine.torch().trunc(hist)
         prob0 = np.exp(engine.prob_t_pairs_batch(self.gtr.n_states, counts, sess["model"], 0.0))
+        states = []  # host copy of the reconstructed states, fetched when a parent changed
         changed = False
         for node in self.tree.find_clades():
             if node.up is None or not node.clades:
@@ -782,7 +823,14 @@ class GPUAncMixin:
             k = layout.local.get(id(node))
             if k is None:
                 continue
-            if node.branch_length < 0.1 * self.one_mutation and prob0[k] > 0.1:
+            if not node.branch_length < 0.1 * self.one_mutation:
+                continue
+            pk = layout.parent[k]
+            if pk >= 0 and layout.nodes[pk] is node.up:
+                p0 = prob0[k]
+            else:
+                p0 = self._prob_zero_reparented(sess, node, states)
+            if p0 > 0.1:
                 node.up.clades = [c for c in node.up.clades if c is not node] + node.clades
                 for c in node.clades:
                     c.up = node.up

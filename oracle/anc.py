@@ -661,6 +661,37 @@ def prune_short_branches(tree, cseq_of, mult, model, one_mutation):
     return out
 
 
+def optimize_tree_joint(tree, aln, mult, model, full_length, one_mutation, max_iter=5, prune_short=True):
+    """TreeAnc.optimize_tree with branch_length_mode='joint' (treeanc.py:
+    1384-1473): joint reconstruction, joint branch lengths, then up to
+    max_iter rounds of (pruning of short branches, joint reconstruction; stop
+    when no character changed; joint branch lengths).  Branch lengths and the
+    topology of ``tree`` are updated in place.  Returns (last joint result,
+    unconstrained_sequence_LH)."""
+    def cseq_of(cseq):
+        return lambda n: cseq[n.name] if n.clades or n.name not in aln else aln[n.name]
+
+    def set_lengths(res):
+        new = optimize_branch_lengths_joint(tree, cseq_of(res["cseq"]), mult, model)
+        for n in postorder(tree.root):
+            if n is not tree.root:
+                n.branch_length = new[n.name]
+                n.mutation_length = new[n.name]
+
+    res = joint(tree, aln, mult, model, full_length)
+    set_lengths(res)
+    n = 0
+    while n < max_iter:
+        n += 1
+        if prune_short:
+            prune_short_branches(tree, cseq_of(res["cseq"]), mult, model, one_mutation)
+        res = joint(tree, aln, mult, model, full_length, prev_cseq=res["cseq"])
+        if res["N_diff"] < 1:
+            break
+        set_lengths(res)
+    return res, float((res["sequence_LH"] * mult).sum())
+
+
 # --------------------------------------------------------------- compression
 def seq2array(seq, fill_overhangs=False, ambiguous="N", convert_upper=True):
     """seq_utils.py:152-204 for word length 1."""

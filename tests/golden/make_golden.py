@@ -12,6 +12,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source --extra-sites   (constant sites beyond the alignment)
     python tests/golden/make_golden.py /path/to/treetime-source --optimize   (optimize_tree_marginal iterations)
     python tests/golden/make_golden.py /path/to/treetime-source --prune   (short-branch pruning with a gap)
+    python tests/golden/make_golden.py /path/to/treetime-source --optimize-joint   (optimize_tree, joint mode)
 
 Biopython and pandas are replaced by the test-only stand-ins under
 ``oracle/bioshim``.  Inputs are seeded synthetic workloads from
@@ -700,6 +701,44 @@ def prune_cases():
     np.savez_compressed(os.path.join(HERE, "prune_gaps.npz"), **out)
 
 
+def optimize_joint_cases():
+    """TreeAnc.optimize_tree(branch_length_mode='joint', prune_short=True): the
+    topology, branch lengths, sequences and unconstrained log-likelihood after
+    TreeTime's joint iterations, on a tree with many branches without
+    mutations (pruned to polytomies)."""
+    from treetime import TreeAnc
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import to_newick
+    rng = np.random.default_rng(95)
+    tree = synth.coalescent_tree(30, 0.004, rng)
+    pi = rng.dirichlet(np.ones(4))
+    W = np.triu(rng.uniform(0.5, 2.0, size=(4, 4)), 1)
+    W = W + W.T
+    g = GTR.custom(mu=1.0, pi=pi, W=W, alphabet="nuc_nogap")
+    aln = synth._to_text(synth.evolve(tree, g, 250, rng), g.alphabet, 0.0, rng)
+    nwk = to_newick(tree)
+    params = {"pi": pi, "W": W, "alphabet": "nuc_nogap", "mu": 1.0}
+    tr, recs = _bio_inputs(nwk, aln)
+    t = TreeAnc(tree=tr, aln=recs, gtr=_ref_gtr("gtr", params), verbose=0)
+    n_before = sum(1 for _ in t.tree.find_clades())
+    t.optimize_tree(branch_length_mode="joint", max_iter=3, prune_short=True)
+    nodes = list(t.tree.find_clades())
+    out = {"newick": np.array(nwk), "aln_names": np.array(list(aln.keys())),
+           "aln_seqs": np.array(list(aln.values())), "kind": np.array("gtr"),
+           "one_mutation": t.one_mutation, "n_nodes_before": n_before}
+    for k, v in params.items():
+        out["param_" + k] = np.asarray(v)
+    out["node_names"] = np.array([n.name for n in nodes])
+    out["parent_names"] = np.array([n.up.name if n.up is not None else "" for n in nodes])
+    out["node_bl"] = np.array([n.branch_length for n in nodes], dtype=float)
+    out["unconstrained_LH"] = t.tree.unconstrained_sequence_LH
+    inner = [n for n in nodes if n.clades]
+    out["cseq_names"] = np.array([n.name for n in inner])
+    out["cseq"] = np.stack([_codes(n._cseq) for n in inner])
+    np.savez_compressed(os.path.join(HERE, "optimize_joint.npz"), **out)
+
+
 def main(ref_path):
     _setup(ref_path)
     from treetime_gb300 import synth
@@ -858,11 +897,14 @@ if __name__ == "__main__":
     elif "--extra-sites" in sys.argv:
         _setup(ref)
         extra_sites_cases()
-    elif "--optimize" in sys.argv:
+    elif "--optimize" in sys.argv and "--optimize-joint" not in sys.argv:
         _setup(ref)
         optimize_cases()
     elif "--prune" in sys.argv:
         _setup(ref)
         prune_cases()
+    elif "--optimize-joint" in sys.argv:
+        _setup(ref)
+        optimize_joint_cases()
     else:
         main(ref)

@@ -321,3 +321,26 @@ def test_oracle_prune_short_branches_matches_treetime():
     assert collapsed == ["X"]
     got = {n.name: (n.up.name if n.up is not None else "") for n in anc.preorder(tree.root)}
     assert got == dict(zip(g["node_names"].tolist(), g["parent_names"].tolist()))
+
+
+def test_oracle_optimize_tree_joint_matches_treetime():
+    """TreeTime's joint optimize_tree loop (reconstruction, branch lengths,
+    pruning of branches without mutations, until no character changes): the
+    oracle's restatement gives the same topology, branch lengths, sequences
+    and unconstrained log-likelihood."""
+    g = gc.load("optimize_joint")
+    tree, aln, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    assert sum(1 for _ in anc.preorder(tree.root)) == int(g["n_nodes_before"])
+    caln, mult, L = gc.compress_inputs(aln, model)
+    res, lh = anc.optimize_tree_joint(tree, caln, mult, model, L, float(g["one_mutation"]), max_iter=3)
+    got = {n.name: (n.up.name if n.up is not None else "") for n in anc.preorder(tree.root)}
+    assert got == dict(zip(g["node_names"].tolist(), g["parent_names"].tolist()))
+    want = _names_map(g["node_names"], g["node_bl"])
+    for n in anc.preorder(tree.root):
+        v = want[n.name]
+        assert abs(n.branch_length - v) <= 1e-9 * abs(v) + 1e-12, (n.name, n.branch_length, v)
+    assert abs(lh - float(g["unconstrained_LH"])) <= 1e-9 * abs(float(g["unconstrained_LH"]))
+    for name, codes in _names_map(g["cseq_names"], g["cseq"]).items():
+        np.testing.assert_array_equal(np.frombuffer(np.asarray(res["cseq"][name]).astype("S1").tobytes(), np.uint8),
+                                      codes)

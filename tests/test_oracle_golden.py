@@ -344,3 +344,59 @@ def test_oracle_optimize_tree_joint_matches_treetime():
     for name, codes in _names_map(g["cseq_names"], g["cseq"]).items():
         np.testing.assert_array_equal(np.frombuffer(np.asarray(res["cseq"][name]).astype("S1").tobytes(), np.uint8),
                                       codes)
+
+
+def test_mixin_prune_logic_matches_treetime(monkeypatch):
+    """GPUAncMixin.prune_short_branches' host logic (preorder visit, collapse,
+    the re-parented node compared with its new parent) on the pruning
+    fixture, with the device pieces (pair histograms of the layout's
+    branches, log P at distance zero) stood in for by the oracle on the CPU."""
+    import torch
+    from types import SimpleNamespace
+    from treetime_gb300 import engine
+    from treetime_gb300.anc_gpu import GPUAncMixin, pair_counts
+    from treetime_gb300.gtr import GTR
+    from treetime_gb300.tree import parse_newick
+    g = gc.load("prune_gaps")
+    tree = parse_newick(str(g["newick"]))
+    anc.prepare_tree(tree)
+    layout = engine.TreeLayout(tree.root)
+    model = GTR.standard("JC69", alphabet="nuc")
+    q, mult = model.n_states, g["multiplicity"]
+    P = len(mult)
+    index = {c: i for i, c in enumerate(model.alphabet)}
+    chars = g["cseq"].view("S1").astype("U1")
+    states = np.zeros((layout.n_nodes, P), np.uint8)
+    for name, row in zip(g["cseq_names"].tolist(), chars):
+        k = next(i for i, n in enumerate(layout.nodes) if n.name == name)
+        states[k] = [index[c] for c in row]
+    hist = np.zeros((layout.n_nodes, q, q))
+    for k in range(layout.n_nodes):
+        if layout.parent[k] >= 0 and k < layout.n_int:
+            hist[k] = pair_counts(states[layout.parent[k]], states[k], mult, q, model.gap_index, True)
+    sess = {"layout": layout, "model": model, "forest": SimpleNamespace(device="cpu"),
+            "bufs": SimpleNamespace(cache={("states", torch.uint8): torch.from_numpy(states.reshape(-1))})}
+
+    def log_p0(q_, counts, model_, t):
+        out = []
+        for c in counts.cpu().numpy():
+            nz = np.argwhere(c > 0)
+            out.append(anc.prob_t_compressed(model_, nz, c[nz[:, 0], nz[:, 1]], t, return_log=True) if len(nz)
+                       else 0.0)
+        return np.array(out)
+
+    monkeypatch.setattr(engine, "prob_t_pairs_batch", log_p0)
+
+    class Host(GPUAncMixin):
+        def logger(self, *args, **kwargs):
+            pass
+
+    host = Host()
+    host.tree, host.gtr = SimpleNamespace(find_clades=tree.find_clades, root=tree.root), model
+    host.data = SimpleNamespace(multiplicity=lambda mask=None: mult if mask is None else mult * mask,
+                                compressed_length=P)
+    host.one_mutation = float(g["one_mutation"])
+    host._pair_histograms = lambda ignore_gaps=None: (sess, torch.from_numpy(hist))
+    host.prune_short_branches()
+    got = {n.name: (n.up.name if n.up is not None else "") for n in anc.preorder(tree.root)}
+    assert got == dict(zip(g["node_names"].tolist(), g["parent_names"].tolist()))

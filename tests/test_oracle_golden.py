@@ -400,3 +400,47 @@ def test_mixin_prune_logic_matches_treetime(monkeypatch):
     host.prune_short_branches()
     got = {n.name: (n.up.name if n.up is not None else "") for n in anc.preorder(tree.root)}
     assert got == dict(zip(g["node_names"].tolist(), g["parent_names"].tolist()))
+
+
+@pytest.mark.parametrize("tag,g", gc.optimize_cases(), ids=lambda x: x if isinstance(x, str) else "")
+def test_mixin_optimize_tree_marginal_logic_matches_treetime(tag, g, monkeypatch):
+    """GPUAncMixin.optimize_tree_marginal's host logic (damping, tolerances,
+    the bifurcating root's pair updated at both children's visits, the stop
+    rule) on TreeTime's fixture, with the device pieces (reconstruction,
+    profile Brent) stood in for by the oracle on the CPU."""
+    from types import SimpleNamespace
+    from treetime_gb300 import engine
+    from treetime_gb300.anc_gpu import GPUAncMixin
+    tree, aln, model, _ = gc.inputs_from(g)
+    anc.prepare_tree(tree)
+    caln, mult, L = gc.compress_inputs(aln, model)
+    monkeypatch.setattr(engine, "optimal_t_compressed",
+                        lambda gtr, pair, m, profiles=False, tol=1e-10:
+                        anc.optimal_t_compressed(model, pair, m, profiles=profiles, tol=tol)[0])
+
+    class Host(GPUAncMixin):
+        def logger(self, *args, **kwargs):
+            pass
+
+        def infer_ancestral_sequences(self, marginal=True, **kwargs):
+            self.res = anc.marginal(tree, caln, mult, model, L)
+            for n in anc.preorder(tree.root):
+                n.marginal_subtree_LH = self.res["subtree_LH"][n.name]
+                n.marginal_outgroup_LH = self.res["outgroup_LH"][n.name]
+
+        def sequence_LH(self):
+            return self.res["total_sequence_LH"]
+
+        def _marginal_branch_lengths(self, nodes, tol):
+            return np.array([anc.optimal_t_compressed(model, (n.marginal_outgroup_LH, n.marginal_subtree_LH), mult,
+                                                      profiles=True, tol=tol)[0] for n in nodes])
+
+    host = Host()
+    host.tree, host.gtr = tree, model
+    host.data = SimpleNamespace(multiplicity=lambda mask=None: mult if mask is None else mult * mask)
+    host.optimize_tree_marginal(max_iter=4)
+    want = _names_map(g["node_names"], g["node_bl"])
+    for n in anc.preorder(tree.root):
+        v = want[n.name]
+        assert abs(n.branch_length - v) <= 1e-9 * abs(v) + 1e-12, (tag, n.name, n.branch_length, v)
+    assert abs(host.sequence_LH() - float(g["total_LH"])) <= 1e-9 * abs(float(g["total_LH"]))

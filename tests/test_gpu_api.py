@@ -222,9 +222,9 @@ def _heavy_pair():
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape", ["many_patterns", "many_heavy"])
 def test_fp32_profile_brent_matches_fp64(shape):
-    """FP32-profile Brent (FP32 objective) against the FP64 path: patterns
-    beyond the shared-memory rows (read from the stored profiles at every
-    evaluation), and more than 64 heavy patterns (the first 64 in FP64).
+    """FP32-profile Brent (FP32 objective) against the FP64 path: more
+    patterns than the kernel's shared memory holds (rows staged in the CTA's
+    workspace slice), and more than 64 heavy patterns (the first 64 in FP64).
     Lengths agree to 2e-3 relative, or the FP64 objective agrees to 1e-6."""
     from oracle import anc as oanc
     if shape == "many_patterns":

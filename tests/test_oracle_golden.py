@@ -444,3 +444,90 @@ def test_mixin_optimize_tree_marginal_logic_matches_treetime(tag, g, monkeypatch
         v = want[n.name]
         assert abs(n.branch_length - v) <= 1e-9 * abs(v) + 1e-12, (tag, n.name, n.branch_length, v)
     assert abs(host.sequence_LH() - float(g["total_LH"])) <= 1e-9 * abs(float(g["total_LH"]))
+
+
+def test_treeanc_optimize_tree_joint_logic_matches_treetime(monkeypatch):
+    """treetime_gb300.TreeAnc.optimize_tree in joint mode (the loop, the
+    mixin's joint branch lengths and pruning, node preparation) on TreeTime's
+    fixture, with the device pieces (joint reconstruction, pair histograms,
+    Brent on pair counts, log P at distance zero) stood in for by the oracle
+    on the CPU."""
+    import torch
+    from types import SimpleNamespace
+    from treetime_gb300 import TreeAnc, engine
+    from treetime_gb300.tree import parse_newick
+    g = gc.load("optimize_joint")
+    _, aln, model, _ = gc.inputs_from(g)
+    q = model.n_states
+
+    def counts_of(c):
+        nz = np.argwhere(c > 0)
+        return nz, c[nz[:, 0], nz[:, 1]]
+
+    def log_p0(q_, counts, model_, t):
+        out = []
+        for c in counts.cpu().numpy():
+            nz, m = counts_of(c)
+            out.append(anc.prob_t_compressed(model, nz, m, t, return_log=True) if len(nz) else 0.0)
+        return np.array(out)
+
+    def brent_pairs(q_, counts, model_, model_of=None, tol=1e-10):
+        ts = []
+        for c in counts.cpu().numpy():
+            nz, m = counts_of(c)
+            ts.append(anc.optimal_t_compressed(model, nz, m, tol=tol)[0] if len(nz) else 0.0)
+        return torch.tensor(ts, dtype=torch.float64), torch.zeros(len(ts), dtype=torch.int32)
+
+    monkeypatch.setattr(engine, "prob_t_pairs_batch", log_p0)
+    monkeypatch.setattr(engine, "optimal_t_pairs", brent_pairs)
+
+    class Host(TreeAnc):
+        def _compressed(self):
+            chars = {k: np.array(list(v)) for k, v in self.data.compressed_alignment.items()}
+            return chars, self.data.multiplicity(), self.data.full_length
+
+        def _ml_anc_joint(self, reconstruct_tip_states=False, **kwargs):
+            caln, mult, L = self._compressed()
+            inner = [n for n in self.tree.find_clades() if n.clades]
+            prev = {n.name: n._cseq for n in inner} if self.sequence_reconstruction else None
+            res = anc.joint(self.tree, caln, mult, model, L, prev_cseq=prev)
+            for n in inner:
+                n._cseq = res["cseq"][n.name]
+            self.tree.sequence_LH = res["sequence_LH"]
+            self.sequence_reconstruction = "joint"
+            self.reconstructed_tip_sequences = False
+            return res["N_diff"]
+
+        def _pair_histograms(self, ignore_gaps=None):
+            ig = self.ignore_gaps if ignore_gaps is None else ignore_gaps
+            caln, mult, _ = self._compressed()
+            layout = engine.TreeLayout(self.tree.root)
+            seq = lambda n: n._cseq if n.clades else caln[n.name]
+            hist = np.zeros((layout.n_nodes, q, q))
+            states = np.zeros((layout.n_nodes, len(mult)), np.uint8)
+            idx = {c: i for i, c in enumerate(model.alphabet)}
+            for k, n in enumerate(layout.nodes):
+                if n.clades:
+                    states[k] = [idx[c] for c in n._cseq]
+                if layout.parent[k] >= 0:
+                    m = mult if getattr(n, "mask", None) is None else mult * n.mask
+                    nz, cnt = anc.state_pair(model, seq(layout.nodes[layout.parent[k]]), seq(n),
+                                             pattern_multiplicity=m, ignore_gaps=ig)
+                    for (i, j), c in zip(nz, cnt):
+                        hist[k, i, j] = c
+            sess = {"layout": layout, "model": model, "forest": SimpleNamespace(device="cpu"),
+                    "bufs": SimpleNamespace(cache={("states", torch.uint8): torch.from_numpy(states.reshape(-1))})}
+            return sess, torch.from_numpy(hist)
+
+    tree = parse_newick(str(g["newick"]))
+    t = Host(tree=tree, aln=aln, gtr=model, verbose=0)
+    assert sum(1 for _ in t.tree.find_clades()) == int(g["n_nodes_before"])
+    t.optimize_tree(branch_length_mode="joint", max_iter=3, prune_short=True)
+    got = {n.name: (n.up.name if n.up is not None else "") for n in t.tree.find_clades()}
+    assert got == dict(zip(g["node_names"].tolist(), g["parent_names"].tolist()))
+    want = _names_map(g["node_names"], g["node_bl"])
+    for n in t.tree.find_clades():
+        v = want[n.name]
+        assert abs(n.branch_length - v) <= 1e-9 * abs(v) + 1e-12, (n.name, n.branch_length, v)
+    lh = float(g["unconstrained_LH"])
+    assert abs(t.tree.unconstrained_sequence_LH - lh) <= 1e-9 * abs(lh)

@@ -1,6 +1,8 @@
-"""Admission policy of the serving loop (host logic, no GPU): jobs are
-admitted in arrival order while a slot is free and their device footprint
-fits; a job that does not fit holds the head of the queue."""
+"""Host logic of the serving loop (no GPU): the admission policy (arrival
+order while a slot is free and the device footprint fits; a job that does not
+fit holds the head of the queue), the staging of tip codes at submission, and
+the scheduler loop with its device work stood in for (admission order, slots,
+collection, error reporting)."""
 
 from types import SimpleNamespace
 

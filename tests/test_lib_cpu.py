@@ -151,3 +151,33 @@ def test_pair_counts_equal_state_pair(alphabet, ignore_gaps):
     for (i, j), c in zip(pairs, cnt):
         want[i, j] = c
     np.testing.assert_array_equal(got, want)
+
+
+def test_model_cache_is_a_bounded_lru(monkeypatch):
+    """engine.model_for keeps the DeviceModels of the most recently used GTR
+    objects (bounded), rebuilds one when the model's numbers change, and an
+    entry keeps its GTR alive (so its id cannot be taken by another object)."""
+    from treetime_gb300 import engine
+    from treetime_gb300.gtr import GTR
+
+    class FakeModel:
+        def __init__(self, gtrs, device=None):
+            self.gtrs = [gtrs]
+
+    monkeypatch.setattr(engine, "DeviceModel", FakeModel)
+    monkeypatch.setattr(engine, "require_device", lambda device=None: "cpu")
+    monkeypatch.setattr(engine, "_MODEL_CACHE", engine.collections.OrderedDict())
+    monkeypatch.setattr(engine, "MODEL_CACHE_SIZE", 3)
+    gs = [GTR.standard("JC69", alphabet="nuc_nogap") for _ in range(5)]
+    first = engine.model_for(gs[0])
+    assert engine.model_for(gs[0]) is first                      # cached
+    for g in gs[1:4]:
+        engine.model_for(g)
+    assert len(engine._MODEL_CACHE) == 3 and id(gs[0]) not in engine._MODEL_CACHE  # least recent evicted
+    engine.model_for(gs[1])                                       # gs[1] becomes the most recent
+    engine.model_for(gs[4])
+    assert id(gs[2]) not in engine._MODEL_CACHE and id(gs[1]) in engine._MODEL_CACHE
+    m1 = engine.model_for(gs[1])
+    gs[1].assign_rates(mu=2.0)                                    # new numbers: rebuilt
+    assert engine.model_for(gs[1]) is not m1
+    assert all(e[1].gtrs[0] is not None for e in engine._MODEL_CACHE.values())

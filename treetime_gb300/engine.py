@@ -13,6 +13,7 @@ Layout of a forest in device memory (see include/treetime_gb300.h):
     (16-byte vector loads); states as [node][pattern] bytes.
 """
 
+import collections
 import ctypes as C
 import time
 
@@ -208,7 +209,12 @@ class DeviceModel:
                               _p(self.lut))
 
 
-_MODEL_CACHE = {}
+# DeviceModels of recently used GTR objects, least recently used first.  An entry holds its GTR
+# (DeviceModel.gtrs), so the id it is filed under cannot be reused by another object while the
+# entry exists; the bound keeps a long-running server that sees a new model per request from
+# holding every model it has seen.
+_MODEL_CACHE = collections.OrderedDict()
+MODEL_CACHE_SIZE = 256
 
 
 def model_key(gtr):
@@ -226,6 +232,9 @@ def model_for(gtr, device=None):
     if m is None or m[0] != key:
         m = (key, DeviceModel(gtr, dev))
         _MODEL_CACHE[id(gtr)] = m
+    _MODEL_CACHE.move_to_end(id(gtr))
+    while len(_MODEL_CACHE) > MODEL_CACHE_SIZE:
+        _MODEL_CACHE.popitem(last=False)
     return m[1]
 
 

@@ -614,6 +614,7 @@ class CapturedMarginal:
         with t.cuda.graph(self.graph):
             self.out = marginal(forest, model, bufs, sync=False, **kw)
         self.status = bufs.get("status", (1,), t.int32)
+        self._keep = (forest, model, bufs)  # the captured launches point into their device buffers
 
     def replay(self, sync=False):
         self.graph.replay()

@@ -9,7 +9,11 @@ Tolerances (written here, per the contract of this port):
     margin at some node is below 1e-9 (counted, reported);
   * marginal argmax states bit-exact except where the reference profile's
     top-two margin is below 1e-9 (FP64) / 1e-5 (FP32);
-  * branch lengths 1e-6 relative + 1e-10 absolute (FP64 profiles / pairs).
+  * branch lengths 1e-6 relative + 1e-10 absolute (FP64 profiles / pairs);
+  * the iterative loops (optimize_tree_marginal, joint optimize_tree with
+    pruning), whose Brent searches stop at TreeTime's loose early tolerances:
+    branch lengths 1e-5 / 1e-4 relative + 1e-10, topology exact,
+    log-likelihoods 1e-9 / 1e-10 relative.
 """
 
 import numpy as np

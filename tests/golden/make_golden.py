@@ -878,7 +878,10 @@ def main(ref_path):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else os.environ.get("TREETIME_SOURCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <path of the TreeTime sources> [--case flag] "
+                 "(or set TREETIME_SOURCE)")
     if "--blgrid" in sys.argv:
         _setup(ref)
         blgrid_cases()

@@ -63,7 +63,7 @@ def test_submit_stages_codes_for_a_bounded_number_of_waiting_jobs():
     g = GTR.standard("JC69", alphabet="nuc_nogap")
     srv = object.__new__(Server)  # the queueing half of the server, without a device
     srv.max_slots, srv._lock, srv._queue = 2, threading.Lock(), collections.deque()
-    srv._staged_waiting, srv._pinned = 0, Pool()
+    srv._staged_waiting, srv._pinned, srv.hbm_bytes = 0, Pool(), 1 << 40
     jobs = [Job(ti, g) for _ in range(6)]
     for j in jobs:
         srv.submit(j)
@@ -98,6 +98,8 @@ def _fake_server(monkeypatch, max_slots, polls_until_done=3):
 
     class FakeActive:
         def __init__(self, job, server):
+            if getattr(job, "oom", False):
+                raise MemoryError("CUDA out of memory (stand-in)")
             self.job, self.stream, self.it, self.done_event, self.phase_events = job, object(), 0, None, None
             self.admitted_with = len(server._active)
 
@@ -155,3 +157,38 @@ def test_scheduler_raises_a_device_error_after_the_other_jobs_finish(monkeypatch
         srv.serve(jobs, np.zeros(len(jobs)))
     assert len(srv.done) == len(jobs)
     assert all(j.result is not None for j in jobs if j is not jobs[1])
+
+
+def test_submit_rejects_a_job_larger_than_the_whole_budget(monkeypatch):
+    """A job whose device footprint exceeds the server's whole memory budget
+    could never be admitted and would hold the head of the queue for good:
+    submit raises MemoryError instead, and the queue stays usable."""
+    from treetime_gb300.serving import Job
+    ti, g = _small_job_inputs()
+    srv = _fake_server(monkeypatch, max_slots=2)
+    big = Job(ti, g)
+    srv.hbm_bytes = big.footprint - 1
+    with pytest.raises(MemoryError, match="budget"):
+        srv.submit(big)
+    assert srv.pending() == 0
+    srv.hbm_bytes = 1 << 40
+    jobs = [Job(ti, g) for _ in range(3)]
+    srv.serve(jobs, np.zeros(3))
+    assert all(j.result is not None for j in jobs)
+
+
+def test_failed_admission_fails_only_that_job(monkeypatch):
+    """A device allocation that fails while a job is admitted (stood in for by
+    a MemoryError from the admission) makes that job fail alone: its slot is
+    given back, the other jobs run to completion, and run() raises the error
+    once they have finished."""
+    from treetime_gb300.serving import Job
+    ti, g = _small_job_inputs()
+    srv = _fake_server(monkeypatch, max_slots=2)
+    jobs = [Job(ti, g) for _ in range(6)]
+    jobs[2].oom = True
+    with pytest.raises(MemoryError, match="out of memory"):
+        srv.serve(jobs, np.zeros(len(jobs)))
+    assert len(srv.done) == len(jobs) and srv.pending() == 0
+    assert jobs[2].result is None and isinstance(jobs[2].error, MemoryError)
+    assert all(j.result is not None and j.error is None for j in jobs if j is not jobs[2])

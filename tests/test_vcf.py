@@ -128,13 +128,13 @@ def test_treetime_vcf_reader_suite_passes_with_this_reader(tmp_path):
     multiple chromosomes, simple files, no-calls and missing alleles, the VCF
     specification's examples, mutation plus insertion, metadata) run against
     this package's reader.  The writing tests (write_vcf) are not part of it.
-    Skipped where the TreeTime sources are not present."""
+    Skipped unless TREETIME_SOURCE names the TreeTime sources."""
     import subprocess
     import sys
-    src = os.environ.get("TREETIME_SOURCE", "/root/reference")
-    suite = os.path.join(src, "test", "test_vcf.py")
-    if not os.path.isfile(suite):
-        pytest.skip("TreeTime sources not present")
+    src = os.environ.get("TREETIME_SOURCE")
+    suite = os.path.join(src, "test", "test_vcf.py") if src else ""
+    if not src or not os.path.isfile(suite):
+        pytest.skip("TreeTime sources not given (set TREETIME_SOURCE to their path)")
     here = os.path.dirname(os.path.abspath(__file__))
     repo = os.path.dirname(here)
     env = dict(os.environ)

@@ -172,11 +172,13 @@ class TreeLayout:
 
 def branch_lengths(layout, full_length, use_mutation_length=False):
     """Branch length used by the model: max(1e-3 / L, length)
-    (TreeAnc._branch_length_to_gtr, treetime/treeanc.py:752-760)."""
+    (TreeAnc._branch_length_to_gtr, treetime/treeanc.py:752-760).  Python's
+    max keeps its first argument when the comparison with a NaN is false, so a
+    NaN length becomes the floor there; np.fmax does the same."""
     floor = ttconf.MIN_BRANCH_LENGTH * (1.0 / full_length)
     attr = "mutation_length" if use_mutation_length else "branch_length"
     bl = np.array([getattr(n, attr) or 0.0 for n in layout.nodes], dtype=np.float64)
-    return np.maximum(floor, bl)
+    return np.fmax(floor, bl)
 
 
 # ----------------------------------------------------------------------------

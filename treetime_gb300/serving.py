@@ -351,6 +351,10 @@ class Server:
         tip codes are staged into pinned memory on the calling thread (a long
         queue does not pin the host memory of every waiting job; the others
         are packed at admission)."""
+        if job.footprint > self.hbm_bytes:
+            # it could never be admitted and would hold the head of the queue for good
+            raise MemoryError("job %s needs about %d bytes of device memory, the server's budget is %d"
+                              % (job.id, job.footprint, self.hbm_bytes))
         job.t_submit = time.perf_counter()
         with self._lock:
             stage = self._staged_waiting < 2 * self.max_slots
@@ -389,12 +393,19 @@ class Server:
                     self._staged_waiting -= 1
         for job in plan:
             job.t_admit = time.perf_counter()
-            a = _Active(job, self)
-            t1 = time.perf_counter()
-            while a.it < job.iterations:
-                a.enqueue_iteration()
-            t2 = time.perf_counter()
-            a.enqueue_results()
+            try:
+                a = _Active(job, self)
+                t1 = time.perf_counter()
+                while a.it < job.iterations:
+                    a.enqueue_iteration()
+                t2 = time.perf_counter()
+                a.enqueue_results()
+            except Exception as e:  # noqa: BLE001 -- e.g. a device allocation that failed
+                # the job fails alone: its slot and budget go back to the queue, run() raises the
+                # error once the other jobs have finished
+                self._fail_admission(job, e)
+                busy = True
+                continue
             self.host_s["admit"] += t1 - job.t_admit
             self.host_s["enqueue"] += t2 - t1
             self.host_s["results"] += time.perf_counter() - t2
@@ -403,6 +414,16 @@ class Server:
         self.peak_active = max(self.peak_active, len(self._active))
         self.peak_bytes = max(self.peak_bytes, self._used_bytes())
         return busy
+
+    def _fail_admission(self, job, err):
+        job.error = err
+        job.t_done = time.perf_counter()
+        if job._codes_buf is not None:
+            self._pinned.give(job._codes_buf)
+            job._codes_buf = None
+        with self._lock:
+            self.done.append(job)
+            self._errors.append(err)
 
     def _collect_loop(self):
         while True:

@@ -146,6 +146,23 @@ def build_workload(seed=1, **over):
     return t, wl
 
 
+def c1_config(t):
+    """The workload's `config` entry, the same in both arms."""
+    n_tip = t.tree.count_terminals()
+    P = t.data.compressed_length
+    return {"workload": WORKLOAD, "tips": n_tip, "nodes": 2 * n_tip - 1, "patterns": P, "sites": t.data.full_length,
+            "node_patterns_per_step": (2 * n_tip - 1) * P, "seed": 1,
+            "l2": "flushed (512 MiB write) before every timed step (GPU arm)", "parallelism": "single GPU"}
+
+
+def joint_bytes(layout, P, w=4):
+    """Algorithmic bytes of one joint reconstruction: per internal node and
+    pattern its sum of messages written and read (2 x w x 8 bytes, FP32
+    pairs), its argmax table (w bytes) and its state (1 byte); one code byte
+    per tip and pattern."""
+    return P * (layout.n_int * (2 * w * 8 + w + 1) + layout.n_tip)
+
+
 def algorithmic_bytes(layout, P, w=4, e=4, s=4):
     """Bytes per marginal reconstruction of one tree: P * [N_int * (5*w*e +
     3*s + 1) + n_tips * 1] + P * (8 + 4): five profile touches per internal
@@ -236,25 +253,32 @@ def run_gpu(args):
             b.record()
             b.synchronize()
             kt.append(a.elapsed_time(b))
-    torch.cuda.synchronize()
-    ms32 = _reduce_max(sum(t32) / len(t32), dev, world)
+        torch.cuda.synchronize()
+        ms32 = _reduce_max(sum(t32) / len(t32), dev, world)
 
-    # end-to-end through host buffers (pinned), copies inside the timed region
-    e2e_ms, h2d, d2h = _e2e(engine, t, forest, graphs["f32"], args.steps, args.warmup, flush)
+        # end to end through the drop-in call (host alignment in, node attributes out)
+        e2e_ms, h2d, d2h = _public_e2e(t, args.steps, args.warmup, flush)
+        # end to end through the captured graph (pinned host buffers, copies inside the timed region)
+        e2eg_ms, gh2d, gd2h = _e2e(engine, t, forest, graphs["f32"], args.steps, args.warmup, flush)
+        # joint reconstruction of the same configuration
+        joint = _joint_block(engine, t, forest, model, bufs, layout, P, args, flush)
 
-    # batched: 8 reconstructions of this workload (own buffers each) as one forest and one
-    # captured launch sequence -- the batched form of the same configuration
+    # batched: k independent instances of this configuration (seeds 1..k: their own trees,
+    # alignments and models) as one forest and one captured launch sequence -- the batched form of
+    # the configuration
     batched = None
     if args.c1_batch > 1:
         k = args.c1_batch
-        bforest = engine.Forest([sess["forest"].inputs[0]] * k, 4, device=dev)
-        bcap = engine.CapturedMarginal(bforest, model, engine.Buffers(bforest), precision="f32")
+        binputs, bgtrs = _c1_instances(k, sess["forest"].inputs[0], t.gtr)
+        bmodel = engine.DeviceModel(bgtrs, dev)
+        bforest = engine.Forest(binputs, 4, device=dev)
+        bcap = engine.CapturedMarginal(bforest, bmodel, engine.Buffers(bforest), precision="f32")
         for _ in range(3):
             bcap.replay()
         torch.cuda.synchronize()
         bt, bk = [], []
         kbufs = engine.Buffers(bforest)  # the marginal kernel timed alone writes into these
-        bpm, _ = engine.branch_pmats(bforest, model, kbufs, need32=True)
+        bpm, _ = engine.branch_pmats(bforest, bmodel, kbufs, need32=True)
         for _ in range(min(args.steps, 50)):
             flush.zero_()
             a0, b0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -266,17 +290,24 @@ def run_gpu(args):
             flush.zero_()
             a1, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a1.record()
-            _marginal_only(engine, bforest, model, kbufs, bpm, "f32")
+            _marginal_only(engine, bforest, bmodel, kbufs, bpm, "f32")
             b1.record()
             b1.synchronize()
             bk.append(a1.elapsed_time(b1))
         bms, bkm = sum(bt) / len(bt), sum(bk) / len(bk)
-        bab = k * algorithmic_bytes(layout, P)
-        batched = {"reconstructions": k, "value": k * units / (bms * 1e-3), "unit": UNIT, "ms_per_step": bms,
+        bab = sum(algorithmic_bytes(ti.layout, ti.n_patterns) for ti in binputs)
+        bunits = sum(ti.layout.n_nodes * ti.n_patterns for ti in binputs)
+        batched = {"reconstructions": k, "value": bunits / (bms * 1e-3), "unit": UNIT, "ms_per_step": bms,
+                   "node_patterns_per_step": bunits,
                    "roofline": {"achieved": bab / (bkm * 1e-3) / 1e9, "frac": bab / (bkm * 1e-3) / 1e9 / _peaks()[0],
-                                "kernel_ms": bkm, "ranges": int(len(bforest.work_f32_host))},
-                   "note": "the same alignment %d times, each with its own profile buffers, one forest, one "
-                           "captured launch sequence per step; L2 flushed before every step" % k}
+                                "kernel_ms": bkm, "ranges": int(len(bforest.work_f32_host)),
+                                "algorithmic_bytes_per_launch": bab},
+                   "note": "%d independent instances of the configuration (seeds 1..%d: own coalescent tree, "
+                           "alignment and GTR each), one forest, one captured launch sequence per step; L2 "
+                           "flushed before every step" % (k, k)}
+
+    # serving: a short run of the request loop (p50 / p99 latency)
+    serving_block = _serving_block(dev, args) if args.serving_seconds > 0 and world == 1 else None
 
     pipeline = _config_pipeline(t)
     if rank != 0:
@@ -287,6 +318,9 @@ def run_gpu(args):
     achieved = ab / (k_ms * 1e-3) / 1e9
     traffic = _traffic("marginal_f32_q4/c1")
     clocks = clk.summary()
+    cfg = c1_config(t)
+    if world > 1:
+        cfg["parallelism"] = "replicas"
     res = {
         "metric": METRIC,
         "value": world * units / (ms32 * 1e-3),
@@ -300,9 +334,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
-        "config": {"workload": WORKLOAD, "tips": layout.n_tip, "nodes": N, "patterns": P, "sites": t.data.full_length,
-                   "node_patterns_per_step": units, "l2": "flushed (512 MiB write) before every timed step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": cfg,
         "fp64_plain": {"value": units / (statistics.mean(t64) * 1e-3), "ms_per_step": statistics.mean(t64)},
         "fp32_over_fp64": statistics.mean(t64) / ms32,
         "rel_logLH_err_vs_fp64": rel_err,
@@ -313,8 +345,16 @@ def run_gpu(args):
                      "range_patterns": int(forest.work_f32_host[:, 2].max()),
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms},
         "e2e": {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms,
+                "path": "TreeAnc.infer_ancestral_sequences(marginal=True) per step: the tip codes copied from pinned "
+                        "host memory into the session's device inputs first, the node states, site and tree "
+                        "log-likelihoods back on the host after it; host clock"},
+        "e2e_graph": {"value": units / (e2eg_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": gh2d,
+                      "d2h_bytes_per_step": gd2h, "ms_per_step": e2eg_ms,
+                      "path": "the captured graph with pinned host inputs and outputs copied every step; CUDA events"},
         "gpu_launches": 3 * args.steps,
+        "joint": joint,
+        "serving": serving_block,
         "batched": batched,
         "config_pipeline": pipeline,
         "autotune": {"best": {"threads": best[0], "ctas_per_sm": best[1], "ranges_per_sm": best[2]},
@@ -1336,6 +1376,171 @@ def _marginal_only(engine, forest, model, bufs, pm, prec):
                                engine._stream()), "tt_marginal")
 
 
+def _public_e2e(t, steps, warmup, flush):
+    """The drop-in call end to end, every step: the step's tip codes are copied
+    from pinned host memory into the session's device inputs (as a new
+    alignment of the same tree would be), TreeAnc.infer_ancestral_sequences
+    (marginal=True) runs (branch lengths up, the reconstruction, the internal
+    nodes' states, the site and tree log-likelihoods and the changed-site count
+    down) and the root's sequence is read.  Host clock, device synchronised on
+    both sides.  Returns (ms per step, bytes up, bytes down)."""
+    import torch
+    sess = t._get_session()
+    forest, lay = sess["forest"], sess["layout"]
+    P = t.data.compressed_length
+    codes_h = torch.from_numpy(np.ascontiguousarray(t.data.compressed_codes).reshape(-1)).pin_memory()
+    h2d = codes_h.numel() + lay.n_nodes * 8
+    d2h = lay.n_int * P + P * 8 + 8 + 8
+    root = t.tree.root
+
+    def one():
+        forest.d_codes[: codes_h.numel()].copy_(codes_h, non_blocking=True)
+        t.infer_ancestral_sequences(marginal=True)
+        return root._cseq[0], t.tree.total_sequence_LH
+
+    for _ in range(max(3, warmup)):
+        one()
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        one()
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t0) * 1e3)
+    return sum(times) / len(times), int(h2d), int(d2h)
+
+
+def _joint_only(engine, forest, model, bufs, pm):
+    """Launch only the joint kernel (branch matrices already made)."""
+    import ctypes as C
+    import torch
+    from treetime_gb300 import _lib
+    lib = _lib.load()
+    w = forest.w
+    g = bufs.get
+    o = _lib.TTJointOut(engine._p(g("joint_msg", (forest.prof_rows, 2, w), torch.float32)),
+                        engine._p(g("cx", (forest.prof_rows, w), torch.uint8)),
+                        engine._p(g("states", (forest.state_rows,), torch.uint8)),
+                        engine._p(g("joint_site_lh", (forest.n_patterns,), torch.float64)),
+                        engine._p(g("joint_tree_lh", (len(forest.inputs),), torch.float64)), None, None, 0, 0,
+                        int(forest.prof_rows))
+    _lib.check(lib.tt_joint(C.byref(forest.struct), C.byref(model.struct), C.byref(pm), C.byref(o), None,
+                            engine._stream()), "tt_joint")
+
+
+def _joint_block(engine, t, forest, model, bufs, layout, P, args, flush):
+    """Joint reconstruction of the configuration: device time of one
+    reconstruction (branch matrices, the kernel, the tree sums; CUDA events),
+    the kernel alone against its algorithmic bytes, and the public call
+    TreeAnc.infer_ancestral_sequences(marginal=False) (host clock)."""
+    import torch
+    units = layout.n_nodes * P
+    steps = max(5, min(args.steps, 50))
+    for _ in range(3):
+        engine.joint(forest, model, bufs, sync=False)
+    torch.cuda.synchronize()
+    full, kern = [], []
+    pm, _ = engine.branch_pmats(forest, model, bufs, needlog=True)
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        engine.joint(forest, model, bufs, sync=False)
+        b.record()
+        b.synchronize()
+        full.append(a.elapsed_time(b))
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        _joint_only(engine, forest, model, bufs, pm)
+        b.record()
+        b.synchronize()
+        kern.append(a.elapsed_time(b))
+    pub = []
+    for _ in range(6):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t.infer_ancestral_sequences(marginal=False)
+        pub.append((time.perf_counter() - t0) * 1e3)
+    ms, kms = sum(full) / len(full), sum(kern) / len(kern)
+    ab = joint_bytes(layout, P)
+    peak, kind = _peaks()
+    return {"value": units / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+            "public_call_ms": statistics.median(pub[1:]),
+            "roofline": {"bound": "hbm", "achieved": ab / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": ab / (kms * 1e-3) / 1e9 / peak, "peak_source": kind,
+                         "kernel": "joint_kernel<Q=4,W=4,LPP=1,NT=%d>" % forest.threads, "kernel_ms": kms,
+                         "algorithmic_bytes_per_launch": ab},
+            "arithmetic": "double-float (FP32 pairs) max-plus; states checked against the oracle in tests"}
+
+
+def _c1_instances(k, first, first_gtr):
+    """k independent instances of the configuration: the bench's own (seed 1)
+    and seeds 2..k, each with its own tree, alignment and GTR (model index =
+    position)."""
+    import copy
+    inputs, gtrs = [], []
+    for s in range(1, k + 1):
+        if s == 1:
+            ti, g = first, first_gtr
+        else:
+            t, _ = build_workload(seed=s)
+            ti, g = t._get_session()["forest"].inputs[0], t.gtr
+        ti = copy.copy(ti)
+        ti.model = len(gtrs)
+        inputs.append(ti)
+        gtrs.append(g)
+    return inputs, gtrs
+
+
+def _serving_block(dev, args):
+    """A short run of the serving loop (Poisson arrivals at --c4-rate for
+    --serving-seconds): 90% nucleotide jobs on trees of the batch's size
+    distribution (a pool of 24 trees and alignments; every request brings its
+    own freshly drawn GTR, so no device model is reused), half reconstruction
+    and half branch-length jobs, 10% protein jobs (site-specific model, two
+    trees and four models).  Reports p50 / p99 latency, throughput and the
+    device-model cache builds and hits."""
+    from treetime_gb300 import TreeAnc, engine, serving, synth
+    from treetime_gb300.gtr import GTR
+    rng = np.random.default_rng(77)
+    nuc, _ = synth.forest_c3(n_trees=24, seed=71)
+    prot = []
+    for s in range(2):
+        wl = synth.make_workload("c2", seed=80 + s)
+        t = TreeAnc(tree=wl["tree"], aln=wl["aln"], gtr=wl["gtr"], compress=False, verbose=0, device=dev)
+        prot.append(t._get_session()["forest"].inputs[0])
+    prot_models = [synth.gtr_c2(np.random.default_rng(90 + s), prot[0].n_patterns) for s in range(4)]
+    rate, window = args.c4_rate, args.serving_seconds
+    n = int(rng.poisson(rate * window))
+    arrivals = np.sort(rng.uniform(0.0, window, size=n))
+    jobs = []
+    for i in range(n):
+        if rng.random() < 0.1:
+            jobs.append(serving.Job(prot[int(rng.integers(2))], prot_models[int(rng.integers(4))], kind="marginal",
+                                    iterations=3))
+        else:
+            g = GTR.random(mu=1.0, alphabet="nuc_nogap", rng=rng)
+            jobs.append(serving.Job(nuc[int(rng.integers(len(nuc)))], g,
+                                    kind="marginal" if rng.random() < 0.5 else "optimize", iterations=3))
+    warm = [serving.Job(nuc[0], GTR.random(mu=1.0, alphabet="nuc_nogap", rng=rng), "marginal"),
+            serving.Job(nuc[1], GTR.random(mu=1.0, alphabet="nuc_nogap", rng=rng), "optimize"),
+            serving.Job(prot[0], prot_models[0], "marginal")]
+    serving.Server(device=dev, max_slots=args.c4_slots).serve(warm, [0.0, 0.0, 0.0])
+    before = dict(engine.CACHE_STATS)
+    srv = serving.Server(device=dev, max_slots=args.c4_slots)
+    done, wall = srv.serve(jobs, arrivals)
+    st = serving.latency_stats(done)
+    cache = {k: engine.CACHE_STATS[k] - before.get(k, 0) for k in engine.CACHE_STATS}
+    return {"window_s": window, "arrival_rate_per_s": rate, "requests": n, "jobs_done": len(done),
+            "jobs_per_s": len(done) / wall, "p50_s": st["p50"], "p99_s": st["p99"], "max_s": st["max"],
+            "node_pattern_updates_per_s": st["node_pattern_updates"] / wall,
+            "device_model_cache": cache,
+            "requests_from": "24 nucleotide trees of the batch's size distribution, each request with a fresh "
+                             "random GTR; 2 protein trees x 4 site-specific models"}
+
+
 def _e2e(engine, t, forest, graph, steps, warmup, flush):
     """Host buffers in, host buffers out: tip codes, branch lengths and
     multiplicities are copied from pinned host memory, the reconstruction runs
@@ -1438,7 +1643,7 @@ def run_reference(args):
     # one step is the whole workload on all cores (smaller samples would be dominated by the
     # per-node Python overhead); the timed steps stop after REFERENCE_BUDGET_S seconds
     with ctx.Pool(cores) as pool:
-        for _ in range(min(args.warmup, 3)):
+        for _ in range(args.warmup):
             pool.map(_oracle_chunk, inputs)
         times = []
         t_start = time.perf_counter()
@@ -1451,10 +1656,10 @@ def run_reference(args):
     sec = sum(times) / len(times)
     v = N * P / sec
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(times),
-            "steps_requested": args.steps, "warmup": min(args.warmup, 3), "ms_per_step": sec * 1e3,
+            "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
             "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "patterns": P, "nodes": N},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded coalescent tree, GTR-evolved alignment)",
+            "config": c1_config(t),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": "full marginal reconstruction per step, patterns split over %d processes"
                                        % cores},
@@ -1479,6 +1684,8 @@ def main():
                          "give more patterns than the kernel's shared memory holds)")
     ap.add_argument("--c1-batch", type=int, default=8, help="c1: reconstructions in the batched measurement (1: none)")
     ap.add_argument("--c4-slots", type=int, default=16, help="c4: jobs admitted at the same time")
+    ap.add_argument("--serving-seconds", type=float, default=2.0,
+                    help="c1: arrival window of the short serving run in the default line (0: none)")
     ap.add_argument("--shape", default="", help="c1: fixed FP32 launch shape threads/ctas_per_sm/ranges_per_sm "
                                                  "instead of the autotuner (profiling runs)")
     ap.add_argument("--c3-trees", type=int, default=256,

@@ -146,24 +146,36 @@ typedef struct tt_model {
     const double* mu;          /* [n_models]                                                       */
     const double* pi;          /* [n_models][q] equilibrium frequencies                            */
     const double* lut;         /* [256][q] profile row of each character byte                     */
+    const float* lut_log2;     /* [256][2][width] log(max(lut, 1e-12)) (non-finite -> -1e10) as
+                                  FP32 pairs hi, lo (hi + lo = the FP64 value to ~48 bits): the
+                                  joint kernel's tip log profiles; may be NULL except for tt_joint */
 } tt_model;
 
 /* Branch matrices produced by tt_branch_pmats for every node (the branch above it), rows padded
  * to `width`: entry (i, j) = P(child state i | parent state j) at [node][i][j]. */
 typedef struct tt_pmats {
     double* p64;               /* [n_nodes][q][width]  P(t) = max(0, V diag(exp(mu lam t)) V^-1)  */
-    float*  p32;               /* [n_nodes][q][width]  FP32 copy (may be NULL)                     */
+    float*  p32;               /* [n_nodes][q][width]  D(t) = P(t) - I in FP32, formed in FP64 as
+                                  V diag(expm1(mu lam t)) V^-1 (off-diagonal entries clamped at 0):
+                                  the FP32 marginal kernel's matrices (may be NULL)                */
     double* logp64;            /* [n_nodes][q][width]  log(max(1e-12, P))  (may be NULL)           */
     float*  p32_pair;          /* [n_nodes][2][q][width]: at an internal node with two children, the
-                                  FP32 matrices of its children side by side, so the FP32 marginal
+                                  FP32 D(t) matrices of its children side by side, so the FP32 marginal
                                   kernel stages a level's matrices with one contiguous copy; needs
                                   tt_forest.pair_slot (may be NULL)                                 */
+    float*  logp2;             /* [n_nodes][q][2][width] log(max(P, 1e-12)) formed in FP64 and
+                                  split into FP32 pairs (row i: width high parts, then width low
+                                  parts): the joint kernel's matrices (may be NULL)                */
+    float*  logp2_pair;        /* [n_nodes][2][q][2][width]: logp2 of the two children of a
+                                  two-child node side by side, at the parent (needs pair_slot;
+                                  may be NULL)                                                     */
 } tt_pmats;
 
 /* Outputs of the marginal pass.  Buffers hold float (TT_PREC_F32) or double (TT_PREC_F64). */
 typedef struct tt_marginal_out {
     void*    partial;          /* internal nodes' subtree profiles (marginal_subtree_LH; FP32 rows
-                                  are power-of-two scaled, not normalised)       REQUIRED           */
+                                  are scaled to a largest entry of exactly 1, not normalised)
+                                                                                 REQUIRED           */
     void*    posterior;        /* internal nodes' marginal profiles              REQUIRED           */
     void*    outgroup;         /* internal nodes' outgroup profiles, or NULL                        */
     void*    tip_posterior;    /* tips' marginal profiles, or NULL (needs reconstruct_tips)         */
@@ -180,8 +192,10 @@ typedef struct tt_marginal_out {
 } tt_marginal_out;
 
 typedef struct tt_joint_out {
-    double*  lx;               /* [rows of internal nodes][width] joint_Lx scratch (FP64)           */
-    uint8_t* cx;               /* [rows of internal nodes][width] argmax child state per parent state */
+    float*   msg;              /* [rows of internal nodes][2][width] scratch: each internal node's
+                                  sum of its children's joint_Lx, FP32 pairs (hi, lo)              */
+    uint8_t* cx;               /* [rows of internal nodes][width] joint_Cx: argmax child state per
+                                  parent state                                                     */
     uint8_t* states;           /* state per node and pattern                                        */
     double*  site_lh;          /* [n_patterns] joint log-likelihood of each pattern                 */
     double*  tree_lh;          /* [n_trees] multiplicity-weighted sum                               */
@@ -189,6 +203,8 @@ typedef struct tt_joint_out {
     const double* root_uniform;/* [n_patterns] or NULL                                              */
     int32_t  reconstruct_tips;
     int32_t  count_diff;
+    int64_t  rows;             /* rows msg and cx hold: a tree whose rows (prof_base + n_int *
+                                  n_patterns) do not fit is skipped with *status = TT_ERR_OOM     */
 } tt_joint_out;
 
 /* ---------------------------------------------------------------- library */
@@ -265,23 +281,63 @@ tt_status tt_marginal_ss_f32(const tt_forest* f, const tt_ss_f32* m, const int32
                              const tt_marginal_out* out, int32_t* status, void* stream);
 
 /* ------------------------------------------------------------ a13: joint
- * Max-product reconstruction in FP64 (log domain), root argmax/sampling, pre-order backtrack.
- * Requires tt_branch_pmats with logp64.  Replaces TreeAnc._ml_anc_joint
+ * Max-product reconstruction in the log domain (double-float: FP32 pairs, ~48 significant bits),
+ * root argmax/sampling, pre-order backtrack, over the pattern ranges of the FP32 marginal kernel
+ * (work_f32, node_rec, child_pair, threads_f32).  Requires tt_branch_pmats with logp2 and
+ * logp2_pair, and tt_model.lut_log2.  Replaces TreeAnc._ml_anc_joint
  * (treetime/treeanc.py:934-1080). */
 tt_status tt_joint(const tt_forest* f, const tt_model* m, const tt_pmats* pm, const tt_joint_out* out,
                    int32_t* status, void* stream);
+
+/* A site-specific model (GTR_site_specific) on the device: per site a, eigenvalues lam_a,
+ * eigenvectors V_a (P_a(t) = V_a diag(exp(mu_a lam_a t)) V_a^-1, entry (i, j) = P(child i |
+ * parent j)), rate mu_a, equilibrium frequencies pi_a; TreeTime's time grid of the interpolated
+ * expQt and, when `approximate`, the exact matrices at its points (tt_ss_pstack). */
+typedef struct tt_ss_model {
+    int32_t n_states;
+    int32_t n_grid;
+    int32_t approximate;       /* TreeTime's GTR_site_specific.approximate                          */
+    int32_t reserved;
+    double rate_scale;         /* t * rate_scale >= 10: exact P(t) (gtr_site_specific.py:367-371)   */
+    const double* lam;         /* [n_sites][q]                                                     */
+    const double* V;           /* [n_sites][q][q]                                                  */
+    const double* Vinv;        /* [n_sites][q][q]                                                  */
+    const double* mu;          /* [n_sites]                                                        */
+    const double* pi;          /* [n_sites][q]                                                     */
+    const double* lut;         /* [256][q] profile row of each character byte                     */
+    const double* grid;        /* [n_grid] time grid (may be NULL when !approximate)              */
+    const double* stack;       /* [n_grid][q][q][n_sites] P at the grid points, or NULL            */
+} tt_ss_model;
+
+/* The exact P_a(t_g) of every grid point g and site a into stack[n_grid][q][q][n_sites] (FP64):
+ * the matrices TreeTime's interpolator is built from (treetime/gtr_site_specific.py:331-348). */
+tt_status tt_ss_pstack(const tt_ss_model* m, int32_t n_sites, double* stack, void* stream);
+
+/* Joint reconstruction under a site-specific model, for a forest of one tree (TreeAnc._ml_anc_joint,
+ * treetime/treeanc.py:934-1080, with GTR_site_specific.expQt, treetime/gtr_site_specific.py:331-371):
+ * per node and site log(max(1e-12, P_a(t))) in FP64 (interpolated on the grid as TreeTime does,
+ * from `stack`, or exact), max-plus with first-index argmax, root with log(pi_a), backtrack.  One
+ * launch per height level: level_off_host[0..n_levels] are the tree's level offsets (host copy of
+ * tt_forest.level_off).  out->msg must hold n_int * n_patterns rows of width doubles (the FP64
+ * joint_Lx; out->rows counts them) and out->cx as many rows of width bytes. */
+tt_status tt_joint_ss(const tt_forest* f, const tt_ss_model* m, const int32_t* level_off_host, int32_t n_levels,
+                      int32_t n_int, int32_t n_tip, const tt_joint_out* out, int32_t* status, void* stream);
 
 /* Joint reconstruction that allocates nothing.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (hosts that only hand out their own pre-sized
  * buffers, pools that reserve all device memory at start-up, paths that cannot afford an
  * allocation's synchronisation).  Same results as tt_branch_pmats + tt_joint; the branch matrices
- * and the joint_Lx / joint_Cx scratch live in one fixed device array of
+ * and the msg / joint_Cx scratch live in one fixed device array of
  * TT_JOINT_NOALLOC_SCRATCH_BYTES inside the library (held by every GPU that loads it).
  * `internal_rows` = sum over trees of n_int * n_patterns.  Problems needing more scratch than
- * 2*align256(n_nodes*q*width*8) + align256(internal_rows*width*8) + align256(internal_rows*width)
- * <= TT_JOINT_NOALLOC_SCRATCH_BYTES are rejected with TT_ERR_OOM.  The first call on each device
- * looks the array's device address up (cudaGetSymbolAddress) and should come before any stream
- * capture; calls share the array, so calls that overlap on the GPU race and must be serialised. */
+ * align256(n_nodes*q*width*8) + align256(n_nodes*q*width*8) + align256(n_nodes*q*width*16)
+ * + align256(internal_rows*width*8) + align256(internal_rows*width)
+ * <= TT_JOINT_NOALLOC_SCRATCH_BYTES are rejected with TT_ERR_OOM, and the kernel checks every
+ * tree's rows against the rows the scratch holds (a tree beyond them is skipped with
+ * *status = TT_ERR_OOM), whatever `internal_rows` says.  The first call on each device looks the
+ * array's device address up (cudaGetSymbolAddress) and keeps it for the life of the process (it
+ * does not survive a cudaDeviceReset); that first call should come before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU race and must be serialised. */
 #define TT_JOINT_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 tt_status tt_joint_noalloc(const tt_forest* f, const tt_model* m, int64_t internal_rows, uint8_t* states,
                            double* site_lh, double* tree_lh, unsigned long long* n_diff, const double* root_uniform,

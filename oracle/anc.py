@@ -99,8 +99,7 @@ def expQt(model, t):
         if t * model.rate_scale < 10 and model.approximate:
             from scipy.interpolate import interp1d
             grid = model.t_grid
-            stack = np.stack([_site_expQt_exact(model, tk) for tk in grid], axis=0)
-            return interp1d(grid, stack, axis=0, assume_sorted=True, copy=False, kind="linear")(t)
+            return interp1d(grid, _site_stack(model), axis=0, assume_sorted=True, copy=False, kind="linear")(t)
         return _site_expQt_exact(model, t)
     log_val = model.mu * t * model.eigenvals
     if any(i > 10 for i in log_val):
@@ -117,6 +116,21 @@ def expQt_expm1(model, t):
     set by the rounding of V diag(exp) V^-1 (exactly 0 at t = 0)."""
     em1 = np.expm1(model.mu * t * model.eigenvals)
     return np.maximum(0, np.eye(len(em1)) + model.v.dot(np.diag(em1).dot(model.v_inv)))
+
+
+def _site_stack(model):
+    """The exact per-site matrices at the grid points that TreeTime's
+    interpolator is built from (gtr_site_specific.py:331-348), computed once
+    per model object (TreeTime builds its interpolator once too)."""
+    key = (id(model.v), id(model.v_inv), id(model.eigenvals), id(model.mu), id(model.t_grid))
+    hit = getattr(model, "_oracle_stack", None)
+    if hit is None or hit[0] != key:
+        hit = (key, np.stack([_site_expQt_exact(model, tk) for tk in model.t_grid], axis=0))
+        try:
+            model._oracle_stack = hit
+        except AttributeError:
+            pass
+    return hit[1]
 
 
 def _site_expQt_exact(model, t):

@@ -122,8 +122,6 @@ def _joint_margin_mask(g, model, tree_prepared):
 @pytest.mark.parametrize("case", CASES)
 def test_joint_matches_treetime(case):
     g = gc.load(case)
-    if str(g["kind"]) != "gtr":
-        pytest.skip("joint reconstruction is defined for single-matrix models")
     t = _tree_anc(g, "f64")
     sample = "root" if bool(g["sample_root"]) else False
     ndiff = t.infer_ancestral_sequences(marginal=False, reconstruct_tip_states=bool(g["reconstruct_tip_states"]),

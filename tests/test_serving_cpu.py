@@ -32,8 +32,9 @@ def test_head_of_queue_blocks_smaller_later_jobs():
 
 def test_footprint_grows_with_size_and_kind():
     from treetime_gb300 import engine, synth
-    (a, b), _ = synth.forest_c3(n_trees=2, seed=1, n_range=(20, 200), L_range=(100, 1000))
-    small, big = sorted((a, b), key=lambda ti: ti.layout.n_nodes * ti.n_patterns)
+    (small,), _ = synth.forest_c3(n_trees=1, seed=1, n_range=(20, 21), L_range=(100, 101))
+    (big,), _ = synth.forest_c3(n_trees=1, seed=1, n_range=(400, 401), L_range=(2000, 2001))
+    assert small.layout.n_nodes * small.n_patterns < big.layout.n_nodes * big.n_patterns
     assert footprint(small, 4, "marginal") < footprint(big, 4, "marginal")
     assert footprint(big, 4, "marginal") < footprint(big, 4, "optimize")
     rows = big.layout.n_int * big.n_patterns * 4 * 4

@@ -43,16 +43,22 @@ class TTForest(C.Structure):
 
 class TTModel(C.Structure):
     _fields_ = [("n_models", i32), ("n_states", i32), ("V", vp), ("Vinv", vp), ("lam", vp), ("mu", vp),
-                ("pi", vp), ("lut", vp)]
+                ("pi", vp), ("lut", vp), ("lut_log2", vp)]
 
 
 class TTPmats(C.Structure):
-    _fields_ = [("p64", vp), ("p32", vp), ("logp64", vp), ("p32_pair", vp)]
+    _fields_ = [("p64", vp), ("p32", vp), ("logp64", vp), ("p32_pair", vp), ("logp2", vp), ("logp2_pair", vp)]
 
 
 class TTSSF32(C.Structure):
     _fields_ = [("n_sites", i32), ("n_grid", i32), ("V", vp), ("Vinv", vp), ("mulam", vp), ("pi", vp),
                 ("em1_grid", vp), ("grid", vp), ("lut", vp), ("rate_scale", C.c_double)]
+
+
+class TTSSModel(C.Structure):
+    _fields_ = [("n_states", i32), ("n_grid", i32), ("approximate", i32), ("reserved", i32),
+                ("rate_scale", C.c_double), ("lam", vp), ("V", vp), ("Vinv", vp), ("mu", vp), ("pi", vp),
+                ("lut", vp), ("grid", vp), ("stack", vp)]
 
 
 class TTMarginalOut(C.Structure):
@@ -62,8 +68,8 @@ class TTMarginalOut(C.Structure):
 
 
 class TTJointOut(C.Structure):
-    _fields_ = [("lx", vp), ("cx", vp), ("states", vp), ("site_lh", vp), ("tree_lh", vp), ("n_diff", vp),
-                ("root_uniform", vp), ("reconstruct_tips", i32), ("count_diff", i32)]
+    _fields_ = [("msg", vp), ("cx", vp), ("states", vp), ("site_lh", vp), ("tree_lh", vp), ("n_diff", vp),
+                ("root_uniform", vp), ("reconstruct_tips", i32), ("count_diff", i32), ("rows", C.c_int64)]
 
 
 P = C.POINTER
@@ -79,6 +85,8 @@ _SIGS = {
     "tt_marginal_ss_f32": (i32, [P(TTForest), P(TTSSF32), vp, i32, P(TTMarginalOut), vp, vp]),
     "tt_joint": (i32, [P(TTForest), P(TTModel), P(TTPmats), P(TTJointOut), vp, vp]),
     "tt_joint_noalloc": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, vp, vp]),
+    "tt_ss_pstack": (i32, [P(TTSSModel), i32, vp, vp]),
+    "tt_joint_ss": (i32, [P(TTForest), P(TTSSModel), vp, i32, i32, i32, P(TTJointOut), vp, vp]),
     "tt_state_pairs": (i32, [P(TTForest), vp, vp, i32, i32, i32, vp, vp, vp]),
     "tt_optimal_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), f64, vp, vp, vp]),
     "tt_prob_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), vp, vp, vp]),

@@ -22,6 +22,8 @@ other clade objects (Bio.Phylo) receive them as attributes right away.
 """
 
 import ctypes as C
+import itertools
+import operator
 
 import numpy as np
 
@@ -32,14 +34,42 @@ from .errors import MissingDataError
 from .tree import LAZY_ATTRS, Clade
 
 
-def _count_clades(root):
-    """Number of clades below and including `root` (one iterative walk)."""
-    n, stack = 0, [root]
-    while stack:
-        c = stack.pop()
-        n += 1
-        stack.extend(c.clades)
-    return n
+def _children_ids(nodes):
+    """Identity of every child of every node, in order (C-level iteration):
+    equal lists mean an unchanged topology below the same root."""
+    return list(map(id, itertools.chain.from_iterable(map(_CLADES, nodes))))
+
+
+def _mask_ids(nodes):
+    return list(map(id, map(getattr, nodes, itertools.repeat("mask"), itertools.repeat(None))))
+
+
+_CLADES = operator.attrgetter("clades")
+
+
+class ResultHolder:
+    """The results a session's clades show (their ``_anc_src``): installing a
+    reconstruction replaces the holder's source, one assignment for the whole
+    tree.  Values assigned to a clade's result attributes (tree._Result)
+    override the source until the next installation."""
+
+    def __init__(self):
+        self.src = None
+        self._overridden = []
+
+    def fetch(self, name, node):
+        return None if self.src is None else self.src.fetch(name, node)
+
+    def overridden(self, node):
+        self._overridden.append(node)
+
+    def install(self, src):
+        for n in self._overridden:
+            ov = n.__dict__.get("_anc_override")
+            if ov:
+                ov.clear()
+        self._overridden.clear()
+        self.src = src
 
 
 def pair_counts(seq_p, seq_ch, mult, q, gap_index, ignore_gaps):
@@ -55,6 +85,25 @@ def pair_counts(seq_p, seq_ch, mult, q, gap_index, ignore_gaps):
     return np.bincount(a * q + b, weights=w, minlength=q * q).reshape(q, q)
 
 
+_PINNED = {}
+
+
+def _pinned_copy(t):
+    """Host copy of a device tensor through a reused page-locked buffer (one
+    asynchronous copy on the current stream, then a wait for it); the array
+    returned is the caller's own."""
+    torch = engine.torch()
+    n = t.numel() * t.element_size()
+    buf = _PINNED.get(t.dtype)
+    if buf is None or buf.numel() * buf.element_size() < n:
+        buf = torch.empty(max(n // t.element_size(), 1), dtype=t.dtype, pin_memory=True)
+        _PINNED[t.dtype] = buf
+    view = buf[:t.numel()]
+    view.copy_(t.reshape(-1), non_blocking=True)
+    torch.cuda.current_stream(t.device).synchronize()
+    return view.numpy().copy()
+
+
 class ResultStore:
     """Host view of one reconstruction's device results; node attributes are
     built from it on first access."""
@@ -68,9 +117,11 @@ class ResultStore:
         self.reconstruct_tips = reconstruct_tips
         self.P = tt.data.compressed_length
         self.q = tt.gtr.n_states
-        n = layout.n_nodes
-        self.states = out["states"].view(-1)[: n * self.P].cpu().numpy().reshape(n, self.P)
+        # the reconstructed rows: internal nodes, and the tips when their states were reconstructed
+        rows = layout.n_nodes if reconstruct_tips else layout.n_int
+        self.states = _pinned_copy(out["states"].view(-1)[: rows * self.P]).reshape(rows, self.P)
         self._host = {}
+        self._cache = {}
 
     def _fetch_buf(self, key):
         if key not in self._host:
@@ -85,6 +136,15 @@ class ResultStore:
         return buf[j * self.P:(j + 1) * self.P, :self.q].astype(np.float64)
 
     def fetch(self, name, node):
+        key = (name, id(node))
+        hit = self._cache.get(key)
+        if hit is None:
+            hit = self._fetch(name, node)
+            if hit is not None:
+                self._cache[key] = hit
+        return hit
+
+    def _fetch(self, name, node):
         L = self.layout
         k = L.local.get(id(node))
         if k is None:
@@ -167,24 +227,20 @@ class GPUAncMixin:
             self._aln_index_cache = cache
         return cache[1], cache[2]
 
-    def _masks_changed(self, sess):
-        cur = {k: id(getattr(n, "mask", None)) for k, n in enumerate(sess["layout"].nodes)
-               if getattr(n, "mask", None) is not None}
-        return cur != sess["mask_ids"]
-
     def _get_session(self):
         """Device-resident schedule and inputs of the current tree, rebuilt when
-        the topology, alignment, model or masks change; branch lengths are
-        refreshed on every call."""
+        the topology (any node's list of children), alignment, model or masks
+        change; branch lengths are refreshed on every call.  The checks are
+        C-level iterations over the session's nodes."""
         s = getattr(self, "_session", None)
         gtr_key = engine.model_key(self.gtr)
-        if s is not None and s["root"] is self.tree.root and s["data"] is self.data and s["gtr_key"] == gtr_key \
-                and s["n_nodes"] == _count_clades(self.tree.root) \
-                and not self._masks_changed(s):
-            bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
-            engine.check_exp(self.gtr, bl)
-            s["forest"].set_branch_lengths([bl])
-            return s
+        if s is not None and s["root"] is self.tree.root and s["data"] is self.data and s["gtr_key"] == gtr_key:
+            nodes = s["layout"].nodes
+            if _children_ids(nodes) == s["children_ids"] and _mask_ids(nodes) == s["mask_id_list"]:
+                bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
+                engine.check_exp(self.gtr, bl)
+                s["forest"].set_branch_lengths([bl])
+                return s
         engine.check_alphabet(self.gtr.n_states, self.gtr.is_site_specific)
         device = getattr(self, "device", None)
         layout = engine.TreeLayout(self.tree.root)
@@ -209,8 +265,22 @@ class GPUAncMixin:
                                ctas_per_sm=getattr(self, "ctas_per_sm", None) or 1,
                                range_patterns=getattr(self, "range_patterns", None))
         model = None if self.gtr.is_site_specific else engine.model_for(self.gtr, device)
+        holder = ResultHolder()
+        foreign = []
+        rm = LAZY_ATTRS + ("_anc_src", "_anc_override", "joint_Lx", "joint_Cx", "seq_idx", "marginal_log_Lx",
+                           "marginal_subtree_LH_prefactor")
+        for n in layout.nodes:
+            d = n.__dict__
+            for a in rm:
+                d.pop(a, None)
+            if isinstance(n, Clade):
+                d["_anc_src"] = holder
+            else:
+                foreign.append(n)
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
-                 root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes)
+                 root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes,
+                 children_ids=_children_ids(layout.nodes), mask_id_list=_mask_ids(layout.nodes), holder=holder,
+                 foreign=foreign)
         self._session = s
         return s
 
@@ -246,22 +316,24 @@ class GPUAncMixin:
         states[layout.n_int * P:].copy_(engine.torch().from_numpy(tip.reshape(-1)))
 
     def _clear_results(self, layout):
-        rm = frozenset(LAZY_ATTRS + ("_anc_src", "joint_Lx", "joint_Cx", "seq_idx", "marginal_log_Lx",
-                                     "marginal_subtree_LH_prefactor"))
-        for n in layout.nodes:
+        """Results of an earlier reconstruction leave with the next one: the
+        session's clades ask its result holder (replaced by _install); other
+        clade objects carry plain attributes, removed here."""
+        sess = self._session
+        rm = LAZY_ATTRS + ("joint_Lx", "joint_Cx", "seq_idx", "marginal_log_Lx", "marginal_subtree_LH_prefactor")
+        for n in sess["foreign"]:
             d = n.__dict__
-            for a in rm.intersection(d):
-                del d[a]
+            for a in rm:
+                d.pop(a, None)
 
     def _install(self, src, layout):
-        for n in layout.nodes:
-            if isinstance(n, Clade):
-                n.__dict__["_anc_src"] = src
-            else:  # foreign clade objects: materialise eagerly
-                for a in LAZY_ATTRS:
-                    v = src.fetch(a, n)
-                    if v is not None:
-                        setattr(n, a, v)
+        sess = self._session
+        sess["holder"].install(src)
+        for n in sess["foreign"]:  # foreign clade objects: materialise eagerly
+            for a in LAZY_ATTRS:
+                v = src.fetch(a, n)
+                if v is not None:
+                    setattr(n, a, v)
 
     def _root_draws(self, sample_from_profile):
         """The root's uniform draws (sample_from_profile 'root' or True), one
@@ -318,8 +390,6 @@ class GPUAncMixin:
 
     def _ml_anc_joint(self, sample_from_profile=False, reconstruct_tip_states=False, debug=False, **kwargs):
         """Joint reconstruction in one device pass (treetime/treeanc.py:934-1080)."""
-        if self.gtr.is_site_specific:
-            raise NotImplementedError("joint reconstruction with site-specific models is not supported")
         self.logger("TreeAnc._ml_anc_joint: type of reconstruction: Joint (GPU)", 2)
         sess = self._get_session()
         layout = sess["layout"]
@@ -327,8 +397,13 @@ class GPUAncMixin:
         if reconstruct_tip_states and count_diff and not self.reconstructed_tip_sequences:
             self._seed_tip_states(sess)
         draws = self._root_draws(sample_from_profile)
-        out = engine.joint(sess["forest"], sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
-                           count_diff=count_diff, root_uniform=draws)
+        if self.gtr.is_site_specific:
+            out = engine.joint_site_specific(sess["forest"], self.gtr, sess["bufs"],
+                                             reconstruct_tips=reconstruct_tip_states, count_diff=count_diff,
+                                             root_uniform=draws)
+        else:
+            out = engine.joint(sess["forest"], sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
+                               count_diff=count_diff, root_uniform=draws)
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
@@ -465,15 +540,13 @@ class GPUAncMixin:
             node.mutation_length = new_len
             max_bl = max(max_bl, new_len)
         bstore = BranchStateStore(layout, counts.cpu().numpy())
-        for n in layout.nodes:
-            if isinstance(n, Clade):
-                n.__dict__.pop("branch_state", None)
-                prev = n.__dict__.get("_anc_src")
-                n.__dict__["_anc_src"] = _ChainedSource(prev, bstore) if prev is not None else bstore
-            else:
-                v = bstore.fetch("branch_state", n)
-                if v is not None:
-                    n.branch_state = v
+        holder = sess.get("holder")
+        if holder is not None:
+            holder.install(_ChainedSource(holder.src, bstore) if holder.src is not None else bstore)
+        for n in (sess.get("foreign", ()) if holder is not None else layout.nodes):
+            v = bstore.fetch("branch_state", n)
+            if v is not None:
+                n.branch_state = v
         if max_bl > 0.15:
             self.logger("TreeAnc.optimize_branch_lengths_joint: THIS TREE HAS LONG BRANCHES."
                         " \n\t ****TreeTime's JOINT IS NOT DESIGNED TO OPTIMIZE LONG BRANCHES."

@@ -2,12 +2,12 @@
 //
 // Same algorithm as the FP64 kernel (tt_marginal_kernels.cuh): a CTA walks a whole tree level by
 // level for a set of patterns, post-order then pre-order.  What differs:
-//   - arithmetic is FP32 in the linear domain: child messages x.P are multiplied and a node's
-//     partial is rescaled by an exact power of two only when its largest entry falls below
-//     2^-16 (messages never exceed the largest entry of the child's partial, so partials stay in
-//     (2^-16 * tiny message, 1]); the exponents are summed per pattern in registers and the only
-//     FP64 operation is the root's log, once per pattern.  Power-of-two scaling is exact, so when
-//     and how often it happens does not change any result;
+//   - arithmetic is FP32 in the linear domain with the branch matrices as D = P(t) - I: a child's
+//     message is x + x.D, and a node's partial is kept in the reference-state form of
+//     tt_marginal_f32.cuh (largest entry exactly 1; the dropped factor's log, formed from the
+//     small D entries without rounding 1 + d, summed per pattern in a compensated FP32
+//     accumulator, power-of-two exponents as integers).  The only FP64 operations are the root's
+//     log and the final sum, once per pattern;
 //   - one CTA per pattern range of any width: the host cuts the forest's patterns into about one
 //     range per SM and the CTA's threads form node groups of (range width x lanes per pattern)
 //     threads, so every SM has work whatever the pattern count;
@@ -40,6 +40,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     __shared__ __align__(16) float lut_s[256 * W];
     __shared__ int red[NT];
     __shared__ float red_corr[NT];
+    __shared__ float red_ph[NT];
+    __shared__ float red_pl[NT];
     __shared__ unsigned diff_red[NT / 32];
     __shared__ int lev_s[kLevCap];
     extern __shared__ __align__(16) unsigned char dyn_s[];  // two stage buffers
@@ -83,11 +85,12 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
             for (int i = tid; i <= nlev; i += NT) lev_s[i] = __ldg(lev + i);
         __syncthreads();
         auto LV = [&](int i) -> int { return lev_sm ? lev_s[i] : __ldg(lev + i); };
+        // per pattern, the dropped factors of this thread's nodes: their product (double-float
+        // ph + pl) and power-of-two exponents (esum); the mask corrections' logs (compensated sum)
         int esum = 0;
-        // log-LH correction for masked internal children: TreeTime masks the log message of the
-        // child's sum-normalised partial and adds its prefactor unmasked; with power-of-two scaled
-        // partials that leaves (1 - m) * log(sum of the scaled partial) to add
-        float lcorr = 0.f;
+        float prh = 1.f, prl = 0.f;
+        float lsum = 0.f, lcomp = 0.f;
+        bool dead = false;  // some node's partial was zero at every state
 
         // row k of this thread's pattern: base + k * (P * W) floats
         const int PW = P * W;
@@ -105,22 +108,23 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                 for (int s = 0; s < S; ++s) x[s] = lut_s[code * W + j0 + s];
             }
         };
-        // mask of the branch above node c applied to its message; correction for internal c
-        auto apply_mask = [&](int c, const float (&x)[S], float (&msg)[S]) {
+        // mask value of the branch above node c (1 without a mask).  TreeTime masks the log message
+        // of the child's sum-normalised partial and adds its prefactor unmasked; with partials
+        // scaled to a largest entry of 1 that leaves (1 - m) * log(sum of the stored partial) to add
+        // for an internal child.  The node (and so the mask offset) is the same for every lane of
+        // a warp when LPP > 1, so the shuffles of group_sum see whole warps.
+        auto mask_of = [&](int c, const float (&x)[S]) -> float {
             const int64_t mo = __ldg(a.f.mask_off + nb + c);
-            if (mo < 0) return;
+            if (mo < 0) return 1.f;
             const float m = (float)__ldg(a.f.masks + mo + pc);
-            // padding states (j >= Q) stay 0 so that products over children keep them 0
-#pragma unroll
-            for (int s = 0; s < S; ++s)
-                if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : (m == 1.f ? msg[s] : exp2f(m * log2f(msg[s])));
             if (c < n_int) {
                 float xs = 0.f;
 #pragma unroll
                 for (int s = 0; s < S; ++s) xs += x[s];
                 xs = group_sum<LPP>(xs);
-                if (m != 1.f) lcorr += (1.f - m) * logf(xs);
+                if (m != 1.f) kahan_add(lsum, lcomp, (1.f - m) * logf(xs));
             }
+            return m;
         };
         // stage the chunk [base, base + cnt) of a level into buffer b
         auto stage = [&](int b, int base, int cnt, bool post) {
@@ -205,54 +209,37 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         const int i = i0 + d * G;
                         if (i >= s1) continue;
                         const int k = base + i;
-                        float r[S];
+                        RefAcc<S> A;
+                        A.template reset<Q>();
                         if (bin[d]) {
                             if (ca[d] >= 0) lut_part(ca[d], xa[d]);
                             if (cb[d] >= 0) lut_part(cb[d], xb[d]);
-                            float m0[S], m1[S];
-                            s_vec_mat<Q, W, LPP>(xa[d], &st.mat[i][0], j0, m0);
-                            s_vec_mat<Q, W, LPP>(xb[d], &st.mat[i][QW], j0, m1);
+                            float d0[S], d1[S];
+                            s_vec_mat<Q, W, LPP>(xa[d], &st.mat[i][0], j0, d0);
+                            s_vec_mat<Q, W, LPP>(xb[d], &st.mat[i][QW], j0, d1);
+                            float m0 = 1.f, m1 = 1.f;
                             if (has_masks) {
                                 const int4 cp = st.pair[i];
-                                apply_mask(cp.x, xa[d], m0);
-                                apply_mask(cp.z, xb[d], m1);
+                                m0 = mask_of(cp.x, xa[d]);
+                                m1 = mask_of(cp.z, xb[d]);
                             }
-#pragma unroll
-                            for (int s = 0; s < S; ++s) r[s] = m0[s] * m1[s];
+                            ref_add<Q, W, LPP>(A, xa[d], d0, m0, j0, esum);
+                            ref_add<Q, W, LPP>(A, xb[d], d1, m1, j0, esum);
                         } else {
                             // more (or fewer) than two children: matrices from global memory
                             const int4 rec = st.rec[i];
-#pragma unroll
-                            for (int s = 0; s < S; ++s) r[s] = (j0 + s < Q) ? 1.f : 0.f;
                             for (int ci = rec.x; ci < rec.y; ++ci) {
                                 const int c = __ldg(a.f.child_idx + ci);
-                                float x[S], m0[S];
+                                float x[S], dx[S];
                                 if (c >= n_int) lut_part(tip_code(__ldg(a.f.tip_row + nb + c)), x);
                                 else ld_part<S>(part0 + (int64_t)c * PW, x);
-                                f_vec_mat<Q, W, LPP>(x, pm + (nb + c) * QW, j0, m0);
-                                if (has_masks) apply_mask(c, x, m0);
-#pragma unroll
-                                for (int s = 0; s < S; ++s) r[s] *= m0[s];
-                                float mx = r[0];
-#pragma unroll
-                                for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
-                                mx = group_max<LPP>(mx);
-                                if (mx < kRescaleBelow) {  // many children: keep the running product in range
-                                    const int e = pow2_exponent(mx);
-                                    scale_pow2<S>(r, e);
-                                    esum += e;
-                                }
+                                f_vec_mat<Q, W, LPP>(x, pm + (nb + c) * QW, j0, dx);
+                                const float mv = has_masks ? mask_of(c, x) : 1.f;
+                                ref_add<Q, W, LPP>(A, x, dx, mv, j0, esum);
                             }
                         }
-                        float mx = r[0];
-#pragma unroll
-                        for (int s = 1; s < S; ++s) mx = fmaxf(mx, r[s]);
-                        mx = group_max<LPP>(mx);
-                        if (mx < kRescaleBelow) {
-                            const int e = pow2_exponent(mx);
-                            scale_pow2<S>(r, e);
-                            esum += e;
-                        }
+                        float r[S];
+                        if (!ref_finish<Q, W, LPP>(A, r, prh, prl, esum, j0)) dead = true;
                         if (valid) st_part<S>(part0 + (int64_t)k * PW, r);
                     }
                 }
@@ -267,7 +254,9 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         }
         // per-pattern exponent sums: lanes of one pattern hold identical values; groups add up
         red[tid] = esum;
-        red_corr[tid] = lcorr;
+        red_corr[tid] = dead ? -INFINITY : lsum - lcomp;
+        red_ph[tid] = prh;
+        red_pl[tid] = prl;
         __syncthreads();  // also: every thread is done with the post-order stage buffers
 
         // pre-order levels n_levels-2 .. 0, then the tips as level -1; the first chunk's copies
@@ -316,24 +305,34 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
 
         // ------------------------------------------------------------------ root
         if (tid < GP) {  // group 0 (whole warps when LPP > 1)
+            // the pattern's dropped factors over all node groups: product, exponents, corrections
             int tot = 0;
             double corr = 0.0;
+            float fh = 1.f, fl = 0.f;
             for (int gg = 0; gg < G; ++gg) {
                 tot += red[gg * GP + tid];
                 corr += (double)red_corr[gg * GP + tid];
+                df_mul(fh, fl, red_ph[gg * GP + tid], red_pl[gg * GP + tid]);
+                df_renorm(fh, fl, tot);
             }
             const int kr = n_int - 1;
             const double* pi = a.pi + (int64_t)tr.model * Q;
             float x[S], pr[S];
             ld_part<S>(part0 + (int64_t)kr * PW, x);
             float s_loc = 0.f;
+            double d_loc = 0.0;
 #pragma unroll
             for (int s = 0; s < S; ++s) {
-                pr[s] = (j0 + s < Q) ? (float)__ldg(pi + j0 + s) * x[s] : 0.f;
+                const double pj = (j0 + s < Q) ? __ldg(pi + j0 + s) : 0.0;
+                pr[s] = (float)pj * x[s];
                 s_loc += pr[s];
+                d_loc += pj * (double)x[s];
             }
             const float ssum = group_sum<LPP>(s_loc);
-            const float inv = 1.f / ssum;
+            double dsum = d_loc;
+#pragma unroll
+            for (int o = LPP / 2; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+            const float inv = __frcp_rn(ssum);
 #pragma unroll
             for (int s = 0; s < S; ++s) pr[s] *= inv;
             int st;
@@ -350,7 +349,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
             if (valid) {
                 st_part<S>(post0 + (int64_t)kr * PW, pr);
                 if (part == 0) {
-                    a.o.site_lh[tr.pat_base + p] = log((double)ssum) + kLn2 * (double)tot + corr;
+                    a.o.site_lh[tr.pat_base + p] = log(dsum * ((double)fh + (double)fl)) + kLn2 * (double)tot + corr;
                     states0[(int64_t)kr * P] = (uint8_t)st;
                 }
                 if (a.o.outgroup) {
@@ -402,9 +401,11 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         if (i >= s1) continue;
                         const int k = base + i;
                         if (tips) lut_part(code[d], x[d]);
-                        const float* Pk = &st.mat[i][0];
+                        const float* Pk = &st.mat[i][0];  // D = P - I of the branch above k
                         float msg[S], o[S];
                         s_vec_mat<Q, W, LPP>(x[d], Pk, j0, msg);
+#pragma unroll
+                        for (int s = 0; s < S; ++s) msg[s] += x[d][s];
                         float m = 1.f;
                         if (has_masks) {
                             const int64_t mo = __ldg(a.f.mask_off + nb + k);
@@ -439,6 +440,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         float ev[S];
                         s_mat_vec<Q, W, LPP>(Pk, o, j0, ev);
                         float s2 = 0.f;
+#pragma unroll
+                        for (int s = 0; s < S; ++s) ev[s] += o[s];
 #pragma unroll
                         for (int s = 0; s < S; ++s) {
                             if (m != 1.f && j0 + s < Q) ev[s] = m * ev[s] + (1.f - m);

@@ -120,6 +120,226 @@ __device__ __forceinline__ void f_mat_vec(const float* __restrict__ P, const flo
     }
 }
 
+// Lowest state j of the pattern with x_j == v across its LPP lanes (Q when there is none).  Every
+// lane of the warp must call it (shuffles).
+template <int Q, int W, int LPP>
+__device__ __forceinline__ int group_first_eq(const float (&x)[W / LPP], float v, int j0) {
+    constexpr int S = W / LPP;
+    int a = Q;
+#pragma unroll
+    for (int s = S - 1; s >= 0; --s)
+        if (j0 + s < Q && x[s] == v) a = j0 + s;
+#pragma unroll
+    for (int o = LPP / 2; o > 0; o >>= 1) a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+    return a;
+}
+
+// v_a of the pattern, from whichever of its lanes holds state a (0 when a >= Q).  Every lane of
+// the warp must call it (shuffles).
+template <int Q, int W, int LPP>
+__device__ __forceinline__ float group_pick(const float (&v)[W / LPP], int a, int j0) {
+    constexpr int S = W / LPP;
+    float r = 0.f;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+        if (j0 + s == a) r = v[s];
+    if constexpr (LPP > 1) r = __shfl_sync(0xffffffffu, r, (a / S) % LPP, LPP);
+    return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// Reference-state form of a node's partial (post-order of the FP32 kernel).
+//
+// A stored partial row has its largest entry exactly 1 at some state a (its reference state)
+// and every other entry <= 1; the factor dropped by that scaling goes into the pattern's
+// log-likelihood.  A child's message is m = x + x.D with D = P(t) - I, so at the reference state
+// m_a = 1 + d with d = (x.D)_a a small number that FP32 holds to its relative precision.  When
+// every child of a node has the same reference state a (x_a == 1), the node's partial is
+// (prod_c m_c) / prod_c (1 + d_c): the entry at a is exactly 1, the others are products of
+// messages divided by one FP32 number, and the dropped factor prod_c (1 + d_c) = 1 + dl (dl formed
+// from the d_c without ever rounding 1 + d) multiplies the pattern's running product of dropped
+// factors, a double-float (an FP32 pair, ~48 significant bits) updated as p + p*dl.  For a short
+// branch that is what keeps the per-node rounding out of the likelihood: with x.P in FP32, every
+// node's dominant entry 1 - O(t) carries a rounding of about 3e-8 that accumulates over the
+// nodes of a pattern (FP32 log-likelihoods of 5,000-tip trees with branches of 1e-4 were off by
+// 5e-6 relative; in this form by about 4e-9).  Nodes where the children disagree on a reference
+// state, where a message entry outgrows the reference entry, or where a mask scales a message
+// take the general form: the plain FP32 product, scaled by the exact power of two and the
+// mantissa of its largest entry (the mantissa, in [0.5, 1), multiplies the running product; the
+// exponent is summed as an integer).  The pattern's log-likelihood takes one FP64 log, at the root.
+// General-form products of many children are rescaled (by an exact power of two) below this
+// largest entry.
+constexpr float kRescaleBelowRef = 0x1p-64f;
+
+template <int S>
+struct RefAcc {
+    float y[S];   // product of the children's messages (the reference entry is not kept in y)
+    float dl;     // prod_c (1 + d_c) - 1 at the reference state (reference form)
+    int a;        // reference state
+    int mode;     // 0: no child yet, 1: reference form, 2: general form
+    template <int Q>
+    __device__ __forceinline__ void reset() {
+        dl = 0.f;
+        a = Q;
+        mode = 0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) y[s] = 0.f;
+    }
+};
+
+// Add child x (its row; tips: the 0/1 profile of the character) with xd = x.D and mask value mv
+// (1 without a mask; 0 drops the message, a message of ones).  Every lane of the warp must call
+// it: the pattern's lanes exchange values (shuffles) whatever the branch taken.
+template <int Q, int W, int LPP>
+__device__ __forceinline__ void ref_add(RefAcc<W / LPP>& A, const float (&x)[W / LPP], const float (&xd)[W / LPP],
+                                        float mv, int j0, int& esum) {
+    constexpr int S = W / LPP;
+    const int ax = group_first_eq<Q, W, LPP>(x, 1.f, j0);
+    const int aref = A.mode == 1 ? A.a : ax;
+    const float x_at = group_pick<Q, W, LPP>(x, aref, j0);
+    const float d_at = group_pick<Q, W, LPP>(xd, aref, j0);
+    float m[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        m[s] = (j0 + s < Q) ? x[s] + xd[s] : 0.f;
+        if (mv != 1.f && j0 + s < Q) m[s] = mv == 0.f ? 1.f : exp2f(mv * log2f(m[s]));
+    }
+    if (mv != 0.f) {
+        if (A.mode == 0) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) A.y[s] = m[s];
+            if (mv == 1.f && ax < Q) {
+                A.mode = 1;
+                A.a = ax;
+                A.dl = d_at;
+            } else {
+                A.mode = 2;
+            }
+        } else if (A.mode == 1 && mv == 1.f && x_at == 1.f) {
+            A.dl = fmaf(A.dl, d_at, A.dl + d_at);
+#pragma unroll
+            for (int s = 0; s < S; ++s) A.y[s] *= m[s];
+        } else {
+            if (A.mode == 1) {  // leave the reference form: restore the product's reference entry
+#pragma unroll
+                for (int s = 0; s < S; ++s)
+                    if (j0 + s == A.a) A.y[s] = 1.f + A.dl;
+                A.mode = 2;
+            }
+#pragma unroll
+            for (int s = 0; s < S; ++s) A.y[s] *= m[s];
+        }
+    }
+    // keep a long general-form product (a polytomy's) in range
+    float mx = 0.f;
+#pragma unroll
+    for (int s = 0; s < S; ++s) mx = fmaxf(mx, A.y[s]);
+    mx = group_max<LPP>(mx);
+    if (A.mode == 2 && mx < kRescaleBelowRef && mx > 0.f) {
+        const int e = pow2_exponent(mx);
+        scale_pow2<S>(A.y, e);
+        esum += e;
+    }
+}
+
+// Double-float helpers of the running product of dropped factors (h + l, |l| <= ulp(h) / 2).
+// (h, l) *= 1 + d for -1 <= d <= 0 (|h d| <= |h|, so the sum h + h d is a Fast2Sum)
+__device__ __forceinline__ void df_mul_1p(float& h, float& l, float d) {
+    const float t = h * d;
+    const float te = fmaf(h, d, -t);
+    const float s = h + t;
+    const float lo = ((h - s) + t) + te + fmaf(l, d, l);
+    h = s + lo;
+    l = lo - (h - s);
+}
+// (h, l) *= m (m an FP32 number)
+__device__ __forceinline__ void df_mulf(float& h, float& l, float m) {
+    const float p = h * m;
+    const float e = fmaf(l, m, fmaf(h, m, -p));
+    h = p + e;
+    l = e - (h - p);
+}
+// (h, l) *= (h2, l2)
+__device__ __forceinline__ void df_mul(float& h, float& l, float h2, float l2) {
+    const float p = h * h2;
+    const float e = fmaf(h, l2, fmaf(l, h2, fmaf(h, h2, -p)));
+    h = p + e;
+    l = e - (h - p);
+}
+// keep the product's high part in [2^-32, 1]: exact power-of-two rescaling, exponent in esum
+__device__ __forceinline__ void df_renorm(float& h, float& l, int& esum) {
+    if (h < 0x1p-32f && h > 0.f) {
+        h *= 0x1p32f;
+        l *= 0x1p32f;
+        esum -= 32;
+    }
+}
+
+// The node's stored row r (largest entry exactly 1); the factor it drops multiplies the running
+// product (ph, pl) and its power-of-two exponent goes to esum.  Returns false when the product is
+// zero at every state (r is then all zero and the pattern's likelihood is 0).  Every lane of the
+// warp must call it.
+template <int Q, int W, int LPP>
+__device__ __forceinline__ bool ref_finish(RefAcc<W / LPP>& A, float (&r)[W / LPP], float& ph, float& pl, int& esum,
+                                           int j0) {
+    constexpr int S = W / LPP;
+    // every shuffle first (the branches below differ between the patterns of a warp)
+    const float f1 = 1.f + A.dl;
+    const float inv = A.mode == 1 && f1 > 0.f ? __frcp_rn(f1) : 0.f;
+    float mo = 0.f;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        r[s] = (j0 + s < Q) ? (j0 + s == A.a ? 1.f : A.y[s] * inv) : 0.f;
+        mo = fmaxf(mo, r[s]);
+    }
+    mo = group_max<LPP>(mo);
+    const bool ref = A.mode == 1 && f1 > 0x1p-64f && mo <= 1.f;
+    if (A.mode == 1 && !ref) {
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+            if (j0 + s == A.a) A.y[s] = f1;
+    }
+    float M = 0.f;
+#pragma unroll
+    for (int s = 0; s < S; ++s) M = fmaxf(M, (j0 + s < Q) ? A.y[s] : 0.f);
+    M = group_max<LPP>(M);
+    const int b = group_first_eq<Q, W, LPP>(A.y, M, j0);
+    if (ref) {
+        df_mul_1p(ph, pl, A.dl);
+        df_renorm(ph, pl, esum);
+        return true;
+    }
+    if (A.mode == 0) {  // every child masked out: a partial of ones
+#pragma unroll
+        for (int s = 0; s < S; ++s) r[s] = (j0 + s < Q) ? 1.f : 0.f;
+        return true;
+    }
+    if (!(M > 0.f)) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) r[s] = 0.f;
+        return false;
+    }
+    const int e = pow2_exponent(M);  // M = mant * 2^e, mant in [0.5, 1)
+    float mm[1] = {M};
+    scale_pow2<1>(mm, e);
+    scale_pow2<S>(A.y, e);
+    esum += e;
+    const float im = __frcp_rn(mm[0]);
+#pragma unroll
+    for (int s = 0; s < S; ++s) r[s] = (j0 + s < Q) ? (j0 + s == b ? 1.f : fminf(1.f, A.y[s] * im)) : 0.f;
+    df_mulf(ph, pl, mm[0]);
+    df_renorm(ph, pl, esum);
+    return true;
+}
+
+// Kahan-compensated FP32 accumulation (the mask corrections' logs).
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
+    const float y = v - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
 // first argmax over the pattern's states (ties -> lowest index), across the LPP lanes
 template <int Q, int W, int LPP>
 __device__ __forceinline__ int group_argmax(const float (&x)[W / LPP], int j0) {
@@ -220,8 +440,6 @@ struct __align__(16) Stage {
     float mat[StageCfg<Q, W>::kChunk][StageCfg<Q, W>::kMatFloats];
 };
 
-// Partials are rescaled (by an exact power of two) only below this largest entry.
-constexpr float kRescaleBelow = 0x1p-16f;
 // Level offsets of trees with fewer levels than this are read from shared memory.
 constexpr int kLevCap = 1024;
 

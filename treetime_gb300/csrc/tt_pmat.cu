@@ -4,6 +4,12 @@
 // GTR.expQt (treetime/gtr.py:1051-1067): the diagonal scaling is applied to V⁻¹'s rows and the
 // product summed over the eigen index in order.  Row layout [node][i][width], entry (i, j) =
 // probability of child state i given parent state j.
+//
+// The FP32 copies used by the FP32 marginal kernel hold D(t) = P(t) - I instead, formed in FP64
+// as V · diag(expm1(mu·lambda·t)) · V⁻¹ (off-diagonal entries clamped at 0 like P, the diagonal
+// at -1): for a short branch P's diagonal is 1 - O(t), which FP32 stores only to 3e-8 absolute,
+// while D keeps every entry to FP32's relative precision.  The kernel then forms messages as
+// x + x·D.
 #include "tt_internal.cuh"
 
 namespace tt {
@@ -34,25 +40,48 @@ __global__ void pmats_kernel(tt_forest f, tt_model m, tt_pmats out, int32_t* sta
         const double* lam = m.lam + (int64_t)mi * q;
         const double mu = m.mu[mi];
         const double bl = f.bl[g];
-        double ex[kMaxQ];
+        double ex[kMaxQ], em1[kMaxQ];
+        const bool need32 = out.p32 != nullptr || out.p32_pair != nullptr;
         for (int k = 0; k < q; ++k) {
             const double lv = mu * bl * lam[k];
             if (lv > 10.0) set_status(status, TT_ERR_NUMERIC);
             ex[k] = exp(lv);
+            em1[k] = need32 ? expm1(lv) : 0.0;
         }
         const int ps = (out.p32_pair && f.pair_slot) ? f.pair_slot[g] : -1;
+        const int lps = (out.logp2 && out.logp2_pair && f.pair_slot) ? f.pair_slot[g] : -1;
         const int64_t o = g * q * w + (int64_t)i * w;
         for (int j = 0; j < w; ++j) {
-            double p = 0.0;
+            double p = 0.0, d = 0.0;
             if (j < q) {
                 double acc = 0.0;
                 for (int k = 0; k < q; ++k) acc = fma(V[i * q + k], ex[k] * Vi[k * q + j], acc);
                 p = acc > 0.0 ? acc : 0.0;
+                if (need32) {
+                    double dacc = 0.0;
+                    for (int k = 0; k < q; ++k) dacc = fma(V[i * q + k], em1[k] * Vi[k * q + j], dacc);
+                    d = i == j ? (dacc > -1.0 ? dacc : -1.0) : (dacc > 0.0 ? dacc : 0.0);
+                }
             }
             out.p64[o + j] = p;
-            if (out.p32) out.p32[o + j] = (float)p;
-            if (ps >= 0) out.p32_pair[(int64_t)ps * q * w + (int64_t)i * w + j] = (float)p;
-            if (out.logp64) out.logp64[o + j] = j < q ? log(p > kTiny ? p : kTiny) : 0.0;
+            if (out.p32) out.p32[o + j] = (float)d;
+            if (ps >= 0) out.p32_pair[(int64_t)ps * q * w + (int64_t)i * w + j] = (float)d;
+            if (out.logp64 || out.logp2) {
+                const double lg = j < q ? log(p > kTiny ? p : kTiny) : 0.0;
+                if (out.logp64) out.logp64[o + j] = lg;
+                if (out.logp2) {
+                    // FP32 pair (hi, lo): row i holds w high parts, then w low parts
+                    const float hi = (float)lg, lo = (float)(lg - (double)hi);
+                    const int64_t r = (g * q + i) * 2 * w;
+                    out.logp2[r + j] = hi;
+                    out.logp2[r + w + j] = lo;
+                    if (lps >= 0) {
+                        const int64_t rp = ((int64_t)lps * q + i) * 2 * w;
+                        out.logp2_pair[rp + j] = hi;
+                        out.logp2_pair[rp + w + j] = lo;
+                    }
+                }
+            }
         }
     }
 }

@@ -207,8 +207,31 @@ class DeviceModel:
         pm = profile_map if profile_map is not None else gtrs[0].profile_map
         self.lut_host = profile_lut(pm, q)
         self.lut = _to_dev(self.lut_host, dev)
+        self.lut_log2 = _to_dev(log_lut_pairs(self.lut_host, WIDTHS[q]), dev)
         self.struct = TTModel(len(gtrs), q, _p(self.V), _p(self.Vinv), _p(self.lam), _p(self.mu), _p(self.pi),
-                              _p(self.lut))
+                              _p(self.lut), _p(self.lut_log2))
+
+
+def float_pairs(x):
+    """FP64 values as FP32 pairs (hi, lo) with hi + lo equal to x to ~48 bits."""
+    x = np.asarray(x, dtype=np.float64)
+    hi = x.astype(np.float32)
+    lo = (x - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo
+
+
+def log_lut_pairs(lut, w):
+    """[256][2][w] FP32 pairs of log(max(lut, 1e-12)) with non-finite values
+    set to -1e10: the tips' log profiles of the joint reconstruction
+    (treetime/treeanc.py:971-978)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lg = np.log(np.maximum(lut, ttconf.TINY_NUMBER))
+    lg[~np.isfinite(lg)] = -ttconf.BIG_NUMBER
+    hi, lo = float_pairs(lg)
+    out = np.zeros((lut.shape[0], 2, w), dtype=np.float32)
+    out[:, 0, :lut.shape[1]] = hi
+    out[:, 1, :lut.shape[1]] = lo
+    return out
 
 
 # DeviceModels of recently used GTR objects, least recently used first.  An entry holds its GTR
@@ -217,6 +240,8 @@ class DeviceModel:
 # holding every model it has seen.
 _MODEL_CACHE = collections.OrderedDict()
 MODEL_CACHE_SIZE = 256
+# hits and builds of the device-model caches (DeviceModel, site-specific FP32 tables)
+CACHE_STATS = collections.Counter()
 
 
 def model_key(gtr):
@@ -234,6 +259,9 @@ def model_for(gtr, device=None):
     if m is None or m[0] != key:
         m = (key, DeviceModel(gtr, dev))
         _MODEL_CACHE[id(gtr)] = m
+        CACHE_STATS["model_build"] += 1
+    else:
+        CACHE_STATS["model_hit"] += 1
     _MODEL_CACHE.move_to_end(id(gtr))
     while len(_MODEL_CACHE) > MODEL_CACHE_SIZE:
         _MODEL_CACHE.popitem(last=False)
@@ -527,16 +555,19 @@ class Buffers:
 
 
 def branch_pmats(forest, model, bufs, need32=False, needlog=False):
+    """P(t) of every branch (FP64), with the FP32 D = P - I copies of the FP32
+    marginal kernel (need32) or the log pairs of the joint kernel (needlog)."""
     t = torch()
     q, w = forest.q, forest.w
     p64 = bufs.get("p64", (forest.n_nodes, q, w), t.float64)
     p32 = bufs.get("p32", (forest.n_nodes, q, w), t.float32) if need32 else None
     p32p = bufs.get("p32_pair", (forest.n_nodes, 2, q, w), t.float32) if need32 else None
-    lg = bufs.get("logp", (forest.n_nodes, q, w), t.float64) if needlog else None
+    lg2 = bufs.get("logp2", (forest.n_nodes, q, 2, w), t.float32) if needlog else None
+    lg2p = bufs.get("logp2_pair", (forest.n_nodes, 2, q, 2, w), t.float32) if needlog else None
     status = bufs.get("status", (1,), t.int32)
     status.zero_()
     lib = _lib.load()
-    pm = TTPmats(_p(p64), _p(p32), _p(lg), _p(p32p))
+    pm = TTPmats(_p(p64), _p(p32), None, _p(p32p), _p(lg2), _p(lg2p))
     check(lib.tt_branch_pmats(C.byref(forest.struct), C.byref(model.struct), pm, _p(status), _stream()),
           "tt_branch_pmats")
     return pm, status
@@ -634,7 +665,9 @@ def _ss_f32_model(forest, gtr, bufs, dev, range_width=None):
     key = (model_key(gtr), forest.w, str(dev), range_width)
     hit = _SS_F32_CACHE.get(key)
     if hit is not None:
+        CACHE_STATS["site_model_hit"] += 1
         return hit
+    CACHE_STATS["site_model_build"] += 1
     t = torch()
     lam, V, Vi = site_matrices(gtr)                    # [P][q], [P][q][q], [P][q][q] (FP64)
     P, q = lam.shape
@@ -714,17 +747,7 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
                                      int(arrs["ranges"].shape[0]), C.byref(o), _p(status), _stream()),
               "tt_marginal_ss_f32")
     else:
-        key = model_key(gtr)
-        cache = bufs.cache.get("ss_model")
-        if cache is None or cache[0] != key:
-            lam, V, Vi = site_matrices(gtr)
-            arrs = dict(lam=_to_dev(lam, dev), V=_to_dev(V, dev), Vi=_to_dev(Vi, dev),
-                        mu=_to_dev(np.asarray(gtr.mu, dtype=np.float64), dev),
-                        pi=_to_dev(np.ascontiguousarray(gtr.Pi.T), dev),
-                        lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev),
-                        grid=_to_dev(site_grid(gtr), dev))
-            bufs.cache["ss_model"] = (key, arrs)
-        arrs = bufs.cache["ss_model"][1]
+        arrs = _ss_model64(gtr, bufs, dev)
         check(lib.tt_marginal_ss(C.byref(forest.struct), _p(arrs["lam"]), _p(arrs["V"]), _p(arrs["Vi"]),
                                  _p(arrs["mu"]), _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]),
                                  int(arrs["grid"].numel()), float(gtr.rate_scale), int(bool(gtr.approximate)),
@@ -735,6 +758,73 @@ def marginal_site_specific(forest, gtr, bufs, precision="f64", reconstruct_tips=
     return out
 
 
+def _ss_model64(gtr, bufs, dev, need_stack=False):
+    """FP64 device arrays of a site-specific model (cached per model in the
+    forest's buffers); with need_stack and TreeTime's interpolated P(t), the
+    exact matrices at the grid points (tt_ss_pstack) as well."""
+    key = model_key(gtr)
+    cache = bufs.cache.get("ss_model")
+    if cache is None or cache[0] != key:
+        lam, V, Vi = site_matrices(gtr)
+        arrs = dict(lam=_to_dev(lam, dev), V=_to_dev(V, dev), Vi=_to_dev(Vi, dev),
+                    mu=_to_dev(np.asarray(gtr.mu, dtype=np.float64), dev),
+                    pi=_to_dev(np.ascontiguousarray(gtr.Pi.T), dev),
+                    lut=_to_dev(profile_lut(gtr.profile_map, gtr.n_states), dev),
+                    grid=_to_dev(site_grid(gtr), dev))
+        bufs.cache["ss_model"] = (key, arrs)
+    arrs = bufs.cache["ss_model"][1]
+    q = gtr.n_states
+    L = int(arrs["mu"].numel())
+    approx = bool(getattr(gtr, "approximate", False))
+    if "struct" not in arrs:
+        arrs["struct"] = _lib.TTSSModel(q, int(arrs["grid"].numel()), int(approx), 0, float(gtr.rate_scale),
+                                        _p(arrs["lam"]), _p(arrs["V"]), _p(arrs["Vi"]), _p(arrs["mu"]),
+                                        _p(arrs["pi"]), _p(arrs["lut"]), _p(arrs["grid"]), None)
+    if need_stack and approx and "stack" not in arrs:
+        t = torch()
+        arrs["stack"] = t.empty((int(arrs["grid"].numel()), q, q, L), dtype=t.float64, device=dev)
+        check(_lib.load().tt_ss_pstack(C.byref(arrs["struct"]), L, _p(arrs["stack"]), _stream()), "tt_ss_pstack")
+        arrs["struct"].stack = _p(arrs["stack"])
+    return arrs
+
+
+def joint_site_specific(forest, gtr, bufs, reconstruct_tips=False, count_diff=False, root_uniform=None, sync=True):
+    """Joint reconstruction under a GTR_site_specific model (single tree): per
+    node and site log P from TreeTime's interpolated (or exact) per-site
+    matrices in FP64, one launch per height level."""
+    t = torch()
+    lib = _lib.load()
+    if len(forest.inputs) != 1:
+        raise ValueError("joint reconstruction with a site-specific model takes one tree")
+    dev = forest.device
+    arrs = _ss_model64(gtr, bufs, dev, need_stack=True)
+    lay = forest.inputs[0].layout
+    w = forest.w
+    out = {
+        "msg": bufs.get("joint_msg", (forest.prof_rows, 2, w), t.float32),
+        "cx": bufs.get("cx", (forest.prof_rows, w), t.uint8),
+        "states": bufs.get("states", (forest.state_rows,), t.uint8),
+        "site_lh": bufs.get("joint_site_lh", (forest.n_patterns,), t.float64),
+        "tree_lh": bufs.get("joint_tree_lh", (1,), t.float64),
+        "n_diff": bufs.get("n_diff", (1,), t.int64),
+    }
+    out["n_diff"].zero_()
+    status = bufs.get("status", (1,), t.int32)
+    status.zero_()
+    ru = _to_dev(root_uniform, dev, t.float64) if root_uniform is not None else None
+    o = TTJointOut(_p(out["msg"]), _p(out["cx"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
+                   _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)),
+                   int(forest.prof_rows))
+    lev = np.ascontiguousarray(lay.level_off, dtype=np.int32)
+    check(lib.tt_joint_ss(C.byref(forest.struct), C.byref(arrs["struct"]), lev.ctypes.data_as(C.c_void_p),
+                          int(lay.n_levels), int(lay.n_int), int(lay.n_tip), C.byref(o), _p(status), _stream()),
+          "tt_joint_ss")
+    if sync:
+        _check_status(status)
+    out["_keep"] = ru
+    return out
+
+
 def joint(forest, model, bufs, reconstruct_tips=False, count_diff=False, root_uniform=None, sync=True):
     t = torch()
     lib = _lib.load()
@@ -742,7 +832,7 @@ def joint(forest, model, bufs, reconstruct_tips=False, count_diff=False, root_un
     pm, status = branch_pmats(forest, model, bufs, needlog=True)
     w = forest.w
     out = {
-        "lx": bufs.get("lx", (forest.prof_rows, w), t.float64),
+        "msg": bufs.get("joint_msg", (forest.prof_rows, 2, w), t.float32),
         "cx": bufs.get("cx", (forest.prof_rows, w), t.uint8),
         "states": bufs.get("states", (forest.state_rows,), t.uint8),
         "site_lh": bufs.get("joint_site_lh", (forest.n_patterns,), t.float64),
@@ -751,8 +841,9 @@ def joint(forest, model, bufs, reconstruct_tips=False, count_diff=False, root_un
     }
     out["n_diff"].zero_()
     ru = _to_dev(root_uniform, forest.device, t.float64) if root_uniform is not None else None
-    o = TTJointOut(_p(out["lx"]), _p(out["cx"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
-                   _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)))
+    o = TTJointOut(_p(out["msg"]), _p(out["cx"]), _p(out["states"]), _p(out["site_lh"]), _p(out["tree_lh"]),
+                   _p(out["n_diff"]), _p(ru), int(bool(reconstruct_tips)), int(bool(count_diff)),
+                   int(forest.prof_rows))
     check(lib.tt_joint(C.byref(forest.struct), C.byref(model.struct), C.byref(pm), C.byref(o), _p(status),
                        _stream()), "tt_joint")
     if sync:

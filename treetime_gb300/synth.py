@@ -143,19 +143,34 @@ def evolve_sparse(tree, gtr, L, rng):
     return out
 
 
-def forest_c3(n_trees=256, seed=3, n_range=(50, 5000), L_range=(1000, 30000), bl_range=(1e-4, 0.05)):
+def c3_sizes(n_trees=256, seed=3, n_range=(50, 5000), L_range=(1000, 30000), bl_range=(1e-4, 0.05)):
+    """(tips, sites, mean branch length) of every tree of ``forest_c3`` with
+    the same arguments, without building any tree: each tree draws them first
+    from its own generator."""
+    out = []
+    for k in range(n_trees):
+        rng = np.random.default_rng([seed, k])
+        lu = lambda lo, hi: float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        out.append((int(lu(*n_range)), int(lu(*L_range)), lu(*bl_range)))
+    return out
+
+
+def forest_c3(n_trees=256, seed=3, n_range=(50, 5000), L_range=(1000, 30000), bl_range=(1e-4, 0.05), only=None):
     """The batched workload as device-ready inputs: ``n_trees`` independent
     coalescent trees with tip counts, site counts and mean branch lengths
-    log-uniform in the given ranges, each with its own random nucleotide GTR
-    (model index = tree index), alignments compressed to patterns.  Built from
-    state codes directly (no alignment text).  Returns (inputs, gtrs)."""
+    log-uniform in the given ranges, each with its own random nucleotide GTR,
+    alignments compressed to patterns.  Tree k draws everything from its own
+    generator (seeded by (seed, k)), so any subset (``only``: tree indices)
+    is built alone with the same result as in the whole batch.  Built from
+    state codes directly (no alignment text).  Returns (inputs, gtrs), model
+    index = position in the returned list."""
     from . import engine
     from .seqdata import compress_codes
-    rng = np.random.default_rng(seed)
-    lu = lambda lo, hi: float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
     alpha = np.frombuffer("".join(alphabets["nuc_nogap"]).encode(), dtype=np.uint8)
     inputs, gtrs = [], []
-    for k in range(n_trees):
+    for k in (range(n_trees) if only is None else only):
+        rng = np.random.default_rng([seed, k])
+        lu = lambda lo, hi: float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
         n = int(lu(*n_range))
         L = int(lu(*L_range))
         bl = lu(*bl_range)
@@ -167,7 +182,9 @@ def forest_c3(n_trees=256, seed=3, n_range=(50, 5000), L_range=(1000, 30000), bl
         codes = alpha[np.stack([st[t.name] for t in tips])]
         pc, mult, _, _ = compress_codes(codes, ord("N"))
         inputs.append(engine.TreeInput(layout, pc, np.arange(len(tips), dtype=np.int32), mult,
-                                       engine.branch_lengths(layout, L), model=k))
+                                       engine.branch_lengths(layout, L), model=len(gtrs)))
+        inputs[-1].tree = tree
+        inputs[-1].full_length = L
         gtrs.append(gtr)
     return inputs, gtrs
 
@@ -272,8 +289,9 @@ def evolve_site_specific(tree, gtr, L, rng):
             continue
         for ch in node.clades:
             e = np.exp(gtr.mu[:, None] * lam * ch.branch_length)        # [L, q]
-            P = np.einsum("aik,ak,akj->aij", V, e, Vi)                     # P_a[child, parent]
-            col = np.maximum(P[sites, :, s], 0.0)                          # [L, q] over child states
+            # column of P_a[child, parent] at each site's parent state: V_a (e_a * V_a^-1[:, s_a])
+            z = e * Vi[sites, :, s]                                        # [L, q] over eigen index
+            col = np.maximum(np.matmul(V, z[:, :, None])[:, :, 0], 0.0)   # [L, q] over child states
             cdf = np.cumsum(col, axis=1)
             cdf /= cdf[:, -1:]
             child = np.minimum((rng.random(L)[:, None] > cdf).sum(axis=1), q - 1)

@@ -100,9 +100,53 @@ class _Traversal:
                 ntips[id(node)] = 1
 
 
-# Per-node results of a reconstruction that are materialised on first access
-# from the device results (see treeanc.ResultStore).
+# Per-node results of a reconstruction, read from the device results of the
+# latest reconstruction (anc_gpu.ResultStore) when first accessed.
 LAZY_ATTRS = ("_cseq", "marginal_profile", "marginal_subtree_LH", "marginal_outgroup_LH", "branch_state")
+
+
+class _Result:
+    """Data descriptor of one per-node result.  A clade of a reconstruction
+    session holds the session's result holder in ``_anc_src``; reading the
+    attribute asks the holder (which answers from the latest reconstruction),
+    so installing a new reconstruction is one assignment for the whole tree
+    instead of a walk over its nodes.  A value assigned to the attribute
+    overrides the holder's until the next reconstruction (the holder is told,
+    and clears the overrides it was told of), as TreeTime's next
+    reconstruction overwrites what was assigned before."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __get__(self, node, owner=None):
+        if node is None:
+            return self
+        d = node.__dict__
+        ov = d.get("_anc_override")
+        if ov is not None and self.name in ov:
+            return ov[self.name]
+        src = d.get("_anc_src")
+        if src is not None:
+            val = src.fetch(self.name, node)
+            if val is not None:
+                return val
+        raise AttributeError(self.name)
+
+    def __set__(self, node, value):
+        d = node.__dict__
+        ov = d.get("_anc_override")
+        if ov is None:
+            ov = d["_anc_override"] = {}
+        ov[self.name] = value
+        src = d.get("_anc_src")
+        if src is not None and hasattr(src, "overridden"):
+            src.overridden(node)
+
+    def __delete__(self, node):
+        ov = node.__dict__.get("_anc_override")
+        if not ov or self.name not in ov:
+            raise AttributeError(self.name)
+        del ov[self.name]
 
 
 class Clade(_Traversal):
@@ -114,17 +158,6 @@ class Clade(_Traversal):
 
     def _start(self):
         return self
-
-    def __getattr__(self, name):
-        # only reached when normal lookup fails: lazy reconstruction results
-        if name in LAZY_ATTRS:
-            src = self.__dict__.get("_anc_src")
-            if src is not None:
-                val = src.fetch(name, self)
-                if val is not None:
-                    self.__dict__[name] = val
-                    return val
-        raise AttributeError(name)
 
     @property
     def cseq(self):
@@ -168,6 +201,12 @@ class Clade(_Traversal):
 
     def __len__(self):
         return len(self.clades)
+
+    _cseq = _Result("_cseq")
+    marginal_profile = _Result("marginal_profile")
+    marginal_subtree_LH = _Result("marginal_subtree_LH")
+    marginal_outgroup_LH = _Result("marginal_outgroup_LH")
+    branch_state = _Result("branch_state")
 
     def __getitem__(self, i):
         return self.clades[i]

@@ -104,11 +104,39 @@ def _pinned_copy(t):
     return view.numpy().copy()
 
 
+def _host_results(sess, out, rows, P, site_key="site_lh", tree_key="tree_lh", n_diff=True):
+    """The results every reconstruction hands to the host -- the states of the
+    reconstructed rows, the site and tree log-likelihoods and the changed-site
+    count -- through page-locked buffers of the session, as asynchronous copies
+    on the current stream followed by one wait.  The states array returned is
+    a view of the session's buffer: valid until the session's next
+    reconstruction (the results installed on the nodes read it only until
+    then)."""
+    torch = engine.torch()
+    nb = rows * P
+    pb = sess.get("pinned")
+    if pb is None or pb[0].numel() < nb or pb[1].numel() < P + 1:
+        pb = (torch.empty(max(nb, 1), dtype=torch.uint8, pin_memory=True),
+              torch.empty(P + 1, dtype=torch.float64, pin_memory=True),
+              torch.empty(1, dtype=torch.int64, pin_memory=True))
+        sess["pinned"] = pb
+    st, sc, nd = pb
+    st[:nb].copy_(out["states"].view(-1)[:nb], non_blocking=True)
+    sc[:P].copy_(out[site_key][:P], non_blocking=True)
+    sc[P:P + 1].copy_(out[tree_key][:1], non_blocking=True)
+    if n_diff:
+        nd.copy_(out["n_diff"][:1], non_blocking=True)
+    torch.cuda.current_stream(out["states"].device).synchronize()
+    scn = sc.numpy()
+    return (st.numpy()[:nb].reshape(rows, P), scn[:P].copy(), float(scn[P]),
+            int(nd.numpy()[0]) if n_diff else 0)
+
+
 class ResultStore:
     """Host view of one reconstruction's device results; node attributes are
     built from it on first access."""
 
-    def __init__(self, tt, layout, kind, out, precision, reconstruct_tips):
+    def __init__(self, tt, layout, kind, out, precision, reconstruct_tips, states=None):
         self.tt = tt
         self.layout = layout
         self.kind = kind
@@ -119,7 +147,9 @@ class ResultStore:
         self.q = tt.gtr.n_states
         # the reconstructed rows: internal nodes, and the tips when their states were reconstructed
         rows = layout.n_nodes if reconstruct_tips else layout.n_int
-        self.states = _pinned_copy(out["states"].view(-1)[: rows * self.P]).reshape(rows, self.P)
+        if states is None:
+            states = _pinned_copy(out["states"].view(-1)[: rows * self.P]).reshape(rows, self.P)
+        self.states = states
         self._host = {}
         self._cache = {}
 
@@ -378,10 +408,13 @@ class GPUAncMixin:
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
-        N_diff = int(out["n_diff"][0].item()) if count_diff else P * n_recon
-        self._install(ResultStore(self, layout, "marginal", out, prec, reconstruct_tip_states), layout)
-        self.tree.sequence_LH = out["site_lh"].cpu().numpy()
-        self.tree.total_sequence_LH = float(out["tree_lh"][0].item())
+        rows = layout.n_nodes if reconstruct_tip_states else layout.n_int
+        states, site_lh, total, nd = _host_results(sess, out, rows, P)
+        N_diff = nd if count_diff else P * n_recon
+        self._install(ResultStore(self, layout, "marginal", out, prec, reconstruct_tip_states, states=states),
+                      layout)
+        self.tree.sequence_LH = site_lh
+        self.tree.total_sequence_LH = total
         self.tree.sequence_marginal_LH = self.tree.total_sequence_LH
         self.reconstructed_tip_sequences = reconstruct_tip_states
         self.sequence_reconstruction = "marginal"
@@ -407,10 +440,12 @@ class GPUAncMixin:
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
-        N_diff = int(out["n_diff"][0].item()) if count_diff else P * n_recon
-        self._install(ResultStore(self, layout, "joint", out, "f64", reconstruct_tip_states), layout)
-        self.tree.sequence_LH = out["site_lh"].cpu().numpy()
-        self.tree.sequence_joint_LH = float(out["tree_lh"][0].item())
+        rows = layout.n_nodes if reconstruct_tip_states else layout.n_int
+        states, site_lh, total, nd = _host_results(sess, out, rows, P)
+        N_diff = nd if count_diff else P * n_recon
+        self._install(ResultStore(self, layout, "joint", out, "f64", reconstruct_tip_states, states=states), layout)
+        self.tree.sequence_LH = site_lh
+        self.tree.sequence_joint_LH = total
         self.reconstructed_tip_sequences = reconstruct_tip_states
         self.sequence_reconstruction = "joint"
         self._last = ("joint", out)

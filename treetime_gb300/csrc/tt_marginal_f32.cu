@@ -53,6 +53,18 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         const int c = i / W, j = i % W;
         lut_s[i] = j < Q ? (float)__ldg(a.lut + c * Q + j) : 0.f;
     }
+    // characters whose profile is a single state (one 1, zeros elsewhere): their message is a row
+    // of D (the first barrier of the work loop publishes the table)
+    __shared__ signed char onehot_s[256];
+    for (int c = tid; c < 256; c += NT) {
+        int st1 = -1, ones = 0;
+        bool ok = true;
+        for (int j = 0; j < Q; ++j) {
+            const double v = __ldg(a.lut + c * Q + j);
+            if (v == 1.0) { ++ones; st1 = j; } else if (v != 0.0) { ok = false; }
+        }
+        onehot_s[c] = (signed char)(ok && ones == 1 ? st1 : -1);
+    }
     const bool has_masks = a.f.mask_off != nullptr;
     float* partial = reinterpret_cast<float*>(a.o.partial);
     float* posterior = reinterpret_cast<float*>(a.o.posterior);
@@ -125,6 +137,25 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                 if (m != 1.f) kahan_add(lsum, lcomp, (1.f - m) * logf(xs));
             }
             return m;
+        };
+        // x.D of a child (code >= 0: a tip with that character; x is filled from the table); with
+        // one lane per pattern a single-state character's x.D is the row of its state
+        auto child_xd = [&](int code, float (&x)[S], const float* Dm, float (&xd)[S]) {
+            if constexpr (LPP == 1) {
+                if (code >= 0) {
+                    const int s1 = onehot_s[code];
+                    if (s1 >= 0) {
+#pragma unroll
+                        for (int s = 0; s < S; ++s) x[s] = s == s1 ? 1.f : 0.f;
+                        ld_part<S>(Dm + s1 * W, xd);
+                        return;
+                    }
+                    lut_part(code, x);
+                }
+            } else {
+                if (code >= 0) lut_part(code, x);
+            }
+            s_vec_mat<Q, W, LPP>(x, Dm, j0, xd);
         };
         // stage the chunk [base, base + cnt) of a level into buffer b
         auto stage = [&](int b, int base, int cnt, bool post) {
@@ -212,11 +243,9 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         RefAcc<S> A;
                         A.template reset<Q>();
                         if (bin[d]) {
-                            if (ca[d] >= 0) lut_part(ca[d], xa[d]);
-                            if (cb[d] >= 0) lut_part(cb[d], xb[d]);
                             float d0[S], d1[S];
-                            s_vec_mat<Q, W, LPP>(xa[d], &st.mat[i][0], j0, d0);
-                            s_vec_mat<Q, W, LPP>(xb[d], &st.mat[i][QW], j0, d1);
+                            child_xd(ca[d], xa[d], &st.mat[i][0], d0);
+                            child_xd(cb[d], xb[d], &st.mat[i][QW], d1);
                             float m0 = 1.f, m1 = 1.f;
                             if (has_masks) {
                                 const int4 cp = st.pair[i];

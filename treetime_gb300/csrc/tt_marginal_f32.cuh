@@ -230,15 +230,18 @@ __device__ __forceinline__ void ref_add(RefAcc<W / LPP>& A, const float (&x)[W /
             for (int s = 0; s < S; ++s) A.y[s] *= m[s];
         }
     }
-    // keep a long general-form product (a polytomy's) in range
-    float mx = 0.f;
+    // keep a long general-form product (a polytomy's) in range; one lane per pattern needs no
+    // shuffle, so it checks only in the general form
+    if (LPP > 1 || A.mode == 2) {
+        float mx = 0.f;
 #pragma unroll
-    for (int s = 0; s < S; ++s) mx = fmaxf(mx, A.y[s]);
-    mx = group_max<LPP>(mx);
-    if (A.mode == 2 && mx < kRescaleBelowRef && mx > 0.f) {
-        const int e = pow2_exponent(mx);
-        scale_pow2<S>(A.y, e);
-        esum += e;
+        for (int s = 0; s < S; ++s) mx = fmaxf(mx, A.y[s]);
+        mx = group_max<LPP>(mx);
+        if (A.mode == 2 && mx < kRescaleBelowRef && mx > 0.f) {
+            const int e = pow2_exponent(mx);
+            scale_pow2<S>(A.y, e);
+            esum += e;
+        }
     }
 }
 
@@ -285,7 +288,8 @@ __device__ __forceinline__ bool ref_finish(RefAcc<W / LPP>& A, float (&r)[W / LP
     constexpr int S = W / LPP;
     // every shuffle first (the branches below differ between the patterns of a warp)
     const float f1 = 1.f + A.dl;
-    const float inv = A.mode == 1 && f1 > 0.f ? __frcp_rn(f1) : 0.f;
+    // the reciprocal's ~2 ulp land on the non-reference entries only
+    const float inv = A.mode == 1 && f1 > 0.f ? __fdividef(1.f, f1) : 0.f;
     float mo = 0.f;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
@@ -298,6 +302,13 @@ __device__ __forceinline__ bool ref_finish(RefAcc<W / LPP>& A, float (&r)[W / LP
 #pragma unroll
         for (int s = 0; s < S; ++s)
             if (j0 + s == A.a) A.y[s] = f1;
+    }
+    if constexpr (LPP == 1) {  // no shuffles: the reference form returns before the general form's work
+        if (ref) {
+            df_mul_1p(ph, pl, A.dl);
+            df_renorm(ph, pl, esum);
+            return true;
+        }
     }
     float M = 0.f;
 #pragma unroll
@@ -324,7 +335,7 @@ __device__ __forceinline__ bool ref_finish(RefAcc<W / LPP>& A, float (&r)[W / LP
     scale_pow2<1>(mm, e);
     scale_pow2<S>(A.y, e);
     esum += e;
-    const float im = __frcp_rn(mm[0]);
+    const float im = __fdividef(1.f, mm[0]);
 #pragma unroll
     for (int s = 0; s < S; ++s) r[s] = (j0 + s < Q) ? (j0 + s == b ? 1.f : fminf(1.f, A.y[s] * im)) : 0.f;
     df_mulf(ph, pl, mm[0]);

@@ -15,6 +15,7 @@ Layout of a forest in device memory (see include/treetime_gb300.h):
 
 import collections
 import ctypes as C
+import operator
 import time
 
 import math
@@ -177,7 +178,8 @@ def branch_lengths(layout, full_length, use_mutation_length=False):
     NaN length becomes the floor there; np.fmax does the same."""
     floor = ttconf.MIN_BRANCH_LENGTH * (1.0 / full_length)
     attr = "mutation_length" if use_mutation_length else "branch_length"
-    bl = np.array([getattr(n, attr) or 0.0 for n in layout.nodes], dtype=np.float64)
+    # None (no length) becomes NaN here and the floor below, as `or 0.0` would make it
+    bl = np.array(list(map(operator.attrgetter(attr), layout.nodes)), dtype=np.float64)
     return np.fmax(floor, bl)
 
 
@@ -448,11 +450,26 @@ class Forest:
         unit = 32 // lanes_per_pattern if lanes_per_pattern > 1 else 1
         slots = max(1, sms * max(1, int(ranges_per_sm)))
         total = sum(ti.layout.n_nodes * ti.n_patterns for ti in inputs)
+        # ranges per tree: when the trees fit in the slots, shares of the slots proportional to
+        # their node x pattern work (largest remainders, at least one each), so that the ranges
+        # fill the GPU once without a second wave; otherwise ranges of about one slot's share
+        shares = None
+        if not range_patterns and 0 < len(inputs) <= slots and total > 0:
+            exact = [slots * ti.layout.n_nodes * ti.n_patterns / total for ti in inputs]
+            shares = [max(1, int(x)) for x in exact]
+            left = slots - sum(shares)
+            for t in sorted(range(len(inputs)), key=lambda t: -(exact[t] - int(exact[t]))):
+                if left <= 0:
+                    break
+                shares[t] += 1
+                left -= 1
         ranges, widths = [], []
         for t, ti in enumerate(inputs):
             P, N = ti.n_patterns, ti.layout.n_nodes
             if range_patterns:
                 want = int(range_patterns)
+            elif shares is not None:
+                want = int(math.ceil(P / max(1, min(shares[t], P))))
             else:
                 want = int(math.ceil(total / slots / max(1, N)))
             want = max(1, min(want, P, max_np))
@@ -462,6 +479,8 @@ class Forest:
                 ws = [want] * len(starts)
             else:
                 n_r = -(-P // want)
+                if shares is not None:  # exactly the tree's share (widths differ by at most one)
+                    n_r = max(n_r, min(shares[t], P))
                 base_w, extra = divmod(P, n_r)
                 ws = [base_w + (1 if r < extra else 0) for r in range(n_r)]
                 starts = list(np.cumsum([0] + ws[:-1]))

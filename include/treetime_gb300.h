@@ -323,6 +323,18 @@ tt_status tt_ss_pstack(const tt_ss_model* m, int32_t n_sites, double* stack, voi
 tt_status tt_joint_ss(const tt_forest* f, const tt_ss_model* m, const int32_t* level_off_host, int32_t n_levels,
                       int32_t n_int, int32_t n_tip, const tt_joint_out* out, int32_t* status, void* stream);
 
+/* The 'marginal' substitution counts of TreeAnc.infer_gtr (treetime/treeanc.py:1544-1563) under a
+ * site-specific model, for a forest of one tree: per listed branch and site the joint distribution
+ * of the states at both ends with the site's own P_a(t) + 1e-24 (get_branch_mutation_matrix,
+ * treetime/treeanc.py:1085-1120, with GTR_site_specific.expQt), summed into n_ija [q][q][n_patterns]
+ * and T_ia [q][n_patterns] (FP64, deterministic: chunks of branches summed in order).  Rows as in
+ * tt_mutation_counts; the model needs tt_ss_pstack's stack when `approximate`.  `workspace`: at
+ * least (q*q + q) * n_patterns doubles. */
+tt_status tt_mutation_counts_ss(const tt_forest* f, const tt_ss_model* m, int32_t tree, int32_t n_patterns, int64_t n,
+                                const int32_t* node_of, const void* pp, const int64_t* pp_row, const void* pc,
+                                const int64_t* pc_row, int32_t prec, double* n_ija, double* T_ia, double* workspace,
+                                int64_t workspace_bytes, void* stream);
+
 /* Joint reconstruction that allocates nothing.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (hosts that only hand out their own pre-sized
  * buffers, pools that reserve all device memory at start-up, paths that cannot afford an

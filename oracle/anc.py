@@ -519,10 +519,13 @@ def pair_resolution(model, grid, seq_pair):
 
 
 def branch_mutation_matrix(model, pp, pc, t):
-    """treeanc.py:1085-1120 (standard models): normalised
-    pc_i pp_j (expQt(t)_ij + 1e-24) per pattern, [L, q, q]."""
+    """treeanc.py:1085-1120: normalised pc_i pp_j (expQt(t)_ij + 1e-24) per
+    pattern, [L, q, q] (site-specific models: the pattern's own expQt)."""
     Qt = expQt(model, t) + SUPERTINY_NUMBER
-    M = np.einsum("ai,aj,ij->aij", pc, pp, Qt)
+    if Qt.ndim == 3:
+        M = np.einsum("ai,aj,ija->aij", pc, pp, Qt)
+    else:
+        M = np.einsum("ai,aj,ij->aij", pc, pp, Qt)
     norm = M.sum(axis=2).sum(axis=1)
     return np.einsum("aij,a->aij", M, 1.0 / norm)
 

@@ -147,3 +147,33 @@ def joint(newick, names, codes, mult, gtr, full_length, tie_tol=1e-9, workers=No
     out = _merge(_run(_joint_worker, jobs, workers), keys=("site_lh", "tie"))
     out["total"] = float((out["site_lh"] * np.asarray(mult)).sum())
     return out
+
+
+def _marginal_bl_worker(args):
+    newick, names, codes, mult, model, full_length, branch_names, tol = args
+    anc, tree, aln, internal = _setup(newick, names, codes)
+    res = anc.marginal(tree, aln, mult, model, full_length)
+    out = {}
+    for k in branch_names:
+        pp, pc = res["outgroup_LH"][k], res["subtree_LH"][k]
+        out[k] = anc.optimal_t_compressed(model, (pp, pc), mult, profiles=True, tol=tol)[0]
+    return out
+
+
+def marginal_branch_lengths(newick, names, codes, mult, gtr, full_length, tol=1e-10, workers=None):
+    """TreeTime's optimal_marginal_branch_length (oracle.anc.optimal_t_compressed
+    with profiles, scipy's Brent) for every non-root branch after a marginal
+    reconstruction, the branches split over a pool (each process reconstructs
+    the whole tree once).  Returns {node name: t}."""
+    from oracle import anc
+    from treetime_gb300.tree import parse_newick
+    tree = anc.prepare_tree(parse_newick(newick))
+    branches = [n.name for n in anc.preorder(tree.root) if n.up is not None]
+    workers = workers or os.cpu_count() or 1
+    n = max(1, min(workers, len(branches)))
+    jobs = [(newick, list(names), np.ascontiguousarray(codes), np.asarray(mult), model_state(gtr), full_length,
+             branches[i::n], tol) for i in range(n)]
+    out = {}
+    for part in _run(_marginal_bl_worker, jobs, workers):
+        out.update(part)
+    return out

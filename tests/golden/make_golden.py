@@ -6,6 +6,7 @@ shipped with this repository and are not needed to run the tests):
     python tests/golden/make_golden.py /path/to/treetime-source
     python tests/golden/make_golden.py /path/to/treetime-source --blgrid   (interpolator grids only)
     python tests/golden/make_golden.py /path/to/treetime-source --infer-gtr   (GTR inference only)
+    python tests/golden/make_golden.py /path/to/treetime-source --infer-gtr-ss   (inference from a site-specific model)
     python tests/golden/make_golden.py /path/to/treetime-source --fitch   (Fitch parsimony only)
     python tests/golden/make_golden.py /path/to/treetime-source --vcf   (VCF reading and sparse alignments)
     python tests/golden/make_golden.py /path/to/treetime-source --sample   (states drawn at every node)
@@ -325,6 +326,27 @@ def infer_gtr_cases():
     W0 = W0 + W0.T
     run_infer_gtr("gtrinf_aa_ss", to_newick(tree), aln, "gtr",
                   {"pi": pi0, "W": W0, "alphabet": synth.AA21, "mu": 1.0}, compress=False, site_specific=True)
+
+
+def infer_gtr_ss_current_cases():
+    """Marginal GTR inference of a site-specific model whose counts come from a
+    site-specific current model (TreeTime's interpolated P(t))."""
+    from treetime_gb300 import synth
+    from treetime_gb300.gtr import GTR_site_specific
+    from treetime_gb300.tree import to_newick
+    rng = np.random.default_rng(34)
+    L = 60
+    tree = synth.yule_tree(14, 0.08, rng)
+    pi_s = rng.dirichlet(np.full(21, 0.5), size=L).T
+    W_s = np.triu(rng.uniform(0.1, 5.0, size=(21, 21)), 1)
+    W_s = W_s + W_s.T
+    gs = GTR_site_specific(seq_len=L, approximate=True, alphabet=synth.AA21)
+    gs.assign_rates(mu=1.0, pi=pi_s, W=W_s)
+    states = synth.evolve_site_specific(tree, gs, L, rng)
+    aln = synth._to_text(states, gs.alphabet, 0.02, rng)
+    run_infer_gtr("gtrinf_ss_current", to_newick(tree), aln, "ss",
+                  {"pi": pi_s, "W": W_s, "alphabet": synth.AA21, "mu": 1.0, "approximate": True}, compress=False,
+                  site_specific=True)
 
 
 def run_fitch(name, newick, aln, kind, params, rng_seed=7):
@@ -885,6 +907,9 @@ if __name__ == "__main__":
     if "--blgrid" in sys.argv:
         _setup(ref)
         blgrid_cases()
+    elif "--infer-gtr-ss" in sys.argv:
+        _setup(ref)
+        infer_gtr_ss_current_cases()
     elif "--infer-gtr" in sys.argv:
         _setup(ref)
         infer_gtr_cases()

@@ -9,7 +9,8 @@ Tolerances (written here, per the contract of this port):
     margin at some node is below 1e-9 (counted, reported);
   * marginal argmax states bit-exact except where the reference profile's
     top-two margin is below 1e-9 (FP64) / 1e-5 (FP32);
-  * branch lengths 1e-6 relative + 1e-10 absolute (FP64 profiles / pairs);
+  * branch lengths 1e-6 relative + 1e-10 absolute (FP64 and FP32 profiles, pairs), or
+    equal objective values (1e-9 relative) where the objective is flat;
   * the iterative loops (optimize_tree_marginal, joint optimize_tree with
     pruning), whose Brent searches stop at TreeTime's loose early tolerances:
     branch lengths 1e-5 / 1e-4 relative + 1e-10, topology exact,
@@ -175,8 +176,8 @@ def test_marginal_branch_lengths_match_treetime(case, precision):
     anc.prepare_tree(tree_o)
     ores = anc.marginal(tree_o, gc.compressed_from(g, model_o), g["multiplicity"], model_o,
                         len(g["full_to_compressed"]), reconstruct_tip_states=bool(g["reconstruct_tip_states"]))
-    rel = 1e-6 if precision == "f64" else 2e-3
-    obj_rel = 1e-9 if precision == "f64" else 1e-6
+    rel = 1e-6  # FP32 profiles: Brent on the FP32 objective, then the Newton polish on its derivative
+    obj_rel = 1e-9
     for name, v, x in zip(names, g["mbl"], got):
         if abs(x - v) <= rel * abs(v) + 1e-10:
             continue

@@ -6,7 +6,8 @@ independent, so the pooled result is the result of one call).
 Workloads (seeded, ``treetime_gb300.synth``):
   * the 2,000-tip x 30,000-site nucleotide tree (90% invariant sites, 2,748
     patterns) through the public TreeAnc API: marginal in FP64 and FP32, joint,
-    and optimize_branch_lengths_joint on all 3,998 branches;
+    optimize_branch_lengths_joint on all 3,998 branches, and the profile-mode
+    (marginal) branch lengths of all branches from FP64 and FP32 profiles;
   * the 500-tip x 1,500-site protein tree under a site-specific model (TreeTime's
     default interpolated P(t)) through TreeAnc: marginal in FP64 and FP32, and
     joint;
@@ -148,6 +149,48 @@ def test_c1_joint_and_branch_lengths_match_oracle(c1, c1_oracle):
         assert abs(f(x) - f(v)) <= 1e-9 * abs(f(v)) + 1e-12, (k, x, v, f(x), f(v))
         flat += 1
     print("c1 joint branch lengths: %d of 3998 differ beyond 1e-6 with equal objective values" % flat)
+
+
+@pytest.fixture(scope="module")
+def c1_marginal_lengths(c1):
+    wl, nwk = c1
+    t = _treeanc(wl, nwk, "f64")
+    d = t.data
+    return parallel.marginal_branch_lengths(nwk, d.sequence_names, d.compressed_codes, d.multiplicity(), wl["gtr"],
+                                            d.full_length)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_c1_marginal_branch_lengths_match_oracle(c1, c1_marginal_lengths, precision):
+    """Profile-mode branch lengths (optimal_marginal_branch_length, tol 1e-10) of
+    all 3,998 branches after a marginal reconstruction: 1e-6 relative + 1e-10
+    absolute, or equal objective values (1e-9 relative, with the oracle's FP64
+    profiles) where the objective is flat enough that its argmin is rounding
+    noise.  The FP32 path searches on its FP32 objective and then polishes the
+    root of the objective's derivative."""
+    wl, nwk = c1
+    want = c1_marginal_lengths
+    t = _treeanc(wl, nwk, precision)
+    t.infer_ancestral_sequences(marginal=True)
+    nodes = {n.name: n for n in t.tree.find_clades()}
+    names = sorted(want)
+    got = dict(zip(names, t._marginal_branch_lengths([nodes[k] for k in names], 1e-10)))
+    far = [k for k in names if abs(got[k] - want[k]) > 1e-6 * abs(want[k]) + 1e-10]
+    if far:
+        from treetime_gb300.tree import parse_newick
+        d = t.data
+        tree_o = anc.prepare_tree(parse_newick(nwk))
+        aln = {k: d.compressed_codes[i].view("S1").astype("U1") for i, k in enumerate(d.sequence_names)}
+        ores = anc.marginal(tree_o, aln, d.multiplicity(), wl["gtr"], d.full_length)
+        for k in far:
+            pp, pc = ores["outgroup_LH"][k], ores["subtree_LH"][k]
+            f = lambda tt: -anc.prob_t_profiles(wl["gtr"], (pp, pc), d.multiplicity(), tt, return_log=True) \
+                + np.exp(tt * tt / 1e4)
+            assert abs(f(got[k]) - f(want[k])) <= 1e-9 * abs(f(want[k])) + 1e-12, (k, got[k], want[k])
+    rel = np.array([abs(got[k] - want[k]) / max(abs(want[k]), 1e-300) for k in names])
+    print("c1 marginal branch lengths %s: median relative difference %.2e, 99th percentile %.2e, %d of %d beyond "
+          "1e-6 with equal objective values" % (precision, np.median(rel), np.percentile(rel, 99), len(far),
+                                                len(names)))
 
 
 # ------------------------------------------------------------------ protein, site-specific

@@ -87,6 +87,8 @@ _SIGS = {
     "tt_joint_noalloc": (i32, [P(TTForest), P(TTModel), i64, vp, vp, vp, vp, vp, i32, i32, vp, vp]),
     "tt_ss_pstack": (i32, [P(TTSSModel), i32, vp, vp]),
     "tt_joint_ss": (i32, [P(TTForest), P(TTSSModel), vp, i32, i32, i32, P(TTJointOut), vp, vp]),
+    "tt_mutation_counts_ss": (i32, [P(TTForest), P(TTSSModel), i32, i32, i64, vp, vp, vp, vp, vp, i32, vp, vp, vp,
+                                    i64, vp]),
     "tt_state_pairs": (i32, [P(TTForest), vp, vp, i32, i32, i32, vp, vp, vp]),
     "tt_optimal_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), f64, vp, vp, vp]),
     "tt_prob_t_pairs": (i32, [i32, i64, vp, vp, P(TTModel), vp, vp, vp]),

@@ -754,10 +754,18 @@ class GPUAncMixin:
         layout, forest = sess["layout"], sess["forest"]
         nodes = self._counting_branches()
         t = engine.torch()
+        if marginal and self.gtr.is_site_specific:
+            n_ija = T_ia = None
+            d = engine._to_dev
+            dev = forest.device
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
+                n1, T1 = engine.mutation_counts_ss(forest, self.gtr, sess["bufs"], d(np.asarray(kk, np.int32), dev),
+                                                   pp, d(np.asarray(pp_row, np.int64), dev), pc,
+                                                   d(np.asarray(pc_row, np.int64), dev), self._gpu_precision())
+                n_ija = n1 if n_ija is None else n_ija + n1
+                T_ia = T1 if T_ia is None else T_ia + T1
+            return n_ija, T_ia
         if marginal:
-            if self.gtr.is_site_specific:
-                raise NotImplementedError("marginal GTR inference from a site-specific model is not supported "
-                                          "on the GPU")
             model = engine.model_for(self.gtr, getattr(self, "device", None))
             engine.branch_pmats(forest, model, sess["bufs"])
             p64 = sess["bufs"].cache[("p64", t.float64)]
@@ -860,12 +868,19 @@ class GPUAncMixin:
             new = dict(zip([id(n) for n in nodes], self._marginal_branch_lengths(nodes, tol))) if nodes else {}
             if special:
                 n1, n2 = root.clades
-                prof_c = n1.marginal_subtree_LH
-                tmp = n2.marginal_subtree_LH * root.marginal_outgroup_LH
-                prof_p = np.einsum("ai,a->ai", tmp, 1.0 / tmp.sum(axis=1))
                 m1, m2 = getattr(n1, "mask", None), getattr(n2, "mask", None)
-                mult = self.data.multiplicity() if m1 is None or m2 is None else self.data.multiplicity(mask=m1 * m2)
-                new_bl = engine.optimal_t_compressed(self.gtr, (prof_p, prof_c), mult, profiles=True, tol=tol)
+                if self._gpu_precision() == "f32" and (m1 is None or m2 is None) and not self.gtr.is_site_specific:
+                    # from the FP32 rows on the device, as the serving loop does
+                    new_bl = float(self._root_pair(n1, n2).optimal_t(
+                        engine.model_for(self.gtr, getattr(self, "device", None)), self._last[1]["partial"],
+                        self.gtr.gap_index, tol)[0].item())
+                else:
+                    prof_c = n1.marginal_subtree_LH
+                    tmp = n2.marginal_subtree_LH * root.marginal_outgroup_LH
+                    prof_p = np.einsum("ai,a->ai", tmp, 1.0 / tmp.sum(axis=1))
+                    mult = self.data.multiplicity() if m1 is None or m2 is None else \
+                        self.data.multiplicity(mask=m1 * m2)
+                    new_bl = engine.optimal_t_compressed(self.gtr, (prof_p, prof_c), mult, profiles=True, tol=tol)
                 # TreeTime's loop meets the pair at both children (treetime/treeanc.py:1318-1341) and
                 # applies the damped update at each visit, the second from the first's lengths
                 for _visit in range(2):
@@ -889,6 +904,18 @@ class GPUAncMixin:
             if deltaLH < LHtol:
                 break
         return ttconf.SUCCESS
+
+    def _root_pair(self, n1, n2):
+        """engine.RootPair of the session's tree (cached with the session)."""
+        sess = self._get_session()
+        rp = sess.get("root_pair")
+        lay = sess["layout"]
+        k1, k2 = lay.local[id(n1)], lay.local[id(n2)]
+        if rp is None or (rp.n1, rp.n2) != (k1, k2):
+            ti = sess["forest"].inputs[0]
+            rp = engine.RootPair(sess["forest"], lay, k1, k2, ti.tip_codes, ti.tip_row)
+            sess["root_pair"] = rp
+        return rp
 
     def _prob_zero_reparented(self, sess, node, states):
         """Probability at distance zero of `node`'s states given its current

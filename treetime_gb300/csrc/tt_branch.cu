@@ -911,6 +911,10 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
     __shared__ int hwarp[32];
     __shared__ float lutS[256 * Q];
     __shared__ int go, lead_w, help_w;
+    // the Newton polish: FP32 eigenvectors, mu lam_k, exp(mu lam_k t) and the parts of L'(t), L''(t)
+    __shared__ float Pd1[Q * Q], Pd2[Q * Q];
+    __shared__ double cd[Q], hd1, hd2;
+    __shared__ float2 redq[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int w = a.f.width;
     for (int j = threadIdx.x; j < 129; j += blockDim.x) {
@@ -1260,6 +1264,94 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
             hi = sacc;
             lo = -c;
         };
+        // this thread's compensated sums of w r'/r and w (r''/r - (r'/r)^2) over its patterns, with
+        // r = pc.P(t).pp + 1e-24, r' = pc.P'(t).pp, r'' = pc.P''(t).pp: the pattern terms of L'(t) and
+        // L''(t) for the Newton polish.  P, P' = V diag(c e^{ct}) V^-1 and P'' (c = mu lam) are formed
+        // in FP64 by the search warp and kept as FP32, so r, a sum of non-negative terms, keeps FP32's
+        // relative precision even where it is small (a pattern whose states differ across a short
+        // branch); the heavy patterns are the helper's, in FP64.
+        auto pattern_deriv = [&](float& h1, float& l1, float& h2, float& l2) {
+            float s1 = 0.0f, c1 = 0.0f, s2 = 0.0f, c2 = 0.0f;
+            float M0[Q * Q], M1[Q * Q], M2[Q * Q];
+#pragma unroll
+            for (int e = 0; e < Q * Q; ++e) { M0[e] = Pt[e]; M1[e] = Pd1[e]; M2[e] = Pd2[e]; }
+            auto add = [&](const float* pa, const float* pb, float wgt) {
+                float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < Q; ++j) {
+                        v0 = fmaf(M0[i * Q + j], pb[j], v0);
+                        v1 = fmaf(M1[i * Q + j], pb[j], v1);
+                        v2 = fmaf(M2[i * Q + j], pb[j], v2);
+                    }
+                    r0 = fmaf(pa[i], v0, r0);
+                    r1 = fmaf(pa[i], v1, r1);
+                    r2 = fmaf(pa[i], v2, r2);
+                }
+                const float inv = 1.0f / (r0 + 1e-24f);
+                const float xq = r1 * inv;
+                const float v1 = wgt * xq - c1, t1 = s1 + v1;
+                c1 = (t1 - s1) - v1;
+                s1 = t1;
+                const float v2 = wgt * (r2 * inv - xq * xq) - c2, t2 = s2 + v2;
+                c2 = (t2 - s2) - v2;
+                s2 = t2;
+            };
+            if (staged) {
+                for (int p = rank; p < P; p += n_sum) {
+                    float pa[Q], pb[Q];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) {
+                        pb[i] = ppS[p * Q + i];
+                        pa[i] = pcS[p * Q + i];
+                    }
+                    add(pa, pb, wS[p]);
+                }
+            } else {
+                for (int p = rank; p < P; p += n_sum) {
+                    float pa[Q], pb[Q], wgt, m32;
+                    fetch32(p, pa, pb, wgt, m32);
+                    if (wgt > 0.5f * kHeavyWeight && H > 0 && listed(p)) continue;  // the helper's
+                    add(pa, pb, wgt);
+                }
+            }
+            h1 = s1; l1 = -c1; h2 = s2; l2 = -c2;
+        };
+        auto warp_part_deriv = [&]() {
+            float h1 = 0.0f, l1 = 0.0f, h2 = 0.0f, l2 = 0.0f;
+            if (!(helper_busy && warp == help)) pattern_deriv(h1, l1, h2, l2);
+            warp_sum_pair(h1, l1);
+            warp_sum_pair(h2, l2);
+            if (lane == 0) {
+                redp[warp] = make_float2(h1, l1);
+                redq[warp] = make_float2(h2, l2);
+            }
+        };
+        auto heavy_deriv = [&]() {
+            double s1 = 0.0, s2 = 0.0;
+            for (int h = lane; h < H; h += 32) {
+                double r0 = 0.0, r1 = 0.0, r2 = 0.0;
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                    const double ue = hu[h][k] * Ed[k];
+                    r0 += ue;
+                    r1 = fma(ue, cd[k], r1);
+                    r2 = fma(ue * cd[k], cd[k], r2);
+                }
+                const double inv = 1.0 / (r0 + kSuperTiny);
+                const double xq = r1 * inv;
+                s1 = fma(hw[h], xq, s1);
+                s2 = fma(hw[h], r2 * inv - xq * xq, s2);
+            }
+            s1 = warp_sum(s1);
+            s2 = warp_sum(s2);
+            if (lane == 0) {
+                hd1 = s1;
+                hd2 = s2;
+            }
+        };
         // the warp's pair into redp[warp] (the helper, when busy, stores a zero pair)
         auto warp_part = [&]() {
             float hi = 0.0f, lo = 0.0f;
@@ -1329,8 +1421,78 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
                 return tail - ((double)hi + (double)lo);
             };
             BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, a.tol, 500);
+            // Newton polish of t = s^2: the FP32 objective's rounding (~1e-4 on sums of ~1e4) leaves
+            // Brent's minimum of a flat objective up to ~1e-3 off; the root of the objective's
+            // derivative in t, -L'(t) + 2e-4 t exp(1e-4 t^2), is found to the rounding of the FP32
+            // rows instead (a few evaluations of L' and L'').  Only for tight tolerances (TreeTime's
+            // final 1e-10; its loose early iterations keep Brent's result), for a minimum away from
+            // t = 0, and while the steps stay small and the curvature positive.
+            double tt = r.x * r.x;
+            if (r.state == 0 && a.tol <= 1e-8 && tt > 1e-10) {
+                // probe: after a point where the objective increases and Newton leads below 0 (or the
+                // curvature is lost in rounding, as it is where no pattern changes across the branch),
+                // the derivative at t = 0 decides whether the minimum is the boundary t = 0
+                bool probe = false;
+                double saved = tt;
+                for (int it = 0; it < 4; ++it) {
+                    if (lane < Q) {
+                        Ed[lane] = exp(mulam * tt);
+                        cd[lane] = mulam;
+                    }
+                    __syncwarp();
+                    if (lane < Q * Q) {  // P, P', P'' at tt (FP64, kept as FP32)
+                        double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+#pragma unroll
+                        for (int k = 0; k < Q; ++k) {
+                            const double we = Wk[k] * Ed[k];
+                            v0 += we;
+                            v1 = fma(we, cd[k], v1);
+                            v2 = fma(we * cd[k], cd[k], v2);
+                        }
+                        Pt[lane] = fmaxf((float)v0, 0.0f);
+                        Pd1[lane] = (float)v1;
+                        Pd2[lane] = (float)v2;
+                    }
+                    if (lane == 0) go = 2;
+                    role_barrier();
+                    warp_part_deriv();
+                    role_barrier();
+                    float h1 = 0.0f, l1 = 0.0f, h2 = 0.0f, l2 = 0.0f;
+                    if (lane < nw) {
+                        h1 = redp[lane].x; l1 = redp[lane].y;
+                        h2 = redq[lane].x; l2 = redq[lane].y;
+                    }
+                    warp_sum_pair(h1, l1);
+                    warp_sum_pair(h2, l2);
+                    double d1 = (double)h1 + (double)l1, d2 = (double)h2 + (double)l2;
+                    if (helper_busy) {
+                        d1 += hd1;
+                        d2 += hd2;
+                    }
+                    const double e = exp(1e-4 * tt * tt);
+                    const double G = -d1 + 2e-4 * tt * e;
+                    const double Gp = -d2 + 2e-4 * e * (1.0 + 2e-4 * tt * tt);
+                    if (probe) {  // at t = 0: increasing from there on means the minimum is at 0
+                        tt = G >= 0.0 ? 0.0 : saved;
+                        probe = false;
+                        break;
+                    }
+                    if (G > 0.0 && (!(Gp > 0.0) || tt - G / Gp <= 0.0)) {
+                        saved = tt;
+                        tt = 0.0;
+                        probe = true;
+                        continue;
+                    }
+                    if (!(Gp > 0.0)) break;
+                    const double step = G / Gp;
+                    if (!(fabs(step) <= 0.1 * tt)) break;
+                    tt -= step;
+                    if (fabs(step) <= 1e-13 * tt) break;
+                }
+                if (probe) tt = saved;  // the probe at t = 0 was not reached
+            }
             if (lane == 0) {
-                a.t_out[b] = r.state == 0 ? r.x * r.x : hamming;
+                a.t_out[b] = r.state == 0 ? tt : hamming;
                 if (a.info) a.info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
                 go = 0;
             }
@@ -1339,8 +1501,13 @@ __global__ void __launch_bounds__(256, 2) optimal_t_profiles_f32_kernel(ProfPara
             while (true) {
                 role_barrier();
                 if (!go) break;
-                if (helper_busy && warp == help) heavy_part();
-                warp_part();
+                if (go == 2) {
+                    if (helper_busy && warp == help) heavy_deriv();
+                    warp_part_deriv();
+                } else {
+                    if (helper_busy && warp == help) heavy_part();
+                    warp_part();
+                }
                 role_barrier();
             }
         }

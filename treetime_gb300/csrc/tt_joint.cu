@@ -74,10 +74,11 @@ struct __align__(16) JStage {
 
 // out[j] = mk * max_i(mk * L[i][j] + in[i]) and its first argmax, for the lane's states j0..j0+S-1.
 // L: [Q][2][W] pairs (shared or global memory).  NaN is the maximum, as numpy's argmax has it.
+// Exact form: every candidate summed as a pair and compared as a pair.
 template <int Q, int W, int LPP, bool kGlobal>
-__device__ __forceinline__ void max_plus2(const float* L, const float (&ih)[W / LPP], const float (&il)[W / LPP],
-                                          float mk, int j0, float (&oh)[W / LPP], float (&ol)[W / LPP],
-                                          int (&oc)[W / LPP]) {
+__device__ __noinline__ void max_plus2_exact(const float* L, const float (&ih)[W / LPP],
+                                                const float (&il)[W / LPP], float mk, int j0, float (&oh)[W / LPP],
+                                                float (&ol)[W / LPP], int (&oc)[W / LPP]) {
     constexpr int S = W / LPP;
 #pragma unroll
     for (int s = 0; s < S; ++s) { oh[s] = 0.f; ol[s] = 0.f; oc[s] = 0; }
@@ -115,6 +116,70 @@ __device__ __forceinline__ void max_plus2(const float* L, const float (&ih)[W / 
 #pragma unroll
     for (int s = 0; s < S; ++s)
         if (j0 + s >= Q) { oh[s] = 0.f; ol[s] = 0.f; oc[s] = 0; }
+}
+
+// out[j] = mk * max_i(mk * L[i][j] + in[i]) and its first argmax, for the lane's states j0..j0+S-1.
+// L: [Q][2][W] pairs (shared or global memory).  NaN is the maximum, as numpy's argmax has it.
+//
+// Screened: every value here is <= 0 (logs of probabilities and their sums), so a candidate formed
+// from the high parts alone, c_i = hi(mk L[i][j]) + hi(in[i]), is within 3 * 2^-24 * |c_i| of its
+// exact value.  When the best screened candidate leads the runner-up by more than 2^-20 times the
+// runner-up's magnitude, it is also the exact maximum, and only its pair sum is formed; otherwise
+// (near-ties, NaN) every candidate is formed exactly, in the same order, as max_plus2_exact does.
+template <int Q, int W, int LPP, bool kGlobal>
+__device__ __forceinline__ void max_plus2(const float* L, const float (&ih)[W / LPP], const float (&il)[W / LPP],
+                                          float mk, int j0, float (&oh)[W / LPP], float (&ol)[W / LPP],
+                                          int (&oc)[W / LPP]) {
+    constexpr int S = W / LPP;
+    float bh[S], b2[S], bxh[S], bxl[S];
+    int bi[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) { bh[s] = -INFINITY; b2[s] = -INFINITY; bxh[s] = 0.f; bxl[s] = 0.f; bi[s] = 0; }
+#pragma unroll
+    for (int r = 0; r < LPP; ++r) {
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+            const int i = r * S + s2;
+            if (i >= Q) continue;
+            const float xh = LPP == 1 ? ih[s2] : __shfl_sync(0xffffffffu, ih[s2], r, LPP);
+            const float xl = LPP == 1 ? il[s2] : __shfl_sync(0xffffffffu, il[s2], r, LPP);
+            float rh[S];
+            if constexpr (kGlobal) ld_part_ro<S>(L + i * 2 * W + j0, rh);
+            else ld_part<S>(L + i * 2 * W + j0, rh);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const float c = (mk != 1.f ? rh[s] * mk : rh[s]) + xh;
+                if (c > bh[s]) {
+                    b2[s] = bh[s];
+                    bh[s] = c;
+                    bi[s] = i;
+                    bxh[s] = xh;
+                    bxl[s] = xl;
+                } else if (c > b2[s]) {
+                    b2[s] = c;
+                }
+            }
+        }
+    }
+    bool exact = false;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+        if (j0 + s < Q && !(bh[s] - b2[s] > 0x1p-20f * fabsf(b2[s]))) exact = true;
+    if constexpr (LPP > 1) exact = __any_sync(0xffffffffu, exact);
+    if (exact) {
+        max_plus2_exact<Q, W, LPP, kGlobal>(L, ih, il, mk, j0, oh, ol, oc);
+        return;
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        if (j0 + s >= Q) { oh[s] = 0.f; ol[s] = 0.f; oc[s] = 0; continue; }
+        const float* row = L + bi[s] * 2 * W + j0 + s;
+        float ph = kGlobal ? __ldg(row) : row[0], pl = kGlobal ? __ldg(row + W) : row[W];
+        if (mk != 1.f) dd_mulf(ph, pl, mk);
+        dd_add(ph, pl, bxh[s], bxl[s], oh[s], ol[s]);
+        if (mk != 1.f) dd_mulf(oh[s], ol[s], mk);
+        oc[s] = bi[s];
+    }
 }
 
 template <int S>

@@ -16,7 +16,7 @@
 // in the same step from their characters.  The root's step adds log(pi_a) and takes the first
 // argmax of the normalised exp profile (or an inverse-CDF draw); the backtrack runs one launch
 // per level top-down.
-#include "tt_internal.cuh"
+#include "tt_ss_common.cuh"
 
 namespace tt {
 
@@ -35,57 +35,6 @@ __device__ __forceinline__ double ssj_mask(const tt_forest& f, int64_t g, int p)
     const int64_t mo = __ldg(f.mask_off + g);
     return mo < 0 ? 1.0 : __ldg(f.masks + mo + p);
 }
-
-// Interpolation bracket of t on the grid (interp1d: searchsorted left, clipped to [1, n-1]).
-__device__ __forceinline__ void ssj_bracket(const tt_ss_model& m, double t, int& ilo, double& w) {
-    int lo = 0, hi = m.n_grid;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(m.grid + mid) < t) lo = mid + 1; else hi = mid;
-    }
-    const int ih = lo < 1 ? 1 : (lo > m.n_grid - 1 ? m.n_grid - 1 : lo);
-    ilo = ih - 1;
-    const double xl = __ldg(m.grid + ih - 1), xh = __ldg(m.grid + ih);
-    w = (t - xl) / (xh - xl);
-}
-
-// log(max(1e-12, P_a(t)[i][j])) of node g's branch at site a
-template <int Q>
-struct SSBranch {
-    bool interp;
-    int ilo;
-    double w, xl, xh, t;
-    double e[Q];  // exp(mu lam t) (exact form)
-    __device__ __forceinline__ void init(const tt_ss_model& m, int a, double bl) {
-        t = bl;
-        interp = m.approximate && m.stack && bl * m.rate_scale < 10.0;
-        if (interp) {
-            ssj_bracket(m, bl, ilo, w);
-            xl = __ldg(m.grid + ilo);
-            xh = __ldg(m.grid + ilo + 1);
-        } else {
-            const double mu = __ldg(m.mu + a);
-#pragma unroll
-            for (int k = 0; k < Q; ++k) e[k] = exp(bl * mu * __ldg(m.lam + (int64_t)a * Q + k));
-        }
-    }
-    __device__ __forceinline__ double logp(const tt_ss_model& m, int a, int L, int i, int j) const {
-        double p;
-        if (interp) {
-            const int64_t qq = (int64_t)Q * Q;
-            const double yl = __ldg(m.stack + ((int64_t)ilo * qq + i * Q + j) * L + a);
-            const double yh = __ldg(m.stack + ((int64_t)(ilo + 1) * qq + i * Q + j) * L + a);
-            p = (yh - yl) / (xh - xl) * (t - xl) + yl;
-        } else {
-            const double* V = m.V + (int64_t)a * Q * Q + i * Q;
-            const double* Vi = m.Vinv + (int64_t)a * Q * Q + j;
-            p = 0.0;
-#pragma unroll
-            for (int k = 0; k < Q; ++k) p = fma(__ldg(V + k) * e[k], __ldg(Vi + k * Q), p);
-        }
-        return log(p > kTiny ? p : kTiny);
-    }
-};
 
 // log(max(profile, 1e-12)) of a tip's character; non-finite -> -1e10; no sequence -> zeros
 template <int Q>

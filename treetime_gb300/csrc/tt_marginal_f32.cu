@@ -31,7 +31,8 @@ namespace tt {
 // at a time (all loads of the D nodes are issued before any of them is computed).  A pattern
 // count that is not a multiple of 32 makes warps straddle two or three nodes, which costs a
 // second shared-memory wavefront for matrix rows and nothing else.
-template <int Q, int W, int LPP, int NT, int D, int MINB>
+// HM: the forest has per-branch masks (a second instance without any mask code serves the rest).
+template <int Q, int W, int LPP, int NT, int D, int MINB, bool HM>
 __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     constexpr int S = W / LPP;
     constexpr int CH = StageCfg<Q, W>::kChunk;
@@ -65,7 +66,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         }
         onehot_s[c] = (signed char)(ok && ones == 1 ? st1 : -1);
     }
-    const bool has_masks = a.f.mask_off != nullptr;
+    constexpr bool has_masks = HM;
     float* partial = reinterpret_cast<float*>(a.o.partial);
     float* posterior = reinterpret_cast<float*>(a.o.posterior);
     const float* pm = reinterpret_cast<const float*>(a.pmat);
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                             child_xd(ca[d], xa[d], &st.mat[i][0], d0);
                             child_xd(cb[d], xb[d], &st.mat[i][QW], d1);
                             float m0 = 1.f, m1 = 1.f;
-                            if (has_masks) {
+                            if constexpr (has_masks) {
                                 const int4 cp = st.pair[i];
                                 m0 = mask_of(cp.x, xa[d]);
                                 m1 = mask_of(cp.z, xb[d]);
@@ -432,11 +433,25 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         if (tips) lut_part(code[d], x[d]);
                         const float* Pk = &st.mat[i][0];  // D = P - I of the branch above k
                         float msg[S], o[S];
-                        s_vec_mat<Q, W, LPP>(x[d], Pk, j0, msg);
+                        // one lane per pattern: the matrix rows are read once for both products
+                        float Dr[LPP == 1 ? Q : 1][LPP == 1 ? W : 1];
+                        if constexpr (LPP == 1) {
 #pragma unroll
-                        for (int s = 0; s < S; ++s) msg[s] += x[d][s];
+                            for (int r = 0; r < Q; ++r) ld_part<W>(Pk + r * W, Dr[r]);
+#pragma unroll
+                            for (int s = 0; s < S; ++s) {
+                                float acc = x[d][s];
+#pragma unroll
+                                for (int r = 0; r < Q; ++r) acc = fmaf(x[d][r], Dr[r][s], acc);
+                                msg[s] = s < Q ? acc : 0.f;
+                            }
+                        } else {
+                            s_vec_mat<Q, W, LPP>(x[d], Pk, j0, msg);
+#pragma unroll
+                            for (int s = 0; s < S; ++s) msg[s] += x[d][s];
+                        }
                         float m = 1.f;
-                        if (has_masks) {
+                        if constexpr (has_masks) {
                             const int64_t mo = __ldg(a.f.mask_off + nb + k);
                             if (mo >= 0) m = (float)__ldg(a.f.masks + mo + pc);
                         }
@@ -467,10 +482,20 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                         }
                         if (tips && !a.o.reconstruct_tips) continue;
                         float ev[S];
-                        s_mat_vec<Q, W, LPP>(Pk, o, j0, ev);
-                        float s2 = 0.f;
+                        if constexpr (LPP == 1) {
 #pragma unroll
-                        for (int s = 0; s < S; ++s) ev[s] += o[s];
+                            for (int s = 0; s < S; ++s) {
+                                float acc = o[s];
+#pragma unroll
+                                for (int c2 = 0; c2 < Q; ++c2) acc = fmaf(Dr[s < Q ? s : 0][c2], o[c2], acc);
+                                ev[s] = s < Q ? acc : 0.f;
+                            }
+                        } else {
+                            s_mat_vec<Q, W, LPP>(Pk, o, j0, ev);
+#pragma unroll
+                            for (int s = 0; s < S; ++s) ev[s] += o[s];
+                        }
+                        float s2 = 0.f;
 #pragma unroll
                         for (int s = 0; s < S; ++s) {
                             if (m != 1.f && j0 + s < Q) ev[s] = m * ev[s] + (1.f - m);
@@ -527,8 +552,8 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     }
 }
 
-template <int Q, int LPP, int NT, int D, int MINB>
-static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
+template <int Q, int LPP, int NT, int D, int MINB, bool HM>
+static tt_status launch_f32_hm(const F32Params& prm, int blocks, cudaStream_t s) {
     constexpr int W = round4(Q);
     static_assert(W % LPP == 0, "width must split over the lanes of a pattern");
     const size_t dyn = 2 * sizeof(Stage<Q, W>);
@@ -537,7 +562,7 @@ static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || dyn > configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(marginal_f32_kernel<Q, W, LPP, NT, D, MINB>,
+        cudaError_t e = cudaFuncSetAttribute(marginal_f32_kernel<Q, W, LPP, NT, D, MINB, HM>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
         if (e != cudaSuccess) {
             set_error("tt_marginal(f32): %zu bytes of shared memory: %s", dyn, cudaGetErrorString(e));
@@ -545,8 +570,14 @@ static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
         }
         if (dev >= 0 && dev < 64) configured[dev] = dyn;
     }
-    marginal_f32_kernel<Q, W, LPP, NT, D, MINB><<<blocks, NT, dyn, s>>>(prm);
+    marginal_f32_kernel<Q, W, LPP, NT, D, MINB, HM><<<blocks, NT, dyn, s>>>(prm);
     return check_launch("tt_marginal(f32)");
+}
+
+template <int Q, int LPP, int NT, int D, int MINB>
+static tt_status launch_f32(const F32Params& prm, int blocks, cudaStream_t s) {
+    return prm.m.f.mask_off != nullptr ? launch_f32_hm<Q, LPP, NT, D, MINB, true>(prm, blocks, s)
+                                       : launch_f32_hm<Q, LPP, NT, D, MINB, false>(prm, blocks, s);
 }
 
 tt_status launch_marginal_f32(int q, int threads, int ctas_per_sm, const MargParams& prm, const int4* items,

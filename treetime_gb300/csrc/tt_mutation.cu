@@ -12,7 +12,7 @@
 // Accumulation is deterministic: the branches are split into `chunks` contiguous chunks, each
 // (pattern, chunk) is summed by one thread (or warp) in branch order into its own slice of the
 // workspace, and a second kernel adds the chunk slices in chunk order.
-#include "tt_internal.cuh"
+#include "tt_ss_common.cuh"
 
 namespace tt {
 
@@ -323,6 +323,62 @@ __global__ void __launch_bounds__(256) mut_joint_kernel(MutParams a) {
 }
 
 // Sum of the chunk slices in chunk order: n_ija from rows [0, q*q), T_ia from rows [q*q, q*q + q).
+// Marginal mode under a site-specific model: one thread per (pattern, chunk of branches); per
+// branch the pattern's own P_a(t) + 1e-24 (treetime/treeanc.py:1104-1107, gtr_site_specific.py:
+// 367-371), formed entry by entry twice -- once for the normaliser, once for the counts -- with
+// the row and column sums of M kept for T.  FP64.
+template <int Q>
+__global__ void __launch_bounds__(128) mut_marginal_ss_kernel(MutParams a, tt_ss_model sm) {
+    const tt_tree tr = a.f.trees[a.tree];
+    const int P = a.P;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (p >= P) return;
+    constexpr int QQ = Q * Q;
+    double* out = a.part + (int64_t)c * a.rows * P + p;
+    for (int e = 0; e < QQ + Q; ++e) out[(int64_t)e * P] = 0.0;
+    const int64_t b0 = c * a.chunk_len;
+    const int64_t b1 = b0 + a.chunk_len < a.n ? b0 + a.chunk_len : a.n;
+    const int site = tr.pat_base + p;
+    for (int64_t b = b0; b < b1; ++b) {
+        const int64_t g = a.node_of[b];
+        const BranchRows rr = branch_rows(a, tr, b, p);
+        double pp[Q], pc[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            pp[j] = rr.parent(j);
+            pc[j] = rr.child(j);
+        }
+        const double t = a.f.bl[g];
+        SSBranch<Q> br;
+        br.init(sm, site, t);
+        double tot = 0.0;
+        for (int i = 0; i < Q; ++i) {
+            double v = 0.0;
+            for (int j = 0; j < Q; ++j) v = fma(br.prob(sm, site, a.f.n_patterns, i, j) + kSuperTiny, pp[j], v);
+            tot = fma(pc[i], v, tot);
+        }
+        const double cw = branch_weight(a, tr, g, p) / tot;
+        const double h = 0.5 * t * cw;
+        double colsum[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) colsum[j] = 0.0;
+        for (int i = 0; i < Q; ++i) {
+            double rowsum = 0.0;
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                const double m = pc[i] * pp[j] * (br.prob(sm, site, a.f.n_patterns, i, j) + kSuperTiny);
+                out[(int64_t)(i * Q + j) * P] += cw * m;
+                rowsum += m;
+                colsum[j] += m;
+            }
+            out[(int64_t)(QQ + i) * P] += h * rowsum;
+        }
+#pragma unroll
+        for (int j = 0; j < Q; ++j) out[(int64_t)(QQ + j) * P] += h * colsum[j];
+    }
+}
+
 __global__ void mut_reduce_kernel(const double* __restrict__ part, int chunks, int rows, int P, int q,
                                   double* __restrict__ n_ija, double* __restrict__ T_ia) {
     const int qq = q * q;
@@ -472,6 +528,67 @@ extern "C" tt_status tt_mutation_counts(const tt_forest* f, const tt_model* m, i
     if (blocks > sm_count() * 16) blocks = sm_count() * 16;
     mut_reduce_kernel<<<blocks, 256, 0, s>>>(a.part, a.chunks, rows, P, q, n_ija, T_ia);
     return check_launch("tt_mutation_counts (reduce)");
+}
+
+extern "C" tt_status tt_mutation_counts_ss(const tt_forest* f, const tt_ss_model* sm, int32_t tree,
+                                           int32_t n_patterns, int64_t n, const int32_t* node_of, const void* pp,
+                                           const int64_t* pp_row, const void* pc, const int64_t* pc_row,
+                                           int32_t prec, double* n_ija, double* T_ia, double* workspace,
+                                           int64_t workspace_bytes, void* stream) {
+    if (!valid_tree(f, tree) || !sm || n < 0 || n_patterns < 0 || !n_ija || !T_ia || !sm->lut || !sm->mu ||
+        !sm->lam || !sm->V || !sm->Vinv || sm->n_states != f->n_states || (sm->approximate && !sm->stack) ||
+        (n > 0 && (!node_of || !pp || !pp_row || !pc_row))) {
+        set_error("tt_mutation_counts_ss: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    const int q = f->n_states, P = n_patterns;
+    if (P == 0) return TT_OK;
+    const int rows = q * q + q;
+    const int chunks = workspace ? fit_chunks(workspace_bytes, rows, P, want_chunks(n > 0 ? n : 1, P, 1)) : 0;
+    if (chunks < 1) {
+        set_error("tt_mutation_counts_ss: workspace smaller than (q*q+q)*patterns doubles");
+        return TT_ERR_OOM;
+    }
+    MutParams a{};
+    a.f = *f;
+    a.m.lut = sm->lut;
+    a.m.n_states = q;
+    a.tree = tree;
+    a.P = P;
+    a.n = n;
+    a.node_of = node_of;
+    a.pp = pp;
+    a.pp_row = pp_row;
+    a.pc = pc;
+    a.pc_row = pc_row;
+    a.prec = prec;
+    a.part = workspace;
+    a.rows = rows;
+    a.chunks = chunks;
+    a.chunk_len = n > 0 ? (n + chunks - 1) / chunks : 0;
+    cudaStream_t s = as_stream(stream);
+    if (n > 0) {
+        dim3 grid((P + 127) / 128, chunks);
+        switch (q) {
+            case 4: mut_marginal_ss_kernel<4><<<grid, 128, 0, s>>>(a, *sm); break;
+            case 20: mut_marginal_ss_kernel<20><<<grid, 128, 0, s>>>(a, *sm); break;
+            case 21: mut_marginal_ss_kernel<21><<<grid, 128, 0, s>>>(a, *sm); break;
+            case 22: mut_marginal_ss_kernel<22><<<grid, 128, 0, s>>>(a, *sm); break;
+            default:
+                set_error("tt_mutation_counts_ss: alphabet size %d not compiled (4, 20, 21, 22)", q);
+                return TT_ERR_UNSUPPORTED;
+        }
+        tt_status st = check_launch("tt_mutation_counts_ss");
+        if (st != TT_OK) return st;
+    } else {
+        cudaMemsetAsync(a.part, 0, (size_t)rows * P * sizeof(double), s);
+        a.chunks = 1;
+    }
+    const int64_t total = (int64_t)rows * P;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > sm_count() * 16) blocks = sm_count() * 16;
+    mut_reduce_kernel<<<blocks, 256, 0, s>>>(a.part, a.chunks, rows, P, q, n_ija, T_ia);
+    return check_launch("tt_mutation_counts_ss (reduce)");
 }
 
 extern "C" tt_status tt_mutation_counts_joint(const tt_forest* f, int32_t tree, int32_t n_patterns, int64_t n,

@@ -927,6 +927,48 @@ def optimal_t_profiles_dev(forest, model, d_node, pp, d_pp_row, pc, d_pc_row, pr
     return tout, info
 
 
+class RootPair:
+    """The bifurcating root's two children as one branch (treetime/treeanc.py:
+    1317-1339) on the device: Brent in profile mode between the first child's
+    subtree profile and the second child's subtree profile times the root's
+    outgroup (pi), normalised, from the FP32 rows of a marginal
+    reconstruction.  Holds the small index arrays of one tree (uploaded once)."""
+
+    def __init__(self, forest, layout, n1, n2, tip_codes, tip_row):
+        t = torch()
+        P = forest.inputs[0].n_patterns if len(forest.inputs) == 1 else None
+        if P is None:
+            raise ValueError("RootPair takes a forest of one tree")
+        self.forest, self.n1, self.n2, self.P = forest, int(n1), int(n2), P
+        dev = forest.device
+        up = Uploader()
+        up.add("n1", np.array([n1], np.int32))
+        up.add("n1_row", np.array([n1 * P if n1 < layout.n_int else -1], np.int64))
+        up.add("zero_row", np.zeros(1, np.int64))
+        self.n2_is_tip = n2 >= layout.n_int
+        if self.n2_is_tip:
+            r = int(tip_row[n2 - layout.n_int])
+            up.add("n2_codes", np.ascontiguousarray(tip_codes[r] if r >= 0 else np.zeros(P, np.uint8)))
+        self.d = up.finish(dev)
+        self._pp = t.empty((P, forest.w), dtype=t.float32, device=dev)
+
+    def optimal_t(self, model, partial, gap_state, tol):
+        """Device tensor [1]: the pair's optimal total length (enqueued only)."""
+        t = torch()
+        q, P = self.forest.q, self.P
+        if not self.n2_is_tip:
+            x2 = partial[self.n2 * P:(self.n2 + 1) * P, :q].to(t.float64)
+        else:
+            x2 = model.lut[self.d["n2_codes"].long()]
+        y = x2 * model.pi[0][None, :]
+        y = y / y.sum(dim=1, keepdim=True)
+        self._pp.zero_()
+        self._pp[:, :q].copy_(y)
+        tn, _ = optimal_t_profiles_dev(self.forest, model, self.d["n1"], self._pp, self.d["zero_row"], partial,
+                                       self.d["n1_row"], "f32", gap_state, True, tol)
+        return tn
+
+
 _PROFILE_WS = {}
 
 
@@ -1087,6 +1129,26 @@ def mutation_counts(forest, model, p64, tree, d_node, pp, d_pp_row, pc, d_pc_row
                                  _p(d_pp_row), _p(pc), _p(d_pc_row),
                                  _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(p64), _p(n_ija),
                                  _p(T_ia), _p(ws), ws_bytes, _stream()), "tt_mutation_counts")
+    return n_ija, T_ia
+
+
+def mutation_counts_ss(forest, gtr, bufs, d_node, pp, d_pp_row, pc, d_pc_row, precision):
+    """mutation_counts under a GTR_site_specific model (one tree): every
+    site's own P_a(t) (TreeTime's interpolated or exact expQt), FP64."""
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    q = forest.q
+    P = int(forest.trees_host["n_patterns"][0])
+    n = int(d_node.numel())
+    arrs = _ss_model64(gtr, bufs, dev, need_stack=True)
+    n_ija = t.empty((q, q, P), dtype=t.float64, device=dev)
+    T_ia = t.empty((q, P), dtype=t.float64, device=dev)
+    ws, ws_bytes = _mutation_workspace(dev, q * q + q, P, n, 1)
+    check(lib.tt_mutation_counts_ss(C.byref(forest.struct), C.byref(arrs["struct"]), 0, P, n, _p(d_node), _p(pp),
+                                    _p(d_pp_row), _p(pc), _p(d_pc_row),
+                                    _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(n_ija),
+                                    _p(T_ia), _p(ws), ws_bytes, _stream()), "tt_mutation_counts_ss")
     return n_ija, T_ia
 
 

@@ -5,12 +5,22 @@ TreeTime's ancestral / branch-length cycle:
 
   * ``"marginal"``: marginal ancestral reconstruction, repeated (FP32 kernel;
     the site-specific kernel for ``GTR_site_specific`` models);
-  * ``"optimize"``: marginal reconstruction, then profile-mode Brent on every
-    branch below the root from the outgroup and subtree profiles
-    (``optimal_marginal_branch_length``, treetime/treeanc.py:1272-1295) and the
-    damped update of ``optimize_tree_marginal`` (treetime/treeanc.py:1297-1360,
-    damping 0.75; the root's two children are optimised independently rather
-    than as one combined branch), repeated on the new branch lengths.
+  * ``"optimize"``: TreeTime's ``optimize_tree_marginal`` (treetime/treeanc.py:
+    1297-1360) with its loop run for a fixed number of iterations (no
+    log-likelihood stop): marginal reconstruction, then profile-mode Brent on
+    every branch below the root from the outgroup and subtree profiles
+    (``optimal_marginal_branch_length``, treetime/treeanc.py:1272-1295) with the
+    damped update (0.75^(i+1), tolerance 1e-8 + 0.01^(i+1)); a bifurcating
+    root's two children are one branch, optimised from the first child's subtree
+    profile and the second's times the root's outgroup, and its update is applied
+    at the visit of each child, as TreeTime's loop does;
+  * ``"joint"``: TreeTime's ``optimize_tree`` in its default joint mode without
+    pruning (treetime/treeanc.py:1384-1473): joint reconstruction, then Brent on
+    every branch's (parent, child) state-pair counts
+    (``optimize_branch_lengths_joint``, :1176-1242), ``iterations`` rounds.
+    TreeTime stops early when a reconstruction changes no state; the rounds
+    after that reproduce the same states and lengths, so running them all gives
+    its result.
 
 The scheduler runs on the calling thread.  Jobs are admitted in arrival order
 while a slot is free and the job's device footprint fits the memory budget
@@ -37,7 +47,7 @@ import numpy as np
 
 from . import engine
 
-KINDS = ("marginal", "optimize")
+KINDS = ("marginal", "optimize", "joint")
 
 
 class Job:
@@ -53,8 +63,10 @@ class Job:
     def __init__(self, inputs, gtr, kind="marginal", iterations=3, job_id=None):
         if kind not in KINDS:
             raise ValueError("kind must be one of %s" % (KINDS,))
-        if kind == "optimize" and getattr(gtr, "is_site_specific", False):
+        if kind != "marginal" and getattr(gtr, "is_site_specific", False):
             raise NotImplementedError("branch-length jobs need a standard GTR model")
+        if kind == "optimize" and inputs.masks:
+            raise NotImplementedError("branch-length jobs with masks are not supported in the serving loop")
         engine.check_alphabet(gtr.n_states, getattr(gtr, "is_site_specific", False))
         self.inputs = inputs
         self.gtr = gtr
@@ -186,16 +198,34 @@ class _Active:
             if job.kind == "optimize":
                 self._prepare_optimize(dev)
                 hs["admit.optimize_setup"] += time.perf_counter() - t1
+            elif job.kind == "joint":
+                self._prepare_joint(dev)
+                hs["admit.optimize_setup"] += time.perf_counter() - t1
         self.it = 0
         self.done_event = None
         self.host = None
         self.phase_events = [] if server.phase_events else None
+
+    def _prepare_joint(self, dev):
+        lay = self.job.inputs.layout
+        up = engine.Uploader()
+        up.add("char_state", engine.char_state_table(self.job.gtr))
+        up.add("bl", np.asarray(self.job.inputs.bl, np.float64))
+        d = up.finish(dev)
+        self.opt = dict(d, floor=engine.ttconf.MIN_BRANCH_LENGTH / float(self.job.inputs.mult.sum()),
+                        root=lay.n_int - 1)
 
     def _prepare_optimize(self, dev):
         t = engine.torch()
         lay, P = self.job.inputs.layout, self.job.inputs.n_patterns
         k = np.arange(lay.n_nodes)
         has_parent = np.asarray(lay.parent) >= 0
+        root = lay.n_int - 1
+        rc = lay.child_idx[lay.child_off[root]:lay.child_off[root + 1]]
+        pair = None
+        if len(rc) == 2:  # a bifurcating root: its two children are one branch
+            pair = (int(rc[0]), int(rc[1]))
+            has_parent = has_parent & (k != pair[0]) & (k != pair[1])
         internal = k[has_parent & (k < lay.n_int)]
         tips = k[has_parent & (k >= lay.n_int)]
         up = engine.Uploader()
@@ -205,7 +235,10 @@ class _Active:
         up.add("d_int", internal.astype(np.int64)).add("d_tip", tips.astype(np.int64))
         up.add("bl", np.asarray(self.job.inputs.bl, np.float64))
         d = up.finish(dev)
-        self.opt = dict(d, internal=len(internal) > 0, tips=len(tips) > 0,
+        rp = None
+        if pair is not None:
+            rp = engine.RootPair(self.forest, lay, pair[0], pair[1], self.job.inputs.tip_codes, self.job.inputs.tip_row)
+        self.opt = dict(d, internal=len(internal) > 0, tips=len(tips) > 0, pair=pair, root_pair=rp,
                         floor=engine.ttconf.MIN_BRANCH_LENGTH / float(self.job.inputs.mult.sum()))
 
     def enqueue_iteration(self):
@@ -216,7 +249,9 @@ class _Active:
         with t.cuda.stream(self.stream):
             if ev is not None:
                 ev.append(("start", self._event()))
-            if job.site_specific:
+            if job.kind == "joint":
+                out = engine.joint(self.forest, self.model, self.bufs, sync=False)
+            elif job.site_specific:
                 out = engine.marginal_site_specific(self.forest, job.gtr, self.bufs, precision="f32", sync=False)
             else:
                 keep = job.kind == "optimize"
@@ -228,6 +263,10 @@ class _Active:
                 ev.append(("marginal", self._event()))
             if job.kind == "optimize":
                 self._branch_lengths(out)
+                if ev is not None:
+                    ev.append(("branch_lengths", self._event()))
+            elif job.kind == "joint":
+                self._joint_lengths()
                 if ev is not None:
                     ev.append(("branch_lengths", self._event()))
             self.out = out
@@ -250,6 +289,49 @@ class _Active:
             prev = e
         return out
 
+    def _joint_lengths(self):
+        """optimize_branch_lengths_joint on the device: pair counts of every branch
+        from the last joint reconstruction (tips: their characters; gaps
+        ignored), truncated to integers, Brent on each, lengths max(0, t); the
+        model's lengths are floored at 1e-3 / L for the next reconstruction."""
+        import ctypes as C
+        t = engine.torch()
+        o = self.opt
+        q = self.job.gtr.n_states
+        gap = self.job.gtr.gap_index
+        hist = self.bufs.get("hist", (self.forest.n_nodes, q, q), t.float64)
+        hist.zero_()
+        states = self.bufs.get("states", (self.forest.state_rows,), t.uint8)
+        engine.check(engine._lib.load().tt_state_pairs(
+            C.byref(self.forest.struct), engine._p(states), engine._p(o["char_state"]), 0,
+            -1 if gap is None else int(gap), 1, None, engine._p(hist), engine._stream()), "tt_state_pairs")
+        tt, info = engine.optimal_t_pairs(q, t.trunc(hist), self.model, tol=1e-10)
+        new = t.clamp(tt, min=0.0)
+        new[o["root"]] = o["bl"][o["root"]]
+        o["bl"] = new
+        info = info.clone()
+        info[o["root"]] = 0  # the root has no branch (TreeTime does not optimise it)
+        bad = (info == -1).any().to(t.int32) * engine._lib.TT_ERR_BRACKET
+        self.status.copy_(t.maximum(self.status, bad.reshape(1)))
+        self.forest.d_bl.copy_(t.clamp(new, min=o["floor"]))
+
+    def _root_pair(self, out, tol, damp):
+        """The bifurcating root's children as one branch (treetime/treeanc.py:
+        1317-1339): Brent from the first child's subtree profile and the second
+        child's subtree profile times the root's outgroup (pi), normalised; the
+        damped update of the pair's total length, split in the current ratio,
+        applied twice (TreeTime's loop meets the pair at both children)."""
+        o = self.opt
+        n1, n2 = o["pair"]
+        tn = o["root_pair"].optimal_t(self.model, out["partial"], self.job.gtr.gap_index, tol)
+        bl = o["bl"]
+        for _visit in range(2):
+            total = bl[n1] + bl[n2]
+            ratio = bl[n1] / total
+            upd = tn[0] * (1 - damp) + total * damp
+            bl[n1] = upd * ratio
+            bl[n2] = upd * (1 - ratio)
+
     def _branch_lengths(self, out):
         t = engine.torch()
         o = self.opt
@@ -267,6 +349,9 @@ class _Active:
                                                   o["tip_rows"], out["partial"], o["no_rows"], "f32", gap, True, tol)
             new[o["d_tip"]] = tt * (1 - damp) + old[o["d_tip"]] * damp
         o["bl"] = new
+        if o["pair"] is not None:
+            self._root_pair(out, tol, damp)
+            new = o["bl"]
         self.forest.d_bl.copy_(t.clamp(new, min=o["floor"]))
 
     def enqueue_results(self):

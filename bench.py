@@ -1471,7 +1471,7 @@ def _joint_block(engine, t, forest, model, bufs, layout, P, args, flush):
             "roofline": {"bound": "hbm", "achieved": ab / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": ab / (kms * 1e-3) / 1e9 / peak, "peak_source": kind,
                          "kernel": "joint_kernel<Q=4,W=4,LPP=1,NT=%d>" % forest.threads, "kernel_ms": kms,
-                         "algorithmic_bytes_per_launch": ab},
+                         "algorithmic_bytes_per_launch": ab, "traffic": _traffic("joint_q4/c1")},
             "arithmetic": "double-float (FP32 pairs) max-plus; states checked against the oracle in tests"}
 
 

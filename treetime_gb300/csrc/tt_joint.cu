@@ -57,6 +57,10 @@ __device__ __forceinline__ void dd_mulf(float& h, float& l, float m) {
     l = e - (h - p);
 }
 
+// log(1e-12) = -27.6310211159285482..., rounded up a little so that a table entry formed by
+// another correctly rounded log of 1e-12 still counts as the floor
+constexpr double kLogTinyBound = -27.631021115928;
+
 template <int Q, int W>
 struct JStageCfg {
     static constexpr int kMatFloats = 2 * Q * 2 * W;       // two children's [Q][2][W]
@@ -72,24 +76,36 @@ struct __align__(16) JStage {
     float mat[JStageCfg<Q, W>::kChunk][JStageCfg<Q, W>::kMatFloats];
 };
 
+// A lane's S values as double-float pairs, and a max-plus result (pairs and argmaxes): passed to
+// and returned from the out-of-line exact form by value, so that they stay in registers (arrays
+// passed by reference would be written to the stack on every call, taken or not).
+template <int S>
+struct DDVec {
+    float h[S], l[S];
+};
+template <int S>
+struct MaxPlusOut {
+    float h[S], l[S];
+    int c[S];
+};
+
 // out[j] = mk * max_i(mk * L[i][j] + in[i]) and its first argmax, for the lane's states j0..j0+S-1.
 // L: [Q][2][W] pairs (shared or global memory).  NaN is the maximum, as numpy's argmax has it.
 // Exact form: every candidate summed as a pair and compared as a pair.
 template <int Q, int W, int LPP, bool kGlobal>
-__device__ __noinline__ void max_plus2_exact(const float* L, const float (&ih)[W / LPP],
-                                                const float (&il)[W / LPP], float mk, int j0, float (&oh)[W / LPP],
-                                                float (&ol)[W / LPP], int (&oc)[W / LPP]) {
+__device__ __noinline__ MaxPlusOut<W / LPP> max_plus2_exact(const float* L, DDVec<W / LPP> in, float mk, int j0) {
     constexpr int S = W / LPP;
+    MaxPlusOut<S> o;
 #pragma unroll
-    for (int s = 0; s < S; ++s) { oh[s] = 0.f; ol[s] = 0.f; oc[s] = 0; }
+    for (int s = 0; s < S; ++s) { o.h[s] = 0.f; o.l[s] = 0.f; o.c[s] = 0; }
 #pragma unroll
     for (int r = 0; r < LPP; ++r) {
 #pragma unroll
         for (int s2 = 0; s2 < S; ++s2) {
             const int i = r * S + s2;
             if (i >= Q) continue;
-            const float xh = LPP == 1 ? ih[s2] : __shfl_sync(0xffffffffu, ih[s2], r, LPP);
-            const float xl = LPP == 1 ? il[s2] : __shfl_sync(0xffffffffu, il[s2], r, LPP);
+            const float xh = LPP == 1 ? in.h[s2] : __shfl_sync(0xffffffffu, in.h[s2], r, LPP);
+            const float xl = LPP == 1 ? in.l[s2] : __shfl_sync(0xffffffffu, in.l[s2], r, LPP);
             float rh[S], rl[S];
             if constexpr (kGlobal) {
                 ld_part_ro<S>(L + i * 2 * W + j0, rh);
@@ -104,18 +120,19 @@ __device__ __noinline__ void max_plus2_exact(const float* L, const float (&ih)[W
                 if (mk != 1.f) dd_mulf(ph, pl, mk);
                 float vh, vl;
                 dd_add(ph, pl, xh, xl, vh, vl);
-                const bool take = i == 0 || vh > oh[s] || (vh == oh[s] && vl > ol[s]) || (vh != vh && oh[s] == oh[s]);
-                if (take) { oh[s] = vh; ol[s] = vl; oc[s] = i; }
+                const bool take = i == 0 || vh > o.h[s] || (vh == o.h[s] && vl > o.l[s]) || (vh != vh && o.h[s] == o.h[s]);
+                if (take) { o.h[s] = vh; o.l[s] = vl; o.c[s] = i; }
             }
         }
     }
     if (mk != 1.f) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) dd_mulf(oh[s], ol[s], mk);
+        for (int s = 0; s < S; ++s) dd_mulf(o.h[s], o.l[s], mk);
     }
 #pragma unroll
     for (int s = 0; s < S; ++s)
-        if (j0 + s >= Q) { oh[s] = 0.f; ol[s] = 0.f; oc[s] = 0; }
+        if (j0 + s >= Q) { o.h[s] = 0.f; o.l[s] = 0.f; o.c[s] = 0; }
+    return o;
 }
 
 // out[j] = mk * max_i(mk * L[i][j] + in[i]) and its first argmax, for the lane's states j0..j0+S-1.
@@ -167,7 +184,12 @@ __device__ __forceinline__ void max_plus2(const float* L, const float (&ih)[W / 
         if (j0 + s < Q && !(bh[s] - b2[s] > 0x1p-20f * fabsf(b2[s]))) exact = true;
     if constexpr (LPP > 1) exact = __any_sync(0xffffffffu, exact);
     if (exact) {
-        max_plus2_exact<Q, W, LPP, kGlobal>(L, ih, il, mk, j0, oh, ol, oc);
+        DDVec<S> in;
+#pragma unroll
+        for (int s = 0; s < S; ++s) { in.h[s] = ih[s]; in.l[s] = il[s]; }
+        const MaxPlusOut<S> o = max_plus2_exact<Q, W, LPP, kGlobal>(L, in, mk, j0);
+#pragma unroll
+        for (int s = 0; s < S; ++s) { oh[s] = o.h[s]; ol[s] = o.l[s]; oc[s] = o.c[s]; }
         return;
     }
 #pragma unroll
@@ -206,6 +228,25 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
     const int warp = tid >> 5, lane = tid & 31;
     const int part = tid % LPP, j0 = part * S;
     for (int i = tid; i < 256 * 2 * W; i += NT) lut_s[i] = __ldg(a.lut_log2 + i);
+    // characters of a single state a (log profile 0 at a, at most log(1e-12) elsewhere): the
+    // message column max_i(mk L[i][j] + log profile_i) is mk L[a][j], because L[i][j] <= 0 and
+    // L[a][j] >= log(1e-12) for a mask mk in [0, 1] (up to the last bit of the pair sums where
+    // the two sides tie, on zero-length branches).  Published by the work loop's first barrier.
+    __shared__ signed char onehot_s[256];
+    for (int c = tid; c < 256; c += NT) {
+        int st1 = -1, zeros = 0;
+        bool ok = true;
+        for (int j = 0; j < Q; ++j) {
+            const float h = __ldg(a.lut_log2 + c * 2 * W + j), l = __ldg(a.lut_log2 + c * 2 * W + W + j);
+            if (h == 0.f && l == 0.f) {
+                ++zeros;
+                st1 = j;
+            } else if (!((double)h + (double)l <= kLogTinyBound)) {
+                ok = false;
+            }
+        }
+        onehot_s[c] = (signed char)(ok && zeros == 1 ? st1 : -1);
+    }
     const bool has_masks = a.f.mask_off != nullptr;
     float* const msg_buf = a.o.msg;
     const bool count_diff = a.o.count_diff != 0;
@@ -268,6 +309,37 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
             if (!has_masks) return 1.f;
             const int64_t mo = __ldg(a.f.mask_off + nb + c);
             return mo < 0 ? 1.f : (float)__ldg(a.f.masks + mo + pc);
+        };
+        // child c's message to this node: max-plus through its branch's log matrix L (shared or
+        // global memory); a single-state tip character takes the column of its state directly
+        auto child_msg = [&](int c, int trow, const float* L, bool glob, float (&oh)[S], float (&ol)[S],
+                             int (&oc)[S]) {
+            float ih[S], il[S];
+            const float mk = mask_of(c);
+            if constexpr (LPP == 1) {
+                if (c >= n_int && trow >= 0) {
+                    const int s1 = onehot_s[(int)__ldg(codes0 + (int64_t)trow * P)];
+                    if (s1 >= 0) {
+#pragma unroll
+                        for (int s = 0; s < S; ++s) {
+                            const float* row = L + s1 * 2 * W + s;
+                            float h = glob ? __ldg(row) : row[0], l = glob ? __ldg(row + W) : row[W];
+                            if (mk != 1.f) {
+                                // mk * max(mk L + 0): the same two roundings as max_plus2
+                                dd_mulf(h, l, mk);
+                                dd_mulf(h, l, mk);
+                            }
+                            oh[s] = s < Q ? h : 0.f;
+                            ol[s] = s < Q ? l : 0.f;
+                            oc[s] = s < Q ? s1 : 0;
+                        }
+                        return;
+                    }
+                }
+            }
+            child_in(c, trow, ih, il);
+            if (glob) max_plus2<Q, W, LPP, true>(L, ih, il, mk, j0, oh, ol, oc);
+            else max_plus2<Q, W, LPP, false>(L, ih, il, mk, j0, oh, ol, oc);
         };
         auto stage = [&](int b, int base, int cnt) {
             JStage<Q, W>& S_ = stg[b];
@@ -369,10 +441,9 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
                             for (int ch = 0; ch < 2; ++ch) {
                                 const int c = ch == 0 ? cp.x : cp.z;
                                 const int trow = ch == 0 ? cp.y : cp.w;
-                                float ih[S], il[S], oh[S], ol[S];
+                                float oh[S], ol[S];
                                 int oc[S];
-                                child_in(c, trow, ih, il);
-                                max_plus2<Q, W, LPP, false>(&st.mat[i][ch * QW2], ih, il, mask_of(c), j0, oh, ol, oc);
+                                child_msg(c, trow, &st.mat[i][ch * QW2], false, oh, ol, oc);
                                 if (c < n_int && valid) st_cx<S>(cx0 + (int64_t)c * P * W, oc);
 #pragma unroll
                                 for (int s = 0; s < S; ++s) dd_add(mh[s], ml[s], oh[s], ol[s], mh[s], ml[s]);
@@ -382,10 +453,9 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
                             for (int ci = rec.x; ci < rec.y; ++ci) {
                                 const int c = __ldg(a.f.child_idx + ci);
                                 const int trow = c >= n_int ? __ldg(a.f.tip_row + nb + c) : -1;
-                                float ih[S], il[S], oh[S], ol[S];
+                                float oh[S], ol[S];
                                 int oc[S];
-                                child_in(c, trow, ih, il);
-                                max_plus2<Q, W, LPP, true>(a.lp2 + (nb + c) * QW2, ih, il, mask_of(c), j0, oh, ol, oc);
+                                child_msg(c, trow, a.lp2 + (nb + c) * QW2, true, oh, ol, oc);
                                 if (c < n_int && valid) st_cx<S>(cx0 + (int64_t)c * P * W, oc);
 #pragma unroll
                                 for (int s = 0; s < S; ++s) dd_add(mh[s], ml[s], oh[s], ol[s], mh[s], ml[s]);

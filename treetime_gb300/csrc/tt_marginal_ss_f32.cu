@@ -35,13 +35,19 @@ constexpr float kSSRescaleBelow = 0x1p-16f;
 template <int Q, int W, int NT>
 __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
     constexpr int QQ = Q * Q;
+    constexpr int KP = (Q + 1) / 2;  // eigen-coordinate pairs (the last one padded for odd q)
     __shared__ float lut_s[256 * W];
     __shared__ int red[NT];
     __shared__ float red_corr[NT];
     __shared__ unsigned diff_red[NT / 32];
-    // V [QQ][kSSMaxSites] then V^-1 [QQ][kSSMaxSites]: a fixed site stride, so that each matrix
-    // element is an immediate offset from the thread's base address
+    // V as [i][k / 2][site][2] (V[i][k] and V[i][k + 1] of a site side by side), then V^-1
+    // transposed the same way, [j][k / 2][site][2] = V^-1[k][j]: one 8-byte load gives a thread two
+    // eigen-coordinates of its own site, the lanes of a warp (consecutive sites) read consecutive
+    // 8-byte words, and with the fixed site stride every element is an immediate offset from the
+    // thread's base address.  Then each thread's d - 1 of its two current branches, [2][2 KP][NT].
     extern __shared__ __align__(16) float mats_s[];
+    constexpr int MS = Q * KP * kSSMaxSites * 2;  // floats of one matrix
+    float* const es = mats_s + 2 * MS;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int i = tid; i < 256 * W; i += NT) {
         const int c = i / W, j = i % W;
@@ -54,6 +60,8 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
     float* partial = reinterpret_cast<float*>(a.o.partial);
     float* posterior = reinterpret_cast<float*>(a.o.posterior);
     const bool has_masks = a.f.mask_off != nullptr;
+    float* const e0 = es + tid;                // this thread's d - 1 of its first branch, stride NT
+    float* const e1 = es + 2 * KP * NT + tid;  // and of its second
 
     for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
         const int4 wi = a.items[it];
@@ -63,10 +71,14 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             continue;
         }
         __syncthreads();  // the previous range is done with the shared matrices
-        for (int e = tid; e < QQ * np; e += NT) {
+        for (int e = tid; e < Q * 2 * KP * np; e += NT) {
+            // element (r, c) of a q x 2KP block: V[r][c] and V^-1[c][r] (zero in the padding column)
             const int el = e / np, s = e - el * np;
-            mats_s[el * kSSMaxSites + s] = __ldg(a.m.V + (int64_t)el * P + wi.y + s);
-            mats_s[(QQ + el) * kSSMaxSites + s] = __ldg(a.m.Vinv + (int64_t)el * P + wi.y + s);
+            const int r = el / (2 * KP), c = el - r * (2 * KP);
+            const int dst = ((r * KP + (c >> 1)) * kSSMaxSites + s) * 2 + (c & 1);
+            const bool in = c < Q;
+            mats_s[dst] = in ? __ldg(a.m.V + (int64_t)(r * Q + c) * P + wi.y + s) : 0.f;
+            mats_s[MS + dst] = in ? __ldg(a.m.Vinv + (int64_t)(c * Q + r) * P + wi.y + s) : 0.f;
         }
         __syncthreads();
         const int G = NT / np;
@@ -76,23 +88,19 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         const int site = wi.y + sl;
         const bool valid = active && site < P;
         const int pc = site < P ? site : P - 1;
-        // V[i][k] = mats_s[m0 + (i*Q + k) * kSSMaxSites], V^-1[k][j] = mats_s[m0 + (QQ + k*Q + j) *
-        // kSSMaxSites] with m0 = sl + an opaque zero per node: the matrices do not change inside a
-        // level, and without it the compiler hoists all 2 q^2 loads out of the node loop into
-        // registers (and spills them)
-        auto mbase = [&]() { int z = 0; asm volatile("" : "+r"(z)); return sl + z; };
+        // (V[i][2kk], V[i][2kk+1]) = float2 at mats_s + m0 + (i*KP + kk) * 2 kSSMaxSites, and
+        // (V^-1[2kk][j], V^-1[2kk+1][j]) the same at MS + ... (j*KP + kk), with m0 = 2 sl + an
+        // opaque zero per node: the matrices do not change inside a level, and without it the
+        // compiler hoists all 2 q^2 loads out of the node loop into registers (and spills them)
+        auto mbase = [&]() { int z = 0; asm volatile("" : "+r"(z)); return 2 * sl + z; };
+        auto m2 = [&](int m0, int off) -> float2 { return *reinterpret_cast<const float2*>(mats_s + m0 + off); };
         int esum = 0;
         float lcorr = 0.f;
 
-        // d_k - 1 on a branch of length t: either a linear interpolation between two rows of the
-        // FP64-computed expm1 table (TreeTime's interpolated P(t)), or expm1f of mu*lambda_k*t
-        struct Branch {
-            const float* lo;  // table row at the lower grid point (interpolated), or mu*lambda row
-            const float* hi;  // table row at the upper grid point; nullptr: exact
-            float w;          // interpolation weight, or t (exact)
-        };
-        auto branch = [&](double t) -> Branch {
-            Branch br;
+        // d_k - 1 on a branch of length t into this thread's slot e (stride NT): either a linear
+        // interpolation between two rows of the FP64-computed expm1 table (TreeTime's interpolated
+        // P(t)), or expm1f of mu*lambda_k*t.  All loads of a branch are issued together, once.
+        auto stage_e = [&](float* e, double t) {
             if (a.m.n_grid > 0 && t * a.m.rate_scale < 10.0) {
                 // interp1d(kind='linear'): hi = searchsorted(grid, t) clipped to [1, n-1], lo = hi - 1
                 int lo = 0, hi = a.m.n_grid;
@@ -102,47 +110,88 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
                 }
                 const int ih = lo < 1 ? 1 : (lo > a.m.n_grid - 1 ? a.m.n_grid - 1 : lo);
                 const double xl = __ldg(a.m.grid + ih - 1), xh = __ldg(a.m.grid + ih);
-                br.w = (float)((t - xl) / (xh - xl));
-                br.lo = a.m.em1_grid + ((int64_t)(ih - 1) * P + pc) * W;
-                br.hi = a.m.em1_grid + ((int64_t)ih * P + pc) * W;
+                const float w = (float)((t - xl) / (xh - xl));
+                const float4* rl = reinterpret_cast<const float4*>(a.m.em1_grid + ((int64_t)(ih - 1) * P + pc) * W);
+                const float4* rh = reinterpret_cast<const float4*>(a.m.em1_grid + ((int64_t)ih * P + pc) * W);
+#pragma unroll
+                for (int q4 = 0; q4 < W / 4; ++q4) {
+                    const float4 l = __ldg(rl + q4), h = __ldg(rh + q4);
+                    const float lv[4] = {l.x, l.y, l.z, l.w}, hv[4] = {h.x, h.y, h.z, h.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (4 * q4 + u < 2 * KP) e[(4 * q4 + u) * NT] = 4 * q4 + u < Q ? fmaf(w, hv[u] - lv[u], lv[u]) : 0.f;
+                }
             } else {
-                br.w = (float)t;
-                br.lo = a.m.mulam + (int64_t)pc * W;
-                br.hi = nullptr;
-            }
-            return br;
-        };
-        auto em1_at = [&](const Branch& br, int k) -> float {
-            const float l = __ldg(br.lo + k);
-            return br.hi ? fmaf(br.w, __ldg(br.hi + k) - l, l) : expm1f(l * br.w);
-        };
-        // msg = x + ((x.V) * (d - 1)).V^-1, one eigen-coordinate k at a time (the k loop is not
-        // unrolled: a fully unrolled q x q transport needs more registers than a thread has)
-        auto propagate = [&](int m0, const Branch& br, const float (&x)[W], float (&msg)[W]) {
+                const float tf = (float)t;
+                const float4* ml = reinterpret_cast<const float4*>(a.m.mulam + (int64_t)pc * W);
 #pragma unroll
-            for (int j = 0; j < W; ++j) msg[j] = j < Q ? x[j] : 0.f;
-#pragma unroll 1
-            for (int k = 0; k < Q; ++k) {
-                float y = 0.f;
+                for (int q4 = 0; q4 < W / 4; ++q4) {
+                    const float4 l = __ldg(ml + q4);
+                    const float lv[4] = {l.x, l.y, l.z, l.w};
 #pragma unroll
-                for (int i = 0; i < Q; ++i) y = fmaf(x[i], mats_s[m0 + (i * Q + k) * kSSMaxSites], y);
-                const float zk = y * em1_at(br, k);
-#pragma unroll
-                for (int j = 0; j < Q; ++j) msg[j] = fmaf(zk, mats_s[m0 + (QQ + k * Q + j) * kSSMaxSites], msg[j]);
+                    for (int u = 0; u < 4; ++u)
+                        if (4 * q4 + u < 2 * KP) e[(4 * q4 + u) * NT] = 4 * q4 + u < Q ? expm1f(lv[u] * tf) : 0.f;
+                }
             }
         };
-        // ev = o + V.((V^-1.o) * (d - 1))
-        auto evolve = [&](int m0, const Branch& br, const float (&o)[W], float (&ev)[W]) {
+        // two messages through one site's eigenbasis, msg = x + ((x.V) * (d - 1)).V^-1, every
+        // matrix element loaded once for both, two eigen-coordinates per step (the step loop is
+        // not unrolled: a fully unrolled q x q transport needs more registers than a thread has)
+        auto propagate2 = [&](int m0, const float* ea, const float* eb, const float (&xa)[W],
+                              const float (&xb)[W], float (&ma)[W], float (&mb)[W]) {
 #pragma unroll
-            for (int i = 0; i < W; ++i) ev[i] = i < Q ? o[i] : 0.f;
+            for (int j = 0; j < W; ++j) {
+                ma[j] = j < Q ? xa[j] : 0.f;
+                mb[j] = j < Q ? xb[j] : 0.f;
+            }
 #pragma unroll 1
-            for (int k = 0; k < Q; ++k) {
-                float y = 0.f;
+            for (int kk = 0; kk < KP; ++kk) {
+                float ya0[2] = {0.f, 0.f}, ya1[2] = {0.f, 0.f}, yb0[2] = {0.f, 0.f}, yb1[2] = {0.f, 0.f};
 #pragma unroll
-                for (int j = 0; j < Q; ++j) y = fmaf(mats_s[m0 + (QQ + k * Q + j) * kSSMaxSites], o[j], y);
-                const float zk = y * em1_at(br, k);
+                for (int i = 0; i < Q; ++i) {
+                    const float2 v = m2(m0, (i * KP + kk) * 2 * kSSMaxSites);
+                    ya0[i & 1] = fmaf(xa[i], v.x, ya0[i & 1]);
+                    ya1[i & 1] = fmaf(xa[i], v.y, ya1[i & 1]);
+                    yb0[i & 1] = fmaf(xb[i], v.x, yb0[i & 1]);
+                    yb1[i & 1] = fmaf(xb[i], v.y, yb1[i & 1]);
+                }
+                const float za0 = (ya0[0] + ya0[1]) * ea[2 * kk * NT], za1 = (ya1[0] + ya1[1]) * ea[(2 * kk + 1) * NT];
+                const float zb0 = (yb0[0] + yb0[1]) * eb[2 * kk * NT], zb1 = (yb1[0] + yb1[1]) * eb[(2 * kk + 1) * NT];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) ev[i] = fmaf(mats_s[m0 + (i * Q + k) * kSSMaxSites], zk, ev[i]);
+                for (int j = 0; j < Q; ++j) {
+                    const float2 u = m2(m0, MS + (j * KP + kk) * 2 * kSSMaxSites);
+                    ma[j] = fmaf(za1, u.y, fmaf(za0, u.x, ma[j]));
+                    mb[j] = fmaf(zb1, u.y, fmaf(zb0, u.x, mb[j]));
+                }
+            }
+        };
+        // ev = o + V.((V^-1.o) * (d - 1)) for two vectors
+        auto evolve2 = [&](int m0, const float* ea, const float* eb, const float (&oa)[W], const float (&ob)[W],
+                           float (&va)[W], float (&vb)[W]) {
+#pragma unroll
+            for (int i = 0; i < W; ++i) {
+                va[i] = i < Q ? oa[i] : 0.f;
+                vb[i] = i < Q ? ob[i] : 0.f;
+            }
+#pragma unroll 1
+            for (int kk = 0; kk < KP; ++kk) {
+                float ya0[2] = {0.f, 0.f}, ya1[2] = {0.f, 0.f}, yb0[2] = {0.f, 0.f}, yb1[2] = {0.f, 0.f};
+#pragma unroll
+                for (int j = 0; j < Q; ++j) {
+                    const float2 u = m2(m0, MS + (j * KP + kk) * 2 * kSSMaxSites);
+                    ya0[j & 1] = fmaf(u.x, oa[j], ya0[j & 1]);
+                    ya1[j & 1] = fmaf(u.y, oa[j], ya1[j & 1]);
+                    yb0[j & 1] = fmaf(u.x, ob[j], yb0[j & 1]);
+                    yb1[j & 1] = fmaf(u.y, ob[j], yb1[j & 1]);
+                }
+                const float za0 = (ya0[0] + ya0[1]) * ea[2 * kk * NT], za1 = (ya1[0] + ya1[1]) * ea[(2 * kk + 1) * NT];
+                const float zb0 = (yb0[0] + yb0[1]) * eb[2 * kk * NT], zb1 = (yb1[0] + yb1[1]) * eb[(2 * kk + 1) * NT];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    const float2 v = m2(m0, (i * KP + kk) * 2 * kSSMaxSites);
+                    va[i] = fmaf(v.y, za1, fmaf(v.x, za0, va[i]));
+                    vb[i] = fmaf(v.y, zb1, fmaf(v.x, zb0, vb[i]));
+                }
             }
         };
         auto tip_row = [&](int64_t gk, float (&x)[W]) {
@@ -157,8 +206,39 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             return mo < 0 ? 1.f : (float)__ldg(a.f.masks + mo + pc);
         };
         auto row = [&](float* base, int k) { return base + (tr.prof_base + (int64_t)k * P + pc) * W; };
+        auto node_in = [&](int c, float (&x)[W]) {
+            if (c >= n_int) tip_row(nb + c, x);
+            else load_row<W>(row(partial, c), x);
+        };
 
         // ------------------------------------------------------------ post-order
+        // r *= max(1e-12, msg)^mask for one child, then the power-of-two rescale
+        auto absorb = [&](int c, const float (&x)[W], const float (&msg)[W], float (&r)[W]) {
+            // an internal child's message waits in its posterior row for the pre-order, which
+            // overwrites it with the posterior once it has used it
+            if (c < n_int && valid) store_row<W>(row(posterior, c), msg);
+            const float m = mask_of(nb + c);
+            if (m != 1.f && c < n_int) {
+                float xs = 0.f;
+#pragma unroll
+                for (int j = 0; j < Q; ++j) xs += x[j];
+                lcorr += (1.f - m) * logf(xs);
+            }
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                float v = fmaxf(1e-12f, msg[j]);
+                if (m != 1.f) v = m == 0.f ? 1.f : exp2f(m * log2f(v));
+                r[j] *= v;
+            }
+            float mx = r[0];
+#pragma unroll
+            for (int j = 1; j < Q; ++j) mx = fmaxf(mx, r[j]);
+            if (mx < kSSRescaleBelow) {
+                const int e = pow2_exponent(mx);
+                scale_pow2<W>(r, e);
+                esum += e;
+            }
+        };
         for (int h = 0; h < tr.n_levels; ++h) {
             const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
             for (int k = active ? lo + g : hi; k < hi; k += G) {
@@ -167,34 +247,24 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
                 float r[W];
 #pragma unroll
                 for (int j = 0; j < W; ++j) r[j] = j < Q ? 1.f : 0.f;
-                for (int ci = c_lo; ci < c_hi; ++ci) {
-                    const int c = __ldg(a.f.child_idx + ci);
-                    const int64_t gc = nb + c;
-                    float x[W], msg[W];
-                    if (c >= n_int) tip_row(gc, x);
-                    else load_row<W>(row(partial, c), x);
-                    propagate(mbase(), branch(__ldg(a.f.bl + gc)), x, msg);
-                    const float m = mask_of(gc);
-                    if (m != 1.f && c < n_int) {
-                        float xs = 0.f;
+                for (int ci = c_lo; ci < c_hi; ci += 2) {
+                    // children two at a time (the last one alone, transported twice)
+                    const int ca = __ldg(a.f.child_idx + ci);
+                    const bool two = ci + 1 < c_hi;
+                    const int cb = two ? __ldg(a.f.child_idx + ci + 1) : ca;
+                    float xa[W], xb[W], ma[W], mb[W];
+                    node_in(ca, xa);
+                    stage_e(e0, __ldg(a.f.bl + nb + ca));
+                    if (two) {
+                        node_in(cb, xb);
+                        stage_e(e1, __ldg(a.f.bl + nb + cb));
+                    } else {
 #pragma unroll
-                        for (int j = 0; j < Q; ++j) xs += x[j];
-                        lcorr += (1.f - m) * logf(xs);
+                        for (int j = 0; j < W; ++j) xb[j] = xa[j];
                     }
-#pragma unroll
-                    for (int j = 0; j < Q; ++j) {
-                        float v = fmaxf(1e-12f, msg[j]);
-                        if (m != 1.f) v = m == 0.f ? 1.f : exp2f(m * log2f(v));
-                        r[j] *= v;
-                    }
-                    float mx = r[0];
-#pragma unroll
-                    for (int j = 1; j < Q; ++j) mx = fmaxf(mx, r[j]);
-                    if (mx < kSSRescaleBelow) {
-                        const int e = pow2_exponent(mx);
-                        scale_pow2<W>(r, e);
-                        esum += e;
-                    }
+                    propagate2(mbase(), e0, two ? e1 : e0, xa, xb, ma, mb);
+                    absorb(ca, xa, ma, r);
+                    if (two) absorb(cb, xb, mb, r);
                 }
                 if (valid) store_row<W>(row(partial, k), r);
             }
@@ -238,69 +308,114 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         __syncthreads();
 
         // ------------------------------------------------------------- pre-order
+        // by parent, top down: a parent's needed children (internal ones; tips too when their
+        // posteriors or outgroup profiles are asked for) two at a time, sharing the matrix loads
         unsigned ndiff = 0;
         const bool keep_outgroup = a.o.outgroup != nullptr || a.o.tip_outgroup != nullptr;
-        const int tip_hi = (a.o.reconstruct_tips || a.o.tip_outgroup) ? n_int + tr.n_tip : n_int;
-        for (int h = tr.n_levels - 2; h >= -1; --h) {
-            const int lo = h >= 0 ? __ldg(lev + h) : n_int;
-            const int hi = h >= 0 ? __ldg(lev + h + 1) : tip_hi;
-            for (int k = active ? lo + g : hi; k < hi; k += G) {
-                const bool is_tip = k >= n_int;
-                const int64_t gk = nb + k;
-                const int par = __ldg(a.f.parent + gk);
-                float pv[W], x[W], msg[W], o[W];
-                load_row<W>(row(posterior, par), pv);
-                if (is_tip) tip_row(gk, x);
-                else load_row<W>(row(partial, k), x);
-                const Branch br = branch(__ldg(a.f.bl + gk));
-                const int m0 = mbase();
-                propagate(m0, br, x, msg);
-                const float m = mask_of(gk);
+        const bool tips_needed = a.o.reconstruct_tips || a.o.tip_outgroup;
+        // the parent's posterior over the child's message -> the child's outgroup profile o
+        auto outgroup_of = [&](int c, const float (&pv)[W], float (&o)[W]) {
+            const float m = mask_of(nb + c);
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                    float v = fmaxf(1e-12f, msg[j]);
-                    if (m != 1.f) v = m == 0.f ? 1.f : exp2f(m * log2f(v));
-                    // parent posterior over this node's message (fast division, <= 2 ulp); its scale
-                    // cancels in the posterior, so it is normalised only when stored
-                    o[j] = j < Q ? __fdividef(fmaxf(1e-12f, pv[j]), v) : 0.f;
-                }
-                if (keep_outgroup) {
-                    float s = 0.f;
-#pragma unroll
-                    for (int j = 0; j < Q; ++j) s += o[j];
-                    const float inv = __fdividef(1.f, s);
-#pragma unroll
-                    for (int j = 0; j < Q; ++j) o[j] *= inv;
-                    float* og = reinterpret_cast<float*>(is_tip ? a.o.tip_outgroup : a.o.outgroup);
-                    const int64_t orow = is_tip ? tr.tipprof_base + (int64_t)(k - n_int) * P + pc
-                                                : tr.prof_base + (int64_t)k * P + pc;
-                    if (valid && og) store_row<W>(og + orow * W, o);
-                }
-                if (is_tip && !a.o.reconstruct_tips) continue;
-                float ev[W];
-                evolve(m0, br, o, ev);
+            for (int j = 0; j < W; ++j) {
+                float v = fmaxf(1e-12f, o[j]);
+                if (m != 1.f) v = m == 0.f ? 1.f : exp2f(m * log2f(v));
+                // parent posterior over this node's message (fast division, <= 2 ulp); its scale
+                // cancels in the posterior, so it is normalised only when stored
+                o[j] = j < Q ? __fdividef(fmaxf(1e-12f, pv[j]), v) : 0.f;
+            }
+            if (keep_outgroup) {
+                const bool is_tip = c >= n_int;
                 float s = 0.f;
 #pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    float e = ev[i];
-                    if (m != 1.f) e = m * e + (1.f - m);
-                    x[i] *= e;
-                    s += x[i];
-                }
+                for (int j = 0; j < Q; ++j) s += o[j];
                 const float inv = __fdividef(1.f, s);
 #pragma unroll
-                for (int i = 0; i < Q; ++i) x[i] *= inv;
-                const int st = a.o.node_uniform
-                                   ? sample_cdf<Q, float, W>(x, a.o.node_uniform[tr.state_base + (int64_t)k * P + pc])
-                                   : argmax_first<Q, float, W>(x);
-                if (valid) {
-                    const int64_t prow = is_tip ? tr.tipprof_base + (int64_t)(k - n_int) * P + pc
-                                                : tr.prof_base + (int64_t)k * P + pc;
-                    float* dst = is_tip ? reinterpret_cast<float*>(a.o.tip_posterior) : posterior;
-                    if (dst) store_row<W>(dst + prow * W, x);
-                    uint8_t* sp = a.o.states + tr.state_base + (int64_t)k * P + pc;
-                    if (a.o.count_diff) ndiff += (*sp != (uint8_t)st);
-                    *sp = (uint8_t)st;
+                for (int j = 0; j < Q; ++j) o[j] *= inv;
+                float* og = reinterpret_cast<float*>(is_tip ? a.o.tip_outgroup : a.o.outgroup);
+                const int64_t orow = is_tip ? tr.tipprof_base + (int64_t)(c - n_int) * P + pc
+                                            : tr.prof_base + (int64_t)c * P + pc;
+                if (valid && og) store_row<W>(og + orow * W, o);
+            }
+        };
+        // posterior of child c from its partial (or tip profile) and ev
+        auto posterior_of = [&](int c, const float (&ev)[W]) {
+            const bool is_tip = c >= n_int;
+            const float m = mask_of(nb + c);
+            float x[W];
+            node_in(c, x);
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                float e = ev[i];
+                if (m != 1.f) e = m * e + (1.f - m);
+                x[i] *= e;
+                s += x[i];
+            }
+            const float inv = __fdividef(1.f, s);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) x[i] *= inv;
+            const int st = a.o.node_uniform
+                               ? sample_cdf<Q, float, W>(x, a.o.node_uniform[tr.state_base + (int64_t)c * P + pc])
+                               : argmax_first<Q, float, W>(x);
+            if (valid) {
+                const int64_t prow = is_tip ? tr.tipprof_base + (int64_t)(c - n_int) * P + pc
+                                            : tr.prof_base + (int64_t)c * P + pc;
+                float* dst = is_tip ? reinterpret_cast<float*>(a.o.tip_posterior) : posterior;
+                if (dst) store_row<W>(dst + prow * W, x);
+                uint8_t* sp = a.o.states + tr.state_base + (int64_t)c * P + pc;
+                if (a.o.count_diff) ndiff += (*sp != (uint8_t)st);
+                *sp = (uint8_t)st;
+            }
+        };
+        // parent levels from the root's down; height-1 parents have only tips below them
+        const int h_end = tips_needed ? 0 : 1;
+        for (int h = tr.n_levels - 1; h >= h_end; --h) {
+            const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
+            for (int p = active ? lo + g : hi; p < hi; p += G) {
+                const int64_t gp = nb + p;
+                const int c_lo = __ldg(a.f.child_off + gp), c_hi = __ldg(a.f.child_off + gp + 1);
+                int ci = c_lo;
+                while (true) {
+                    while (ci < c_hi && !tips_needed && __ldg(a.f.child_idx + ci) >= n_int) ++ci;
+                    if (ci >= c_hi) break;
+                    const int ca = __ldg(a.f.child_idx + ci++);
+                    while (ci < c_hi && !tips_needed && __ldg(a.f.child_idx + ci) >= n_int) ++ci;
+                    const bool two = ci < c_hi;
+                    const int cb = two ? __ldg(a.f.child_idx + ci++) : ca;
+                    float pv[W], oa[W], ob[W];
+                    load_row<W>(row(posterior, p), pv);
+                    stage_e(e0, __ldg(a.f.bl + nb + ca));
+                    if (two) stage_e(e1, __ldg(a.f.bl + nb + cb));
+                    const float* eb = two ? e1 : e0;
+                    if (ca < n_int && (!two || cb < n_int)) {
+                        // the children's messages as the post-order formed them
+                        load_row<W>(row(posterior, ca), oa);
+                        if (two) load_row<W>(row(posterior, cb), ob);
+                        else {
+#pragma unroll
+                            for (int j = 0; j < W; ++j) ob[j] = oa[j];
+                        }
+                    } else {
+                        // a tip among them: the same messages again
+                        float xa[W], xb[W];
+                        node_in(ca, xa);
+                        if (two) node_in(cb, xb);
+                        else {
+#pragma unroll
+                            for (int j = 0; j < W; ++j) xb[j] = xa[j];
+                        }
+                        propagate2(mbase(), e0, eb, xa, xb, oa, ob);
+                    }
+                    outgroup_of(ca, pv, oa);
+                    if (two) outgroup_of(cb, pv, ob);
+                    const bool post_a = ca < n_int || a.o.reconstruct_tips;
+                    const bool post_b = two && (cb < n_int || a.o.reconstruct_tips);
+                    if (!post_a && !post_b) continue;
+                    float va[W], vb[W];
+                    evolve2(mbase(), e0, eb, oa, ob, va, vb);
+                    if (post_a) posterior_of(ca, va);
+                    if (post_b) posterior_of(cb, vb);
                 }
             }
             __syncthreads();
@@ -325,7 +440,8 @@ static tt_status launch_ss_f32(const SSF32Params& prm, int max_np, int blocks, c
     // 20+ states keep about 90 floats live per thread (a message, its eigen-coordinates and the
     // node's running product): 384 threads (170 registers a thread, 12 warps per SM)
     constexpr int NT = Q >= 20 ? 384 : 512;
-    const size_t dyn = (size_t)2 * Q * Q * max_np * sizeof(float);
+    constexpr int KP = (Q + 1) / 2;
+    const size_t dyn = ((size_t)2 * Q * KP * max_np * 2 + (size_t)2 * 2 * KP * NT) * sizeof(float);
     static size_t configured[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);

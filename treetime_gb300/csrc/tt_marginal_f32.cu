@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
     __shared__ float red_corr[NT];
     __shared__ float red_ph[NT];
     __shared__ float red_pl[NT];
+    __shared__ double red_cd[HM ? NT : 1];  // partial mask corrections (root step, masks only)
     __shared__ unsigned diff_red[NT / 32];
     __shared__ int lev_s[kLevCap];
     extern __shared__ __align__(16) unsigned char dyn_s[];  // two stage buffers
@@ -334,15 +335,43 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         }
 
         // ------------------------------------------------------------------ root
+        // The pattern's dropped factors over all node groups (product, exponents, corrections), in
+        // two fixed-order steps: reducer r of a pattern combines groups r, r + R, r + 2R, ... and
+        // leaves its partial in group r's slot (which no other reducer reads), then group 0
+        // combines the R partials.  Without masks a group's correction is 0 or -inf (a partial that
+        // was zero at every state), so no FP64 sum is needed.
+        {
+            const int R = min(8, G);
+            const int rr = tid / GP, rp = tid - rr * GP;
+            if (rr < R && active) {
+                int t_r = 0;
+                double c_r = 0.0;
+                bool d_r = false;
+                float h_r = 1.f, l_r = 0.f;
+                for (int gg = rr; gg < G; gg += R) {
+                    t_r += red[gg * GP + rp];
+                    if constexpr (has_masks) c_r += (double)red_corr[gg * GP + rp];
+                    else d_r |= red_corr[gg * GP + rp] != 0.f;
+                    df_mul(h_r, l_r, red_ph[gg * GP + rp], red_pl[gg * GP + rp]);
+                    df_renorm(h_r, l_r, t_r);
+                }
+                red[rr * GP + rp] = t_r;
+                if constexpr (has_masks) red_cd[rr * GP + rp] = c_r;
+                else red_corr[rr * GP + rp] = d_r ? -INFINITY : 0.f;
+                red_ph[rr * GP + rp] = h_r;
+                red_pl[rr * GP + rp] = l_r;
+            }
+            __syncthreads();
+        }
         if (tid < GP) {  // group 0 (whole warps when LPP > 1)
-            // the pattern's dropped factors over all node groups: product, exponents, corrections
+            const int R = min(8, G);
             int tot = 0;
             double corr = 0.0;
             float fh = 1.f, fl = 0.f;
-            for (int gg = 0; gg < G; ++gg) {
-                tot += red[gg * GP + tid];
-                corr += (double)red_corr[gg * GP + tid];
-                df_mul(fh, fl, red_ph[gg * GP + tid], red_pl[gg * GP + tid]);
+            for (int r = 0; r < R; ++r) {
+                tot += red[r * GP + tid];
+                corr += has_masks ? red_cd[r * GP + tid] : (double)red_corr[r * GP + tid];
+                df_mul(fh, fl, red_ph[r * GP + tid], red_pl[r * GP + tid]);
                 df_renorm(fh, fl, tot);
             }
             const int kr = n_int - 1;

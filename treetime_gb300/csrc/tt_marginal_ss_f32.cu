@@ -30,16 +30,140 @@ struct SSF32Params {
 };
 
 constexpr int kSSMaxSites = 32;
+constexpr int kSSGridCap = 128;  // time grids up to this many points are searched in shared memory
 constexpr float kSSRescaleBelow = 0x1p-16f;
 
+// a row by value (registers) for the out-of-line slow paths
+template <int W>
+struct SSRow {
+    float v[W];
+};
+
+// r * 2^-e for exponents outside the range of one power-of-two factor (a subnormal row maximum):
+// out of line, so that the common path's code stays compact
+template <int W>
+__device__ __noinline__ SSRow<W> ss_ldexp_row(SSRow<W> r, int e) {
+#pragma unroll
+    for (int j = 0; j < W; ++j) r.v[j] = ldexpf(r.v[j], -e);
+    return r;
+}
+
+// Two messages through one site's eigenbasis, msg = x + ((x.V) * (d - 1)).V^-1, every matrix
+// element loaded once for both, two eigen-coordinates per step (the step loop is not unrolled: a
+// fully unrolled q x q transport needs more registers than a thread has).  mats: the CTA's V and
+// V^-1 (layout in marginal_ss_f32_kernel), m0: the thread's offset in it, ea / eb: d - 1 of the two
+// branches at stride NT.
 template <int Q, int W, int NT>
+__device__ __forceinline__ void ss_propagate2(const float* mats, int m0, const float* ea, const float* eb,
+                                              const float (&xa)[W], const float (&xb)[W], float (&ma)[W],
+                                              float (&mb)[W]) {
+    constexpr int KP = (Q + 1) / 2, MS = Q * KP * kSSMaxSites * 2;
+    auto m2 = [&](int off) -> float2 { return *reinterpret_cast<const float2*>(mats + m0 + off); };
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+        ma[j] = j < Q ? xa[j] : 0.f;
+        mb[j] = j < Q ? xb[j] : 0.f;
+    }
+#pragma unroll 1
+    for (int kk = 0; kk < KP; ++kk) {
+        float ya0[2] = {0.f, 0.f}, ya1[2] = {0.f, 0.f}, yb0[2] = {0.f, 0.f}, yb1[2] = {0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const float2 v = m2((i * KP + kk) * 2 * kSSMaxSites);
+            ya0[i & 1] = fmaf(xa[i], v.x, ya0[i & 1]);
+            ya1[i & 1] = fmaf(xa[i], v.y, ya1[i & 1]);
+            yb0[i & 1] = fmaf(xb[i], v.x, yb0[i & 1]);
+            yb1[i & 1] = fmaf(xb[i], v.y, yb1[i & 1]);
+        }
+        const float za0 = (ya0[0] + ya0[1]) * ea[2 * kk * NT], za1 = (ya1[0] + ya1[1]) * ea[(2 * kk + 1) * NT];
+        const float zb0 = (yb0[0] + yb0[1]) * eb[2 * kk * NT], zb1 = (yb1[0] + yb1[1]) * eb[(2 * kk + 1) * NT];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const float2 u = m2(MS + (j * KP + kk) * 2 * kSSMaxSites);
+            ma[j] = fmaf(za1, u.y, fmaf(za0, u.x, ma[j]));
+            mb[j] = fmaf(zb1, u.y, fmaf(zb0, u.x, mb[j]));
+        }
+    }
+}
+
+// ev = o + V.((V^-1.o) * (d - 1)) for two vectors
+template <int Q, int W, int NT>
+__device__ __forceinline__ void ss_evolve2(const float* mats, int m0, const float* ea, const float* eb,
+                                           const float (&oa)[W], const float (&ob)[W], float (&va)[W],
+                                           float (&vb)[W]) {
+    constexpr int KP = (Q + 1) / 2, MS = Q * KP * kSSMaxSites * 2;
+    auto m2 = [&](int off) -> float2 { return *reinterpret_cast<const float2*>(mats + m0 + off); };
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+        va[i] = i < Q ? oa[i] : 0.f;
+        vb[i] = i < Q ? ob[i] : 0.f;
+    }
+#pragma unroll 1
+    for (int kk = 0; kk < KP; ++kk) {
+        float ya0[2] = {0.f, 0.f}, ya1[2] = {0.f, 0.f}, yb0[2] = {0.f, 0.f}, yb1[2] = {0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const float2 u = m2(MS + (j * KP + kk) * 2 * kSSMaxSites);
+            ya0[j & 1] = fmaf(u.x, oa[j], ya0[j & 1]);
+            ya1[j & 1] = fmaf(u.y, oa[j], ya1[j & 1]);
+            yb0[j & 1] = fmaf(u.x, ob[j], yb0[j & 1]);
+            yb1[j & 1] = fmaf(u.y, ob[j], yb1[j & 1]);
+        }
+        const float za0 = (ya0[0] + ya0[1]) * ea[2 * kk * NT], za1 = (ya1[0] + ya1[1]) * ea[(2 * kk + 1) * NT];
+        const float zb0 = (yb0[0] + yb0[1]) * eb[2 * kk * NT], zb1 = (yb1[0] + yb1[1]) * eb[(2 * kk + 1) * NT];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const float2 v = m2((i * KP + kk) * 2 * kSSMaxSites);
+            va[i] = fmaf(v.y, za1, fmaf(v.x, za0, va[i]));
+            vb[i] = fmaf(v.y, zb1, fmaf(v.x, zb0, vb[i]));
+        }
+    }
+}
+
+template <int W>
+struct SSRowPair {
+    float a[W], b[W];
+};
+
+// the same transport out of line (the pre-order's rare recomputation for tips), rows by value
+template <int Q, int W, int NT>
+__device__ __noinline__ SSRowPair<W> ss_propagate2_ool(const float* mats, int m0, const float* ea, const float* eb,
+                                                      SSRow<W> xa, SSRow<W> xb) {
+    SSRowPair<W> m;
+    ss_propagate2<Q, W, NT>(mats, m0, ea, eb, xa.v, xb.v, m.a, m.b);
+    return m;
+}
+
+// o / sum(o) over the first Q entries (fast reciprocal), out of line: only for stored outgroup rows
+template <int Q, int W>
+__device__ __noinline__ SSRow<W> ss_normalized(SSRow<W> o) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < Q; ++j) s += o.v[j];
+    const float inv = __fdividef(1.f, s);
+#pragma unroll
+    for (int j = 0; j < Q; ++j) o.v[j] *= inv;
+    return o;
+}
+
+// inverse-CDF draw from a posterior row, out of line (sample_from_profile only)
+template <int Q, int W>
+__device__ __noinline__ int ss_sample(SSRow<W> x, double u) {
+    return sample_cdf<Q, float, W>(x.v, u);
+}
+
+// HM: the forest has per-branch masks (a second instance without any mask code serves the rest:
+// a narrow level runs its node code once per warp, so code that is never executed but sits
+// between the executed instructions costs instruction-cache misses on every level)
+template <int Q, int W, int NT, bool HM>
 __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
     constexpr int QQ = Q * Q;
     constexpr int KP = (Q + 1) / 2;  // eigen-coordinate pairs (the last one padded for odd q)
-    __shared__ float lut_s[256 * W];
+    __shared__ __align__(16) float lut_s[256 * W];
     __shared__ int red[NT];
     __shared__ float red_corr[NT];
     __shared__ unsigned diff_red[NT / 32];
+    __shared__ double grid_s[kSSGridCap];
     // V as [i][k / 2][site][2] (V[i][k] and V[i][k + 1] of a site side by side), then V^-1
     // transposed the same way, [j][k / 2][site][2] = V^-1[k][j]: one 8-byte load gives a thread two
     // eigen-coordinates of its own site, the lanes of a warp (consecutive sites) read consecutive
@@ -53,13 +177,16 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         const int c = i / W, j = i % W;
         lut_s[i] = j < Q ? (float)__ldg(a.m.lut + c * Q + j) : 0.f;
     }
+    const bool grid_sm = a.m.n_grid <= kSSGridCap;
+    if (grid_sm)
+        for (int i = tid; i < a.m.n_grid; i += NT) grid_s[i] = __ldg(a.m.grid + i);
     const tt_tree tr = a.f.trees[0];
     const int P = tr.n_patterns, n_int = tr.n_int;
     const int64_t nb = tr.node_base;
     const int32_t* lev = a.f.level_off + tr.level_base;
     float* partial = reinterpret_cast<float*>(a.o.partial);
     float* posterior = reinterpret_cast<float*>(a.o.posterior);
-    const bool has_masks = a.f.mask_off != nullptr;
+    constexpr bool has_masks = HM;
     float* const e0 = es + tid;                // this thread's d - 1 of its first branch, stride NT
     float* const e1 = es + 2 * KP * NT + tid;  // and of its second
 
@@ -71,6 +198,30 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             continue;
         }
         __syncthreads();  // the previous range is done with the shared matrices
+        {
+            // Bring what the walk reads along its dependent chains into L2 now, all at once: the
+            // tree's node records, child pairs and branch lengths, this range's rows of the d - 1
+            // table and its columns of the tip characters (scattered reads that would otherwise
+            // come from DRAM one level at a time)
+            auto pf = [](const void* q) { asm volatile("prefetch.global.L2 [%0];" ::"l"(q)); };
+            const int n_nodes = n_int + tr.n_tip;
+            const int nb128 = (int)(((int64_t)n_nodes * 16 + 127) / 128);
+            for (int i = tid; i < nb128; i += NT) {
+                pf(reinterpret_cast<const char*>(a.f.node_rec + 4 * nb) + 128 * (int64_t)i);
+                pf(reinterpret_cast<const char*>(a.f.child_pair + 4 * nb) + 128 * (int64_t)i);
+            }
+            for (int i = tid; i < (n_nodes * 8 + 127) / 128; i += NT)
+                pf(reinterpret_cast<const char*>(a.f.bl + nb) + 128 * (int64_t)i);
+            const int row_bytes = np * W * 4, rl = (row_bytes + 127) / 128;  // this range's sites, one grid point
+            for (int i = tid; i < a.m.n_grid * rl; i += NT) {
+                const int gpt = i / rl, l = i - gpt * rl;
+                pf(reinterpret_cast<const char*>(a.m.em1_grid + ((int64_t)gpt * P + wi.y) * W) + 128 * l);
+            }
+            for (int i = tid; i < tr.n_tip; i += NT) {
+                const int trow = __ldg(a.f.tip_row + nb + n_int + i);
+                if (trow >= 0) pf(a.f.tip_codes + tr.tip_base + (int64_t)trow * P + wi.y);
+            }
+        }
         for (int e = tid; e < Q * 2 * KP * np; e += NT) {
             // element (r, c) of a q x 2KP block: V[r][c] and V^-1[c][r] (zero in the padding column)
             const int el = e / np, s = e - el * np;
@@ -93,7 +244,6 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         // opaque zero per node: the matrices do not change inside a level, and without it the
         // compiler hoists all 2 q^2 loads out of the node loop into registers (and spills them)
         auto mbase = [&]() { int z = 0; asm volatile("" : "+r"(z)); return 2 * sl + z; };
-        auto m2 = [&](int m0, int off) -> float2 { return *reinterpret_cast<const float2*>(mats_s + m0 + off); };
         int esum = 0;
         float lcorr = 0.f;
 
@@ -103,13 +253,14 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         auto stage_e = [&](float* e, double t) {
             if (a.m.n_grid > 0 && t * a.m.rate_scale < 10.0) {
                 // interp1d(kind='linear'): hi = searchsorted(grid, t) clipped to [1, n-1], lo = hi - 1
+                auto gv = [&](int i) -> double { return grid_sm ? grid_s[i] : __ldg(a.m.grid + i); };
                 int lo = 0, hi = a.m.n_grid;
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (__ldg(a.m.grid + mid) < t) lo = mid + 1; else hi = mid;
+                    if (gv(mid) < t) lo = mid + 1; else hi = mid;
                 }
                 const int ih = lo < 1 ? 1 : (lo > a.m.n_grid - 1 ? a.m.n_grid - 1 : lo);
-                const double xl = __ldg(a.m.grid + ih - 1), xh = __ldg(a.m.grid + ih);
+                const double xl = gv(ih - 1), xh = gv(ih);
                 const float w = (float)((t - xl) / (xh - xl));
                 const float4* rl = reinterpret_cast<const float4*>(a.m.em1_grid + ((int64_t)(ih - 1) * P + pc) * W);
                 const float4* rh = reinterpret_cast<const float4*>(a.m.em1_grid + ((int64_t)ih * P + pc) * W);
@@ -122,86 +273,36 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
                         if (4 * q4 + u < 2 * KP) e[(4 * q4 + u) * NT] = 4 * q4 + u < Q ? fmaf(w, hv[u] - lv[u], lv[u]) : 0.f;
                 }
             } else {
+                // long branches (or no grid): one exponential at a time, a rolled loop (the
+                // inlined q expm1f would crowd the instruction cache of the common path)
                 const float tf = (float)t;
-                const float4* ml = reinterpret_cast<const float4*>(a.m.mulam + (int64_t)pc * W);
-#pragma unroll
-                for (int q4 = 0; q4 < W / 4; ++q4) {
-                    const float4 l = __ldg(ml + q4);
-                    const float lv[4] = {l.x, l.y, l.z, l.w};
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (4 * q4 + u < 2 * KP) e[(4 * q4 + u) * NT] = 4 * q4 + u < Q ? expm1f(lv[u] * tf) : 0.f;
-                }
+                const float* ml = a.m.mulam + (int64_t)pc * W;
+#pragma unroll 1
+                for (int k = 0; k < 2 * KP; ++k) e[k * NT] = k < Q ? expm1f(__ldg(ml + k) * tf) : 0.f;
             }
         };
-        // two messages through one site's eigenbasis, msg = x + ((x.V) * (d - 1)).V^-1, every
-        // matrix element loaded once for both, two eigen-coordinates per step (the step loop is
-        // not unrolled: a fully unrolled q x q transport needs more registers than a thread has)
         auto propagate2 = [&](int m0, const float* ea, const float* eb, const float (&xa)[W],
                               const float (&xb)[W], float (&ma)[W], float (&mb)[W]) {
-#pragma unroll
-            for (int j = 0; j < W; ++j) {
-                ma[j] = j < Q ? xa[j] : 0.f;
-                mb[j] = j < Q ? xb[j] : 0.f;
-            }
-#pragma unroll 1
-            for (int kk = 0; kk < KP; ++kk) {
-                float ya0[2] = {0.f, 0.f}, ya1[2] = {0.f, 0.f}, yb0[2] = {0.f, 0.f}, yb1[2] = {0.f, 0.f};
-#pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    const float2 v = m2(m0, (i * KP + kk) * 2 * kSSMaxSites);
-                    ya0[i & 1] = fmaf(xa[i], v.x, ya0[i & 1]);
-                    ya1[i & 1] = fmaf(xa[i], v.y, ya1[i & 1]);
-                    yb0[i & 1] = fmaf(xb[i], v.x, yb0[i & 1]);
-                    yb1[i & 1] = fmaf(xb[i], v.y, yb1[i & 1]);
-                }
-                const float za0 = (ya0[0] + ya0[1]) * ea[2 * kk * NT], za1 = (ya1[0] + ya1[1]) * ea[(2 * kk + 1) * NT];
-                const float zb0 = (yb0[0] + yb0[1]) * eb[2 * kk * NT], zb1 = (yb1[0] + yb1[1]) * eb[(2 * kk + 1) * NT];
-#pragma unroll
-                for (int j = 0; j < Q; ++j) {
-                    const float2 u = m2(m0, MS + (j * KP + kk) * 2 * kSSMaxSites);
-                    ma[j] = fmaf(za1, u.y, fmaf(za0, u.x, ma[j]));
-                    mb[j] = fmaf(zb1, u.y, fmaf(zb0, u.x, mb[j]));
-                }
-            }
+            ss_propagate2<Q, W, NT>(mats_s, m0, ea, eb, xa, xb, ma, mb);
         };
-        // ev = o + V.((V^-1.o) * (d - 1)) for two vectors
         auto evolve2 = [&](int m0, const float* ea, const float* eb, const float (&oa)[W], const float (&ob)[W],
                            float (&va)[W], float (&vb)[W]) {
+            ss_evolve2<Q, W, NT>(mats_s, m0, ea, eb, oa, ob, va, vb);
+        };
+        auto lut_row = [&](int code, float (&x)[W]) {
+            const float4* l4 = reinterpret_cast<const float4*>(lut_s + code * W);
 #pragma unroll
-            for (int i = 0; i < W; ++i) {
-                va[i] = i < Q ? oa[i] : 0.f;
-                vb[i] = i < Q ? ob[i] : 0.f;
-            }
-#pragma unroll 1
-            for (int kk = 0; kk < KP; ++kk) {
-                float ya0[2] = {0.f, 0.f}, ya1[2] = {0.f, 0.f}, yb0[2] = {0.f, 0.f}, yb1[2] = {0.f, 0.f};
-#pragma unroll
-                for (int j = 0; j < Q; ++j) {
-                    const float2 u = m2(m0, MS + (j * KP + kk) * 2 * kSSMaxSites);
-                    ya0[j & 1] = fmaf(u.x, oa[j], ya0[j & 1]);
-                    ya1[j & 1] = fmaf(u.y, oa[j], ya1[j & 1]);
-                    yb0[j & 1] = fmaf(u.x, ob[j], yb0[j & 1]);
-                    yb1[j & 1] = fmaf(u.y, ob[j], yb1[j & 1]);
-                }
-                const float za0 = (ya0[0] + ya0[1]) * ea[2 * kk * NT], za1 = (ya1[0] + ya1[1]) * ea[(2 * kk + 1) * NT];
-                const float zb0 = (yb0[0] + yb0[1]) * eb[2 * kk * NT], zb1 = (yb1[0] + yb1[1]) * eb[(2 * kk + 1) * NT];
-#pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    const float2 v = m2(m0, (i * KP + kk) * 2 * kSSMaxSites);
-                    va[i] = fmaf(v.y, za1, fmaf(v.x, za0, va[i]));
-                    vb[i] = fmaf(v.y, zb1, fmaf(v.x, zb0, vb[i]));
-                }
+            for (int q4 = 0; q4 < W / 4; ++q4) {
+                const float4 v = l4[q4];
+                x[4 * q4] = v.x; x[4 * q4 + 1] = v.y; x[4 * q4 + 2] = v.z; x[4 * q4 + 3] = v.w;
             }
         };
         auto tip_row = [&](int64_t gk, float (&x)[W]) {
             const int r = __ldg(a.f.tip_row + gk);
-            const int code = r < 0 ? 0 : (int)__ldg(a.f.tip_codes + tr.tip_base + (int64_t)r * P + pc);
-#pragma unroll
-            for (int j = 0; j < W; ++j) x[j] = lut_s[code * W + j];
+            lut_row(r < 0 ? 0 : (int)__ldg(a.f.tip_codes + tr.tip_base + (int64_t)r * P + pc), x);
         };
         auto mask_of = [&](int64_t gk) -> float {
-            if (!has_masks) return 1.f;
+            if constexpr (!has_masks) return 1.f;
             const int64_t mo = __ldg(a.f.mask_off + gk);
             return mo < 0 ? 1.f : (float)__ldg(a.f.masks + mo + pc);
         };
@@ -210,6 +311,16 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             if (c >= n_int) tip_row(nb + c, x);
             else load_row<W>(row(partial, c), x);
         };
+        // the same with the tip's row already known (from child_pair)
+        auto node_in_t = [&](int c, int trow, float (&x)[W]) {
+            if (c < n_int) {
+                load_row<W>(row(partial, c), x);
+            } else {
+                lut_row(trow < 0 ? 0 : (int)__ldg(a.f.tip_codes + tr.tip_base + (int64_t)trow * P + pc), x);
+            }
+        };
+        const int4* const nrec = reinterpret_cast<const int4*>(a.f.node_rec);
+        const int4* const cpair = reinterpret_cast<const int4*>(a.f.child_pair);
 
         // ------------------------------------------------------------ post-order
         // r *= max(1e-12, msg)^mask for one child, then the power-of-two rescale
@@ -235,7 +346,18 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             for (int j = 1; j < Q; ++j) mx = fmaxf(mx, r[j]);
             if (mx < kSSRescaleBelow) {
                 const int e = pow2_exponent(mx);
-                scale_pow2<W>(r, e);
+                if (e >= -125 && e <= 126) {
+                    const float sc = __uint_as_float((unsigned)(127 - e) << 23);
+#pragma unroll
+                    for (int j = 0; j < W; ++j) r[j] *= sc;
+                } else {
+                    SSRow<W> t;
+#pragma unroll
+                    for (int j = 0; j < W; ++j) t.v[j] = r[j];
+                    t = ss_ldexp_row<W>(t, e);
+#pragma unroll
+                    for (int j = 0; j < W; ++j) r[j] = t.v[j];
+                }
                 esum += e;
             }
         };
@@ -243,25 +365,31 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
             for (int k = active ? lo + g : hi; k < hi; k += G) {
                 const int64_t gk = nb + k;
-                const int c_lo = __ldg(a.f.child_off + gk), c_hi = __ldg(a.f.child_off + gk + 1);
+                // the node's record and (two children) its children with their tip rows, one load each
+                const int4 rec = __ldg(nrec + gk), cpq = __ldg(cpair + gk);
+                const int c_lo = rec.x, c_hi = rec.y;
+                const bool bin = c_hi - c_lo == 2;
                 float r[W];
 #pragma unroll
                 for (int j = 0; j < W; ++j) r[j] = j < Q ? 1.f : 0.f;
                 for (int ci = c_lo; ci < c_hi; ci += 2) {
                     // children two at a time (the last one alone, transported twice)
-                    const int ca = __ldg(a.f.child_idx + ci);
+                    const int ca = bin ? cpq.x : __ldg(a.f.child_idx + ci);
                     const bool two = ci + 1 < c_hi;
-                    const int cb = two ? __ldg(a.f.child_idx + ci + 1) : ca;
+                    const int cb = bin ? cpq.z : (two ? __ldg(a.f.child_idx + ci + 1) : ca);
+                    const int ta = bin ? cpq.y : (ca >= n_int ? __ldg(a.f.tip_row + nb + ca) : -1);
+                    const int tb = bin ? cpq.w : (cb >= n_int ? __ldg(a.f.tip_row + nb + cb) : -1);
+                    const double ba = __ldg(a.f.bl + nb + ca), bb = two ? __ldg(a.f.bl + nb + cb) : 0.0;
                     float xa[W], xb[W], ma[W], mb[W];
-                    node_in(ca, xa);
-                    stage_e(e0, __ldg(a.f.bl + nb + ca));
-                    if (two) {
-                        node_in(cb, xb);
-                        stage_e(e1, __ldg(a.f.bl + nb + cb));
-                    } else {
+                    node_in_t(ca, ta, xa);
+                    if (two) node_in_t(cb, tb, xb);
+                    else {
 #pragma unroll
                         for (int j = 0; j < W; ++j) xb[j] = xa[j];
                     }
+                    // one copy of the staging code for both branches
+#pragma unroll 1
+                    for (int c2 = 0; c2 < (two ? 2 : 1); ++c2) stage_e(c2 ? e1 : e0, c2 ? bb : ba);
                     propagate2(mbase(), e0, two ? e1 : e0, xa, xb, ma, mb);
                     absorb(ca, xa, ma, r);
                     if (two) absorb(cb, xb, mb, r);
@@ -280,7 +408,8 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             double corr = 0.0;
             for (int gg = 0; gg < G; ++gg) {
                 tot += red[gg * np + tid];
-                corr += (double)red_corr[gg * np + tid];
+                // mask corrections exist only with masks (GB300 issues FP64 adds slowly)
+                if constexpr (has_masks) corr += (double)red_corr[gg * np + tid];
             }
             const int kr = n_int - 1;
             float x[W], pr[W];
@@ -326,12 +455,12 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             }
             if (keep_outgroup) {
                 const bool is_tip = c >= n_int;
-                float s = 0.f;
+                SSRow<W> t;
 #pragma unroll
-                for (int j = 0; j < Q; ++j) s += o[j];
-                const float inv = __fdividef(1.f, s);
+                for (int j = 0; j < W; ++j) t.v[j] = o[j];
+                t = ss_normalized<Q, W>(t);
 #pragma unroll
-                for (int j = 0; j < Q; ++j) o[j] *= inv;
+                for (int j = 0; j < W; ++j) o[j] = t.v[j];
                 float* og = reinterpret_cast<float*>(is_tip ? a.o.tip_outgroup : a.o.outgroup);
                 const int64_t orow = is_tip ? tr.tipprof_base + (int64_t)(c - n_int) * P + pc
                                             : tr.prof_base + (int64_t)c * P + pc;
@@ -355,9 +484,15 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             const float inv = __fdividef(1.f, s);
 #pragma unroll
             for (int i = 0; i < Q; ++i) x[i] *= inv;
-            const int st = a.o.node_uniform
-                               ? sample_cdf<Q, float, W>(x, a.o.node_uniform[tr.state_base + (int64_t)c * P + pc])
-                               : argmax_first<Q, float, W>(x);
+            int st;
+            if (a.o.node_uniform) {
+                SSRow<W> t;
+#pragma unroll
+                for (int j = 0; j < W; ++j) t.v[j] = x[j];
+                st = ss_sample<Q, W>(t, a.o.node_uniform[tr.state_base + (int64_t)c * P + pc]);
+            } else {
+                st = argmax_first<Q, float, W>(x);
+            }
             if (valid) {
                 const int64_t prow = is_tip ? tr.tipprof_base + (int64_t)(c - n_int) * P + pc
                                             : tr.prof_base + (int64_t)c * P + pc;
@@ -374,19 +509,23 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
             for (int p = active ? lo + g : hi; p < hi; p += G) {
                 const int64_t gp = nb + p;
-                const int c_lo = __ldg(a.f.child_off + gp), c_hi = __ldg(a.f.child_off + gp + 1);
+                const int4 rec = __ldg(nrec + gp), cpq = __ldg(cpair + gp);
+                const int c_lo = rec.x, c_hi = rec.y;
+                const bool bin = c_hi - c_lo == 2;
                 int ci = c_lo;
                 while (true) {
-                    while (ci < c_hi && !tips_needed && __ldg(a.f.child_idx + ci) >= n_int) ++ci;
+                    // the next needed children, two at a time (two-child parents: from child_pair)
+                    auto child = [&](int i) { return bin ? (i == c_lo ? cpq.x : cpq.z) : __ldg(a.f.child_idx + i); };
+                    while (ci < c_hi && !tips_needed && child(ci) >= n_int) ++ci;
                     if (ci >= c_hi) break;
-                    const int ca = __ldg(a.f.child_idx + ci++);
-                    while (ci < c_hi && !tips_needed && __ldg(a.f.child_idx + ci) >= n_int) ++ci;
+                    const int ca = child(ci++);
+                    while (ci < c_hi && !tips_needed && child(ci) >= n_int) ++ci;
                     const bool two = ci < c_hi;
-                    const int cb = two ? __ldg(a.f.child_idx + ci++) : ca;
+                    const int cb = two ? child(ci++) : ca;
                     float pv[W], oa[W], ob[W];
                     load_row<W>(row(posterior, p), pv);
-                    stage_e(e0, __ldg(a.f.bl + nb + ca));
-                    if (two) stage_e(e1, __ldg(a.f.bl + nb + cb));
+#pragma unroll 1
+                    for (int c2 = 0; c2 < (two ? 2 : 1); ++c2) stage_e(c2 ? e1 : e0, __ldg(a.f.bl + nb + (c2 ? cb : ca)));
                     const float* eb = two ? e1 : e0;
                     if (ca < n_int && (!two || cb < n_int)) {
                         // the children's messages as the post-order formed them
@@ -405,7 +544,12 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
 #pragma unroll
                             for (int j = 0; j < W; ++j) xb[j] = xa[j];
                         }
-                        propagate2(mbase(), e0, eb, xa, xb, oa, ob);
+                        SSRow<W> ra, rb;
+#pragma unroll
+                        for (int j = 0; j < W; ++j) { ra.v[j] = xa[j]; rb.v[j] = xb[j]; }
+                        const SSRowPair<W> m = ss_propagate2_ool<Q, W, NT>(mats_s, mbase(), e0, eb, ra, rb);
+#pragma unroll
+                        for (int j = 0; j < W; ++j) { oa[j] = m.a[j]; ob[j] = m.b[j]; }
                     }
                     outgroup_of(ca, pv, oa);
                     if (two) outgroup_of(cb, pv, ob);
@@ -434,19 +578,19 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
     }
 }
 
-template <int Q>
-static tt_status launch_ss_f32(const SSF32Params& prm, int max_np, int blocks, cudaStream_t s) {
+template <int Q, bool HM>
+static tt_status launch_ss_f32_hm(const SSF32Params& prm, int max_np, int blocks, cudaStream_t s) {
     constexpr int W = round4(Q);
     // 20+ states keep about 90 floats live per thread (a message, its eigen-coordinates and the
     // node's running product): 384 threads (170 registers a thread, 12 warps per SM)
     constexpr int NT = Q >= 20 ? 384 : 512;
     constexpr int KP = (Q + 1) / 2;
     const size_t dyn = ((size_t)2 * Q * KP * max_np * 2 + (size_t)2 * 2 * KP * NT) * sizeof(float);
-    static size_t configured[64] = {};
+    static size_t configured[64] = {};  // per instance (Q, HM) and device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || dyn > configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(marginal_ss_f32_kernel<Q, W, NT>,
+        cudaError_t e = cudaFuncSetAttribute(marginal_ss_f32_kernel<Q, W, NT, HM>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
         if (e != cudaSuccess) {
             set_error("tt_marginal_ss_f32: %zu bytes of shared memory: %s", dyn, cudaGetErrorString(e));
@@ -454,8 +598,14 @@ static tt_status launch_ss_f32(const SSF32Params& prm, int max_np, int blocks, c
         }
         if (dev >= 0 && dev < 64) configured[dev] = dyn;
     }
-    marginal_ss_f32_kernel<Q, W, NT><<<blocks, NT, dyn, s>>>(prm);
+    marginal_ss_f32_kernel<Q, W, NT, HM><<<blocks, NT, dyn, s>>>(prm);
     return check_launch("tt_marginal_ss_f32");
+}
+
+template <int Q>
+static tt_status launch_ss_f32(const SSF32Params& prm, int max_np, int blocks, cudaStream_t s) {
+    return prm.f.mask_off ? launch_ss_f32_hm<Q, true>(prm, max_np, blocks, s)
+                          : launch_ss_f32_hm<Q, false>(prm, max_np, blocks, s);
 }
 
 tt_status tree_sums(const tt_forest* f, const double* site_lh, double* tree_lh, cudaStream_t s);

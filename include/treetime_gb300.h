@@ -149,6 +149,9 @@ typedef struct tt_model {
     const float* lut_log2;     /* [256][2][width] log(max(lut, 1e-12)) (non-finite -> -1e10) as
                                   FP32 pairs hi, lo (hi + lo = the FP64 value to ~48 bits): the
                                   joint kernel's tip log profiles; may be NULL except for tt_joint */
+    const float* logpi2;       /* [n_models][2][width] log(pi) as FP32 pairs (log 0 -> hi -inf,
+                                  lo 0): the joint kernel's root prior; may be NULL except for
+                                  tt_joint */
 } tt_model;
 
 /* Branch matrices produced by tt_branch_pmats for every node (the branch above it), rows padded
@@ -284,7 +287,7 @@ tt_status tt_marginal_ss_f32(const tt_forest* f, const tt_ss_f32* m, const int32
  * Max-product reconstruction in the log domain (double-float: FP32 pairs, ~48 significant bits),
  * root argmax/sampling, pre-order backtrack, over the pattern ranges of the FP32 marginal kernel
  * (work_f32, node_rec, child_pair, threads_f32).  Requires tt_branch_pmats with logp2 and
- * logp2_pair, and tt_model.lut_log2.  Replaces TreeAnc._ml_anc_joint
+ * logp2_pair, and tt_model.lut_log2 and logpi2.  Replaces TreeAnc._ml_anc_joint
  * (treetime/treeanc.py:934-1080). */
 tt_status tt_joint(const tt_forest* f, const tt_model* m, const tt_pmats* pm, const tt_joint_out* out,
                    int32_t* status, void* stream);
@@ -338,7 +341,8 @@ tt_status tt_mutation_counts_ss(const tt_forest* f, const tt_ss_model* m, int32_
 /* Joint reconstruction that allocates nothing.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (hosts that only hand out their own pre-sized
  * buffers, pools that reserve all device memory at start-up, paths that cannot afford an
- * allocation's synchronisation).  Same results as tt_branch_pmats + tt_joint; the branch matrices
+ * allocation's synchronisation).  Same results as tt_branch_pmats + tt_joint (the model needs
+ * lut_log2 and logpi2, as for tt_joint); the branch matrices
  * and the msg / joint_Cx scratch live in one fixed device array of
  * TT_JOINT_NOALLOC_SCRATCH_BYTES inside the library (held by every GPU that loads it).
  * `internal_rows` = sum over trees of n_int * n_patterns.  Problems needing more scratch than
@@ -461,6 +465,12 @@ tt_status tt_branch_mutation_matrix(const tt_forest* f, const tt_model* m, int32
                                     const int32_t* node, const void* pp, const int64_t* pp_row, const void* pc,
                                     const int64_t* pc_row, int32_t prec, const double* p64, double* out,
                                     void* stream);
+/* The same under a site-specific model (one tree): every site's own P_a(t) + 1e-24
+ * (GTR_site_specific.expQt, treetime/gtr_site_specific.py:365-371, in
+ * treetime/treeanc.py:1106-1108); the model needs tt_ss_pstack's stack when `approximate`. */
+tt_status tt_branch_mutation_matrix_ss(const tt_forest* f, const tt_ss_model* m, int32_t tree, int32_t n_patterns,
+                                       const int32_t* node, const void* pp, const int64_t* pp_row, const void* pc,
+                                       const int64_t* pc_row, int32_t prec, double* out, void* stream);
 
 /* ------------------------------------------------------------ Fitch parsimony
  * TreeAnc._fitch_anc (treetime/treeanc.py:575-686) with TreeTime's list semantics: a node's list

@@ -6,7 +6,8 @@ GTR.infer) and the CPU oracle's per-pattern counts.
 Tolerances: counts and times 1e-10 relative (+1e-10 absolute) per pattern and
 summed (FP64 profiles), 2e-5 of the largest entry (FP32 profiles, counted in
 FP32); inferred W, pi, mu 1e-9 relative from FP64 profiles, 1e-5 relative
-from FP32-scaled profiles; mutation matrices 1e-12 absolute (FP64)."""
+from FP32-scaled profiles; mutation matrices 1e-12 absolute (FP64; site-specific
+models 1e-10 relative + 1e-12 absolute), 1e-5 absolute (FP32)."""
 
 import numpy as np
 import pytest
@@ -82,8 +83,11 @@ def test_infer_gtr_matches_treetime(case, precision):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_branch_mutation_matrix_matches_oracle(precision):
-    g = gc.load("gtrinf_nuc5")
+@pytest.mark.parametrize("case", ["gtrinf_nuc5", "gtrinf_ss_current"])
+def test_branch_mutation_matrix_matches_oracle(case, precision):
+    """A single-matrix model, and a site-specific one (each site's own
+    interpolated P_a(t), treeanc.py:1106-1108)."""
+    g = gc.load(case)
     t = _tree_anc(g, precision)
     t.infer_ancestral_sequences(marginal=True)
     _, _, res = gc.gtrinf_oracle(g, "marginal")
@@ -94,7 +98,13 @@ def test_branch_mutation_matrix_matches_oracle(precision):
         got = t.get_branch_mutation_matrix(n)
         want = anc.branch_mutation_matrix(model, res["outgroup_LH"][n.name], res["subtree_LH"][n.name],
                                           anc.branch_length_to_gtr(n, L))
-        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 if precision == "f64" else 1e-5, err_msg=n.name)
+        if precision == "f32":
+            np.testing.assert_allclose(got, want, rtol=0, atol=1e-5, err_msg=n.name)
+        elif bool(g["site_specific"]):
+            # each site's interpolated P_a(t) and the FP64 profiles summed in another order
+            np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-12, err_msg=n.name)
+        else:
+            np.testing.assert_allclose(got, want, rtol=0, atol=1e-12, err_msg=n.name)
         full = t.get_branch_mutation_matrix(n, full_sequence=True)
         assert full.shape == (L,) + got.shape[1:]
 

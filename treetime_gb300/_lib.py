@@ -43,7 +43,7 @@ class TTForest(C.Structure):
 
 class TTModel(C.Structure):
     _fields_ = [("n_models", i32), ("n_states", i32), ("V", vp), ("Vinv", vp), ("lam", vp), ("mu", vp),
-                ("pi", vp), ("lut", vp), ("lut_log2", vp)]
+                ("pi", vp), ("lut", vp), ("lut_log2", vp), ("logpi2", vp)]
 
 
 class TTPmats(C.Structure):
@@ -104,6 +104,7 @@ _SIGS = {
                                  i64, vp]),
     "tt_mutation_counts_joint": (i32, [P(TTForest), i32, i32, i64, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp]),
     "tt_branch_mutation_matrix": (i32, [P(TTForest), P(TTModel), i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp]),
+    "tt_branch_mutation_matrix_ss": (i32, [P(TTForest), P(TTSSModel), i32, i32, vp, vp, vp, vp, vp, i32, vp, vp]),
     "tt_compress_columns": (i32, [vp, i64, i64, i32, vp, vp, vp]),
 }
 

@@ -735,15 +735,19 @@ class GPUAncMixin:
         """[L, q, q] joint distribution of the states at both ends of the branch
         above `node` from the last marginal reconstruction (i child, j parent),
         computed on the device (treetime/treeanc.py:1085-1120)."""
-        if self.gtr.is_site_specific:
-            raise NotImplementedError("mutation matrices with site-specific models are not supported on the GPU")
         sess = self._get_session()
-        model = engine.model_for(self.gtr, getattr(self, "device", None))
-        engine.branch_pmats(sess["forest"], model, sess["bufs"])
-        p64 = sess["bufs"].cache[("p64", engine.torch().float64)]
-        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups([node], sess):
-            m = engine.branch_mutation_matrix(sess["forest"], model, p64, 0, int(kk[0]), pp, int(pp_row[0]), pc,
-                                              int(pc_row[0]), self._gpu_precision()).cpu().numpy()
+        if self.gtr.is_site_specific:
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups([node], sess):
+                m = engine.branch_mutation_matrix_ss(sess["forest"], self.gtr, sess["bufs"], int(kk[0]), pp,
+                                                     int(pp_row[0]), pc, int(pc_row[0]),
+                                                     self._gpu_precision()).cpu().numpy()
+        else:
+            model = engine.model_for(self.gtr, getattr(self, "device", None))
+            engine.branch_pmats(sess["forest"], model, sess["bufs"])
+            p64 = sess["bufs"].cache[("p64", engine.torch().float64)]
+            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups([node], sess):
+                m = engine.branch_mutation_matrix(sess["forest"], model, p64, 0, int(kk[0]), pp, int(pp_row[0]),
+                                                  pc, int(pc_row[0]), self._gpu_precision()).cpu().numpy()
         if full_sequence:
             return m[self.data.full_to_compressed_sequence_map]
         return m

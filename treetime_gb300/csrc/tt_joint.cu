@@ -27,6 +27,7 @@ namespace tt {
 struct JointParams {
     tt_forest f;
     const double* pi;
+    const float* logpi2;     // [n_models][2][W] pairs of log(pi)
     const float* lut_log2;   // [256][2][W] pairs of log(max(profile, 1e-12)), non-finite -> -1e10
     const float* lp2;        // [n_nodes][Q][2][W] pairs of log(max(P, 1e-12))
     const float* lp2_pair;   // [n_nodes][2][Q][2][W]: children of two-child nodes side by side
@@ -355,49 +356,66 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
             }
             cp_async_commit();
         };
-        // the root's step: Lx + log(pi), first argmax of the normalised exp profile (or a draw)
+        // the root's step: Lx + log(pi) (pairs), its first argmax, or a draw from the normalised exp
+        // profile.  The argmax is taken on the pairs themselves: exp and the normalisation are
+        // monotone, so they change the choice only between values equal to FP64's last bits (and
+        // FP64 issues at 1/64 of the FP32 rate on GB300); the draw keeps TreeTime's FP64 profile.
         auto root_step = [&](int k, const float (&mh)[S], const float (&ml)[S]) {
-            const double* pi = a.pi + (int64_t)tr.model * Q;
+            const float* lpi = a.logpi2 + (int64_t)tr.model * 2 * W;
             float rh[S], rlo[S];
 #pragma unroll
             for (int s = 0; s < S; ++s) {
                 rh[s] = 0.f;
                 rlo[s] = 0.f;
                 if (j0 + s < Q) {
-                    const double lp = log(__ldg(pi + j0 + s));
-                    const float h = (float)lp;
-                    dd_add(mh[s], ml[s], h, (float)(lp - (double)h), rh[s], rlo[s]);
+                    const float h = __ldg(lpi + j0 + s), l = __ldg(lpi + W + j0 + s);
+                    if (h == -INFINITY) { rh[s] = -INFINITY; rlo[s] = 0.f; }  // pi = 0
+                    else dd_add(mh[s], ml[s], h, l, rh[s], rlo[s]);
                 }
             }
             // gather the pattern's Q values (every lane of a pattern holds all of them)
-            double full[W];
+            float fh[W], fl[W];
 #pragma unroll
             for (int r = 0; r < LPP; ++r)
 #pragma unroll
                 for (int s2 = 0; s2 < S; ++s2) {
-                    const float h = LPP == 1 ? rh[s2] : __shfl_sync(0xffffffffu, rh[s2], r, LPP);
-                    const float l = LPP == 1 ? rlo[s2] : __shfl_sync(0xffffffffu, rlo[s2], r, LPP);
-                    full[r * S + s2] = (double)h + (double)l;
+                    fh[r * S + s2] = LPP == 1 ? rh[s2] : __shfl_sync(0xffffffffu, rh[s2], r, LPP);
+                    fl[r * S + s2] = LPP == 1 ? rlo[s2] : __shfl_sync(0xffffffffu, rlo[s2], r, LPP);
                 }
-            double mx = full[0];
+            int st = 0;
+            if (a.o.root_uniform) {
+                double full[W];
 #pragma unroll
-            for (int j = 1; j < Q; ++j) mx = full[j] > mx ? full[j] : mx;
-            double pr[W], sum = 0.0;
+                for (int j = 0; j < W; ++j) full[j] = (double)fh[j] + (double)fl[j];
+                double mx = full[0];
 #pragma unroll
-            for (int j = 0; j < W; ++j) {
-                pr[j] = j < Q ? exp(full[j] - mx) : 0.0;
-                sum += pr[j];
+                for (int j = 1; j < Q; ++j) mx = full[j] > mx ? full[j] : mx;
+                double pr[W], sum = 0.0;
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                    pr[j] = j < Q ? exp(full[j] - mx) : 0.0;
+                    sum += pr[j];
+                }
+                const double inv = 1.0 / sum;
+#pragma unroll
+                for (int j = 0; j < Q; ++j) pr[j] *= inv;
+                st = sample_cdf<Q, double, W>(pr, a.o.root_uniform[tr.pat_base + pc]);
+            } else {
+                // first maximum of the pairs; a NaN is the maximum (numpy's argmax)
+                float bh = fh[0], bl = fl[0];
+#pragma unroll
+                for (int j = 1; j < Q; ++j) {
+                    const bool take = (fh[j] > bh || (fh[j] == bh && fl[j] > bl) || (fh[j] != fh[j] && bh == bh)) &&
+                                      bh == bh;
+                    if (take) { bh = fh[j]; bl = fl[j]; st = j; }
+                }
             }
-            const double inv = 1.0 / sum;
+            float sh = fh[0], sl = fl[0];
 #pragma unroll
-            for (int j = 0; j < Q; ++j) pr[j] *= inv;
-            const int st = a.o.root_uniform ? sample_cdf<Q, double, W>(pr, a.o.root_uniform[tr.pat_base + pc])
-                                            : argmax_first<Q, double, W>(pr);
-            double lh = full[0];
-#pragma unroll
-            for (int j = 1; j < Q; ++j) lh = st == j ? full[j] : lh;
+            for (int j = 1; j < Q; ++j)
+                if (st == j) { sh = fh[j]; sl = fl[j]; }
             if (valid && part == 0) {
-                a.o.site_lh[tr.pat_base + p] = lh;
+                a.o.site_lh[tr.pat_base + p] = (double)sh + (double)sl;
                 states0[(int64_t)k * P] = (uint8_t)st;
             }
         };
@@ -568,7 +586,7 @@ using namespace tt;
 
 extern "C" tt_status tt_joint(const tt_forest* f, const tt_model* m, const tt_pmats* pm, const tt_joint_out* out,
                               int32_t* status, void* stream) {
-    if (!f || !m || !pm || !pm->logp2 || !pm->logp2_pair || !m->lut_log2 || !out || !out->msg || !out->cx ||
+    if (!f || !m || !pm || !pm->logp2 || !pm->logp2_pair || !m->lut_log2 || !m->logpi2 || !out || !out->msg || !out->cx ||
         !out->states || !out->site_lh || !out->tree_lh || out->rows < 0 || f->width != round4(f->n_states) ||
         m->n_states != f->n_states || !f->work_f32 || f->n_work_f32 <= 0 || !f->node_rec || !f->child_pair) {
         set_error("tt_joint: invalid arguments");
@@ -583,6 +601,7 @@ extern "C" tt_status tt_joint(const tt_forest* f, const tt_model* m, const tt_pm
     JointParams prm;
     prm.f = *f;
     prm.pi = m->pi;
+    prm.logpi2 = m->logpi2;
     prm.lut_log2 = m->lut_log2;
     prm.lp2 = pm->logp2;
     prm.lp2_pair = pm->logp2_pair;

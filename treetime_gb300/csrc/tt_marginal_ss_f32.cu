@@ -163,7 +163,10 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
     __shared__ int red[NT];
     __shared__ float red_corr[NT];
     __shared__ unsigned diff_red[NT / 32];
-    __shared__ double grid_s[kSSGridCap];
+    // the time grid in FP32 and the reciprocals of its steps (FP64 issues at 1/64 of the FP32 rate
+    // on GB300: an FP64 search and division per branch cost thousands of cycles on every level)
+    __shared__ float grid_f[kSSGridCap];
+    __shared__ float grid_inv[kSSGridCap];
     // V as [i][k / 2][site][2] (V[i][k] and V[i][k + 1] of a site side by side), then V^-1
     // transposed the same way, [j][k / 2][site][2] = V^-1[k][j]: one 8-byte load gives a thread two
     // eigen-coordinates of its own site, the lanes of a warp (consecutive sites) read consecutive
@@ -178,8 +181,13 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         lut_s[i] = j < Q ? (float)__ldg(a.m.lut + c * Q + j) : 0.f;
     }
     const bool grid_sm = a.m.n_grid <= kSSGridCap;
+    const float rate_f = (float)a.m.rate_scale;
     if (grid_sm)
-        for (int i = tid; i < a.m.n_grid; i += NT) grid_s[i] = __ldg(a.m.grid + i);
+        for (int i = tid; i < a.m.n_grid; i += NT) {
+            const double gi = __ldg(a.m.grid + i);
+            grid_f[i] = (float)gi;
+            grid_inv[i] = i > 0 ? 1.f / (float)(gi - __ldg(a.m.grid + i - 1)) : 0.f;
+        }
     const tt_tree tr = a.f.trees[0];
     const int P = tr.n_patterns, n_int = tr.n_int;
     const int64_t nb = tr.node_base;
@@ -251,17 +259,31 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         // interpolation between two rows of the FP64-computed expm1 table (TreeTime's interpolated
         // P(t)), or expm1f of mu*lambda_k*t.  All loads of a branch are issued together, once.
         auto stage_e = [&](float* e, double t) {
-            if (a.m.n_grid > 0 && t * a.m.rate_scale < 10.0) {
-                // interp1d(kind='linear'): hi = searchsorted(grid, t) clipped to [1, n-1], lo = hi - 1
-                auto gv = [&](int i) -> double { return grid_sm ? grid_s[i] : __ldg(a.m.grid + i); };
-                int lo = 0, hi = a.m.n_grid;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (gv(mid) < t) lo = mid + 1; else hi = mid;
+            const float tf = (float)t;
+            // interp1d(kind='linear'): hi = searchsorted(grid, t) clipped to [1, n-1], lo = hi - 1,
+            // in FP32 from the shared grid (the interpolation is continuous across grid points, so
+            // a bracket or a branch that FP32 rounding flips at a boundary gives the same value to
+            // FP32 precision); in FP64 only for grids longer than the shared copy
+            const bool interp = a.m.n_grid > 0 && (grid_sm ? tf * rate_f < 10.f : t * a.m.rate_scale < 10.0);
+            if (interp) {
+                int lo = 0, hi = a.m.n_grid, ih;
+                float w;
+                if (grid_sm) {
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (grid_f[mid] < tf) lo = mid + 1; else hi = mid;
+                    }
+                    ih = lo < 1 ? 1 : (lo > a.m.n_grid - 1 ? a.m.n_grid - 1 : lo);
+                    w = (tf - grid_f[ih - 1]) * grid_inv[ih];
+                } else {
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (__ldg(a.m.grid + mid) < t) lo = mid + 1; else hi = mid;
+                    }
+                    ih = lo < 1 ? 1 : (lo > a.m.n_grid - 1 ? a.m.n_grid - 1 : lo);
+                    const double xl = __ldg(a.m.grid + ih - 1), xh = __ldg(a.m.grid + ih);
+                    w = (float)((t - xl) / (xh - xl));
                 }
-                const int ih = lo < 1 ? 1 : (lo > a.m.n_grid - 1 ? a.m.n_grid - 1 : lo);
-                const double xl = gv(ih - 1), xh = gv(ih);
-                const float w = (float)((t - xl) / (xh - xl));
                 const float4* rl = reinterpret_cast<const float4*>(a.m.em1_grid + ((int64_t)(ih - 1) * P + pc) * W);
                 const float4* rh = reinterpret_cast<const float4*>(a.m.em1_grid + ((int64_t)ih * P + pc) * W);
 #pragma unroll
@@ -275,7 +297,6 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             } else {
                 // long branches (or no grid): one exponential at a time, a rolled loop (the
                 // inlined q expm1f would crowd the instruction cache of the common path)
-                const float tf = (float)t;
                 const float* ml = a.m.mulam + (int64_t)pc * W;
 #pragma unroll 1
                 for (int k = 0; k < 2 * KP; ++k) e[k * NT] = k < Q ? expm1f(__ldg(ml + k) * tf) : 0.f;

@@ -18,12 +18,6 @@ namespace tt {
 
 namespace {
 
-__device__ __forceinline__ double warp_total(double v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
-
 struct MutParams {
     tt_forest f;
     tt_model m;
@@ -416,6 +410,38 @@ __global__ void branch_mutation_matrix_kernel(MutParams a, double* __restrict__ 
     }
 }
 
+// get_branch_mutation_matrix under a site-specific model: each site's own P_a(t) (not clamped, as
+// GTR_site_specific.expQt) + 1e-24, one thread per site.
+template <int Q>
+__global__ void __launch_bounds__(128) branch_mutation_matrix_ss_kernel(MutParams a, tt_ss_model sm,
+                                                                         double* __restrict__ out) {
+    const tt_tree tr = a.f.trees[a.tree];
+    const int P = a.P;
+    const int64_t g = a.node_of[0];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const BranchRows r = branch_rows(a, tr, 0, p);
+        const int site = tr.pat_base + p;
+        SSBranch<Q> br;
+        br.init(sm, site, a.f.bl[g]);
+        double pp[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) pp[j] = r.parent(j);
+        double* o = out + (int64_t)p * Q * Q;
+        double tot = 0.0;
+        for (int i = 0; i < Q; ++i) {
+            const double ci = r.child(i);
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                const double v = ci * pp[j] * (br.prob(sm, site, a.f.n_patterns, i, j) + kSuperTiny);
+                o[i * Q + j] = v;
+                tot += v;
+            }
+        }
+        const double inv = 1.0 / tot;
+        for (int e = 0; e < Q * Q; ++e) o[e] *= inv;
+    }
+}
+
 bool valid_tree(const tt_forest* f, int tree) { return f && tree >= 0 && tree < f->n_trees; }
 
 // chunks that fit in the workspace, at most `want`
@@ -668,4 +694,42 @@ extern "C" tt_status tt_branch_mutation_matrix(const tt_forest* f, const tt_mode
     const int blocks = sm_count() * 2;
     branch_mutation_matrix_kernel<<<blocks, 128, 0, as_stream(stream)>>>(a, out);
     return check_launch("tt_branch_mutation_matrix");
+}
+
+extern "C" tt_status tt_branch_mutation_matrix_ss(const tt_forest* f, const tt_ss_model* sm, int32_t tree,
+                                                  int32_t n_patterns, const int32_t* node, const void* pp,
+                                                  const int64_t* pp_row, const void* pc, const int64_t* pc_row,
+                                                  int32_t prec, double* out, void* stream) {
+    if (!valid_tree(f, tree) || !sm || n_patterns < 0 || !node || !pp || !pp_row || !pc_row || !out || !sm->lut ||
+        !sm->mu || !sm->lam || !sm->V || !sm->Vinv || sm->n_states != f->n_states ||
+        (sm->approximate && !sm->stack)) {
+        set_error("tt_branch_mutation_matrix_ss: invalid arguments");
+        return TT_ERR_INVALID;
+    }
+    if (n_patterns == 0) return TT_OK;
+    MutParams a{};
+    a.f = *f;
+    a.m.lut = sm->lut;
+    a.m.n_states = f->n_states;
+    a.tree = tree;
+    a.P = n_patterns;
+    a.n = 1;
+    a.node_of = node;
+    a.pp = pp;
+    a.pp_row = pp_row;
+    a.pc = pc;
+    a.pc_row = pc_row;
+    a.prec = prec;
+    const int blocks = (n_patterns + 127) / 128;
+    cudaStream_t s = as_stream(stream);
+    switch (f->n_states) {
+        case 4: branch_mutation_matrix_ss_kernel<4><<<blocks, 128, 0, s>>>(a, *sm, out); break;
+        case 20: branch_mutation_matrix_ss_kernel<20><<<blocks, 128, 0, s>>>(a, *sm, out); break;
+        case 21: branch_mutation_matrix_ss_kernel<21><<<blocks, 128, 0, s>>>(a, *sm, out); break;
+        case 22: branch_mutation_matrix_ss_kernel<22><<<blocks, 128, 0, s>>>(a, *sm, out); break;
+        default:
+            set_error("tt_branch_mutation_matrix_ss: alphabet size %d not compiled (4, 20, 21, 22)", f->n_states);
+            return TT_ERR_UNSUPPORTED;
+    }
+    return check_launch("tt_branch_mutation_matrix_ss");
 }

@@ -210,8 +210,9 @@ class DeviceModel:
         self.lut_host = profile_lut(pm, q)
         self.lut = _to_dev(self.lut_host, dev)
         self.lut_log2 = _to_dev(log_lut_pairs(self.lut_host, WIDTHS[q]), dev)
+        self.logpi2 = _to_dev(log_pi_pairs(np.stack([g.Pi for g in gtrs]), WIDTHS[q]), dev)
         self.struct = TTModel(len(gtrs), q, _p(self.V), _p(self.Vinv), _p(self.lam), _p(self.mu), _p(self.pi),
-                              _p(self.lut), _p(self.lut_log2))
+                              _p(self.lut), _p(self.lut_log2), _p(self.logpi2))
 
 
 def float_pairs(x):
@@ -233,6 +234,20 @@ def log_lut_pairs(lut, w):
     out = np.zeros((lut.shape[0], 2, w), dtype=np.float32)
     out[:, 0, :lut.shape[1]] = hi
     out[:, 1, :lut.shape[1]] = lo
+    return out
+
+
+def log_pi_pairs(pi, w):
+    """[n_models][2][w] FP32 pairs of log(pi) (the joint reconstruction's root
+    prior, treetime/treeanc.py:1021-1023); log 0 is (-inf, 0)."""
+    pi = np.asarray(pi, dtype=np.float64)
+    with np.errstate(divide="ignore"):
+        lg = np.log(pi)
+    hi, lo = float_pairs(lg)
+    lo[~np.isfinite(lg)] = 0.0
+    out = np.zeros((pi.shape[0], 2, w), dtype=np.float32)
+    out[:, 0, :pi.shape[1]] = hi
+    out[:, 1, :pi.shape[1]] = lo
     return out
 
 
@@ -1189,6 +1204,26 @@ def branch_mutation_matrix(forest, model, p64, tree, node, pp, pp_row, pc, pc_ro
                                         _p(pp), _p(d_pp), _p(pc), _p(d_pc),
                                         _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64, _p(p64),
                                         _p(out), _stream()), "tt_branch_mutation_matrix")
+    return out
+
+
+def branch_mutation_matrix_ss(forest, gtr, bufs, node, pp, pp_row, pc, pc_row, precision):
+    """branch_mutation_matrix under a GTR_site_specific model (one tree): every
+    site's own P_a(t) (treetime/treeanc.py:1106-1108)."""
+    t = torch()
+    lib = _lib.load()
+    dev = forest.device
+    q = forest.q
+    P = int(forest.trees_host["n_patterns"][0])
+    arrs = _ss_model64(gtr, bufs, dev, need_stack=True)
+    out = t.empty((P, q, q), dtype=t.float64, device=dev)
+    d_node = _to_dev(np.array([node], np.int32), dev)
+    d_pp = _to_dev(np.array([pp_row], np.int64), dev)
+    d_pc = _to_dev(np.array([pc_row], np.int64), dev)
+    check(lib.tt_branch_mutation_matrix_ss(C.byref(forest.struct), C.byref(arrs["struct"]), 0, P, _p(d_node),
+                                           _p(pp), _p(d_pp), _p(pc), _p(d_pc),
+                                           _lib.TT_PREC_F32 if precision == "f32" else _lib.TT_PREC_F64,
+                                           _p(out), _stream()), "tt_branch_mutation_matrix_ss")
     return out
 
 

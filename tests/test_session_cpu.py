@@ -1,0 +1,80 @@
+"""The session cache's change detection (host logic, no GPU): a device
+session is reused only while every node keeps the same children, in the same
+order, and the same mask objects; anything else rebuilds it."""
+
+from treetime_gb300.anc_gpu import _children, _masks, _same_children, _same_masks
+from treetime_gb300.tree import Clade, parse_newick
+
+
+def _nodes(tree):
+    return list(tree.find_clades())
+
+
+def test_unchanged_tree_matches():
+    t = parse_newick("((A:0.1,B:0.2)x:0.05,(C:0.1,D:0.1)y:0.2,E:0.3)r;")
+    nodes = _nodes(t)
+    ch, ms = _children(nodes), _masks(nodes)
+    assert _same_children(nodes, ch)
+    assert _same_masks(nodes, ms)
+    # branch lengths are not part of the check (they are refreshed on every call)
+    nodes[1].branch_length = 0.7
+    assert _same_children(nodes, ch)
+
+
+def test_topology_changes_are_seen():
+    t = parse_newick("((A:0.1,B:0.2)x:0.05,(C:0.1,D:0.1)y:0.2,E:0.3)r;")
+    nodes = _nodes(t)
+    ch = _children(nodes)
+    x = next(n for n in nodes if n.name == "x")
+    # a child gained (the list grows past the reference)
+    x.clades.append(Clade(name="F", branch_length=0.1))
+    assert not _same_children(nodes, ch)
+    x.clades.pop()
+    assert _same_children(nodes, ch)
+    # a child lost (the list ends early)
+    gone = x.clades.pop()
+    assert not _same_children(nodes, ch)
+    x.clades.append(gone)
+    assert _same_children(nodes, ch)
+    # children reordered
+    x.clades.reverse()
+    assert not _same_children(nodes, ch)
+    x.clades.reverse()
+    # a child replaced by another object with the same name
+    x.clades[0] = Clade(name=x.clades[0].name, branch_length=0.1)
+    assert not _same_children(nodes, ch)
+
+
+def test_mask_changes_are_seen():
+    t = parse_newick("((A:0.1,B:0.2)x:0.05,C:0.3)r;")
+    nodes = _nodes(t)
+    ms = _masks(nodes)
+    nodes[2].mask = [1.0, 0.0]
+    assert not _same_masks(nodes, ms)
+    ms = _masks(nodes)
+    assert _same_masks(nodes, ms)
+    nodes[2].mask = [1.0, 0.0]  # an equal but new mask object
+    assert not _same_masks(nodes, ms)
+
+
+def test_dist2root_by_levels_equals_the_preorder_sums():
+    """The distances to the root that optimize_branch_lengths_joint sets after
+    new lengths are the sums of TreeTime's _calc_dist2root
+    (treetime/treeanc.py:499-510), bit for bit."""
+    import numpy as np
+    from treetime_gb300 import engine, synth
+    from treetime_gb300.anc_gpu import _set_dist2root
+    from treetime_gb300.tree import iter_clades
+    tree = synth.coalescent_tree(300, 0.01, np.random.default_rng(3))
+    lay = engine.TreeLayout(tree.root)
+    lengths = np.random.default_rng(4).random(lay.n_nodes) * 0.01
+    lengths[lay.n_int - 1] = 0.0
+    for n, v in zip(lay.nodes, lengths.tolist()):
+        n.mutation_length = v
+    _set_dist2root(lay, lengths)
+    fast = [n.dist2root for n in lay.nodes]
+    lay.root.dist2root = 0.0
+    for c in iter_clades(lay.root):
+        for ch in c.clades:
+            ch.dist2root = c.dist2root + ch.mutation_length
+    assert fast == [n.dist2root for n in lay.nodes]

@@ -34,17 +34,47 @@ from .errors import MissingDataError
 from .tree import LAZY_ATTRS, Clade
 
 
-def _children_ids(nodes):
-    """Identity of every child of every node, in order (C-level iteration):
-    equal lists mean an unchanged topology below the same root."""
-    return list(map(id, itertools.chain.from_iterable(map(_CLADES, nodes))))
-
-
-def _mask_ids(nodes):
-    return list(map(id, map(getattr, nodes, itertools.repeat("mask"), itertools.repeat(None))))
+def _set_dist2root(layout, lengths):
+    """dist2root of every node from the root's 0 and each node's length, parents
+    before children (internal nodes by decreasing height, then the tips): the
+    additions of TreeTime's _calc_dist2root (treetime/treeanc.py:499-510), in
+    numpy, one height level at a time."""
+    d = np.zeros(layout.n_nodes)
+    par = layout.parent
+    lev = layout.level_off
+    for h in range(layout.n_levels - 1, -1, -1):
+        ks = np.arange(lev[h], lev[h + 1])
+        ks = ks[par[ks] >= 0]
+        d[ks] = d[par[ks]] + lengths[ks]
+    tips = np.arange(layout.n_int, layout.n_nodes)
+    d[tips] = d[par[tips]] + lengths[tips]
+    for node, v in zip(layout.nodes, d.tolist()):
+        node.dist2root = v
 
 
 _CLADES = operator.attrgetter("clades")
+_END = object()  # closes the list of children, so that a longer or shorter list differs
+
+
+def _children(nodes):
+    """Every child of every node, in order, then _END (C-level iteration): the
+    same objects in the same order mean an unchanged topology below the same
+    root."""
+    return list(itertools.chain(itertools.chain.from_iterable(map(_CLADES, nodes)), (_END,)))
+
+
+def _same_children(nodes, ref):
+    """The nodes' children are the objects of ``ref`` (from _children), in order
+    (compared by identity, without building a list)."""
+    return all(map(operator.is_, itertools.chain(itertools.chain.from_iterable(map(_CLADES, nodes)), (_END,)), ref))
+
+
+def _masks(nodes):
+    return list(map(getattr, nodes, itertools.repeat("mask"), itertools.repeat(None)))
+
+
+def _same_masks(nodes, ref):
+    return all(map(operator.is_, map(getattr, nodes, itertools.repeat("mask"), itertools.repeat(None)), ref))
 
 
 class ResultHolder:
@@ -266,7 +296,7 @@ class GPUAncMixin:
         gtr_key = engine.model_key(self.gtr)
         if s is not None and s["root"] is self.tree.root and s["data"] is self.data and s["gtr_key"] == gtr_key:
             nodes = s["layout"].nodes
-            if _children_ids(nodes) == s["children_ids"] and _mask_ids(nodes) == s["mask_id_list"]:
+            if _same_children(nodes, s["children"]) and _same_masks(nodes, s["masks"]):
                 bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
                 engine.check_exp(self.gtr, bl)
                 s["forest"].set_branch_lengths([bl])
@@ -309,7 +339,7 @@ class GPUAncMixin:
                 foreign.append(n)
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
                  root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes,
-                 children_ids=_children_ids(layout.nodes), mask_id_list=_mask_ids(layout.nodes), holder=holder,
+                 children=_children(layout.nodes), masks=_masks(layout.nodes), holder=holder,
                  foreign=foreign)
         self._session = s
         return s
@@ -559,21 +589,25 @@ class GPUAncMixin:
         t = t.cpu().numpy()
         info = info.cpu().numpy()
         root_k = layout.n_int - 1
-        if any(info[k] == -1 for k in range(layout.n_nodes) if k != root_k):
+        failed = info == -1
+        failed[root_k] = False
+        if failed.any():
             engine.check(engine._lib.TT_ERR_BRACKET, "optimize_branch_lengths_joint")
-        max_bl = 0.0
-        for k, node in enumerate(layout.nodes):
-            if k == root_k:
-                continue
+        lengths = np.maximum(0.0, t)
+        lengths[root_k] = 0.0
+        max_bl = float(lengths.max()) if len(lengths) else 0.0
+        if (lengths > 0.9 * ttconf.MAX_BRANCH_LENGTH).any():
+            self.logger("WARNING: GTR.optimal_t_compressed -- The branch length seems to be very long!", 4, warn=True)
+        for node, new_len in zip(layout.nodes[:root_k], lengths[:root_k].tolist()):
             if store_old:
                 node._old_length = node.branch_length
-            new_len = max(0.0, float(t[k]))
-            if new_len > 0.9 * ttconf.MAX_BRANCH_LENGTH:
-                self.logger("WARNING: GTR.optimal_t_compressed -- The branch length seems to be very long!", 4,
-                            warn=True)
             node.branch_length = new_len
             node.mutation_length = new_len
-            max_bl = max(max_bl, new_len)
+        for node, new_len in zip(layout.nodes[root_k + 1:], lengths[root_k + 1:].tolist()):
+            if store_old:
+                node._old_length = node.branch_length
+            node.branch_length = new_len
+            node.mutation_length = new_len
         bstore = BranchStateStore(layout, counts.cpu().numpy())
         holder = sess.get("holder")
         if holder is not None:
@@ -589,7 +623,13 @@ class GPUAncMixin:
                         " \n\t ****branch_length_mode='input' or 'marginal'", 0, warn=True)
         self.tree.root.up = None
         self.tree.root.dist2root = 0.0
-        self._prepare_nodes()
+        from .treeanc import TreeAnc as _OwnTreeAnc  # (treeanc imports this module)
+        if type(self)._prepare_nodes is _OwnTreeAnc._prepare_nodes:
+            # the topology is the session's (checked when this call began), so of what
+            # _prepare_nodes re-derives only the distances to the root change
+            _set_dist2root(layout, lengths)
+        else:
+            self._prepare_nodes()
         return ttconf.SUCCESS
 
     def optimal_branch_length(self, node):

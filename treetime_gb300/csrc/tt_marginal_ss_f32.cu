@@ -120,6 +120,59 @@ __device__ __forceinline__ void ss_evolve2(const float* mats, int m0, const floa
     }
 }
 
+// One message alone (the narrow levels, where each of a site's two lanes takes one child):
+// msg = x + ((x.V) * (d - 1)).V^-1, two eigen-coordinates per step
+template <int Q, int W, int NT>
+__device__ __forceinline__ void ss_propagate1(const float* mats, int m0, const float* ea, const float (&x)[W],
+                                              float (&m)[W]) {
+    constexpr int KP = (Q + 1) / 2, MS = Q * KP * kSSMaxSites * 2;
+    auto m2 = [&](int off) -> float2 { return *reinterpret_cast<const float2*>(mats + m0 + off); };
+#pragma unroll
+    for (int j = 0; j < W; ++j) m[j] = j < Q ? x[j] : 0.f;
+#pragma unroll 1
+    for (int kk = 0; kk < KP; ++kk) {
+        float y0[2] = {0.f, 0.f}, y1[2] = {0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const float2 v = m2((i * KP + kk) * 2 * kSSMaxSites);
+            y0[i & 1] = fmaf(x[i], v.x, y0[i & 1]);
+            y1[i & 1] = fmaf(x[i], v.y, y1[i & 1]);
+        }
+        const float z0 = (y0[0] + y0[1]) * ea[2 * kk * NT], z1 = (y1[0] + y1[1]) * ea[(2 * kk + 1) * NT];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const float2 u = m2(MS + (j * KP + kk) * 2 * kSSMaxSites);
+            m[j] = fmaf(z1, u.y, fmaf(z0, u.x, m[j]));
+        }
+    }
+}
+
+// ev = o + V.((V^-1.o) * (d - 1)), one vector
+template <int Q, int W, int NT>
+__device__ __forceinline__ void ss_evolve1(const float* mats, int m0, const float* ea, const float (&o)[W],
+                                           float (&v)[W]) {
+    constexpr int KP = (Q + 1) / 2, MS = Q * KP * kSSMaxSites * 2;
+    auto m2 = [&](int off) -> float2 { return *reinterpret_cast<const float2*>(mats + m0 + off); };
+#pragma unroll
+    for (int i = 0; i < W; ++i) v[i] = i < Q ? o[i] : 0.f;
+#pragma unroll 1
+    for (int kk = 0; kk < KP; ++kk) {
+        float y0[2] = {0.f, 0.f}, y1[2] = {0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const float2 u = m2(MS + (j * KP + kk) * 2 * kSSMaxSites);
+            y0[j & 1] = fmaf(u.x, o[j], y0[j & 1]);
+            y1[j & 1] = fmaf(u.y, o[j], y1[j & 1]);
+        }
+        const float z0 = (y0[0] + y0[1]) * ea[2 * kk * NT], z1 = (y1[0] + y1[1]) * ea[(2 * kk + 1) * NT];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const float2 w2 = m2((i * KP + kk) * 2 * kSSMaxSites);
+            v[i] = fmaf(w2.y, z1, fmaf(w2.x, z0, v[i]));
+        }
+    }
+}
+
 template <int W>
 struct SSRowPair {
     float a[W], b[W];
@@ -157,10 +210,10 @@ __device__ __noinline__ int ss_sample(SSRow<W> x, double u) {
 // between the executed instructions costs instruction-cache misses on every level)
 template <int Q, int W, int NT, bool HM>
 __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
-    constexpr int QQ = Q * Q;
     constexpr int KP = (Q + 1) / 2;  // eigen-coordinate pairs (the last one padded for odd q)
     __shared__ __align__(16) float lut_s[256 * W];
     __shared__ int red[NT];
+    __shared__ int esum_site[kSSMaxSites];  // rescale exponents of the narrow levels, per site
     __shared__ float red_corr[NT];
     __shared__ unsigned diff_red[NT / 32];
     // the time grid in FP32 and the reciprocals of its steps (FP64 issues at 1/64 of the FP32 rate
@@ -205,7 +258,8 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             if (tid == 0) set_status(a.status, TT_ERR_INVALID);
             continue;
         }
-        __syncthreads();  // the previous range is done with the shared matrices
+        __syncthreads();  // the previous range is done with the shared matrices and counters
+        for (int i = tid; i < kSSMaxSites; i += NT) esum_site[i] = 0;  // published by the next barrier
         {
             // Bring what the walk reads along its dependent chains into L2 now, all at once: the
             // tree's node records, child pairs and branch lengths, this range's rows of the d - 1
@@ -240,13 +294,28 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
             mats_s[MS + dst] = in ? __ldg(a.m.Vinv + (int64_t)(c * Q + r) * P + wi.y + s) : 0.f;
         }
         __syncthreads();
+        // Two thread layouts.  Wide levels: node groups of np threads, one per site (G groups).
+        // Levels of at most G2 nodes ("narrow"; not with masks): node groups of 2 np threads, two
+        // adjacent lanes per site, each taking one of a node's children.  sl / site / valid / pc
+        // follow the level's layout.
         const int G = NT / np;
         const bool active = tid < G * np;
         const int g = tid / np;
-        const int sl = tid - g * np;  // this thread's site within the range
-        const int site = wi.y + sl;
-        const bool valid = active && site < P;
-        const int pc = site < P ? site : P - 1;
+        const int G2 = NT / (2 * np);
+        const bool active2 = tid < G2 * 2 * np;
+        const int g2 = tid / (2 * np);
+        const int c2 = (tid - g2 * 2 * np) & 1;  // which child in the narrow layout
+        const unsigned pair_mask = 3u << (lane & ~1);
+        int sl = 0, site = 0, pc = 0;
+        bool valid = false, narrow = false;
+        auto set_layout = [&](bool nw) {
+            narrow = nw;
+            sl = nw ? (tid - g2 * 2 * np) >> 1 : tid - g * np;
+            site = wi.y + sl;
+            valid = (nw ? active2 : active) && site < P;
+            pc = site < P ? site : P - 1;
+        };
+        set_layout(false);
         // (V[i][2kk], V[i][2kk+1]) = float2 at mats_s + m0 + (i*KP + kk) * 2 kSSMaxSites, and
         // (V^-1[2kk][j], V^-1[2kk+1][j]) the same at MS + ... (j*KP + kk), with m0 = 2 sl + an
         // opaque zero per node: the matrices do not change inside a level, and without it the
@@ -345,10 +414,13 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
 
         // ------------------------------------------------------------ post-order
         // r *= max(1e-12, msg)^mask for one child, then the power-of-two rescale
-        auto absorb = [&](int c, const float (&x)[W], const float (&msg)[W], float (&r)[W]) {
-            // an internal child's message waits in its posterior row for the pre-order, which
-            // overwrites it with the posterior once it has used it
+        // an internal child's message waits in its posterior row for the pre-order, which
+        // overwrites it with the posterior once it has used it
+        auto keep_msg = [&](int c, const float (&msg)[W]) {
             if (c < n_int && valid) store_row<W>(row(posterior, c), msg);
+        };
+        auto absorb = [&](int c, const float (&x)[W], const float (&msg)[W], float (&r)[W], bool store) {
+            if (store) keep_msg(c, msg);
             const float m = mask_of(nb + c);
             if (m != 1.f && c < n_int) {
                 float xs = 0.f;
@@ -379,11 +451,11 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
 #pragma unroll
                     for (int j = 0; j < W; ++j) r[j] = t.v[j];
                 }
-                esum += e;
+                if (narrow) atomicAdd(&esum_site[sl], e);
+                else esum += e;
             }
         };
-        for (int h = 0; h < tr.n_levels; ++h) {
-            const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
+        auto post_level_wide = [&](int lo, int hi) {
             for (int k = active ? lo + g : hi; k < hi; k += G) {
                 const int64_t gk = nb + k;
                 // the node's record and (two children) its children with their tip rows, one load each
@@ -410,15 +482,60 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
                     }
                     // one copy of the staging code for both branches
 #pragma unroll 1
-                    for (int c2 = 0; c2 < (two ? 2 : 1); ++c2) stage_e(c2 ? e1 : e0, c2 ? bb : ba);
+                    for (int cb2 = 0; cb2 < (two ? 2 : 1); ++cb2) stage_e(cb2 ? e1 : e0, cb2 ? bb : ba);
                     propagate2(mbase(), e0, two ? e1 : e0, xa, xb, ma, mb);
-                    absorb(ca, xa, ma, r);
-                    if (two) absorb(cb, xb, mb, r);
+                    absorb(ca, xa, ma, r, true);
+                    if (two) absorb(cb, xb, mb, r, true);
                 }
                 if (valid) store_row<W>(row(partial, k), r);
             }
+        };
+        // a node of a narrow level: lane c2 transports child c2 (two-child nodes), lane 0 collects;
+        // other nodes: lane 0 takes the children one at a time
+        auto post_node_narrow = [&](int k) {
+            const int64_t gk = nb + k;
+            const int4 rec = __ldg(nrec + gk), cpq = __ldg(cpair + gk);
+            const bool bin = rec.y - rec.x == 2;
+            float r[W];
+#pragma unroll
+            for (int j = 0; j < W; ++j) r[j] = j < Q ? 1.f : 0.f;
+            if (bin) {
+                const int c = c2 ? cpq.z : cpq.x, trow = c2 ? cpq.w : cpq.y;
+                float x[W], m[W], mo[W];
+                node_in_t(c, trow, x);
+                stage_e(e0, __ldg(a.f.bl + nb + c));
+                ss_propagate1<Q, W, NT>(mats_s, mbase(), e0, x, m);
+                keep_msg(c, m);
+#pragma unroll
+                for (int j = 0; j < W; ++j) mo[j] = __shfl_sync(pair_mask, m[j], (lane & ~1) | 1);
+                if (c2 == 0) {
+                    absorb(cpq.x, x, m, r, false);
+                    absorb(cpq.z, x, mo, r, false);
+                }
+            } else if (c2 == 0) {
+                for (int ci = rec.x; ci < rec.y; ++ci) {
+                    const int c = __ldg(a.f.child_idx + ci);
+                    float x[W], m[W];
+                    node_in(c, x);
+                    stage_e(e0, __ldg(a.f.bl + nb + c));
+                    ss_propagate1<Q, W, NT>(mats_s, mbase(), e0, x, m);
+                    absorb(c, x, m, r, true);
+                }
+            }
+            if (c2 == 0 && valid) store_row<W>(row(partial, k), r);
+        };
+        for (int h = 0; h < tr.n_levels; ++h) {
+            const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
+            if (!has_masks && hi - lo <= G2) {
+                set_layout(true);
+                for (int k = active2 ? lo + g2 : hi; k < hi; k += G2) post_node_narrow(k);
+            } else {
+                set_layout(false);
+                post_level_wide(lo, hi);
+            }
             __syncthreads();
         }
+        set_layout(false);
         red[tid] = esum;
         red_corr[tid] = lcorr;
         __syncthreads();
@@ -427,6 +544,7 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         if (tid < np) {
             int tot = 0;
             double corr = 0.0;
+            tot = esum_site[tid];
             for (int gg = 0; gg < G; ++gg) {
                 tot += red[gg * np + tid];
                 // mask corrections exist only with masks (GB300 issues FP64 adds slowly)
@@ -526,8 +644,40 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
         };
         // parent levels from the root's down; height-1 parents have only tips below them
         const int h_end = tips_needed ? 0 : 1;
+        // a parent of a narrow level: lane c2 takes children c2, c2 + 2, ... on its own
+        auto pre_parent_narrow = [&](int p) {
+            const int64_t gp = nb + p;
+            const int4 rec = __ldg(nrec + gp), cpq = __ldg(cpair + gp);
+            const bool bin = rec.y - rec.x == 2;
+            for (int ci = rec.x + c2; ci < rec.y; ci += 2) {
+                const int c = bin ? (c2 ? cpq.z : cpq.x) : __ldg(a.f.child_idx + ci);
+                if (c >= n_int && !tips_needed) continue;
+                float pv[W], o[W];
+                load_row<W>(row(posterior, p), pv);
+                stage_e(e0, __ldg(a.f.bl + nb + c));
+                if (c < n_int) {
+                    load_row<W>(row(posterior, c), o);  // the message the post-order formed
+                } else {
+                    float x[W];
+                    node_in(c, x);
+                    ss_propagate1<Q, W, NT>(mats_s, mbase(), e0, x, o);
+                }
+                outgroup_of(c, pv, o);
+                if (c >= n_int && !a.o.reconstruct_tips) continue;
+                float v[W];
+                ss_evolve1<Q, W, NT>(mats_s, mbase(), e0, o, v);
+                posterior_of(c, v);
+            }
+        };
         for (int h = tr.n_levels - 1; h >= h_end; --h) {
             const int lo = __ldg(lev + h), hi = __ldg(lev + h + 1);
+            if (!has_masks && hi - lo <= G2) {
+                set_layout(true);
+                for (int p = active2 ? lo + g2 : hi; p < hi; p += G2) pre_parent_narrow(p);
+                __syncthreads();
+                continue;
+            }
+            set_layout(false);
             for (int p = active ? lo + g : hi; p < hi; p += G) {
                 const int64_t gp = nb + p;
                 const int4 rec = __ldg(nrec + gp), cpq = __ldg(cpair + gp);
@@ -546,7 +696,7 @@ __global__ void __launch_bounds__(NT, 1) marginal_ss_f32_kernel(SSF32Params a) {
                     float pv[W], oa[W], ob[W];
                     load_row<W>(row(posterior, p), pv);
 #pragma unroll 1
-                    for (int c2 = 0; c2 < (two ? 2 : 1); ++c2) stage_e(c2 ? e1 : e0, __ldg(a.f.bl + nb + (c2 ? cb : ca)));
+                    for (int cb2 = 0; cb2 < (two ? 2 : 1); ++cb2) stage_e(cb2 ? e1 : e0, __ldg(a.f.bl + nb + (cb2 ? cb : ca)));
                     const float* eb = two ? e1 : e0;
                     if (ca < n_int && (!two || cb < n_int)) {
                         // the children's messages as the post-order formed them

@@ -23,31 +23,44 @@ __device__ __forceinline__ int tree_of_node(const tt_tree* trees, int n_trees, i
     return lo;
 }
 
-// One thread per matrix row (node g, child state i): the q factors exp(mu*lambda_k*t) are computed
-// once per row (FP64 exp is slow on this GPU) and the row's w entries summed over k in order.
-__global__ void pmats_kernel(tt_forest f, tt_model m, tt_pmats out, int32_t* status) {
+// One thread per matrix row (node g, child state i), a CTA per slice of kPmatRows consecutive rows.
+// The CTA first forms the q factors exp(mu*lambda_k*t) (and expm1 for D) of every node its rows
+// touch, once per (node, k), in shared memory: FP64 exp issues at 1/64 of the FP32 rate on this
+// GPU, and every row of a node needs the same q factors.  Then each thread sums its row's w entries
+// over k in order.
+constexpr int kPmatRows = 128;
+
+__global__ void __launch_bounds__(kPmatRows) pmats_kernel(tt_forest f, tt_model m, tt_pmats out, int32_t* status) {
     constexpr int kMaxQ = 32;
+    constexpr int kPairs = kPmatRows + 2 * kMaxQ;  // (node, k) pairs a slice can touch
+    __shared__ double sh_ex[kPairs], sh_em1[kPairs];
     const int q = f.n_states, w = f.width;
     const int64_t rows = f.n_nodes * q;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows;
-         idx += (int64_t)gridDim.x * blockDim.x) {
+    const bool need32 = out.p32 != nullptr || out.p32_pair != nullptr;
+    for (int64_t r0 = blockIdx.x * (int64_t)kPmatRows; r0 < rows; r0 += (int64_t)gridDim.x * kPmatRows) {
+        const int64_t g0 = r0 / q;
+        const int64_t r1 = r0 + kPmatRows < rows ? r0 + kPmatRows : rows;
+        const int nn = (int)((r1 - 1) / q - g0 + 1);
+        __syncthreads();  // the previous slice is done with the factors
+        for (int e = threadIdx.x; e < nn * q; e += kPmatRows) {
+            const int64_t g = g0 + e / q;
+            const int k = e % q;
+            const int mi = f.trees[tree_of_node(f.trees, f.n_trees, g)].model;
+            const double lv = m.mu[mi] * f.bl[g] * m.lam[(int64_t)mi * q + k];
+            if (lv > 10.0) set_status(status, TT_ERR_NUMERIC);
+            sh_ex[e] = exp(lv);
+            sh_em1[e] = need32 ? expm1(lv) : 0.0;
+        }
+        __syncthreads();
+        const int64_t idx = r0 + threadIdx.x;
+        if (idx >= r1) continue;
         const int64_t g = idx / q;
         const int i = (int)(idx - g * q);
-        const int t = tree_of_node(f.trees, f.n_trees, g);
-        const int mi = f.trees[t].model;
+        const int mi = f.trees[tree_of_node(f.trees, f.n_trees, g)].model;
         const double* V = m.V + (int64_t)mi * q * q;
         const double* Vi = m.Vinv + (int64_t)mi * q * q;
-        const double* lam = m.lam + (int64_t)mi * q;
-        const double mu = m.mu[mi];
-        const double bl = f.bl[g];
-        double ex[kMaxQ], em1[kMaxQ];
-        const bool need32 = out.p32 != nullptr || out.p32_pair != nullptr;
-        for (int k = 0; k < q; ++k) {
-            const double lv = mu * bl * lam[k];
-            if (lv > 10.0) set_status(status, TT_ERR_NUMERIC);
-            ex[k] = exp(lv);
-            em1[k] = need32 ? expm1(lv) : 0.0;
-        }
+        const double* ex = sh_ex + (g - g0) * q;
+        const double* em1 = sh_em1 + (g - g0) * q;
         const int ps = (out.p32_pair && f.pair_slot) ? f.pair_slot[g] : -1;
         const int lps = (out.logp2 && out.logp2_pair && f.pair_slot) ? f.pair_slot[g] : -1;
         const int64_t o = g * q * w + (int64_t)i * w;
@@ -113,10 +126,9 @@ extern "C" tt_status tt_branch_pmats(const tt_forest* f, const tt_model* m, tt_p
     }
     const int64_t total = f->n_nodes * f->n_states;  // one thread per matrix row
     if (total == 0) return TT_OK;
-    const int threads = 128;
-    int64_t blocks = (total + threads - 1) / threads;
+    int64_t blocks = (total + kPmatRows - 1) / kPmatRows;
     if (blocks > 65535LL * 8) blocks = 65535LL * 8;
-    pmats_kernel<<<(unsigned)blocks, threads, 0, as_stream(stream)>>>(*f, *m, out, status);
+    pmats_kernel<<<(unsigned)blocks, kPmatRows, 0, as_stream(stream)>>>(*f, *m, out, status);
     return check_launch("tt_branch_pmats");
 }
 

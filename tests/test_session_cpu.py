@@ -78,3 +78,31 @@ def test_dist2root_by_levels_equals_the_preorder_sums():
         for ch in c.clades:
             ch.dist2root = c.dist2root + ch.mutation_length
     assert fast == [n.dist2root for n in lay.nodes]
+
+
+def test_change_counter_moves_on_every_change_and_only_then():
+    """The O(1) session check: the counter moves on any mutation of a children
+    list, a new list, a new or deleted mask, and not on reads or on other
+    attributes (branch lengths are refreshed on every call anyway)."""
+    from treetime_gb300.tree import topology_epoch
+    t = parse_newick("((A:0.1,B:0.2)x:0.05,C:0.3)r;")
+    x = next(n for n in t.find_clades() if n.name == "x")
+    e = topology_epoch()
+    _ = [n.clades for n in t.find_clades()], getattr(x, "mask", None)
+    x.branch_length = 0.9
+    x.name = "y"
+    assert topology_epoch() == e
+    for change in (lambda: x.clades.append(Clade(name="D")), lambda: x.clades.pop(),
+                   lambda: x.clades.reverse(), lambda: x.clades.sort(key=lambda c: c.name),
+                   lambda: x.clades.insert(0, Clade(name="E")), lambda: x.clades.remove(x.clades[0]),
+                   lambda: x.clades.__setitem__(0, x.clades[0]), lambda: x.clades.extend([]),
+                   lambda: setattr(x, "clades", list(x.clades)), lambda: setattr(x, "mask", None),
+                   lambda: delattr(x, "mask")):
+        before = topology_epoch()
+        change()
+        assert topology_epoch() > before
+    # a list assigned to a clade is wrapped, so its own later mutations are seen too
+    x.clades = [Clade(name="F")]
+    before = topology_epoch()
+    x.clades += [Clade(name="G")]
+    assert topology_epoch() > before and [c.name for c in x.clades] == ["F", "G"]

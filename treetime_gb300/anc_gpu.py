@@ -31,7 +31,7 @@ from . import config as ttconf
 from . import engine
 from .alphabets import chars_to_codes, profile_lut
 from .errors import MissingDataError
-from .tree import LAZY_ATTRS, Clade
+from .tree import LAZY_ATTRS, Clade, topology_epoch
 
 
 def _set_dist2root(layout, lengths):
@@ -296,7 +296,12 @@ class GPUAncMixin:
         gtr_key = engine.model_key(self.gtr)
         if s is not None and s["root"] is self.tree.root and s["data"] is self.data and s["gtr_key"] == gtr_key:
             nodes = s["layout"].nodes
-            if _same_children(nodes, s["children"]) and _same_masks(nodes, s["masks"]):
+            # a tree of this package's clades that nothing has changed since (tree.topology_epoch)
+            # needs no walk; otherwise every child and mask is compared by identity
+            epoch = topology_epoch()
+            if (s["own"] and epoch == s["epoch"]) or (_same_children(nodes, s["children"]) and
+                                                       _same_masks(nodes, s["masks"])):
+                s["epoch"] = epoch
                 bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
                 engine.check_exp(self.gtr, bl)
                 s["forest"].set_branch_lengths([bl])
@@ -340,7 +345,7 @@ class GPUAncMixin:
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
                  root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes,
                  children=_children(layout.nodes), masks=_masks(layout.nodes), holder=holder,
-                 foreign=foreign)
+                 foreign=foreign, own=not foreign, epoch=topology_epoch())
         self._session = s
         return s
 

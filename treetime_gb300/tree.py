@@ -16,6 +16,7 @@ accepted.
 """
 
 import io
+import operator
 import os
 
 
@@ -149,7 +150,103 @@ class _Result:
         del ov[self.name]
 
 
+# Bumped by every change to a Clade's children or mask: a mutation of a children list, a new list
+# or a new or deleted mask.  A device session built from a tree of these clades stays valid while
+# the epoch has not moved (an O(1) check per call instead of a walk over the tree); any change,
+# to any tree, sends the next call through the full check.
+_EPOCH = [0]
+
+
+def topology_epoch():
+    """The current value of the change counter of Clade children and masks."""
+    return _EPOCH[0]
+
+
+class _Children(list):
+    """A Clade's list of children: every mutation bumps the change counter."""
+
+    __slots__ = ()
+
+    def __setitem__(self, i, v):
+        _EPOCH[0] += 1
+        list.__setitem__(self, i, v)
+
+    def __delitem__(self, i):
+        _EPOCH[0] += 1
+        list.__delitem__(self, i)
+
+    def __iadd__(self, other):
+        _EPOCH[0] += 1
+        list.extend(self, other)
+        return self
+
+    def __imul__(self, n):
+        _EPOCH[0] += 1
+        return list.__imul__(self, n)
+
+    def append(self, v):
+        _EPOCH[0] += 1
+        list.append(self, v)
+
+    def extend(self, it):
+        _EPOCH[0] += 1
+        list.extend(self, it)
+
+    def insert(self, i, v):
+        _EPOCH[0] += 1
+        list.insert(self, i, v)
+
+    def remove(self, v):
+        _EPOCH[0] += 1
+        list.remove(self, v)
+
+    def pop(self, *i):
+        _EPOCH[0] += 1
+        return list.pop(self, *i)
+
+    def clear(self):
+        _EPOCH[0] += 1
+        list.clear(self)
+
+    def sort(self, *args, **kwargs):
+        _EPOCH[0] += 1
+        list.sort(self, *args, **kwargs)
+
+    def reverse(self):
+        _EPOCH[0] += 1
+        list.reverse(self)
+
+
+def _set_clades(node, value):
+    _EPOCH[0] += 1
+    node.__dict__["_clades"] = value if type(value) is _Children else _Children(value)
+
+
+def _get_mask(node):
+    try:
+        return node.__dict__["mask"]
+    except KeyError:
+        raise AttributeError("mask") from None
+
+
+def _set_mask(node, value):
+    _EPOCH[0] += 1
+    node.__dict__["mask"] = value
+
+
+def _del_mask(node):
+    _EPOCH[0] += 1
+    try:
+        del node.__dict__["mask"]
+    except KeyError:
+        raise AttributeError("mask") from None
+
+
 class Clade(_Traversal):
+    # children and mask go through the change counter; the read of `clades` is a C-level getter
+    clades = property(operator.attrgetter("_clades"), _set_clades)
+    mask = property(_get_mask, _set_mask, _del_mask)
+
     def __init__(self, branch_length=None, name=None, clades=None, confidence=None):
         self.branch_length = branch_length
         self.name = name

@@ -3,14 +3,16 @@
 // Max-product pruning in the log domain: for a non-root node c, joint_Lx_c[j] = max_i(log P_c[i][j]
 // + in_c[i]) with its first-index argmax joint_Cx_c[j], where in_c is the sum of c's children's
 // joint_Lx (internal c) or log(max(profile, 1e-12)) of its character (tip c); the root adds
-// log(pi), takes the first argmax of the normalised exp profile (or an inverse-CDF draw) and the
-// pre-order backtrack sets state_c = joint_Cx_c[state_parent].
+// log(pi) and takes the first argmax of the normalised exp profile, which is the first argmax of
+// the sums themselves (or an inverse-CDF draw from the profile), and the pre-order backtrack sets
+// state_c = joint_Cx_c[state_parent].
 //
 // Arithmetic: double-float (an FP32 pair hi + lo holding about 48 significant bits) on the FP32
 // pipe; GB300's FP64 pipe issues at 1/64 of the FP32 rate and q^2 additions and comparisons per
 // node and pattern made the FP64 version bound by it.  The branch matrices' logs are formed in
-// FP64 by tt_branch_pmats and split into pairs, the tips' log profiles come from a 256-character
-// table of pairs (tt_model.lut_log2), so nothing is rounded below FP64 before the max-plus sums.
+// FP64 by tt_branch_pmats and split into pairs, the tips' log profiles and log(pi) come from
+// tables of pairs (tt_model.lut_log2, logpi2), so nothing is rounded below FP64 before the
+// max-plus sums.
 // Values differ from FP64 sums by ~1e-14 relative; a state can differ only where two candidates
 // are that close (the reference's own top-two margin far below 1e-9).
 //

@@ -5,16 +5,22 @@
 // eigenbasis in the form  x.P = x + ((x.V) * (d - 1)).V^-1  (P_a(t) = V_a diag(d) V_a^-1 is never
 // formed), with the arithmetic and layouts chosen for FP32 throughput:
 //   - one CTA per range of at most 32 sites; the range's V and V^-1 (FP32) sit in shared memory
-//     for the whole pass, stored site-interleaved so that the lanes of a warp (consecutive sites)
-//     read consecutive words;
-//   - the CTA's threads form node groups of `range width` threads (one thread per site) that
-//     share the nodes of a height level, one CTA barrier per level;
+//     for the whole pass, site-interleaved with two eigen-coordinates of a site side by side, so
+//     that one 8-byte load gives a thread two of its own site's entries and the lanes of a warp
+//     (consecutive sites) read consecutive words;
+//   - wide levels: node groups of `range width` threads (one thread per site) share the nodes
+//     of a height level, and a thread transports a node's two children together (every matrix
+//     element loaded once for both); narrow levels (at most NT / (2 range width) nodes): two
+//     lanes per site, one child each; one CTA barrier per level;
+//   - the post-order leaves each internal child's message in its posterior row; the pre-order
+//     (by parent, top down) reuses it instead of transporting the child's partial again;
 //   - d - 1 for TreeTime's interpolated P(t) (approximate=True, t * rate_scale < 10) comes from
 //     a table of expm1(t_g * mu_a * lambda_a,k) on the model's time grid, computed in FP64 on the
 //     host and interpolated linearly like scipy's interp1d (the interpolated matrices share V, so
-//     interpolating d - 1 is interpolating P); other branches use expm1f directly;
+//     interpolating d - 1 is interpolating P); other branches use expm1f directly; staged per
+//     branch in shared memory, with the bracket and weight in FP32;
 //   - partials are rescaled by exact powers of two only when their largest entry falls below
-//     2^-16, the exponents summed per site in registers; FP64 only for the root's log.
+//     2^-16, the exponents summed per site; FP64 only for the root's log.
 // As in TreeTime, child messages are floored at 1e-12 and parent messages are not clamped.
 #include "tt_marginal_kernels.cuh"
 

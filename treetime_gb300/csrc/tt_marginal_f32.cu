@@ -248,6 +248,13 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                             float d0[S], d1[S];
                             child_xd(ca[d], xa[d], &st.mat[i][0], d0);
                             child_xd(cb[d], xb[d], &st.mat[i][QW], d1);
+                            if constexpr (!has_masks && LPP == 1) {
+                                float r[S];
+                                if (ref_pair<Q, W>(xa[d], d0, xb[d], d1, r, prh, prl, esum)) {
+                                    if (valid) st_part<S>(part0 + (int64_t)k * PW, r);
+                                    continue;
+                                }
+                            }
                             float m0 = 1.f, m1 = 1.f;
                             if constexpr (has_masks) {
                                 const int4 cp = st.pair[i];

@@ -278,6 +278,40 @@ __device__ __forceinline__ void df_renorm(float& h, float& l, int& esum) {
     }
 }
 
+// Two children, no masks, one lane per pattern, when the first child has a reference state a
+// (its first entry equal to 1) and the second child is 1 at a too: the reference form of
+// ref_add(first), ref_add(second), ref_finish with the same operations in the same order, without
+// the general form's bookkeeping (bit-identical results).  Returns false (nothing changed) when
+// the node needs the general path: no shared reference state, a factor too small, or an entry
+// outgrowing the reference.
+template <int Q, int W>
+__device__ __forceinline__ bool ref_pair(const float (&xa)[W], const float (&da)[W], const float (&xb)[W],
+                                         const float (&db)[W], float (&r)[W], float& ph, float& pl, int& esum) {
+    int a = Q;
+#pragma unroll
+    for (int s = Q - 1; s >= 0; --s)
+        if (xa[s] == 1.f) a = s;
+    float xb_a = 0.f, da_a = 0.f, db_a = 0.f;
+#pragma unroll
+    for (int s = 0; s < Q; ++s)
+        if (s == a) { xb_a = xb[s]; da_a = da[s]; db_a = db[s]; }
+    if (a >= Q || xb_a != 1.f) return false;
+    const float dl = fmaf(da_a, db_a, da_a + db_a);
+    const float f1 = 1.f + dl;
+    if (!(f1 > 0x1p-64f)) return false;
+    const float inv = __fdividef(1.f, f1);
+    float mo = 0.f;
+#pragma unroll
+    for (int s = 0; s < W; ++s) {
+        r[s] = s < Q ? (s == a ? 1.f : ((xa[s] + da[s]) * (xb[s] + db[s])) * inv) : 0.f;
+        mo = fmaxf(mo, r[s]);
+    }
+    if (!(mo <= 1.f)) return false;
+    df_mul_1p(ph, pl, dl);
+    df_renorm(ph, pl, esum);
+    return true;
+}
+
 // The node's stored row r (largest entry exactly 1); the factor it drops multiplies the running
 // product (ph, pl) and its power-of-two exponent goes to esum.  Returns false when the product is
 // zero at every state (r is then all zero and the pattern's likelihood is 0).  Every lane of the

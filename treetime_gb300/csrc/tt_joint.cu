@@ -217,7 +217,8 @@ __device__ __forceinline__ void st_cx(uint8_t* p, const int (&c)[S]) {
     }
 }
 
-template <int Q, int W, int LPP, int NT>
+// HM: the forest has per-branch masks (a second instance without any mask code serves the rest)
+template <int Q, int W, int LPP, int NT, bool HM>
 __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
     constexpr int S = W / LPP;
     constexpr int CH = JStageCfg<Q, W>::kChunk;
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
         }
         onehot_s[c] = (signed char)(ok && zeros == 1 ? st1 : -1);
     }
-    const bool has_masks = a.f.mask_off != nullptr;
+    constexpr bool has_masks = HM;
     float* const msg_buf = a.o.msg;
     const bool count_diff = a.o.count_diff != 0;
 
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
             }
         };
         auto mask_of = [&](int c) -> float {
-            if (!has_masks) return 1.f;
+            if constexpr (!has_masks) return 1.f;
             const int64_t mo = __ldg(a.f.mask_off + nb + c);
             return mo < 0 ? 1.f : (float)__ldg(a.f.masks + mo + pc);
         };
@@ -560,15 +561,15 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
     }
 }
 
-template <int Q, int LPP, int NT>
-static tt_status launch_joint(const JointParams& prm, int blocks, cudaStream_t s) {
+template <int Q, int LPP, int NT, bool HM>
+static tt_status launch_joint_hm(const JointParams& prm, int blocks, cudaStream_t s) {
     constexpr int W = round4(Q);
     const size_t dyn = 2 * sizeof(JStage<Q, W>);
-    static size_t configured[64] = {};
+    static size_t configured[64] = {};  // per instance and device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || dyn > configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(joint_kernel<Q, W, LPP, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(joint_kernel<Q, W, LPP, NT, HM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)dyn);
         if (e != cudaSuccess) {
             set_error("tt_joint: %zu bytes of shared memory: %s", dyn, cudaGetErrorString(e));
@@ -576,8 +577,14 @@ static tt_status launch_joint(const JointParams& prm, int blocks, cudaStream_t s
         }
         if (dev >= 0 && dev < 64) configured[dev] = dyn;
     }
-    joint_kernel<Q, W, LPP, NT><<<blocks, NT, dyn, s>>>(prm);
+    joint_kernel<Q, W, LPP, NT, HM><<<blocks, NT, dyn, s>>>(prm);
     return check_launch("tt_joint");
+}
+
+template <int Q, int LPP, int NT>
+static tt_status launch_joint(const JointParams& prm, int blocks, cudaStream_t s) {
+    return prm.f.mask_off ? launch_joint_hm<Q, LPP, NT, true>(prm, blocks, s)
+                          : launch_joint_hm<Q, LPP, NT, false>(prm, blocks, s);
 }
 
 tt_status tree_sums(const tt_forest* f, const double* site_lh, double* tree_lh, cudaStream_t s);

@@ -340,7 +340,7 @@ def run_gpu(args):
         "rel_logLH_err_vs_fp64": rel_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d>" % (forest.threads, forest.ctas_per_sm),
+                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d,HM=0>" % (forest.threads, forest.ctas_per_sm),
                      "ranges": int(len(forest.work_f32_host)),
                      "range_patterns": int(forest.work_f32_host[:, 2].max()),
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms},
@@ -1179,7 +1179,7 @@ def run_c3(args):
         "roofline": {"bound": "hbm", "achieved": ab / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": ab / (k_ms * 1e-3) / 1e9 / peak, "traffic": _traffic("marginal_f32_q4/c3"),
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": ab, "kernel_ms": k_ms,
-                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d>" % (forest.threads, forest.ctas_per_sm)},
+                     "kernel": "marginal_f32_kernel<Q=4,W=4,LPP=1,NT=%d,MINB=%d,HM=0>" % (forest.threads, forest.ctas_per_sm)},
         "e2e": {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
         "gpu_launches": 3 * args.steps,
@@ -1470,7 +1470,7 @@ def _joint_block(engine, t, forest, model, bufs, layout, P, args, flush):
             "public_call_ms": statistics.median(pub[1:]),
             "roofline": {"bound": "hbm", "achieved": ab / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": ab / (kms * 1e-3) / 1e9 / peak, "peak_source": kind,
-                         "kernel": "joint_kernel<Q=4,W=4,LPP=1,NT=%d>" % forest.threads, "kernel_ms": kms,
+                         "kernel": "joint_kernel<Q=4,W=4,LPP=1,NT=%d,HM=0>" % forest.threads, "kernel_ms": kms,
                          "algorithmic_bytes_per_launch": ab, "traffic": _traffic("joint_q4/c1")},
             "arithmetic": "double-float (FP32 pairs) max-plus; states checked against the oracle in tests"}
 

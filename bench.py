@@ -77,43 +77,62 @@ def _traffic(kernel_key):
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region; the raw
     samples go to ``clocks_<gpu>.csv`` in $TT_BENCH_OUT (default: the system's
-    temporary directory)."""
+    temporary directory).  Entering waits (at most 5 s) for the first sample, so
+    that sampling covers the region and not only nvidia-smi's start-up."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.lines = []
         out = os.environ.get("TT_BENCH_OUT") or tempfile.gettempdir()
         self.path = os.path.join(out, "clocks_%d.csv" % index)
 
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line)
+            self.first.set()
+        self.first.set()
+
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        import threading
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
+        self.first = threading.Event()
         try:
-            self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
                                           "--format=csv,noheader,nounits", "-lms", "20"],
-                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+            return self
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
+        self.first.wait(5.0)
         return self
 
     def __exit__(self, *exc):
-        if self.proc is not None:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except Exception:
-                self.proc.kill()
-            self.fh.close()
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.reader.join(timeout=5)
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            with open(self.path, "w") as fh:
+                fh.writelines(self.lines)
+        except OSError:
+            pass
 
     def summary(self):
-        if self.proc is None or not os.path.exists(self.path):
+        if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, mx, util, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in list(self.lines):
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -301,7 +320,8 @@ def run_gpu(args):
                    "node_patterns_per_step": bunits,
                    "roofline": {"achieved": bab / (bkm * 1e-3) / 1e9, "frac": bab / (bkm * 1e-3) / 1e9 / _peaks()[0],
                                 "kernel_ms": bkm, "ranges": int(len(bforest.work_f32_host)),
-                                "algorithmic_bytes_per_launch": bab},
+                                "algorithmic_bytes_per_launch": bab,
+                                "traffic": _traffic("marginal_f32_q4/c1x%d" % k)},
                    "note": "%d independent instances of the configuration (seeds 1..%d: own coalescent tree, "
                            "alignment and GTR each), one forest, one captured launch sequence per step; L2 "
                            "flushed before every step" % (k, k)}

@@ -390,8 +390,9 @@ def _config_pipeline(t, repeats=3):
     """The configuration's whole step through the public TreeAnc calls:
     marginal reconstruction (FP32-scaled), joint reconstruction (FP64) and
     optimal_t_compressed on every branch (optimize_branch_lengths_joint), host
-    clock, median of `repeats`; the tree's branch lengths are restored
-    afterwards."""
+    clock, median of `repeats`.  The steps follow one another as in TreeTime's
+    optimisation loop (each reconstruction sees the lengths of the step
+    before); the tree's branch lengths are restored afterwards."""
     import torch
     nodes = list(t.tree.find_clades())
     saved = [(n.branch_length, getattr(n, "mutation_length", n.branch_length)) for n in nodes]
@@ -406,11 +407,11 @@ def _config_pipeline(t, repeats=3):
         t.optimize_branch_lengths_joint()
         torch.cuda.synchronize()
         t3 = time.perf_counter()
-        for n, (bl, ml) in zip(nodes, saved):
-            n.branch_length, n.mutation_length = bl, ml
         parts["marginal"].append(t1 - t0)
         parts["joint"].append(t2 - t1)
         parts["branch_lengths"].append(t3 - t2)
+    for n, (bl, ml) in zip(nodes, saved):
+        n.branch_length, n.mutation_length = bl, ml
     out = {k: statistics.median(v[1:]) * 1e3 for k, v in parts.items()}
     out["total_ms"] = sum(out.values())
     out["note"] = ("one TreeTime step of this configuration through TreeAnc: infer_ancestral_sequences(marginal=True), "

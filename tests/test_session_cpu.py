@@ -83,7 +83,7 @@ def test_dist2root_by_levels_equals_the_preorder_sums():
 def test_change_counter_moves_on_every_change_and_only_then():
     """The O(1) session check: the counter moves on any mutation of a children
     list, a new list, a new or deleted mask, and not on reads or on other
-    attributes (branch lengths are refreshed on every call anyway)."""
+    attributes (branch lengths have their own counter)."""
     from treetime_gb300.tree import topology_epoch
     t = parse_newick("((A:0.1,B:0.2)x:0.05,C:0.3)r;")
     x = next(n for n in t.find_clades() if n.name == "x")
@@ -106,3 +106,33 @@ def test_change_counter_moves_on_every_change_and_only_then():
     before = topology_epoch()
     x.clades += [Clade(name="G")]
     assert topology_epoch() > before and [c.name for c in x.clades] == ["F", "G"]
+
+
+def test_length_counter_moves_on_every_assignment_and_only_then():
+    """Branch lengths reach the device again only when the length counter moved
+    since the session's copy: every assignment of a Clade's branch_length moves
+    it (to the same value too), reads and other attributes do not, and the bulk
+    assignment of new lengths moves it once."""
+    import copy
+    from treetime_gb300.tree import assign_lengths, length_epoch, topology_epoch
+    t = parse_newick("((A:0.1,B:0.2)x:0.05,C:0.3)r;")
+    nodes = _nodes(t)
+    e, te = length_epoch(), topology_epoch()
+    _ = [n.branch_length for n in nodes]
+    nodes[1].mutation_length = 0.4
+    nodes[1].name = "z"
+    assert length_epoch() == e
+    nodes[1].branch_length = nodes[1].branch_length
+    assert length_epoch() == e + 1 and topology_epoch() == te
+    assign_lengths([n.__dict__ for n in nodes[1:]], [0.5, 0.6, 0.7, 0.8])
+    assert length_epoch() == e + 2
+    assert [n.branch_length for n in nodes[1:]] == [0.5, 0.6, 0.7, 0.8]
+    assert [n.mutation_length for n in nodes[1:]] == [0.5, 0.6, 0.7, 0.8]
+    assign_lengths([n.__dict__ for n in nodes[1:3]], [0.1, 0.2], dist2root=[1.0, 2.0])
+    assert length_epoch() == e + 3
+    assert [(n.branch_length, n.mutation_length, n.dist2root) for n in nodes[1:3]] == [(0.1, 0.1, 1.0),
+                                                                                      (0.2, 0.2, 2.0)]
+    # a clade without a length reads None; copies keep the lengths
+    assert Clade(name="N").branch_length is None
+    c = copy.deepcopy(t)
+    assert [n.branch_length for n in c.find_clades()] == [n.branch_length for n in nodes]

@@ -31,10 +31,10 @@ from . import config as ttconf
 from . import engine
 from .alphabets import chars_to_codes, profile_lut
 from .errors import MissingDataError
-from .tree import LAZY_ATTRS, Clade, topology_epoch
+from .tree import LAZY_ATTRS, Clade, assign_lengths, length_epoch, topology_epoch
 
 
-def _set_dist2root(layout, lengths):
+def _dist2root(layout, lengths):
     """dist2root of every node from the root's 0 and each node's length, parents
     before children (internal nodes by decreasing height, then the tips): the
     additions of TreeTime's _calc_dist2root (treetime/treeanc.py:499-510), in
@@ -48,7 +48,12 @@ def _set_dist2root(layout, lengths):
         d[ks] = d[par[ks]] + lengths[ks]
     tips = np.arange(layout.n_int, layout.n_nodes)
     d[tips] = d[par[tips]] + lengths[tips]
-    for node, v in zip(layout.nodes, d.tolist()):
+    return d
+
+
+def _set_dist2root(layout, lengths):
+    """_dist2root stored on the nodes."""
+    for node, v in zip(layout.nodes, _dist2root(layout, lengths).tolist()):
         node.dist2root = v
 
 
@@ -134,29 +139,56 @@ def _pinned_copy(t):
     return view.numpy().copy()
 
 
+def _pinned_pair(sess, a, b):
+    """Host copies of two small device tensors through page-locked buffers of
+    the session: two asynchronous copies, one wait."""
+    torch = engine.torch()
+    if not a.is_cuda:  # host tensors (stand-ins of the device pieces in host-logic tests)
+        return a.numpy().copy(), b.numpy().copy()
+    bufs = sess.setdefault("pinned_small", {})
+    outs = []
+    for key, x in (("a", a), ("b", b)):
+        buf = bufs.get((key, x.dtype))
+        if buf is None or buf.numel() < x.numel():
+            buf = torch.empty(max(x.numel(), 1), dtype=x.dtype, pin_memory=True)
+            bufs[(key, x.dtype)] = buf
+        view = buf[:x.numel()]
+        view.copy_(x.reshape(-1), non_blocking=True)
+        outs.append(view)
+    torch.cuda.current_stream(a.device).synchronize()
+    return tuple(v.numpy().copy().reshape(x.shape) for v, x in zip(outs, (a, b)))
+
+
 def _host_results(sess, out, rows, P, site_key="site_lh", tree_key="tree_lh", n_diff=True):
     """The results every reconstruction hands to the host -- the states of the
     reconstructed rows, the site and tree log-likelihoods and the changed-site
     count -- through page-locked buffers of the session, as asynchronous copies
-    on the current stream followed by one wait.  The states array returned is
-    a view of the session's buffer: valid until the session's next
-    reconstruction (the results installed on the nodes read it only until
-    then)."""
+    on the current stream followed by one wait; the kernels' status word comes
+    with them (the passes are launched without a wait of their own) and is
+    checked before anything is returned.  The states array returned is a view
+    of the session's buffer: valid until the session's next reconstruction (the
+    results installed on the nodes read it only until then)."""
     torch = engine.torch()
     nb = rows * P
     pb = sess.get("pinned")
     if pb is None or pb[0].numel() < nb or pb[1].numel() < P + 1:
         pb = (torch.empty(max(nb, 1), dtype=torch.uint8, pin_memory=True),
               torch.empty(P + 1, dtype=torch.float64, pin_memory=True),
-              torch.empty(1, dtype=torch.int64, pin_memory=True))
+              torch.empty(1, dtype=torch.int64, pin_memory=True),
+              torch.empty(1, dtype=torch.int32, pin_memory=True))
         sess["pinned"] = pb
-    st, sc, nd = pb
+    st, sc, nd, stat = pb
+    status = sess["bufs"].get("status", (1,), torch.int32)
+    stat.copy_(status, non_blocking=True)
     st[:nb].copy_(out["states"].view(-1)[:nb], non_blocking=True)
     sc[:P].copy_(out[site_key][:P], non_blocking=True)
     sc[P:P + 1].copy_(out[tree_key][:1], non_blocking=True)
     if n_diff:
         nd.copy_(out["n_diff"][:1], non_blocking=True)
     torch.cuda.current_stream(out["states"].device).synchronize()
+    s = int(stat.numpy()[0])
+    if s:
+        engine.check(s, "kernel status")
     scn = sc.numpy()
     return (st.numpy()[:nb].reshape(rows, P), scn[:P].copy(), float(scn[P]),
             int(nd.numpy()[0]) if n_diff else 0)
@@ -237,11 +269,21 @@ class ResultStore:
 
 
 class BranchStateStore:
-    """``branch_state`` dictionaries from the device pair histograms."""
+    """``branch_state`` dictionaries from the pair histograms (a device tensor
+    of this store's own, copied to the host on the first read, or a host
+    array)."""
 
     def __init__(self, layout, hist):
         self.layout = layout
-        self.hist = hist
+        self._hist = hist
+        self._host = None
+
+    @property
+    def hist(self):
+        if self._host is None:
+            h = self._hist
+            self._host = h.cpu().numpy() if hasattr(h, "cpu") else np.asarray(h)
+        return self._host
 
     def fetch(self, name, node):
         if name != "branch_state":
@@ -302,9 +344,7 @@ class GPUAncMixin:
             if (s["own"] and epoch == s["epoch"]) or (_same_children(nodes, s["children"]) and
                                                        _same_masks(nodes, s["masks"])):
                 s["epoch"] = epoch
-                bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
-                engine.check_exp(self.gtr, bl)
-                s["forest"].set_branch_lengths([bl])
+                self._refresh_lengths(s)
                 return s
         engine.check_alphabet(self.gtr.n_states, self.gtr.is_site_specific)
         device = getattr(self, "device", None)
@@ -321,6 +361,7 @@ class GPUAncMixin:
             if m is not None:
                 masks[k] = np.asarray(m, dtype=np.float64)
                 mask_ids[k] = id(m)
+        bl_key = self._lengths_key()
         bl = engine.branch_lengths(layout, self.data.full_length, self.use_mutation_length)
         engine.check_exp(self.gtr, bl)
         ti = engine.TreeInput(layout, codes, tip_row, self.data.multiplicity(), bl, masks=masks)
@@ -345,9 +386,26 @@ class GPUAncMixin:
         s = dict(layout=layout, forest=forest, model=model, bufs=engine.Buffers(forest), mask_ids=mask_ids,
                  root=self.tree.root, data=self.data, gtr_key=gtr_key, n_nodes=layout.n_nodes,
                  children=_children(layout.nodes), masks=_masks(layout.nodes), holder=holder,
-                 foreign=foreign, own=not foreign, epoch=topology_epoch())
+                 foreign=foreign, own=not foreign, epoch=topology_epoch(), bl_key=bl_key,
+                 dicts=None if foreign else [n.__dict__ for n in layout.nodes])
         self._session = s
         return s
+
+    def _lengths_key(self):
+        return (length_epoch(), self.data.full_length, bool(self.use_mutation_length))
+
+    def _refresh_lengths(self, s):
+        """Branch lengths to the device, unless the session's copy is current: a
+        tree of this package's clades none of whose branch lengths was assigned
+        since the copy (tree.length_epoch), for the same alignment length (the
+        floor 1e-3 / L) and length attribute.  Otherwise every node is read."""
+        key = self._lengths_key()
+        if s["own"] and not key[2] and s["bl_key"] == key:
+            return
+        bl = engine.branch_lengths(s["layout"], self.data.full_length, self.use_mutation_length)
+        engine.check_exp(self.gtr, bl)
+        s["forest"].set_branch_lengths([bl])
+        s["bl_key"] = key
 
     def _tip_profile(self, node):
         name_to_row, codes = self._aln_index()
@@ -400,6 +458,21 @@ class GPUAncMixin:
                 if v is not None:
                     setattr(n, a, v)
 
+    def _pass(self, sess, fn, key, *args, **kw):
+        """One pass of the session launched without a wait: the first call with a set of options
+        runs it directly, the second captures it as a CUDA graph (engine.CapturedCall), later
+        ones replay the graph -- the same kernels on the same buffers with one host call instead
+        of a dozen launches.  The graphs live with the session (a new topology, alignment or
+        model starts without them); branch lengths and tip codes are read at replay."""
+        graphs = sess.setdefault("graphs", {})
+        g = graphs.get(key)
+        if g is None:
+            graphs[key] = 1
+            return fn(*args, sync=False, **kw)
+        if g == 1:
+            g = graphs[key] = engine.CapturedCall(fn, *args, **kw)
+        return g.replay()
+
     def _root_draws(self, sample_from_profile):
         """The root's uniform draws (sample_from_profile 'root' or True), one
         rng.random(L) as TreeTime's prof2seq (treetime/seq_utils.py:265-269)."""
@@ -437,9 +510,12 @@ class GPUAncMixin:
         kw = dict(precision=prec, reconstruct_tips=reconstruct_tip_states, keep_outgroup=keep_outgroup,
                   tip_outgroup=keep_outgroup, count_diff=count_diff, root_uniform=draws, node_uniform=node_draws)
         if self.gtr.is_site_specific:
-            out = engine.marginal_site_specific(sess["forest"], self.gtr, sess["bufs"], **kw)
+            out = engine.marginal_site_specific(sess["forest"], self.gtr, sess["bufs"], sync=False, **kw)
+        elif draws is None and node_draws is None:
+            out = self._pass(sess, engine.marginal, ("marginal",) + tuple(sorted(kw.items())),
+                             sess["forest"], sess["model"], sess["bufs"], **kw)
         else:
-            out = engine.marginal(sess["forest"], sess["model"], sess["bufs"], **kw)
+            out = engine.marginal(sess["forest"], sess["model"], sess["bufs"], sync=False, **kw)
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
@@ -468,10 +544,14 @@ class GPUAncMixin:
         if self.gtr.is_site_specific:
             out = engine.joint_site_specific(sess["forest"], self.gtr, sess["bufs"],
                                              reconstruct_tips=reconstruct_tip_states, count_diff=count_diff,
-                                             root_uniform=draws)
+                                             root_uniform=draws, sync=False)
+        elif draws is None:
+            out = self._pass(sess, engine.joint, ("joint", reconstruct_tip_states, count_diff), sess["forest"],
+                             sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
+                             count_diff=count_diff)
         else:
             out = engine.joint(sess["forest"], sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
-                               count_diff=count_diff, root_uniform=draws)
+                               count_diff=count_diff, root_uniform=draws, sync=False)
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
@@ -564,17 +644,25 @@ class GPUAncMixin:
         setting)."""
         sess = self._get_session()
         layout = sess["layout"]
-        name_to_row, _ = self._aln_index()
         if not self.reconstructed_tip_sequences:
-            for n in layout.nodes[layout.n_int:]:
-                if n.name not in name_to_row:
-                    raise MissingDataError(
-                        "TreeAnc.optimal_branch_length: terminal node alignments required; sequence is missing for "
-                        "leaf: '%s'. Missing terminal sequences can be inferred from sister nodes by rerunning with "
-                        "`reconstruct_tip_states=True` or `--reconstruct-tip-states`" % n.name)
+            # the session's tips and their alignment rows are fixed when it is built: a tip
+            # without a row is looked for once per session
+            missing = sess.get("tip_missing")
+            if missing is None:
+                name_to_row, _ = self._aln_index()
+                missing = sess["tip_missing"] = next(
+                    (n.name for n in layout.nodes[layout.n_int:] if n.name not in name_to_row), False)
+            if missing is not False:
+                raise MissingDataError(
+                    "TreeAnc.optimal_branch_length: terminal node alignments required; sequence is missing for "
+                    "leaf: '%s'. Missing terminal sequences can be inferred from sister nodes by rerunning with "
+                    "`reconstruct_tip_states=True` or `--reconstruct-tip-states`" % missing)
         ig = self.ignore_gaps if ignore_gaps is None else ignore_gaps
-        hist, _ = engine.state_pairs(sess["forest"], sess["bufs"], engine.char_state_table(self.gtr),
-                                     self.gtr.gap_index, ig, self.reconstructed_tip_sequences)
+        cs = sess.get("char_state")  # the alphabet's byte -> state table (the model is the session's)
+        if cs is None:
+            cs = sess["char_state"] = engine._to_dev(engine.char_state_table(self.gtr), sess["forest"].device)
+        hist, _ = engine.state_pairs(sess["forest"], sess["bufs"], cs, self.gtr.gap_index, ig,
+                                     self.reconstructed_tip_sequences)
         return sess, hist
 
     def optimize_branch_lengths_joint(self, **kwargs):
@@ -591,8 +679,7 @@ class GPUAncMixin:
         layout = sess["layout"]
         counts = engine.torch().trunc(hist)  # TreeTime casts pair counts to int
         t, info = engine.optimal_t_pairs(self.gtr.n_states, counts, sess["model"], tol=1e-10)
-        t = t.cpu().numpy()
-        info = info.cpu().numpy()
+        t, info = _pinned_pair(sess, t, info)
         root_k = layout.n_int - 1
         failed = info == -1
         failed[root_k] = False
@@ -603,17 +690,42 @@ class GPUAncMixin:
         max_bl = float(lengths.max()) if len(lengths) else 0.0
         if (lengths > 0.9 * ttconf.MAX_BRANCH_LENGTH).any():
             self.logger("WARNING: GTR.optimal_t_compressed -- The branch length seems to be very long!", 4, warn=True)
-        for node, new_len in zip(layout.nodes[:root_k], lengths[:root_k].tolist()):
-            if store_old:
+        rest = layout.nodes[:root_k] + layout.nodes[root_k + 1:]  # every node but the root
+        vals = lengths[:root_k].tolist() + lengths[root_k + 1:].tolist()
+        if store_old:
+            for node in rest:
                 node._old_length = node.branch_length
-            node.branch_length = new_len
-            node.mutation_length = new_len
-        for node, new_len in zip(layout.nodes[root_k + 1:], lengths[root_k + 1:].tolist()):
-            if store_old:
-                node._old_length = node.branch_length
-            node.branch_length = new_len
-            node.mutation_length = new_len
-        bstore = BranchStateStore(layout, counts.cpu().numpy())
+        from .treeanc import TreeAnc as _OwnTreeAnc  # (treeanc imports this module)
+        # with TreeAnc's own _prepare_nodes, of what it re-derives only the distances to the root
+        # change (the topology is the session's, checked when this call began)
+        own_prepare = type(self)._prepare_nodes is _OwnTreeAnc._prepare_nodes
+        dicts = sess.get("dicts") if sess.get("own") else None
+        d2r = None
+        if dicts is not None and not self.use_mutation_length:
+            # the session's clades take the lengths (and distances to the root) in one loop with
+            # one bump of the change counter, and the device copy is made here from the same
+            # numbers (the root keeps its length)
+            if own_prepare:
+                d2r = _dist2root(layout, lengths).tolist()
+                dicts[root_k]["dist2root"] = 0.0
+            assign_lengths(dicts[:root_k] + dicts[root_k + 1:], vals,
+                           None if d2r is None else d2r[:root_k] + d2r[root_k + 1:])
+            bl = lengths.astype(np.float64)
+            r = layout.nodes[root_k].branch_length
+            bl[root_k] = np.nan if r is None else r
+            bl = engine.length_floor(bl, self.data.full_length)
+            try:
+                engine.check_exp(self.gtr, bl)
+            except ValueError:
+                sess["bl_key"] = None  # the next call reads the lengths again and raises there
+            else:
+                sess["forest"].set_branch_lengths([bl])
+                sess["bl_key"] = self._lengths_key()
+        else:
+            for node, new_len in zip(rest, vals):
+                node.branch_length = new_len
+                node.mutation_length = new_len
+        bstore = BranchStateStore(layout, counts)
         holder = sess.get("holder")
         if holder is not None:
             holder.install(_ChainedSource(holder.src, bstore) if holder.src is not None else bstore)
@@ -628,13 +740,10 @@ class GPUAncMixin:
                         " \n\t ****branch_length_mode='input' or 'marginal'", 0, warn=True)
         self.tree.root.up = None
         self.tree.root.dist2root = 0.0
-        from .treeanc import TreeAnc as _OwnTreeAnc  # (treeanc imports this module)
-        if type(self)._prepare_nodes is _OwnTreeAnc._prepare_nodes:
-            # the topology is the session's (checked when this call began), so of what
-            # _prepare_nodes re-derives only the distances to the root change
-            _set_dist2root(layout, lengths)
-        else:
+        if not own_prepare:
             self._prepare_nodes()
+        elif d2r is None:
+            _set_dist2root(layout, lengths)
         return ttconf.SUCCESS
 
     def optimal_branch_length(self, node):

@@ -1,7 +1,9 @@
 // Branch-length optimisation (TreeAnc.optimize_branch_lengths_joint and the marginal variant):
 //   - state-pair histograms per branch (GTR.state_pair, treetime/gtr.py:631-712);
 //   - Brent minimisation over s = sqrt(t) of the pair likelihood (GTR.optimal_t_compressed with
-//     GTR.prob_t_compressed, treetime/gtr.py:717-749, :816-920), one warp per branch;
+//     GTR.prob_t_compressed, treetime/gtr.py:717-749, :816-920), one warp per branch (8 lanes
+//     when q <= 8), over the branch's nonzero pairs only, each exponential of an evaluation
+//     formed once;
 //   - the same for profile pairs (GTR.prob_t_profiles, treetime/gtr.py:922-963), one CTA per
 //     branch with the per-pattern eigen coefficients staged in shared memory.
 //
@@ -24,36 +26,79 @@ __device__ __forceinline__ int tree_of(const tt_tree* trees, int n_trees, int64_
 }
 
 // -------------------------------------------------------------- state pairs
-__global__ void state_pairs_kernel(tt_forest f, const uint8_t* __restrict__ states,
-                                   const uint8_t* __restrict__ char_state, int tips_use_states, int gap,
-                                   int ignore_gaps, const uint8_t* __restrict__ use, double* __restrict__ hist) {
-    extern __shared__ double h[];
-    const int q = f.n_states;
+// One CTA per branch, threads over patterns.  The weight of a pattern is its multiplicity (times
+// the branch's mask value where the branch has a mask).  Multiplicities are whole numbers, so on
+// a branch without a mask the sums are formed in 32-bit integers -- exact, the same numbers as
+// TreeTime's float sums of whole numbers -- without floating-point atomics: with few states
+// (q*q <= 32 bins) each warp adds every bin with one integer warp reduction per 32 patterns (32
+// weights of at most 2^24 cannot overflow it), bin b's running total held by lane b in 64 bits;
+// with more states each warp adds into its own 64-bit bins in shared memory.  A weight that is
+// not a whole number in [0, 2^24] (and every weight of a masked branch) goes to FP64 bins instead.
+constexpr int kPairThreads = 256;
+
+__global__ void __launch_bounds__(kPairThreads) state_pairs_kernel(
+    tt_forest f, const uint8_t* __restrict__ states, const uint8_t* __restrict__ char_state, int tips_use_states,
+    int gap, int ignore_gaps, const uint8_t* __restrict__ use, double* __restrict__ hist) {
+    extern __shared__ double h[];                                   // [q*q] FP64 bins
+    unsigned long long* hi = reinterpret_cast<unsigned long long*>(h + f.n_states * f.n_states);  // [warps][q*q]
+    const int q = f.n_states, qq = q * q;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int NW = kPairThreads / 32;
+    const bool few = qq <= 32;
     for (int64_t g = blockIdx.x; g < f.n_nodes; g += gridDim.x) {
         if (use && !use[g]) continue;
         const tt_tree tr = f.trees[tree_of(f.trees, f.n_trees, g)];
         const int k = (int)(g - tr.node_base);
         const int par = f.parent[g];
         if (par < 0) continue;
-        for (int i = threadIdx.x; i < q * q; i += blockDim.x) h[i] = 0.0;
+        for (int i = threadIdx.x; i < qq; i += blockDim.x) h[i] = 0.0;
+        if (!few)
+            for (int i = threadIdx.x; i < NW * qq; i += blockDim.x) hi[i] = 0ull;
         __syncthreads();
         const int P = tr.n_patterns;
         const bool tip = k >= tr.n_int && !tips_use_states;
         const int r = tip ? f.tip_row[g] : 0;
         const int64_t mo = f.mask_off ? f.mask_off[g] : -1;
-        for (int p = threadIdx.x; p < P; p += blockDim.x) {
-            const int sp = states[tr.state_base + (int64_t)par * P + p];
-            int sc;
-            if (tip) sc = r < 0 ? 255 : char_state[f.tip_codes[tr.tip_base + (int64_t)r * P + p]];
-            else sc = states[tr.state_base + (int64_t)k * P + p];
-            if (sp >= q || sc >= q) continue;
-            if (ignore_gaps && (sp == gap || sc == gap)) continue;
-            double w = f.mult[tr.pat_base + p];
-            if (mo >= 0) w *= f.masks[mo + p];
-            atomicAdd(&h[sp * q + sc], w);
+        const uint8_t* sp_row = states + tr.state_base + (int64_t)par * P;
+        const uint8_t* sc_row = states + tr.state_base + (int64_t)k * P;
+        const uint8_t* code_row = f.tip_codes + tr.tip_base + (int64_t)(r < 0 ? 0 : r) * P;
+        unsigned long long acc = 0;  // few states: lane b's running total of bin b
+        // warp-uniform trip count (the integer warp reductions need every lane)
+        for (int p0 = 0; p0 < P; p0 += kPairThreads) {
+            const int p = p0 + (int)threadIdx.x;
+            int bin = -1;
+            unsigned iw = 0;
+            if (p < P) {
+                const int sp = sp_row[p];
+                const int sc = tip ? (r < 0 ? 255 : char_state[code_row[p]]) : sc_row[p];
+                if (sp < q && sc < q && !(ignore_gaps && (sp == gap || sc == gap))) {
+                    const double w = f.mult[tr.pat_base + p];
+                    if (mo < 0 && w >= 0.0 && w <= 16777216.0 && w == rint(w)) {
+                        bin = sp * q + sc;
+                        iw = (unsigned)w;
+                    } else {
+                        atomicAdd(&h[sp * q + sc], mo >= 0 ? w * f.masks[mo + p] : w);
+                    }
+                }
+            }
+            if (few) {
+                for (int b2 = 0; b2 < qq; ++b2) {
+                    const unsigned v = __reduce_add_sync(0xffffffffu, bin == b2 ? iw : 0u);
+                    if (lane == b2) acc += v;
+                }
+            } else if (bin >= 0) {
+                atomicAdd(&hi[warp * qq + bin], (unsigned long long)iw);
+            }
+        }
+        if (few) {
+            if (lane < qq) hi[warp * qq + lane] = acc;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < q * q; i += blockDim.x) hist[g * q * q + i] = h[i];
+        for (int i = threadIdx.x; i < qq; i += blockDim.x) {
+            unsigned long long tot = 0;
+            for (int w2 = 0; w2 < NW; ++w2) tot += hi[w2 * qq + i];
+            hist[g * qq + i] = (double)tot + h[i];
+        }
         __syncthreads();
     }
 }
@@ -127,77 +172,150 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// -log-likelihood of the pair histogram at t (lanes split the q*q pairs)
+// Sum over the LB lanes of a group (LB = 8 or 32; the mask holds the group's lanes): an xor
+// butterfly, every lane ends with the same value.
+__device__ __forceinline__ double group_sum(double v, unsigned mask, int LB) {
+    if (LB == 32) {
+        v += __shfl_xor_sync(mask, v, 16);
+        v += __shfl_xor_sync(mask, v, 8);
+    }
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off);
+    return v;
+}
+
+// Group layout of the pair kernels: with q <= 8 states a group of 8 lanes takes a branch (four
+// branches per warp, each FP64 instruction of the search serving all four), otherwise a warp.
+__host__ __device__ __forceinline__ int pair_group_lanes(int q) { return q <= 8 ? 8 : 32; }
+
+// A group's branch in shared memory: the nonzero pairs of its histogram, in (parent, child)
+// order, and the q exponentials of the current evaluation.
+struct PairSlot {
+    double* c;    // [q*q] counts of the nonzero pairs
+    int* idx;     // [q*q] their pair index parent * q + child
+    double* ex;   // [q]
+};
+
+__device__ __forceinline__ PairSlot pair_slot(double* base, int slot, int q) {
+    const int qq = q * q;
+    double* s = base + (int64_t)slot * (2 * qq + q);
+    return PairSlot{s, reinterpret_cast<int*>(s + qq), s + qq + qq / 2 + 1};
+}
+
+// Stage branch b's nonzero pairs (order kept, by ballots over the group); returns their number
+// and the group sums of all counts (tot) and of the changes (diff).
+__device__ __forceinline__ int stage_pairs(const double* __restrict__ counts, int64_t b, int q, const PairSlot& ps,
+                                           int gl, int sub, int LB, unsigned mask, double& tot, double& diff) {
+    const int qq = q * q;
+    int nnz = 0;
+    tot = 0.0;
+    diff = 0.0;
+    for (int i0 = 0; i0 < qq; i0 += LB) {
+        const int idx = i0 + gl;
+        const double c = idx < qq ? counts[b * qq + idx] : 0.0;
+        const bool nz = c != 0.0;
+        const unsigned bal = __ballot_sync(mask, nz);
+        const unsigned bits = LB == 32 ? bal : (bal >> (sub * LB)) & ((1u << LB) - 1u);
+        if (nz) {
+            const int pos = nnz + __popc(bits & ((1u << gl) - 1u));
+            ps.c[pos] = c;
+            ps.idx[pos] = idx;
+        }
+        nnz += __popc(bits);
+        tot += c;
+        if (idx < qq && idx / q != idx % q) diff += c;
+    }
+    __syncwarp(mask);
+    tot = group_sum(tot, mask, LB);
+    diff = group_sum(diff, mask, LB);
+    return nnz;
+}
+
+// -log-likelihood of the pair histogram at t: the LB lanes of a group split the nonzero pairs.
+// The q exponentials exp(mu lam_k t) are formed once per evaluation (lane k of the group) and
+// shared through shared memory.
 struct PairObjective {
     int q;
     const double* V;
     const double* Vi;
     const double* lam;
     double mu;
-    const double* cnt;   // [q][q] truncated counts, parent-major
-    int lane;
+    PairSlot ps;
+    int nnz;
+    int lane;            // lane within the group
+    int LB;              // lanes per group
+    unsigned mask;       // the group's lanes
     __device__ double operator()(double s) const { return at_t(s * s); }
     // the objective at branch length t itself (prob_t_compressed takes t, the search s = sqrt(t))
     __device__ double at_t(double t) const {
+        __syncwarp(mask);  // the previous evaluation's readers are done with ex
+        for (int k = lane; k < q; k += LB) ps.ex[k] = exp(mu * lam[k] * t);
+        __syncwarp(mask);
         double acc = 0.0;
-        for (int idx = lane; idx < q * q; idx += 32) {
-            const double c = cnt[idx];
-            if (c == 0.0) continue;
+        for (int j = lane; j < nnz; j += LB) {
+            const int idx = ps.idx[j];
             const int ip = idx / q, jc = idx % q;  // parent state, child state
             double pv = 0.0;
-            for (int k = 0; k < q; ++k) pv = fma(V[jc * q + k], exp(mu * lam[k] * t) * Vi[k * q + ip], pv);
+            for (int k = 0; k < q; ++k) pv = fma(V[jc * q + k], ps.ex[k] * Vi[k * q + ip], pv);
             pv = pv > 0.0 ? pv : 0.0;
-            acc += log(pv > kSuperTiny ? pv : kSuperTiny) * c;
+            acc += log(pv > kSuperTiny ? pv : kSuperTiny) * ps.c[j];
         }
-        return -warp_sum(acc);
+        return -group_sum(acc, mask, LB);
     }
 };
 
+// Shared memory of the pair kernels: per group 2 q^2 + q doubles.
+static inline size_t pair_smem(int q, int groups) { return (size_t)groups * (2 * q * q + q) * sizeof(double); }
+
+// One group of LB lanes per branch: Brent over s = sqrt(t) from the bracket (-2, sqrt(hamming), 2)
+// (treetime/gtr.py:816-920); the groups of a warp run their own branches independently.
 __global__ void optimal_t_pairs_kernel(int q, int64_t n, const double* __restrict__ counts,
                                        const int32_t* __restrict__ model_of, tt_model m, double tol,
                                        double* __restrict__ t_out, int32_t* __restrict__ info) {
-    extern __shared__ double cnt_s[];
+    extern __shared__ double pair_s[];
+    const int LB = pair_group_lanes(q), gpw = 32 / LB;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    double* cnt = cnt_s + warp * q * q;
-    for (int64_t b = (int64_t)blockIdx.x * nw + warp; b < n; b += (int64_t)gridDim.x * nw) {
-        double tot = 0.0, diff = 0.0;
-        for (int idx = lane; idx < q * q; idx += 32) {
-            const double c = counts[b * q * q + idx];
-            cnt[idx] = c;
-            tot += c;
-            if (idx / q != idx % q) diff += c;
-        }
-        __syncwarp();
-        tot = warp_sum(tot);
-        diff = warp_sum(diff);
+    const int sub = lane / LB, gl = lane % LB;
+    const unsigned mask = LB == 32 ? 0xffffffffu : (((1u << LB) - 1u) << (LB * sub));
+    const int slot = warp * gpw + sub;
+    const PairSlot ps = pair_slot(pair_s, slot, q);
+    const int64_t groups = (int64_t)gridDim.x * nw * gpw;
+    for (int64_t b = (int64_t)blockIdx.x * nw * gpw + slot; b < n; b += groups) {
+        double tot, diff;
+        const int nnz = stage_pairs(counts, b, q, ps, gl, sub, LB, mask, tot, diff);
         const int mi = model_of ? model_of[b] : 0;
         PairObjective f{q, m.V + (int64_t)mi * q * q, m.Vinv + (int64_t)mi * q * q, m.lam + (int64_t)mi * q,
-                        m.mu[mi], cnt, lane};
+                        m.mu[mi], ps, nnz, gl, LB, mask};
         const double hamming = diff / tot;
         BrentOut r = brent_minimize(f, -2.0, sqrt(hamming), 2.0, tol, 500);
-        if (lane == 0) {
+        if (gl == 0) {
             t_out[b] = r.state == 0 ? r.x * r.x : hamming;
             if (info) info[b] = r.state == 2 ? -1 : (r.state == 1 ? -2 : r.iters);
         }
-        __syncwarp();
+        __syncwarp(mask);
     }
 }
 
 __global__ void prob_t_pairs_kernel(int q, int64_t n, const double* __restrict__ counts,
                                     const int32_t* __restrict__ model_of, tt_model m, const double* __restrict__ t,
                                     double* __restrict__ out) {
-    extern __shared__ double cnt_s[];
+    extern __shared__ double pair_s[];
+    const int LB = pair_group_lanes(q), gpw = 32 / LB;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    double* cnt = cnt_s + warp * q * q;
-    for (int64_t b = (int64_t)blockIdx.x * nw + warp; b < n; b += (int64_t)gridDim.x * nw) {
-        for (int idx = lane; idx < q * q; idx += 32) cnt[idx] = counts[b * q * q + idx];
-        __syncwarp();
+    const int sub = lane / LB, gl = lane % LB;
+    const unsigned mask = LB == 32 ? 0xffffffffu : (((1u << LB) - 1u) << (LB * sub));
+    const int slot = warp * gpw + sub;
+    const PairSlot ps = pair_slot(pair_s, slot, q);
+    const int64_t groups = (int64_t)gridDim.x * nw * gpw;
+    for (int64_t b = (int64_t)blockIdx.x * nw * gpw + slot; b < n; b += groups) {
+        double tot, diff;
+        const int nnz = stage_pairs(counts, b, q, ps, gl, sub, LB, mask, tot, diff);
         const int mi = model_of ? model_of[b] : 0;
         PairObjective f{q, m.V + (int64_t)mi * q * q, m.Vinv + (int64_t)mi * q * q, m.lam + (int64_t)mi * q,
-                        m.mu[mi], cnt, lane};
+                        m.mu[mi], ps, nnz, gl, LB, mask};
         const double v = t[b] < 0 ? kBig : f.at_t(t[b]);
-        if (lane == 0) out[b] = -v;
-        __syncwarp();
+        if (gl == 0) out[b] = -v;
+        __syncwarp(mask);
     }
 }
 
@@ -478,7 +596,10 @@ extern "C" tt_status tt_state_pairs(const tt_forest* f, const uint8_t* states, c
     if (f->n_nodes == 0) return TT_OK;
     const int q = f->n_states;
     int64_t blocks = f->n_nodes < 65535 * 4 ? f->n_nodes : 65535 * 4;
-    state_pairs_kernel<<<(unsigned)blocks, 256, q * q * sizeof(double), as_stream(stream)>>>(
+    const size_t smem = q * q * sizeof(double) + (kPairThreads / 32) * q * q * sizeof(unsigned long long);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(state_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    state_pairs_kernel<<<(unsigned)blocks, kPairThreads, smem, as_stream(stream)>>>(
         *f, states, char_state, tips_use_states, gap_state, ignore_gaps, use, hist);
     return check_launch("tt_state_pairs");
 }
@@ -491,10 +612,13 @@ extern "C" tt_status tt_optimal_t_pairs(int32_t q, int64_t n, const double* coun
         return TT_ERR_INVALID;
     }
     if (n == 0) return TT_OK;
-    const int warps = 4;
-    int64_t blocks = (n + warps - 1) / warps;
+    const int warps = 4, per_block = warps * (32 / pair_group_lanes(q));
+    int64_t blocks = (n + per_block - 1) / per_block;
     if (blocks > 65535 * 4) blocks = 65535 * 4;
-    optimal_t_pairs_kernel<<<(unsigned)blocks, warps * 32, warps * q * q * sizeof(double), as_stream(stream)>>>(
+    const size_t smem = pair_smem(q, per_block);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(optimal_t_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    optimal_t_pairs_kernel<<<(unsigned)blocks, warps * 32, smem, as_stream(stream)>>>(
         q, n, counts, model_of, *m, tol, t_out, info);
     return check_launch("tt_optimal_t_pairs");
 }
@@ -506,10 +630,13 @@ extern "C" tt_status tt_prob_t_pairs(int32_t q, int64_t n, const double* counts,
         return TT_ERR_INVALID;
     }
     if (n == 0) return TT_OK;
-    const int warps = 4;
-    int64_t blocks = (n + warps - 1) / warps;
+    const int warps = 4, per_block = warps * (32 / pair_group_lanes(q));
+    int64_t blocks = (n + per_block - 1) / per_block;
     if (blocks > 65535 * 4) blocks = 65535 * 4;
-    prob_t_pairs_kernel<<<(unsigned)blocks, warps * 32, warps * q * q * sizeof(double), as_stream(stream)>>>(
+    const size_t smem = pair_smem(q, per_block);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(prob_t_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    prob_t_pairs_kernel<<<(unsigned)blocks, warps * 32, smem, as_stream(stream)>>>(
         q, n, counts, model_of, *m, t, logp_out);
     return check_launch("tt_prob_t_pairs");
 }

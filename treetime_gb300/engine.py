@@ -176,11 +176,15 @@ def branch_lengths(layout, full_length, use_mutation_length=False):
     (TreeAnc._branch_length_to_gtr, treetime/treeanc.py:752-760).  Python's
     max keeps its first argument when the comparison with a NaN is false, so a
     NaN length becomes the floor there; np.fmax does the same."""
-    floor = ttconf.MIN_BRANCH_LENGTH * (1.0 / full_length)
     attr = "mutation_length" if use_mutation_length else "branch_length"
     # None (no length) becomes NaN here and the floor below, as `or 0.0` would make it
     bl = np.array(list(map(operator.attrgetter(attr), layout.nodes)), dtype=np.float64)
-    return np.fmax(floor, bl)
+    return length_floor(bl, full_length)
+
+
+def length_floor(bl, full_length):
+    """max(1e-3 / L, length) of an array of lengths (NaN becomes the floor)."""
+    return np.fmax(ttconf.MIN_BRANCH_LENGTH * (1.0 / full_length), bl)
 
 
 # ----------------------------------------------------------------------------
@@ -657,6 +661,26 @@ def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_
     return out
 
 
+class CapturedCall:
+    """One call of a pass function (marginal, joint: its buffer clears and launches) captured as
+    a CUDA graph, replayed with a single host call.  The kernels read the forest's device inputs
+    (tip codes, branch lengths, multiplicities) at replay, so values written there in place are
+    seen; the outputs are the same device buffers every time.  The function must have run on
+    this forest with the same options before (buffers allocated, kernel attributes set), so that
+    nothing is allocated or configured inside the capture."""
+
+    def __init__(self, fn, *args, **kw):
+        t = torch()
+        self.graph = t.cuda.CUDAGraph()
+        with t.cuda.graph(self.graph):
+            self.out = fn(*args, sync=False, **kw)
+        self._keep = args  # the captured launches point into these objects' device buffers
+
+    def replay(self):
+        self.graph.replay()
+        return self.out
+
+
 class CapturedMarginal:
     """One marginal pass over a forest captured as a CUDA graph: the buffer
     clears and the three launches (branch matrices, the pass, the per-tree
@@ -887,13 +911,14 @@ def joint(forest, model, bufs, reconstruct_tips=False, count_diff=False, root_un
 
 
 def state_pairs(forest, bufs, char_state, gap_state, ignore_gaps, tips_use_states):
-    """[n_nodes, q, q] multiplicity-weighted (parent, child) histograms."""
+    """[n_nodes, q, q] multiplicity-weighted (parent, child) histograms
+    (char_state: the byte -> state table, host array or device tensor)."""
     t = torch()
     lib = _lib.load()
     q = forest.q
     hist = bufs.get("hist", (forest.n_nodes, q, q), t.float64)
     hist.zero_()
-    cs = _to_dev(char_state, forest.device)
+    cs = char_state if hasattr(char_state, "data_ptr") else _to_dev(char_state, forest.device)
     check(lib.tt_state_pairs(C.byref(forest.struct), _p(bufs.cache[("states", t.uint8)]), _p(cs), int(bool(tips_use_states)),
                              -1 if gap_state is None else int(gap_state), int(bool(ignore_gaps)), None, _p(hist),
                              _stream()), "tt_state_pairs")

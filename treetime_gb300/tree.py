@@ -162,6 +162,35 @@ def topology_epoch():
     return _EPOCH[0]
 
 
+# Bumped by every assignment of a Clade's branch length: a session whose device copy of the
+# lengths was made at the current value needs neither the walk over the nodes that reads them
+# nor the upload.
+_BL_EPOCH = [0]
+
+
+def length_epoch():
+    """The current value of the change counter of Clade branch lengths."""
+    return _BL_EPOCH[0]
+
+
+def assign_lengths(dicts, lengths, dist2root=None):
+    """New branch lengths for many Clades, given their ``__dict__``s, with one
+    bump of the change counter (the caller then owns keeping any device copy
+    in step): branch_length and mutation_length take the length, dist2root the
+    given distance.  One loop of dictionary stores, ~25 ns a value, where three
+    loops of attribute assignments cost ~75 ns a value."""
+    _BL_EPOCH[0] += 1
+    if dist2root is None:
+        for d, v in zip(dicts, lengths):
+            d["_branch_length"] = v
+            d["mutation_length"] = v
+    else:
+        for d, v, r in zip(dicts, lengths, dist2root):
+            d["_branch_length"] = v
+            d["mutation_length"] = v
+            d["dist2root"] = r
+
+
 class _Children(list):
     """A Clade's list of children: every mutation bumps the change counter."""
 
@@ -222,6 +251,11 @@ def _set_clades(node, value):
     node.__dict__["_clades"] = value if type(value) is _Children else _Children(value)
 
 
+def _set_branch_length(node, value):
+    _BL_EPOCH[0] += 1
+    node.__dict__["_branch_length"] = value
+
+
 def _get_mask(node):
     try:
         return node.__dict__["mask"]
@@ -243,9 +277,11 @@ def _del_mask(node):
 
 
 class Clade(_Traversal):
-    # children and mask go through the change counter; the read of `clades` is a C-level getter
+    # children, mask and branch length go through the change counters; the reads of `clades` and
+    # `branch_length` are C-level getters
     clades = property(operator.attrgetter("_clades"), _set_clades)
     mask = property(_get_mask, _set_mask, _del_mask)
+    branch_length = property(operator.attrgetter("_branch_length"), _set_branch_length)
 
     def __init__(self, branch_length=None, name=None, clades=None, confidence=None):
         self.branch_length = branch_length

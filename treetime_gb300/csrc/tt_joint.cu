@@ -424,8 +424,11 @@ __global__ void __launch_bounds__(NT, 1) joint_kernel(JointParams a) {
         };
 
         // ------------------------------------------------------------ post-order
+        // a level of more than CH nodes is cut into chunks of whole node rounds (the largest
+        // multiple of G that fits the stage buffer), so that only its last chunk has idle groups
+        const int CHR = G <= CH ? CH / G * G : CH;
         auto post_chunk = [&](int h, int base, int& he) -> int {
-            if (LV(h + 1) - base > CH) { he = h; return base + CH; }
+            if (LV(h + 1) - base > CH) { he = h; return base + CHR; }
             int e = h + 1;
             while (e < nlev && LV(e + 1) - base <= CH) ++e;
             he = e - 1;

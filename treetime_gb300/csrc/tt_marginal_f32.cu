@@ -184,6 +184,10 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
             cp_async_commit();
         };
         const int GD = G * D;
+        // a level of more than CH nodes is cut into chunks of whole node rounds (the largest
+        // multiple of GD that fits the stage buffer), so that only its last chunk has idle
+        // groups: 265 nodes with 53 groups take 5 rounds as 212 + 53, 6 as 256 + 9
+        const int CHR = GD <= CH ? CH / GD * GD : CH;
 
         // ------------------------------------------------------------ post-order
         // A chunk is a slice of CH nodes of a wide level, or several whole narrow levels together
@@ -191,7 +195,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         // CTA barrier only.  post_chunk returns the end of the chunk starting at node `base` of
         // level h and its last level.
         auto post_chunk = [&](int h, int base, int& he) -> int {
-            if (LV(h + 1) - base > CH) { he = h; return base + CH; }
+            if (LV(h + 1) - base > CH) { he = h; return base + CHR; }
             int e = h + 1;
             while (e < nlev && LV(e + 1) - base <= CH) ++e;
             he = e - 1;
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
         auto pre_chunk = [&](int h, int cur, int& lo, int& hi, int& hb, int& nh, int& ncur) {
             if (h < 0) {
                 lo = cur;
-                hi = min(cur + CH, n_int + tr.n_tip);
+                hi = n_int + tr.n_tip - cur > CH ? cur + CHR : n_int + tr.n_tip;
                 hb = -1;
                 nh = hi < n_int + tr.n_tip ? -1 : -2;
                 ncur = hi;
@@ -319,7 +323,7 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
             }
             hi = cur;
             if (cur - LV(h) > CH) {
-                lo = cur - CH;
+                lo = cur - CHR;
                 hb = h;
                 nh = h;
                 ncur = lo;

@@ -245,6 +245,24 @@ tt_status tt_propagate(int32_t q, int64_t n, const double* prof, const double* p
 tt_status tt_marginal(const tt_forest* f, const tt_model* m, const tt_pmats* pm, int32_t precision,
                       const tt_marginal_out* out, int32_t* status, void* stream);
 
+/* Outgroup profiles of a finished FP32 marginal pass run without them (out->outgroup and
+ * tip_outgroup NULL): per non-root node and pattern, normalise(max(1e-12, parent's posterior) /
+ * the node's message x + x.D, masked as the pass masks it), from `posterior` and `partial` of the
+ * pass and the FP32 D matrices (pm->p32) of the branch lengths the pass used; the same FP32
+ * operations as the pass's pre-order, so the rows equal the ones the pass would have stored.
+ * Either output may be NULL.  Alphabets of 2 to 5 states (one lane per pattern).
+ * Replaces the marginal_outgroup_LH step of TreeAnc.preorder_traversal_marginal
+ * (treetime/treeanc.py:894-899). */
+tt_status tt_outgroups_f32(const tt_forest* f, const tt_model* m, const tt_pmats* pm, const float* posterior,
+                           const float* partial, float* outgroup, float* tip_outgroup, void* stream);
+
+/* Changed-site counts of a marginal pass run without count_diff: states (a copy taken before the
+ * pass) against the pass's states, on the rows the pass counts -- internal nodes but the root,
+ * and the tips when `tips` -- added to n_diff[tree] (zero it first).  The N_diff of
+ * TreeAnc.preorder_traversal_marginal (treetime/treeanc.py:924-927). */
+tt_status tt_count_changes(const tt_forest* f, const uint8_t* old_states, const uint8_t* states, int32_t tips,
+                           int64_t* n_diff, void* stream);
+
 /* Site-specific model (GTR_site_specific): per-pattern V, V^-1, eigenvalues, rates and
  * equilibrium frequencies; P_a(t) evaluated in the eigenbasis, with TreeTime's linear
  * interpolation on the time grid `t_grid` (n_grid points) when `approximate` is set and

@@ -81,6 +81,8 @@ _SIGS = {
     "tt_branch_pmats": (i32, [P(TTForest), P(TTModel), TTPmats, vp, vp]),
     "tt_propagate": (i32, [i32, i64, vp, vp, vp, i32, i32, vp, vp]),
     "tt_marginal": (i32, [P(TTForest), P(TTModel), P(TTPmats), i32, P(TTMarginalOut), vp, vp]),
+    "tt_outgroups_f32": (i32, [P(TTForest), P(TTModel), P(TTPmats), vp, vp, vp, vp, vp]),
+    "tt_count_changes": (i32, [P(TTForest), vp, vp, i32, vp, vp]),
     "tt_marginal_ss": (i32, [P(TTForest), vp, vp, vp, vp, vp, vp, vp, i32, f64, i32, i32, P(TTMarginalOut), vp, vp]),
     "tt_marginal_ss_f32": (i32, [P(TTForest), P(TTSSF32), vp, i32, P(TTMarginalOut), vp, vp]),
     "tt_joint": (i32, [P(TTForest), P(TTModel), P(TTPmats), P(TTJointOut), vp, vp]),

@@ -159,37 +159,58 @@ def _pinned_pair(sess, a, b):
     return tuple(v.numpy().copy().reshape(x.shape) for v, x in zip(outs, (a, b)))
 
 
-def _host_results(sess, out, rows, P, site_key="site_lh", tree_key="tree_lh", n_diff=True):
-    """The results every reconstruction hands to the host -- the states of the
-    reconstructed rows, the site and tree log-likelihoods and the changed-site
-    count -- through page-locked buffers of the session, as asynchronous copies
-    on the current stream followed by one wait; the kernels' status word comes
-    with them (the passes are launched without a wait of their own) and is
-    checked before anything is returned.  The states array returned is a view
-    of the session's buffer: valid until the session's next reconstruction (the
-    results installed on the nodes read it only until then)."""
-    torch = engine.torch()
-    nb = rows * P
+def _pinned_results(sess, P):
+    """The session's page-locked result buffers (states of every node, site
+    and tree log-likelihoods, changed-site count, status word), made once at
+    their largest size: the session's CUDA graphs copy into them, so they are
+    never replaced."""
     pb = sess.get("pinned")
-    if pb is None or pb[0].numel() < nb or pb[1].numel() < P + 1:
-        pb = (torch.empty(max(nb, 1), dtype=torch.uint8, pin_memory=True),
+    if pb is None:
+        torch = engine.torch()
+        n = sess["layout"].n_nodes * P
+        pb = (torch.empty(max(n, 1), dtype=torch.uint8, pin_memory=True),
               torch.empty(P + 1, dtype=torch.float64, pin_memory=True),
               torch.empty(1, dtype=torch.int64, pin_memory=True),
               torch.empty(1, dtype=torch.int32, pin_memory=True))
         sess["pinned"] = pb
-    st, sc, nd, stat = pb
-    status = sess["bufs"].get("status", (1,), torch.int32)
-    stat.copy_(status, non_blocking=True)
+    return pb
+
+
+def _copy_results(sess, out, rows, P, site_key="site_lh", tree_key="tree_lh", n_diff=True):
+    """Asynchronous copies of a reconstruction's host results into the
+    session's page-locked buffers, on the current stream (also inside a CUDA
+    graph capture)."""
+    torch = engine.torch()
+    st, sc, nd, stat = _pinned_results(sess, P)
+    nb = rows * P
+    stat.copy_(sess["bufs"].get("status", (1,), torch.int32), non_blocking=True)
     st[:nb].copy_(out["states"].view(-1)[:nb], non_blocking=True)
     sc[:P].copy_(out[site_key][:P], non_blocking=True)
     sc[P:P + 1].copy_(out[tree_key][:1], non_blocking=True)
     if n_diff:
         nd.copy_(out["n_diff"][:1], non_blocking=True)
+
+
+def _host_results(sess, out, rows, P, site_key="site_lh", tree_key="tree_lh", n_diff=True, copied=False):
+    """The results every reconstruction hands to the host -- the states of the
+    reconstructed rows, the site and tree log-likelihoods and the changed-site
+    count -- through page-locked buffers of the session, as asynchronous copies
+    on the current stream (already queued when `copied`: a session graph
+    holds them) followed by one wait; the kernels' status word comes with them
+    (the passes are launched without a wait of their own) and is checked
+    before anything is returned.  The states array returned is a view of the
+    session's buffer: valid until the session's next reconstruction (the
+    results installed on the nodes read it only until then)."""
+    torch = engine.torch()
+    if not copied:
+        _copy_results(sess, out, rows, P, site_key, tree_key, n_diff)
+    st, sc, nd, stat = _pinned_results(sess, P)
     torch.cuda.current_stream(out["states"].device).synchronize()
     s = int(stat.numpy()[0])
     if s:
         engine.check(s, "kernel status")
     scn = sc.numpy()
+    nb = rows * P
     return (st.numpy()[:nb].reshape(rows, P), scn[:P].copy(), float(scn[P]),
             int(nd.numpy()[0]) if n_diff else 0)
 
@@ -217,6 +238,8 @@ class ResultStore:
 
     def _fetch_buf(self, key):
         if key not in self._host:
+            if key in ("outgroup", "tip_outgroup") and self.out.get("_outgroups") is not None:
+                self.out["_outgroups"]()  # rows formed on request (engine.outgroups)
             buf = self.out.get(key)
             self._host[key] = None if buf is None else buf.cpu().numpy()
         return self._host[key]
@@ -458,20 +481,25 @@ class GPUAncMixin:
                 if v is not None:
                     setattr(n, a, v)
 
-    def _pass(self, sess, fn, key, *args, **kw):
-        """One pass of the session launched without a wait: the first call with a set of options
-        runs it directly, the second captures it as a CUDA graph (engine.CapturedCall), later
-        ones replay the graph -- the same kernels on the same buffers with one host call instead
-        of a dozen launches.  The graphs live with the session (a new topology, alignment or
-        model starts without them); branch lengths and tip codes are read at replay."""
+    def _pass(self, sess, fn, key, rows, *args, **kw):
+        """One pass of the session launched without a wait, returning (device outputs, whether
+        the host results are already queued for copying): the first call with a set of options
+        runs it directly, the second captures it as a CUDA graph (engine.CapturedCall) together
+        with the copies of its host results into the session's page-locked buffers, later ones
+        replay the graph -- the same kernels and copies on the same buffers with one host call
+        instead of a dozen launches.  The graphs live with the session (a new topology, alignment
+        or model starts without them); branch lengths and tip codes are read at replay."""
         graphs = sess.setdefault("graphs", {})
         g = graphs.get(key)
         if g is None:
             graphs[key] = 1
-            return fn(*args, sync=False, **kw)
+            return fn(*args, sync=False, **kw), False
         if g == 1:
-            g = graphs[key] = engine.CapturedCall(fn, *args, **kw)
-        return g.replay()
+            P = self.data.compressed_length
+            _pinned_results(sess, P)  # page-locked memory is allocated outside the capture
+            g = graphs[key] = engine.CapturedCall(fn, *args, after=lambda out: _copy_results(sess, out, rows, P),
+                                                  **kw)
+        return g.replay(), True
 
     def _root_draws(self, sample_from_profile):
         """The root's uniform draws (sample_from_profile 'root' or True), one
@@ -509,18 +537,39 @@ class GPUAncMixin:
         prec = self._gpu_precision()
         kw = dict(precision=prec, reconstruct_tips=reconstruct_tip_states, keep_outgroup=keep_outgroup,
                   tip_outgroup=keep_outgroup, count_diff=count_diff, root_uniform=draws, node_uniform=node_draws)
-        if self.gtr.is_site_specific:
+        rows = layout.n_nodes if reconstruct_tip_states else layout.n_int
+        copied = False
+        if prec == "f32" and not self.gtr.is_site_specific and self.gtr.n_states <= 5:
+            # the pass without its outgroup rows (formed when first asked for, from the branch
+            # lengths it used) and with the changed-site count by a compare kernel: the same
+            # results, without the pre-order's tip level and the outgroup stores
+            snap = sess.setdefault("snap", {})
+            lkw = dict(reconstruct_tips=reconstruct_tip_states, count_diff=count_diff, root_uniform=draws,
+                       node_uniform=node_draws)
+            if draws is None and node_draws is None:
+                out, copied = self._pass(sess, engine.marginal_lean, ("lean",) + tuple(sorted(lkw.items())), rows,
+                                         sess["forest"], sess["model"], sess["bufs"], snap, **lkw)
+            else:
+                out = engine.marginal_lean(sess["forest"], sess["model"], sess["bufs"], snap, sync=False, **lkw)
+            out = dict(out)  # this reconstruction's view: its outgroup rows are not formed yet
+            out["outgroup"] = out["tip_outgroup"] = None
+            if keep_outgroup:
+                scratch = sess.get("og_scratch")
+                if scratch is None:
+                    scratch = sess["og_scratch"] = engine.Buffers(sess["forest"])
+                f, m, b = sess["forest"], sess["model"], sess["bufs"]
+                out["_outgroups"] = lambda o=out: engine.outgroups(f, m, b, o, snap, scratch)
+        elif self.gtr.is_site_specific:
             out = engine.marginal_site_specific(sess["forest"], self.gtr, sess["bufs"], sync=False, **kw)
         elif draws is None and node_draws is None:
-            out = self._pass(sess, engine.marginal, ("marginal",) + tuple(sorted(kw.items())),
-                             sess["forest"], sess["model"], sess["bufs"], **kw)
+            out, copied = self._pass(sess, engine.marginal, ("marginal",) + tuple(sorted(kw.items())), rows,
+                                     sess["forest"], sess["model"], sess["bufs"], **kw)
         else:
             out = engine.marginal(sess["forest"], sess["model"], sess["bufs"], sync=False, **kw)
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
-        rows = layout.n_nodes if reconstruct_tip_states else layout.n_int
-        states, site_lh, total, nd = _host_results(sess, out, rows, P)
+        states, site_lh, total, nd = _host_results(sess, out, rows, P, copied=copied)
         N_diff = nd if count_diff else P * n_recon
         self._install(ResultStore(self, layout, "marginal", out, prec, reconstruct_tip_states, states=states),
                       layout)
@@ -541,22 +590,23 @@ class GPUAncMixin:
         if reconstruct_tip_states and count_diff and not self.reconstructed_tip_sequences:
             self._seed_tip_states(sess)
         draws = self._root_draws(sample_from_profile)
+        rows = layout.n_nodes if reconstruct_tip_states else layout.n_int
+        copied = False
         if self.gtr.is_site_specific:
             out = engine.joint_site_specific(sess["forest"], self.gtr, sess["bufs"],
                                              reconstruct_tips=reconstruct_tip_states, count_diff=count_diff,
                                              root_uniform=draws, sync=False)
         elif draws is None:
-            out = self._pass(sess, engine.joint, ("joint", reconstruct_tip_states, count_diff), sess["forest"],
-                             sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
-                             count_diff=count_diff)
+            out, copied = self._pass(sess, engine.joint, ("joint", reconstruct_tip_states, count_diff), rows,
+                                     sess["forest"], sess["model"], sess["bufs"],
+                                     reconstruct_tips=reconstruct_tip_states, count_diff=count_diff)
         else:
             out = engine.joint(sess["forest"], sess["model"], sess["bufs"], reconstruct_tips=reconstruct_tip_states,
                                count_diff=count_diff, root_uniform=draws, sync=False)
         self._clear_results(layout)
         P = self.data.compressed_length
         n_recon = layout.n_int - 1 + (layout.n_tip if reconstruct_tip_states else 0)
-        rows = layout.n_nodes if reconstruct_tip_states else layout.n_int
-        states, site_lh, total, nd = _host_results(sess, out, rows, P)
+        states, site_lh, total, nd = _host_results(sess, out, rows, P, copied=copied)
         N_diff = nd if count_diff else P * n_recon
         self._install(ResultStore(self, layout, "joint", out, "f64", reconstruct_tip_states, states=states), layout)
         self.tree.sequence_LH = site_lh
@@ -766,6 +816,8 @@ class GPUAncMixin:
         outgroup buffer, parent rows, child rows, partials buffer); the ids and
         rows are numpy arrays (int32, int64, int64)."""
         last = getattr(self, "_last", None)
+        if last is not None and last[0] == "marginal" and last[1].get("_outgroups") is not None:
+            last[1]["_outgroups"]()  # rows formed on request (engine.outgroups)
         if last is None or last[0] != "marginal" or last[1].get("outgroup") is None:
             raise Exception("marginal ancestral inference needs to be performed first!")
         out = last[1]

@@ -501,23 +501,27 @@ __global__ void __launch_bounds__(NT, MINB) marginal_f32_kernel(F32Params fp) {
                                 if (j0 + s < Q) msg[s] = m == 0.f ? 1.f : exp2f(m * log2f(msg[s]));
                         }
                         // outgroup message: parent's posterior divided by this node's message
-                        // (fast division, <= 2 ulp).  Its scale cancels in the posterior, so it is
-                        // normalised only when it is stored.
+                        // (fast division, <= 2 ulp).  Its scale cancels in the posterior, which is
+                        // formed from it unnormalised, so the posteriors do not depend on whether
+                        // the outgroup rows are kept; a kept row is normalised as it is stored.
 #pragma unroll
                         for (int s = 0; s < S; ++s)
                             o[s] = (j0 + s < Q) ? __fdividef(fmaxf(1e-12f, pv[d][s]), msg[s]) : 0.f;
                         if (keep_outgroup) {
+                            // rounded adds and products (no contraction): tt_outgroups_f32 forms
+                            // the same rows with the same operations
                             float sl = 0.f;
 #pragma unroll
-                            for (int s = 0; s < S; ++s) sl += o[s];
+                            for (int s = 0; s < S; ++s) sl = __fadd_rn(sl, o[s]);
                             const float inv = __fdividef(1.f, group_sum<LPP>(sl));
-#pragma unroll
-                            for (int s = 0; s < S; ++s) o[s] *= inv;
                             if (valid) {
+                                float on[S];
+#pragma unroll
+                                for (int s = 0; s < S; ++s) on[s] = __fmul_rn(o[s], inv);
                                 float* og = reinterpret_cast<float*>(tips ? a.o.tip_outgroup : a.o.outgroup);
                                 const int64_t row = tips ? (tr.tipprof_base + (int64_t)(k - n_int) * P + pc) * W + j0
                                                          : (tr.prof_base + (int64_t)k * P + pc) * W + j0;
-                                if (og) st_part<S>(og + row, o);
+                                if (og) st_part<S>(og + row, on);
                             }
                         }
                         if (tips && !a.o.reconstruct_tips) continue;

@@ -661,6 +661,65 @@ def marginal(forest, model, bufs, precision="f64", reconstruct_tips=False, keep_
     return out
 
 
+def marginal_lean(forest, model, bufs, snap, reconstruct_tips=False, count_diff=False, root_uniform=None,
+                  node_uniform=None, sync=True):
+    """The FP32 marginal pass (alphabets up to 5 states) without the outputs nothing in the pass
+    depends on: the outgroup rows (formed on request by `outgroups`) and the changed-site count
+    (tt_count_changes against the states taken before the pass).  `snap` is a dict of device
+    buffers owned by the caller; it receives the branch lengths the pass used ("bl") and, with
+    count_diff, the states before it ("old").  Same outputs as marginal() otherwise."""
+    t = torch()
+    bl = snap.get("bl")
+    if bl is None or bl.shape != forest.d_bl.shape:
+        bl = snap["bl"] = t.empty_like(forest.d_bl)
+    bl.copy_(forest.d_bl)
+    snap["forest"] = forest
+    states = bufs.get("states", (forest.state_rows,), t.uint8)
+    if count_diff:
+        old = snap.get("old")
+        if old is None or old.shape != states.shape:
+            old = snap["old"] = t.empty_like(states)
+        old.copy_(states)
+    out = marginal(forest, model, bufs, precision="f32", reconstruct_tips=reconstruct_tips, count_diff=False,
+                   root_uniform=root_uniform, node_uniform=node_uniform, sync=False)
+    if count_diff:
+        check(_lib.load().tt_count_changes(C.byref(forest.struct), _p(snap["old"]), _p(states),
+                                           int(bool(reconstruct_tips)), _p(out["n_diff"]), _stream()),
+              "tt_count_changes")
+    if sync:
+        _check_status(bufs.get("status", (1,), t.int32))
+    return out
+
+
+def outgroups(forest, model, bufs, out, snap, scratch):
+    """The outgroup rows (internal nodes and tips) of a pass run by marginal_lean, formed once
+    into `bufs`' outgroup buffers and entered into `out`: the branch matrices of the lengths the
+    pass used (snap["bl"]) into `scratch` (a Buffers of its own, so the forest's matrices stay as
+    they are), then tt_outgroups_f32.  Waits for the result and checks the status."""
+    if out.get("outgroup") is not None:
+        return out
+    t = torch()
+    lib = _lib.load()
+    q, w = forest.q, forest.w
+    fs = TTForest.from_buffer_copy(forest.struct)  # the forest with the pass's branch lengths
+    fs.bl = _p(snap["bl"])
+    p64 = scratch.get("p64", (forest.n_nodes, q, w), t.float64)
+    p32 = scratch.get("p32", (forest.n_nodes, q, w), t.float32)
+    status = scratch.get("status", (1,), t.int32)
+    status.zero_()
+    check(lib.tt_branch_pmats(C.byref(fs), C.byref(model.struct), TTPmats(_p(p64), _p(p32), None, None, None, None),
+                              _p(status), _stream()), "tt_branch_pmats")
+    og = bufs.get("outgroup", (forest.prof_rows, w), t.float32)
+    tog = bufs.get("tip_outgroup", (forest.tip_rows, w), t.float32)
+    check(lib.tt_outgroups_f32(C.byref(fs), C.byref(model.struct), C.byref(TTPmats(_p(p64), _p(p32), None, None,
+                                                                                   None, None)),
+                               _p(out["posterior"]), _p(out["partial"]), _p(og), _p(tog), _stream()),
+          "tt_outgroups_f32")
+    _check_status(status)
+    out["outgroup"], out["tip_outgroup"] = og, tog
+    return out
+
+
 class CapturedCall:
     """One call of a pass function (marginal, joint: its buffer clears and launches) captured as
     a CUDA graph, replayed with a single host call.  The kernels read the forest's device inputs
@@ -669,11 +728,13 @@ class CapturedCall:
     this forest with the same options before (buffers allocated, kernel attributes set), so that
     nothing is allocated or configured inside the capture."""
 
-    def __init__(self, fn, *args, **kw):
+    def __init__(self, fn, *args, after=None, **kw):
         t = torch()
         self.graph = t.cuda.CUDAGraph()
         with t.cuda.graph(self.graph):
             self.out = fn(*args, sync=False, **kw)
+            if after is not None:  # further work on the outputs, captured with them (copies)
+                after(self.out)
         self._keep = args  # the captured launches point into these objects' device buffers
 
     def replay(self):

@@ -368,10 +368,10 @@ tt_status tt_mutation_counts_ss(const tt_forest* f, const tt_ss_model* m, int32_
  * + align256(internal_rows*width*8) + align256(internal_rows*width)
  * <= TT_JOINT_NOALLOC_SCRATCH_BYTES are rejected with TT_ERR_OOM, and the kernel checks every
  * tree's rows against the rows the scratch holds (a tree beyond them is skipped with
- * *status = TT_ERR_OOM), whatever `internal_rows` says.  The first call on each device looks the
- * array's device address up (cudaGetSymbolAddress) and keeps it for the life of the process (it
- * does not survive a cudaDeviceReset); that first call should come before any stream capture.
- * Calls share the array, so calls that overlap on the GPU race and must be serialised. */
+ * *status = TT_ERR_OOM), whatever `internal_rows` says.  Every call looks the array's device
+ * address up (cudaGetSymbolAddress), so it stays right after a cudaDeviceReset; the first call
+ * on a device may load the library's module and should come before any stream capture.  Calls
+ * share the array, so calls that overlap on the GPU race and must be serialised. */
 #define TT_JOINT_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 tt_status tt_joint_noalloc(const tt_forest* f, const tt_model* m, int64_t internal_rows, uint8_t* states,
                            double* site_lh, double* tree_lh, unsigned long long* n_diff, const double* root_uniform,

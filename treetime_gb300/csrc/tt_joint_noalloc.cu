@@ -9,18 +9,16 @@
 //
 // The array is a file-scope __device__ object of TT_JOINT_NOALLOC_SCRATCH_BYTES bytes; every
 // GPU that loads this library holds it until the process exits.  Host code must not use the
-// symbol's host-side name as a device address: the device address is looked up once per
-// device with cudaGetSymbolAddress (on the first call made while that device is current) and
-// cached for the life of the process (a cudaDeviceReset, which reloads the module, invalidates
-// it).  That first call per device therefore touches the module and should come before any
-// stream capture.  All calls share the one array and it keeps the last call's contents:
+// symbol's host-side name as a device address: the device address is looked up with
+// cudaGetSymbolAddress on every call, so it stays right after a device reset (the first call on
+// a device may load the module and should come before any stream capture).  All calls share
+// the one array and it keeps the last call's contents:
 // nothing in it has to start at zero (every scratch entry is written before it is read), but
 // calls that overlap on the GPU (different streams, or host threads) race on it and must be
 // serialised by the caller.  The rows of the message and argmax scratch are bounded twice: on
 // the host by the caller's `internal_rows`, and in the kernel by the rows that region holds
 // (a tree whose rows do not fit is skipped with TT_ERR_OOM in *status), so a wrong
 // `internal_rows` cannot make the kernel write past the array.
-#include <mutex>
 
 #include "tt_internal.cuh"
 
@@ -28,29 +26,17 @@ static __device__ __align__(256) unsigned char tt_joint_noalloc_scratch[TT_JOINT
 
 namespace {
 
-std::mutex g_scratch_mu;
-constexpr int kMaxDevices = 256;
-void* g_scratch_dev[kMaxDevices] = {};
-
+// The array's device address, looked up on every call (a driver query of about a microsecond):
+// a cached address would outlive a device reset or a new primary context, after which the module
+// is loaded again at another address.
 tt_status scratch_address(void** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        tt::set_error("tt_joint_noalloc: no current CUDA device (%s)", cudaGetErrorString(e));
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, tt_joint_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        tt::set_error("tt_joint_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
         return TT_ERR_CUDA;
     }
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_dev[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, tt_joint_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            tt::set_error("tt_joint_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-                          cudaGetErrorString(e));
-            return TT_ERR_CUDA;
-        }
-        g_scratch_dev[dev] = p;
-    }
-    *out = g_scratch_dev[dev];
+    *out = p;
     return TT_OK;
 }
 

@@ -646,11 +646,10 @@ class GPUAncMixin:
         if self.reconstructed_tip_sequences:
             tip_chars = self._previous_chars(sess)
         else:
-            name_to_row, _ = self._aln_index()
-            for n in layout.nodes[layout.n_int:]:
-                if n.name not in name_to_row:
-                    raise MissingDataError("TreeAnc._fitch_anc: terminal node alignments required; sequence is "
-                                           "missing for leaf: '%s'." % n.name)
+            missing = self._missing_tip(sess)
+            if missing is not False:
+                raise MissingDataError("TreeAnc._fitch_anc: terminal node alignments required; sequence is "
+                                       "missing for leaf: '%s'." % missing)
         prev = self._previous_chars(sess)
         lists = bufs.get("fitch_lists", (forest.prof_rows, 16), t.uint8)
         status = bufs.get("status", (1,), t.int32)
@@ -662,11 +661,17 @@ class GPUAncMixin:
         root = lists[(layout.n_int - 1) * P:layout.n_int * P].cpu().numpy()
         lens = root[:, 15].astype(np.int64)
         root_chars = root[:, 0].copy()
-        for i in np.nonzero(lens > 1)[0]:
-            choices = root[i, :lens[i]].tobytes().decode("latin-1")
-            self.logger("Ambiguous state of the root sequence in the position %d: %s, choosing %s"
-                        % (i, str(list(choices)), choices[0]), 4)
-            root_chars[i] = root[i, self.rng.integers(lens[i])]
+        amb = np.flatnonzero(lens > 1)
+        if amb.size and 4 < getattr(self, "verbose", 5):  # messages formed only when they are printed
+            for i in amb:
+                choices = root[i, :lens[i]].tobytes().decode("latin-1")
+                self.logger("Ambiguous state of the root sequence in the position %d: %s, choosing %s"
+                            % (i, str(list(choices)), choices[0]), 4)
+        if amb.size:
+            # one draw per ambiguous position in position order (treetime/treeanc.py:615-617): a
+            # vector of bounds gives the scalar calls' sequence and leaves the generator in the
+            # same state
+            root_chars[amb] = root[amb, self.rng.integers(lens[amb])]
         self.logger("TreeAnc._fitch_anc: Walking down the self.tree, generating sequences from the Fitch profiles.", 2)
         chars = bufs.get("fitch_chars", (forest.state_rows,), t.uint8)
         states = bufs.get("states", (forest.state_rows,), t.uint8)
@@ -687,6 +692,17 @@ class GPUAncMixin:
         self.logger("Done ancestral state reconstruction", 3)
         return N_diff
 
+    def _missing_tip(self, sess):
+        """The name of a tip without an alignment row, or False.  The session's tips and their
+        rows are fixed when it is built, so the tips are looked through once per session."""
+        missing = sess.get("tip_missing")
+        if missing is None:
+            layout = sess["layout"]
+            name_to_row, _ = self._aln_index()
+            missing = sess["tip_missing"] = next(
+                (n.name for n in layout.nodes[layout.n_int:] if n.name not in name_to_row), False)
+        return missing
+
     # --------------------------------------------------------- branch lengths
     def _pair_histograms(self, ignore_gaps=None):
         """(session, [n_nodes, q, q] device histograms of (parent, child) states
@@ -695,13 +711,7 @@ class GPUAncMixin:
         sess = self._get_session()
         layout = sess["layout"]
         if not self.reconstructed_tip_sequences:
-            # the session's tips and their alignment rows are fixed when it is built: a tip
-            # without a row is looked for once per session
-            missing = sess.get("tip_missing")
-            if missing is None:
-                name_to_row, _ = self._aln_index()
-                missing = sess["tip_missing"] = next(
-                    (n.name for n in layout.nodes[layout.n_int:] if n.name not in name_to_row), False)
+            missing = self._missing_tip(sess)
             if missing is not False:
                 raise MissingDataError(
                     "TreeAnc.optimal_branch_length: terminal node alignments required; sequence is missing for "

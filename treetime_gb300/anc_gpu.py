@@ -833,8 +833,7 @@ class GPUAncMixin:
         out = last[1]
         layout = (sess or self._get_session())["layout"]
         P = self.data.compressed_length
-        local = layout.local
-        ks = np.fromiter((local[id(n)] for n in nodes), dtype=np.int64, count=len(nodes))
+        ks = np.fromiter(map(layout.local.__getitem__, map(id, nodes)), dtype=np.int64, count=len(nodes))
         tip = ks >= layout.n_int
         for sel, pp, tips in ((~tip, out["outgroup"], False), (tip, out["tip_outgroup"], True)):
             idx = np.flatnonzero(sel)
@@ -845,6 +844,22 @@ class GPUAncMixin:
             pc_row = np.full(idx.size, -1, np.int64) if tips else kk * P
             yield idx, kk.astype(np.int32), pp, pp_row, pc_row, out["partial"]
 
+    def _device_branch_groups(self, nodes, sess):
+        """_profile_branch_groups with the node ids and row offsets on the device, all uploaded
+        before the caller launches anything; kept by the session while the same branches are
+        asked for again (the TreeTime loops ask for every branch at every iteration)."""
+        groups = list(self._profile_branch_groups(nodes, sess))
+        cache = sess.get("branch_groups")
+        if cache is not None and len(cache) == len(groups) and all(
+                np.array_equal(c[0], g[1]) for c, g in zip(cache, groups)):
+            dev_idx = [c[1] for c in cache]
+        else:
+            dev = sess["forest"].device
+            dev_idx = [(engine._to_dev(kk, dev), engine._to_dev(pp_row, dev), engine._to_dev(pc_row, dev))
+                       for idx, kk, pp, pp_row, pc_row, pc in groups]
+            sess["branch_groups"] = [(g[1], d) for g, d in zip(groups, dev_idx)]
+        return [(idx, d[0], pp, d[1], pc, d[2]) for (idx, kk, pp, pp_row, pc_row, pc), d in zip(groups, dev_idx)]
+
     def _marginal_branch_lengths(self, nodes, tol):
         """Profile-mode Brent for the given nodes in one device pass, from the
         outgroup and subtree profiles of the last marginal reconstruction."""
@@ -852,11 +867,12 @@ class GPUAncMixin:
         model = engine.model_for(self.gtr, getattr(self, "device", None))
         res = np.zeros(len(nodes))
         info = np.zeros(len(nodes), dtype=np.int32)
-        # both branch groups are queued before either result is read back
+        # both branch groups are queued before either result is read back; their index arrays
+        # go up first (a synchronous upload after a launch would wait for that launch)
         pending = []
-        for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
-            t, inf = engine.optimal_t_profiles(sess["forest"], model, kk, pp, pp_row, pc, pc_row,
-                                               self._gpu_precision(), self.gtr.gap_index, True, tol)
+        for idx, d_kk, pp, d_pp_row, pc, d_pc_row in self._device_branch_groups(nodes, sess):
+            t, inf = engine.optimal_t_profiles_dev(sess["forest"], model, d_kk, pp, d_pp_row, pc, d_pc_row,
+                                                   self._gpu_precision(), self.gtr.gap_index, True, tol)
             pending.append((idx, t, inf))
         for idx, t, inf in pending:
             res[idx] = t.cpu().numpy()
@@ -893,12 +909,12 @@ class GPUAncMixin:
         logp = np.empty(padded.shape)
         if branch_length_mode == "marginal":
             model = engine.model_for(self.gtr, getattr(self, "device", None))
-            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
-                d = engine._to_dev
-                v = engine.prob_t_profiles_grid_dev(sess["forest"], model, d(np.asarray(kk, np.int32), dev), pp,
-                                                    d(np.asarray(pp_row, np.int64), dev), pc,
-                                                    d(np.asarray(pc_row, np.int64), dev), self._gpu_precision(),
-                                                    self.gtr.gap_index, True, d(padded[idx], dev))
+            groups = self._device_branch_groups(nodes, sess)  # uploads before any launch
+            grids = [engine._to_dev(padded[g[0]], dev) for g in groups]
+            pending = [(idx, engine.prob_t_profiles_grid_dev(sess["forest"], model, d_kk, pp, d_pp_row, pc, d_pc_row,
+                                                             self._gpu_precision(), self.gtr.gap_index, True, grid))
+                       for (idx, d_kk, pp, d_pp_row, pc, d_pc_row), grid in zip(groups, grids)]
+            for idx, v in pending:
                 logp[idx] = v.cpu().numpy()
         else:
             if not self.sequence_reconstruction:
@@ -976,12 +992,9 @@ class GPUAncMixin:
         t = engine.torch()
         if marginal and self.gtr.is_site_specific:
             n_ija = T_ia = None
-            d = engine._to_dev
-            dev = forest.device
-            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
-                n1, T1 = engine.mutation_counts_ss(forest, self.gtr, sess["bufs"], d(np.asarray(kk, np.int32), dev),
-                                                   pp, d(np.asarray(pp_row, np.int64), dev), pc,
-                                                   d(np.asarray(pc_row, np.int64), dev), self._gpu_precision())
+            for idx, d_kk, pp, d_pp_row, pc, d_pc_row in self._device_branch_groups(nodes, sess):
+                n1, T1 = engine.mutation_counts_ss(forest, self.gtr, sess["bufs"], d_kk, pp, d_pp_row, pc, d_pc_row,
+                                                   self._gpu_precision())
                 n_ija = n1 if n_ija is None else n_ija + n1
                 T_ia = T1 if T_ia is None else T_ia + T1
             return n_ija, T_ia
@@ -990,12 +1003,9 @@ class GPUAncMixin:
             engine.branch_pmats(forest, model, sess["bufs"])
             p64 = sess["bufs"].cache[("p64", t.float64)]
             n_ija = T_ia = None
-            for idx, kk, pp, pp_row, pc_row, pc in self._profile_branch_groups(nodes, sess):
-                d = engine._to_dev
-                dev = forest.device
-                n1, T1 = engine.mutation_counts(forest, model, p64, 0, d(np.asarray(kk, np.int32), dev), pp,
-                                                d(np.asarray(pp_row, np.int64), dev), pc,
-                                                d(np.asarray(pc_row, np.int64), dev), self._gpu_precision())
+            for idx, d_kk, pp, d_pp_row, pc, d_pc_row in self._device_branch_groups(nodes, sess):
+                n1, T1 = engine.mutation_counts(forest, model, p64, 0, d_kk, pp, d_pp_row, pc, d_pc_row,
+                                                self._gpu_precision())
                 n_ija = n1 if n_ija is None else n_ija + n1
                 T_ia = T1 if T_ia is None else T_ia + T1
             return n_ija, T_ia

@@ -136,3 +136,17 @@ def test_length_counter_moves_on_every_assignment_and_only_then():
     assert Clade(name="N").branch_length is None
     c = copy.deepcopy(t)
     assert [n.branch_length for n in c.find_clades()] == [n.branch_length for n in nodes]
+
+
+def test_vector_draws_equal_scalar_draws():
+    """The Fitch root's ambiguous positions draw rng.integers(bounds) in one call; TreeTime
+    draws rng.integers(bound) position by position (treetime/treeanc.py:615-617).  The two give
+    the same numbers and leave the generator in the same state (numpy's bounded draws take the
+    bit generator's 32-bit outputs in order either way)."""
+    import numpy as np
+    for seed in range(6):
+        bounds = np.random.default_rng(50 + seed).integers(2, 5, size=700)
+        a = np.random.default_rng(seed)
+        b = np.random.default_rng(seed)
+        assert [int(a.integers(k)) for k in bounds] == b.integers(bounds).tolist()
+        assert a.random() == b.random()

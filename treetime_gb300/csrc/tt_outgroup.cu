@@ -15,7 +15,7 @@
 //     (the root's row: pi, as the pass stores it);
 //   - tt_count_changes: the states the pass replaced (a copy taken before it) against the new
 //     ones, on the rows the pass would have counted (internal nodes but the root; the tips when
-//     their states are reconstructed), per tree.
+//     their states are reconstructed), per tree, in 4-byte words.
 #include "tt_internal.cuh"
 
 namespace tt {
@@ -116,31 +116,48 @@ __global__ void __launch_bounds__(kOgThreads) outgroup_f32_kernel(tt_forest f, c
     }
 }
 
-// One CTA per node: the changed states of its row, added to its tree's count.
+// The rows a tree's pass counts are contiguous in the state buffer: internal nodes 0 .. n_int - 2
+// (the root, row n_int - 1, is not counted), then the tips n_int .. n_int + n_tip - 1 when their
+// states are reconstructed.  Each range is compared in 4-byte words (__vcmpne4 marks the bytes
+// that differ), its unaligned head and tail bytewise.  blockIdx.y = tree.
+__device__ __forceinline__ unsigned count_range(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b,
+                                                int64_t lo, int64_t hi, int64_t t0, int64_t stride) {
+    unsigned c = 0;
+    const int64_t lo4 = (lo + 3) & ~int64_t(3), hi4 = hi & ~int64_t(3);
+    if (lo4 >= hi4) {  // no whole word inside
+        for (int64_t i = lo + t0; i < hi; i += stride) c += a[i] != b[i];
+        return c;
+    }
+    for (int64_t i = lo + t0; i < lo4; i += stride) c += a[i] != b[i];
+    const uint32_t* aw = reinterpret_cast<const uint32_t*>(a);
+    const uint32_t* bw = reinterpret_cast<const uint32_t*>(b);
+    for (int64_t w = (lo4 >> 2) + t0; w < (hi4 >> 2); w += stride)
+        c += __popc(__vcmpne4(aw[w], bw[w])) >> 3;
+    for (int64_t i = hi4 + t0; i < hi; i += stride) c += a[i] != b[i];
+    return c;
+}
+
 __global__ void __launch_bounds__(kOgThreads) count_changes_kernel(tt_forest f, const uint8_t* __restrict__ old_states,
                                                                    const uint8_t* __restrict__ states, int tips,
                                                                    int64_t* __restrict__ n_diff) {
     __shared__ unsigned warp_sum[kOgThreads / 32];
-    for (int64_t g = blockIdx.x; g < f.n_nodes; g += gridDim.x) {
-        const int ti = og_tree_of(f.trees, f.n_trees, g);
-        const tt_tree tr = f.trees[ti];
-        const int k = (int)(g - tr.node_base);
-        // the pass counts the nodes of its pre-order: internal nodes but the root, tips if asked
-        if (k == tr.n_int - 1 || (k >= tr.n_int && !tips)) continue;
-        const int P = tr.n_patterns;
-        const int64_t base = tr.state_base + (int64_t)k * P;
-        unsigned c = 0;
-        for (int p = threadIdx.x; p < P; p += blockDim.x) c += old_states[base + p] != states[base + p];
+    const int ti = blockIdx.y;
+    const tt_tree tr = f.trees[ti];
+    const int64_t P = tr.n_patterns;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned c = 0;
+    if (tr.n_int > 1) c += count_range(old_states, states, tr.state_base, tr.state_base + (tr.n_int - 1) * P, t0, stride);
+    if (tips && tr.n_tip > 0)
+        c += count_range(old_states, states, tr.state_base + tr.n_int * P,
+                         tr.state_base + (int64_t)(tr.n_int + tr.n_tip) * P, t0, stride);
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
-        if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = c;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long t = 0;
-            for (int w = 0; w < kOgThreads / 32; ++w) t += warp_sum[w];
-            if (t) atomicAdd(reinterpret_cast<unsigned long long*>(n_diff + ti), t);
-        }
-        __syncthreads();
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < kOgThreads / 32; ++w) t += warp_sum[w];
+        if (t) atomicAdd(reinterpret_cast<unsigned long long*>(n_diff + ti), t);
     }
 }
 
@@ -183,8 +200,17 @@ extern "C" tt_status tt_count_changes(const tt_forest* f, const uint8_t* old_sta
         set_error("tt_count_changes: invalid arguments");
         return TT_ERR_INVALID;
     }
-    if (f->n_nodes == 0) return TT_OK;
-    const int blocks = f->n_nodes < 65535 * 8 ? (int)f->n_nodes : 65535 * 8;
-    count_changes_kernel<<<blocks, kOgThreads, 0, as_stream(stream)>>>(*f, old_states, states, tips, n_diff);
+    if (f->n_nodes == 0 || f->n_trees < 1) return TT_OK;
+    if (f->n_trees > 65535) {
+        set_error("tt_count_changes: %d trees (at most 65535)", f->n_trees);
+        return TT_ERR_INVALID;
+    }
+    // blocks per tree for about 4 words a thread on the average tree
+    const int64_t words = (f->n_nodes / f->n_trees + 1) * (f->n_patterns / f->n_trees + 1) / 4 + 1;
+    int64_t bx = (words + 4 * kOgThreads - 1) / (4 * kOgThreads);
+    if (bx < 1) bx = 1;
+    if (bx > 1024) bx = 1024;
+    count_changes_kernel<<<dim3((unsigned)bx, (unsigned)f->n_trees), kOgThreads, 0, as_stream(stream)>>>(
+        *f, old_states, states, tips, n_diff);
     return check_launch("tt_count_changes");
 }

@@ -99,3 +99,19 @@ def test_changed_site_count_between_reconstructions():
         n_diff = t.infer_ancestral_sequences(marginal=True)
         want = sum(int((np.array(n._cseq) != before[id(n)]).sum()) for n in lay.nodes[:lay.n_int - 1])
         assert n_diff == want, step
+
+
+def test_changed_site_count_with_tip_states():
+    """With tip states reconstructed the pass counts the tips' rows too (the second range of
+    tt_count_changes); the first such call counts against the alignment's states."""
+    t = _treeanc("nuc_nogap", False, False, seed=12)
+    lay = t._get_session()["layout"]
+    rows = lay.nodes[:lay.n_int - 1] + lay.nodes[lay.n_int:]
+    t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=True)
+    for step in range(3):
+        before = {id(n): np.array(n._cseq) for n in rows}
+        for n in list(t.tree.find_clades())[1::5]:
+            n.branch_length = n.branch_length * (0.3 if step % 2 else 4.0) + 1e-4
+        n_diff = t.infer_ancestral_sequences(marginal=True, reconstruct_tip_states=True)
+        want = sum(int((np.array(n._cseq) != before[id(n)]).sum()) for n in rows)
+        assert n_diff == want, step

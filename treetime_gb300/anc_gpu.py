@@ -39,15 +39,21 @@ def _dist2root(layout, lengths):
     before children (internal nodes by decreasing height, then the tips): the
     additions of TreeTime's _calc_dist2root (treetime/treeanc.py:499-510), in
     numpy, one height level at a time."""
+    steps = getattr(layout, "_d2r_steps", None)
+    if steps is None:  # (nodes, their parents) per level from the top, then the tips; per layout
+        par = np.asarray(layout.parent)
+        lev = layout.level_off
+        steps = []
+        for h in range(layout.n_levels - 1, -1, -1):
+            ks = np.arange(lev[h], lev[h + 1])
+            ks = ks[par[ks] >= 0]
+            steps.append((ks, par[ks]))
+        tips = np.arange(layout.n_int, layout.n_nodes)
+        steps.append((tips, par[tips]))
+        layout._d2r_steps = steps
     d = np.zeros(layout.n_nodes)
-    par = layout.parent
-    lev = layout.level_off
-    for h in range(layout.n_levels - 1, -1, -1):
-        ks = np.arange(lev[h], lev[h + 1])
-        ks = ks[par[ks] >= 0]
-        d[ks] = d[par[ks]] + lengths[ks]
-    tips = np.arange(layout.n_int, layout.n_nodes)
-    d[tips] = d[par[tips]] + lengths[tips]
+    for ks, pk in steps:
+        d[ks] = d[pk] + lengths[ks]
     return d
 
 
